@@ -1,0 +1,99 @@
+"""The oracle against golden vectors produced by the reference itself (CPU)."""
+
+from __future__ import annotations
+
+import warnings
+
+import numpy as np
+import pytest
+
+from conftest import golden, golden_csr, rel_err, sparse_rel_err
+from oracle import beam as ob
+from oracle import contact as oc
+
+SECTION_KEYS = ["E", "G", "A", "Iy", "Iz", "J", "kappa_y", "kappa_z"]
+
+
+def _section(z, **kw):
+    return ob.Section(*(float(z[k]) for k in SECTION_KEYS), **kw)
+
+
+def test_beam_elements_large_rotations():
+    z = golden("beam_elements")
+    n = 6 * len(z["X"])
+    K, f = ob.assemble_beam(z["X"], z["conn"], z["u"], _section(z))
+    assert rel_err(f, z["beam_f"]) < 1e-13
+    assert sparse_rel_err(K, golden_csr(z, "beam_K", n)) < 1e-13
+
+
+def test_beam_vref_and_scf():
+    z = golden("beam_elements")
+    n = 6 * len(z["X"])
+    K, f = ob.assemble_beam(z["X"], z["conn"], z["u"], _section(z, scf=0.25), v_ref=np.array([0.3, -0.2, 0.9]))
+    assert rel_err(f, z["beam_f_vref_scf"]) < 1e-13
+    assert sparse_rel_err(K, golden_csr(z, "beam_K_vref_scf", n)) < 1e-13
+
+
+def test_narrowphase_bit_exact():
+    z = golden("narrowphase")
+    s, t, dist, normal, par = oc.closest_point(z["xA0"], z["xA1"], z["xB0"], z["xB1"])
+    for a, b in ((s, z["s"]), (t, z["t"]), (dist, z["dist"]), (normal, z["normal"]), (par, z["parallel"])):
+        assert np.array_equal(a, b)
+
+
+def test_contact_frame_bit_exact():
+    z = golden("narrowphase")
+    n, t1, t2 = oc.contact_frame(z["normal"], z["prev_t1"], z["prev_n"])
+    assert np.array_equal(n, z["n"]) and np.array_equal(t1, z["t1"]) and np.array_equal(t2, z["t2"])
+
+
+@pytest.mark.parametrize("name", ["strand7", "strand7_nogap", "strand19_slip"])
+def test_strand_sequence(name):
+    """Detect, active set and Newton iterations, state carried across increments."""
+    z = golden(name)
+    X, conn, layer = z["X"], z["conn"], z["elem_layer"]
+    n = 6 * len(X)
+    radii = np.full(len(conn), float(z["radius"]))
+    K, f = ob.assemble_beam(X, conn, z["u0"], _section(z))
+    assert rel_err(f, z["beam_f"]) < 1e-12
+    assert sparse_rel_err(K, golden_csr(z, "beam_K", n)) < 1e-13
+    kp, mu, ktr, sd = (float(z[k]) for k in ("k_pen", "mu", "k_t_ratio", "smoothing_delta"))
+    table = oc.empty_table()
+    for inc in range(int(z["n_incr"])):
+        cd = oc.deformed_coords(X, z[f"inc{inc}_u"])
+        table, cands, _ = oc.detect(table, cd, conn, radii, elem_layer=layer, exclude_same_layer=True)
+        assert np.array_equal(cands, z[f"inc{inc}_candidates"])
+        p = f"inc{inc}_detect_"
+        for k in ("ea", "eb", "status"):
+            assert np.array_equal(table[k], z[p + k])
+        table = oc.update_geometry(table, cd)
+        p = f"inc{inc}_geom_"
+        for k in ("s", "t", "gap", "normal", "status"):
+            assert np.array_equal(table[k], z[p + k]), k
+        for it in range(int(z["n_iter"])):
+            p = f"inc{inc}_it{it}_"
+            table, _, _, parts = oc.contact_iteration(table, X, z[p + "u"], z[f"inc{inc}_u_ref"], n, k_pen=kp,
+                                                      k_t_ratio=ktr, mu_eff=mu, smoothing_delta=sd)
+            assert rel_err(parts["f_n"], z[p + "f_n"]) < 1e-12
+            assert rel_err(parts["f_f"], z[p + "f_f"]) < 1e-12
+            assert sparse_rel_err(parts["K_n"], golden_csr(z, p + "K_n", n)) < 1e-12
+            assert sparse_rel_err(parts["K_f"], golden_csr(z, p + "K_f", n)) < 1e-12
+            for k in ("status", "stick"):
+                assert np.array_equal(table[k], z[p + k]), k
+            for k in ("p_n", "z_t", "q_trial_norm", "k_pen", "k_t", "dissipation"):
+                assert rel_err(table[k], z[p + k]) < 1e-12, k
+
+
+def test_strand_mesh_generator_matches_reference():
+    from xkgpu import strand as xs
+
+    z = golden("meshes")
+    warnings.simplefilter("ignore")
+    for tag, args, kw in (("w7", (7, 2.0, 40.0, 1, 16), dict(gap=-0.01)),
+                          ("w19", (19, 1.0, 20.0, 2, 32), dict(gap=0.0)),
+                          ("w37", (37, 0.5, 20.0, 2, 48), dict(gap=-0.0025))):
+        m = xs.make_strand(*args, **kw)
+        assert np.array_equal(m.conn, z[tag + "_conn"])
+        # bit-identical on the platform the fixtures were made on; libm may differ elsewhere
+        assert rel_err(m.coords, z[tag + "_X"]) < 1e-15
+        assert np.array_equal(np.array([w.layer for w in m.wires]), z[tag + "_layer"])
