@@ -1,0 +1,231 @@
+/*
+ * xkgpu: GPU (sm_103a) assembly of the CR-beam + frictional-contact Newton
+ * iteration of the xkep-cae strand solver, as a plain C ABI.
+ *
+ * All array arguments are DEVICE pointers unless marked "host".  Nothing here
+ * takes a framework type: callers pass raw pointers, sizes and a CUDA stream
+ * (cudaStream_t cast to void*; NULL is the legacy default stream).  Every
+ * function returns an xk_status; xk_last_error() gives a message.
+ *
+ * Layouts (see the package documentation for byte counts):
+ *   u, f, R        double[6*n_nodes], node-major [ux,uy,uz,rx,ry,rz]
+ *   beam K_T       block-CSR of 6x6 node blocks, row-major inside a block
+ *   contact K_c    block-CSR of 3x3 translational node blocks
+ *   pair table     structure of arrays, vector fields component-major with
+ *                  stride `cap` (x[c*cap + i])
+ */
+#ifndef XKGPU_H
+#define XKGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int xk_status;
+#define XK_OK 0
+#define XK_ERR_ARG 1       /* bad argument */
+#define XK_ERR_CUDA 2      /* CUDA runtime error */
+#define XK_ERR_CAPACITY 3  /* an output buffer is too small; required size is reported */
+#define XK_ERR_OVERFLOW 4  /* a bounded per-item work list overflowed */
+
+#define XK_FP64 0   /* every operation in double */
+#define XK_MIXED 1  /* float arithmetic, double frames / strain / gap / reductions */
+
+typedef void* xk_stream;
+
+const char* xk_version(void);
+const char* xk_last_error(void);
+
+/* ------------------------------------------------------------------ model */
+
+/* Beam section and material; ULCRBeamAssembler.__init__
+ * (xkep_cae/elements/_beam_assembler.py:33-67).  scf <= 0 disables the
+ * slenderness compensation of timo_beam3d_ke_local (_beam_cr.py:116-122). */
+typedef struct {
+  double E, G, A, Iy, Iz, J, kappa_y, kappa_z, scf;
+} xk_section;
+
+/* Mesh: reference coordinates, two-node elements, contact radius and layer of
+ * every element (DetectCandidatesInput, xkep_cae/contact/_manager_process.py:135-146,
+ * and _ContactConfigInput.elem_layer_map, _contact_pair.py:109). */
+typedef struct {
+  int32_t n_nodes, n_elems;
+  const double* X;      /* [3*n_nodes] */
+  const int32_t* conn;  /* [2*n_elems] */
+  const double* radii;  /* [n_elems] */
+  const int32_t* layer; /* [n_elems], -1 = no layer; NULL = no layer map */
+} xk_mesh;
+
+/* Pair table: _ContactPairOutput / _ContactStateOutput as structure of arrays
+ * (xkep_cae/contact/_contact_pair.py:38-81).  Sorted by (ea, eb), ea < eb. */
+typedef struct {
+  int32_t n, cap;
+  int32_t *ea, *eb;
+  double *s, *t, *gap;
+  double *normal, *t1, *t2; /* [3*cap] */
+  double *lambda_n, *k_pen, *k_t, *p_n;
+  double *z_t;              /* [2*cap] */
+  double *q_trial_norm, *dissipation;
+  uint8_t *status, *stick;  /* status: 0 INACTIVE, 1 ACTIVE, 2 SLIDING (_types.py:8-13) */
+} xk_pairs;
+
+/* -------------------------------------------------------------- beam path */
+
+/* Per-element reference frame [L0, R0 (3x3 row-major)] as 10 SoA columns of
+ * n_elems doubles.  v_ref: host double[3] or NULL (smallest-component axis).
+ * Replaces the reference-frame part of _assemble_cr_beam3d_batch_impl
+ * (xkep_cae/elements/_beam_assembly.py:241-245, _beam_cr.py:831-853). */
+xk_status xk_beam_reference(const xk_mesh* m, const double* v_ref, double* elem_ref, xk_stream s);
+
+/* Colouring plan for a deterministic, atomic-free write of element blocks into
+ * the fixed block-CSR pattern of K_T. */
+typedef struct {
+  int32_t n_colors;
+  const int32_t* color_ptr_host; /* host [n_colors+1], ranges of elem_order */
+  const int32_t* elem_order;     /* [n_elems] elements grouped by colour */
+  const int32_t* blk;            /* [4*n_elems] block index of (aa, ab, ba, bb) per element */
+  const uint8_t* first;          /* [n_elems] bits 0..3: this element is the first writer of
+                                    block aa, ab, ba, bb (aa / bb also: of the f rows of a / b) */
+  int64_t nnzb;
+} xk_beam_plan;
+
+/* Corotational Timoshenko internal force f_int and analytic tangent K_T of all
+ * elements at displacement u: assemble_cr_beam3d (_beam_assembly.py:26-152)
+ * as called by ULCRBeamAssembler.assemble_internal_force / assemble_tangent
+ * (_beam_assembler.py:73-115).  f_int (double) and K_vals (double for XK_FP64,
+ * float for XK_MIXED; 36*nnzb) may each be NULL.  Rows/blocks of nodes that
+ * no element touches are not written. */
+xk_status xk_beam_assemble(const xk_mesh* m, const xk_section* sec, const double* elem_ref,
+                           const xk_beam_plan* plan, const double* u, int precision,
+                           double* f_int, void* K_vals, xk_stream s);
+
+/* Diagonal lumped mass (ULCRBeamAssembler.assemble_mass(lumped=True),
+ * _beam_assembler.py:148-169, _beam_cr.py:267-296).  out: double[6*n_nodes],
+ * overwritten. */
+xk_status xk_beam_lumped_mass(const xk_mesh* m, const xk_section* sec, const xk_beam_plan* plan, double rho,
+                              double* out, xk_stream s);
+
+/* ----------------------------------------------------------- contact path */
+
+typedef struct {
+  double k_pen;            /* penalty (PenaltyStrategy.compute_k_pen) */
+  double k_t_ratio;        /* tangential / normal penalty (_ContactConfigInput.k_t_ratio) */
+  double mu_eff;           /* friction coefficient after the mu ramp (law_friction.py:183-195) */
+  double smoothing_delta;  /* Huber smoothing; 0 = plain max(0, x) (contact_force/strategy.py:139) */
+  double g_on, g_off;      /* active-set hysteresis (_manager_process.py:475-494) */
+  int32_t allow_deactivation;
+} xk_contact_params;
+
+typedef struct {
+  double margin;                 /* AABB inflation added to every radius */
+  int32_t exclude_shared;        /* drop pairs whose elements share a node */
+  int32_t exclude_same_layer;    /* drop pairs of one layer (needs mesh layer) */
+  int32_t midpoint_prescreening; /* _manager_process.py:260-286 */
+  double prescreening_margin;    /* <= 0: half the mean of r_a + r_b over the candidates */
+} xk_bp_params;
+
+/* Broadphase on the deformed coordinates X + u: every element pair (i<j) whose
+ * closed inflated AABBs overlap, then the shared-node, same-layer and midpoint
+ * filters; output sorted by (i, j).  Replaces _broadphase_aabb
+ * (xkep_cae/contact/_broadphase.py:13-96) and the filtering part of
+ * DetectCandidatesProcess.process (_manager_process.py:172-217).
+ * out_pairs: int32[2*cap] as (i, j) rows.  If cap is too small the function
+ * returns XK_ERR_CAPACITY and *n_out holds the required count.  n_raw and
+ * n_prefilter (host, nullable) receive the raw AABB-overlap count and the count
+ * before the midpoint prescreen.  Synchronises the stream. */
+xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_bp_params* bp, int32_t* out_pairs,
+                        int64_t cap, int64_t* n_out, int64_t* n_raw, int64_t* n_prefilter,
+                        xk_stream s);
+
+/* Pair-list update of DetectCandidatesProcess (_manager_process.py:219-250):
+ * the union of `old` and the sorted candidates; old pairs that are not
+ * candidates become INACTIVE with their state kept, new ones get a fresh state.
+ * out->cap must be >= old->n + n_cands; out->n is set.  `old` may be empty. */
+xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const int32_t* cands, int64_t n_cands,
+                         xk_pairs* out, xk_stream s);
+
+/* Narrowphase of every pair at X + u in exact reference arithmetic: closest
+ * point, gap, transported frame (UpdateGeometryProcess.process,
+ * _manager_process.py:327-403, geometry/_compute.py:55-261); with
+ * update_active != 0 the active-set hysteresis follows
+ * (_update_active_set_state, _manager_process.py:475-494). */
+xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double* u, const xk_contact_params* cp,
+                         int update_active, xk_stream s);
+
+#define XK_STAGE_NARROW 1   /* frozen-active-set narrowphase (_newton_steps.py:91-94) */
+#define XK_STAGE_NORMAL 2   /* HuberContactForceProcess.evaluate (contact_force/strategy.py:126-170) */
+#define XK_STAGE_FRICTION 4 /* CoulombReturnMappingProcess.evaluate (friction/strategy.py:111-148) */
+#define XK_STAGE_TANGENT 8  /* .tangent of both (contact_force/strategy.py:172-254, friction/_assembly.py:108-257) */
+#define XK_OUT_COMBINED 0   /* v = v_n + v_f (3), B = B_n - B_f (9) */
+#define XK_OUT_SPLIT 1      /* v_n (3), v_f (3), B_n (9), B_f (9) */
+
+/* Per-pair contact evaluation, fused over the selected stages.  A pair's
+ * translational force on its node k (A0, A1, B0, B1) is c_k * v and its
+ * tangent block (k, l) is c_k * c_l * B, with c = [1-s, s, -(1-t), -t].
+ * pv / pB are written (double for XK_FP64, float for XK_MIXED, column stride
+ * out_stride) for every pair that can contribute in this increment
+ * (status != INACTIVE or p_n > 0 on entry); others are left untouched. */
+xk_status xk_pair_eval(const xk_mesh* m, xk_pairs* p, const double* u, const double* u_ref,
+                       const xk_contact_params* cp, int stages, int precision, int out_mode, void* pv,
+                       void* pB, int64_t out_stride, xk_stream s);
+
+/* Node incidence of the contributing pairs and the block pattern of K_c, built
+ * once per increment (after detection and the active-set update). */
+typedef struct {
+  int32_t n_nodes;
+  int32_t n_members;   /* contributing pairs */
+  int64_t nnzb;        /* contact blocks */
+  int64_t cap_members; /* capacity of inc (4 entries per member) */
+  int64_t cap_blocks;  /* capacity of col / blk_row */
+  int32_t* inc_ptr;    /* [n_nodes+1] */
+  int32_t* inc;        /* [4*cap_members] (pair << 2) | local node */
+  int32_t* row_ptr;    /* [n_nodes+1] */
+  int32_t* col;        /* [cap_blocks] */
+  int32_t* blk_row;    /* [cap_blocks] */
+} xk_contact_pattern;
+
+/* Returns XK_ERR_CAPACITY (with n_members / nnzb set) when a capacity is too
+ * small.  Synchronises the stream. */
+xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* p, xk_contact_pattern* pat,
+                                   xk_stream s);
+
+#define XK_WHICH_COMBINED 0
+#define XK_WHICH_NORMAL 1
+#define XK_WHICH_FRICTION 2
+
+/* out[dof] = base[dof] + scale * sum_{pairs at node} c_k v_k  - f_ext[dof],
+ * then out[dof] = 0 where fixed[dof] != 0.  base, f_ext, fixed nullable.
+ * With base = f_int, scale = -1 this is the residual of
+ * ContactForceAssemblyProcess (_newton_steps.py:123-129).  norm2 (nullable,
+ * device double) receives sum(out^2) in a fixed-order FP64 reduction
+ * (ConvergenceCheckProcess, _newton_steps.py:194-203). */
+xk_status xk_contact_gather_force(const xk_mesh* m, const xk_pairs* p, const xk_contact_pattern* pat,
+                                  const void* pv, int precision, int out_mode, int which,
+                                  int64_t out_stride, const double* base, double scale,
+                                  const double* f_ext, const uint8_t* fixed, double* out,
+                                  double* norm2, xk_stream s);
+
+/* K_c block values (9 per block, double|float): sum of c_k c_l B over the
+ * pairs at each block; which selects B_n - B_f, B_n or B_f. */
+xk_status xk_contact_gather_tangent(const xk_mesh* m, const xk_pairs* p, const xk_contact_pattern* pat,
+                                    const void* pB, int precision, int out_mode, int which,
+                                    int64_t out_stride, void* Kc_vals, xk_stream s);
+
+/* Constraint Jacobian rows c_k n of the non-INACTIVE pairs in table order
+ * (_build_constraint_jacobian_ptp, xkep_cae/contact/geometry/strategy.py:83-132).
+ * rows/cols/vals: [12*cap]; *n_rows (host) gets the number of active pairs;
+ * XK_ERR_CAPACITY if cap < active pairs.  Synchronises the stream. */
+xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p, int32_t* rows, int32_t* cols,
+                                 double* vals, int32_t* pair_index, int64_t cap, int64_t* n_rows,
+                                 xk_stream s);
+
+/* Fixed-order FP64 sum of squares of x[0..n) into *out (device). */
+xk_status xk_norm2(const double* x, int64_t n, double* out, xk_stream s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XKGPU_H */

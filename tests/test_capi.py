@@ -1,0 +1,53 @@
+"""The C-ABI library builds, loads without a GPU and exports every declared symbol (CPU)."""
+
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared() -> set[str]:
+    text = (ROOT / "include" / "xkgpu.h").read_text()
+    return set(re.findall(r"^\s*(?:xk_status|const char\*)\s+(xk_\w+)\s*\(", text, flags=re.M))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from xkgpu import _lib as L
+    from xkgpu import build
+
+    build.build()
+    return L.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert "xk_pair_eval" in names and len(names) >= 14
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+
+
+def test_binding_covers_header(lib):
+    from xkgpu import _lib as L
+
+    assert _declared() == set(L.exported_symbols())
+    assert lib.xk_version().startswith(b"xkgpu")
+
+
+def test_struct_layouts_match_header():
+    import ctypes as C
+
+    from xkgpu import _lib as L
+
+    # field order and sizes as declared in include/xkgpu.h (LP64)
+    assert C.sizeof(L.Section) == 9 * 8
+    assert C.sizeof(L.Mesh) == 8 + 4 * 8
+    assert C.sizeof(L.Pairs) == 8 + 17 * 8
+    assert C.sizeof(L.BeamPlan) == 8 + 4 * 8 + 8
+    assert C.sizeof(L.ContactParams) == 6 * 8 + 8
+    assert C.sizeof(L.BPParams) == 8 + 3 * 4 + 4 + 8
+    assert C.sizeof(L.ContactPattern) == 8 + 3 * 8 + 5 * 8

@@ -1,0 +1,235 @@
+"""GPU path against the golden vectors and the oracle (through the C ABI).
+
+Tolerances: FP64 mode 1e-10 relative (max-norm), mixed mode 1e-5 relative;
+candidate sets, active sets and narrowphase results of the exact kernels are
+compared bit for bit.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import golden, golden_csr, rel_err, sparse_rel_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # collected on CPU-only hosts, skipped there
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from oracle import beam as ob  # noqa: E402
+from oracle import contact as oc  # noqa: E402
+from xkgpu import _lib as L  # noqa: E402
+from xkgpu.device import DeviceBeam, DeviceMesh, DevicePairTable  # noqa: E402
+from xkgpu.engine import AssemblyEngine  # noqa: E402
+
+SECTION_KEYS = ["E", "G", "A", "Iy", "Iz", "J", "kappa_y", "kappa_z"]
+TOL64, TOLMIX = 1e-10, 1e-5
+
+
+def _sec(z, scf=None):
+    d = {k: float(z[k]) for k in SECTION_KEYS}
+    d["scf"] = scf
+    return d
+
+
+def _dev(x, dtype=torch.float64):
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype, device="cuda")
+
+
+def _beam_eval(coords, conn, u, sec, precision, v_ref=None):
+    mesh = DeviceMesh(coords, conn, 0.0)
+    beam = DeviceBeam(mesh, sec, v_ref=v_ref)
+    f = torch.zeros(mesh.ndof, dtype=torch.float64, device="cuda")
+    K = torch.zeros(36 * beam.nnzb, dtype=beam.k_dtype(precision), device="cuda")
+    beam.assemble(_dev(u), precision, f, K)
+    torch.cuda.synchronize()
+    nb = beam.nnzb
+    Kc = sp.bsr_matrix((K.double().cpu().numpy().reshape(nb, 6, 6), beam.col.cpu().numpy(),
+                        beam.row_ptr.cpu().numpy()), shape=(mesh.ndof, mesh.ndof)).tocsr()
+    return f.cpu().numpy(), Kc
+
+
+@pytest.mark.parametrize("precision,tol", [(L.XK_FP64, TOL64), (L.XK_MIXED, TOLMIX)])
+def test_beam_large_rotation_elements(precision, tol):
+    z = golden("beam_elements")
+    n = 6 * len(z["X"])
+    f, K = _beam_eval(z["X"], z["conn"], z["u"], _sec(z), precision)
+    assert rel_err(f, z["beam_f"]) < tol
+    assert sparse_rel_err(K, golden_csr(z, "beam_K", n)) < tol
+    f, K = _beam_eval(z["X"], z["conn"], z["u"], _sec(z, scf=0.25), precision, v_ref=[0.3, -0.2, 0.9])
+    assert rel_err(f, z["beam_f_vref_scf"]) < tol
+    assert sparse_rel_err(K, golden_csr(z, "beam_K_vref_scf", n)) < tol
+
+
+@pytest.mark.parametrize("name", ["strand7", "strand19_slip"])
+@pytest.mark.parametrize("precision,tol", [(L.XK_FP64, TOL64), (L.XK_MIXED, TOLMIX)])
+def test_beam_strand(name, precision, tol):
+    z = golden(name)
+    n = 6 * len(z["X"])
+    f, K = _beam_eval(z["X"], z["conn"], z["u0"], _sec(z), precision)
+    # f_int of a near-straight strand is a small difference of large element forces:
+    # compare against the element force scale
+    fe, _ = ob.element_batch(z["X"], z["conn"], z["u0"], ob.Section(**_sec(z)), stiffness=False)
+    assert np.max(np.abs(f - z["beam_f"])) < tol * np.max(np.abs(fe))
+    assert sparse_rel_err(K, golden_csr(z, "beam_K", n)) < tol
+
+
+def test_narrowphase_bit_exact():
+    z = golden("narrowphase")
+    N = len(z["s"])
+    coords = np.concatenate([z["xA0"], z["xA1"], z["xB0"], z["xB1"]])
+    idx = np.arange(N)
+    conn = np.concatenate([np.stack([idx, N + idx], 1), np.stack([2 * N + idx, 3 * N + idx], 1)])
+    mesh = DeviceMesh(coords, conn, 0.0)
+    tab = oc.new_pairs(np.stack([idx, N + idx], 1), conn, np.zeros(2 * N))
+    tab["normal"] = z["prev_n"].copy()
+    tab["t1"] = z["prev_t1"].copy()
+    pt = DevicePairTable(mesh.device)
+    pt.from_host(tab)
+    cp = L.ContactParams(1.0, 0.5, 0.1, 0.0, 0.0, 1e-6, 1)
+    import ctypes as C
+    L.call("xk_narrowphase", C.byref(mesh.c), C.byref(pt.c), C.c_void_p(_dev(np.zeros(6 * 4 * N)).data_ptr()),
+           C.byref(cp), 0, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    h = pt.to_host()
+    assert np.array_equal(h["s"], z["s"]) and np.array_equal(h["t"], z["t"])
+    assert np.array_equal(h["gap"], z["dist"])
+    assert np.array_equal(h["normal"], z["n"])
+    assert np.array_equal(h["t1"], z["t1"]) and np.array_equal(h["t2"], z["t2"])
+
+
+def _engine_for(z, precision="fp64"):
+    X, conn = z["X"], z["conn"]
+    return AssemblyEngine(X, conn, float(z["radius"]), _sec(z), layer=z["elem_layer"], precision=precision,
+                          k_pen=float(z["k_pen"]), k_t_ratio=float(z["k_t_ratio"]), mu=float(z["mu"]),
+                          smoothing_delta=float(z["smoothing_delta"]))
+
+
+@pytest.mark.parametrize("name", ["strand7", "strand7_nogap", "strand19_slip"])
+def test_strand_sequence_fp64(name):
+    """Detect / active set / Newton iterations against the reference's own outputs."""
+    z = golden(name)
+    eng = _engine_for(z, "fp64")
+    X, conn = z["X"], z["conn"]
+    n = 6 * len(X)
+    sec = ob.Section(**_sec(z))
+    for inc in range(int(z["n_incr"])):
+        u_ref = _dev(z[f"inc{inc}_u_ref"])
+        st = eng.detect(_dev(z[f"inc{inc}_u"]))
+        assert st["candidates"] == len(z[f"inc{inc}_candidates"])
+        h = eng.pairs.to_host()
+        p = f"inc{inc}_geom_"
+        assert np.array_equal(h["ea"], z[p + "ea"]) and np.array_equal(h["eb"], z[p + "eb"])
+        assert np.array_equal(h["status"], z[p + "status"])
+        assert np.array_equal(h["gap"], z[p + "gap"])
+        for it in range(int(z["n_iter"])):
+            p = f"inc{inc}_it{it}_"
+            u = z[p + "u"]
+            eng.assemble(_dev(u), u_ref)
+            torch.cuda.synchronize()
+            h = eng.pairs.to_host()
+            assert np.array_equal(h["status"], z[p + "status"])
+            assert np.array_equal(h["stick"], z[p + "stick"])
+            for k in ("p_n", "z_t", "q_trial_norm", "k_t"):
+                assert rel_err(h[k], z[p + k]) < TOL64, k
+            Kb, fb = ob.assemble_beam(X, conn, u, sec)
+            R_exp = fb - (z[p + "f_n"] + z[p + "f_f"])
+            assert rel_err(eng.R.cpu().numpy(), R_exp) < TOL64
+            Kc_exp = (golden_csr(z, p + "K_n", n) - golden_csr(z, p + "K_f", n)).tocsr()
+            assert sparse_rel_err(eng.K_contact_csr(), Kc_exp) < TOL64
+            assert sparse_rel_err(eng.K_beam_csr(), Kb) < TOL64
+            assert abs(eng.residual_norm() - np.linalg.norm(R_exp)) <= TOL64 * np.linalg.norm(R_exp) + 1e-300
+
+
+def test_strand_sequence_mixed():
+    z = golden("strand19_slip")
+    e64, emx = _engine_for(z, "fp64"), _engine_for(z, "mixed")
+    for inc in range(int(z["n_incr"])):
+        u0 = _dev(z[f"inc{inc}_u"])
+        u_ref = _dev(z[f"inc{inc}_u_ref"])
+        s64, smx = e64.detect(u0), emx.detect(u0)
+        assert s64 == smx  # detection is exact FP64 in both modes
+        for it in range(int(z["n_iter"])):
+            u = _dev(z[f"inc{inc}_it{it}_u"])
+            e64.assemble(u, u_ref)
+            emx.assemble(u, u_ref)
+            torch.cuda.synchronize()
+            fc64 = e64.R.cpu().numpy()
+            fcmx = emx.R.cpu().numpy()
+            assert rel_err(fcmx, fc64) < TOLMIX
+            assert sparse_rel_err(emx.K_contact_csr(), e64.K_contact_csr()) < TOLMIX
+            assert sparse_rel_err(emx.K_beam_csr(), e64.K_beam_csr()) < TOLMIX
+            h64, hmx = e64.pairs.to_host(), emx.pairs.to_host()
+            assert np.array_equal(h64["status"], hmx["status"])
+
+
+@pytest.mark.parametrize("cfg", ["strand37"])
+def test_engine_vs_oracle_medium(cfg):
+    """37-wire strand (4,736 elements, ~30k pairs): GPU against the oracle on the same inputs."""
+    from xkgpu import workloads as W
+
+    w = W.config_workload(cfg, seed=1)
+    st = w.strand
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="fp64", **w.engine_kwargs())
+    n = st.ndof
+    u = w.u
+    stats = eng.detect(_dev(u))
+    table, cands, raw = oc.detect(oc.empty_table(), oc.deformed_coords(st.coords, u), st.conn, st.radii,
+                                  elem_layer=st.elem_layer, exclude_same_layer=True)
+    assert stats["raw"] == len(raw)
+    assert stats["candidates"] == len(cands)
+    table = oc.update_geometry(table, oc.deformed_coords(st.coords, u))
+    h = eng.pairs.to_host()
+    assert np.array_equal(h["ea"], table["ea"]) and np.array_equal(h["eb"], table["eb"])
+    assert np.array_equal(h["status"], table["status"])
+    rng = np.random.default_rng(3)
+    u_ref = u.copy()
+    for it in range(2):
+        u = u + rng.normal(0.0, 3e-4 * w.meta["d"], n) * np.tile([1, 1, 1, 0, 0, 0], st.n_nodes)
+        eng.assemble(_dev(u), _dev(u_ref))
+        torch.cuda.synchronize()
+        table, fc, Kc, _ = oc.contact_iteration(table, st.coords, u, u_ref, n, k_pen=w.k_pen, k_t_ratio=w.k_t_ratio,
+                                                mu_eff=w.mu)
+        Kb, fb = ob.assemble_beam(st.coords, st.conn, u, ob.Section(**w.section, scf=None))
+        h = eng.pairs.to_host()
+        assert np.array_equal(h["status"], table["status"])
+        assert np.array_equal(h["stick"], table["stick"])
+        assert rel_err(eng.R.cpu().numpy(), fb + fc) < TOL64
+        assert sparse_rel_err(eng.K_contact_csr(), Kc) < TOL64
+        assert sparse_rel_err(eng.K_beam_csr(), Kb) < TOL64
+
+
+def test_graph_replay_matches_eager():
+    z = golden("strand7")
+    a, b = _engine_for(z), _engine_for(z)
+    u0 = _dev(z["inc0_u"])
+    a.detect(u0)
+    b.detect(u0)
+    u = _dev(z["inc0_it0_u"])
+    u_ref = _dev(z["inc0_u_ref"])
+    a.assemble(u, u_ref)
+    b.capture(u, u_ref)  # warm-up + capture: runs assemble once
+    torch.cuda.synchronize()
+    assert torch.equal(a.R, b.R)
+    a.assemble(u, u_ref)
+    b.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(a.R, b.R) and torch.equal(a.K_c, b.K_c) and torch.equal(a.K_beam, b.K_beam)
+
+
+def test_deterministic_repeat():
+    from xkgpu import workloads as W
+
+    w = W.config_workload("strand37", seed=2)
+    st = w.strand
+    outs = []
+    for _ in range(2):
+        eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **w.engine_kwargs())
+        eng.detect(_dev(w.u))
+        eng.assemble(_dev(w.u * 1.01), _dev(w.u))
+        torch.cuda.synchronize()
+        outs.append((eng.R.clone(), eng.K_c[: 9 * eng.pattern.nnzb].clone(), eng.K_beam.clone()))
+    for x, y in zip(outs[0], outs[1]):
+        assert torch.equal(x, y)

@@ -1,0 +1,532 @@
+// Broadphase and pair-list update.
+//
+// The reference bins AABBs into a hash grid (xkep_cae/contact/_broadphase.py:52-87)
+// and keeps the pairs whose closed AABBs overlap (:93-96); its output is the
+// set of all overlapping pairs, whatever the cell size.  Here the segments are
+// binned by the cell of their lower AABB corner on a grid whose cell is at
+// least the largest AABB extent, sorted by the Morton code of that cell, and a
+// warp per segment sweeps the 27 neighbouring cells, testing the exact double
+// AABBs and compacting hits with ballot/popc.  Filters follow
+// DetectCandidatesProcess (_manager_process.py:200-217,260-286).
+#include <cstdio>
+
+#include "xk_common.cuh"
+
+namespace {
+
+constexpr int BP_T = 128;  // 4 warps per block, one warp per segment
+
+struct Grid {
+  double origin[3];
+  double cell;
+  int dims[3];
+  int bits;
+};
+
+XK_D unsigned long long enc_min(double x) {  // order-preserving map of doubles to u64
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+XK_D double dec_min(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+XK_D unsigned long long spread21(unsigned long long v) {
+  v &= 0x1fffffull;
+  v = (v | (v << 32)) & 0x1f00000000ffffull;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+  v = (v | (v << 8)) & 0x100f00f00f00f00full;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+__global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, double* __restrict__ box,
+                       unsigned long long* __restrict__ ext) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ne = m.n_elems;
+  unsigned long long lmin[3] = {~0ull, ~0ull, ~0ull}, lmax[3] = {0ull, 0ull, 0ull}, lext = 0ull;
+  if (e < m.n_elems) {
+    int a = m.conn[2 * e], b = m.conn[2 * e + 1];
+    const double ex = xadd(m.radii[e], margin);
+    double mx = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      double x0 = u ? xadd(m.X[3LL * a + c], u[6LL * a + c]) : m.X[3LL * a + c];
+      double x1 = u ? xadd(m.X[3LL * b + c], u[6LL * b + c]) : m.X[3LL * b + c];
+      double lo = xsub(x0 < x1 ? x0 : x1, ex);
+      double hi = xadd(x0 < x1 ? x1 : x0, ex);
+      box[c * ne + e] = lo;
+      box[(3 + c) * ne + e] = hi;
+      lmin[c] = enc_min(lo);
+      lmax[c] = enc_min(hi);
+      mx = fmax(mx, hi - lo);
+    }
+    lext = (unsigned long long)__double_as_longlong(mx);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    for (int c = 0; c < 3; ++c) {
+      unsigned long long y = __shfl_down_sync(0xffffffffu, lmin[c], o);
+      lmin[c] = y < lmin[c] ? y : lmin[c];
+      y = __shfl_down_sync(0xffffffffu, lmax[c], o);
+      lmax[c] = y > lmax[c] ? y : lmax[c];
+    }
+    unsigned long long y = __shfl_down_sync(0xffffffffu, lext, o);
+    lext = y > lext ? y : lext;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int c = 0; c < 3; ++c) {
+      atomicMin(&ext[1 + c], lmin[c]);
+      atomicMax(&ext[4 + c], lmax[c]);
+    }
+    atomicMax(&ext[0], lext);
+  }
+}
+
+__global__ void k_grid(const unsigned long long* __restrict__ ext, long long cap_cells, Grid* g) {
+  double mx = __longlong_as_double((long long)ext[0]);
+  double lo[3], hi[3];
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = dec_min(ext[1 + c]);
+    hi[c] = dec_min(ext[4 + c]);
+  }
+  double cell = mx * (1.0 + 1e-6) + 1e-300;
+  long long tot;
+  int dims[3];
+  for (int it = 0; it < 200; ++it) {
+    tot = 1;
+    for (int c = 0; c < 3; ++c) {
+      double n = floor((hi[c] - lo[c]) / cell) + 1.0;
+      if (n > 2097151.0) n = 2097151.0;
+      dims[c] = (int)n;
+      tot *= dims[c];
+    }
+    if (tot <= cap_cells) break;
+    cell *= 1.25;
+  }
+  int md = max(dims[0], max(dims[1], dims[2]));
+  int b = 1;
+  while ((1 << b) < md) ++b;
+  for (int c = 0; c < 3; ++c) {
+    g->origin[c] = lo[c];
+    g->dims[c] = dims[c];
+  }
+  g->cell = cell;
+  g->bits = 3 * b;
+}
+
+XK_D void cell_of(const Grid& g, double lo0, double lo1, double lo2, int* c) {
+  const double l[3] = {lo0, lo1, lo2};
+  for (int k = 0; k < 3; ++k) {
+    double f = floor((l[k] - g.origin[k]) / g.cell);
+    int ci = (int)f;
+    c[k] = ci < 0 ? 0 : (ci >= g.dims[k] ? g.dims[k] - 1 : ci);
+  }
+}
+
+__global__ void k_keys(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
+                       unsigned long long* __restrict__ keys, int32_t* __restrict__ segs) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const Grid g = *gp;
+  int c[3];
+  cell_of(g, box[e], box[ne + e], box[2 * ne + e], c);
+  keys[e] = spread21(c[0]) | (spread21(c[1]) << 1) | (spread21(c[2]) << 2);
+  segs[e] = (int32_t)e;
+}
+
+__global__ void k_cells(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
+                        const unsigned long long* __restrict__ keys, const int32_t* __restrict__ segs,
+                        int32_t* __restrict__ cstart, int32_t* __restrict__ cend) {
+  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ne) return;
+  const Grid g = *gp;
+  int e = segs[k];
+  int c[3];
+  cell_of(g, box[e], box[ne + e], box[2 * ne + e], c);
+  long long lin = ((long long)c[2] * g.dims[1] + c[1]) * g.dims[0] + c[0];
+  if (k == 0 || keys[k] != keys[k - 1]) cstart[lin] = (int32_t)k;
+  if (k == ne - 1 || keys[k] != keys[k + 1]) cend[lin] = (int32_t)(k + 1);
+}
+
+XK_D bool overlap(const double* box, long long ne, int i, int j) {
+  for (int c = 0; c < 3; ++c)
+    if (!(box[c * ne + i] <= box[(3 + c) * ne + j]) || !(box[c * ne + j] <= box[(3 + c) * ne + i])) return false;
+  return true;
+}
+
+// MODE 0: count per segment; MODE 1: emit (i, j) sorted by j within each segment.
+template <int MODE>
+__global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restrict__ box, const Grid* __restrict__ gp,
+                                                const int32_t* __restrict__ segs, const int32_t* __restrict__ cstart,
+                                                const int32_t* __restrict__ cend, int excl_shared, int excl_layer,
+                                                int32_t* __restrict__ cnt, unsigned long long* __restrict__ raw_total,
+                                                const int32_t* __restrict__ off, int32_t* __restrict__ tmp,
+                                                int32_t* __restrict__ out) {
+  const long long ne = m.n_elems;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= ne) return;
+  const Grid g = *gp;
+  const int i = segs[w];
+  int c[3];
+  cell_of(g, box[i], box[ne + i], box[2 * ne + i], c);
+  const int ia = m.conn[2 * i], ib = m.conn[2 * i + 1];
+  const int li = (excl_layer && m.layer) ? m.layer[i] : -1;
+  int n_raw = 0, n_keep = 0;
+  const long long base = MODE == 1 ? (long long)off[i] : 0;
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int z = c[2] + dz;
+    if (z < 0 || z >= g.dims[2]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = c[1] + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int x = c[0] + dx;
+        if (x < 0 || x >= g.dims[0]) continue;
+        const long long lin = ((long long)z * g.dims[1] + y) * g.dims[0] + x;
+        const int k0 = cstart[lin], k1 = cend[lin];
+        for (int kk = k0; kk < k1; kk += 32) {
+          const int k = kk + lane;
+          bool hit = false, keep = false;
+          int j = -1;
+          if (k < k1) {
+            j = segs[k];
+            if (j > i && overlap(box, ne, i, j)) {
+              hit = true;
+              keep = true;
+              if (excl_shared) {
+                const int ja = m.conn[2 * j], jb = m.conn[2 * j + 1];
+                if (ia == ja || ia == jb || ib == ja || ib == jb) keep = false;
+              }
+              if (keep && li >= 0 && m.layer[j] == li) keep = false;
+            }
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, keep);
+          n_raw += __popc(__ballot_sync(0xffffffffu, hit));
+          if (MODE == 1 && keep) tmp[base + n_keep + __popc(bal & ((1u << lane) - 1u))] = j;
+          n_keep += __popc(bal);
+        }
+      }
+    }
+  }
+  if (MODE == 0) {
+    if (lane == 0) {
+      cnt[i] = n_keep;
+      atomicAdd(raw_total, (unsigned long long)n_raw);
+    }
+  } else {
+    __syncwarp();
+    // rank sort of this segment's list: j values are distinct
+    for (int l = lane; l < n_keep; l += 32) {
+      const int v = tmp[base + l];
+      int r = 0;
+      for (int q = 0; q < n_keep; ++q) r += tmp[base + q] < v;
+      out[2 * (base + r)] = i;
+      out[2 * (base + r) + 1] = v;
+    }
+  }
+}
+
+constexpr int RED_BLOCKS = 304, RED_T = 256;
+
+__global__ void k_radsum_partial(xk_mesh m, const int32_t* __restrict__ pairs, long long n, double* __restrict__ part) {
+  __shared__ double sm[RED_T];
+  double acc = 0.0;
+  for (long long k = (long long)blockIdx.x * RED_T + threadIdx.x; k < n; k += (long long)RED_BLOCKS * RED_T)
+    acc += xadd(m.radii[pairs[2 * k]], m.radii[pairs[2 * k + 1]]);
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = RED_T / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+__global__ void k_margin(const double* __restrict__ part, long long n, double fixed, double* __restrict__ out) {
+  if (fixed > 0.0) { *out = fixed; return; }
+  double s = 0.0;
+  for (int b = 0; b < RED_BLOCKS; ++b) s += part[b];
+  *out = xmul(xdiv(s, (double)n), 0.5);
+}
+
+__global__ void k_midpoint(xk_mesh m, const double* __restrict__ u, const int32_t* __restrict__ pairs, long long n,
+                           const double* __restrict__ extra, int32_t* __restrict__ keep) {
+  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int i = pairs[2 * k], j = pairs[2 * k + 1];
+  const int nd[4] = {m.conn[2 * i], m.conn[2 * i + 1], m.conn[2 * j], m.conn[2 * j + 1]};
+  double x[4][3];
+  for (int q = 0; q < 4; ++q)
+    for (int c = 0; c < 3; ++c) x[q][c] = u ? xadd(m.X[3LL * nd[q] + c], u[6LL * nd[q] + c]) : m.X[3LL * nd[q] + c];
+  double ma[3], mb[3], da[3], db[3], dm[3];
+  for (int c = 0; c < 3; ++c) {
+    ma[c] = xmul(0.5, xadd(x[0][c], x[1][c]));
+    mb[c] = xmul(0.5, xadd(x[2][c], x[3][c]));
+    da[c] = xsub(x[1][c], x[0][c]);
+    db[c] = xsub(x[3][c], x[2][c]);
+  }
+  for (int c = 0; c < 3; ++c) dm[c] = xsub(ma[c], mb[c]);
+  const double ha = xmul(0.5, xsqrt(xdot_seq(da, da)));
+  const double hb = xmul(0.5, xsqrt(xdot_seq(db, db)));
+  const double md = xsqrt(xdot_seq(dm, dm));
+  double mp = xsub(xsub(md, ha), hb);
+  mp = (mp > 0.0 || mp != mp) ? mp : 0.0;
+  const double cut = xadd(xadd(m.radii[i], m.radii[j]), *extra);
+  keep[k] = (mp <= cut) ? 1 : 0;
+}
+
+__global__ void k_compact_pairs(const int32_t* __restrict__ in, const int32_t* __restrict__ keep,
+                                const int32_t* __restrict__ pos, long long n, int32_t* __restrict__ out) {
+  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || !keep[k]) return;
+  long long d = pos[k];
+  out[2 * d] = in[2 * k];
+  out[2 * d + 1] = in[2 * k + 1];
+}
+
+// ------------------------------------------------------------------------- merge
+
+XK_D unsigned long long pkey(int a, int b) { return ((unsigned long long)(uint32_t)a << 32) | (uint32_t)b; }
+
+XK_D long long lower_bound_old(const xk_pairs& p, unsigned long long key) {
+  long long lo = 0, hi = p.n;
+  while (lo < hi) {
+    long long mid = (lo + hi) >> 1;
+    if (pkey(p.ea[mid], p.eb[mid]) < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+XK_D long long lower_bound_cand(const int32_t* c, long long n, unsigned long long key) {
+  long long lo = 0, hi = n;
+  while (lo < hi) {
+    long long mid = (lo + hi) >> 1;
+    if (pkey(c[2 * mid], c[2 * mid + 1]) < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+XK_D void copy_state(const xk_pairs& a, long long i, xk_pairs& b, long long j) {
+  const long long ca = a.cap, cb = b.cap;
+  b.ea[j] = a.ea[i];
+  b.eb[j] = a.eb[i];
+  b.s[j] = a.s[i];
+  b.t[j] = a.t[i];
+  b.gap[j] = a.gap[i];
+  for (int c = 0; c < 3; ++c) {
+    b.normal[c * cb + j] = a.normal[c * ca + i];
+    b.t1[c * cb + j] = a.t1[c * ca + i];
+    b.t2[c * cb + j] = a.t2[c * ca + i];
+  }
+  b.lambda_n[j] = a.lambda_n[i];
+  b.k_pen[j] = a.k_pen[i];
+  b.k_t[j] = a.k_t[i];
+  b.p_n[j] = a.p_n[i];
+  b.z_t[j] = a.z_t[i];
+  b.z_t[cb + j] = a.z_t[ca + i];
+  b.q_trial_norm[j] = a.q_trial_norm[i];
+  b.dissipation[j] = a.dissipation[i];
+  b.status[j] = a.status[i];
+  b.stick[j] = a.stick[i];
+}
+
+__global__ void k_merge_flags(xk_pairs old, const int32_t* __restrict__ cand, long long nc, int32_t* __restrict__ r) {
+  long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o > old.n) return;
+  if (o == old.n) { r[o] = 0; return; }
+  unsigned long long key = pkey(old.ea[o], old.eb[o]);
+  long long l = lower_bound_cand(cand, nc, key);
+  bool found = l < nc && pkey(cand[2 * l], cand[2 * l + 1]) == key;
+  r[o] = found ? 0 : 1;
+}
+
+__global__ void k_merge_new(xk_pairs old, const int32_t* __restrict__ cand, long long nc,
+                            const int32_t* __restrict__ R, xk_pairs out) {
+  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  unsigned long long key = pkey(cand[2 * k], cand[2 * k + 1]);
+  long long lo = lower_bound_old(old, key);
+  long long pos = k + R[lo];
+  if (lo < old.n && pkey(old.ea[lo], old.eb[lo]) == key) {
+    copy_state(old, lo, out, pos);
+    return;
+  }
+  const long long cb = out.cap;
+  out.ea[pos] = cand[2 * k];
+  out.eb[pos] = cand[2 * k + 1];
+  out.s[pos] = 0.0;
+  out.t[pos] = 0.0;
+  out.gap[pos] = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    out.normal[c * cb + pos] = 0.0;
+    out.t1[c * cb + pos] = 0.0;
+    out.t2[c * cb + pos] = 0.0;
+  }
+  out.lambda_n[pos] = 0.0;
+  out.k_pen[pos] = 0.0;
+  out.k_t[pos] = 0.0;
+  out.p_n[pos] = 0.0;
+  out.z_t[pos] = 0.0;
+  out.z_t[cb + pos] = 0.0;
+  out.q_trial_norm[pos] = 0.0;
+  out.dissipation[pos] = 0.0;
+  out.status[pos] = 0;
+  out.stick[pos] = 1;
+}
+
+__global__ void k_merge_old(xk_pairs old, const int32_t* __restrict__ cand, long long nc,
+                            const int32_t* __restrict__ r, const int32_t* __restrict__ R, xk_pairs out) {
+  long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= old.n || !r[o]) return;
+  long long pos = R[o] + lower_bound_cand(cand, nc, pkey(old.ea[o], old.eb[o]));
+  copy_state(old, o, out, pos);
+  out.status[pos] = 0;  // INACTIVE
+}
+
+struct Scratch {
+  cudaStream_t s;
+  void* p[16];
+  int n = 0;
+  template <typename T>
+  xk_status get(T** out, long long count) {
+    if (count < 1) count = 1;
+    cudaError_t e = cudaMallocAsync((void**)out, sizeof(T) * count, s);
+    if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);
+    p[n++] = *out;
+    return XK_OK;
+  }
+  ~Scratch() {
+    for (int i = 0; i < n; ++i) cudaFreeAsync(p[i], s);
+  }
+};
+
+#define XK_TRY(x)                  \
+  do {                             \
+    xk_status r__ = (x);           \
+    if (r__ != XK_OK) return r__;  \
+  } while (0)
+
+}  // namespace
+
+extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_bp_params* bp, int32_t* out_pairs,
+                                   int64_t cap, int64_t* n_out, int64_t* n_raw, int64_t* n_prefilter, xk_stream s) {
+  if (!m || !bp || !n_out) return xk_set_error(XK_ERR_ARG, "xk_broadphase: null argument");
+  cudaStream_t st = (cudaStream_t)s;
+  *n_out = 0;
+  if (n_raw) *n_raw = 0;
+  if (n_prefilter) *n_prefilter = 0;
+  const long long ne = m->n_elems;
+  if (ne < 2) return XK_OK;
+  Scratch S{st};
+  double* box;
+  unsigned long long* ext;
+  Grid* grid;
+  XK_TRY(S.get(&box, 6 * ne));
+  XK_TRY(S.get(&ext, 8));
+  XK_TRY(S.get(&grid, 1));
+  unsigned long long init[8] = {0ull, ~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull};
+  XK_CUDA(cudaMemcpyAsync(ext, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  k_aabb<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, u, bp->margin, box, ext);
+  const long long cap_cells = ne * 8 > 4096 ? ne * 8 : 4096;
+  k_grid<<<1, 1, 0, st>>>(ext, cap_cells, grid);
+  XK_CHECK_LAUNCH();
+  Grid hg;
+  XK_CUDA(cudaMemcpyAsync(&hg, grid, sizeof(Grid), cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaStreamSynchronize(st));
+  const long long ncell = (long long)hg.dims[0] * hg.dims[1] * hg.dims[2];
+  unsigned long long* keys;
+  int32_t *segs, *cstart, *cend, *cnt, *off;
+  XK_TRY(S.get(&keys, ne));
+  XK_TRY(S.get(&segs, ne));
+  XK_TRY(S.get(&cstart, ncell));
+  XK_TRY(S.get(&cend, ncell));
+  XK_TRY(S.get(&cnt, ne + 1));
+  XK_TRY(S.get(&off, ne + 1));
+  k_keys<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, keys, segs);
+  XK_CHECK_LAUNCH();
+  XK_TRY(xk_radix_sort_u64((uint64_t*)keys, segs, ne, hg.bits, st));
+  XK_CUDA(cudaMemsetAsync(cstart, 0, sizeof(int32_t) * ncell, st));
+  XK_CUDA(cudaMemsetAsync(cend, 0, sizeof(int32_t) * ncell, st));
+  k_cells<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, keys, segs, cstart, cend);
+  XK_CHECK_LAUNCH();
+  unsigned long long* raw_dev = ext + 7;
+  XK_CUDA(cudaMemsetAsync(raw_dev, 0, sizeof(unsigned long long), st));
+  XK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (ne + 1), st));
+  const int sweep_blocks = xk_blocks(ne * 32, BP_T);
+  const int excl_layer = (bp->exclude_same_layer && m->layer) ? 1 : 0;
+  k_sweep<0><<<sweep_blocks, BP_T, 0, st>>>(*m, box, grid, segs, cstart, cend, bp->exclude_shared, excl_layer, cnt,
+                                             raw_dev, nullptr, nullptr, nullptr);
+  XK_CHECK_LAUNCH();
+  int64_t* tot;
+  XK_TRY(S.get(&tot, 2));
+  XK_TRY(xk_exclusive_scan_i32(cnt, off, ne + 1, tot, st));
+  int64_t h[2];
+  unsigned long long hraw = 0;
+  XK_CUDA(cudaMemcpyAsync(h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaMemcpyAsync(&hraw, raw_dev, sizeof(hraw), cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaStreamSynchronize(st));
+  const long long n1 = h[0];
+  if (n_raw) *n_raw = (int64_t)hraw;
+  if (n_prefilter) *n_prefilter = n1;
+  if (n1 == 0) return XK_OK;
+  if (n1 > 0x7fffffffLL) return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: more than 2^31 candidates");
+  int32_t *tmp, *pairs1;
+  XK_TRY(S.get(&tmp, n1));
+  XK_TRY(S.get(&pairs1, 2 * n1));
+  k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, box, grid, segs, cstart, cend, bp->exclude_shared, excl_layer, cnt,
+                                             raw_dev, off, tmp, pairs1);
+  XK_CHECK_LAUNCH();
+  if (!bp->midpoint_prescreening) {
+    *n_out = n1;
+    if (n1 > cap) return xk_set_error(XK_ERR_CAPACITY, "xk_broadphase: output capacity too small");
+    XK_CUDA(cudaMemcpyAsync(out_pairs, pairs1, sizeof(int32_t) * 2 * n1, cudaMemcpyDeviceToDevice, st));
+    XK_CUDA(cudaStreamSynchronize(st));
+    return XK_OK;
+  }
+  double *part, *extra;
+  int32_t *keep, *pos;
+  XK_TRY(S.get(&part, RED_BLOCKS));
+  XK_TRY(S.get(&extra, 1));
+  XK_TRY(S.get(&keep, n1));
+  XK_TRY(S.get(&pos, n1));
+  if (!(bp->prescreening_margin > 0.0))
+    k_radsum_partial<<<RED_BLOCKS, RED_T, 0, st>>>(*m, pairs1, n1, part);
+  k_margin<<<1, 1, 0, st>>>(part, n1, bp->prescreening_margin, extra);
+  k_midpoint<<<xk_blocks(n1, 256), 256, 0, st>>>(*m, u, pairs1, n1, extra, keep);
+  XK_CHECK_LAUNCH();
+  XK_TRY(xk_exclusive_scan_i32(keep, pos, n1, tot + 1, st));
+  XK_CUDA(cudaMemcpyAsync(h + 1, tot + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaStreamSynchronize(st));
+  *n_out = h[1];
+  if (h[1] > cap) return xk_set_error(XK_ERR_CAPACITY, "xk_broadphase: output capacity too small");
+  k_compact_pairs<<<xk_blocks(n1, 256), 256, 0, st>>>(pairs1, keep, pos, n1, out_pairs);
+  XK_CHECK_LAUNCH();
+  XK_CUDA(cudaStreamSynchronize(st));
+  return XK_OK;
+}
+
+extern "C" xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const int32_t* cands, int64_t n_cands,
+                                    xk_pairs* out, xk_stream s) {
+  if (!m || !old || !out || (n_cands > 0 && !cands)) return xk_set_error(XK_ERR_ARG, "xk_pairs_merge: null argument");
+  if ((long long)out->cap < (long long)old->n + n_cands)
+    return xk_set_error(XK_ERR_CAPACITY, "xk_pairs_merge: out->cap < old->n + n_cands");
+  cudaStream_t st = (cudaStream_t)s;
+  Scratch S{st};
+  int32_t *r, *R;
+  int64_t* tot;
+  XK_TRY(S.get(&r, (long long)old->n + 1));
+  XK_TRY(S.get(&R, (long long)old->n + 1));
+  XK_TRY(S.get(&tot, 1));
+  k_merge_flags<<<xk_blocks((long long)old->n + 1, 256), 256, 0, st>>>(*old, cands, n_cands, r);
+  XK_CHECK_LAUNCH();
+  XK_TRY(xk_exclusive_scan_i32(r, R, (long long)old->n + 1, tot, st));
+  if (n_cands > 0) k_merge_new<<<xk_blocks(n_cands, 256), 256, 0, st>>>(*old, cands, n_cands, R, *out);
+  if (old->n > 0) k_merge_old<<<xk_blocks(old->n, 256), 256, 0, st>>>(*old, cands, n_cands, r, R, *out);
+  XK_CHECK_LAUNCH();
+  int64_t h = 0;
+  XK_CUDA(cudaMemcpyAsync(&h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaStreamSynchronize(st));
+  out->n = (int32_t)(n_cands + h);
+  return XK_OK;
+}

@@ -1,0 +1,543 @@
+// Contact pairs: narrowphase, Huber normal force, Coulomb return mapping and
+// the factorised pair tangent, one pair per thread over the SoA pair table.
+#include "xk_common.cuh"
+
+namespace {
+
+constexpr int PAIR_T = 256;
+constexpr uint8_t ST_INACTIVE = 0, ST_ACTIVE = 1, ST_SLIDING = 2;
+
+struct PairNodes {
+  int n[4];
+};
+
+XK_D PairNodes pair_nodes(const xk_mesh& m, int ea, int eb) {
+  PairNodes p;
+  p.n[0] = m.conn[2 * ea];
+  p.n[1] = m.conn[2 * ea + 1];
+  p.n[2] = m.conn[2 * eb];
+  p.n[3] = m.conn[2 * eb + 1];
+  return p;
+}
+
+// Deformed coordinates X + u[0:3] (DeformedCoordsProcess, contact/solver/_utils.py:16-28).
+XK_D void deformed(const xk_mesh& m, const double* u, int node, double* x) {
+  x[0] = xadd(m.X[3LL * node], u[6LL * node]);
+  x[1] = xadd(m.X[3LL * node + 1], u[6LL * node + 1]);
+  x[2] = xadd(m.X[3LL * node + 2], u[6LL * node + 2]);
+}
+
+// _closest_point_segments_batch (geometry/_compute.py:55-151), operation for operation.
+XK_D void closest_exact(const double* xA0, const double* xA1, const double* xB0, const double* xB1, double& s,
+                        double& t, double& dist, double* normal, double* diff) {
+  const double TOL = 1e-10;
+  double dA[3], dB[3], w0[3];
+  for (int i = 0; i < 3; ++i) {
+    dA[i] = xsub(xA1[i], xA0[i]);
+    dB[i] = xsub(xB1[i], xB0[i]);
+    w0[i] = xsub(xA0[i], xB0[i]);
+  }
+  const double a = xdot_es(dA, dA), b = xdot_es(dA, dB), c = xdot_es(dB, dB);
+  const double d = xdot_es(dA, w0), e = xdot_es(dB, w0);
+  const double det = xsub(xmul(a, c), xmul(b, b));
+  double ac = xmul(a, c);
+  if (!(ac >= 1e-30)) ac = (ac != ac) ? ac : 1e-30;  // np.maximum keeps NaN
+  const bool par = det < xmul(TOL, ac);
+  const double sdet = par ? 1.0 : det;
+  const double s_unc = par ? 0.0 : xdiv(xsub(xmul(b, e), xmul(c, d)), sdet);
+  const double t_unc = par ? 0.0 : xdiv(xsub(xmul(a, e), xmul(b, d)), sdet);
+  const bool cok = c > TOL, aok = a > TOL;
+  const double sc = cok ? c : 1.0, sa = aok ? a : 1.0;
+  s = par ? 0.0 : xclip01(s_unc);
+  t = par ? (cok ? xclip01(xdiv(e, sc)) : 0.0) : xclip01(t_unc);
+  const bool s_cl = (s_unc < 0.0) || (s_unc > 1.0);
+  const bool t_cl = (t_unc < 0.0) || (t_unc > 1.0);
+  if (s_cl && !par) t = cok ? xclip01(xdiv(xadd(xmul(b, s), e), sc)) : 0.0;
+  if (t_cl && !par) {
+    s = aok ? xclip01(xdiv(xsub(xmul(b, t), d), sa)) : 0.0;
+    t = cok ? xclip01(xdiv(xadd(xmul(b, s), e), sc)) : 0.0;
+  }
+  for (int i = 0; i < 3; ++i) diff[i] = xsub(xadd(xA0[i], xmul(s, dA[i])), xadd(xB0[i], xmul(t, dB[i])));
+  dist = xsqrt(xdot_es(diff, diff));
+  const double sd = (dist >= 1e-30 || dist != dist) ? dist : 1e-30;
+  for (int i = 0; i < 3; ++i) normal[i] = xdiv(diff[i], sd);
+  if (dist < 1e-30) { normal[0] = 0.0; normal[1] = 0.0; normal[2] = 1.0; }
+}
+
+// _build_contact_frame_batch (geometry/_compute.py:154-261) for one pair, reference op order.
+XK_D void frame_exact(const double* nrm, const double* pt1, const double* pn, double* n, double* t1, double* t2) {
+  double nn = xsqrt(xdot_es(nrm, nrm));
+  if (!(nn >= 1e-30)) nn = (nn != nn) ? nn : 1e-30;
+  for (int i = 0; i < 3; ++i) n[i] = xdiv(nrm[i], nn);
+  const bool has_t1 = xsqrt(xdot_es(pt1, pt1)) > 1e-10;
+  const double pnn = xsqrt(xdot_es(pn, pn));
+  const bool has_n = pnn > 1e-10;
+  bool done = false;
+  if (has_t1 && has_n) {
+    double so = (pnn >= 1e-30) ? pnn : 1e-30;
+    double no[3] = {xdiv(pn[0], so), xdiv(pn[1], so), xdiv(pn[2], so)};
+    double v[3];
+    xcross(no, n, v);
+    const double sv = xsqrt(xdot_es(v, v));
+    const double cv = xdot_es(no, n);
+    double tr[3] = {pt1[0], pt1[1], pt1[2]};
+    if (sv >= 1e-12) {
+      double vx[3], vvx[3];
+      xcross(v, pt1, vx);
+      xcross(v, vx, vvx);
+      const double f = xdiv(xsub(1.0, cv), xmul(sv, sv));
+      for (int i = 0; i < 3; ++i) tr[i] = xadd(xadd(pt1[i], vx[i]), xmul(f, vvx[i]));
+    }
+    const double dn = xdot_es(tr, n);
+    double raw[3];
+    for (int i = 0; i < 3; ++i) raw[i] = xsub(tr[i], xmul(dn, n[i]));
+    const double nr = xsqrt(xdot_es(raw, raw));
+    if (nr > 1e-10) {
+      for (int i = 0; i < 3; ++i) t1[i] = xdiv(raw[i], nr);
+      xcross(n, t1, t2);
+      done = true;
+    }
+  }
+  if (!done && has_t1) {
+    const double dn = xdot_es(pt1, n);
+    double raw[3];
+    for (int i = 0; i < 3; ++i) raw[i] = xsub(pt1[i], xmul(dn, n[i]));
+    const double nr = xsqrt(xdot_es(raw, raw));
+    if (nr > 1e-10) {
+      for (int i = 0; i < 3; ++i) t1[i] = xdiv(raw[i], nr);
+      xcross(n, t1, t2);
+      done = true;
+    }
+  }
+  if (!done) {
+    double ref[3] = {0.0, 0.0, 0.0};
+    const double a0 = fabs(n[0]), a1 = fabs(n[1]), a2 = fabs(n[2]);
+    ref[(a0 <= a1 && a0 <= a2) ? 0 : (a1 <= a2 ? 1 : 2)] = 1.0;
+    const double dn = xdot_es(ref, n);
+    double raw[3];
+    for (int i = 0; i < 3; ++i) raw[i] = xsub(ref[i], xmul(dn, n[i]));
+    double nr = xsqrt(xdot_es(raw, raw));
+    if (!(nr >= 1e-30)) nr = (nr != nr) ? nr : 1e-30;
+    for (int i = 0; i < 3; ++i) t1[i] = xdiv(raw[i], nr);
+    xcross(n, t1, t2);
+  }
+}
+
+// Mixed-precision closest point: the difference vectors and the distance are
+// double, the 2x2 parameter solve is float unless the segments are close to
+// parallel, in which case the exact routine decides.
+XK_D void closest_mixed(const double* xA0, const double* xA1, const double* xB0, const double* xB1, double& s,
+                        double& t, double& dist, double* normal) {
+  double dA[3], dB[3], w0[3];
+  for (int i = 0; i < 3; ++i) {
+    dA[i] = xA1[i] - xA0[i];
+    dB[i] = xB1[i] - xB0[i];
+    w0[i] = xA0[i] - xB0[i];
+  }
+  float fa[3] = {(float)dA[0], (float)dA[1], (float)dA[2]};
+  float fb[3] = {(float)dB[0], (float)dB[1], (float)dB[2]};
+  float fw[3] = {(float)w0[0], (float)w0[1], (float)w0[2]};
+  float a = dot3(fa, fa), b = dot3(fa, fb), c = dot3(fb, fb), d = dot3(fa, fw), e = dot3(fb, fw);
+  float ac = a * c;
+  float det = ac - b * b;
+  if (!(det > 1e-3f * ac)) {  // near-parallel or degenerate: exact double routine
+    double diff[3];
+    closest_exact(xA0, xA1, xB0, xB1, s, t, dist, normal, diff);
+    return;
+  }
+  float idet = 1.0f / det;
+  float su = (b * e - c * d) * idet, tu = (a * e - b * d) * idet;
+  float sf = fminf(fmaxf(su, 0.0f), 1.0f), tf = fminf(fmaxf(tu, 0.0f), 1.0f);
+  if (su < 0.0f || su > 1.0f) tf = fminf(fmaxf((b * sf + e) / c, 0.0f), 1.0f);
+  if (tu < 0.0f || tu > 1.0f) {
+    sf = fminf(fmaxf((b * tf - d) / a, 0.0f), 1.0f);
+    tf = fminf(fmaxf((b * sf + e) / c, 0.0f), 1.0f);
+  }
+  s = sf;
+  t = tf;
+  double diff[3];
+  for (int i = 0; i < 3; ++i) diff[i] = w0[i] + s * dA[i] - t * dB[i];
+  dist = sqrt(diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]);
+  if (dist < 1e-30) { normal[0] = 0.0; normal[1] = 0.0; normal[2] = 1.0; return; }
+  const double id = 1.0 / dist;
+  for (int i = 0; i < 3; ++i) normal[i] = diff[i] * id;
+}
+
+// Frame transport in float; (1-c)/s^2 is written 1/(1+c), equal for unit vectors.
+XK_D void frame_mixed(const double* nrm, const double* pt1d, const double* pnd, double* nout, double* t1o,
+                      double* t2o) {
+  float n[3] = {(float)nrm[0], (float)nrm[1], (float)nrm[2]};
+  float inv = rsqrtf(fmaxf(dot3(n, n), 1e-30f));
+  for (int i = 0; i < 3; ++i) n[i] *= inv;
+  float pt1[3] = {(float)pt1d[0], (float)pt1d[1], (float)pt1d[2]};
+  float pn[3] = {(float)pnd[0], (float)pnd[1], (float)pnd[2]};
+  const bool has_t1 = dot3(pt1, pt1) > 1e-20f, has_n = dot3(pn, pn) > 1e-20f;
+  float t1[3], t2[3];
+  bool done = false;
+  if (has_t1) {
+    float tr[3] = {pt1[0], pt1[1], pt1[2]};
+    if (has_n) {
+      float ip = rsqrtf(dot3(pn, pn));
+      float no[3] = {pn[0] * ip, pn[1] * ip, pn[2] * ip};
+      float v[3], vx[3], vvx[3];
+      cross3(no, n, v);
+      float cv = dot3(no, n);
+      if (cv > -0.99f) {
+        cross3(v, pt1, vx);
+        cross3(v, vx, vvx);
+        float f = 1.0f / (1.0f + cv);
+        for (int i = 0; i < 3; ++i) tr[i] = pt1[i] + vx[i] + f * vvx[i];
+      }
+    }
+    float dn = dot3(tr, n);
+    float raw[3] = {tr[0] - dn * n[0], tr[1] - dn * n[1], tr[2] - dn * n[2]};
+    float r2 = dot3(raw, raw);
+    if (r2 > 1e-20f) {
+      float ir = rsqrtf(r2);
+      for (int i = 0; i < 3; ++i) t1[i] = raw[i] * ir;
+      done = true;
+    }
+  }
+  if (!done) {
+    float ref[3] = {0.f, 0.f, 0.f};
+    float a0 = fabsf(n[0]), a1 = fabsf(n[1]), a2 = fabsf(n[2]);
+    ref[(a0 <= a1 && a0 <= a2) ? 0 : (a1 <= a2 ? 1 : 2)] = 1.0f;
+    float dn = dot3(ref, n);
+    float raw[3] = {ref[0] - dn * n[0], ref[1] - dn * n[1], ref[2] - dn * n[2]};
+    float ir = rsqrtf(fmaxf(dot3(raw, raw), 1e-30f));
+    for (int i = 0; i < 3; ++i) t1[i] = raw[i] * ir;
+  }
+  cross3(n, t1, t2);
+  for (int i = 0; i < 3; ++i) { nout[i] = n[i]; t1o[i] = t1[i]; t2o[i] = t2[i]; }
+}
+
+XK_D void load3(const double* base, long long stride, long long i, double* v) {
+  v[0] = base[i];
+  v[1] = base[stride + i];
+  v[2] = base[2 * stride + i];
+}
+XK_D void store3(double* base, long long stride, long long i, const double* v) {
+  base[i] = v[0];
+  base[stride + i] = v[1];
+  base[2 * stride + i] = v[2];
+}
+
+__global__ void k_narrow_exact(xk_mesh m, xk_pairs p, const double* __restrict__ u, double g_on, double g_off,
+                               int allow_deact, int update_active) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const long long cap = p.cap;
+  PairNodes nd = pair_nodes(m, p.ea[i], p.eb[i]);
+  double x[4][3];
+  for (int k = 0; k < 4; ++k) deformed(m, u, nd.n[k], x[k]);
+  double s, t, dist, nrm[3], diff[3];
+  closest_exact(x[0], x[1], x[2], x[3], s, t, dist, nrm, diff);
+  const double gap = xsub(dist, xadd(m.radii[p.ea[i]], m.radii[p.eb[i]]));
+  double pt1[3], pn[3], n[3], t1[3], t2[3];
+  load3(p.t1, cap, i, pt1);
+  load3(p.normal, cap, i, pn);
+  frame_exact(nrm, pt1, pn, n, t1, t2);
+  p.s[i] = s;
+  p.t[i] = t;
+  p.gap[i] = gap;
+  store3(p.normal, cap, i, n);
+  store3(p.t1, cap, i, t1);
+  store3(p.t2, cap, i, t2);
+  if (update_active) {  // _update_active_set_state (_manager_process.py:475-494)
+    uint8_t st = p.status[i];
+    if (st == ST_INACTIVE) {
+      if (gap <= g_on) p.status[i] = ST_ACTIVE;
+    } else if (allow_deact && gap >= g_off) {
+      p.status[i] = ST_INACTIVE;
+    }
+  }
+}
+
+XK_HD double huber(double x, double d) {  // contact_force/strategy.py:104-113
+  if (d <= 0.0) return x > 0.0 ? x : 0.0;
+  if (x < -d) return 0.0;
+  if (x > d) return x;
+  return (x + d) * (x + d) / (4.0 * d);
+}
+XK_HD double huber_deriv(double x, double d) {  // contact_force/strategy.py:115-124
+  if (d <= 0.0) return x > 0.0 ? 1.0 : 0.0;
+  if (x < -d) return 0.0;
+  if (x > d) return 1.0;
+  return (x + d) / (2.0 * d);
+}
+
+template <int P, int OUT>
+__global__ void __launch_bounds__(PAIR_T) k_pair(xk_mesh m, xk_pairs p, const double* __restrict__ u,
+                                                 const double* __restrict__ u_ref, xk_contact_params cp, int stages,
+                                                 typename Prec<P>::T* __restrict__ pv,
+                                                 typename Prec<P>::T* __restrict__ pB, long long ostride) {
+  typedef typename Prec<P>::T T;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const long long cap = p.cap;
+  const int ea = p.ea[i], eb = p.eb[i];
+  uint8_t status = p.status[i];
+  double p_n = p.p_n[i];
+  const bool member = (status != ST_INACTIVE) || (p_n > 0.0);
+  if (!member && !(stages & XK_STAGE_NARROW)) return;
+  const PairNodes nd = pair_nodes(m, ea, eb);
+  const double ra = m.radii[ea], rb = m.radii[eb];
+  double s, t, gap, n[3], t1[3], t2[3];
+  if (stages & XK_STAGE_NARROW) {
+    double x[4][3];
+    for (int k = 0; k < 4; ++k) {
+      x[k][0] = m.X[3LL * nd.n[k]] + u[6LL * nd.n[k]];
+      x[k][1] = m.X[3LL * nd.n[k] + 1] + u[6LL * nd.n[k] + 1];
+      x[k][2] = m.X[3LL * nd.n[k] + 2] + u[6LL * nd.n[k] + 2];
+    }
+    double dist, nrm[3], pt1[3], pn[3];
+    load3(p.t1, cap, i, pt1);
+    load3(p.normal, cap, i, pn);
+    if (P == XK_FP64) {
+      double diff[3];
+      closest_exact(x[0], x[1], x[2], x[3], s, t, dist, nrm, diff);
+      gap = xsub(dist, xadd(ra, rb));
+      frame_exact(nrm, pt1, pn, n, t1, t2);
+    } else {
+      closest_mixed(x[0], x[1], x[2], x[3], s, t, dist, nrm);
+      gap = dist - (ra + rb);
+      frame_mixed(nrm, pt1, pn, n, t1, t2);
+    }
+    p.s[i] = s;
+    p.t[i] = t;
+    p.gap[i] = gap;
+    store3(p.normal, cap, i, n);
+    store3(p.t1, cap, i, t1);
+    store3(p.t2, cap, i, t2);
+  } else {
+    s = p.s[i];
+    t = p.t[i];
+    gap = p.gap[i];
+    load3(p.normal, cap, i, n);
+    load3(p.t1, cap, i, t1);
+    load3(p.t2, cap, i, t2);
+  }
+  if (!member) return;
+  const double dh = cp.smoothing_delta > 0.0 ? cp.k_pen / cp.smoothing_delta : 0.0;
+  const double xpen = cp.k_pen * (-gap);
+  T vn[3] = {T(0), T(0), T(0)}, vf[3] = {T(0), T(0), T(0)};
+  const T nT[3] = {(T)n[0], (T)n[1], (T)n[2]};
+  const T t1T[3] = {(T)t1[0], (T)t1[1], (T)t1[2]};
+  const T t2T[3] = {(T)t2[0], (T)t2[1], (T)t2[2]};
+  // ---------------------------------------------------------------- normal force
+  if ((stages & XK_STAGE_NORMAL) && status != ST_INACTIVE) {
+    p_n = huber(xpen, dh);
+    p.p_n[i] = p_n;
+    if (p_n > 1e-30)
+      for (int k = 0; k < 3; ++k) vn[k] = (T)p_n * nT[k];
+  }
+  // ---------------------------------------------------------------- friction
+  double kt = p.k_t[i];
+  double zt0 = p.z_t[i], zt1 = p.z_t[cap + i];
+  double qtn = p.q_trial_norm[i];
+  bool stick = p.stick[i] != 0;
+  const bool fproc = (p_n > 0.0) && (cp.mu_eff > 0.0);
+  if ((stages & XK_STAGE_FRICTION) && fproc) {
+    if (p.k_pen[i] <= 0.0) {
+      p.k_pen[i] = cp.k_pen;
+      kt = cp.k_pen * cp.k_t_ratio;
+      p.k_t[i] = kt;
+    }
+    T du[4][3];
+    for (int k = 0; k < 4; ++k)
+      for (int c = 0; c < 3; ++c) {
+        long long dof = 6LL * nd.n[k] + c;
+        du[k][c] = (T)(u_ref ? u[dof] - u_ref[dof] : u[dof]);
+      }
+    const T sT = (T)s, tT = (T)t;
+    T dr[3];
+    for (int c = 0; c < 3; ++c)
+      dr[c] = ((T(1) - tT) * du[2][c] + tT * du[3][c]) - ((T(1) - sT) * du[0][c] + sT * du[1][c]);
+    const T d0 = dot3(dr, t1T), d1 = dot3(dr, t2T);
+    const T ktT = (T)kt;
+    const T q0 = (T)zt0 + ktT * d0, q1 = (T)zt1 + ktT * d1;
+    const T qn = my_sqrt<T>(q0 * q0 + q1 * q1);
+    const T fy = (T)cp.mu_eff * (T)p_n;
+    stick = qn <= fy;
+    T r0 = q0, r1 = q1;
+    if (!stick) { r0 = fy * q0 / qn; r1 = fy * q1 / qn; }
+    zt0 = r0;
+    zt1 = r1;
+    qtn = qn;
+    p.z_t[i] = zt0;
+    p.z_t[cap + i] = zt1;
+    p.stick[i] = stick ? 1 : 0;
+    p.q_trial_norm[i] = qtn;
+    p.dissipation[i] = (double)(r0 * d0 + r1 * d1);
+    status = stick ? ST_ACTIVE : ST_SLIDING;
+    p.status[i] = status;
+    if (my_sqrt<T>(r0 * r0 + r1 * r1) >= T(1e-30)) {
+      const T a0 = fabs(r0) < T(1e-30) ? T(0) : r0, a1 = fabs(r1) < T(1e-30) ? T(0) : r1;
+      for (int k = 0; k < 3; ++k) vf[k] = a0 * t1T[k] + a1 * t2T[k];
+    }
+  }
+  // ---------------------------------------------------------------- tangent
+  T Bn[9], Bf[9];
+  for (int k = 0; k < 9; ++k) { Bn[k] = T(0); Bf[k] = T(0); }
+  if ((stages & XK_STAGE_TANGENT) && status != ST_INACTIVE) {
+    const double dist = (gap + ra) + rb;
+    const double hd = huber_deriv(xpen, dh);
+    if (!(hd < 1e-30 && p_n < 1e-30)) {
+      const T wm = (T)(hd * cp.k_pen);
+      const T wg = (T)(dist > 1e-15 ? p_n / dist : 0.0);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          T nn = nT[a] * nT[b];
+          Bn[3 * a + b] = wm * nn - wg * ((a == b ? T(1) : T(0)) - nn);
+        }
+    }
+    const T q0 = (T)zt0, q1 = (T)zt1;
+    const T qnorm = my_sqrt<T>(q0 * q0 + q1 * q1);
+    if (fproc && qnorm >= T(1e-30)) {
+      const T ktT = (T)kt;
+      T D00 = ktT, D01 = T(0), D11 = ktT;
+      if (!stick && qnorm >= T(1e-30) && (T)qtn >= T(1e-30)) {
+        const T qh0 = q0 / qnorm, qh1 = q1 / qnorm;
+        const T ratio = (T)cp.mu_eff * (T)p_n / (T)qtn;
+        D00 = ratio * ktT * (T(1) - qh0 * qh0);
+        D01 = -ratio * ktT * qh0 * qh1;
+        D11 = ratio * ktT * (T(1) - qh1 * qh1);
+      }
+      if (fabs(D00) < T(1e-30)) D00 = T(0);
+      if (fabs(D01) < T(1e-30)) D01 = T(0);
+      if (fabs(D11) < T(1e-30)) D11 = T(0);
+      const bool geo = (dist >= 1e-15) && !(fabs(q0) < T(1e-30) && fabs(q1) < T(1e-30));
+      const T idist = geo ? (T)(1.0 / dist) : T(0);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          T mat = D00 * t1T[a] * t1T[b] + D01 * (t1T[a] * t2T[b] + t2T[a] * t1T[b]) + D11 * t2T[a] * t2T[b];
+          T M = -q0 * nT[a] * t1T[b] - q1 * t2T[a] * nT[b];
+          Bf[3 * a + b] = mat + idist * M;
+        }
+      // q2 [t1]x^T
+      Bf[1] += idist * q1 * t1T[2];
+      Bf[2] -= idist * q1 * t1T[1];
+      Bf[3] -= idist * q1 * t1T[2];
+      Bf[5] += idist * q1 * t1T[0];
+      Bf[6] += idist * q1 * t1T[1];
+      Bf[7] -= idist * q1 * t1T[0];
+    }
+  }
+  // ---------------------------------------------------------------- outputs
+  if (OUT == XK_OUT_COMBINED) {
+    if (pv)
+      for (int k = 0; k < 3; ++k) pv[k * ostride + i] = vn[k] + vf[k];
+    if (pB)
+      for (int k = 0; k < 9; ++k) pB[k * ostride + i] = Bn[k] - Bf[k];
+  } else {
+    if (pv) {
+      if (stages & XK_STAGE_NORMAL)
+        for (int k = 0; k < 3; ++k) pv[k * ostride + i] = vn[k];
+      if (stages & XK_STAGE_FRICTION)
+        for (int k = 0; k < 3; ++k) pv[(3 + k) * ostride + i] = vf[k];
+    }
+    if (pB && (stages & XK_STAGE_TANGENT)) {
+      for (int k = 0; k < 9; ++k) pB[k * ostride + i] = Bn[k];
+      for (int k = 0; k < 9; ++k) pB[(9 + k) * ostride + i] = Bf[k];
+    }
+  }
+}
+
+__global__ void k_active_flags(xk_pairs p, int32_t* __restrict__ flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p.n) flag[i] = p.status[i] != ST_INACTIVE ? 1 : 0;
+}
+
+__global__ void k_jacobian(xk_mesh m, xk_pairs p, const int32_t* __restrict__ off, int32_t* __restrict__ rows,
+                           int32_t* __restrict__ cols, double* __restrict__ vals, int32_t* __restrict__ pidx) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n || p.status[i] == ST_INACTIVE) return;
+  const long long cap = p.cap;
+  int r = off[i];
+  PairNodes nd = pair_nodes(m, p.ea[i], p.eb[i]);
+  double s = p.s[i], t = p.t[i];
+  double c[4] = {1.0 - s, s, -(1.0 - t), -t};
+  if (pidx) pidx[r] = i;
+  for (int k = 0; k < 4; ++k)
+    for (int d = 0; d < 3; ++d) {
+      long long o = 12LL * r + 3 * k + d;
+      rows[o] = r;
+      cols[o] = 6 * nd.n[k] + d;
+      vals[o] = c[k] * p.normal[d * cap + i];
+    }
+}
+
+}  // namespace
+
+extern "C" xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double* u, const xk_contact_params* cp,
+                                    int update_active, xk_stream s) {
+  if (!m || !p || !u || !cp) return xk_set_error(XK_ERR_ARG, "xk_narrowphase: null argument");
+  if (p->n == 0) return XK_OK;
+  k_narrow_exact<<<xk_blocks(p->n, PAIR_T), PAIR_T, 0, (cudaStream_t)s>>>(*m, *p, u, cp->g_on, cp->g_off,
+                                                                          cp->allow_deactivation, update_active);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
+extern "C" xk_status xk_pair_eval(const xk_mesh* m, xk_pairs* p, const double* u, const double* u_ref,
+                                  const xk_contact_params* cp, int stages, int precision, int out_mode, void* pv,
+                                  void* pB, int64_t out_stride, xk_stream s) {
+  if (!m || !p || !cp) return xk_set_error(XK_ERR_ARG, "xk_pair_eval: null argument");
+  if (((stages & XK_STAGE_NARROW) || (stages & XK_STAGE_FRICTION)) && !u)
+    return xk_set_error(XK_ERR_ARG, "xk_pair_eval: u is required for the narrowphase and friction stages");
+  if (out_mode == XK_OUT_COMBINED && (stages & (XK_STAGE_NORMAL | XK_STAGE_FRICTION | XK_STAGE_TANGENT)) !=
+                                         (XK_STAGE_NORMAL | XK_STAGE_FRICTION | XK_STAGE_TANGENT))
+    return xk_set_error(XK_ERR_ARG, "xk_pair_eval: the combined output needs the normal, friction and tangent stages");
+  if (out_stride < p->n) return xk_set_error(XK_ERR_ARG, "xk_pair_eval: out_stride < n");
+  if (p->n == 0) return XK_OK;
+  cudaStream_t st = (cudaStream_t)s;
+  const int nb = xk_blocks(p->n, PAIR_T);
+#define XK_PAIR_LAUNCH(PP, OO, TT) \
+  k_pair<PP, OO><<<nb, PAIR_T, 0, st>>>(*m, *p, u, u_ref, *cp, stages, (TT*)pv, (TT*)pB, out_stride)
+  if (precision == XK_FP64) {
+    if (out_mode == XK_OUT_COMBINED) XK_PAIR_LAUNCH(XK_FP64, XK_OUT_COMBINED, double);
+    else XK_PAIR_LAUNCH(XK_FP64, XK_OUT_SPLIT, double);
+  } else if (precision == XK_MIXED) {
+    if (out_mode == XK_OUT_COMBINED) XK_PAIR_LAUNCH(XK_MIXED, XK_OUT_COMBINED, float);
+    else XK_PAIR_LAUNCH(XK_MIXED, XK_OUT_SPLIT, float);
+  } else {
+    return xk_set_error(XK_ERR_ARG, "xk_pair_eval: precision");
+  }
+#undef XK_PAIR_LAUNCH
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
+extern "C" xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p, int32_t* rows, int32_t* cols,
+                                            double* vals, int32_t* pair_index, int64_t cap, int64_t* n_rows,
+                                            xk_stream s) {
+  if (!m || !p || !n_rows) return xk_set_error(XK_ERR_ARG, "xk_constraint_jacobian: null argument");
+  cudaStream_t st = (cudaStream_t)s;
+  *n_rows = 0;
+  if (p->n == 0) return XK_OK;
+  int32_t* flag = nullptr;
+  int64_t* tot = nullptr;
+  XK_CUDA(cudaMallocAsync((void**)&flag, sizeof(int32_t) * p->n, st));
+  XK_CUDA(cudaMallocAsync((void**)&tot, sizeof(int64_t), st));
+  k_active_flags<<<xk_blocks(p->n, 256), 256, 0, st>>>(*p, flag);
+  xk_status r = xk_exclusive_scan_i32(flag, flag, p->n, tot, st);
+  int64_t h = 0;
+  if (r == XK_OK) {
+    cudaError_t e = cudaMemcpyAsync(&h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) r = xk_set_cuda_error(e, __FILE__, __LINE__);
+  }
+  if (r == XK_OK) {
+    *n_rows = h;
+    if (h > cap) {
+      r = xk_set_error(XK_ERR_CAPACITY, "xk_constraint_jacobian: capacity below the number of active pairs");
+    } else if (h > 0) {
+      k_jacobian<<<xk_blocks(p->n, 256), 256, 0, st>>>(*m, *p, flag, rows, cols, vals, pair_index);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) r = xk_set_cuda_error(e, __FILE__, __LINE__);
+    }
+  }
+  cudaFreeAsync(flag, st);
+  cudaFreeAsync(tot, st);
+  return r;
+}

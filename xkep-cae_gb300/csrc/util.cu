@@ -1,0 +1,287 @@
+// Error state, device-wide scans, radix sort and FP64 reductions.
+#include <cstdio>
+#include <cstring>
+
+#include "xk_common.cuh"
+
+static thread_local char g_err[512] = "";
+
+extern "C" const char* xk_version(void) { return "xkgpu 0.1 (sm_103a)"; }
+extern "C" const char* xk_last_error(void) { return g_err; }
+
+xk_status xk_set_cuda_error(cudaError_t e, const char* file, int line) {
+  snprintf(g_err, sizeof(g_err), "CUDA error %d (%s) at %s:%d", (int)e, cudaGetErrorString(e), file, line);
+  return XK_ERR_CUDA;
+}
+xk_status xk_set_error(xk_status code, const char* msg) {
+  snprintf(g_err, sizeof(g_err), "%s", msg);
+  return code;
+}
+
+// --------------------------------------------------------------------------- scan
+
+namespace {
+constexpr int SCAN_T = 256;
+constexpr int SCAN_I = 8;
+constexpr int SCAN_TILE = SCAN_T * SCAN_I;
+
+template <typename T>
+__device__ T block_exclusive_scan(T v, T* warp_tot, T* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T w = (lane < (SCAN_T / 32)) ? warp_tot[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < (SCAN_T / 32)) warp_tot[lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  T before = (warp > 0) ? warp_tot[warp - 1] : T(0);
+  if (total) *total = warp_tot[SCAN_T / 32 - 1];
+  return before + x - v;
+}
+
+template <typename TI>
+__global__ void k_tile_sums(const TI* __restrict__ in, long long n, int64_t* __restrict__ bsum) {
+  __shared__ int64_t wt[SCAN_T / 32];
+  long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_I;
+  int64_t s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_I; ++i)
+    if (base + i < n) s += (int64_t)in[base + i];
+  int64_t tot;
+  block_exclusive_scan<int64_t>(s, wt, &tot);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_bsums(int64_t* bsum, long long nb, int64_t* total) {
+  __shared__ int64_t wt[SCAN_T / 32];
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (long long b0 = 0; b0 < nb; b0 += SCAN_T) {
+    long long i = b0 + threadIdx.x;
+    int64_t v = (i < nb) ? bsum[i] : 0;
+    int64_t tot;
+    int64_t ex = block_exclusive_scan<int64_t>(v, wt, &tot);
+    int64_t c = carry;
+    if (i < nb) bsum[i] = c + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c + tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && total) *total = carry;
+}
+
+template <typename TI, typename TO>
+__global__ void k_tile_scan(const TI* __restrict__ in, TO* __restrict__ out, long long n,
+                            const int64_t* __restrict__ bsum) {
+  __shared__ int64_t wt[SCAN_T / 32];
+  long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_I;
+  int64_t loc[SCAN_I];
+  int64_t s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_I; ++i) {
+    loc[i] = (base + i < n) ? (int64_t)in[base + i] : 0;
+    s += loc[i];
+  }
+  int64_t ex = block_exclusive_scan<int64_t>(s, wt, nullptr) + bsum[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < SCAN_I; ++i) {
+    if (base + i < n) out[base + i] = (TO)ex;
+    ex += loc[i];
+  }
+}
+
+template <typename TI, typename TO>
+xk_status scan_impl(const TI* in, TO* out, long long n, int64_t* total_dev, cudaStream_t s) {
+  if (n <= 0) {
+    if (total_dev) XK_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int64_t), s));
+    return XK_OK;
+  }
+  long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  int64_t* bsum = nullptr;
+  XK_CUDA(cudaMallocAsync((void**)&bsum, sizeof(int64_t) * nb, s));
+  k_tile_sums<TI><<<(unsigned)nb, SCAN_T, 0, s>>>(in, n, bsum);
+  k_scan_bsums<<<1, SCAN_T, 0, s>>>(bsum, nb, total_dev);
+  k_tile_scan<TI, TO><<<(unsigned)nb, SCAN_T, 0, s>>>(in, out, n, bsum);
+  cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(bsum, s);
+  if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);
+  return XK_OK;
+}
+}  // namespace
+
+xk_status xk_exclusive_scan_i32(const int32_t* in, int32_t* out, long long n, int64_t* total_dev,
+                                cudaStream_t s) {
+  return scan_impl<int32_t, int32_t>(in, out, n, total_dev, s);
+}
+xk_status xk_exclusive_scan_i64(const int64_t* in, int64_t* out, long long n, int64_t* total_dev,
+                                cudaStream_t s) {
+  return scan_impl<int64_t, int64_t>(in, out, n, total_dev, s);
+}
+
+// --------------------------------------------------------------------------- radix sort
+
+namespace {
+constexpr int RS_T = 256;
+constexpr int RS_I = 8;
+constexpr int RS_TILE = RS_T * RS_I;
+
+__global__ void k_rs_hist(const uint64_t* __restrict__ keys, long long n, int shift,
+                          int32_t* __restrict__ hist, int nblocks) {
+  __shared__ int cnt[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  long long t0 = (long long)blockIdx.x * RS_TILE;
+  for (int i = 0; i < RS_I; ++i) {
+    long long idx = t0 + (long long)i * RS_T + threadIdx.x;
+    if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & 255u], 1);
+  }
+  __syncthreads();
+  hist[(long long)threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void k_rs_scatter(const uint64_t* __restrict__ kin, const int32_t* __restrict__ vin,
+                             uint64_t* __restrict__ kout, int32_t* __restrict__ vout, long long n,
+                             int shift, const int32_t* __restrict__ off, int nblocks) {
+  __shared__ int run[256];
+  run[threadIdx.x] = off[(long long)threadIdx.x * nblocks + blockIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  long long t0 = (long long)blockIdx.x * RS_TILE;
+  for (int i = 0; i < RS_I; ++i) {
+    long long idx = t0 + (long long)i * RS_T + threadIdx.x;
+    bool valid = idx < n;
+    uint64_t k = valid ? kin[idx] : 0ull;
+    int32_t v = valid ? vin[idx] : 0;
+    int d = valid ? (int)((k >> shift) & 255u) : 256;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    int rank = __popc(peers & lt);
+    int cntw = __popc(peers);
+    int leader = __ffs(peers) - 1;
+    for (int w = 0; w < RS_T / 32; ++w) {
+      __syncthreads();
+      if (warp == w) {
+        int base = (lane == leader && valid) ? run[d] : 0;
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (valid) {
+          long long dst = (long long)base + rank;
+          kout[dst] = k;
+          vout[dst] = v;
+        }
+        if (lane == leader && valid) run[d] = base + cntw;
+      }
+    }
+    __syncthreads();
+  }
+}
+}  // namespace
+
+xk_status xk_radix_sort_u64(uint64_t* keys, int32_t* vals, long long n, int bits, cudaStream_t s) {
+  if (n <= 1) return XK_OK;
+  int passes = (bits + 7) / 8;
+  if (passes <= 0) return XK_OK;
+  int nb = (int)((n + RS_TILE - 1) / RS_TILE);
+  uint64_t* k2 = nullptr;
+  int32_t *v2 = nullptr, *hist = nullptr;
+  XK_CUDA(cudaMallocAsync((void**)&k2, sizeof(uint64_t) * n, s));
+  XK_CUDA(cudaMallocAsync((void**)&v2, sizeof(int32_t) * n, s));
+  XK_CUDA(cudaMallocAsync((void**)&hist, sizeof(int32_t) * 256 * (long long)nb, s));
+  uint64_t *ka = keys, *kb = k2;
+  int32_t *va = vals, *vb = v2;
+  xk_status st = XK_OK;
+  for (int p = 0; p < passes && st == XK_OK; ++p) {
+    int shift = 8 * p;
+    k_rs_hist<<<nb, RS_T, 0, s>>>(ka, n, shift, hist, nb);
+    st = xk_exclusive_scan_i32(hist, hist, 256LL * nb, nullptr, s);
+    if (st != XK_OK) break;
+    k_rs_scatter<<<nb, RS_T, 0, s>>>(ka, va, kb, vb, n, shift, hist, nb);
+    uint64_t* tk = ka; ka = kb; kb = tk;
+    int32_t* tv = va; va = vb; vb = tv;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (st == XK_OK && e == cudaSuccess && ka != keys) {
+    e = cudaMemcpyAsync(keys, ka, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(vals, va, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s);
+  }
+  cudaFreeAsync(k2, s);
+  cudaFreeAsync(v2, s);
+  cudaFreeAsync(hist, s);
+  if (st != XK_OK) return st;
+  if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);
+  return XK_OK;
+}
+
+// --------------------------------------------------------------------------- FP64 sum of squares
+
+namespace {
+constexpr int N2_BLOCKS = 304;  // 2 x 152 SMs; fixed so that the summation order is fixed
+constexpr int N2_T = 256;
+
+__global__ void k_sumsq_partial(const double* __restrict__ x, long long n, double* __restrict__ part) {
+  __shared__ double sm[N2_T];
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * N2_T + threadIdx.x; i < n; i += (long long)N2_BLOCKS * N2_T)
+    acc = fma(x[i], x[i], acc);
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = N2_T / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+__global__ void k_sum_final(const double* __restrict__ part, int np, double* __restrict__ out) {
+  __shared__ double sm[512];
+  double a = 0.0;
+  for (int i = threadIdx.x; i < np; i += 512) a += part[i];
+  sm[threadIdx.x] = a;
+  __syncthreads();
+  for (int w = 256; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sm[0];
+}
+}  // namespace
+
+// Partials buffer for the fixed-order reductions; one per device, set up on the
+// first call (cudaMalloc outside any capture).
+static double* g_part[64] = {nullptr};
+
+xk_status xk_partials_buffer(double** out) {
+  int dev = 0;
+  XK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return xk_set_error(XK_ERR_ARG, "device ordinal out of range");
+  if (!g_part[dev]) XK_CUDA(cudaMalloc((void**)&g_part[dev], sizeof(double) * N2_BLOCKS));
+  *out = g_part[dev];
+  return XK_OK;
+}
+
+xk_status xk_sumsq_into(const double* x, long long n, double* out, cudaStream_t s) {
+  double* part = nullptr;
+  xk_status st = xk_partials_buffer(&part);
+  if (st != XK_OK) return st;
+  k_sumsq_partial<<<N2_BLOCKS, N2_T, 0, s>>>(x, n, part);
+  k_sum_final<<<1, 512, 0, s>>>(part, N2_BLOCKS, out);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
+extern "C" xk_status xk_norm2(const double* x, int64_t n, double* out, xk_stream s) {
+  if (!x || !out || n < 0) return xk_set_error(XK_ERR_ARG, "xk_norm2: bad arguments");
+  return xk_sumsq_into(x, n, out, (cudaStream_t)s);
+}

@@ -1,0 +1,108 @@
+// Shared device/host helpers for the xkgpu kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/xkgpu.h"
+
+#define XK_HD __host__ __device__ __forceinline__
+#define XK_D __device__ __forceinline__
+
+// ---------------------------------------------------------------------------
+// Exactly rounded double operations.  The parts of the path whose results are
+// compared bit for bit with the reference (AABBs, closest point, gap, active
+// set, midpoint prescreen) use these so that nvcc cannot contract a*b+c into
+// an FMA; the reference's NumPy arithmetic rounds every product and sum.
+// ---------------------------------------------------------------------------
+#ifdef __CUDA_ARCH__
+XK_D double xadd(double a, double b) { return __dadd_rn(a, b); }
+XK_D double xsub(double a, double b) { return __dsub_rn(a, b); }
+XK_D double xmul(double a, double b) { return __dmul_rn(a, b); }
+XK_D double xdiv(double a, double b) { return __ddiv_rn(a, b); }
+XK_D double xsqrt(double a) { return __dsqrt_rn(a); }
+#else
+inline double xadd(double a, double b) { return a + b; }
+inline double xsub(double a, double b) { return a - b; }
+inline double xmul(double a, double b) { return a * b; }
+inline double xdiv(double a, double b) { return a / b; }
+inline double xsqrt(double a) { return sqrt(a); }
+#endif
+
+// einsum('ij,ij->i') order measured for the reference's NumPy: (p0 + p2) + p1
+XK_HD double xdot_es(const double* a, const double* b) {
+  return xadd(xadd(xmul(a[0], b[0]), xmul(a[2], b[2])), xmul(a[1], b[1]));
+}
+// np.sum(axis=1) / np.linalg.norm order: (p0 + p1) + p2
+XK_HD double xdot_seq(const double* a, const double* b) {
+  return xadd(xadd(xmul(a[0], b[0]), xmul(a[1], b[1])), xmul(a[2], b[2]));
+}
+XK_HD void xcross(const double* a, const double* b, double* c) {
+  c[0] = xsub(xmul(a[1], b[2]), xmul(a[2], b[1]));
+  c[1] = xsub(xmul(a[2], b[0]), xmul(a[0], b[2]));
+  c[2] = xsub(xmul(a[0], b[1]), xmul(a[1], b[0]));
+}
+// np.clip(x, 0, 1): NaN propagates
+XK_HD double xclip01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
+
+// ---------------------------------------------------------------------------
+// Generic small-vector helpers for the non-exact (FP64 plain or FP32 mixed) math.
+// ---------------------------------------------------------------------------
+template <typename T>
+XK_HD T dot3(const T* a, const T* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+template <typename T>
+XK_HD void cross3(const T* a, const T* b, T* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+template <typename T>
+XK_HD T my_sqrt(T x);
+template <>
+XK_HD double my_sqrt<double>(double x) { return sqrt(x); }
+template <>
+XK_HD float my_sqrt<float>(float x) { return sqrtf(x); }
+
+// Precision policy: P == XK_FP64 computes everything in double; P == XK_MIXED
+// computes the bulk in float and keeps the rotation frames, the axial strain,
+// the contact gap and all reductions in double.
+template <int P>
+struct Prec;
+template <>
+struct Prec<XK_FP64> { typedef double T; };
+template <>
+struct Prec<XK_MIXED> { typedef float T; };
+
+// ---------------------------------------------------------------------------
+// Launch helpers
+// ---------------------------------------------------------------------------
+static inline int xk_blocks(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > 0x7fffffffLL) b = 0x7fffffffLL;
+  return (int)b;
+}
+
+#define XK_CHECK_LAUNCH()                                      \
+  do {                                                         \
+    cudaError_t e__ = cudaGetLastError();                      \
+    if (e__ != cudaSuccess) return xk_set_cuda_error(e__, __FILE__, __LINE__); \
+  } while (0)
+
+#define XK_CUDA(call)                                          \
+  do {                                                         \
+    cudaError_t e__ = (call);                                  \
+    if (e__ != cudaSuccess) return xk_set_cuda_error(e__, __FILE__, __LINE__); \
+  } while (0)
+
+xk_status xk_set_cuda_error(cudaError_t e, const char* file, int line);
+xk_status xk_set_error(xk_status code, const char* msg);
+
+// Device-wide exclusive scans (scan.cu).  Scratch is allocated stream-ordered.
+xk_status xk_exclusive_scan_i32(const int32_t* in, int32_t* out, long long n, int64_t* total_dev,
+                                cudaStream_t s);
+xk_status xk_exclusive_scan_i64(const int64_t* in, int64_t* out, long long n, int64_t* total_dev,
+                                cudaStream_t s);
+// Stable LSD radix sort of 64-bit keys with 32-bit values; `bits` low key bits are sorted.
+xk_status xk_radix_sort_u64(uint64_t* keys, int32_t* vals, long long n, int bits, cudaStream_t s);

@@ -1,0 +1,119 @@
+"""ctypes binding of the xkgpu C ABI (``include/xkgpu.h``).
+
+The library is the in-tree ``libxkgpu.so`` built by ``xkgpu.build``.  Loading
+fails loudly when it is missing: there is no CPU path behind this module.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libxkgpu.so"
+
+XK_OK, XK_ERR_ARG, XK_ERR_CUDA, XK_ERR_CAPACITY, XK_ERR_OVERFLOW = 0, 1, 2, 3, 4
+XK_FP64, XK_MIXED = 0, 1
+XK_STAGE_NARROW, XK_STAGE_NORMAL, XK_STAGE_FRICTION, XK_STAGE_TANGENT = 1, 2, 4, 8
+XK_STAGE_ALL = 15
+XK_OUT_COMBINED, XK_OUT_SPLIT = 0, 1
+XK_WHICH_COMBINED, XK_WHICH_NORMAL, XK_WHICH_FRICTION = 0, 1, 2
+
+vp = C.c_void_p
+
+
+class Section(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("E", "G", "A", "Iy", "Iz", "J", "kappa_y", "kappa_z", "scf")]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("n_nodes", C.c_int32), ("n_elems", C.c_int32), ("X", vp), ("conn", vp), ("radii", vp),
+                ("layer", vp)]
+
+
+class Pairs(C.Structure):
+    _fields_ = [("n", C.c_int32), ("cap", C.c_int32)] + [
+        (n, vp) for n in ("ea", "eb", "s", "t", "gap", "normal", "t1", "t2", "lambda_n", "k_pen", "k_t", "p_n",
+                          "z_t", "q_trial_norm", "dissipation", "status", "stick")]
+
+
+class BeamPlan(C.Structure):
+    _fields_ = [("n_colors", C.c_int32), ("color_ptr_host", vp), ("elem_order", vp), ("blk", vp), ("first", vp),
+                ("nnzb", C.c_int64)]
+
+
+class ContactParams(C.Structure):
+    _fields_ = [("k_pen", C.c_double), ("k_t_ratio", C.c_double), ("mu_eff", C.c_double),
+                ("smoothing_delta", C.c_double), ("g_on", C.c_double), ("g_off", C.c_double),
+                ("allow_deactivation", C.c_int32)]
+
+
+class BPParams(C.Structure):
+    _fields_ = [("margin", C.c_double), ("exclude_shared", C.c_int32), ("exclude_same_layer", C.c_int32),
+                ("midpoint_prescreening", C.c_int32), ("prescreening_margin", C.c_double)]
+
+
+class ContactPattern(C.Structure):
+    _fields_ = [("n_nodes", C.c_int32), ("n_members", C.c_int32), ("nnzb", C.c_int64), ("cap_members", C.c_int64),
+                ("cap_blocks", C.c_int64), ("inc_ptr", vp), ("inc", vp), ("row_ptr", vp), ("col", vp),
+                ("blk_row", vp)]
+
+
+P = C.POINTER
+i64p = P(C.c_int64)
+
+# name -> (argtypes); every function returns xk_status (int)
+SIGNATURES = {
+    "xk_beam_reference": [P(Mesh), P(C.c_double), vp, vp],
+    "xk_beam_assemble": [P(Mesh), P(Section), vp, P(BeamPlan), vp, C.c_int, vp, vp, vp],
+    "xk_beam_lumped_mass": [P(Mesh), P(Section), P(BeamPlan), C.c_double, vp, vp],
+    "xk_broadphase": [P(Mesh), vp, P(BPParams), vp, C.c_int64, i64p, i64p, i64p, vp],
+    "xk_pairs_merge": [P(Mesh), P(Pairs), vp, C.c_int64, P(Pairs), vp],
+    "xk_narrowphase": [P(Mesh), P(Pairs), vp, P(ContactParams), C.c_int, vp],
+    "xk_pair_eval": [P(Mesh), P(Pairs), vp, vp, P(ContactParams), C.c_int, C.c_int, C.c_int, vp, vp, C.c_int64, vp],
+    "xk_contact_pattern_build": [P(Mesh), P(Pairs), P(ContactPattern), vp],
+    "xk_contact_gather_force": [P(Mesh), P(Pairs), P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, C.c_int64, vp,
+                                C.c_double, vp, vp, vp, vp, vp],
+    "xk_contact_gather_tangent": [P(Mesh), P(Pairs), P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, C.c_int64, vp,
+                                  vp],
+    "xk_constraint_jacobian": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
+    "xk_norm2": [vp, C.c_int64, vp, vp],
+}
+
+
+class XkError(RuntimeError):
+    def __init__(self, code: int, where: str, message: str):
+        super().__init__(f"{where}: status {code}: {message}")
+        self.code = code
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load ``libxkgpu.so``; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA library first (xkgpu.build.build())")
+    lib = C.CDLL(str(LIB_PATH))
+    lib.xk_version.restype = C.c_char_p
+    lib.xk_last_error.restype = C.c_char_p
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return ["xk_version", "xk_last_error", *SIGNATURES.keys()]
+
+
+def call(name: str, *args, allow=()) -> int:
+    lib = load()
+    code = getattr(lib, name)(*args)
+    if code != XK_OK and code not in allow:
+        raise XkError(code, name, lib.xk_last_error().decode(errors="replace"))
+    return code

@@ -1,0 +1,337 @@
+"""Device-resident data of the assembly path: mesh, beam plan, pair table, contact pattern.
+
+PyTorch supplies device memory and the CUDA stream; all arithmetic runs in the
+xkgpu kernels behind the C ABI.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+INACTIVE, ACTIVE, SLIDING = 0, 1, 2
+
+
+def require_cuda(device=None) -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("xkgpu needs a CUDA device: no GPU is visible to this process")
+    L.load()
+    return torch.device(device if device is not None else "cuda")
+
+
+def stream_handle(stream=None) -> C.c_void_p:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def ptr(t: torch.Tensor | None) -> C.c_void_p:
+    return C.c_void_p(0 if t is None else t.data_ptr())
+
+
+def as_dev(x, dtype, device) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype, device=device)
+
+
+# ----------------------------------------------------------------------------- mesh
+
+
+class DeviceMesh:
+    """Reference coordinates, connectivity, radii and layer ids on the device."""
+
+    def __init__(self, coords, conn, radii, layer=None, device=None):
+        self.device = require_cuda(device)
+        coords = np.asarray(coords, dtype=np.float64).reshape(-1, 3)
+        conn = np.asarray(conn, dtype=np.int64).reshape(-1, 2)
+        self.n_nodes = int(coords.shape[0])
+        self.n_elems = int(conn.shape[0])
+        radii = np.broadcast_to(np.asarray(radii, dtype=np.float64), (self.n_elems,))
+        if self.n_elems and (conn.min() < 0 or conn.max() >= self.n_nodes):
+            raise ValueError("connectivity refers to nodes outside [0, n_nodes)")
+        if layer is not None and np.asarray(layer).shape[0] != self.n_elems:
+            raise ValueError("layer must hold one entry per element")
+        self.X = as_dev(coords.ravel(), torch.float64, self.device)
+        self.conn = as_dev(conn.ravel().astype(np.int32), torch.int32, self.device)
+        self.radii = as_dev(radii, torch.float64, self.device)
+        self.layer = None if layer is None else as_dev(np.asarray(layer).astype(np.int32), torch.int32, self.device)
+        self.conn_host = conn
+        self.refresh()
+
+    def refresh(self):
+        self.c = L.Mesh(self.n_nodes, self.n_elems, ptr(self.X), ptr(self.conn), ptr(self.radii), ptr(self.layer))
+
+    def set_coords(self, coords):
+        self.X.copy_(as_dev(np.asarray(coords, dtype=np.float64).ravel(), torch.float64, self.device))
+
+    @property
+    def ndof(self) -> int:
+        return 6 * self.n_nodes
+
+
+# ----------------------------------------------------------------------------- beam plan
+
+
+def beam_block_pattern(conn: np.ndarray, n_nodes: int):
+    """6x6 block-CSR pattern of the beam tangent and each element's 4 block ids.
+
+    Blocks (a,a), (a,b), (b,a), (b,b) of every element a-b, rows sorted by
+    column: the structural pattern of ``assemble_cr_beam3d``'s CSR
+    (``_beam_assembly.py:146-150``) in 6x6 blocks.
+    """
+    conn = np.asarray(conn, dtype=np.int64)
+    a, b = conn[:, 0], conn[:, 1]
+    rows = np.stack([a, a, b, b], axis=1)
+    cols = np.stack([a, b, a, b], axis=1)
+    keys = rows * n_nodes + cols
+    uk = np.unique(keys.ravel())
+    brow = uk // n_nodes
+    bcol = (uk % n_nodes).astype(np.int32)
+    row_ptr = np.zeros(n_nodes + 1, dtype=np.int64)
+    np.add.at(row_ptr, brow + 1, 1)
+    row_ptr = np.cumsum(row_ptr)
+    blk = np.searchsorted(uk, keys).astype(np.int32)
+    return row_ptr.astype(np.int32), bcol, blk
+
+
+def greedy_coloring(conn: np.ndarray, n_nodes: int) -> np.ndarray:
+    """Colour elements so that no two elements of one colour share a node."""
+    conn = np.asarray(conn, dtype=np.int64)
+    ne = conn.shape[0]
+    colors = np.empty(ne, dtype=np.int32)
+    used: list[set] = [set() for _ in range(n_nodes)]
+    for e in range(ne):
+        a, b = int(conn[e, 0]), int(conn[e, 1])
+        forbid = used[a] | used[b]
+        c = 0
+        while c in forbid:
+            c += 1
+        colors[e] = c
+        used[a].add(c)
+        used[b].add(c)
+    return colors
+
+
+@dataclass
+class BeamPlanHost:
+    row_ptr: np.ndarray
+    col: np.ndarray
+    blk: np.ndarray  # (n_elems, 4)
+    colors: np.ndarray
+    order: np.ndarray
+    color_ptr: np.ndarray
+    first: np.ndarray  # (n_elems,) uint8 bits
+
+    @property
+    def nnzb(self) -> int:
+        return int(self.col.shape[0])
+
+
+def make_beam_plan(conn: np.ndarray, n_nodes: int) -> BeamPlanHost:
+    row_ptr, col, blk = beam_block_pattern(conn, n_nodes)
+    colors = greedy_coloring(conn, n_nodes)
+    order = np.argsort(colors, kind="stable").astype(np.int32)
+    ncol = int(colors.max()) + 1 if colors.size else 0
+    color_ptr = np.zeros(ncol + 1, dtype=np.int32)
+    np.add.at(color_ptr, colors + 1, 1)
+    color_ptr = np.cumsum(color_ptr).astype(np.int32)
+    # first writer of each block: the element of the lowest colour touching it
+    nblk = col.shape[0]
+    best = np.full(nblk, np.iinfo(np.int32).max, dtype=np.int64)
+    ecol = np.repeat(colors[:, None], 4, axis=1)
+    np.minimum.at(best, blk.ravel(), ecol.ravel())
+    isfirst = ecol == best[blk]
+    first = (isfirst * (1 << np.arange(4))[None, :]).sum(axis=1).astype(np.uint8)
+    return BeamPlanHost(row_ptr, col, blk, colors, order, color_ptr, first)
+
+
+class DeviceBeam:
+    """CR beam data: section, per-element reference frames and the K_T plan."""
+
+    def __init__(self, mesh: DeviceMesh, section: dict, *, v_ref=None):
+        self.mesh = mesh
+        dev = mesh.device
+        scf = section.get("scf")
+        self.section = L.Section(section["E"], section["G"], section["A"], section["Iy"], section["Iz"],
+                                 section["J"], section["kappa_y"], section["kappa_z"],
+                                 float(scf) if scf is not None and scf > 0 else 0.0)
+        self.v_ref = None if v_ref is None else np.asarray(v_ref, dtype=np.float64)
+        self.plan_host = make_beam_plan(mesh.conn_host, mesh.n_nodes)
+        ph = self.plan_host
+        self.order = torch.as_tensor(ph.order, device=dev)
+        self.blk = torch.as_tensor(ph.blk.ravel(), device=dev)
+        self.first = torch.as_tensor(ph.first, device=dev)
+        self.row_ptr = torch.as_tensor(ph.row_ptr, device=dev)
+        self.col = torch.as_tensor(ph.col, device=dev)
+        self._color_ptr = (C.c_int32 * len(ph.color_ptr))(*ph.color_ptr.tolist())
+        self.plan = L.BeamPlan(len(ph.color_ptr) - 1, C.cast(self._color_ptr, C.c_void_p), ptr(self.order),
+                               ptr(self.blk), ptr(self.first), ph.nnzb)
+        self.elem_ref = torch.empty(10 * max(mesh.n_elems, 1), dtype=torch.float64, device=dev)
+        self.update_reference_frames()
+
+    def update_reference_frames(self, stream=None):
+        vr = None if self.v_ref is None else (C.c_double * 3)(*self.v_ref.tolist())
+        L.call("xk_beam_reference", C.byref(self.mesh.c), vr, ptr(self.elem_ref), stream_handle(stream))
+
+    def assemble(self, u: torch.Tensor, precision: int, f_int: torch.Tensor | None, K_vals: torch.Tensor | None,
+                 stream=None):
+        L.call("xk_beam_assemble", C.byref(self.mesh.c), C.byref(self.section), ptr(self.elem_ref),
+               C.byref(self.plan), ptr(u), precision, ptr(f_int), ptr(K_vals), stream_handle(stream))
+
+    def lumped_mass(self, rho: float, out: torch.Tensor, stream=None):
+        L.call("xk_beam_lumped_mass", C.byref(self.mesh.c), C.byref(self.section), C.byref(self.plan),
+               float(rho), ptr(out), stream_handle(stream))
+
+    @property
+    def nnzb(self) -> int:
+        return self.plan_host.nnzb
+
+    def k_dtype(self, precision: int):
+        return torch.float64 if precision == L.XK_FP64 else torch.float32
+
+
+# ----------------------------------------------------------------------------- pair table
+
+F64_FIELDS = {"s": 1, "t": 1, "gap": 1, "normal": 3, "t1": 3, "t2": 3, "lambda_n": 1, "k_pen": 1, "k_t": 1,
+              "p_n": 1, "z_t": 2, "q_trial_norm": 1, "dissipation": 1}
+U8_FIELDS = ("status", "stick")
+
+
+class DevicePairTable:
+    """Structure-of-arrays pair table (``xk_pairs``), vector fields component-major."""
+
+    def __init__(self, device, cap: int = 1024):
+        self.device = device
+        self.n = 0
+        self.cap = 0
+        self.t: dict[str, torch.Tensor] = {}
+        self.reserve(max(cap, 16))
+
+    def reserve(self, cap: int, keep: bool = True):
+        if cap <= self.cap:
+            return
+        cap = int(cap)
+        new = {"ea": torch.zeros(cap, dtype=torch.int32, device=self.device),
+               "eb": torch.zeros(cap, dtype=torch.int32, device=self.device)}
+        for k, w in F64_FIELDS.items():
+            new[k] = torch.zeros(w * cap, dtype=torch.float64, device=self.device)
+        for k in U8_FIELDS:
+            new[k] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
+        if keep and self.n:
+            n, oc = self.n, self.cap
+            for k in ("ea", "eb", *U8_FIELDS):
+                new[k][:n] = self.t[k][:n]
+            for k, w in F64_FIELDS.items():
+                for c in range(w):
+                    new[k][c * cap : c * cap + n] = self.t[k][c * oc : c * oc + n]
+        self.t = new
+        self.cap = cap
+        self.refresh()
+
+    def refresh(self):
+        t = self.t
+        self.c = L.Pairs(self.n, self.cap, *(ptr(t[k]) for k in (
+            "ea", "eb", "s", "t", "gap", "normal", "t1", "t2", "lambda_n", "k_pen", "k_t", "p_n", "z_t",
+            "q_trial_norm", "dissipation", "status", "stick")))
+
+    def set_n(self, n: int):
+        self.n = int(n)
+        self.c.n = self.n
+
+    def to_host(self) -> dict:
+        """Copy the table to host arrays in the oracle's layout (for checks and strategies)."""
+        n, cap = self.n, self.cap
+        out = {"ea": self.t["ea"][:n].cpu().numpy().astype(np.int64),
+               "eb": self.t["eb"][:n].cpu().numpy().astype(np.int64)}
+        for k, w in F64_FIELDS.items():
+            a = self.t[k].view(w, cap)[:, :n].cpu().numpy() if w > 1 else self.t[k][:n].cpu().numpy()
+            out[k] = a.T.copy() if w > 1 else a.copy()
+        out["status"] = self.t["status"][:n].cpu().numpy().astype(np.int8)
+        out["stick"] = self.t["stick"][:n].cpu().numpy().astype(bool)
+        return out
+
+    def from_host(self, d: dict, n_elems: int | None = None):
+        n = int(np.asarray(d["ea"]).shape[0])
+        if n_elems is not None and n and (min(np.min(d["ea"]), np.min(d["eb"])) < 0
+                                          or max(np.max(d["ea"]), np.max(d["eb"])) >= n_elems):
+            raise ValueError("pair table refers to elements outside [0, n_elems)")
+        self.reserve(n, keep=False)
+        cap = self.cap
+        self.t["ea"][:n] = torch.as_tensor(np.asarray(d["ea"], dtype=np.int32), device=self.device)
+        self.t["eb"][:n] = torch.as_tensor(np.asarray(d["eb"], dtype=np.int32), device=self.device)
+        for k, w in F64_FIELDS.items():
+            a = np.asarray(d[k], dtype=np.float64).reshape(n, w) if w > 1 else np.asarray(d[k], dtype=np.float64)
+            if w > 1:
+                self.t[k].view(w, cap)[:, :n] = torch.as_tensor(a.T.copy(), device=self.device)
+            else:
+                self.t[k][:n] = torch.as_tensor(a, device=self.device)
+        self.t["status"][:n] = torch.as_tensor(np.asarray(d["status"]).astype(np.uint8), device=self.device)
+        self.t["stick"][:n] = torch.as_tensor(np.asarray(d["stick"]).astype(np.uint8), device=self.device)
+        self.set_n(n)
+        self.refresh()
+
+    def copy_from(self, other: "DevicePairTable"):
+        self.reserve(other.n, keep=False)
+        n, cap, oc = other.n, self.cap, other.cap
+        for k in ("ea", "eb", *U8_FIELDS):
+            self.t[k][:n] = other.t[k][:n]
+        for k, w in F64_FIELDS.items():
+            for c in range(w):
+                self.t[k][c * cap : c * cap + n] = other.t[k][c * oc : c * oc + n]
+        self.set_n(n)
+        self.refresh()
+
+
+# ----------------------------------------------------------------------------- contact pattern
+
+
+class DeviceContactPattern:
+    """Incidence of the contributing pairs and the 3x3 block pattern of K_c."""
+
+    def __init__(self, mesh: DeviceMesh):
+        self.mesh = mesh
+        dev = mesh.device
+        self.inc_ptr = torch.zeros(mesh.n_nodes + 1, dtype=torch.int32, device=dev)
+        self.row_ptr = torch.zeros(mesh.n_nodes + 1, dtype=torch.int32, device=dev)
+        self.inc = torch.zeros(4 * 1024, dtype=torch.int32, device=dev)
+        self.col = torch.zeros(1024, dtype=torch.int32, device=dev)
+        self.blk_row = torch.zeros(1024, dtype=torch.int32, device=dev)
+        self.c = L.ContactPattern()
+        self._sync_struct()
+
+    def _sync_struct(self):
+        c = self.c
+        c.n_nodes = self.mesh.n_nodes
+        c.cap_members = self.inc.numel() // 4
+        c.cap_blocks = self.col.numel()
+        c.inc_ptr, c.inc, c.row_ptr = ptr(self.inc_ptr), ptr(self.inc), ptr(self.row_ptr)
+        c.col, c.blk_row = ptr(self.col), ptr(self.blk_row)
+
+    def build(self, pairs: DevicePairTable, stream=None):
+        for _ in range(3):
+            code = L.call("xk_contact_pattern_build", C.byref(self.mesh.c), C.byref(pairs.c), C.byref(self.c),
+                          stream_handle(stream), allow=(L.XK_ERR_CAPACITY,))
+            if code == L.XK_OK:
+                return
+            dev = self.mesh.device
+            if self.c.n_members > self.inc.numel() // 4:
+                self.inc = torch.zeros(4 * int(self.c.n_members * 1.25 + 64), dtype=torch.int32, device=dev)
+            if self.c.nnzb > self.col.numel():
+                m = int(self.c.nnzb * 1.25 + 64)
+                self.col = torch.zeros(m, dtype=torch.int32, device=dev)
+                self.blk_row = torch.zeros(m, dtype=torch.int32, device=dev)
+            self._sync_struct()
+        raise RuntimeError("contact pattern capacity did not converge")
+
+    @property
+    def n_members(self) -> int:
+        return int(self.c.n_members)
+
+    @property
+    def nnzb(self) -> int:
+        return int(self.c.nnzb)

@@ -1,0 +1,174 @@
+"""Device-resident assembly of one Newton iteration of the strand contact solver.
+
+Per increment (``detect``), as at the top of the reference's step loop
+(``xkep_cae/contact/solver/process.py:406-429``):
+
+1. broadphase + shared-node / same-layer / midpoint filters on X + u
+   (``DetectCandidatesProcess``),
+2. merge into the pair table (disappeared pairs turn INACTIVE),
+3. exact narrowphase with the active-set update (``UpdateGeometryProcess``),
+4. node incidence of the pairs that can contribute and the K_c block pattern.
+
+Per Newton iteration (``assemble``), as ``ContactForceAssemblyProcess`` +
+``TangentAssemblyProcess`` (``contact/solver/_newton_steps.py:79-135,289-313``):
+
+1. fused pair kernel: frozen narrowphase, Huber normal force, Coulomb return
+   mapping (state z_t <- q), factorised pair tangent,
+2. beam f_int and K_T (coloured, atomic-free),
+3. residual R = f_int - (f_n + f_f) - f_ext with R[fixed] = 0 and its FP64
+   squared norm,
+4. contact tangent K_c = K_n - K_f in 3x3 blocks.
+
+``K_T = K_beam + K_c`` is kept as two block matrices on the device; scipy
+views are built on request only.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from . import _lib as L
+from .device import (DeviceBeam, DeviceContactPattern, DeviceMesh, DevicePairTable, ptr, require_cuda,
+                     stream_handle)
+
+PRECISIONS = {"fp64": L.XK_FP64, "mixed": L.XK_MIXED}
+
+
+class AssemblyEngine:
+    def __init__(self, coords, conn, radii, section: dict, *, layer=None, precision: str = "fp64",
+                 k_pen: float, k_t_ratio: float = 0.5, mu: float = 0.1, smoothing_delta: float = 0.0,
+                 g_on: float = 0.0, g_off: float = 1e-6, allow_deactivation: bool = True,
+                 exclude_same_layer: bool = True, exclude_shared: bool = True, midpoint_prescreening: bool = True,
+                 prescreening_margin: float = 0.0, margin: float = 0.0, v_ref=None, device=None):
+        self.device = require_cuda(device)
+        self.mesh = DeviceMesh(coords, conn, radii, layer, device=self.device)
+        self.beam = DeviceBeam(self.mesh, section, v_ref=v_ref)
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.cp = L.ContactParams(k_pen, k_t_ratio, mu, smoothing_delta, g_on, g_off, int(allow_deactivation))
+        self.bp = L.BPParams(margin, int(exclude_shared), int(exclude_same_layer and layer is not None),
+                             int(midpoint_prescreening), prescreening_margin)
+        dev = self.device
+        nd = self.mesh.ndof
+        self.pairs = DevicePairTable(dev)
+        self._spare = DevicePairTable(dev)
+        self.pattern = DeviceContactPattern(self.mesh)
+        self.f_int = torch.zeros(nd, dtype=torch.float64, device=dev)
+        self.R = torch.zeros(nd, dtype=torch.float64, device=dev)
+        self.norm2 = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.cands = torch.zeros(2 * 1024, dtype=torch.int32, device=dev)
+        self._alloc_outputs()
+        self.stats: dict = {}
+        self.graph = None
+
+    # ------------------------------------------------------------------ buffers
+    @property
+    def t_dtype(self):
+        return torch.float64 if self.precision == L.XK_FP64 else torch.float32
+
+    def _alloc_outputs(self):
+        dev = self.device
+        self.K_beam = torch.zeros(36 * max(self.beam.nnzb, 1), dtype=self.t_dtype, device=dev)
+        cap = self.pairs.cap
+        self.pv = torch.zeros(3 * cap, dtype=self.t_dtype, device=dev)
+        self.pB = torch.zeros(9 * cap, dtype=self.t_dtype, device=dev)
+        self.K_c = torch.zeros(9 * max(self.pattern.col.numel(), 1), dtype=self.t_dtype, device=dev)
+        self.graph = None
+
+    def set_precision(self, precision):
+        p = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        if p != self.precision:
+            self.precision = p
+            self._alloc_outputs()
+
+    # ------------------------------------------------------------------ per increment
+    def detect(self, u: torch.Tensor, stream=None) -> dict:
+        """Broadphase, pair-table merge, active-set narrowphase and contact pattern at X + u."""
+        s = stream_handle(stream)
+        n_out, n_raw, n_pre = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        for _ in range(3):
+            code = L.call("xk_broadphase", C.byref(self.mesh.c), ptr(u), C.byref(self.bp), ptr(self.cands),
+                          self.cands.numel() // 2, C.byref(n_out), C.byref(n_raw), C.byref(n_pre), s,
+                          allow=(L.XK_ERR_CAPACITY,))
+            if code == L.XK_OK:
+                break
+            self.cands = torch.zeros(2 * int(n_out.value * 1.25 + 1024), dtype=torch.int32, device=self.device)
+        nc = int(n_out.value)
+        need = self.pairs.n + nc
+        if self._spare.cap < need:
+            self._spare.reserve(int(need * 1.25) + 64, keep=False)
+        L.call("xk_pairs_merge", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(self.cands), nc,
+               C.byref(self._spare.c), s)
+        self._spare.set_n(self._spare.c.n)
+        self.pairs, self._spare = self._spare, self.pairs
+        L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), C.byref(self.cp), 1, s)
+        self.pattern.build(self.pairs, stream)
+        if self.pv.numel() < 3 * self.pairs.cap or self.K_c.numel() < 9 * max(self.pattern.col.numel(), 1):
+            self._alloc_outputs()
+        self.graph = None
+        self.stats = {"raw": int(n_raw.value), "prefilter": int(n_pre.value), "candidates": nc,
+                      "pairs": self.pairs.n, "members": self.pattern.n_members, "contact_blocks": self.pattern.nnzb}
+        return self.stats
+
+    # ------------------------------------------------------------------ per iteration
+    def assemble(self, u: torch.Tensor, u_ref: torch.Tensor | None = None, f_ext: torch.Tensor | None = None,
+                 fixed: torch.Tensor | None = None, stream=None, *, tangent: bool = True):
+        s = stream_handle(stream)
+        p = self.precision
+        stride = self.pairs.cap
+        L.call("xk_pair_eval", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), ptr(u_ref), C.byref(self.cp),
+               L.XK_STAGE_ALL, p, L.XK_OUT_COMBINED, ptr(self.pv), ptr(self.pB), stride, s)
+        self.beam.assemble(u, p, self.f_int, self.K_beam if tangent else None, stream)
+        L.call("xk_contact_gather_force", C.byref(self.mesh.c), C.byref(self.pairs.c), C.byref(self.pattern.c),
+               ptr(self.pv), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, stride, ptr(self.f_int), -1.0, ptr(f_ext),
+               ptr(fixed), ptr(self.R), ptr(self.norm2), s)
+        if tangent and self.pattern.nnzb > 0:
+            L.call("xk_contact_gather_tangent", C.byref(self.mesh.c), C.byref(self.pairs.c), C.byref(self.pattern.c),
+                   ptr(self.pB), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, stride, ptr(self.K_c), s)
+        return self.R
+
+    def capture(self, u, u_ref=None, f_ext=None, fixed=None):
+        """Record ``assemble`` on these (static) buffers as a CUDA graph."""
+        st = torch.cuda.Stream(device=self.device)
+        st.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(st):
+            self.assemble(u, u_ref, f_ext, fixed, stream=st)  # warm-up outside capture
+        torch.cuda.current_stream().wait_stream(st)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=st):
+            self.assemble(u, u_ref, f_ext, fixed, stream=st)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    # ------------------------------------------------------------------ host views
+    def residual_norm(self) -> float:
+        return float(np.sqrt(self.norm2.item()))
+
+    def K_beam_csr(self) -> sp.csr_matrix:
+        nb = self.beam.nnzb
+        vals = self.K_beam[: 36 * nb].double().cpu().numpy().reshape(nb, 6, 6)
+        nd = self.mesh.ndof
+        return sp.bsr_matrix((vals, self.beam.col.cpu().numpy(), self.beam.row_ptr.cpu().numpy()),
+                             shape=(nd, nd)).tocsr()
+
+    def K_contact_csr(self, vals: torch.Tensor | None = None) -> sp.csr_matrix:
+        nb = self.pattern.nnzb
+        nd = self.mesh.ndof
+        if nb == 0:
+            return sp.csr_matrix((nd, nd))
+        v = (self.K_c if vals is None else vals)[: 9 * nb].double().cpu().numpy().reshape(nb, 3, 3)
+        r = self.pattern.blk_row[:nb].cpu().numpy().astype(np.int64)
+        c = self.pattern.col[:nb].cpu().numpy().astype(np.int64)
+        rows = (6 * r)[:, None, None] + np.arange(3)[None, :, None]
+        cols = (6 * c)[:, None, None] + np.arange(3)[None, None, :]
+        rows, cols = np.broadcast_to(rows, v.shape), np.broadcast_to(cols, v.shape)
+        return sp.csr_matrix((v.ravel(), (rows.ravel(), cols.ravel())), shape=(nd, nd))
+
+    def K_total_csr(self) -> sp.csr_matrix:
+        return (self.K_beam_csr() + self.K_contact_csr()).tocsr()

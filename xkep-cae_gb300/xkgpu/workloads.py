@@ -1,0 +1,85 @@
+"""Strand workloads with the material, section, penalty and contact settings of the benchmarks.
+
+Steel wires (E = 200 GPa, nu = 0.3) in mm-N-MPa units, circular sections with
+Cowper's shear factor (``xkep_cae/elements/_beam_section.py:59-65,129-136``),
+penalty ``k_pen = 1e3 * E A / L_mean`` (``AutoEALPenalty``,
+``xkep_cae/contact/penalty/strategy.py:111-131``), mu = 0.1, k_t_ratio = 0.5,
+same-layer pairs excluded.  Positions are perturbed by N(0, (1e-3 d)^2) and
+rotations by N(0, (1e-3 rad)^2) from ``numpy.random.default_rng(seed)``.
+"""
+
+from __future__ import annotations
+
+import math
+import warnings
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import strand as S
+
+E_STEEL = 2.0e5
+NU_STEEL = 0.3
+
+
+def circle_section(d: float, E: float = E_STEEL, nu: float = NU_STEEL) -> dict:
+    r = d / 2.0
+    kappa = 6.0 * (1.0 + nu) / (7.0 + 6.0 * nu)
+    return {"E": E, "G": E / (2.0 * (1.0 + nu)), "A": math.pi * r * r, "Iy": math.pi * d**4 / 64.0,
+            "Iz": math.pi * d**4 / 64.0, "J": math.pi * d**4 / 32.0, "kappa_y": kappa, "kappa_z": kappa}
+
+
+def mean_element_length(coords, conn) -> float:
+    conn = np.asarray(conn)
+    return float(np.mean(np.linalg.norm(coords[conn[:, 1]] - coords[conn[:, 0]], axis=1)))
+
+
+@dataclass
+class Workload:
+    name: str
+    strand: S.Strand
+    section: dict
+    u: np.ndarray
+    k_pen: float
+    mu: float = 0.1
+    k_t_ratio: float = 0.5
+    smoothing_delta: float = 0.0
+    meta: dict = field(default_factory=dict)
+
+    def engine_kwargs(self) -> dict:
+        return dict(layer=self.strand.elem_layer, k_pen=self.k_pen, k_t_ratio=self.k_t_ratio, mu=self.mu,
+                    smoothing_delta=self.smoothing_delta)
+
+
+def strand_workload(name: str, n_wires: int, d: float, pitch: float, n_pitches: float, n_el_per_pitch: int, *,
+                    gap_frac: float = -0.005, seed: int = 0, mu: float = 0.1, compress_layer: int | None = None,
+                    compress_frac: float = 0.0) -> Workload:
+    n_el = int(round(n_el_per_pitch * n_pitches))
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        st = S.make_strand(n_wires, d, pitch, n_pitches, n_el, gap=gap_frac * d)
+    u = S.perturbation(st, seed, sigma_pos=1e-3 * d, sigma_rot=1e-3)
+    if compress_layer is not None:
+        u = u + S.radial_compression(st, compress_layer, compress_frac * d)
+    sec = circle_section(d)
+    k_pen = 1e3 * sec["E"] * sec["A"] / mean_element_length(st.coords, st.conn)
+    return Workload(name, st, sec, u, k_pen, mu=mu, meta={"n_wires": n_wires, "d": d, "pitch": pitch,
+                                                          "n_pitches": n_pitches, "n_el_per_pitch": n_el_per_pitch,
+                                                          "gap_frac": gap_frac, "seed": seed})
+
+
+def wires_for_layers(n_layers: int) -> int:
+    return 1 + sum(6 * k for k in range(1, n_layers + 1))
+
+
+# The benchmark strands (wire count, diameter, pitch, pitches, elements per pitch)
+CONFIGS = {
+    "strand7": dict(n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el_per_pitch=16),
+    "strand37": dict(n_wires=37, d=2.0, pitch=40.0, n_pitches=4, n_el_per_pitch=32),
+    "strand91": dict(n_wires=91, d=2.0, pitch=40.0, n_pitches=4, n_el_per_pitch=32),
+    "strand1027": dict(n_wires=wires_for_layers(18), d=0.5, pitch=20.0, n_pitches=4, n_el_per_pitch=24),
+}
+
+
+def config_workload(name: str, seed: int = 0) -> Workload:
+    return strand_workload(name, seed=seed, **CONFIGS[name])
