@@ -1,0 +1,464 @@
+"""Benchmark: assembly + contact evaluations per second of one Newton iteration.
+
+Workload: the 1027-wire hexagonally layered strand (18 layers, wire diameter
+0.5 mm, lay pitch 20 mm, 4 pitches, 24 elements per pitch: 99,619 nodes,
+98,592 CR beam elements), nodes perturbed by seeded Gaussian noise, contact
+forced by a nominal layer gap of -0.005 d; synthetic inputs of the reference's
+shapes.  One step is one Newton-iteration assembly on the device: the fused
+pair kernel over every pair of the table (frozen narrowphase, Huber normal
+force, Coulomb return mapping, pair tangent), the CR beam f_int and K_T, the
+residual with its FP64 norm and the contact tangent K_c.  The per-increment
+detection (broadphase, merge, active set, pattern) runs before the timed
+region and is reported separately.
+
+metric value = (N_e + N_c) / seconds per step, N_c = pairs in the table.
+The headline is the mixed-precision path; the plain FP64 path is timed in the
+same run (``fp64_plain``) together with the error of mixed against FP64.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT), str(ROOT / "xkep-cae_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "assembly+contact evals/s at 1027-wire vs FP64 plain on GB300; err vs FP64"
+UNIT = "evals/s"
+
+
+# --------------------------------------------------------------------------- helpers
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        out_dir = ROOT / "gpurun_out" if (ROOT / "gpurun_out").is_dir() else Path(tempfile.gettempdir())
+        self.path = out_dir / f"clocks_{os.getpid()}.csv"
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def slab_workload(w, frac: float):
+    """The first ``frac`` of every wire: a bounded sample of the same strand for CPU timing."""
+    from xkgpu import strand as S
+
+    st = w.strand
+    nel = st.n_elems_per_wire
+    keep_el = max(2, int(round(nel * frac)))
+    npw = nel + 1
+    nodes, elems = [], []
+    for wi in range(len(st.wires)):
+        nodes.append(np.arange(wi * npw, wi * npw + keep_el + 1))
+        elems.append(np.arange(wi * nel, wi * nel + keep_el))
+    nodes = np.concatenate(nodes)
+    elems = np.concatenate(elems)
+    remap = -np.ones(st.n_nodes, dtype=np.int64)
+    remap[nodes] = np.arange(nodes.size)
+    sub = S.Strand(coords=st.coords[nodes], conn=remap[st.conn[elems]].astype(np.int32),
+                   elem_layer=st.elem_layer[elems], radii=st.radii[elems], wires=st.wires,
+                   wire_diameter=st.wire_diameter, pitch=st.pitch, length=st.length, n_elems_per_wire=keep_el)
+    u = w.u.reshape(-1, 6)[nodes].ravel().copy()
+    return sub, u
+
+
+def oracle_sample_timing(w, frac: float, reps: int = 1, prepared=None):
+    """Time the oracle (NumPy port) on a slab of the strand; returns (units, seconds, prepared)."""
+    from oracle import beam as ob
+    from oracle import contact as oc
+
+    if prepared is None:
+        sub, u = slab_workload(w, frac)
+        cd = oc.deformed_coords(sub.coords, u)
+        table, _, _ = oc.detect(oc.empty_table(), cd, sub.conn, sub.radii, elem_layer=sub.elem_layer,
+                                exclude_same_layer=True)
+        table = oc.update_geometry(table, cd)
+        prepared = (sub, u, table)
+    sub, u, table = prepared
+    sec = ob.Section(**w.section, scf=None)
+    u1 = u * 1.001
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        oc.contact_iteration(table, sub.coords, u1, u, sub.ndof, k_pen=w.k_pen, k_t_ratio=w.k_t_ratio, mu_eff=w.mu)
+        ob.assemble_beam(sub.coords, sub.conn, u1, sec)
+    dt = time.perf_counter() - t0
+    units = reps * (sub.n_elems + table["ea"].shape[0])
+    return units, dt, prepared
+
+
+def pair_kernel_bytes(n_nodes, n_elems, n_others, n_members, tsize):
+    """Algorithmic (compulsory) DRAM bytes of one pair step (both launches).
+
+    Node data X, u, u_ref once per node (72 B); conn and radius once per
+    element (16 B).  A non-contributing pair reads its list entry, keys and
+    previous normal / tangent (60 B) and writes s, t, gap and the frame
+    (96 B).  A contributing pair also reads its node ids and friction state
+    (126 B read in all), writes the updated state (138 B) and its record
+    (s, t, v, B: 14 values in the compute precision).
+    """
+    return 72 * n_nodes + 16 * n_elems + 156 * n_others + n_members * (264 + 14 * tsize)
+
+
+# --------------------------------------------------------------------------- GPU arm
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    from xkgpu import _lib as L
+    from xkgpu import workloads as W
+    from xkgpu.engine import AssemblyEngine
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    w = W.config_workload(args.workload, seed=rank)
+    st = w.strand
+    n_e = st.n_elems
+
+    def make(prec):
+        return AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=prec, device=dev,
+                              **w.engine_kwargs())
+
+    u0 = torch.as_tensor(w.u, device=dev)
+    rng = np.random.default_rng(100 + rank)
+    du = rng.normal(0.0, 2e-4 * w.meta["d"], (st.n_nodes, 6))
+    du[:, 3:] *= 0.0
+    u1 = torch.as_tensor(w.u + du.ravel(), device=dev)
+
+    results = {}
+    engines = {}
+    for prec in ("fp64", "mixed"):
+        eng = make(prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        stats = eng.detect(u0)
+        torch.cuda.synchronize()
+        t_det_first = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        eng.detect(u0)  # steady state: merge into an existing table
+        torch.cuda.synchronize()
+        t_det = time.perf_counter() - t0
+        eng.capture(u1, u0)
+        for _ in range(args.warmup):
+            eng.replay()
+        torch.cuda.synchronize()
+        engines[prec] = eng
+        results[prec] = {"stats": stats, "detect_ms": 1e3 * t_det, "detect_first_ms": 1e3 * t_det_first}
+
+    # error of mixed against FP64 on the same state (fresh engines)
+    e64, emx = make("fp64"), make("mixed")
+    e64.detect(u0)
+    emx.detect(u0)
+    e64.assemble(u1, u0)
+    emx.assemble(u1, u0)
+    torch.cuda.synchronize()
+
+    def relmax(a, b):
+        a, b = a.double(), b.double()
+        return float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+
+    nb = e64.pattern.nnzb
+    err = {"R": relmax(emx.R, e64.R), "K_beam": relmax(emx.K_beam, e64.K_beam),
+           "K_contact": relmax(emx.K_c[: 9 * nb], e64.K_c[: 9 * nb]),
+           "active_set_equal": bool(torch.equal(emx.pairs.t["status"][: emx.pairs.n],
+                                                e64.pairs.t["status"][: e64.pairs.n]))}
+    del e64, emx
+
+    if world > 1:
+        torch.distributed.barrier()
+
+    def timed(eng, k):
+        s = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(s)
+        for _ in range(k):
+            eng.replay()
+        b.record(s)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+    with ClockSampler(dev.index if dev.index is not None else 0) as clk:
+        t_mixed = timed(engines["mixed"], args.steps)
+        t_fp64 = timed(engines["fp64"], args.steps)
+    clocks = clk.summary()
+
+    if world > 1:
+        t = torch.tensor([t_mixed, t_fp64], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_mixed, t_fp64 = float(t[0]), float(t[1])
+
+    n_c = engines["mixed"].pairs.n
+    units = world * (n_e + n_c)
+    ms_mixed = 1e3 * t_mixed / args.steps
+    ms_fp64 = 1e3 * t_fp64 / args.steps
+
+    # dominant kernel alone: the fused pair kernel, CUDA events on its stream
+    import ctypes as C
+
+    from xkgpu.device import ptr, stream_handle
+
+    def pair_kernel_time(eng, k):
+        s = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        args_ = (C.byref(eng.mesh.c), C.byref(eng.pairs.c), C.byref(eng.pattern.c), ptr(u1), ptr(u0),
+                 C.byref(eng.cp), L.XK_STAGE_ALL, eng.precision, L.XK_OUT_COMBINED, ptr(eng.rec), stream_handle(s))
+        for _ in range(3):
+            L.call("xk_pair_step", *args_)
+        torch.cuda.synchronize()
+        a.record(s)
+        for _ in range(k):
+            L.call("xk_pair_step", *args_)
+        b.record(s)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / k
+
+    kreps = max(20, min(args.steps, 200))
+    tk_mixed = pair_kernel_time(engines["mixed"], kreps)
+    tk_fp64 = pair_kernel_time(engines["fp64"], kreps)
+    m = engines["mixed"].pattern.n_members
+    by_mixed = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, 4)
+    by_fp64 = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, 8)
+    peak, peak_kind = _peaks()
+
+    # end to end through the public engine API with host buffers
+    eng = engines["mixed"]
+    uh = torch.empty_like(u1, device="cpu").pin_memory()
+    uh.copy_(u1.cpu())
+    urh = torch.empty_like(u0, device="cpu").pin_memory()
+    urh.copy_(u0.cpu())
+    Rh = torch.empty(eng.R.numel(), dtype=torch.float64).pin_memory()
+    Kbh = torch.empty(eng.K_beam.numel(), dtype=eng.K_beam.dtype).pin_memory()
+    nkc = 9 * eng.pattern.nnzb
+    Kch = torch.empty(nkc, dtype=eng.K_c.dtype).pin_memory()
+    u_in, ur_in = torch.empty_like(u1), torch.empty_like(u0)
+    eng.capture(u_in, ur_in)
+
+    def e2e_step():
+        u_in.copy_(uh, non_blocking=True)
+        ur_in.copy_(urh, non_blocking=True)
+        eng.replay()
+        Rh.copy_(eng.R, non_blocking=True)
+        Kbh.copy_(eng.K_beam, non_blocking=True)
+        Kch.copy_(eng.K_c[:nkc], non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(args.steps):
+        e2e_step()
+    b.record(s)
+    torch.cuda.synchronize()
+    t_e2e = a.elapsed_time(b) / 1e3
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t[0])
+    h2d = 2 * uh.numel() * 8
+    d2h = Rh.numel() * 8 + Kbh.numel() * Kbh.element_size() + Kch.numel() * Kch.element_size()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        frac = 1.0 / 48.0
+        _, dt, prep = oracle_sample_timing(w, frac)  # includes a warm first call
+        units_c, dt, _ = oracle_sample_timing(w, frac, reps=1, prepared=prep)
+        sub = prep[0]
+        cpu = {"value": units_c / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"NumPy oracle, one Newton-iteration assembly (contact + beam) on the first 1/48 of every "
+                         f"wire ({sub.n_elems} elements, {prep[2]['ea'].shape[0]} pairs), host of the GPU box"}
+
+    per_launch = 8  # 2 pair kernels, 2 beam colours, force gather, 2 norm kernels, tangent gather
+    out = {
+        "metric": METRIC, "value": units / t_mixed * args.steps, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed: float arithmetic, double frames/gap/norm)",
+        "data": "synthetic (seeded strand geometry and perturbations of the reference's configuration)",
+        "config": {"workload": "strand1027: 1027 wires (18 layers), d=0.5 mm, pitch 20 mm, 4 pitches, "
+                               "24 el/pitch, gap -0.005 d, seeded noise", "n_nodes": st.n_nodes,
+                   "n_elems": n_e, "n_pairs": n_c, "raw_aabb_pairs": results["mixed"]["stats"]["raw"],
+                   "contributing_pairs": m, "contact_blocks": engines["mixed"].pattern.nnzb,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (pair table alone > 1 GB)", "cuda_graph": True},
+        "fp64_plain": {"value": units / t_fp64 * args.steps, "ms_per_step": ms_fp64,
+                       "speedup_mixed_vs_fp64": t_fp64 / t_mixed},
+        "err_vs_fp64": err,
+        "detect_ms": {"mixed": results["mixed"]["detect_ms"], "fp64": results["fp64"]["detect_ms"],
+                      "first": results["mixed"]["detect_first_ms"]},
+        "roofline": {"bound": "hbm", "kernel": "pair step: k_pair_member + k_pair_other (narrowphase+Huber+Coulomb+tangent)",
+                     "achieved": by_mixed / tk_mixed / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": by_mixed / tk_mixed / 1e9 / peak, "peak_kind": peak_kind,
+                     "bytes_per_launch": by_mixed, "launch_ms": 1e3 * tk_mixed, "traffic": None,
+                     "fp64_kernel": {"achieved": by_fp64 / tk_fp64 / 1e9, "launch_ms": 1e3 * tk_fp64,
+                                     "bytes_per_launch": by_fp64}},
+        "e2e": {"value": units / t_e2e * args.steps, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": per_launch * args.steps,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    tr = ROOT / "profiles" / "pair_kernel_traffic.json"
+    if tr.exists():
+        out["roofline"]["traffic"] = json.loads(tr.read_text()).get("bytes_per_launch_strand1027")
+    return out
+
+
+# --------------------------------------------------------------------------- reference arm
+
+
+def run_reference(args):
+    from xkgpu import workloads as W
+
+    w = W.config_workload(args.workload, seed=0)
+    budget = float(os.environ.get("XK_REF_BUDGET_S", "150"))
+    frac = 1.0 / 96.0
+    _, dt0, prep = oracle_sample_timing(w, frac)
+    per_step = budget / max(1, args.steps + args.warmup)
+    # shrink the slab until one step fits its share of the budget
+    while dt0 > per_step and frac > 1.0 / 768.0:
+        frac /= 2.0
+        _, dt0, prep = oracle_sample_timing(w, frac)
+    for _ in range(args.warmup):
+        oracle_sample_timing(w, frac, prepared=prep)
+    units = 0
+    tt = 0.0
+    for _ in range(args.steps):
+        u, dt, _ = oracle_sample_timing(w, frac, prepared=prep)
+        units += u
+        tt += dt
+    v = units / tt
+    sub, _, table = prep
+    sample = (f"NumPy port of the reference path (oracle), one Newton-iteration assembly per step on the first "
+              f"{frac:.4g} of every wire ({sub.n_elems} elements, {table['ea'].shape[0]} pairs)")
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "strand1027 slab sample", "sample_fraction": frac},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_profile(args):
+    """Small driver for ncu: one engine, one detection, ``--steps`` eager assemblies."""
+    import torch
+
+    from xkgpu import workloads as W
+    from xkgpu.engine import AssemblyEngine
+
+    w = W.config_workload(args.workload, seed=0)
+    st = w.strand
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=args.profile, **w.engine_kwargs())
+    u0 = torch.as_tensor(w.u, device="cuda")
+    u1 = u0 * 1.001
+    stats = eng.detect(u0)
+    for _ in range(args.steps):
+        eng.assemble(u1, u0)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "workload": args.workload, **stats}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="xkgpu", choices=["xkgpu", "reference"])
+    ap.add_argument("--workload", default="strand1027")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+                    help="profiling driver: detect once, then --steps eager assemblies, no timing")
+    args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    out = run_gpu(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

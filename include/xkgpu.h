@@ -158,60 +158,71 @@ xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double* u, const x
 #define XK_STAGE_NORMAL 2   /* HuberContactForceProcess.evaluate (contact_force/strategy.py:126-170) */
 #define XK_STAGE_FRICTION 4 /* CoulombReturnMappingProcess.evaluate (friction/strategy.py:111-148) */
 #define XK_STAGE_TANGENT 8  /* .tangent of both (contact_force/strategy.py:172-254, friction/_assembly.py:108-257) */
-#define XK_OUT_COMBINED 0   /* v = v_n + v_f (3), B = B_n - B_f (9) */
-#define XK_OUT_SPLIT 1      /* v_n (3), v_f (3), B_n (9), B_f (9) */
+#define XK_OUT_COMBINED 0   /* record (s, t, v = v_n + v_f, B = B_n - B_f): 14 columns */
+#define XK_OUT_SPLIT 1      /* record (s, t, v_n, v_f, B_n, B_f): 26 columns */
+#define XK_REC_COLS_COMBINED 14
+#define XK_REC_COLS_SPLIT 26
 
-/* Per-pair contact evaluation, fused over the selected stages.  A pair's
- * translational force on its node k (A0, A1, B0, B1) is c_k * v and its
- * tangent block (k, l) is c_k * c_l * B, with c = [1-s, s, -(1-t), -t].
- * pv / pB are written (double for XK_FP64, float for XK_MIXED, column stride
- * out_stride) for every pair that can contribute in this increment
- * (status != INACTIVE or p_n > 0 on entry); others are left untouched. */
-xk_status xk_pair_eval(const xk_mesh* m, xk_pairs* p, const double* u, const double* u_ref,
-                       const xk_contact_params* cp, int stages, int precision, int out_mode, void* pv,
-                       void* pB, int64_t out_stride, xk_stream s);
-
-/* Node incidence of the contributing pairs and the block pattern of K_c, built
- * once per increment (after detection and the active-set update). */
+/* The pairs that can contribute in an increment ("members": status != INACTIVE
+ * or p_n > 0 after detection and the active-set update), the rest, the node
+ * incidence of the members and the block pattern of K_c with each block's
+ * contributor list.  Built once per increment; every array is caller-owned. */
 typedef struct {
   int32_t n_nodes;
-  int32_t n_members;   /* contributing pairs */
+  int32_t n_members, n_others;
   int64_t nnzb;        /* contact blocks */
-  int64_t cap_members; /* capacity of inc (4 entries per member) */
-  int64_t cap_blocks;  /* capacity of col / blk_row */
-  int32_t* inc_ptr;    /* [n_nodes+1] */
-  int32_t* inc;        /* [4*cap_members] (pair << 2) | local node */
-  int32_t* row_ptr;    /* [n_nodes+1] */
-  int32_t* col;        /* [cap_blocks] */
-  int32_t* blk_row;    /* [cap_blocks] */
+  int64_t n_contrib;   /* 16 per member */
+  int64_t cap_members, cap_others, cap_blocks;
+  int32_t* members;      /* [cap_members] pair index of each member, ascending */
+  int32_t* member_nodes; /* [4*cap_members] nodes A0 A1 B0 B1 of each member */
+  int32_t* others;       /* [cap_others] the remaining pairs, ascending */
+  int32_t* inc_ptr;      /* [n_nodes+1] */
+  int32_t* inc;          /* [4*cap_members] (member << 2) | local node k */
+  int32_t* row_ptr;      /* [n_nodes+1] block rows of K_c */
+  int32_t* col;          /* [cap_blocks] */
+  int32_t* blk_row;      /* [cap_blocks] */
+  int32_t* blk_ptr;      /* [cap_blocks+1] */
+  int32_t* contrib;      /* [16*cap_members] (member << 4) | (k << 2) | l */
 } xk_contact_pattern;
 
-/* Returns XK_ERR_CAPACITY (with n_members / nnzb set) when a capacity is too
- * small.  Synchronises the stream. */
+/* Returns XK_ERR_CAPACITY (with n_members, n_others, nnzb set) when a capacity
+ * is too small.  Synchronises the stream. */
 xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* p, xk_contact_pattern* pat,
                                    xk_stream s);
+
+/* Per-iteration pair evaluation, fused over the selected stages.  A member's
+ * translational force on its local node k (A0, A1, B0, B1) is c_k v and its
+ * tangent block (k, l) is c_k c_l B with c = [1-s, s, -(1-t), -t]; these go
+ * to the member-compact record rec[col*cap_members + member] (double for
+ * XK_FP64, float for XK_MIXED).  With XK_STAGE_NARROW the other pairs get the
+ * narrowphase too, as in the reference.  The four stages together replace the
+ * contact part of ContactForceAssemblyProcess + TangentAssemblyProcess
+ * (_newton_steps.py:79-135,289-313). */
+xk_status xk_pair_step(const xk_mesh* m, xk_pairs* p, const xk_contact_pattern* pat, const double* u,
+                       const double* u_ref, const xk_contact_params* cp, int stages, int precision,
+                       int out_mode, void* rec, xk_stream s);
 
 #define XK_WHICH_COMBINED 0
 #define XK_WHICH_NORMAL 1
 #define XK_WHICH_FRICTION 2
 
-/* out[dof] = base[dof] + scale * sum_{pairs at node} c_k v_k  - f_ext[dof],
- * then out[dof] = 0 where fixed[dof] != 0.  base, f_ext, fixed nullable.
- * With base = f_int, scale = -1 this is the residual of
- * ContactForceAssemblyProcess (_newton_steps.py:123-129).  norm2 (nullable,
- * device double) receives sum(out^2) in a fixed-order FP64 reduction
- * (ConvergenceCheckProcess, _newton_steps.py:194-203). */
-xk_status xk_contact_gather_force(const xk_mesh* m, const xk_pairs* p, const xk_contact_pattern* pat,
-                                  const void* pv, int precision, int out_mode, int which,
-                                  int64_t out_stride, const double* base, double scale,
-                                  const double* f_ext, const uint8_t* fixed, double* out,
-                                  double* norm2, xk_stream s);
+/* out[dof] = base[dof] + scale * sum_{members at the node} c_k v  - f_ext[dof],
+ * then out[dof] = 0 where fixed[dof] != 0; base, f_ext, fixed nullable.  With
+ * base = f_int and scale = -1 this is the residual R = f_int + f_c - f_ext of
+ * ContactForceAssemblyProcess (_newton_steps.py:123-129); with base = NULL,
+ * scale = 1 and which = normal / friction it is the force returned by
+ * HuberContactForceProcess / CoulombReturnMappingProcess.evaluate.  norm2
+ * (nullable, device double) receives sum(out^2) in a fixed-order FP64
+ * reduction (ConvergenceCheckProcess, _newton_steps.py:194-203). */
+xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec, int precision, int out_mode,
+                                  int which, const double* base, double scale, const double* f_ext,
+                                  const uint8_t* fixed, double* out, double* norm2, xk_stream s);
 
-/* K_c block values (9 per block, double|float): sum of c_k c_l B over the
- * pairs at each block; which selects B_n - B_f, B_n or B_f. */
-xk_status xk_contact_gather_tangent(const xk_mesh* m, const xk_pairs* p, const xk_contact_pattern* pat,
-                                    const void* pB, int precision, int out_mode, int which,
-                                    int64_t out_stride, void* Kc_vals, xk_stream s);
+/* K_c block values (9 per block, double|float, nnzb blocks): sum over each
+ * block's contributors of c_k c_l B; which selects B_n - B_f (combined
+ * records), B_n or B_f (split records). */
+xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* rec, int precision, int out_mode,
+                                    int which, void* Kc_vals, xk_stream s);
 
 /* Constraint Jacobian rows c_k n of the non-INACTIVE pairs in table order
  * (_build_constraint_jacobian_ptp, xkep_cae/contact/geometry/strategy.py:83-132).

@@ -26,7 +26,7 @@ def lib():
 
 def test_every_declared_symbol_is_exported(lib):
     names = _declared()
-    assert "xk_pair_eval" in names and len(names) >= 14
+    assert "xk_pair_step" in names and len(names) >= 14
     for n in sorted(names):
         assert hasattr(lib, n), n
 
@@ -50,4 +50,4 @@ def test_struct_layouts_match_header():
     assert C.sizeof(L.BeamPlan) == 8 + 4 * 8 + 8
     assert C.sizeof(L.ContactParams) == 6 * 8 + 8
     assert C.sizeof(L.BPParams) == 8 + 3 * 4 + 4 + 8
-    assert C.sizeof(L.ContactPattern) == 8 + 3 * 8 + 5 * 8
+    assert C.sizeof(L.ContactPattern) == 16 + 5 * 8 + 10 * 8

@@ -1,12 +1,13 @@
-// Deterministic, atomic-free reduction of pair contributions into nodal forces
-// and the block pattern / values of the contact tangent.
+// Per-increment contact pattern and the deterministic, atomic-free reduction of
+// pair contributions into nodal forces and 3x3 contact-tangent blocks.
 //
 // The reference scatters per-pair 12-vectors and 12x12 COO blocks and lets
-// np.add.at / scipy sum duplicates (contact_force/strategy.py:161-167,249-253;
-// friction/_assembly.py:85-105,119-157,184-257).  Here every pair is reduced
-// to v (3) and B (3x3) by the pair kernel, and each node (for forces) or each
-// 3x3 node block (for the tangent) sums the pairs incident to it in a fixed
-// order: contribution c_k v to node k, and c_k c_l B to block (k, l).
+// np.add.at / scipy sum the duplicates (contact_force/strategy.py:161-167,249-253;
+// friction/_assembly.py:85-105,119-157,184-257).  Here the pair kernel reduces
+// every contributing pair ("member") to a record (s, t, v, B): its force on
+// local node k is c_k v and its tangent block (k, l) is c_k c_l B with
+// c = [1-s, s, -(1-t), -t].  Each node sums its incident members and each
+// K_c block sums its contributor list, both in a fixed order.
 #include "xk_common.cuh"
 
 xk_status xk_sumsq_into(const double* x, long long n, double* out, cudaStream_t s);
@@ -23,71 +24,83 @@ XK_D void pair_nodes4(const xk_mesh& m, const xk_pairs& p, int i, int* nd) {
   nd[3] = m.conn[2 * eb + 1];
 }
 
-XK_D double shape_c(const xk_pairs& p, int i, int k) {
-  const double s = p.s[i], t = p.t[i];
+template <typename T>
+XK_D T shape_c(T s, T t, int k) {
   switch (k) {
-    case 0: return 1.0 - s;
+    case 0: return T(1) - s;
     case 1: return s;
-    case 2: return -(1.0 - t);
+    case 2: return -(T(1) - t);
     default: return -t;
   }
 }
 
-__global__ void k_member_count(xk_mesh m, xk_pairs p, int32_t* __restrict__ cnt, int32_t* __restrict__ nmem) {
+XK_D bool is_member(const xk_pairs& p, int i) { return (p.status[i] != 0) || (p.p_n[i] > 0.0); }
+
+__global__ void k_flags(xk_pairs p, int32_t* __restrict__ flag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool mem = false;
-  if (i < p.n) {
-    mem = (p.status[i] != 0) || (p.p_n[i] > 0.0);
-    if (mem) {
-      int nd[4];
-      pair_nodes4(m, p, i, nd);
-      for (int k = 0; k < 4; ++k) atomicAdd(&cnt[nd[k]], 1);
-    }
-  }
-  unsigned b = __ballot_sync(0xffffffffu, mem);
-  if ((threadIdx.x & 31) == 0 && b) atomicAdd(nmem, __popc(b));
+  if (i < p.n) flag[i] = is_member(p, i) ? 1 : 0;
+  else if (i == p.n) flag[i] = 0;
 }
 
-__global__ void k_inc_fill(xk_mesh m, xk_pairs p, const int32_t* __restrict__ ptr, int32_t* __restrict__ fill,
-                           int32_t* __restrict__ inc) {
+__global__ void k_split_lists(xk_mesh m, xk_pairs p, const int32_t* __restrict__ mpos, int32_t* __restrict__ members,
+                              int32_t* __restrict__ mnodes, int32_t* __restrict__ others) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
-  if (!((p.status[i] != 0) || (p.p_n[i] > 0.0))) return;
-  int nd[4];
-  pair_nodes4(m, p, i, nd);
-  for (int k = 0; k < 4; ++k) {
-    int slot = ptr[nd[k]] + atomicAdd(&fill[nd[k]], 1);
-    inc[slot] = (i << 2) | k;
+  const int k = mpos[i];
+  if (is_member(p, i)) {
+    members[k] = i;
+    int nd[4];
+    pair_nodes4(m, p, i, nd);
+    for (int q = 0; q < 4; ++q) mnodes[4LL * k + q] = nd[q];
+  } else {
+    others[i - k] = i;
   }
 }
 
-// Sort every node's incidence list (insertion sort; lists are short) so that
-// all later sums run in pair order, independent of the atomic fill order.
-__global__ void k_inc_sort(const int32_t* __restrict__ ptr, int n_nodes, int32_t* __restrict__ inc) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= n_nodes) return;
-  int a = ptr[v], b = ptr[v + 1];
-  for (int x = a + 1; x < b; ++x) {
-    int key = inc[x], y = x - 1;
-    while (y >= a && inc[y] > key) { inc[y + 1] = inc[y]; --y; }
-    inc[y + 1] = key;
+__global__ void k_inc_count(const int32_t* __restrict__ mnodes, int nm, int32_t* __restrict__ cnt) {
+  int mi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mi >= nm) return;
+  for (int k = 0; k < 4; ++k) atomicAdd(&cnt[mnodes[4LL * mi + k]], 1);
+}
+
+__global__ void k_inc_fill(const int32_t* __restrict__ mnodes, int nm, const int32_t* __restrict__ ptr,
+                           int32_t* __restrict__ fill, int32_t* __restrict__ inc) {
+  int mi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mi >= nm) return;
+  for (int k = 0; k < 4; ++k) {
+    const int v = mnodes[4LL * mi + k];
+    inc[ptr[v] + atomicAdd(&fill[v], 1)] = (mi << 2) | k;
+  }
+}
+
+// Insertion sort of every segment [ptr[v], ptr[v+1]) so that sums run in a
+// fixed order whatever the order of the atomic fill.
+__global__ void k_segment_sort(const int32_t* __restrict__ ptr, long long nseg, int32_t* __restrict__ a) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nseg) return;
+  const int lo = ptr[v], hi = ptr[v + 1];
+  for (int x = lo + 1; x < hi; ++x) {
+    const int key = a[x];
+    int y = x - 1;
+    while (y >= lo && a[y] > key) { a[y + 1] = a[y]; --y; }
+    a[y + 1] = key;
   }
 }
 
 // MODE 0: count the distinct column nodes of each row; MODE 1: write them sorted.
 template <int MODE>
-__global__ void k_row_cols(xk_mesh m, xk_pairs p, const int32_t* __restrict__ ptr, const int32_t* __restrict__ inc,
-                           int n_nodes, int32_t* __restrict__ rcnt, const int32_t* __restrict__ rptr,
-                           int32_t* __restrict__ col, int32_t* __restrict__ brow, int32_t* __restrict__ err) {
+__global__ void k_row_cols(const int32_t* __restrict__ mnodes, const int32_t* __restrict__ ptr,
+                           const int32_t* __restrict__ inc, int n_nodes, int32_t* __restrict__ rcnt,
+                           const int32_t* __restrict__ rptr, int32_t* __restrict__ col, int32_t* __restrict__ brow,
+                           int32_t* __restrict__ err) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n_nodes) return;
   int buf[MAX_COLS];
   int n = 0;
   for (int x = ptr[v]; x < ptr[v + 1]; ++x) {
-    int nd[4];
-    pair_nodes4(m, p, inc[x] >> 2, nd);
+    const long long mi = inc[x] >> 2;
     for (int k = 0; k < 4; ++k) {
-      int c = nd[k];
+      const int c = mnodes[4 * mi + k];
       int y = n - 1;
       while (y >= 0 && buf[y] > c) --y;
       if (y >= 0 && buf[y] == c) continue;
@@ -100,7 +113,7 @@ __global__ void k_row_cols(xk_mesh m, xk_pairs p, const int32_t* __restrict__ pt
   if (MODE == 0) {
     rcnt[v] = n;
   } else {
-    int o = rptr[v];
+    const int o = rptr[v];
     for (int k = 0; k < n; ++k) {
       col[o + k] = buf[k];
       brow[o + k] = v;
@@ -108,21 +121,50 @@ __global__ void k_row_cols(xk_mesh m, xk_pairs p, const int32_t* __restrict__ pt
   }
 }
 
+XK_D int find_block(const int32_t* __restrict__ rptr, const int32_t* __restrict__ col, int row, int c) {
+  int lo = rptr[row], hi = rptr[row + 1];
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (col[mid] < c) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// MODE 0: count contributions per block; MODE 1: fill (member << 4 | k << 2 | l).
+template <int MODE>
+__global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int32_t* __restrict__ rptr,
+                          const int32_t* __restrict__ col, int32_t* __restrict__ cnt,
+                          const int32_t* __restrict__ bptr, int32_t* __restrict__ contrib) {
+  int mi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mi >= nm) return;
+  int nd[4];
+  for (int q = 0; q < 4; ++q) nd[q] = mnodes[4LL * mi + q];
+  for (int k = 0; k < 4; ++k)
+    for (int l = 0; l < 4; ++l) {
+      const int b = find_block(rptr, col, nd[k], nd[l]);
+      if (MODE == 0) {
+        atomicAdd(&cnt[b], 1);
+      } else {
+        contrib[bptr[b] + atomicAdd(&cnt[b], 1)] = (mi << 4) | (k << 2) | l;
+      }
+    }
+}
+
 template <typename T>
-__global__ void k_gather_force(xk_mesh m, xk_pairs p, const int32_t* __restrict__ ptr, const int32_t* __restrict__ inc,
-                               const T* __restrict__ pv, int vcol, int vcol2, long long os, const double* __restrict__ base,
-                               double scale, const double* __restrict__ f_ext, const uint8_t* __restrict__ fixed,
-                               double* __restrict__ out) {
+__global__ void k_gather_force(int n_nodes, const int32_t* __restrict__ ptr, const int32_t* __restrict__ inc,
+                               const T* __restrict__ rec, long long rs, int vcol, int vcol2,
+                               const double* __restrict__ base, double scale, const double* __restrict__ f_ext,
+                               const uint8_t* __restrict__ fixed, double* __restrict__ out) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= m.n_nodes) return;
+  if (v >= n_nodes) return;
   double acc[3] = {0.0, 0.0, 0.0};
   if (ptr)
     for (int x = ptr[v]; x < ptr[v + 1]; ++x) {
-      const int code = inc[x], i = code >> 2, k = code & 3;
-      const double c = shape_c(p, i, k);
+      const int code = inc[x], mi = code >> 2, k = code & 3;
+      const double c = (double)shape_c<T>(rec[mi], rec[rs + mi], k);
       for (int d = 0; d < 3; ++d) {
-        double w = (double)pv[(vcol + d) * os + i];
-        if (vcol2 >= 0) w += (double)pv[(vcol2 + d) * os + i];
+        double w = (double)rec[(vcol + d) * rs + mi];
+        if (vcol2 >= 0) w += (double)rec[(vcol2 + d) * rs + mi];
         acc[d] += c * w;
       }
     }
@@ -137,26 +179,51 @@ __global__ void k_gather_force(xk_mesh m, xk_pairs p, const int32_t* __restrict_
 }
 
 template <typename T>
-__global__ void k_gather_tangent(xk_mesh m, xk_pairs p, const int32_t* __restrict__ ptr, const int32_t* __restrict__ inc,
-                                 const int32_t* __restrict__ col, const int32_t* __restrict__ brow, long long nnzb,
-                                 const T* __restrict__ pB, int bcol, long long os, T* __restrict__ K) {
+__global__ void k_gather_tangent(long long nnzb, const int32_t* __restrict__ bptr, const int32_t* __restrict__ contrib,
+                                 const T* __restrict__ rec, long long rs, int bcol, T* __restrict__ K) {
   long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nnzb) return;
-  const int row = brow[b], cn = col[b];
   T acc[9];
+#pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] = T(0);
-  for (int x = ptr[row]; x < ptr[row + 1]; ++x) {
-    const int code = inc[x], i = code >> 2, k = code & 3;
-    int nd[4];
-    pair_nodes4(m, p, i, nd);
-    const double ck = shape_c(p, i, k);
-    for (int l = 0; l < 4; ++l) {
-      if (nd[l] != cn) continue;
-      const T w = (T)(ck * shape_c(p, i, l));
-      for (int q = 0; q < 9; ++q) acc[q] += w * pB[(bcol + q) * os + i];
-    }
+  for (int x = bptr[b]; x < bptr[b + 1]; ++x) {
+    const int code = contrib[x], mi = code >> 4, k = (code >> 2) & 3, l = code & 3;
+    const T s = rec[mi], t = rec[rs + mi];
+    const T w = shape_c<T>(s, t, k) * shape_c<T>(s, t, l);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] += w * rec[(bcol + q) * rs + mi];
   }
+#pragma unroll
   for (int q = 0; q < 9; ++q) K[9 * b + q] = acc[q];
+}
+
+struct Scratch {
+  cudaStream_t s;
+  void* p[8];
+  int n = 0;
+  template <typename T>
+  xk_status get(T** out, long long count) {
+    if (count < 1) count = 1;
+    cudaError_t e = cudaMallocAsync((void**)out, sizeof(T) * count, s);
+    if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);
+    p[n++] = *out;
+    return XK_OK;
+  }
+  ~Scratch() {
+    for (int i = 0; i < n; ++i) cudaFreeAsync(p[i], s);
+  }
+};
+
+#define XK_TRY(x)                 \
+  do {                            \
+    xk_status r__ = (x);          \
+    if (r__ != XK_OK) return r__; \
+  } while (0)
+
+xk_status fetch_i64(const int64_t* dev, int64_t* host, int n, cudaStream_t st) {
+  XK_CUDA(cudaMemcpyAsync(host, dev, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaStreamSynchronize(st));
+  return XK_OK;
 }
 
 }  // namespace
@@ -167,119 +234,135 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   if (!pat->inc_ptr || !pat->row_ptr) return xk_set_error(XK_ERR_ARG, "xk_contact_pattern_build: row arrays missing");
   cudaStream_t st = (cudaStream_t)s;
   const int nn = m->n_nodes;
+  const long long np = p->n;
   pat->n_nodes = nn;
-  int32_t *cnt = nullptr, *fill = nullptr, *scal = nullptr;
-  int64_t* tot = nullptr;
-  XK_CUDA(cudaMallocAsync((void**)&cnt, sizeof(int32_t) * (nn + 1), st));
-  XK_CUDA(cudaMallocAsync((void**)&fill, sizeof(int32_t) * (nn + 1), st));
-  XK_CUDA(cudaMallocAsync((void**)&scal, sizeof(int32_t) * 2, st));
-  XK_CUDA(cudaMallocAsync((void**)&tot, sizeof(int64_t) * 2, st));
-  xk_status r = XK_OK;
-  int32_t hs[2] = {0, 0};
-  int64_t ht[2] = {0, 0};
-  auto fail = [&](cudaError_t e) { r = xk_set_cuda_error(e, __FILE__, __LINE__); };
-  do {
-    cudaError_t e;
-    if ((e = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nn + 1), st)) != cudaSuccess) { fail(e); break; }
-    if ((e = cudaMemsetAsync(scal, 0, sizeof(int32_t) * 2, st)) != cudaSuccess) { fail(e); break; }
-    if (p->n > 0) k_member_count<<<xk_blocks(p->n, 256), 256, 0, st>>>(*m, *p, cnt, scal);
-    if ((e = cudaGetLastError()) != cudaSuccess) { fail(e); break; }
-    if ((r = xk_exclusive_scan_i32(cnt, pat->inc_ptr, nn + 1, tot, st)) != XK_OK) break;
-    if ((e = cudaMemcpyAsync(hs, scal, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, st)) != cudaSuccess) { fail(e); break; }
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) { fail(e); break; }
-    pat->n_members = hs[0];
-    if ((long long)hs[0] > pat->cap_members) {
-      r = xk_set_error(XK_ERR_CAPACITY, "xk_contact_pattern_build: member capacity too small");
-      break;
-    }
-    if ((e = cudaMemsetAsync(fill, 0, sizeof(int32_t) * (nn + 1), st)) != cudaSuccess) { fail(e); break; }
-    if (p->n > 0) k_inc_fill<<<xk_blocks(p->n, 256), 256, 0, st>>>(*m, *p, pat->inc_ptr, fill, pat->inc);
-    k_inc_sort<<<xk_blocks(nn, 128), 128, 0, st>>>(pat->inc_ptr, nn, pat->inc);
-    k_row_cols<0><<<xk_blocks(nn, 64), 64, 0, st>>>(*m, *p, pat->inc_ptr, pat->inc, nn, cnt, nullptr, nullptr,
-                                                     nullptr, scal + 1);
-    if ((e = cudaGetLastError()) != cudaSuccess) { fail(e); break; }
-    if ((e = cudaMemsetAsync(cnt + nn, 0, sizeof(int32_t), st)) != cudaSuccess) { fail(e); break; }
-    if ((r = xk_exclusive_scan_i32(cnt, pat->row_ptr, nn + 1, tot + 1, st)) != XK_OK) break;
-    if ((e = cudaMemcpyAsync(ht, tot, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, st)) != cudaSuccess) { fail(e); break; }
-    if ((e = cudaMemcpyAsync(hs, scal, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, st)) != cudaSuccess) { fail(e); break; }
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) { fail(e); break; }
-    if (hs[1]) {
-      r = xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: a node touches more than 256 distinct contact column nodes");
-      break;
-    }
-    pat->nnzb = ht[1];
-    if (ht[1] > pat->cap_blocks) {
-      r = xk_set_error(XK_ERR_CAPACITY, "xk_contact_pattern_build: block capacity too small");
-      break;
-    }
-    k_row_cols<1><<<xk_blocks(nn, 64), 64, 0, st>>>(*m, *p, pat->inc_ptr, pat->inc, nn, nullptr, pat->row_ptr,
-                                                     pat->col, pat->blk_row, scal + 1);
-    if ((e = cudaGetLastError()) != cudaSuccess) { fail(e); break; }
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) { fail(e); break; }
-  } while (0);
-  cudaFreeAsync(cnt, st);
-  cudaFreeAsync(fill, st);
-  cudaFreeAsync(scal, st);
-  cudaFreeAsync(tot, st);
-  return r;
+  Scratch S{st};
+  int32_t *flag, *mpos, *cnt, *fill, *err;
+  int64_t* tot;
+  XK_TRY(S.get(&flag, np + 1));
+  XK_TRY(S.get(&mpos, np + 1));
+  XK_TRY(S.get(&cnt, nn + 1));
+  XK_TRY(S.get(&fill, nn + 1));
+  XK_TRY(S.get(&err, 1));
+  XK_TRY(S.get(&tot, 4));
+  // members and others
+  k_flags<<<xk_blocks(np + 1, 256), 256, 0, st>>>(*p, flag);
+  XK_CHECK_LAUNCH();
+  XK_TRY(xk_exclusive_scan_i32(flag, mpos, np + 1, tot, st));
+  int64_t h[4] = {0, 0, 0, 0};
+  XK_TRY(fetch_i64(tot, h, 1, st));
+  const long long nm = h[0];
+  pat->n_members = (int32_t)nm;
+  pat->n_others = (int32_t)(np - nm);
+  if (nm > pat->cap_members || np - nm > pat->cap_others)
+    return xk_set_error(XK_ERR_CAPACITY, "xk_contact_pattern_build: member / other-pair capacity too small");
+  if (np > 0) k_split_lists<<<xk_blocks(np, 256), 256, 0, st>>>(*m, *p, mpos, pat->members, pat->member_nodes,
+                                                                 pat->others);
+  // node incidence of the members
+  XK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nn + 1), st));
+  if (nm > 0) k_inc_count<<<xk_blocks(nm, 256), 256, 0, st>>>(pat->member_nodes, (int)nm, cnt);
+  XK_CHECK_LAUNCH();
+  XK_TRY(xk_exclusive_scan_i32(cnt, pat->inc_ptr, nn + 1, nullptr, st));
+  XK_CUDA(cudaMemsetAsync(fill, 0, sizeof(int32_t) * (nn + 1), st));
+  if (nm > 0) k_inc_fill<<<xk_blocks(nm, 256), 256, 0, st>>>(pat->member_nodes, (int)nm, pat->inc_ptr, fill, pat->inc);
+  k_segment_sort<<<xk_blocks(nn, 128), 128, 0, st>>>(pat->inc_ptr, nn, pat->inc);
+  // block pattern rows
+  XK_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), st));
+  k_row_cols<0><<<xk_blocks(nn, 64), 64, 0, st>>>(pat->member_nodes, pat->inc_ptr, pat->inc, nn, cnt, nullptr,
+                                                   nullptr, nullptr, err);
+  XK_CHECK_LAUNCH();
+  XK_CUDA(cudaMemsetAsync(cnt + nn, 0, sizeof(int32_t), st));
+  XK_TRY(xk_exclusive_scan_i32(cnt, pat->row_ptr, nn + 1, tot + 1, st));
+  int32_t herr = 0;
+  XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  XK_TRY(fetch_i64(tot, h, 2, st));
+  if (herr) return xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: a node touches more than 256 contact nodes");
+  const long long nb = h[1];
+  pat->nnzb = nb;
+  pat->n_contrib = 16 * nm;
+  if (nb > pat->cap_blocks) return xk_set_error(XK_ERR_CAPACITY, "xk_contact_pattern_build: block capacity too small");
+  k_row_cols<1><<<xk_blocks(nn, 64), 64, 0, st>>>(pat->member_nodes, pat->inc_ptr, pat->inc, nn, nullptr,
+                                                   pat->row_ptr, pat->col, pat->blk_row, err);
+  XK_CHECK_LAUNCH();
+  // contributor lists of the blocks
+  int32_t *bcnt, *bfill;
+  XK_TRY(S.get(&bcnt, nb + 1));
+  XK_TRY(S.get(&bfill, nb + 1));
+  XK_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int32_t) * (nb + 1), st));
+  if (nm > 0) k_contrib<0><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
+                                                                bcnt, nullptr, nullptr);
+  XK_CHECK_LAUNCH();
+  XK_TRY(xk_exclusive_scan_i32(bcnt, pat->blk_ptr, nb + 1, nullptr, st));
+  XK_CUDA(cudaMemsetAsync(bfill, 0, sizeof(int32_t) * (nb + 1), st));
+  if (nm > 0) k_contrib<1><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
+                                                                bfill, pat->blk_ptr, pat->contrib);
+  if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
+  XK_CHECK_LAUNCH();
+  XK_CUDA(cudaStreamSynchronize(st));
+  return XK_OK;
 }
 
-extern "C" xk_status xk_contact_gather_force(const xk_mesh* m, const xk_pairs* p, const xk_contact_pattern* pat,
-                                             const void* pv, int precision, int out_mode, int which,
-                                             int64_t out_stride, const double* base, double scale,
+static xk_status rec_columns(int out_mode, int which, bool tangent, int* c1, int* c2) {
+  *c2 = -1;
+  if (out_mode == XK_OUT_COMBINED) {
+    if (which != XK_WHICH_COMBINED) return xk_set_error(XK_ERR_ARG, "combined records hold only combined values");
+    *c1 = tangent ? 5 : 2;
+    return XK_OK;
+  }
+  if (out_mode != XK_OUT_SPLIT) return xk_set_error(XK_ERR_ARG, "out_mode");
+  if (tangent) {
+    if (which == XK_WHICH_NORMAL) *c1 = 8;
+    else if (which == XK_WHICH_FRICTION) *c1 = 17;
+    else return xk_set_error(XK_ERR_ARG, "split tangent records need which = normal or friction");
+  } else {
+    if (which == XK_WHICH_NORMAL) *c1 = 2;
+    else if (which == XK_WHICH_FRICTION) *c1 = 5;
+    else { *c1 = 2; *c2 = 5; }
+  }
+  return XK_OK;
+}
+
+extern "C" xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec, int precision,
+                                             int out_mode, int which, const double* base, double scale,
                                              const double* f_ext, const uint8_t* fixed, double* out, double* norm2,
                                              xk_stream s) {
-  if (!m || !p || !out) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force: null argument");
-  int vcol = 0, vcol2 = -1;
-  if (out_mode == XK_OUT_SPLIT) {
-    if (which == XK_WHICH_NORMAL) vcol = 0;
-    else if (which == XK_WHICH_FRICTION) vcol = 3;
-    else { vcol = 0; vcol2 = 3; }
-  } else if (which != XK_WHICH_COMBINED) {
-    return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force: combined output holds only the combined force");
-  }
-  const bool use_pairs = pat && pat->n_members > 0 && pv;
-  const int32_t* ptr = use_pairs ? pat->inc_ptr : nullptr;
-  const int32_t* inc = use_pairs ? pat->inc : nullptr;
+  if (!pat || !out) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force: null argument");
+  int c1, c2;
+  XK_TRY(rec_columns(out_mode, which, false, &c1, &c2));
+  const bool use = pat->n_members > 0 && rec;
+  const int32_t* ptr = use ? pat->inc_ptr : nullptr;
+  const int32_t* inc = use ? pat->inc : nullptr;
   cudaStream_t st = (cudaStream_t)s;
-  if (m->n_nodes > 0) {
+  const int nn = pat->n_nodes;
+  if (nn > 0) {
     if (precision == XK_FP64)
-      k_gather_force<double><<<xk_blocks(m->n_nodes, 128), 128, 0, st>>>(*m, *p, ptr, inc, (const double*)pv, vcol,
-                                                                          vcol2, out_stride, base, scale, f_ext, fixed,
-                                                                          out);
+      k_gather_force<double><<<xk_blocks(nn, 128), 128, 0, st>>>(nn, ptr, inc, (const double*)rec, pat->cap_members,
+                                                                  c1, c2, base, scale, f_ext, fixed, out);
     else if (precision == XK_MIXED)
-      k_gather_force<float><<<xk_blocks(m->n_nodes, 128), 128, 0, st>>>(*m, *p, ptr, inc, (const float*)pv, vcol,
-                                                                         vcol2, out_stride, base, scale, f_ext, fixed,
-                                                                         out);
+      k_gather_force<float><<<xk_blocks(nn, 128), 128, 0, st>>>(nn, ptr, inc, (const float*)rec, pat->cap_members,
+                                                                 c1, c2, base, scale, f_ext, fixed, out);
     else
       return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force: precision");
     XK_CHECK_LAUNCH();
   }
-  if (norm2) return xk_sumsq_into(out, 6LL * m->n_nodes, norm2, st);
+  if (norm2) return xk_sumsq_into(out, 6LL * nn, norm2, st);
   return XK_OK;
 }
 
-extern "C" xk_status xk_contact_gather_tangent(const xk_mesh* m, const xk_pairs* p, const xk_contact_pattern* pat,
-                                               const void* pB, int precision, int out_mode, int which,
-                                               int64_t out_stride, void* Kc_vals, xk_stream s) {
-  if (!m || !p || !pat || !pB || !Kc_vals) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: null argument");
-  int bcol = 0;
-  if (out_mode == XK_OUT_SPLIT) {
-    if (which == XK_WHICH_NORMAL) bcol = 0;
-    else if (which == XK_WHICH_FRICTION) bcol = 9;
-    else return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: split output needs which = normal or friction");
-  } else if (which != XK_WHICH_COMBINED) {
-    return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: combined output holds only the combined tangent");
-  }
+extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* rec, int precision,
+                                               int out_mode, int which, void* Kc_vals, xk_stream s) {
+  if (!pat || !rec || !Kc_vals) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: null argument");
+  int c1, c2;
+  XK_TRY(rec_columns(out_mode, which, true, &c1, &c2));
   if (pat->nnzb == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
   const int nb = xk_blocks(pat->nnzb, 128);
   if (precision == XK_FP64)
-    k_gather_tangent<double><<<nb, 128, 0, st>>>(*m, *p, pat->inc_ptr, pat->inc, pat->col, pat->blk_row, pat->nnzb,
-                                                 (const double*)pB, bcol, out_stride, (double*)Kc_vals);
+    k_gather_tangent<double><<<nb, 128, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const double*)rec,
+                                                 pat->cap_members, c1, (double*)Kc_vals);
   else if (precision == XK_MIXED)
-    k_gather_tangent<float><<<nb, 128, 0, st>>>(*m, *p, pat->inc_ptr, pat->inc, pat->col, pat->blk_row, pat->nnzb,
-                                                (const float*)pB, bcol, out_stride, (float*)Kc_vals);
+    k_gather_tangent<float><<<nb, 128, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const float*)rec,
+                                                pat->cap_members, c1, (float*)Kc_vals);
   else
     return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: precision");
   XK_CHECK_LAUNCH();

@@ -1,5 +1,7 @@
 // Contact pairs: narrowphase, Huber normal force, Coulomb return mapping and
-// the factorised pair tangent, one pair per thread over the SoA pair table.
+// the factorised pair tangent.  One thread per pair; contributing pairs and
+// the rest run as two launches over the per-increment lists so that warps do
+// not diverge between the two kinds of work.
 #include "xk_common.cuh"
 
 namespace {
@@ -182,10 +184,13 @@ XK_D void frame_mixed(const double* nrm, const double* pt1d, const double* pnd, 
       float v[3], vx[3], vvx[3];
       cross3(no, n, v);
       float cv = dot3(no, n);
-      if (cv > -0.99f) {
+      float s2 = dot3(v, v);
+      // (1 - c) / s^2 of the reference equals 1 / (1 + c) for unit vectors and
+      // has no cancellation; near c = -1 the reference form is the stable one
+      if (cv > 0.0f || s2 >= 1e-24f) {
         cross3(v, pt1, vx);
         cross3(v, vx, vvx);
-        float f = 1.0f / (1.0f + cv);
+        float f = cv > 0.0f ? 1.0f / (1.0f + cv) : (1.0f - cv) / s2;
         for (int i = 0; i < 3; ++i) tr[i] = pt1[i] + vx[i] + f * vvx[i];
       }
     }
@@ -266,49 +271,73 @@ XK_HD double huber_deriv(double x, double d) {  // contact_force/strategy.py:115
   return (x + d) / (2.0 * d);
 }
 
-template <int P, int OUT>
-__global__ void __launch_bounds__(PAIR_T) k_pair(xk_mesh m, xk_pairs p, const double* __restrict__ u,
-                                                 const double* __restrict__ u_ref, xk_contact_params cp, int stages,
-                                                 typename Prec<P>::T* __restrict__ pv,
-                                                 typename Prec<P>::T* __restrict__ pB, long long ostride) {
-  typedef typename Prec<P>::T T;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
+// Narrowphase of one pair at X + u, exact (FP64) or mixed, written to the pair table.
+template <int P>
+XK_D void pair_narrow(const xk_mesh& m, xk_pairs& p, int i, const int* nd, const double* __restrict__ u, double& s,
+                      double& t, double& gap, double* n, double* t1, double* t2) {
   const long long cap = p.cap;
+  const double ra = m.radii[p.ea[i]], rb = m.radii[p.eb[i]];
+  double x[4][3];
+  for (int k = 0; k < 4; ++k)
+    for (int c = 0; c < 3; ++c) x[k][c] = xadd(m.X[3LL * nd[k] + c], u[6LL * nd[k] + c]);
+  double dist, nrm[3], pt1[3], pn[3];
+  load3(p.t1, cap, i, pt1);
+  load3(p.normal, cap, i, pn);
+  if (P == XK_FP64) {
+    double diff[3];
+    closest_exact(x[0], x[1], x[2], x[3], s, t, dist, nrm, diff);
+    gap = xsub(dist, xadd(ra, rb));
+    frame_exact(nrm, pt1, pn, n, t1, t2);
+  } else {
+    closest_mixed(x[0], x[1], x[2], x[3], s, t, dist, nrm);
+    gap = dist - (ra + rb);
+    frame_mixed(nrm, pt1, pn, n, t1, t2);
+  }
+  p.s[i] = s;
+  p.t[i] = t;
+  p.gap[i] = gap;
+  store3(p.normal, cap, i, n);
+  store3(p.t1, cap, i, t1);
+  store3(p.t2, cap, i, t2);
+}
+
+// Pairs that cannot contribute in this increment: only the frozen narrowphase,
+// which the reference runs on every pair (_newton_steps.py:91-94) and which
+// carries the frame transport history.
+template <int P>
+__global__ void __launch_bounds__(PAIR_T) k_pair_other(xk_mesh m, xk_pairs p, const int32_t* __restrict__ others,
+                                                       int n_o, const double* __restrict__ u) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n_o) return;
+  const int i = others[o];
+  int nd[4];
   const int ea = p.ea[i], eb = p.eb[i];
+  nd[0] = m.conn[2 * ea]; nd[1] = m.conn[2 * ea + 1]; nd[2] = m.conn[2 * eb]; nd[3] = m.conn[2 * eb + 1];
+  double s, t, gap, n[3], t1[3], t2[3];
+  pair_narrow<P>(m, p, i, nd, u, s, t, gap, n, t1, t2);
+}
+
+// Contributing pairs: narrowphase, Huber normal force, Coulomb return mapping
+// and the pair tangent, one record (s, t, v, B) per member.
+template <int P, int OUT>
+__global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, const int32_t* __restrict__ members,
+                                                        const int32_t* __restrict__ mnodes, int n_m,
+                                                        const double* __restrict__ u, const double* __restrict__ u_ref,
+                                                        xk_contact_params cp, int stages,
+                                                        typename Prec<P>::T* __restrict__ rec, long long rs) {
+  typedef typename Prec<P>::T T;
+  const int mi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mi >= n_m) return;
+  const int i = members[mi];
+  const long long cap = p.cap;
+  int nd[4];
+  for (int k = 0; k < 4; ++k) nd[k] = mnodes[4LL * mi + k];
   uint8_t status = p.status[i];
   double p_n = p.p_n[i];
-  const bool member = (status != ST_INACTIVE) || (p_n > 0.0);
-  if (!member && !(stages & XK_STAGE_NARROW)) return;
-  const PairNodes nd = pair_nodes(m, ea, eb);
-  const double ra = m.radii[ea], rb = m.radii[eb];
+  const double ra = m.radii[p.ea[i]], rb = m.radii[p.eb[i]];
   double s, t, gap, n[3], t1[3], t2[3];
   if (stages & XK_STAGE_NARROW) {
-    double x[4][3];
-    for (int k = 0; k < 4; ++k) {
-      x[k][0] = m.X[3LL * nd.n[k]] + u[6LL * nd.n[k]];
-      x[k][1] = m.X[3LL * nd.n[k] + 1] + u[6LL * nd.n[k] + 1];
-      x[k][2] = m.X[3LL * nd.n[k] + 2] + u[6LL * nd.n[k] + 2];
-    }
-    double dist, nrm[3], pt1[3], pn[3];
-    load3(p.t1, cap, i, pt1);
-    load3(p.normal, cap, i, pn);
-    if (P == XK_FP64) {
-      double diff[3];
-      closest_exact(x[0], x[1], x[2], x[3], s, t, dist, nrm, diff);
-      gap = xsub(dist, xadd(ra, rb));
-      frame_exact(nrm, pt1, pn, n, t1, t2);
-    } else {
-      closest_mixed(x[0], x[1], x[2], x[3], s, t, dist, nrm);
-      gap = dist - (ra + rb);
-      frame_mixed(nrm, pt1, pn, n, t1, t2);
-    }
-    p.s[i] = s;
-    p.t[i] = t;
-    p.gap[i] = gap;
-    store3(p.normal, cap, i, n);
-    store3(p.t1, cap, i, t1);
-    store3(p.t2, cap, i, t2);
+    pair_narrow<P>(m, p, i, nd, u, s, t, gap, n, t1, t2);
   } else {
     s = p.s[i];
     t = p.t[i];
@@ -317,7 +346,6 @@ __global__ void __launch_bounds__(PAIR_T) k_pair(xk_mesh m, xk_pairs p, const do
     load3(p.t1, cap, i, t1);
     load3(p.t2, cap, i, t2);
   }
-  if (!member) return;
   const double dh = cp.smoothing_delta > 0.0 ? cp.k_pen / cp.smoothing_delta : 0.0;
   const double xpen = cp.k_pen * (-gap);
   T vn[3] = {T(0), T(0), T(0)}, vf[3] = {T(0), T(0), T(0)};
@@ -346,7 +374,7 @@ __global__ void __launch_bounds__(PAIR_T) k_pair(xk_mesh m, xk_pairs p, const do
     T du[4][3];
     for (int k = 0; k < 4; ++k)
       for (int c = 0; c < 3; ++c) {
-        long long dof = 6LL * nd.n[k] + c;
+        const long long dof = 6LL * nd[k] + c;
         du[k][c] = (T)(u_ref ? u[dof] - u_ref[dof] : u[dof]);
       }
     const T sT = (T)s, tT = (T)t;
@@ -372,7 +400,7 @@ __global__ void __launch_bounds__(PAIR_T) k_pair(xk_mesh m, xk_pairs p, const do
     status = stick ? ST_ACTIVE : ST_SLIDING;
     p.status[i] = status;
     if (my_sqrt<T>(r0 * r0 + r1 * r1) >= T(1e-30)) {
-      const T a0 = fabs(r0) < T(1e-30) ? T(0) : r0, a1 = fabs(r1) < T(1e-30) ? T(0) : r1;
+      const T a0 = my_abs<T>(r0) < T(1e-30) ? T(0) : r0, a1 = my_abs<T>(r1) < T(1e-30) ? T(0) : r1;
       for (int k = 0; k < 3; ++k) vf[k] = a0 * t1T[k] + a1 * t2T[k];
     }
   }
@@ -387,7 +415,7 @@ __global__ void __launch_bounds__(PAIR_T) k_pair(xk_mesh m, xk_pairs p, const do
       const T wg = (T)(dist > 1e-15 ? p_n / dist : 0.0);
       for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
-          T nn = nT[a] * nT[b];
+          const T nn = nT[a] * nT[b];
           Bn[3 * a + b] = wm * nn - wg * ((a == b ? T(1) : T(0)) - nn);
         }
     }
@@ -396,25 +424,25 @@ __global__ void __launch_bounds__(PAIR_T) k_pair(xk_mesh m, xk_pairs p, const do
     if (fproc && qnorm >= T(1e-30)) {
       const T ktT = (T)kt;
       T D00 = ktT, D01 = T(0), D11 = ktT;
-      if (!stick && qnorm >= T(1e-30) && (T)qtn >= T(1e-30)) {
+      if (!stick && (T)qtn >= T(1e-30)) {
         const T qh0 = q0 / qnorm, qh1 = q1 / qnorm;
         const T ratio = (T)cp.mu_eff * (T)p_n / (T)qtn;
         D00 = ratio * ktT * (T(1) - qh0 * qh0);
         D01 = -ratio * ktT * qh0 * qh1;
         D11 = ratio * ktT * (T(1) - qh1 * qh1);
       }
-      if (fabs(D00) < T(1e-30)) D00 = T(0);
-      if (fabs(D01) < T(1e-30)) D01 = T(0);
-      if (fabs(D11) < T(1e-30)) D11 = T(0);
-      const bool geo = (dist >= 1e-15) && !(fabs(q0) < T(1e-30) && fabs(q1) < T(1e-30));
+      if (my_abs<T>(D00) < T(1e-30)) D00 = T(0);
+      if (my_abs<T>(D01) < T(1e-30)) D01 = T(0);
+      if (my_abs<T>(D11) < T(1e-30)) D11 = T(0);
+      const bool geo = (dist >= 1e-15) && !(my_abs<T>(q0) < T(1e-30) && my_abs<T>(q1) < T(1e-30));
       const T idist = geo ? (T)(1.0 / dist) : T(0);
       for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
-          T mat = D00 * t1T[a] * t1T[b] + D01 * (t1T[a] * t2T[b] + t2T[a] * t1T[b]) + D11 * t2T[a] * t2T[b];
-          T M = -q0 * nT[a] * t1T[b] - q1 * t2T[a] * nT[b];
+          const T mat = D00 * t1T[a] * t1T[b] + D01 * (t1T[a] * t2T[b] + t2T[a] * t1T[b]) + D11 * t2T[a] * t2T[b];
+          const T M = -q0 * nT[a] * t1T[b] - q1 * t2T[a] * nT[b];
           Bf[3 * a + b] = mat + idist * M;
         }
-      // q2 [t1]x^T
+      // + q2 [t1]x^T
       Bf[1] += idist * q1 * t1T[2];
       Bf[2] -= idist * q1 * t1T[1];
       Bf[3] -= idist * q1 * t1T[2];
@@ -423,22 +451,20 @@ __global__ void __launch_bounds__(PAIR_T) k_pair(xk_mesh m, xk_pairs p, const do
       Bf[7] -= idist * q1 * t1T[0];
     }
   }
-  // ---------------------------------------------------------------- outputs
+  // ---------------------------------------------------------------- record
+  rec[mi] = (T)s;
+  rec[rs + mi] = (T)t;
   if (OUT == XK_OUT_COMBINED) {
-    if (pv)
-      for (int k = 0; k < 3; ++k) pv[k * ostride + i] = vn[k] + vf[k];
-    if (pB)
-      for (int k = 0; k < 9; ++k) pB[k * ostride + i] = Bn[k] - Bf[k];
+    for (int k = 0; k < 3; ++k) rec[(2 + k) * rs + mi] = vn[k] + vf[k];
+    for (int k = 0; k < 9; ++k) rec[(5 + k) * rs + mi] = Bn[k] - Bf[k];
   } else {
-    if (pv) {
-      if (stages & XK_STAGE_NORMAL)
-        for (int k = 0; k < 3; ++k) pv[k * ostride + i] = vn[k];
-      if (stages & XK_STAGE_FRICTION)
-        for (int k = 0; k < 3; ++k) pv[(3 + k) * ostride + i] = vf[k];
-    }
-    if (pB && (stages & XK_STAGE_TANGENT)) {
-      for (int k = 0; k < 9; ++k) pB[k * ostride + i] = Bn[k];
-      for (int k = 0; k < 9; ++k) pB[(9 + k) * ostride + i] = Bf[k];
+    if (stages & XK_STAGE_NORMAL)
+      for (int k = 0; k < 3; ++k) rec[(2 + k) * rs + mi] = vn[k];
+    if (stages & XK_STAGE_FRICTION)
+      for (int k = 0; k < 3; ++k) rec[(5 + k) * rs + mi] = vf[k];
+    if (stages & XK_STAGE_TANGENT) {
+      for (int k = 0; k < 9; ++k) rec[(8 + k) * rs + mi] = Bn[k];
+      for (int k = 0; k < 9; ++k) rec[(17 + k) * rs + mi] = Bf[k];
     }
   }
 }
@@ -479,31 +505,45 @@ extern "C" xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double*
   return XK_OK;
 }
 
-extern "C" xk_status xk_pair_eval(const xk_mesh* m, xk_pairs* p, const double* u, const double* u_ref,
-                                  const xk_contact_params* cp, int stages, int precision, int out_mode, void* pv,
-                                  void* pB, int64_t out_stride, xk_stream s) {
-  if (!m || !p || !cp) return xk_set_error(XK_ERR_ARG, "xk_pair_eval: null argument");
+extern "C" xk_status xk_pair_step(const xk_mesh* m, xk_pairs* p, const xk_contact_pattern* pat, const double* u,
+                                  const double* u_ref, const xk_contact_params* cp, int stages, int precision,
+                                  int out_mode, void* rec, xk_stream s) {
+  if (!m || !p || !pat || !cp) return xk_set_error(XK_ERR_ARG, "xk_pair_step: null argument");
   if (((stages & XK_STAGE_NARROW) || (stages & XK_STAGE_FRICTION)) && !u)
-    return xk_set_error(XK_ERR_ARG, "xk_pair_eval: u is required for the narrowphase and friction stages");
-  if (out_mode == XK_OUT_COMBINED && (stages & (XK_STAGE_NORMAL | XK_STAGE_FRICTION | XK_STAGE_TANGENT)) !=
-                                         (XK_STAGE_NORMAL | XK_STAGE_FRICTION | XK_STAGE_TANGENT))
-    return xk_set_error(XK_ERR_ARG, "xk_pair_eval: the combined output needs the normal, friction and tangent stages");
-  if (out_stride < p->n) return xk_set_error(XK_ERR_ARG, "xk_pair_eval: out_stride < n");
-  if (p->n == 0) return XK_OK;
+    return xk_set_error(XK_ERR_ARG, "xk_pair_step: u is required for the narrowphase and friction stages");
+  const int all = XK_STAGE_NORMAL | XK_STAGE_FRICTION | XK_STAGE_TANGENT;
+  if (out_mode == XK_OUT_COMBINED && (stages & all) != all)
+    return xk_set_error(XK_ERR_ARG, "xk_pair_step: combined records need the normal, friction and tangent stages");
+  if (pat->n_members > 0 && !rec) return xk_set_error(XK_ERR_ARG, "xk_pair_step: rec is null");
+  if ((long long)pat->n_members + pat->n_others != p->n)
+    return xk_set_error(XK_ERR_ARG, "xk_pair_step: pattern was built for another pair table");
   cudaStream_t st = (cudaStream_t)s;
-  const int nb = xk_blocks(p->n, PAIR_T);
-#define XK_PAIR_LAUNCH(PP, OO, TT) \
-  k_pair<PP, OO><<<nb, PAIR_T, 0, st>>>(*m, *p, u, u_ref, *cp, stages, (TT*)pv, (TT*)pB, out_stride)
-  if (precision == XK_FP64) {
-    if (out_mode == XK_OUT_COMBINED) XK_PAIR_LAUNCH(XK_FP64, XK_OUT_COMBINED, double);
-    else XK_PAIR_LAUNCH(XK_FP64, XK_OUT_SPLIT, double);
-  } else if (precision == XK_MIXED) {
-    if (out_mode == XK_OUT_COMBINED) XK_PAIR_LAUNCH(XK_MIXED, XK_OUT_COMBINED, float);
-    else XK_PAIR_LAUNCH(XK_MIXED, XK_OUT_SPLIT, float);
-  } else {
-    return xk_set_error(XK_ERR_ARG, "xk_pair_eval: precision");
+  if ((stages & XK_STAGE_NARROW) && pat->n_others > 0) {
+    const int nb = xk_blocks(pat->n_others, PAIR_T);
+    if (precision == XK_FP64)
+      k_pair_other<XK_FP64><<<nb, PAIR_T, 0, st>>>(*m, *p, pat->others, pat->n_others, u);
+    else if (precision == XK_MIXED)
+      k_pair_other<XK_MIXED><<<nb, PAIR_T, 0, st>>>(*m, *p, pat->others, pat->n_others, u);
+    else
+      return xk_set_error(XK_ERR_ARG, "xk_pair_step: precision");
+    XK_CHECK_LAUNCH();
   }
-#undef XK_PAIR_LAUNCH
+  if (pat->n_members == 0) return XK_OK;
+  const int nb = xk_blocks(pat->n_members, PAIR_T);
+  const long long rs = pat->cap_members;
+#define XK_MEMBER_LAUNCH(PP, OO, TT)                                                                                \
+  k_pair_member<PP, OO><<<nb, PAIR_T, 0, st>>>(*m, *p, pat->members, pat->member_nodes, pat->n_members, u, u_ref, \
+                                               *cp, stages, (TT*)rec, rs)
+  if (precision == XK_FP64) {
+    if (out_mode == XK_OUT_COMBINED) XK_MEMBER_LAUNCH(XK_FP64, XK_OUT_COMBINED, double);
+    else XK_MEMBER_LAUNCH(XK_FP64, XK_OUT_SPLIT, double);
+  } else if (precision == XK_MIXED) {
+    if (out_mode == XK_OUT_COMBINED) XK_MEMBER_LAUNCH(XK_MIXED, XK_OUT_COMBINED, float);
+    else XK_MEMBER_LAUNCH(XK_MIXED, XK_OUT_SPLIT, float);
+  } else {
+    return xk_set_error(XK_ERR_ARG, "xk_pair_step: precision");
+  }
+#undef XK_MEMBER_LAUNCH
   XK_CHECK_LAUNCH();
   return XK_OK;
 }

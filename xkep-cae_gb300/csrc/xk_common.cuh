@@ -63,6 +63,8 @@ template <>
 XK_HD double my_sqrt<double>(double x) { return sqrt(x); }
 template <>
 XK_HD float my_sqrt<float>(float x) { return sqrtf(x); }
+template <typename T>
+XK_HD T my_abs(T x) { return x < T(0) ? -x : x; }
 
 // Precision policy: P == XK_FP64 computes everything in double; P == XK_MIXED
 // computes the bulk in float and keeps the rotation frames, the axial strain,

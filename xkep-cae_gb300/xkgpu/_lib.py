@@ -17,6 +17,7 @@ XK_STAGE_NARROW, XK_STAGE_NORMAL, XK_STAGE_FRICTION, XK_STAGE_TANGENT = 1, 2, 4,
 XK_STAGE_ALL = 15
 XK_OUT_COMBINED, XK_OUT_SPLIT = 0, 1
 XK_WHICH_COMBINED, XK_WHICH_NORMAL, XK_WHICH_FRICTION = 0, 1, 2
+REC_COLS = {XK_OUT_COMBINED: 14, XK_OUT_SPLIT: 26}
 
 vp = C.c_void_p
 
@@ -53,9 +54,11 @@ class BPParams(C.Structure):
 
 
 class ContactPattern(C.Structure):
-    _fields_ = [("n_nodes", C.c_int32), ("n_members", C.c_int32), ("nnzb", C.c_int64), ("cap_members", C.c_int64),
-                ("cap_blocks", C.c_int64), ("inc_ptr", vp), ("inc", vp), ("row_ptr", vp), ("col", vp),
-                ("blk_row", vp)]
+    _fields_ = [("n_nodes", C.c_int32), ("n_members", C.c_int32), ("n_others", C.c_int32),
+                ("nnzb", C.c_int64), ("n_contrib", C.c_int64), ("cap_members", C.c_int64),
+                ("cap_others", C.c_int64), ("cap_blocks", C.c_int64)] + [
+        (n, vp) for n in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row",
+                          "blk_ptr", "contrib")]
 
 
 P = C.POINTER
@@ -69,12 +72,12 @@ SIGNATURES = {
     "xk_broadphase": [P(Mesh), vp, P(BPParams), vp, C.c_int64, i64p, i64p, i64p, vp],
     "xk_pairs_merge": [P(Mesh), P(Pairs), vp, C.c_int64, P(Pairs), vp],
     "xk_narrowphase": [P(Mesh), P(Pairs), vp, P(ContactParams), C.c_int, vp],
-    "xk_pair_eval": [P(Mesh), P(Pairs), vp, vp, P(ContactParams), C.c_int, C.c_int, C.c_int, vp, vp, C.c_int64, vp],
     "xk_contact_pattern_build": [P(Mesh), P(Pairs), P(ContactPattern), vp],
-    "xk_contact_gather_force": [P(Mesh), P(Pairs), P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, C.c_int64, vp,
-                                C.c_double, vp, vp, vp, vp, vp],
-    "xk_contact_gather_tangent": [P(Mesh), P(Pairs), P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, C.c_int64, vp,
-                                  vp],
+    "xk_pair_step": [P(Mesh), P(Pairs), P(ContactPattern), vp, vp, P(ContactParams), C.c_int, C.c_int, C.c_int, vp,
+                     vp],
+    "xk_contact_gather_force": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, vp, C.c_double, vp, vp, vp, vp,
+                                vp],
+    "xk_contact_gather_tangent": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, vp, vp],
     "xk_constraint_jacobian": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
     "xk_norm2": [vp, C.c_int64, vp, vp],
 }

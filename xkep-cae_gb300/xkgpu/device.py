@@ -36,7 +36,7 @@ def ptr(t: torch.Tensor | None) -> C.c_void_p:
 def as_dev(x, dtype, device) -> torch.Tensor:
     if isinstance(x, torch.Tensor):
         return x.to(device=device, dtype=dtype).contiguous()
-    return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype, device=device)
+    return torch.as_tensor(np.array(x, copy=True, order="C"), dtype=dtype, device=device)
 
 
 # ----------------------------------------------------------------------------- mesh
@@ -291,41 +291,60 @@ class DevicePairTable:
 
 
 class DeviceContactPattern:
-    """Incidence of the contributing pairs and the 3x3 block pattern of K_c."""
+    """Members / other pairs, member incidence, K_c block pattern and contributor lists."""
+
+    GROW = 1.25
 
     def __init__(self, mesh: DeviceMesh):
         self.mesh = mesh
-        dev = mesh.device
-        self.inc_ptr = torch.zeros(mesh.n_nodes + 1, dtype=torch.int32, device=dev)
-        self.row_ptr = torch.zeros(mesh.n_nodes + 1, dtype=torch.int32, device=dev)
-        self.inc = torch.zeros(4 * 1024, dtype=torch.int32, device=dev)
-        self.col = torch.zeros(1024, dtype=torch.int32, device=dev)
-        self.blk_row = torch.zeros(1024, dtype=torch.int32, device=dev)
         self.c = L.ContactPattern()
-        self._sync_struct()
+        self.inc_ptr = self._i32(mesh.n_nodes + 1)
+        self.row_ptr = self._i32(mesh.n_nodes + 1)
+        self._alloc_members(256)
+        self._alloc_others(256)
+        self._alloc_blocks(1024)
+        self.version = 0
+
+    def _i32(self, n):
+        return torch.zeros(max(int(n), 1), dtype=torch.int32, device=self.mesh.device)
+
+    def _alloc_members(self, cap):
+        cap = int(cap)
+        self.members, self.member_nodes = self._i32(cap), self._i32(4 * cap)
+        self.inc, self.contrib = self._i32(4 * cap), self._i32(16 * cap)
+        self.cap_members = cap
+
+    def _alloc_others(self, cap):
+        self.others = self._i32(cap)
+        self.cap_others = int(cap)
+
+    def _alloc_blocks(self, cap):
+        cap = int(cap)
+        self.col, self.blk_row, self.blk_ptr = self._i32(cap), self._i32(cap), self._i32(cap + 1)
+        self.cap_blocks = cap
 
     def _sync_struct(self):
         c = self.c
         c.n_nodes = self.mesh.n_nodes
-        c.cap_members = self.inc.numel() // 4
-        c.cap_blocks = self.col.numel()
-        c.inc_ptr, c.inc, c.row_ptr = ptr(self.inc_ptr), ptr(self.inc), ptr(self.row_ptr)
-        c.col, c.blk_row = ptr(self.col), ptr(self.blk_row)
+        c.cap_members, c.cap_others, c.cap_blocks = self.cap_members, self.cap_others, self.cap_blocks
+        for k in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row", "blk_ptr",
+                  "contrib"):
+            setattr(c, k, ptr(getattr(self, k)))
 
     def build(self, pairs: DevicePairTable, stream=None):
-        for _ in range(3):
+        for _ in range(4):
+            self._sync_struct()
             code = L.call("xk_contact_pattern_build", C.byref(self.mesh.c), C.byref(pairs.c), C.byref(self.c),
                           stream_handle(stream), allow=(L.XK_ERR_CAPACITY,))
             if code == L.XK_OK:
+                self.version += 1
                 return
-            dev = self.mesh.device
-            if self.c.n_members > self.inc.numel() // 4:
-                self.inc = torch.zeros(4 * int(self.c.n_members * 1.25 + 64), dtype=torch.int32, device=dev)
-            if self.c.nnzb > self.col.numel():
-                m = int(self.c.nnzb * 1.25 + 64)
-                self.col = torch.zeros(m, dtype=torch.int32, device=dev)
-                self.blk_row = torch.zeros(m, dtype=torch.int32, device=dev)
-            self._sync_struct()
+            if self.c.n_members > self.cap_members:
+                self._alloc_members(self.c.n_members * self.GROW + 64)
+            if self.c.n_others > self.cap_others:
+                self._alloc_others(self.c.n_others * self.GROW + 64)
+            if self.c.nnzb > self.cap_blocks:
+                self._alloc_blocks(self.c.nnzb * self.GROW + 64)
         raise RuntimeError("contact pattern capacity did not converge")
 
     @property

@@ -72,10 +72,9 @@ class AssemblyEngine:
     def _alloc_outputs(self):
         dev = self.device
         self.K_beam = torch.zeros(36 * max(self.beam.nnzb, 1), dtype=self.t_dtype, device=dev)
-        cap = self.pairs.cap
-        self.pv = torch.zeros(3 * cap, dtype=self.t_dtype, device=dev)
-        self.pB = torch.zeros(9 * cap, dtype=self.t_dtype, device=dev)
-        self.K_c = torch.zeros(9 * max(self.pattern.col.numel(), 1), dtype=self.t_dtype, device=dev)
+        self.rec = torch.zeros(L.REC_COLS[L.XK_OUT_COMBINED] * self.pattern.cap_members, dtype=self.t_dtype,
+                               device=dev)
+        self.K_c = torch.zeros(9 * max(self.pattern.cap_blocks, 1), dtype=self.t_dtype, device=dev)
         self.graph = None
 
     def set_precision(self, precision):
@@ -106,7 +105,8 @@ class AssemblyEngine:
         self.pairs, self._spare = self._spare, self.pairs
         L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), C.byref(self.cp), 1, s)
         self.pattern.build(self.pairs, stream)
-        if self.pv.numel() < 3 * self.pairs.cap or self.K_c.numel() < 9 * max(self.pattern.col.numel(), 1):
+        if (self.rec.numel() != L.REC_COLS[L.XK_OUT_COMBINED] * self.pattern.cap_members
+                or self.K_c.numel() < 9 * self.pattern.cap_blocks):
             self._alloc_outputs()
         self.graph = None
         self.stats = {"raw": int(n_raw.value), "prefilter": int(n_pre.value), "candidates": nc,
@@ -118,16 +118,15 @@ class AssemblyEngine:
                  fixed: torch.Tensor | None = None, stream=None, *, tangent: bool = True):
         s = stream_handle(stream)
         p = self.precision
-        stride = self.pairs.cap
-        L.call("xk_pair_eval", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), ptr(u_ref), C.byref(self.cp),
-               L.XK_STAGE_ALL, p, L.XK_OUT_COMBINED, ptr(self.pv), ptr(self.pB), stride, s)
+        pat = C.byref(self.pattern.c)
+        L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
+               C.byref(self.cp), L.XK_STAGE_ALL, p, L.XK_OUT_COMBINED, ptr(self.rec), s)
         self.beam.assemble(u, p, self.f_int, self.K_beam if tangent else None, stream)
-        L.call("xk_contact_gather_force", C.byref(self.mesh.c), C.byref(self.pairs.c), C.byref(self.pattern.c),
-               ptr(self.pv), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, stride, ptr(self.f_int), -1.0, ptr(f_ext),
-               ptr(fixed), ptr(self.R), ptr(self.norm2), s)
+        L.call("xk_contact_gather_force", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
+               ptr(self.f_int), -1.0, ptr(f_ext), ptr(fixed), ptr(self.R), ptr(self.norm2), s)
         if tangent and self.pattern.nnzb > 0:
-            L.call("xk_contact_gather_tangent", C.byref(self.mesh.c), C.byref(self.pairs.c), C.byref(self.pattern.c),
-                   ptr(self.pB), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, stride, ptr(self.K_c), s)
+            L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
+                   ptr(self.K_c), s)
         return self.R
 
     def capture(self, u, u_ref=None, f_ext=None, fixed=None):

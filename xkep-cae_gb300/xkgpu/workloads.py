@@ -77,6 +77,7 @@ CONFIGS = {
     "strand7": dict(n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el_per_pitch=16),
     "strand37": dict(n_wires=37, d=2.0, pitch=40.0, n_pitches=4, n_el_per_pitch=32),
     "strand91": dict(n_wires=91, d=2.0, pitch=40.0, n_pitches=4, n_el_per_pitch=32),
+    "strand397": dict(n_wires=wires_for_layers(11), d=0.5, pitch=20.0, n_pitches=4, n_el_per_pitch=24),
     "strand1027": dict(n_wires=wires_for_layers(18), d=0.5, pitch=20.0, n_pitches=4, n_el_per_pitch=24),
 }
 
