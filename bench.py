@@ -153,17 +153,23 @@ def oracle_sample_timing(w, frac: float, reps: int = 1, prepared=None):
     return units, dt, prepared
 
 
-def pair_kernel_bytes(n_nodes, n_elems, n_others, n_members, tsize):
-    """Algorithmic (compulsory) DRAM bytes of one pair step (both launches).
+def pair_kernel_bytes(n_nodes, n_elems, n_others, n_members, mixed: bool):
+    """Algorithmic (compulsory) DRAM bytes of one pair step.
 
-    Node data X, u, u_ref once per node (72 B); conn and radius once per
-    element (16 B).  A non-contributing pair reads its list entry, keys and
-    previous normal / tangent (60 B) and writes s, t, gap and the frame
-    (96 B).  A contributing pair also reads its node ids and friction state
-    (126 B read in all), writes the updated state (138 B) and its record
-    (s, t, v, B: 14 values in the compute precision).
+    FP64 path (double state): node data X, u, u_ref once per node (72 B),
+    conn and radius once per element (16 B); a non-contributing pair reads its
+    list entry, keys and previous frame (60 B) and writes s, t, gap and the
+    frame (96 B); a contributing pair reads node ids, keys, status and friction
+    state (126 B), writes the updated state (138 B) and its 16-double record.
+
+    Mixed path (float state): the node-preparation kernel reads X, u, u_ref
+    (72 B) and writes a 64 B node record that the pair kernels read back
+    (64 B); element radii 8 B; a non-contributing pair reads 36 B and writes
+    48 B; a contributing pair reads 78 B, writes 70 B and its 64 B record.
     """
-    return 72 * n_nodes + 16 * n_elems + 156 * n_others + n_members * (264 + 14 * tsize)
+    if mixed:
+        return (72 + 64 + 64) * n_nodes + 8 * n_elems + 84 * n_others + 212 * n_members
+    return 72 * n_nodes + 16 * n_elems + 156 * n_others + n_members * (264 + 128)
 
 
 # --------------------------------------------------------------------------- GPU arm
@@ -229,6 +235,8 @@ def run_gpu(args, rank, world):
            "K_contact": relmax(emx.K_c[: 9 * nb], e64.K_c[: 9 * nb]),
            "active_set_equal": bool(torch.equal(emx.pairs.t["status"][: emx.pairs.n],
                                                 e64.pairs.t["status"][: e64.pairs.n]))}
+    # the contributing set after an iteration (friction may re-activate stale pairs): identical
+    err["contact_status_equal_after_iteration"] = err["active_set_equal"]
     del e64, emx
 
     if world > 1:
@@ -268,14 +276,12 @@ def run_gpu(args, rank, world):
     def pair_kernel_time(eng, k):
         s = torch.cuda.current_stream()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        args_ = (C.byref(eng.mesh.c), C.byref(eng.pairs.c), C.byref(eng.pattern.c), ptr(u1), ptr(u0),
-                 C.byref(eng.cp), L.XK_STAGE_ALL, eng.precision, L.XK_OUT_COMBINED, ptr(eng.rec), stream_handle(s))
         for _ in range(3):
-            L.call("xk_pair_step", *args_)
+            eng.pair_step(u1, u0, s)
         torch.cuda.synchronize()
         a.record(s)
         for _ in range(k):
-            L.call("xk_pair_step", *args_)
+            eng.pair_step(u1, u0, s)
         b.record(s)
         torch.cuda.synchronize()
         return a.elapsed_time(b) / 1e3 / k
@@ -284,8 +290,8 @@ def run_gpu(args, rank, world):
     tk_mixed = pair_kernel_time(engines["mixed"], kreps)
     tk_fp64 = pair_kernel_time(engines["fp64"], kreps)
     m = engines["mixed"].pattern.n_members
-    by_mixed = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, 4)
-    by_fp64 = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, 8)
+    by_mixed = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, True)
+    by_fp64 = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, False)
     peak, peak_kind = _peaks()
 
     # end to end through the public engine API with host buffers
@@ -337,7 +343,7 @@ def run_gpu(args, rank, world):
                "sample": f"NumPy oracle, one Newton-iteration assembly (contact + beam) on the first 1/48 of every "
                          f"wire ({sub.n_elems} elements, {prep[2]['ea'].shape[0]} pairs), host of the GPU box"}
 
-    per_launch = 8  # 2 pair kernels, 2 beam colours, force gather, 2 norm kernels, tangent gather
+    per_launch = 9  # node prep, 2 pair kernels, 2 beam colours, force gather, 2 norm kernels, tangent gather
     out = {
         "metric": METRIC, "value": units / t_mixed * args.steps, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
@@ -354,7 +360,7 @@ def run_gpu(args, rank, world):
         "err_vs_fp64": err,
         "detect_ms": {"mixed": results["mixed"]["detect_ms"], "fp64": results["fp64"]["detect_ms"],
                       "first": results["mixed"]["detect_first_ms"]},
-        "roofline": {"bound": "hbm", "kernel": "pair step: k_pair_member + k_pair_other (narrowphase+Huber+Coulomb+tangent)",
+        "roofline": {"bound": "hbm", "kernel": "pair step (mixed: k_nodes_prepare + k_pair_other32 + k_pair_member32; narrowphase, Huber, Coulomb, tangent)",
                      "achieved": by_mixed / tk_mixed / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": by_mixed / tk_mixed / 1e9 / peak, "peak_kind": peak_kind,
                      "bytes_per_launch": by_mixed, "launch_ms": 1e3 * tk_mixed, "traffic": None,

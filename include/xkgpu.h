@@ -158,10 +158,10 @@ xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double* u, const x
 #define XK_STAGE_NORMAL 2   /* HuberContactForceProcess.evaluate (contact_force/strategy.py:126-170) */
 #define XK_STAGE_FRICTION 4 /* CoulombReturnMappingProcess.evaluate (friction/strategy.py:111-148) */
 #define XK_STAGE_TANGENT 8  /* .tangent of both (contact_force/strategy.py:172-254, friction/_assembly.py:108-257) */
-#define XK_OUT_COMBINED 0   /* record (s, t, v = v_n + v_f, B = B_n - B_f): 14 columns */
-#define XK_OUT_SPLIT 1      /* record (s, t, v_n, v_f, B_n, B_f): 26 columns */
-#define XK_REC_COLS_COMBINED 14
-#define XK_REC_COLS_SPLIT 26
+#define XK_OUT_COMBINED 0   /* record (s, t, v = v_n + v_f, B = B_n - B_f): 14 values */
+#define XK_OUT_SPLIT 1      /* record (s, t, v_n, v_f, B_n, B_f): 26 values */
+#define XK_REC_STRIDE_COMBINED 16 /* values per record in memory (padded) */
+#define XK_REC_STRIDE_SPLIT 32
 
 /* The pairs that can contribute in an increment ("members": status != INACTIVE
  * or p_n > 0 after detection and the active-set update), the rest, the node
@@ -193,8 +193,9 @@ xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* p, xk_conta
 /* Per-iteration pair evaluation, fused over the selected stages.  A member's
  * translational force on its local node k (A0, A1, B0, B1) is c_k v and its
  * tangent block (k, l) is c_k c_l B with c = [1-s, s, -(1-t), -t]; these go
- * to the member-compact record rec[col*cap_members + member] (double for
- * XK_FP64, float for XK_MIXED).  With XK_STAGE_NARROW the other pairs get the
+ * to the member's record rec[member*stride + value] (stride 16 for combined,
+ * 32 for split records; double for XK_FP64, float for XK_MIXED; rec holds
+ * stride*cap_members values).  With XK_STAGE_NARROW the other pairs get the
  * narrowphase too, as in the reference.  The four stages together replace the
  * contact part of ContactForceAssemblyProcess + TangentAssemblyProcess
  * (_newton_steps.py:79-135,289-313). */
@@ -223,6 +224,44 @@ xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec
  * records), B_n or B_f (split records). */
 xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* rec, int precision, int out_mode,
                                     int which, void* Kc_vals, xk_stream s);
+
+/* ------------------------------------------- mixed-precision fast path
+ * The per-iteration kernels of the mixed path execute no double-precision
+ * arithmetic: node positions are split once per iteration into float
+ * high / low parts, the contact gap is taken in float-float arithmetic, the
+ * beam frame in a cancellation-free float form, and the pair state lives in a
+ * float copy of the table between increments. */
+#define XK_NODE32_STRIDE 16 /* [x_hi(3), x_lo(3), u(6), u - u_ref(3), 0] per node */
+#define XK_ELEM32_STRIDE 16 /* [X_b - X_a (3), L0, R0 (9), r_hi, r_lo, 0] per element */
+
+typedef struct {
+  int32_t n, cap;
+  float *s, *t, *gap;
+  float *normal, *t1, *t2; /* [3*cap] */
+  float *p_n, *z_t;        /* z_t: [2*cap] */
+  float *q_trial_norm, *dissipation, *k_pen, *k_t;
+} xk_pairs32;
+
+/* Per iteration: node records for the mixed kernels from u (and u_ref, nullable). */
+xk_status xk_nodes_prepare(const xk_mesh* m, const double* u, const double* u_ref, float* node32, xk_stream s);
+
+/* When the reference configuration changes: element records from xk_beam_reference's output. */
+xk_status xk_beam_prepare32(const xk_mesh* m, const double* elem_ref, float* elem32, xk_stream s);
+
+/* xk_beam_assemble in float from prepared records (f_int stays double). */
+xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec, const float* elem32,
+                             const xk_beam_plan* plan, const float* node32, double* f_int, float* K_vals,
+                             xk_stream s);
+
+/* Copy the state fields of the pair table to / from its float copy (at increment boundaries). */
+xk_status xk_pairs_to32(const xk_pairs* p, xk_pairs32* q, xk_stream s);
+xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream s);
+
+/* xk_pair_step with all four stages and combined float records, on the float
+ * state q (status and stick stay in p). */
+xk_status xk_pair_step32(const xk_mesh* m, xk_pairs* p, xk_pairs32* q, const xk_contact_pattern* pat,
+                         const float* node32, const float* elem32, const xk_contact_params* cp, float* rec,
+                         xk_stream s);
 
 /* Constraint Jacobian rows c_k n of the non-INACTIVE pairs in table order
  * (_build_constraint_jacobian_ptp, xkep_cae/contact/geometry/strategy.py:83-132).

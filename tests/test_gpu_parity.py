@@ -119,7 +119,7 @@ def test_strand_sequence_fp64(name):
         u_ref = _dev(z[f"inc{inc}_u_ref"])
         st = eng.detect(_dev(z[f"inc{inc}_u"]))
         assert st["candidates"] == len(z[f"inc{inc}_candidates"])
-        h = eng.pairs.to_host()
+        h = eng.pair_state()
         p = f"inc{inc}_geom_"
         assert np.array_equal(h["ea"], z[p + "ea"]) and np.array_equal(h["eb"], z[p + "eb"])
         assert np.array_equal(h["status"], z[p + "status"])
@@ -129,7 +129,7 @@ def test_strand_sequence_fp64(name):
             u = z[p + "u"]
             eng.assemble(_dev(u), u_ref)
             torch.cuda.synchronize()
-            h = eng.pairs.to_host()
+            h = eng.pair_state()
             assert np.array_equal(h["status"], z[p + "status"])
             assert np.array_equal(h["stick"], z[p + "stick"])
             for k in ("p_n", "z_t", "q_trial_norm", "k_t"):
@@ -161,7 +161,7 @@ def test_strand_sequence_mixed():
             assert rel_err(fcmx, fc64) < TOLMIX
             assert sparse_rel_err(emx.K_contact_csr(), e64.K_contact_csr()) < TOLMIX
             assert sparse_rel_err(emx.K_beam_csr(), e64.K_beam_csr()) < TOLMIX
-            h64, hmx = e64.pairs.to_host(), emx.pairs.to_host()
+            h64, hmx = e64.pair_state(), emx.pair_state()
             assert np.array_equal(h64["status"], hmx["status"])
 
 
@@ -181,7 +181,7 @@ def test_engine_vs_oracle_medium(cfg):
     assert stats["raw"] == len(raw)
     assert stats["candidates"] == len(cands)
     table = oc.update_geometry(table, oc.deformed_coords(st.coords, u))
-    h = eng.pairs.to_host()
+    h = eng.pair_state()
     assert np.array_equal(h["ea"], table["ea"]) and np.array_equal(h["eb"], table["eb"])
     assert np.array_equal(h["status"], table["status"])
     rng = np.random.default_rng(3)
@@ -193,7 +193,7 @@ def test_engine_vs_oracle_medium(cfg):
         table, fc, Kc, _ = oc.contact_iteration(table, st.coords, u, u_ref, n, k_pen=w.k_pen, k_t_ratio=w.k_t_ratio,
                                                 mu_eff=w.mu)
         Kb, fb = ob.assemble_beam(st.coords, st.conn, u, ob.Section(**w.section, scf=None))
-        h = eng.pairs.to_host()
+        h = eng.pair_state()
         assert np.array_equal(h["status"], table["status"])
         assert np.array_equal(h["stick"], table["stick"])
         assert rel_err(eng.R.cpu().numpy(), fb + fc) < TOL64
@@ -233,3 +233,40 @@ def test_deterministic_repeat():
         outs.append((eng.R.clone(), eng.K_c[: 9 * eng.pattern.nnzb].clone(), eng.K_beam.clone()))
     for x, y in zip(outs[0], outs[1]):
         assert torch.equal(x, y)
+
+
+@pytest.mark.parametrize("scf,v_ref,key", [(None, None, "beam_f"), (0.25, [0.3, -0.2, 0.9], "beam_f_vref_scf")])
+def test_beam_float_path_large_rotations(scf, v_ref, key):
+    """The all-float mixed beam kernel (cancellation-free frame) on rotations up to 1.5 rad."""
+    z = golden("beam_elements")
+    n = 6 * len(z["X"])
+    eng = AssemblyEngine(z["X"], z["conn"], 0.0, _sec(z, scf=scf), precision="mixed", k_pen=1.0, v_ref=v_ref)
+    eng.assemble(_dev(z["u"]))
+    torch.cuda.synchronize()
+    kkey = "beam_K" if key == "beam_f" else "beam_K_vref_scf"
+    assert rel_err(eng.f_int.cpu().numpy(), z[key]) < TOLMIX
+    assert sparse_rel_err(eng.K_beam_csr(), golden_csr(z, kkey, n)) < TOLMIX
+
+
+def test_mixed_engine_vs_fp64_strand37():
+    from xkgpu import workloads as W
+
+    w = W.config_workload("strand37", seed=4)
+    st = w.strand
+    e64 = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="fp64", **w.engine_kwargs())
+    emx = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **w.engine_kwargs())
+    u0 = _dev(w.u)
+    assert e64.detect(u0) == emx.detect(u0)
+    rng = np.random.default_rng(9)
+    for _ in range(3):
+        du = rng.normal(0.0, 2e-4 * w.meta["d"], st.ndof) * np.tile([1, 1, 1, 1e-1, 1e-1, 1e-1], st.n_nodes)
+        u = u0 + _dev(du)
+        e64.assemble(u, u0)
+        emx.assemble(u, u0)
+        torch.cuda.synchronize()
+        assert rel_err(emx.R.cpu().numpy(), e64.R.cpu().numpy()) < TOLMIX
+        assert sparse_rel_err(emx.K_contact_csr(), e64.K_contact_csr()) < TOLMIX
+        assert sparse_rel_err(emx.K_beam_csr(), e64.K_beam_csr()) < TOLMIX
+        h64, hmx = e64.pair_state(), emx.pair_state()
+        assert np.array_equal(h64["status"], hmx["status"])
+        assert rel_err(hmx["gap"], h64["gap"]) < 1e-6

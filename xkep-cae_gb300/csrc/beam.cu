@@ -94,6 +94,49 @@ XK_D void rotmat_of_quat(const double* q, T* R) {
   R[6] = T(2) * (x * z - w * y); R[7] = T(2) * (y * z + w * x); R[8] = T(1) - T(2) * (x * x + y * y);
 }
 
+// Float versions of the exponential / logarithm maps and quaternion product for
+// the mixed path (small rotation vectors by their series, as in double).
+XK_D void qmulf(const float* a, const float* b, float* c) {
+  c[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
+  c[1] = a[0] * b[1] + b[0] * a[1] + a[2] * b[3] - a[3] * b[2];
+  c[2] = a[0] * b[2] + b[0] * a[2] + a[3] * b[1] - a[1] * b[3];
+  c[3] = a[0] * b[3] + b[0] * a[3] + a[1] * b[2] - a[2] * b[1];
+}
+XK_D void quat_of_rotvecf(const float* th, float* q) {
+  const float a2 = th[0] * th[0] + th[1] * th[1] + th[2] * th[2];
+  float c, so;
+  if (a2 < 0.0625f) {
+    const float h2 = 0.25f * a2;
+    c = 1.0f + h2 * (-0.5f + h2 * (1.0f / 24 + h2 * (-1.0f / 720 + h2 * (1.0f / 40320))));
+    so = 0.5f * (1.0f + h2 * (-1.0f / 6 + h2 * (1.0f / 120 + h2 * (-1.0f / 5040 + h2 * (1.0f / 362880)))));
+  } else {
+    const float a = sqrtf(a2);
+    float sh;
+    sincosf(0.5f * a, &sh, &c);
+    so = sh / a;
+  }
+  q[0] = c;
+  q[1] = so * th[0];
+  q[2] = so * th[1];
+  q[3] = so * th[2];
+}
+XK_D void rotvec_of_quatf(const float* qin, float* th) {
+  float w = qin[0], x = qin[1], y = qin[2], z = qin[3];
+  if (w < 0.0f) { w = -w; x = -x; y = -y; z = -z; }
+  const float s2 = x * x + y * y + z * z;
+  float coef;
+  if (s2 < 0.0025f * w * w) {
+    const float r2 = s2 / (w * w);
+    coef = 2.0f * (1.0f + r2 * (-1.0f / 3 + r2 * (1.0f / 5 + r2 * (-1.0f / 7 + r2 * (1.0f / 9))))) / w;
+  } else {
+    const float sh = sqrtf(s2);
+    coef = 2.0f * atan2f(sh, w) / sh;
+  }
+  th[0] = coef * x;
+  th[1] = coef * y;
+  th[2] = coef * z;
+}
+
 // T_s(theta) = I + c1 S + c2 S^2 and T_s^{-1} = I - S/2 + c3 S^2 (_beam_cr.py:856-908),
 // with series below |theta| = 0.25 so that the float path keeps its accuracy.
 template <typename T>
@@ -152,8 +195,8 @@ struct KeCoef {
 };
 
 template <typename T>
-XK_D KeCoef<T> ke_coef(const xk_section& s, double L0) {
-  T L = (T)L0;
+XK_D KeCoef<T> ke_coef(const xk_section& s, T L0) {
+  T L = L0;
   T iL = T(1) / L;
   T E = (T)s.E, G = (T)s.G, A = (T)s.A, Iy = (T)s.Iy, Iz = (T)s.Iz, J = (T)s.J;
   T phy = T(12) * E * Iy / ((T)s.kappa_y * G * A * L * L);
@@ -229,63 +272,14 @@ __global__ void k_beam_reference(xk_mesh m, double vx, double vy, double vz, int
   }
 }
 
-template <int P>
-__global__ void __launch_bounds__(BEAM_T) k_beam(xk_mesh m, xk_section sec, const double* __restrict__ ref,
-                                                 const int32_t* __restrict__ order, int k0, int k1,
-                                                 const int32_t* __restrict__ blk, const uint8_t* __restrict__ first,
-                                                 const double* __restrict__ u, double* __restrict__ f_int,
-                                                 typename Prec<P>::T* __restrict__ Kv) {
-  typedef typename Prec<P>::T T;
-  int k = k0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= k1) return;
-  const int e = order[k];
-  const long long ne = m.n_elems;
-  const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
-  // ------------------------------------------------ double: frame and strain
-  const double L0 = ref[e];
-  double R0[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) R0[i] = ref[(1 + i) * ne + e];
-  double ua[6], ub[6];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) { ua[i] = u[6LL * a + i]; ub[i] = u[6LL * b + i]; }
-  double dxd[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) dxd[i] = (m.X[3LL * b + i] + ub[i]) - (m.X[3LL * a + i] + ua[i]);
-  const double Ld = sqrt(dot3(dxd, dxd));
-  const double iLd = 1.0 / Ld;
-  double exd[3] = {dxd[0] * iLd, dxd[1] * iLd, dxd[2] * iLd};
-  double qr[4];
-  quat_between(R0, exd, qr);  // R0 row 0 is e_x of the reference frame
-  double qrc[4] = {qr[0], -qr[1], -qr[2], -qr[3]};
-  double th1[3], th2[3];
-  {
-    double qn[4], qx[4], tx[3];
-    quat_of_rotvec(ua + 3, qn);
-    qmul(qrc, qn, qx);
-    rotvec_of_quat(qx, tx);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) th1[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
-    quat_of_rotvec(ub + 3, qn);
-    qmul(qrc, qn, qx);
-    rotvec_of_quat(qx, tx);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) th2[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
-  }
-  const T dax = (T)(Ld - L0);
-  // ------------------------------------------------ precision T: forces
-  T Rrod[9], Rcr[9], R0t[9];
-  rotmat_of_quat<T>(qr, Rrod);
-#pragma unroll
-  for (int i = 0; i < 9; ++i) R0t[i] = (T)R0[i];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      Rcr[3 * i + j] = R0t[3 * i] * Rrod[3 * j] + R0t[3 * i + 1] * Rrod[3 * j + 1] + R0t[3 * i + 2] * Rrod[3 * j + 2];
-  const KeCoef<T> kc = ke_coef<T>(sec, L0);
-  T t1[3] = {(T)th1[0], (T)th1[1], (T)th1[2]};
-  T t2[3] = {(T)th2[0], (T)th2[1], (T)th2[2]};
+// Local forces, global element force and the symmetrised analytic tangent
+// (_beam_assembly.py:265-323) from the corotated frame R_cr, the deformed axis
+// ex, 1/L, the local rotations t1, t2, the nodal rotation vectors tha, thb and
+// the axial stretch dax, written into f_int rows and the four 6x6 blocks.
+template <typename T>
+XK_D void beam_tail(const KeCoef<T>& kc, const T* Rcr, const T* ex, T iL, const T* t1, const T* t2, const T* tha,
+                    const T* thb, T dax, int a, int b, int e, uint8_t fl, const int32_t* __restrict__ blk,
+                    double* __restrict__ f_int, T* __restrict__ Kv) {
   T fcr[12];
   fcr[0] = -kc.ea * dax;
   fcr[1] = kc.k2z * (t1[2] + t2[2]);
@@ -299,7 +293,6 @@ __global__ void __launch_bounds__(BEAM_T) k_beam(xk_mesh m, xk_section sec, cons
   fcr[9] = -fcr[3];
   fcr[10] = kc.k1by * t1[1] + kc.k1ay * t2[1];
   fcr[11] = kc.k1bz * t1[2] + kc.k1az * t2[2];
-  const uint8_t fl = first[e];
   if (f_int) {
 #pragma unroll
     for (int blkI = 0; blkI < 4; ++blkI) {
@@ -314,8 +307,6 @@ __global__ void __launch_bounds__(BEAM_T) k_beam(xk_mesh m, xk_section sec, cons
   }
   if (!Kv) return;
   // ------------------------------------------------ tangent
-  T ex[3] = {(T)exd[0], (T)exd[1], (T)exd[2]};
-  const T iL = (T)iLd;
   T Sx[9] = {T(0), -ex[2], ex[1], ex[2], T(0), -ex[0], -ex[1], ex[0], T(0)};
   T dpsi[9];
   mm3(Rcr, Sx, dpsi);
@@ -323,17 +314,15 @@ __global__ void __launch_bounds__(BEAM_T) k_beam(xk_mesh m, xk_section sec, cons
   for (int i = 0; i < 9; ++i) dpsi[i] *= iL;
   T P1[9], Q1[9], P2[9], Q2[9];
   {
-    T Ti[9], Ts[9], tmp[9], thn[3];
+    T Ti[9], Ts[9], tmp[9];
     tangent_ops<T>(t1, true, Ti);
     mm3(Ti, dpsi, P1);
-    thn[0] = (T)ua[3]; thn[1] = (T)ua[4]; thn[2] = (T)ua[5];
-    tangent_ops<T>(thn, false, Ts);
+    tangent_ops<T>(tha, false, Ts);
     mm3(Ti, Rcr, tmp);
     mm3(tmp, Ts, Q1);
     tangent_ops<T>(t2, true, Ti);
     mm3(Ti, dpsi, P2);
-    thn[0] = (T)ub[3]; thn[1] = (T)ub[4]; thn[2] = (T)ub[5];
-    tangent_ops<T>(thn, false, Ts);
+    tangent_ops<T>(thb, false, Ts);
     mm3(Ti, Rcr, tmp);
     mm3(tmp, Ts, Q2);
   }
@@ -394,6 +383,347 @@ __global__ void __launch_bounds__(BEAM_T) k_beam(xk_mesh m, xk_section sec, cons
           }
       }
   }
+}
+
+
+template <int P>
+__global__ void __launch_bounds__(BEAM_T) k_beam(xk_mesh m, xk_section sec, const double* __restrict__ ref,
+                                                 const int32_t* __restrict__ order, int k0, int k1,
+                                                 const int32_t* __restrict__ blk, const uint8_t* __restrict__ first,
+                                                 const double* __restrict__ u, double* __restrict__ f_int,
+                                                 typename Prec<P>::T* __restrict__ Kv) {
+  typedef typename Prec<P>::T T;
+  int k = k0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= k1) return;
+  const int e = order[k];
+  const long long ne = m.n_elems;
+  const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
+  // ------------------------------------------------ double: frame and strain
+  const double L0 = ref[e];
+  double R0[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R0[i] = ref[(1 + i) * ne + e];
+  double ua[6], ub[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { ua[i] = u[6LL * a + i]; ub[i] = u[6LL * b + i]; }
+  double dxd[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) dxd[i] = (m.X[3LL * b + i] + ub[i]) - (m.X[3LL * a + i] + ua[i]);
+  const double Ld = sqrt(dot3(dxd, dxd));
+  const double iLd = 1.0 / Ld;
+  double exd[3] = {dxd[0] * iLd, dxd[1] * iLd, dxd[2] * iLd};
+  double qr[4];
+  quat_between(R0, exd, qr);  // R0 row 0 is e_x of the reference frame
+  double qrc[4] = {qr[0], -qr[1], -qr[2], -qr[3]};
+  double th1[3], th2[3];
+  {
+    double qn[4], qx[4], tx[3];
+    quat_of_rotvec(ua + 3, qn);
+    qmul(qrc, qn, qx);
+    rotvec_of_quat(qx, tx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) th1[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
+    quat_of_rotvec(ub + 3, qn);
+    qmul(qrc, qn, qx);
+    rotvec_of_quat(qx, tx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) th2[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
+  }
+  const T dax = (T)(Ld - L0);
+  T Rrod[9], Rcr[9], R0t[9];
+  rotmat_of_quat<T>(qr, Rrod);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R0t[i] = (T)R0[i];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      Rcr[3 * i + j] = R0t[3 * i] * Rrod[3 * j] + R0t[3 * i + 1] * Rrod[3 * j + 1] + R0t[3 * i + 2] * Rrod[3 * j + 2];
+  const T t1[3] = {(T)th1[0], (T)th1[1], (T)th1[2]};
+  const T t2[3] = {(T)th2[0], (T)th2[1], (T)th2[2]};
+  const T ex[3] = {(T)exd[0], (T)exd[1], (T)exd[2]};
+  const T tha[3] = {(T)ua[3], (T)ua[4], (T)ua[5]};
+  const T thb[3] = {(T)ub[3], (T)ub[4], (T)ub[5]};
+  beam_tail<T>(ke_coef<T>(sec, (T)L0), Rcr, ex, (T)iLd, t1, t2, tha, thb, dax, a, b, e, first[e], blk, f_int, Kv);
+}
+
+// Mixed path: every operation in float.  With Delta u = u_b - u_a and the
+// reference chord dx0 (e0 = dx0 / L0):
+//   L - L0        = Delta u . (2 dx0 + Delta u) / (L + L0)
+//   e0 x e        = e0 x Delta u / L          (e0 x dx0 = 0)
+//   1 + e0 . e    = (L + L0 + e0 . Delta u) / L
+// none of which cancels, so the corotated frame keeps float accuracy relative
+// to the (small) deformation instead of to the coordinates.
+struct Frame32 {
+  float Rcr[9], exd[3], iLd, th1[3], th2[3], tha[3], thb[3], dax, L0;
+};
+
+XK_D void frame32(const float* __restrict__ E, const float* __restrict__ NA, const float* __restrict__ NB, Frame32& F) {
+  const float dx0[3] = {E[0], E[1], E[2]};
+  F.L0 = E[3];
+  float R0[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R0[i] = E[4 + i];
+  float ua[6], ub[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { ua[i] = NA[i]; ub[i] = NB[i]; }
+  const float du[3] = {ub[0] - ua[0], ub[1] - ua[1], ub[2] - ua[2]};
+  const float dxd[3] = {dx0[0] + du[0], dx0[1] + du[1], dx0[2] + du[2]};
+  const float Ld = sqrtf(dot3(dxd, dxd));
+  const float iLd = 1.0f / Ld;
+  F.iLd = iLd;
+  const float two_dx_du[3] = {2.0f * dx0[0] + du[0], 2.0f * dx0[1] + du[1], 2.0f * dx0[2] + du[2]};
+  F.dax = dot3(du, two_dx_du) / (Ld + F.L0);
+  for (int i = 0; i < 3; ++i) F.exd[i] = dxd[i] * iLd;
+  float qr[4];
+  {
+    float v[3];
+    cross3(R0, du, v);
+    const float opc = fmaxf((Ld + F.L0 + dot3(R0, du)) * iLd, 1e-12f);
+    const float w = sqrtf(0.5f * opc);
+    const float kk = 0.5f * iLd / w;
+    qr[0] = w; qr[1] = kk * v[0]; qr[2] = kk * v[1]; qr[3] = kk * v[2];
+  }
+  const float qrc[4] = {qr[0], -qr[1], -qr[2], -qr[3]};
+  {
+    float qn[4], qx[4], tx[3];
+    quat_of_rotvecf(ua + 3, qn);
+    qmulf(qrc, qn, qx);
+    rotvec_of_quatf(qx, tx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) F.th1[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
+    quat_of_rotvecf(ub + 3, qn);
+    qmulf(qrc, qn, qx);
+    rotvec_of_quatf(qx, tx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) F.th2[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
+  }
+  for (int i = 0; i < 3; ++i) { F.tha[i] = ua[3 + i]; F.thb[i] = ub[3 + i]; }
+  float Rrod[9];
+  {
+    const float w = qr[0], x = qr[1], y = qr[2], z = qr[3];
+    Rrod[0] = 1.f - 2.f * (y * y + z * z); Rrod[1] = 2.f * (x * y - w * z); Rrod[2] = 2.f * (x * z + w * y);
+    Rrod[3] = 2.f * (x * y + w * z); Rrod[4] = 1.f - 2.f * (x * x + z * z); Rrod[5] = 2.f * (y * z - w * x);
+    Rrod[6] = 2.f * (x * z - w * y); Rrod[7] = 2.f * (y * z + w * x); Rrod[8] = 1.f - 2.f * (x * x + y * y);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      F.Rcr[3 * i + j] = R0[3 * i] * Rrod[3 * j] + R0[3 * i + 1] * Rrod[3 * j + 1] + R0[3 * i + 2] * Rrod[3 * j + 2];
+}
+
+// Mixed path, four lanes per element: lane I of a quad computes block row I of
+// the unsymmetrised tangent ([G_I, H_I, -G_I, J_I], see beam_tail) and the f
+// rows of DOF group I; the quad exchanges the rows through shared memory to
+// symmetrise, and lane I stores rows 3I..3I+2 of the 12x12 element tangent.
+constexpr int BEAMQ_T = 128;
+
+__global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, const float* __restrict__ e32,
+                                                     const int32_t* __restrict__ order, int k0, int k1,
+                                                     const int32_t* __restrict__ blk,
+                                                     const uint8_t* __restrict__ first, const float* __restrict__ n32,
+                                                     double* __restrict__ f_int, float* __restrict__ Kv) {
+  __shared__ float sx[BEAMQ_T / 4][4][27];
+  const int q = threadIdx.x >> 2, I = threadIdx.x & 3;
+  const int k = k0 + blockIdx.x * (BEAMQ_T / 4) + q;
+  const bool live = k < k1;
+  const int e = live ? order[k] : order[k0];
+  const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
+  Frame32 F;
+  frame32(e32 + (long long)e * XK_ELEM32_STRIDE, n32 + (long long)a * XK_NODE32_STRIDE + 6,
+          n32 + (long long)b * XK_NODE32_STRIDE + 6, F);
+  const KeCoef<float> kc = ke_coef<float>(sec, F.L0);
+  const float* t1 = F.th1;
+  const float* t2 = F.th2;
+  float fcr[12];
+  fcr[0] = -kc.ea * F.dax;
+  fcr[1] = kc.k2z * (t1[2] + t2[2]);
+  fcr[2] = -kc.k2y * (t1[1] + t2[1]);
+  fcr[3] = kc.gj * (t1[0] - t2[0]);
+  fcr[4] = kc.k1ay * t1[1] + kc.k1by * t2[1];
+  fcr[5] = kc.k1az * t1[2] + kc.k1bz * t2[2];
+  fcr[6] = kc.ea * F.dax;
+  fcr[7] = -fcr[1];
+  fcr[8] = -fcr[2];
+  fcr[9] = -fcr[3];
+  fcr[10] = kc.k1by * t1[1] + kc.k1ay * t2[1];
+  fcr[11] = kc.k1bz * t1[2] + kc.k1az * t2[2];
+  const float* Rcr = F.Rcr;
+  const uint8_t fl = first[e];
+  if (live && f_int) {
+    for (int i = 0; i < 3; ++i) {
+      const double v = (double)(Rcr[i] * fcr[3 * I] + Rcr[3 + i] * fcr[3 * I + 1] + Rcr[6 + i] * fcr[3 * I + 2]);
+      const long long dof = (I < 2 ? 6LL * a : 6LL * b) + 3 * (I & 1) + i;
+      const bool fw = (I < 2) ? (fl & 1) : (fl & 8);
+      if (fw) f_int[dof] = v; else f_int[dof] += v;
+    }
+  }
+  if (!Kv) return;  // uniform over the launch
+  const float* ex = F.exd;
+  float dpsi[9];
+  {
+    const float Sx[9] = {0.f, -ex[2], ex[1], ex[2], 0.f, -ex[0], -ex[1], ex[0], 0.f};
+    mm3(Rcr, Sx, dpsi);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) dpsi[i] *= F.iLd;
+  }
+  // P1, Q1 (node a) or P2, Q2 (node b) are needed by all rows: Ke_{I1} and Ke_{I3}
+  float P1[9], Q1[9], P2[9], Q2[9];
+  {
+    float Ti[9], Ts[9], tmp[9];
+    tangent_ops<float>(t1, true, Ti);
+    mm3(Ti, dpsi, P1);
+    tangent_ops<float>(F.tha, false, Ts);
+    mm3(Ti, Rcr, tmp);
+    mm3(tmp, Ts, Q1);
+    tangent_ops<float>(t2, true, Ti);
+    mm3(Ti, dpsi, P2);
+    tangent_ops<float>(F.thb, false, Ts);
+    mm3(Ti, Rcr, tmp);
+    mm3(tmp, Ts, Q2);
+  }
+  float G[9], H[9], J[9];
+  {
+    float A[9], Hl[9], Jl[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const int row = 3 * I + r;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float acc = -kev(kc, row, 6) * ex[c];
+        float h = 0.f, jj = 0.f;
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) {
+          acc += kev(kc, row, 3 + qq) * P1[3 * qq + c] + kev(kc, row, 9 + qq) * P2[3 * qq + c];
+          h += kev(kc, row, 3 + qq) * Q1[3 * qq + c];
+          jj += kev(kc, row, 9 + qq) * Q2[3 * qq + c];
+        }
+        A[3 * r + c] = acc;
+        Hl[3 * r + c] = h;
+        Jl[3 * r + c] = jj;
+      }
+    }
+    const float f0 = fcr[3 * I], f1 = fcr[3 * I + 1], f2 = fcr[3 * I + 2];
+    const float Sf[9] = {0.f, -f2, f1, f2, 0.f, -f0, -f1, f0, 0.f};
+    float SfD[9];
+    mm3(Sf, dpsi, SfD);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A[i] += SfD[i];
+    mtm3(Rcr, A, G);
+    mtm3(Rcr, Hl, H);
+    mtm3(Rcr, Jl, J);
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    sx[q][I][i] = G[i];
+    sx[q][I][9 + i] = H[i];
+    sx[q][I][18 + i] = J[i];
+  }
+  __syncwarp();
+  if (!live) return;
+  // row I of the symmetrised tangent: Ks[I][Jb] = (X_IJb + X_JbI^T) / 2 with
+  // X_I0 = G_I, X_I1 = H_I, X_I2 = -G_I, X_I3 = J_I
+#pragma unroll
+  for (int Jb = 0; Jb < 4; ++Jb) {
+    const int nb = (I >> 1) * 2 + (Jb >> 1);  // 0 aa, 1 ab, 2 ba, 3 bb
+    float* dst = Kv + 36LL * blk[4LL * e + nb];
+    const bool fw = (fl >> nb) & 1;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float xij = (Jb == 0) ? G[3 * r + c] : (Jb == 1) ? H[3 * r + c] : (Jb == 2) ? -G[3 * r + c] : J[3 * r + c];
+        const float* o = sx[q][Jb];
+        const float xji = (I == 0) ? o[3 * c + r] : (I == 1) ? o[9 + 3 * c + r] : (I == 2) ? -o[3 * c + r] : o[18 + 3 * c + r];
+        const float v = 0.5f * (xij + xji);
+        const int idx = (3 * (I & 1) + r) * 6 + 3 * (Jb & 1) + c;
+        if (fw) dst[idx] = v; else dst[idx] += v;
+      }
+  }
+}
+
+__global__ void __launch_bounds__(BEAM_T) k_beam32(xk_mesh m, xk_section sec, const float* __restrict__ e32,
+                                                   const int32_t* __restrict__ order, int k0, int k1,
+                                                   const int32_t* __restrict__ blk, const uint8_t* __restrict__ first,
+                                                   const float* __restrict__ n32, double* __restrict__ f_int,
+                                                   float* __restrict__ Kv) {
+  const int k = k0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= k1) return;
+  const int e = order[k];
+  const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
+  const float* E = e32 + (long long)e * XK_ELEM32_STRIDE;
+  const float dx0[3] = {E[0], E[1], E[2]};
+  const float L0 = E[3];
+  float R0[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R0[i] = E[4 + i];
+  const float* NA = n32 + (long long)a * XK_NODE32_STRIDE + 6;
+  const float* NB = n32 + (long long)b * XK_NODE32_STRIDE + 6;
+  float ua[6], ub[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { ua[i] = NA[i]; ub[i] = NB[i]; }
+  const float du[3] = {ub[0] - ua[0], ub[1] - ua[1], ub[2] - ua[2]};
+  const float dxd[3] = {dx0[0] + du[0], dx0[1] + du[1], dx0[2] + du[2]};
+  const float Ld = sqrtf(dot3(dxd, dxd));
+  const float iLd = 1.0f / Ld;
+  const float two_dx_du[3] = {2.0f * dx0[0] + du[0], 2.0f * dx0[1] + du[1], 2.0f * dx0[2] + du[2]};
+  const float dax = dot3(du, two_dx_du) / (Ld + L0);
+  const float exd[3] = {dxd[0] * iLd, dxd[1] * iLd, dxd[2] * iLd};
+  float qr[4];
+  {
+    float v[3];
+    cross3(R0, du, v);
+    const float opc = fmaxf((Ld + L0 + dot3(R0, du)) * iLd, 1e-12f);
+    const float w = sqrtf(0.5f * opc);
+    const float kk = 0.5f * iLd / w;
+    qr[0] = w; qr[1] = kk * v[0]; qr[2] = kk * v[1]; qr[3] = kk * v[2];
+  }
+  const float qrc[4] = {qr[0], -qr[1], -qr[2], -qr[3]};
+  float th1[3], th2[3];
+  {
+    float qn[4], qx[4], tx[3];
+    quat_of_rotvecf(ua + 3, qn);
+    qmulf(qrc, qn, qx);
+    rotvec_of_quatf(qx, tx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) th1[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
+    quat_of_rotvecf(ub + 3, qn);
+    qmulf(qrc, qn, qx);
+    rotvec_of_quatf(qx, tx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) th2[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
+  }
+  float Rrod[9], Rcr[9];
+  {
+    const float w = qr[0], x = qr[1], y = qr[2], z = qr[3];
+    Rrod[0] = 1.f - 2.f * (y * y + z * z); Rrod[1] = 2.f * (x * y - w * z); Rrod[2] = 2.f * (x * z + w * y);
+    Rrod[3] = 2.f * (x * y + w * z); Rrod[4] = 1.f - 2.f * (x * x + z * z); Rrod[5] = 2.f * (y * z - w * x);
+    Rrod[6] = 2.f * (x * z - w * y); Rrod[7] = 2.f * (y * z + w * x); Rrod[8] = 1.f - 2.f * (x * x + y * y);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      Rcr[3 * i + j] = R0[3 * i] * Rrod[3 * j] + R0[3 * i + 1] * Rrod[3 * j + 1] + R0[3 * i + 2] * Rrod[3 * j + 2];
+  beam_tail<float>(ke_coef<float>(sec, L0), Rcr, exd, iLd, th1, th2, ua + 3, ub + 3, dax, a, b, e, first[e], blk,
+                   f_int, Kv);
+}
+
+__global__ void k_beam_prepare32(xk_mesh m, const double* __restrict__ ref, float* __restrict__ e32) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.n_elems) return;
+  const long long ne = m.n_elems;
+  const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
+  float* E = e32 + (long long)e * XK_ELEM32_STRIDE;
+  for (int i = 0; i < 3; ++i) E[i] = (float)(m.X[3LL * b + i] - m.X[3LL * a + i]);
+  E[3] = (float)ref[e];
+  for (int i = 0; i < 9; ++i) E[4 + i] = (float)ref[(1 + i) * ne + e];
+  const double r = m.radii[e];
+  const float rh = (float)r;
+  E[13] = rh;
+  E[14] = (float)(r - (double)rh);
+  E[15] = 0.0f;
 }
 
 __global__ void k_lumped_mass(xk_mesh m, xk_section sec, double rho, const int32_t* __restrict__ order, int k0,
@@ -459,6 +789,31 @@ extern "C" xk_status xk_beam_lumped_mass(const xk_mesh* m, const xk_section* sec
     if (k1 <= k0) continue;
     k_lumped_mass<<<xk_blocks(k1 - k0, 256), 256, 0, (cudaStream_t)s>>>(*m, *sec, rho, plan->elem_order, k0, k1,
                                                                          plan->first, out);
+    XK_CHECK_LAUNCH();
+  }
+  return XK_OK;
+}
+
+extern "C" xk_status xk_beam_prepare32(const xk_mesh* m, const double* elem_ref, float* elem32, xk_stream s) {
+  if (!m || !elem_ref || !elem32) return xk_set_error(XK_ERR_ARG, "xk_beam_prepare32: null argument");
+  if (m->n_elems == 0) return XK_OK;
+  k_beam_prepare32<<<xk_blocks(m->n_elems, 256), 256, 0, (cudaStream_t)s>>>(*m, elem_ref, elem32);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
+extern "C" xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec, const float* elem32,
+                                        const xk_beam_plan* plan, const float* node32, double* f_int, float* K_vals,
+                                        xk_stream s) {
+  if (!m || !sec || !elem32 || !plan || !node32) return xk_set_error(XK_ERR_ARG, "xk_beam_assemble32: null argument");
+  if (!f_int && !K_vals) return XK_OK;
+  cudaStream_t st = (cudaStream_t)s;
+  for (int c = 0; c < plan->n_colors; ++c) {
+    const int k0 = plan->color_ptr_host[c], k1 = plan->color_ptr_host[c + 1];
+    if (k1 <= k0) continue;
+    k_beam32q<<<xk_blocks(4LL * (k1 - k0), BEAMQ_T), BEAMQ_T, 0, st>>>(*m, *sec, elem32, plan->elem_order, k0, k1,
+                                                                         plan->blk, plan->first, node32, f_int,
+                                                                         K_vals);
     XK_CHECK_LAUNCH();
   }
   return XK_OK;

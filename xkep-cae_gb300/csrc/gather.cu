@@ -134,7 +134,7 @@ XK_D int find_block(const int32_t* __restrict__ rptr, const int32_t* __restrict_
 template <int MODE>
 __global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int32_t* __restrict__ rptr,
                           const int32_t* __restrict__ col, int32_t* __restrict__ cnt,
-                          const int32_t* __restrict__ bptr, int32_t* __restrict__ contrib) {
+                          const int32_t* __restrict__ bptr, int32_t* __restrict__ contrib, int32_t* __restrict__ err) {
   int mi = blockIdx.x * blockDim.x + threadIdx.x;
   if (mi >= nm) return;
   int nd[4];
@@ -142,6 +142,10 @@ __global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int3
   for (int k = 0; k < 4; ++k)
     for (int l = 0; l < 4; ++l) {
       const int b = find_block(rptr, col, nd[k], nd[l]);
+      if (b >= rptr[nd[k] + 1] || col[b] != nd[l]) {  // cannot happen for a consistent pattern
+        atomicOr(err, 2);
+        continue;
+      }
       if (MODE == 0) {
         atomicAdd(&cnt[b], 1);
       } else {
@@ -150,51 +154,98 @@ __global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int3
     }
 }
 
+// One member record (16 values for combined records) through vector loads.
+template <typename T, int N>
+XK_D void load_rec(const T* __restrict__ r, T* out);
+template <>
+XK_D void load_rec<float, 16>(const float* __restrict__ r, float* out) {
+  const float4* p = reinterpret_cast<const float4*>(r);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float4 v = __ldg(p + i);
+    out[4 * i] = v.x; out[4 * i + 1] = v.y; out[4 * i + 2] = v.z; out[4 * i + 3] = v.w;
+  }
+}
+template <>
+XK_D void load_rec<double, 16>(const double* __restrict__ r, double* out) {
+  const double2* p = reinterpret_cast<const double2*>(r);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const double2 v = __ldg(p + i);
+    out[2 * i] = v.x; out[2 * i + 1] = v.y;
+  }
+}
+
+// Warp per node: lane l takes incidences l, l+32, ...; the lanes' partial sums
+// are combined by a fixed shuffle tree, so the result does not depend on timing.
 template <typename T>
 __global__ void k_gather_force(int n_nodes, const int32_t* __restrict__ ptr, const int32_t* __restrict__ inc,
-                               const T* __restrict__ rec, long long rs, int vcol, int vcol2,
+                               const T* __restrict__ rec, int rs, int vcol, int vcol2,
                                const double* __restrict__ base, double scale, const double* __restrict__ f_ext,
                                const uint8_t* __restrict__ fixed, double* __restrict__ out) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (v >= n_nodes) return;
   double acc[3] = {0.0, 0.0, 0.0};
   if (ptr)
-    for (int x = ptr[v]; x < ptr[v + 1]; ++x) {
-      const int code = inc[x], mi = code >> 2, k = code & 3;
-      const double c = (double)shape_c<T>(rec[mi], rec[rs + mi], k);
+    for (int x = ptr[v] + lane; x < ptr[v + 1]; x += 32) {
+      const int code = inc[x], k = code & 3;
+      const T* r = rec + (long long)(code >> 2) * rs;
+      const double c = (double)shape_c<T>(r[0], r[1], k);
       for (int d = 0; d < 3; ++d) {
-        double w = (double)rec[(vcol + d) * rs + mi];
-        if (vcol2 >= 0) w += (double)rec[(vcol2 + d) * rs + mi];
+        double w = (double)r[vcol + d];
+        if (vcol2 >= 0) w += (double)r[vcol2 + d];
         acc[d] += c * w;
       }
     }
-  for (int d = 0; d < 6; ++d) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) acc[d] += __shfl_down_sync(0xffffffffu, acc[d], o);
+  if (lane < 6) {
+    const int d = lane;
     const long long dof = 6LL * v + d;
     double r = base ? base[dof] : 0.0;
-    if (d < 3) r += scale * acc[d];
+    if (d < 3) r += scale * (d == 0 ? acc[0] : (d == 1 ? acc[1] : acc[2]));
     if (f_ext) r -= f_ext[dof];
     if (fixed && fixed[dof]) r = 0.0;
     out[dof] = r;
   }
 }
 
-template <typename T>
-__global__ void k_gather_tangent(long long nnzb, const int32_t* __restrict__ bptr, const int32_t* __restrict__ contrib,
-                                 const T* __restrict__ rec, long long rs, int bcol, T* __restrict__ K) {
-  long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nnzb) return;
+// Thread per K_c block; the 9 values of the block-row tile of a CTA are staged
+// in shared memory and stored contiguously.
+constexpr int GT_T = 128;
+template <typename T, int RS>
+__global__ void __launch_bounds__(GT_T) k_gather_tangent(long long nnzb, const int32_t* __restrict__ bptr,
+                                                         const int32_t* __restrict__ contrib,
+                                                         const T* __restrict__ rec, int bcol, T* __restrict__ K) {
+  __shared__ T sk[GT_T * 9];
+  const long long b0 = (long long)blockIdx.x * GT_T;
+  const long long b = b0 + threadIdx.x;
   T acc[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] = T(0);
-  for (int x = bptr[b]; x < bptr[b + 1]; ++x) {
-    const int code = contrib[x], mi = code >> 4, k = (code >> 2) & 3, l = code & 3;
-    const T s = rec[mi], t = rec[rs + mi];
-    const T w = shape_c<T>(s, t, k) * shape_c<T>(s, t, l);
+  if (b < nnzb) {
+    for (int x = bptr[b]; x < bptr[b + 1]; ++x) {
+      const int code = contrib[x], k = (code >> 2) & 3, l = code & 3;
+      T r[RS];
+      if (RS == 16) {
+        load_rec<T, 16>(rec + (long long)(code >> 4) * RS, r);
+      } else {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) acc[q] += w * rec[(bcol + q) * rs + mi];
+        for (int q = 0; q < RS; ++q) r[q] = rec[(long long)(code >> 4) * RS + q];
+      }
+      const T w = shape_c<T>(r[0], r[1], k) * shape_c<T>(r[0], r[1], l);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) acc[q] += w * r[bcol + q];
+    }
   }
 #pragma unroll
-  for (int q = 0; q < 9; ++q) K[9 * b + q] = acc[q];
+  for (int q = 0; q < 9; ++q) sk[threadIdx.x * 9 + q] = acc[q];
+  __syncthreads();
+  const long long nv = 9 * ((nnzb - b0) < GT_T ? (nnzb - b0) : GT_T);
+  for (int i = threadIdx.x; i < nv; i += GT_T) K[9 * b0 + i] = sk[i];
 }
 
 struct Scratch {
@@ -290,15 +341,17 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   XK_TRY(S.get(&bfill, nb + 1));
   XK_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int32_t) * (nb + 1), st));
   if (nm > 0) k_contrib<0><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
-                                                                bcnt, nullptr, nullptr);
+                                                                bcnt, nullptr, nullptr, err);
   XK_CHECK_LAUNCH();
   XK_TRY(xk_exclusive_scan_i32(bcnt, pat->blk_ptr, nb + 1, nullptr, st));
   XK_CUDA(cudaMemsetAsync(bfill, 0, sizeof(int32_t) * (nb + 1), st));
   if (nm > 0) k_contrib<1><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
-                                                                bfill, pat->blk_ptr, pat->contrib);
+                                                                bfill, pat->blk_ptr, pat->contrib, err);
   if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
   XK_CHECK_LAUNCH();
+  XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
+  if (herr) return xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: inconsistent block pattern");
   return XK_OK;
 }
 
@@ -329,6 +382,7 @@ extern "C" xk_status xk_contact_gather_force(const xk_contact_pattern* pat, cons
   if (!pat || !out) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force: null argument");
   int c1, c2;
   XK_TRY(rec_columns(out_mode, which, false, &c1, &c2));
+  const int rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
   const bool use = pat->n_members > 0 && rec;
   const int32_t* ptr = use ? pat->inc_ptr : nullptr;
   const int32_t* inc = use ? pat->inc : nullptr;
@@ -336,11 +390,11 @@ extern "C" xk_status xk_contact_gather_force(const xk_contact_pattern* pat, cons
   const int nn = pat->n_nodes;
   if (nn > 0) {
     if (precision == XK_FP64)
-      k_gather_force<double><<<xk_blocks(nn, 128), 128, 0, st>>>(nn, ptr, inc, (const double*)rec, pat->cap_members,
-                                                                  c1, c2, base, scale, f_ext, fixed, out);
+      k_gather_force<double><<<xk_blocks(32LL * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const double*)rec, rs, c1, c2,
+                                                                         base, scale, f_ext, fixed, out);
     else if (precision == XK_MIXED)
-      k_gather_force<float><<<xk_blocks(nn, 128), 128, 0, st>>>(nn, ptr, inc, (const float*)rec, pat->cap_members,
-                                                                 c1, c2, base, scale, f_ext, fixed, out);
+      k_gather_force<float><<<xk_blocks(32LL * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const float*)rec, rs, c1, c2,
+                                                                        base, scale, f_ext, fixed, out);
     else
       return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force: precision");
     XK_CHECK_LAUNCH();
@@ -354,17 +408,20 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   if (!pat || !rec || !Kc_vals) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: null argument");
   int c1, c2;
   XK_TRY(rec_columns(out_mode, which, true, &c1, &c2));
+  const int rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
   if (pat->nnzb == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
-  const int nb = xk_blocks(pat->nnzb, 128);
-  if (precision == XK_FP64)
-    k_gather_tangent<double><<<nb, 128, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const double*)rec,
-                                                 pat->cap_members, c1, (double*)Kc_vals);
-  else if (precision == XK_MIXED)
-    k_gather_tangent<float><<<nb, 128, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const float*)rec,
-                                                pat->cap_members, c1, (float*)Kc_vals);
-  else
+  const int nb = xk_blocks(pat->nnzb, GT_T);
+  const bool comb = out_mode == XK_OUT_COMBINED;
+  if (precision == XK_FP64) {
+    if (comb) k_gather_tangent<double, 16><<<nb, GT_T, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const double*)rec, c1, (double*)Kc_vals);
+    else k_gather_tangent<double, 32><<<nb, GT_T, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const double*)rec, c1, (double*)Kc_vals);
+  } else if (precision == XK_MIXED) {
+    if (comb) k_gather_tangent<float, 16><<<nb, GT_T, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const float*)rec, c1, (float*)Kc_vals);
+    else k_gather_tangent<float, 32><<<nb, GT_T, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const float*)rec, c1, (float*)Kc_vals);
+  } else {
     return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: precision");
+  }
   XK_CHECK_LAUNCH();
   return XK_OK;
 }

@@ -452,21 +452,379 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, c
     }
   }
   // ---------------------------------------------------------------- record
-  rec[mi] = (T)s;
-  rec[rs + mi] = (T)t;
+  T* r = rec + (long long)mi * rs;  // array-of-structs record, rs values per member
+  r[0] = (T)s;
+  r[1] = (T)t;
   if (OUT == XK_OUT_COMBINED) {
-    for (int k = 0; k < 3; ++k) rec[(2 + k) * rs + mi] = vn[k] + vf[k];
-    for (int k = 0; k < 9; ++k) rec[(5 + k) * rs + mi] = Bn[k] - Bf[k];
+    for (int k = 0; k < 3; ++k) r[2 + k] = vn[k] + vf[k];
+    for (int k = 0; k < 9; ++k) r[5 + k] = Bn[k] - Bf[k];
   } else {
     if (stages & XK_STAGE_NORMAL)
-      for (int k = 0; k < 3; ++k) rec[(2 + k) * rs + mi] = vn[k];
+      for (int k = 0; k < 3; ++k) r[2 + k] = vn[k];
     if (stages & XK_STAGE_FRICTION)
-      for (int k = 0; k < 3; ++k) rec[(5 + k) * rs + mi] = vf[k];
+      for (int k = 0; k < 3; ++k) r[5 + k] = vf[k];
     if (stages & XK_STAGE_TANGENT) {
-      for (int k = 0; k < 9; ++k) rec[(8 + k) * rs + mi] = Bn[k];
-      for (int k = 0; k < 9; ++k) rec[(17 + k) * rs + mi] = Bf[k];
+      for (int k = 0; k < 9; ++k) r[8 + k] = Bn[k];
+      for (int k = 0; k < 9; ++k) r[17 + k] = Bf[k];
     }
   }
+}
+
+// ===========================================================================
+// Mixed fast path: no double-precision instruction per pair.
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the per-iteration
+// pair kernels of the mixed path use float only.  The one quantity float
+// cannot resolve is the gap dist - (r_a + r_b): dist is about r_a + r_b and
+// the gap is a few tenths of a percent of it.  It is taken in float-float
+// ("df") arithmetic: error-free two-sum / two-product transformations on the
+// FP32 pipe, from node positions that xk_nodes_prepare splits once per
+// iteration into a float high part and a float remainder.
+// ===========================================================================
+
+struct df {
+  float h, l;
+};
+XK_D df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+XK_D df fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+XK_D df df_sub(df a, df b) {
+  const df s = two_sum(a.h, -b.h);
+  return fast_two_sum(s.h, s.l + (a.l - b.l));
+}
+XK_D df df_add(df a, df b) {
+  const df s = two_sum(a.h, b.h);
+  return fast_two_sum(s.h, s.l + (a.l + b.l));
+}
+XK_D df df_mulf(df a, float b) {
+  const float p = a.h * b;
+  const float e = fmaf(a.h, b, -p);
+  return fast_two_sum(p, fmaf(a.l, b, e));
+}
+
+__global__ void k_nodes_prepare(xk_mesh m, const double* __restrict__ u, const double* __restrict__ u_ref,
+                                float* __restrict__ n32) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m.n_nodes) return;
+  float* N = n32 + (long long)v * XK_NODE32_STRIDE;
+  for (int c = 0; c < 3; ++c) {
+    const double x = m.X[3LL * v + c] + u[6LL * v + c];
+    const float h = (float)x;
+    N[c] = h;
+    N[3 + c] = (float)(x - (double)h);
+  }
+  for (int c = 0; c < 6; ++c) N[6 + c] = (float)u[6LL * v + c];
+  for (int c = 0; c < 3; ++c) N[12 + c] = (float)(u_ref ? u[6LL * v + c] - u_ref[6LL * v + c] : u[6LL * v + c]);
+  N[15] = 0.0f;
+}
+
+__global__ void k_pairs_convert(xk_pairs p, xk_pairs32 q, int to32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const long long cp = p.cap, cq = q.cap;
+  if (to32) {
+    q.s[i] = (float)p.s[i]; q.t[i] = (float)p.t[i]; q.gap[i] = (float)p.gap[i];
+    for (int c = 0; c < 3; ++c) {
+      q.normal[c * cq + i] = (float)p.normal[c * cp + i];
+      q.t1[c * cq + i] = (float)p.t1[c * cp + i];
+      q.t2[c * cq + i] = (float)p.t2[c * cp + i];
+    }
+    q.p_n[i] = (float)p.p_n[i];
+    q.z_t[i] = (float)p.z_t[i]; q.z_t[cq + i] = (float)p.z_t[cp + i];
+    q.q_trial_norm[i] = (float)p.q_trial_norm[i]; q.dissipation[i] = (float)p.dissipation[i];
+    q.k_pen[i] = (float)p.k_pen[i]; q.k_t[i] = (float)p.k_t[i];
+  } else {
+    p.s[i] = q.s[i]; p.t[i] = q.t[i]; p.gap[i] = q.gap[i];
+    for (int c = 0; c < 3; ++c) {
+      p.normal[c * cp + i] = q.normal[c * cq + i];
+      p.t1[c * cp + i] = q.t1[c * cq + i];
+      p.t2[c * cp + i] = q.t2[c * cq + i];
+    }
+    p.p_n[i] = q.p_n[i];
+    p.z_t[i] = q.z_t[i]; p.z_t[cp + i] = q.z_t[cq + i];
+    p.q_trial_norm[i] = q.q_trial_norm[i]; p.dissipation[i] = q.dissipation[i];
+    p.k_pen[i] = q.k_pen[i]; p.k_t[i] = q.k_t[i];
+  }
+}
+
+XK_D float clamp01f(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+
+// Closest point and gap of one pair from prepared nodes; frame transported from
+// the previous float frame.  Near-parallel pairs fall back to the exact routine.
+XK_D void narrow32(const float* __restrict__ n32, const int* nd, df R, float& s, float& t, float& gap, float* n,
+                   float* pt1_io, float* t2) {
+  df x[4][3];
+  for (int k = 0; k < 4; ++k) {
+    const float* N = n32 + (long long)nd[k] * XK_NODE32_STRIDE;
+    for (int c = 0; c < 3; ++c) x[k][c] = {N[c], N[3 + c]};
+  }
+  float fa[3], fb[3], fw[3];
+  for (int c = 0; c < 3; ++c) {
+    fa[c] = (x[1][c].h - x[0][c].h) + (x[1][c].l - x[0][c].l);
+    fb[c] = (x[3][c].h - x[2][c].h) + (x[3][c].l - x[2][c].l);
+    fw[c] = (x[0][c].h - x[2][c].h) + (x[0][c].l - x[2][c].l);
+  }
+  const float a = dot3(fa, fa), b = dot3(fa, fb), c = dot3(fb, fb), d = dot3(fa, fw), e = dot3(fb, fw);
+  const float ac = a * c, det = ac - b * b;
+  float nrm[3];
+  if (!(det > 1e-3f * ac)) {
+    // rare: near-parallel or degenerate segments, exact double routine
+    double xd[4][3], sd, td, dist, nd3[3], diff[3];
+    for (int k = 0; k < 4; ++k)
+      for (int q = 0; q < 3; ++q) xd[k][q] = (double)x[k][q].h + (double)x[k][q].l;
+    closest_exact(xd[0], xd[1], xd[2], xd[3], sd, td, dist, nd3, diff);
+    s = (float)sd;
+    t = (float)td;
+    gap = (float)(dist - ((double)R.h + (double)R.l));
+    for (int q = 0; q < 3; ++q) nrm[q] = (float)nd3[q];
+  } else {
+    const float idet = 1.0f / det;
+    const float su = (b * e - c * d) * idet, tu = (a * e - b * d) * idet;
+    float sf = clamp01f(su), tf = clamp01f(tu);
+    if (su < 0.0f || su > 1.0f) tf = clamp01f((b * sf + e) / c);
+    if (tu < 0.0f || tu > 1.0f) {
+      sf = clamp01f((b * tf - d) / a);
+      tf = clamp01f((b * sf + e) / c);
+    }
+    s = sf;
+    t = tf;
+    // diff = (xA0 - xB0) + s (xA1 - xA0) - t (xB1 - xB0) in float-float
+    df D[3];
+    for (int q = 0; q < 3; ++q) {
+      const df w0 = df_sub(x[0][q], x[2][q]);
+      const df dA = df_sub(x[1][q], x[0][q]);
+      const df dB = df_sub(x[3][q], x[2][q]);
+      D[q] = df_sub(df_add(w0, df_mulf(dA, sf)), df_mulf(dB, tf));
+    }
+    // |D|^2 with the squares of the high parts taken exactly
+    df S = {0.0f, 0.0f};
+    float cross_terms = 0.0f;
+    for (int q = 0; q < 3; ++q) {
+      const float p = D[q].h * D[q].h;
+      const df sq = {p, fmaf(D[q].h, D[q].h, -p)};
+      S = df_add(S, sq);
+      cross_terms = fmaf(2.0f * D[q].h, D[q].l, cross_terms);
+    }
+    S = fast_two_sum(S.h, S.l + cross_terms);
+    const float dh = sqrtf(S.h);
+    const float dl = (fmaf(-dh, dh, S.h) + S.l) / (2.0f * dh);
+    gap = (dh - R.h) + (dl - R.l);
+    const float id = 1.0f / dh;
+    for (int q = 0; q < 3; ++q) nrm[q] = D[q].h * id;
+    if (!(dh > 1e-30f)) { nrm[0] = 0.0f; nrm[1] = 0.0f; nrm[2] = 1.0f; }
+  }
+  // frame transport (float)
+  float pn[3] = {n[0], n[1], n[2]};  // previous normal on entry
+  float pt1[3] = {pt1_io[0], pt1_io[1], pt1_io[2]};
+  const float inv = rsqrtf(fmaxf(dot3(nrm, nrm), 1e-30f));
+  for (int q = 0; q < 3; ++q) n[q] = nrm[q] * inv;
+  const bool has_t1 = dot3(pt1, pt1) > 1e-20f, has_n = dot3(pn, pn) > 1e-20f;
+  bool done = false;
+  float t1[3];
+  if (has_t1) {
+    float tr[3] = {pt1[0], pt1[1], pt1[2]};
+    if (has_n) {
+      const float ip = rsqrtf(dot3(pn, pn));
+      const float no[3] = {pn[0] * ip, pn[1] * ip, pn[2] * ip};
+      float v[3], vx[3], vvx[3];
+      cross3(no, n, v);
+      const float cv = dot3(no, n), s2 = dot3(v, v);
+      if (cv > 0.0f || s2 >= 1e-24f) {
+        cross3(v, pt1, vx);
+        cross3(v, vx, vvx);
+        const float f = cv > 0.0f ? 1.0f / (1.0f + cv) : (1.0f - cv) / s2;
+        for (int q = 0; q < 3; ++q) tr[q] = pt1[q] + vx[q] + f * vvx[q];
+      }
+    }
+    const float dn = dot3(tr, n);
+    const float raw[3] = {tr[0] - dn * n[0], tr[1] - dn * n[1], tr[2] - dn * n[2]};
+    const float r2 = dot3(raw, raw);
+    if (r2 > 1e-20f) {
+      const float ir = rsqrtf(r2);
+      for (int q = 0; q < 3; ++q) t1[q] = raw[q] * ir;
+      done = true;
+    }
+  }
+  if (!done) {
+    float ref[3] = {0.f, 0.f, 0.f};
+    const float a0 = fabsf(n[0]), a1 = fabsf(n[1]), a2 = fabsf(n[2]);
+    ref[(a0 <= a1 && a0 <= a2) ? 0 : (a1 <= a2 ? 1 : 2)] = 1.0f;
+    const float dn = dot3(ref, n);
+    const float raw[3] = {ref[0] - dn * n[0], ref[1] - dn * n[1], ref[2] - dn * n[2]};
+    const float ir = rsqrtf(fmaxf(dot3(raw, raw), 1e-30f));
+    for (int q = 0; q < 3; ++q) t1[q] = raw[q] * ir;
+  }
+  cross3(n, t1, t2);
+  for (int q = 0; q < 3; ++q) pt1_io[q] = t1[q];
+}
+
+XK_D df radius_sum(const float* __restrict__ e32, int ea, int eb) {
+  const float* A = e32 + (long long)ea * XK_ELEM32_STRIDE + 13;
+  const float* B = e32 + (long long)eb * XK_ELEM32_STRIDE + 13;
+  const df s = two_sum(A[0], B[0]);
+  return fast_two_sum(s.h, s.l + (A[1] + B[1]));
+}
+
+XK_D void load3f(const float* base, long long stride, long long i, float* v) {
+  v[0] = base[i];
+  v[1] = base[stride + i];
+  v[2] = base[2 * stride + i];
+}
+XK_D void store3f(float* base, long long stride, long long i, const float* v) {
+  base[i] = v[0];
+  base[stride + i] = v[1];
+  base[2 * stride + i] = v[2];
+}
+
+__global__ void __launch_bounds__(PAIR_T) k_pair_other32(xk_mesh m, xk_pairs p, xk_pairs32 q,
+                                                         const int32_t* __restrict__ others, int n_o,
+                                                         const float* __restrict__ n32, const float* __restrict__ e32) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n_o) return;
+  const int i = others[o];
+  const long long cq = q.cap;
+  const int ea = p.ea[i], eb = p.eb[i];
+  const int nd[4] = {m.conn[2 * ea], m.conn[2 * ea + 1], m.conn[2 * eb], m.conn[2 * eb + 1]};
+  float s, t, gap, n[3], t1[3], t2[3];
+  load3f(q.normal, cq, i, n);
+  load3f(q.t1, cq, i, t1);
+  narrow32(n32, nd, radius_sum(e32, ea, eb), s, t, gap, n, t1, t2);
+  q.s[i] = s;
+  q.t[i] = t;
+  q.gap[i] = gap;
+  store3f(q.normal, cq, i, n);
+  store3f(q.t1, cq, i, t1);
+  store3f(q.t2, cq, i, t2);
+}
+
+__global__ void __launch_bounds__(PAIR_T) k_pair_member32(xk_mesh m, xk_pairs p, xk_pairs32 q,
+                                                          const int32_t* __restrict__ members,
+                                                          const int32_t* __restrict__ mnodes, int n_m,
+                                                          const float* __restrict__ n32, const float* __restrict__ e32,
+                                                          xk_contact_params cp, float* __restrict__ rec) {
+  const int mi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mi >= n_m) return;
+  const int i = members[mi];
+  const long long cq = q.cap;
+  int nd[4];
+  for (int k = 0; k < 4; ++k) nd[k] = mnodes[4LL * mi + k];
+  uint8_t status = p.status[i];
+  const df R = radius_sum(e32, p.ea[i], p.eb[i]);
+  float s, t, gap, n[3], t1[3], t2[3];
+  load3f(q.normal, cq, i, n);
+  load3f(q.t1, cq, i, t1);
+  narrow32(n32, nd, R, s, t, gap, n, t1, t2);
+  q.s[i] = s;
+  q.t[i] = t;
+  q.gap[i] = gap;
+  store3f(q.normal, cq, i, n);
+  store3f(q.t1, cq, i, t1);
+  store3f(q.t2, cq, i, t2);
+  // normal force (Huber)
+  const float kpen = (float)cp.k_pen;
+  const float dh = cp.smoothing_delta > 0.0 ? (float)(cp.k_pen / cp.smoothing_delta) : 0.0f;
+  const float xpen = kpen * (-gap);
+  float p_n = q.p_n[i];
+  float vn[3] = {0.f, 0.f, 0.f}, vf[3] = {0.f, 0.f, 0.f};
+  if (status != ST_INACTIVE) {
+    p_n = (dh <= 0.0f) ? fmaxf(xpen, 0.0f)
+                       : (xpen < -dh ? 0.0f : (xpen > dh ? xpen : (xpen + dh) * (xpen + dh) / (4.0f * dh)));
+    q.p_n[i] = p_n;
+    if (p_n > 1e-30f)
+      for (int k = 0; k < 3; ++k) vn[k] = p_n * n[k];
+  }
+  // friction (Coulomb return mapping)
+  const float mu = (float)cp.mu_eff;
+  float kt = q.k_t[i];
+  float zt0 = q.z_t[i], zt1 = q.z_t[cq + i];
+  float qtn = q.q_trial_norm[i];
+  bool stick = p.stick[i] != 0;
+  const bool fproc = (p_n > 0.0f) && (mu > 0.0f);
+  if (fproc) {
+    if (q.k_pen[i] <= 0.0f) {
+      q.k_pen[i] = kpen;
+      kt = (float)(cp.k_pen * cp.k_t_ratio);
+      q.k_t[i] = kt;
+    }
+    float du[4][3];
+    for (int k = 0; k < 4; ++k) {
+      const float* N = n32 + (long long)nd[k] * XK_NODE32_STRIDE + 12;
+      du[k][0] = N[0]; du[k][1] = N[1]; du[k][2] = N[2];
+    }
+    float dr[3];
+    for (int c = 0; c < 3; ++c) dr[c] = ((1.f - t) * du[2][c] + t * du[3][c]) - ((1.f - s) * du[0][c] + s * du[1][c]);
+    const float d0 = dot3(dr, t1), d1 = dot3(dr, t2);
+    const float q0 = zt0 + kt * d0, q1 = zt1 + kt * d1;
+    const float qn = sqrtf(q0 * q0 + q1 * q1);
+    const float fy = mu * p_n;
+    stick = qn <= fy;
+    float r0 = q0, r1 = q1;
+    if (!stick) { r0 = fy * q0 / qn; r1 = fy * q1 / qn; }
+    zt0 = r0; zt1 = r1; qtn = qn;
+    q.z_t[i] = zt0;
+    q.z_t[cq + i] = zt1;
+    p.stick[i] = stick ? 1 : 0;
+    q.q_trial_norm[i] = qtn;
+    q.dissipation[i] = r0 * d0 + r1 * d1;
+    status = stick ? ST_ACTIVE : ST_SLIDING;
+    p.status[i] = status;
+    if (sqrtf(r0 * r0 + r1 * r1) >= 1e-30f) {
+      const float a0 = fabsf(r0) < 1e-30f ? 0.f : r0, a1 = fabsf(r1) < 1e-30f ? 0.f : r1;
+      for (int k = 0; k < 3; ++k) vf[k] = a0 * t1[k] + a1 * t2[k];
+    }
+  }
+  // pair tangent B = B_n - B_f
+  float B[9];
+  for (int k = 0; k < 9; ++k) B[k] = 0.f;
+  if (status != ST_INACTIVE) {
+    const float dist = gap + (R.h + R.l);
+    const float hd = (dh <= 0.0f) ? (xpen > 0.0f ? 1.0f : 0.0f)
+                                  : (xpen < -dh ? 0.0f : (xpen > dh ? 1.0f : (xpen + dh) / (2.0f * dh)));
+    if (!(hd < 1e-30f && p_n < 1e-30f)) {
+      const float wm = hd * kpen, wg = dist > 1e-15f ? p_n / dist : 0.0f;
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          const float nn = n[a] * n[b];
+          B[3 * a + b] = wm * nn - wg * ((a == b ? 1.f : 0.f) - nn);
+        }
+    }
+    const float qnorm = sqrtf(zt0 * zt0 + zt1 * zt1);
+    if (fproc && qnorm >= 1e-30f) {
+      float D00 = kt, D01 = 0.f, D11 = kt;
+      if (!stick && qtn >= 1e-30f) {
+        const float qh0 = zt0 / qnorm, qh1 = zt1 / qnorm, ratio = mu * p_n / qtn;
+        D00 = ratio * kt * (1.f - qh0 * qh0);
+        D01 = -ratio * kt * qh0 * qh1;
+        D11 = ratio * kt * (1.f - qh1 * qh1);
+      }
+      const bool geo = (dist >= 1e-15f) && !(fabsf(zt0) < 1e-30f && fabsf(zt1) < 1e-30f);
+      const float idist = geo ? 1.0f / dist : 0.0f;
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          const float mat = D00 * t1[a] * t1[b] + D01 * (t1[a] * t2[b] + t2[a] * t1[b]) + D11 * t2[a] * t2[b];
+          const float M = -zt0 * n[a] * t1[b] - zt1 * t2[a] * n[b];
+          B[3 * a + b] -= mat + idist * M;
+        }
+      const float g = idist * zt1;
+      B[1] -= g * t1[2];
+      B[2] += g * t1[1];
+      B[3] += g * t1[2];
+      B[5] -= g * t1[0];
+      B[6] -= g * t1[1];
+      B[7] += g * t1[0];
+    }
+  }
+  float4* r = reinterpret_cast<float4*>(rec + (long long)mi * XK_REC_STRIDE_COMBINED);
+  r[0] = make_float4(s, t, vn[0] + vf[0], vn[1] + vf[1]);
+  r[1] = make_float4(vn[2] + vf[2], B[0], B[1], B[2]);
+  r[2] = make_float4(B[3], B[4], B[5], B[6]);
+  r[3] = make_float4(B[7], B[8], 0.f, 0.f);
 }
 
 __global__ void k_active_flags(xk_pairs p, int32_t* __restrict__ flag) {
@@ -530,7 +888,7 @@ extern "C" xk_status xk_pair_step(const xk_mesh* m, xk_pairs* p, const xk_contac
   }
   if (pat->n_members == 0) return XK_OK;
   const int nb = xk_blocks(pat->n_members, PAIR_T);
-  const long long rs = pat->cap_members;
+  const long long rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
 #define XK_MEMBER_LAUNCH(PP, OO, TT)                                                                                \
   k_pair_member<PP, OO><<<nb, PAIR_T, 0, st>>>(*m, *p, pat->members, pat->member_nodes, pat->n_members, u, u_ref, \
                                                *cp, stages, (TT*)rec, rs)
@@ -580,4 +938,51 @@ extern "C" xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p,
   cudaFreeAsync(flag, st);
   cudaFreeAsync(tot, st);
   return r;
+}
+
+extern "C" xk_status xk_nodes_prepare(const xk_mesh* m, const double* u, const double* u_ref, float* node32,
+                                      xk_stream s) {
+  if (!m || !u || !node32) return xk_set_error(XK_ERR_ARG, "xk_nodes_prepare: null argument");
+  if (m->n_nodes == 0) return XK_OK;
+  k_nodes_prepare<<<xk_blocks(m->n_nodes, 256), 256, 0, (cudaStream_t)s>>>(*m, u, u_ref, node32);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
+static xk_status pairs_convert(const xk_pairs* p, const xk_pairs32* q, int to32, xk_stream s) {
+  if (!p || !q) return xk_set_error(XK_ERR_ARG, "xk_pairs_to32/from32: null argument");
+  if (q->cap < p->n) return xk_set_error(XK_ERR_CAPACITY, "xk_pairs_to32/from32: float table capacity below n");
+  if (p->n == 0) return XK_OK;
+  k_pairs_convert<<<xk_blocks(p->n, 256), 256, 0, (cudaStream_t)s>>>(*p, *q, to32);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
+extern "C" xk_status xk_pairs_to32(const xk_pairs* p, xk_pairs32* q, xk_stream s) {
+  xk_status r = pairs_convert(p, q, 1, s);
+  if (r == XK_OK) q->n = p->n;
+  return r;
+}
+
+extern "C" xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream s) {
+  return pairs_convert(p, q, 0, s);
+}
+
+extern "C" xk_status xk_pair_step32(const xk_mesh* m, xk_pairs* p, xk_pairs32* q, const xk_contact_pattern* pat,
+                                    const float* node32, const float* elem32, const xk_contact_params* cp, float* rec,
+                                    xk_stream s) {
+  if (!m || !p || !q || !pat || !node32 || !elem32 || !cp) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: null argument");
+  if ((long long)pat->n_members + pat->n_others != p->n || q->n != p->n)
+    return xk_set_error(XK_ERR_ARG, "xk_pair_step32: pattern or float table built for another pair table");
+  if (pat->n_members > 0 && !rec) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: rec is null");
+  cudaStream_t st = (cudaStream_t)s;
+  if (pat->n_others > 0)
+    k_pair_other32<<<xk_blocks(pat->n_others, PAIR_T), PAIR_T, 0, st>>>(*m, *p, *q, pat->others, pat->n_others,
+                                                                        node32, elem32);
+  if (pat->n_members > 0)
+    k_pair_member32<<<xk_blocks(pat->n_members, PAIR_T), PAIR_T, 0, st>>>(*m, *p, *q, pat->members,
+                                                                          pat->member_nodes, pat->n_members, node32,
+                                                                          elem32, *cp, rec);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
 }

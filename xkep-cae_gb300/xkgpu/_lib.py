@@ -17,7 +17,7 @@ XK_STAGE_NARROW, XK_STAGE_NORMAL, XK_STAGE_FRICTION, XK_STAGE_TANGENT = 1, 2, 4,
 XK_STAGE_ALL = 15
 XK_OUT_COMBINED, XK_OUT_SPLIT = 0, 1
 XK_WHICH_COMBINED, XK_WHICH_NORMAL, XK_WHICH_FRICTION = 0, 1, 2
-REC_COLS = {XK_OUT_COMBINED: 14, XK_OUT_SPLIT: 26}
+REC_STRIDE = {XK_OUT_COMBINED: 16, XK_OUT_SPLIT: 32}
 
 vp = C.c_void_p
 
@@ -35,6 +35,12 @@ class Pairs(C.Structure):
     _fields_ = [("n", C.c_int32), ("cap", C.c_int32)] + [
         (n, vp) for n in ("ea", "eb", "s", "t", "gap", "normal", "t1", "t2", "lambda_n", "k_pen", "k_t", "p_n",
                           "z_t", "q_trial_norm", "dissipation", "status", "stick")]
+
+
+class Pairs32(C.Structure):
+    _fields_ = [("n", C.c_int32), ("cap", C.c_int32)] + [
+        (n, vp) for n in ("s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm", "dissipation", "k_pen",
+                          "k_t")]
 
 
 class BeamPlan(C.Structure):
@@ -80,7 +86,15 @@ SIGNATURES = {
     "xk_contact_gather_tangent": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, vp, vp],
     "xk_constraint_jacobian": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
     "xk_norm2": [vp, C.c_int64, vp, vp],
+    "xk_nodes_prepare": [P(Mesh), vp, vp, vp, vp],
+    "xk_beam_prepare32": [P(Mesh), vp, vp, vp],
+    "xk_beam_assemble32": [P(Mesh), P(Section), vp, P(BeamPlan), vp, vp, vp, vp],
+    "xk_pairs_to32": [P(Pairs), P(Pairs32), vp],
+    "xk_pairs_from32": [P(Pairs32), P(Pairs), vp],
+    "xk_pair_step32": [P(Mesh), P(Pairs), P(Pairs32), P(ContactPattern), vp, vp, P(ContactParams), vp, vp],
 }
+NODE32_STRIDE = 16
+ELEM32_STRIDE = 16
 
 
 class XkError(RuntimeError):

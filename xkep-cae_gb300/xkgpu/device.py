@@ -287,6 +287,28 @@ class DevicePairTable:
         self.refresh()
 
 
+F32_FIELDS = {"s": 1, "t": 1, "gap": 1, "normal": 3, "t1": 3, "t2": 3, "p_n": 1, "z_t": 2, "q_trial_norm": 1,
+              "dissipation": 1, "k_pen": 1, "k_t": 1}
+
+
+class DevicePairTable32:
+    """Float copy of the pair-state fields (``xk_pairs32``) for the mixed per-iteration kernels."""
+
+    def __init__(self, device):
+        self.device = device
+        self.cap = 0
+        self.t: dict[str, torch.Tensor] = {}
+        self.c = L.Pairs32()
+
+    def ensure(self, cap: int):
+        if cap <= self.cap:
+            return
+        cap = int(cap)
+        self.t = {k: torch.zeros(w * cap, dtype=torch.float32, device=self.device) for k, w in F32_FIELDS.items()}
+        self.cap = cap
+        self.c = L.Pairs32(0, cap, *(ptr(self.t[k]) for k in F32_FIELDS))
+
+
 # ----------------------------------------------------------------------------- contact pattern
 
 

@@ -32,8 +32,8 @@ import scipy.sparse as sp
 import torch
 
 from . import _lib as L
-from .device import (DeviceBeam, DeviceContactPattern, DeviceMesh, DevicePairTable, ptr, require_cuda,
-                     stream_handle)
+from .device import (DeviceBeam, DeviceContactPattern, DeviceMesh, DevicePairTable, DevicePairTable32, ptr,
+                     require_cuda, stream_handle)
 
 PRECISIONS = {"fp64": L.XK_FP64, "mixed": L.XK_MIXED}
 
@@ -60,6 +60,12 @@ class AssemblyEngine:
         self.R = torch.zeros(nd, dtype=torch.float64, device=dev)
         self.norm2 = torch.zeros(1, dtype=torch.float64, device=dev)
         self.cands = torch.zeros(2 * 1024, dtype=torch.int32, device=dev)
+        # mixed fast path: float node / element records and the float copy of the pair state
+        self.node32 = torch.zeros(L.NODE32_STRIDE * max(self.mesh.n_nodes, 1), dtype=torch.float32, device=dev)
+        self.elem32 = torch.zeros(L.ELEM32_STRIDE * max(self.mesh.n_elems, 1), dtype=torch.float32, device=dev)
+        self.pairs32 = DevicePairTable32(dev)
+        self._state_in32 = False
+        self.update_reference_frames()
         self._alloc_outputs()
         self.stats: dict = {}
         self.graph = None
@@ -72,10 +78,22 @@ class AssemblyEngine:
     def _alloc_outputs(self):
         dev = self.device
         self.K_beam = torch.zeros(36 * max(self.beam.nnzb, 1), dtype=self.t_dtype, device=dev)
-        self.rec = torch.zeros(L.REC_COLS[L.XK_OUT_COMBINED] * self.pattern.cap_members, dtype=self.t_dtype,
+        self.rec = torch.zeros(L.REC_STRIDE[L.XK_OUT_COMBINED] * self.pattern.cap_members, dtype=self.t_dtype,
                                device=dev)
         self.K_c = torch.zeros(9 * max(self.pattern.cap_blocks, 1), dtype=self.t_dtype, device=dev)
         self.graph = None
+
+    def update_reference_frames(self, stream=None):
+        """Recompute per-element reference data after the reference coordinates changed."""
+        self.beam.update_reference_frames(stream)
+        L.call("xk_beam_prepare32", C.byref(self.mesh.c), ptr(self.beam.elem_ref), ptr(self.elem32),
+               stream_handle(stream))
+
+    def sync_state(self, stream=None):
+        """Bring the double pair table up to date with the float copy (mixed path)."""
+        if self._state_in32:
+            L.call("xk_pairs_from32", C.byref(self.pairs32.c), C.byref(self.pairs.c), stream_handle(stream))
+            self._state_in32 = False
 
     def set_precision(self, precision):
         p = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -87,6 +105,7 @@ class AssemblyEngine:
     def detect(self, u: torch.Tensor, stream=None) -> dict:
         """Broadphase, pair-table merge, active-set narrowphase and contact pattern at X + u."""
         s = stream_handle(stream)
+        self.sync_state(stream)
         n_out, n_raw, n_pre = C.c_int64(0), C.c_int64(0), C.c_int64(0)
         for _ in range(3):
             code = L.call("xk_broadphase", C.byref(self.mesh.c), ptr(u), C.byref(self.bp), ptr(self.cands),
@@ -105,7 +124,11 @@ class AssemblyEngine:
         self.pairs, self._spare = self._spare, self.pairs
         L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), C.byref(self.cp), 1, s)
         self.pattern.build(self.pairs, stream)
-        if (self.rec.numel() != L.REC_COLS[L.XK_OUT_COMBINED] * self.pattern.cap_members
+        if self.precision == L.XK_MIXED:
+            self.pairs32.ensure(self.pairs.cap)
+            L.call("xk_pairs_to32", C.byref(self.pairs.c), C.byref(self.pairs32.c), s)
+            self._state_in32 = True
+        if (self.rec.numel() != L.REC_STRIDE[L.XK_OUT_COMBINED] * self.pattern.cap_members
                 or self.K_c.numel() < 9 * self.pattern.cap_blocks):
             self._alloc_outputs()
         self.graph = None
@@ -119,15 +142,35 @@ class AssemblyEngine:
         s = stream_handle(stream)
         p = self.precision
         pat = C.byref(self.pattern.c)
-        L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
-               C.byref(self.cp), L.XK_STAGE_ALL, p, L.XK_OUT_COMBINED, ptr(self.rec), s)
-        self.beam.assemble(u, p, self.f_int, self.K_beam if tangent else None, stream)
+        self.pair_step(u, u_ref, stream)
+        if p == L.XK_MIXED:
+            L.call("xk_beam_assemble32", C.byref(self.mesh.c), C.byref(self.beam.section), ptr(self.elem32),
+                   C.byref(self.beam.plan), ptr(self.node32), ptr(self.f_int), ptr(self.K_beam) if tangent else None,
+                   s)
+        else:
+            self.beam.assemble(u, p, self.f_int, self.K_beam if tangent else None, stream)
         L.call("xk_contact_gather_force", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
                ptr(self.f_int), -1.0, ptr(f_ext), ptr(fixed), ptr(self.R), ptr(self.norm2), s)
         if tangent and self.pattern.nnzb > 0:
             L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
                    ptr(self.K_c), s)
         return self.R
+
+    def pair_step(self, u: torch.Tensor, u_ref: torch.Tensor | None = None, stream=None):
+        """The pair part of ``assemble``: narrowphase of every pair and the member records."""
+        s = stream_handle(stream)
+        pat = C.byref(self.pattern.c)
+        if self.precision == L.XK_MIXED:
+            if not self._state_in32:
+                self.pairs32.ensure(self.pairs.cap)
+                L.call("xk_pairs_to32", C.byref(self.pairs.c), C.byref(self.pairs32.c), s)
+                self._state_in32 = True
+            L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u_ref), ptr(self.node32), s)
+            L.call("xk_pair_step32", C.byref(self.mesh.c), C.byref(self.pairs.c), C.byref(self.pairs32.c), pat,
+                   ptr(self.node32), ptr(self.elem32), C.byref(self.cp), ptr(self.rec), s)
+        else:
+            L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
+                   C.byref(self.cp), L.XK_STAGE_ALL, self.precision, L.XK_OUT_COMBINED, ptr(self.rec), s)
 
     def capture(self, u, u_ref=None, f_ext=None, fixed=None):
         """Record ``assemble`` on these (static) buffers as a CUDA graph."""
@@ -146,6 +189,11 @@ class AssemblyEngine:
         self.graph.replay()
 
     # ------------------------------------------------------------------ host views
+    def pair_state(self) -> dict:
+        """Host copy of the pair table (after syncing the float copy in mixed mode)."""
+        self.sync_state()
+        return self.pairs.to_host()
+
     def residual_norm(self) -> float:
         return float(np.sqrt(self.norm2.item()))
 
