@@ -552,8 +552,11 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
   const float* Rcr = F.Rcr;
   const uint8_t fl = first[e];
   if (live && f_int) {
+    const float g0 = I == 0 ? fcr[0] : I == 1 ? fcr[3] : I == 2 ? fcr[6] : fcr[9];
+    const float g1 = I == 0 ? fcr[1] : I == 1 ? fcr[4] : I == 2 ? fcr[7] : fcr[10];
+    const float g2 = I == 0 ? fcr[2] : I == 1 ? fcr[5] : I == 2 ? fcr[8] : fcr[11];
     for (int i = 0; i < 3; ++i) {
-      const double v = (double)(Rcr[i] * fcr[3 * I] + Rcr[3 + i] * fcr[3 * I + 1] + Rcr[6 + i] * fcr[3 * I + 2]);
+      const double v = (double)(Rcr[i] * g0 + Rcr[3 + i] * g1 + Rcr[6 + i] * g2);
       const long long dof = (I < 2 ? 6LL * a : 6LL * b) + 3 * (I & 1) + i;
       const bool fw = (I < 2) ? (fl & 1) : (fl & 8);
       if (fw) f_int[dof] = v; else f_int[dof] += v;
@@ -583,29 +586,41 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
     mm3(Ti, Rcr, tmp);
     mm3(tmp, Ts, Q2);
   }
+  // block row I of the local stiffness against the theta1 (K1), theta2 (K3) and
+  // axial (k6) columns, built with selects so that the quad does not diverge
+  const bool i0 = I == 0, i1 = I == 1, i2 = I == 2;
+  float K1[9], K3[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) { K1[i] = 0.f; K3[i] = 0.f; }
+  const float tz = i0 ? kc.k2z : -kc.k2z, ty = i0 ? -kc.k2y : kc.k2y;  // rows of I = 0 / 2
+  const bool trans = i0 || i2;
+  K1[5] = trans ? tz : 0.f;
+  K3[5] = K1[5];
+  K1[7] = trans ? ty : 0.f;
+  K3[7] = K1[7];
+  K1[0] = trans ? 0.f : (i1 ? kc.gj : -kc.gj);
+  K3[0] = -K1[0];
+  K1[4] = trans ? 0.f : (i1 ? kc.k1ay : kc.k1by);
+  K3[4] = trans ? 0.f : (i1 ? kc.k1by : kc.k1ay);
+  K1[8] = trans ? 0.f : (i1 ? kc.k1az : kc.k1bz);
+  K3[8] = trans ? 0.f : (i1 ? kc.k1bz : kc.k1az);
+  const float k6 = i0 ? -kc.ea : (i2 ? kc.ea : 0.f);  // only row 3I of the block
+  const float fI0 = i0 ? fcr[0] : i1 ? fcr[3] : i2 ? fcr[6] : fcr[9];
+  const float fI1 = i0 ? fcr[1] : i1 ? fcr[4] : i2 ? fcr[7] : fcr[10];
+  const float fI2 = i0 ? fcr[2] : i1 ? fcr[5] : i2 ? fcr[8] : fcr[11];
   float G[9], H[9], J[9];
   {
     float A[9], Hl[9], Jl[9];
+    mm3(K1, P1, A);
+    float tmp[9];
+    mm3(K3, P2, tmp);
 #pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      const int row = 3 * I + r;
+    for (int i = 0; i < 9; ++i) A[i] += tmp[i];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float acc = -kev(kc, row, 6) * ex[c];
-        float h = 0.f, jj = 0.f;
-#pragma unroll
-        for (int qq = 0; qq < 3; ++qq) {
-          acc += kev(kc, row, 3 + qq) * P1[3 * qq + c] + kev(kc, row, 9 + qq) * P2[3 * qq + c];
-          h += kev(kc, row, 3 + qq) * Q1[3 * qq + c];
-          jj += kev(kc, row, 9 + qq) * Q2[3 * qq + c];
-        }
-        A[3 * r + c] = acc;
-        Hl[3 * r + c] = h;
-        Jl[3 * r + c] = jj;
-      }
-    }
-    const float f0 = fcr[3 * I], f1 = fcr[3 * I + 1], f2 = fcr[3 * I + 2];
-    const float Sf[9] = {0.f, -f2, f1, f2, 0.f, -f0, -f1, f0, 0.f};
+    for (int c = 0; c < 3; ++c) A[c] -= k6 * ex[c];
+    mm3(K1, Q1, Hl);
+    mm3(K3, Q2, Jl);
+    const float Sf[9] = {0.f, -fI2, fI1, fI2, 0.f, -fI0, -fI1, fI0, 0.f};
     float SfD[9];
     mm3(Sf, dpsi, SfD);
 #pragma unroll
@@ -635,7 +650,8 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
       for (int c = 0; c < 3; ++c) {
         const float xij = (Jb == 0) ? G[3 * r + c] : (Jb == 1) ? H[3 * r + c] : (Jb == 2) ? -G[3 * r + c] : J[3 * r + c];
         const float* o = sx[q][Jb];
-        const float xji = (I == 0) ? o[3 * c + r] : (I == 1) ? o[9 + 3 * c + r] : (I == 2) ? -o[3 * c + r] : o[18 + 3 * c + r];
+        const int off = i1 ? 9 : ((I == 3) ? 18 : 0);
+        const float xji = (i2 ? -1.f : 1.f) * o[off + 3 * c + r];
         const float v = 0.5f * (xij + xji);
         const int idx = (3 * (I & 1) + r) * 6 + 3 * (Jb & 1) + c;
         if (fw) dst[idx] = v; else dst[idx] += v;

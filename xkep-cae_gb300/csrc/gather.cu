@@ -176,76 +176,120 @@ XK_D void load_rec<double, 16>(const double* __restrict__ r, double* out) {
   }
 }
 
-// Warp per node: lane l takes incidences l, l+32, ...; the lanes' partial sums
-// are combined by a fixed shuffle tree, so the result does not depend on timing.
+// Eight lanes per node: lane l of the group takes incidences l, l+8, ...; the
+// group's partial sums are combined by a fixed shuffle tree, so the result does
+// not depend on timing.  Sums run in the record precision T (the mixed path
+// accumulates in float) and are converted once per degree of freedom.
+constexpr int GF_LANES = 8;
 template <typename T>
 __global__ void k_gather_force(int n_nodes, const int32_t* __restrict__ ptr, const int32_t* __restrict__ inc,
                                const T* __restrict__ rec, int rs, int vcol, int vcol2,
                                const double* __restrict__ base, double scale, const double* __restrict__ f_ext,
                                const uint8_t* __restrict__ fixed, double* __restrict__ out) {
-  const int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (v >= n_nodes) return;
-  double acc[3] = {0.0, 0.0, 0.0};
-  if (ptr)
-    for (int x = ptr[v] + lane; x < ptr[v + 1]; x += 32) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = gid / GF_LANES, lane = gid % GF_LANES;
+  const bool live = v < n_nodes;
+  T acc[3] = {T(0), T(0), T(0)};
+  if (live && ptr)
+    for (int x = ptr[v] + lane; x < ptr[v + 1]; x += GF_LANES) {
       const int code = inc[x], k = code & 3;
       const T* r = rec + (long long)(code >> 2) * rs;
-      const double c = (double)shape_c<T>(r[0], r[1], k);
+      const T c = shape_c<T>(r[0], r[1], k);
       for (int d = 0; d < 3; ++d) {
-        double w = (double)r[vcol + d];
-        if (vcol2 >= 0) w += (double)r[vcol2 + d];
+        T w = r[vcol + d];
+        if (vcol2 >= 0) w += r[vcol2 + d];
         acc[d] += c * w;
       }
     }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
+  for (int o = GF_LANES / 2; o > 0; o >>= 1)
 #pragma unroll
-    for (int d = 0; d < 3; ++d) acc[d] += __shfl_down_sync(0xffffffffu, acc[d], o);
-  if (lane < 6) {
+    for (int d = 0; d < 3; ++d) acc[d] += __shfl_down_sync(0xffffffffu, acc[d], o, GF_LANES);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) acc[d] = __shfl_sync(0xffffffffu, acc[d], 0, GF_LANES);
+  if (live && lane < 6) {
     const int d = lane;
     const long long dof = 6LL * v + d;
     double r = base ? base[dof] : 0.0;
-    if (d < 3) r += scale * (d == 0 ? acc[0] : (d == 1 ? acc[1] : acc[2]));
+    if (d < 3) r += scale * (double)(d == 0 ? acc[0] : (d == 1 ? acc[1] : acc[2]));
     if (f_ext) r -= f_ext[dof];
     if (fixed && fixed[dof]) r = 0.0;
     out[dof] = r;
   }
 }
 
-// Thread per K_c block; the 9 values of the block-row tile of a CTA are staged
-// in shared memory and stored contiguously.
-constexpr int GT_T = 128;
-template <typename T, int RS>
-__global__ void __launch_bounds__(GT_T) k_gather_tangent(long long nnzb, const int32_t* __restrict__ bptr,
-                                                         const int32_t* __restrict__ contrib,
-                                                         const T* __restrict__ rec, int bcol, T* __restrict__ K) {
-  __shared__ T sk[GT_T * 9];
-  const long long b0 = (long long)blockIdx.x * GT_T;
-  const long long b = b0 + threadIdx.x;
+// Contributor counts are very uneven: a node's diagonal block and the blocks
+// of an element's own node pair collect every member at that node (~30 at the
+// 1027-wire strand), a cross block one or two.  Light blocks (<= 8
+// contributors) take a thread each, heavy blocks a warp each whose lanes split
+// the contributors and combine them by a fixed shuffle tree.
+constexpr int HEAVY_MIN = 9;
+
+template <typename T, int RS, int BCOL>
+XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
+  const int k = (code >> 2) & 3, l = code & 3;
+  T r[RS];
+  if (RS == 16) {
+    load_rec<T, 16>(rec + (long long)(code >> 4) * RS, r);
+  } else {
+#pragma unroll
+    for (int q = 0; q < RS; ++q) r[q] = rec[(long long)(code >> 4) * RS + q];
+  }
+  const T w = shape_c<T>(r[0], r[1], k) * shape_c<T>(r[0], r[1], l);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) acc[q] += w * r[BCOL + q];
+}
+
+template <typename T, int RS, int BCOL>
+__global__ void k_gather_tangent_light(int n_light, const int32_t* __restrict__ light, const int32_t* __restrict__ bptr,
+                                       const int32_t* __restrict__ contrib, const T* __restrict__ rec,
+                                       T* __restrict__ K) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_light) return;
+  const int b = light[j];
   T acc[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] = T(0);
-  if (b < nnzb) {
-    for (int x = bptr[b]; x < bptr[b + 1]; ++x) {
-      const int code = contrib[x], k = (code >> 2) & 3, l = code & 3;
-      T r[RS];
-      if (RS == 16) {
-        load_rec<T, 16>(rec + (long long)(code >> 4) * RS, r);
-      } else {
+  for (int x = bptr[b]; x < bptr[b + 1]; ++x) add_contrib<T, RS, BCOL>(rec, contrib[x], acc);
 #pragma unroll
-        for (int q = 0; q < RS; ++q) r[q] = rec[(long long)(code >> 4) * RS + q];
-      }
-      const T w = shape_c<T>(r[0], r[1], k) * shape_c<T>(r[0], r[1], l);
+  for (int q = 0; q < 9; ++q) K[9LL * b + q] = acc[q];
+}
+
+template <typename T, int RS, int BCOL>
+__global__ void k_gather_tangent_heavy(int n_heavy, const int32_t* __restrict__ heavy, const int32_t* __restrict__ bptr,
+                                       const int32_t* __restrict__ contrib, const T* __restrict__ rec,
+                                       T* __restrict__ K) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= n_heavy) return;
+  const int b = heavy[w];
+  T acc[9];
 #pragma unroll
-      for (int q = 0; q < 9; ++q) acc[q] += w * r[bcol + q];
-    }
-  }
+  for (int q = 0; q < 9; ++q) acc[q] = T(0);
+  for (int x = bptr[b] + lane; x < bptr[b + 1]; x += 32) add_contrib<T, RS, BCOL>(rec, contrib[x], acc);
 #pragma unroll
-  for (int q = 0; q < 9; ++q) sk[threadIdx.x * 9 + q] = acc[q];
-  __syncthreads();
-  const long long nv = 9 * ((nnzb - b0) < GT_T ? (nnzb - b0) : GT_T);
-  for (int i = threadIdx.x; i < nv; i += GT_T) K[9 * b0 + i] = sk[i];
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) acc[q] = __shfl_sync(0xffffffffu, acc[q], 0);  // lane 0 holds the totals
+  T v = acc[0];
+#pragma unroll
+  for (int q = 1; q < 9; ++q) if (lane == q) v = acc[q];
+  if (lane < 9) K[9LL * b + lane] = v;
+}
+
+__global__ void k_block_class(long long nnzb, const int32_t* __restrict__ bptr, int32_t* __restrict__ flag) {
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nnzb) flag[b] = (bptr[b + 1] - bptr[b]) >= HEAVY_MIN ? 1 : 0;
+  else if (b == nnzb) flag[b] = 0;
+}
+
+__global__ void k_block_split(long long nnzb, const int32_t* __restrict__ flag, const int32_t* __restrict__ hpos,
+                              int32_t* __restrict__ heavy, int32_t* __restrict__ light) {
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nnzb) return;
+  const int h = hpos[b];
+  if (flag[b]) heavy[h] = (int32_t)b; else light[b - h] = (int32_t)b;
 }
 
 struct Scratch {
@@ -349,6 +393,14 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
                                                                 bfill, pat->blk_ptr, pat->contrib, err);
   if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
   XK_CHECK_LAUNCH();
+  // heavy / light block lists
+  k_block_class<<<xk_blocks(nb + 1, 256), 256, 0, st>>>(nb, pat->blk_ptr, bcnt);
+  XK_CHECK_LAUNCH();
+  XK_TRY(xk_exclusive_scan_i32(bcnt, bfill, nb + 1, tot + 2, st));
+  if (nb > 0) k_block_split<<<xk_blocks(nb, 256), 256, 0, st>>>(nb, bcnt, bfill, pat->heavy, pat->light);
+  XK_CHECK_LAUNCH();
+  XK_TRY(fetch_i64(tot + 2, h + 2, 1, st));
+  pat->n_heavy = (int32_t)h[2];
   XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
   if (herr) return xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: inconsistent block pattern");
@@ -390,10 +442,10 @@ extern "C" xk_status xk_contact_gather_force(const xk_contact_pattern* pat, cons
   const int nn = pat->n_nodes;
   if (nn > 0) {
     if (precision == XK_FP64)
-      k_gather_force<double><<<xk_blocks(32LL * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const double*)rec, rs, c1, c2,
+      k_gather_force<double><<<xk_blocks((long long)GF_LANES * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const double*)rec, rs, c1, c2,
                                                                          base, scale, f_ext, fixed, out);
     else if (precision == XK_MIXED)
-      k_gather_force<float><<<xk_blocks(32LL * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const float*)rec, rs, c1, c2,
+      k_gather_force<float><<<xk_blocks((long long)GF_LANES * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const float*)rec, rs, c1, c2,
                                                                         base, scale, f_ext, fixed, out);
     else
       return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force: precision");
@@ -411,17 +463,30 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   const int rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
   if (pat->nnzb == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
-  const int nb = xk_blocks(pat->nnzb, GT_T);
+  const int nl = (int)(pat->nnzb - pat->n_heavy), nh = pat->n_heavy;
+  const int bl = xk_blocks(nl, 128), bh = xk_blocks(32LL * nh, 128);
   const bool comb = out_mode == XK_OUT_COMBINED;
+#define XK_GT(TT, RSV, BC)                                                                                      \
+  do {                                                                                                         \
+    if (nl > 0)                                                                                                \
+      k_gather_tangent_light<TT, RSV, BC><<<bl, 128, 0, st>>>(nl, pat->light, pat->blk_ptr, pat->contrib,      \
+                                                              (const TT*)rec, (TT*)Kc_vals);                   \
+    if (nh > 0)                                                                                                \
+      k_gather_tangent_heavy<TT, RSV, BC><<<bh, 128, 0, st>>>(nh, pat->heavy, pat->blk_ptr, pat->contrib,      \
+                                                              (const TT*)rec, (TT*)Kc_vals);                   \
+  } while (0)
   if (precision == XK_FP64) {
-    if (comb) k_gather_tangent<double, 16><<<nb, GT_T, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const double*)rec, c1, (double*)Kc_vals);
-    else k_gather_tangent<double, 32><<<nb, GT_T, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const double*)rec, c1, (double*)Kc_vals);
+    if (comb) XK_GT(double, 16, 5);
+    else if (c1 == 8) XK_GT(double, 32, 8);
+    else XK_GT(double, 32, 17);
   } else if (precision == XK_MIXED) {
-    if (comb) k_gather_tangent<float, 16><<<nb, GT_T, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const float*)rec, c1, (float*)Kc_vals);
-    else k_gather_tangent<float, 32><<<nb, GT_T, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib, (const float*)rec, c1, (float*)Kc_vals);
+    if (comb) XK_GT(float, 16, 5);
+    else if (c1 == 8) XK_GT(float, 32, 8);
+    else XK_GT(float, 32, 17);
   } else {
     return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: precision");
   }
+#undef XK_GT
   XK_CHECK_LAUNCH();
   return XK_OK;
 }

@@ -562,7 +562,11 @@ XK_D void narrow32(const float* __restrict__ n32, const int* nd, df R, float& s,
   df x[4][3];
   for (int k = 0; k < 4; ++k) {
     const float* N = n32 + (long long)nd[k] * XK_NODE32_STRIDE;
-    for (int c = 0; c < 3; ++c) x[k][c] = {N[c], N[3 + c]};
+    const float4 p0 = __ldg(reinterpret_cast<const float4*>(N));
+    const float2 p1 = __ldg(reinterpret_cast<const float2*>(N + 4));
+    x[k][0] = {p0.x, p0.w};
+    x[k][1] = {p0.y, p1.x};
+    x[k][2] = {p0.z, p1.y};
   }
   float fa[3], fb[3], fw[3];
   for (int c = 0; c < 3; ++c) {
@@ -682,7 +686,7 @@ XK_D void store3f(float* base, long long stride, long long i, const float* v) {
   base[2 * stride + i] = v[2];
 }
 
-__global__ void __launch_bounds__(PAIR_T) k_pair_other32(xk_mesh m, xk_pairs p, xk_pairs32 q,
+__global__ void __launch_bounds__(PAIR_T, 3) k_pair_other32(xk_mesh m, xk_pairs p, xk_pairs32 q,
                                                          const int32_t* __restrict__ others, int n_o,
                                                          const float* __restrict__ n32, const float* __restrict__ e32) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
@@ -703,7 +707,7 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_other32(xk_mesh m, xk_pairs p, 
   store3f(q.t2, cq, i, t2);
 }
 
-__global__ void __launch_bounds__(PAIR_T) k_pair_member32(xk_mesh m, xk_pairs p, xk_pairs32 q,
+__global__ void __launch_bounds__(PAIR_T, 3) k_pair_member32(xk_mesh m, xk_pairs p, xk_pairs32 q,
                                                           const int32_t* __restrict__ members,
                                                           const int32_t* __restrict__ mnodes, int n_m,
                                                           const float* __restrict__ n32, const float* __restrict__ e32,
@@ -754,8 +758,8 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_member32(xk_mesh m, xk_pairs p,
     }
     float du[4][3];
     for (int k = 0; k < 4; ++k) {
-      const float* N = n32 + (long long)nd[k] * XK_NODE32_STRIDE + 12;
-      du[k][0] = N[0]; du[k][1] = N[1]; du[k][2] = N[2];
+      const float4 d4 = __ldg(reinterpret_cast<const float4*>(n32 + (long long)nd[k] * XK_NODE32_STRIDE + 12));
+      du[k][0] = d4.x; du[k][1] = d4.y; du[k][2] = d4.z;
     }
     float dr[3];
     for (int c = 0; c < 3; ++c) dr[c] = ((1.f - t) * du[2][c] + t * du[3][c]) - ((1.f - s) * du[0][c] + s * du[1][c]);
