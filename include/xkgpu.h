@@ -237,12 +237,20 @@ xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* r
 #define XK_NODE32_STRIDE 16 /* [x_hi(3), x_lo(3), u(6), u - u_ref(3), 0] per node */
 #define XK_ELEM32_STRIDE 16 /* [X_b - X_a (3), L0, R0 (9), r_hi, r_lo, 0] per element */
 
+/* Float copy of the pair state in slot order: the increment's members first
+ * (slot = member index of the contact pattern), then the other pairs, so that
+ * every per-iteration access is coalesced.  Node ids and the float-float
+ * radius sum r_a + r_b are stored per slot. */
 typedef struct {
-  int32_t n, cap;
+  int32_t n, cap, n_members;
+  int32_t* pair;           /* [cap] pair index of each slot */
+  int32_t* nodes;          /* [4*cap] nodes A0 A1 B0 B1 */
+  float* rad;              /* [2*cap] (hi, lo) of r_a + r_b */
   float *s, *t, *gap;
   float *normal, *t1, *t2; /* [3*cap] */
   float *p_n, *z_t;        /* z_t: [2*cap] */
   float *q_trial_norm, *dissipation, *k_pen, *k_t;
+  uint8_t *status, *stick;
 } xk_pairs32;
 
 /* Per iteration: node records for the mixed kernels from u (and u_ref, nullable). */
@@ -256,14 +264,17 @@ xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec, const floa
                              const xk_beam_plan* plan, const float* node32, double* f_int, float* K_vals,
                              xk_stream s);
 
-/* Copy the state fields of the pair table to / from its float copy (at increment boundaries). */
-xk_status xk_pairs_to32(const xk_pairs* p, xk_pairs32* q, xk_stream s);
+/* Gather the pair table into the slot-ordered float copy (after the contact
+ * pattern of the increment is built) and scatter it back (before the next
+ * detection). */
+xk_status xk_pairs_to32(const xk_mesh* m, const xk_pairs* p, const xk_contact_pattern* pat, xk_pairs32* q,
+                        xk_stream s);
 xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream s);
 
-/* xk_pair_step with all four stages and combined float records, on the float
- * state q (status and stick stay in p). */
-xk_status xk_pair_step32(const xk_mesh* m, xk_pairs* p, xk_pairs32* q, const xk_contact_pattern* pat,
-                         const float* node32, const float* elem32, const xk_contact_params* cp, float* rec,
+/* xk_pair_step with all four stages and combined float records on the float
+ * state: slots [0, n_members) are the members (record index = slot), the rest
+ * get the narrowphase only. */
+xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk_contact_params* cp, float* rec,
                          xk_stream s);
 
 /* Constraint Jacobian rows c_k n of the non-INACTIVE pairs in table order

@@ -386,10 +386,11 @@ __global__ void k_merge_old(xk_pairs old, const int32_t* __restrict__ cand, long
 
 struct Scratch {
   cudaStream_t s;
-  void* p[16];
+  void* p[24];
   int n = 0;
   template <typename T>
   xk_status get(T** out, long long count) {
+    if (n >= (int)(sizeof(p) / sizeof(p[0]))) return xk_set_error(XK_ERR_OVERFLOW, "scratch table full");
     if (count < 1) count = 1;
     cudaError_t e = cudaMallocAsync((void**)out, sizeof(T) * count, s);
     if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);

@@ -255,27 +255,42 @@ __global__ void k_gather_tangent_light(int n_light, const int32_t* __restrict__ 
   for (int q = 0; q < 9; ++q) K[9LL * b + q] = acc[q];
 }
 
+constexpr int GH_LANES = 8;
 template <typename T, int RS, int BCOL>
 __global__ void k_gather_tangent_heavy(int n_heavy, const int32_t* __restrict__ heavy, const int32_t* __restrict__ bptr,
                                        const int32_t* __restrict__ contrib, const T* __restrict__ rec,
                                        T* __restrict__ K) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (w >= n_heavy) return;
-  const int b = heavy[w];
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int w = gid / GH_LANES, sub = gid % GH_LANES;
+  const bool live = w < n_heavy;
+  const int b = live ? heavy[w] : 0;
   T acc[9];
 #pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] = T(0);
-  for (int x = bptr[b] + lane; x < bptr[b + 1]; x += 32) add_contrib<T, RS, BCOL>(rec, contrib[x], acc);
+  if (live)
+    for (int x = bptr[b] + sub; x < bptr[b + 1]; x += GH_LANES) add_contrib<T, RS, BCOL>(rec, contrib[x], acc);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
+  for (int o = GH_LANES / 2; o > 0; o >>= 1)
 #pragma unroll
-    for (int q = 0; q < 9; ++q) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+    for (int q = 0; q < 9; ++q) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o, GH_LANES);
 #pragma unroll
-  for (int q = 0; q < 9; ++q) acc[q] = __shfl_sync(0xffffffffu, acc[q], 0);  // lane 0 holds the totals
+  for (int q = 0; q < 9; ++q) acc[q] = __shfl_sync(0xffffffffu, acc[q], 0, GH_LANES);  // group lane 0: totals
   T v = acc[0];
 #pragma unroll
-  for (int q = 1; q < 9; ++q) if (lane == q) v = acc[q];
-  if (lane < 9) K[9LL * b + lane] = v;
+  for (int q = 1; q < 8; ++q) if (sub == q) v = acc[q];
+  if (live) {
+    K[9LL * b + sub] = v;
+    if (sub == 0) K[9LL * b + 8] = acc[8];
+  }
+}
+
+__global__ void k_light_keys(int n_light, const int32_t* __restrict__ light, const int32_t* __restrict__ bptr,
+                             unsigned long long* __restrict__ key, int32_t* __restrict__ val) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_light) return;
+  const int b = light[j];
+  key[j] = ((unsigned long long)(bptr[b + 1] - bptr[b]) << 32) | (unsigned)b;
+  val[j] = b;
 }
 
 __global__ void k_block_class(long long nnzb, const int32_t* __restrict__ bptr, int32_t* __restrict__ flag) {
@@ -294,10 +309,11 @@ __global__ void k_block_split(long long nnzb, const int32_t* __restrict__ flag, 
 
 struct Scratch {
   cudaStream_t s;
-  void* p[8];
+  void* p[24];
   int n = 0;
   template <typename T>
   xk_status get(T** out, long long count) {
+    if (n >= (int)(sizeof(p) / sizeof(p[0]))) return xk_set_error(XK_ERR_OVERFLOW, "scratch table full");
     if (count < 1) count = 1;
     cudaError_t e = cudaMallocAsync((void**)out, sizeof(T) * count, s);
     if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);
@@ -401,6 +417,18 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   XK_CHECK_LAUNCH();
   XK_TRY(fetch_i64(tot + 2, h + 2, 1, st));
   pat->n_heavy = (int32_t)h[2];
+  // light blocks ordered by contributor count, so that a warp's loops have equal trip counts
+  const long long nl = nb - h[2];
+  if (nl > 1) {
+    unsigned long long* lkey;
+    int32_t* lval;
+    XK_TRY(S.get(&lkey, nl));
+    XK_TRY(S.get(&lval, nl));
+    k_light_keys<<<xk_blocks(nl, 256), 256, 0, st>>>((int)nl, pat->light, pat->blk_ptr, lkey, lval);
+    XK_CHECK_LAUNCH();
+    XK_TRY(xk_radix_sort_u64((uint64_t*)lkey, lval, nl, 36, st));
+    XK_CUDA(cudaMemcpyAsync(pat->light, lval, sizeof(int32_t) * nl, cudaMemcpyDeviceToDevice, st));
+  }
   XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
   if (herr) return xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: inconsistent block pattern");
@@ -464,7 +492,7 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   if (pat->nnzb == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
   const int nl = (int)(pat->nnzb - pat->n_heavy), nh = pat->n_heavy;
-  const int bl = xk_blocks(nl, 128), bh = xk_blocks(32LL * nh, 128);
+  const int bl = xk_blocks(nl, 128), bh = xk_blocks((long long)GH_LANES * nh, 128);
   const bool comb = out_mode == XK_OUT_COMBINED;
 #define XK_GT(TT, RSV, BC)                                                                                      \
   do {                                                                                                         \

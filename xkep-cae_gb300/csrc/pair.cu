@@ -524,33 +524,51 @@ __global__ void k_nodes_prepare(xk_mesh m, const double* __restrict__ u, const d
   N[15] = 0.0f;
 }
 
-__global__ void k_pairs_convert(xk_pairs p, xk_pairs32 q, int to32) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
+__global__ void k_pairs_to32(xk_mesh m, xk_pairs p, xk_contact_pattern pat, xk_pairs32 q) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= q.n) return;
+  const bool mem = j < pat.n_members;
+  const int i = mem ? pat.members[j] : pat.others[j - pat.n_members];
   const long long cp = p.cap, cq = q.cap;
-  if (to32) {
-    q.s[i] = (float)p.s[i]; q.t[i] = (float)p.t[i]; q.gap[i] = (float)p.gap[i];
-    for (int c = 0; c < 3; ++c) {
-      q.normal[c * cq + i] = (float)p.normal[c * cp + i];
-      q.t1[c * cq + i] = (float)p.t1[c * cp + i];
-      q.t2[c * cq + i] = (float)p.t2[c * cp + i];
-    }
-    q.p_n[i] = (float)p.p_n[i];
-    q.z_t[i] = (float)p.z_t[i]; q.z_t[cq + i] = (float)p.z_t[cp + i];
-    q.q_trial_norm[i] = (float)p.q_trial_norm[i]; q.dissipation[i] = (float)p.dissipation[i];
-    q.k_pen[i] = (float)p.k_pen[i]; q.k_t[i] = (float)p.k_t[i];
-  } else {
-    p.s[i] = q.s[i]; p.t[i] = q.t[i]; p.gap[i] = q.gap[i];
-    for (int c = 0; c < 3; ++c) {
-      p.normal[c * cp + i] = q.normal[c * cq + i];
-      p.t1[c * cp + i] = q.t1[c * cq + i];
-      p.t2[c * cp + i] = q.t2[c * cq + i];
-    }
-    p.p_n[i] = q.p_n[i];
-    p.z_t[i] = q.z_t[i]; p.z_t[cp + i] = q.z_t[cq + i];
-    p.q_trial_norm[i] = q.q_trial_norm[i]; p.dissipation[i] = q.dissipation[i];
-    p.k_pen[i] = q.k_pen[i]; p.k_t[i] = q.k_t[i];
+  q.pair[j] = i;
+  const int ea = p.ea[i], eb = p.eb[i];
+  q.nodes[4LL * j] = m.conn[2 * ea];
+  q.nodes[4LL * j + 1] = m.conn[2 * ea + 1];
+  q.nodes[4LL * j + 2] = m.conn[2 * eb];
+  q.nodes[4LL * j + 3] = m.conn[2 * eb + 1];
+  const double R = m.radii[ea] + m.radii[eb];
+  const float rh = (float)R;
+  q.rad[2LL * j] = rh;
+  q.rad[2LL * j + 1] = (float)(R - (double)rh);
+  q.s[j] = (float)p.s[i]; q.t[j] = (float)p.t[i]; q.gap[j] = (float)p.gap[i];
+  for (int c = 0; c < 3; ++c) {
+    q.normal[c * cq + j] = (float)p.normal[c * cp + i];
+    q.t1[c * cq + j] = (float)p.t1[c * cp + i];
+    q.t2[c * cq + j] = (float)p.t2[c * cp + i];
   }
+  q.p_n[j] = (float)p.p_n[i];
+  q.z_t[j] = (float)p.z_t[i]; q.z_t[cq + j] = (float)p.z_t[cp + i];
+  q.q_trial_norm[j] = (float)p.q_trial_norm[i]; q.dissipation[j] = (float)p.dissipation[i];
+  q.k_pen[j] = (float)p.k_pen[i]; q.k_t[j] = (float)p.k_t[i];
+  q.status[j] = p.status[i]; q.stick[j] = p.stick[i];
+}
+
+__global__ void k_pairs_from32(xk_pairs32 q, xk_pairs p) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= q.n) return;
+  const int i = q.pair[j];
+  const long long cp = p.cap, cq = q.cap;
+  p.s[i] = q.s[j]; p.t[i] = q.t[j]; p.gap[i] = q.gap[j];
+  for (int c = 0; c < 3; ++c) {
+    p.normal[c * cp + i] = q.normal[c * cq + j];
+    p.t1[c * cp + i] = q.t1[c * cq + j];
+    p.t2[c * cp + i] = q.t2[c * cq + j];
+  }
+  p.p_n[i] = q.p_n[j];
+  p.z_t[i] = q.z_t[j]; p.z_t[cp + i] = q.z_t[cq + j];
+  p.q_trial_norm[i] = q.q_trial_norm[j]; p.dissipation[i] = q.dissipation[j];
+  p.k_pen[i] = q.k_pen[j]; p.k_t[i] = q.k_t[j];
+  p.status[i] = q.status[j]; p.stick[i] = q.stick[j];
 }
 
 XK_D float clamp01f(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
@@ -668,13 +686,6 @@ XK_D void narrow32(const float* __restrict__ n32, const int* nd, df R, float& s,
   for (int q = 0; q < 3; ++q) pt1_io[q] = t1[q];
 }
 
-XK_D df radius_sum(const float* __restrict__ e32, int ea, int eb) {
-  const float* A = e32 + (long long)ea * XK_ELEM32_STRIDE + 13;
-  const float* B = e32 + (long long)eb * XK_ELEM32_STRIDE + 13;
-  const df s = two_sum(A[0], B[0]);
-  return fast_two_sum(s.h, s.l + (A[1] + B[1]));
-}
-
 XK_D void load3f(const float* base, long long stride, long long i, float* v) {
   v[0] = base[i];
   v[1] = base[stride + i];
@@ -686,40 +697,36 @@ XK_D void store3f(float* base, long long stride, long long i, const float* v) {
   base[2 * stride + i] = v[2];
 }
 
-__global__ void __launch_bounds__(PAIR_T, 3) k_pair_other32(xk_mesh m, xk_pairs p, xk_pairs32 q,
-                                                         const int32_t* __restrict__ others, int n_o,
-                                                         const float* __restrict__ n32, const float* __restrict__ e32) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= n_o) return;
-  const int i = others[o];
+__global__ void __launch_bounds__(PAIR_T, 3) k_pair_other32(xk_pairs32 q, const float* __restrict__ n32) {
+  const int j = q.n_members + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= q.n) return;
   const long long cq = q.cap;
-  const int ea = p.ea[i], eb = p.eb[i];
-  const int nd[4] = {m.conn[2 * ea], m.conn[2 * ea + 1], m.conn[2 * eb], m.conn[2 * eb + 1]};
+  const int4 nd4 = __ldg(reinterpret_cast<const int4*>(q.nodes) + j);
+  const int nd[4] = {nd4.x, nd4.y, nd4.z, nd4.w};
+  const float2 R2 = __ldg(reinterpret_cast<const float2*>(q.rad) + j);
   float s, t, gap, n[3], t1[3], t2[3];
-  load3f(q.normal, cq, i, n);
-  load3f(q.t1, cq, i, t1);
-  narrow32(n32, nd, radius_sum(e32, ea, eb), s, t, gap, n, t1, t2);
-  q.s[i] = s;
-  q.t[i] = t;
-  q.gap[i] = gap;
-  store3f(q.normal, cq, i, n);
-  store3f(q.t1, cq, i, t1);
-  store3f(q.t2, cq, i, t2);
+  load3f(q.normal, cq, j, n);
+  load3f(q.t1, cq, j, t1);
+  narrow32(n32, nd, {R2.x, R2.y}, s, t, gap, n, t1, t2);
+  q.s[j] = s;
+  q.t[j] = t;
+  q.gap[j] = gap;
+  store3f(q.normal, cq, j, n);
+  store3f(q.t1, cq, j, t1);
+  store3f(q.t2, cq, j, t2);
 }
 
-__global__ void __launch_bounds__(PAIR_T, 3) k_pair_member32(xk_mesh m, xk_pairs p, xk_pairs32 q,
-                                                          const int32_t* __restrict__ members,
-                                                          const int32_t* __restrict__ mnodes, int n_m,
-                                                          const float* __restrict__ n32, const float* __restrict__ e32,
-                                                          xk_contact_params cp, float* __restrict__ rec) {
-  const int mi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (mi >= n_m) return;
-  const int i = members[mi];
+__global__ void __launch_bounds__(PAIR_T, 3) k_pair_member32(xk_pairs32 q, const float* __restrict__ n32,
+                                                             xk_contact_params cp, float* __restrict__ rec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // slot = member index
+  if (i >= q.n_members) return;
+  const int mi = i;
   const long long cq = q.cap;
-  int nd[4];
-  for (int k = 0; k < 4; ++k) nd[k] = mnodes[4LL * mi + k];
-  uint8_t status = p.status[i];
-  const df R = radius_sum(e32, p.ea[i], p.eb[i]);
+  const int4 nd4 = __ldg(reinterpret_cast<const int4*>(q.nodes) + i);
+  const int nd[4] = {nd4.x, nd4.y, nd4.z, nd4.w};
+  uint8_t status = q.status[i];
+  const float2 R2 = __ldg(reinterpret_cast<const float2*>(q.rad) + i);
+  const df R = {R2.x, R2.y};
   float s, t, gap, n[3], t1[3], t2[3];
   load3f(q.normal, cq, i, n);
   load3f(q.t1, cq, i, t1);
@@ -748,7 +755,7 @@ __global__ void __launch_bounds__(PAIR_T, 3) k_pair_member32(xk_mesh m, xk_pairs
   float kt = q.k_t[i];
   float zt0 = q.z_t[i], zt1 = q.z_t[cq + i];
   float qtn = q.q_trial_norm[i];
-  bool stick = p.stick[i] != 0;
+  bool stick = q.stick[i] != 0;
   const bool fproc = (p_n > 0.0f) && (mu > 0.0f);
   if (fproc) {
     if (q.k_pen[i] <= 0.0f) {
@@ -773,11 +780,11 @@ __global__ void __launch_bounds__(PAIR_T, 3) k_pair_member32(xk_mesh m, xk_pairs
     zt0 = r0; zt1 = r1; qtn = qn;
     q.z_t[i] = zt0;
     q.z_t[cq + i] = zt1;
-    p.stick[i] = stick ? 1 : 0;
+    q.stick[i] = stick ? 1 : 0;
     q.q_trial_norm[i] = qtn;
     q.dissipation[i] = r0 * d0 + r1 * d1;
     status = stick ? ST_ACTIVE : ST_SLIDING;
-    p.status[i] = status;
+    q.status[i] = status;
     if (sqrtf(r0 * r0 + r1 * r1) >= 1e-30f) {
       const float a0 = fabsf(r0) < 1e-30f ? 0.f : r0, a1 = fabsf(r1) < 1e-30f ? 0.f : r1;
       for (int k = 0; k < 3; ++k) vf[k] = a0 * t1[k] + a1 * t2[k];
@@ -953,40 +960,38 @@ extern "C" xk_status xk_nodes_prepare(const xk_mesh* m, const double* u, const d
   return XK_OK;
 }
 
-static xk_status pairs_convert(const xk_pairs* p, const xk_pairs32* q, int to32, xk_stream s) {
-  if (!p || !q) return xk_set_error(XK_ERR_ARG, "xk_pairs_to32/from32: null argument");
-  if (q->cap < p->n) return xk_set_error(XK_ERR_CAPACITY, "xk_pairs_to32/from32: float table capacity below n");
+extern "C" xk_status xk_pairs_to32(const xk_mesh* m, const xk_pairs* p, const xk_contact_pattern* pat, xk_pairs32* q,
+                                   xk_stream s) {
+  if (!m || !p || !pat || !q) return xk_set_error(XK_ERR_ARG, "xk_pairs_to32: null argument");
+  if ((long long)pat->n_members + pat->n_others != p->n)
+    return xk_set_error(XK_ERR_ARG, "xk_pairs_to32: the pattern was built for another pair table");
+  if (q->cap < p->n) return xk_set_error(XK_ERR_CAPACITY, "xk_pairs_to32: float table capacity below n");
+  q->n = p->n;
+  q->n_members = pat->n_members;
   if (p->n == 0) return XK_OK;
-  k_pairs_convert<<<xk_blocks(p->n, 256), 256, 0, (cudaStream_t)s>>>(*p, *q, to32);
+  k_pairs_to32<<<xk_blocks(p->n, 256), 256, 0, (cudaStream_t)s>>>(*m, *p, *pat, *q);
   XK_CHECK_LAUNCH();
   return XK_OK;
 }
 
-extern "C" xk_status xk_pairs_to32(const xk_pairs* p, xk_pairs32* q, xk_stream s) {
-  xk_status r = pairs_convert(p, q, 1, s);
-  if (r == XK_OK) q->n = p->n;
-  return r;
-}
-
 extern "C" xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream s) {
-  return pairs_convert(p, q, 0, s);
+  if (!q || !p) return xk_set_error(XK_ERR_ARG, "xk_pairs_from32: null argument");
+  if (q->n != p->n) return xk_set_error(XK_ERR_ARG, "xk_pairs_from32: table sizes differ");
+  if (q->n == 0) return XK_OK;
+  k_pairs_from32<<<xk_blocks(q->n, 256), 256, 0, (cudaStream_t)s>>>(*q, *p);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
 }
 
-extern "C" xk_status xk_pair_step32(const xk_mesh* m, xk_pairs* p, xk_pairs32* q, const xk_contact_pattern* pat,
-                                    const float* node32, const float* elem32, const xk_contact_params* cp, float* rec,
+extern "C" xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk_contact_params* cp, float* rec,
                                     xk_stream s) {
-  if (!m || !p || !q || !pat || !node32 || !elem32 || !cp) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: null argument");
-  if ((long long)pat->n_members + pat->n_others != p->n || q->n != p->n)
-    return xk_set_error(XK_ERR_ARG, "xk_pair_step32: pattern or float table built for another pair table");
-  if (pat->n_members > 0 && !rec) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: rec is null");
+  if (!q || !node32 || !cp) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: null argument");
+  if (q->n_members > 0 && !rec) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: rec is null");
   cudaStream_t st = (cudaStream_t)s;
-  if (pat->n_others > 0)
-    k_pair_other32<<<xk_blocks(pat->n_others, PAIR_T), PAIR_T, 0, st>>>(*m, *p, *q, pat->others, pat->n_others,
-                                                                        node32, elem32);
-  if (pat->n_members > 0)
-    k_pair_member32<<<xk_blocks(pat->n_members, PAIR_T), PAIR_T, 0, st>>>(*m, *p, *q, pat->members,
-                                                                          pat->member_nodes, pat->n_members, node32,
-                                                                          elem32, *cp, rec);
+  const int n_o = q->n - q->n_members;
+  if (n_o > 0) k_pair_other32<<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
+  if (q->n_members > 0)
+    k_pair_member32<<<xk_blocks(q->n_members, PAIR_T), PAIR_T, 0, st>>>(*q, node32, *cp, rec);
   XK_CHECK_LAUNCH();
   return XK_OK;
 }

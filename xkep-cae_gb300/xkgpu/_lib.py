@@ -38,9 +38,9 @@ class Pairs(C.Structure):
 
 
 class Pairs32(C.Structure):
-    _fields_ = [("n", C.c_int32), ("cap", C.c_int32)] + [
-        (n, vp) for n in ("s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm", "dissipation", "k_pen",
-                          "k_t")]
+    _fields_ = [("n", C.c_int32), ("cap", C.c_int32), ("n_members", C.c_int32)] + [
+        (n, vp) for n in ("pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
+                          "dissipation", "k_pen", "k_t", "status", "stick")]
 
 
 class BeamPlan(C.Structure):
@@ -89,9 +89,9 @@ SIGNATURES = {
     "xk_nodes_prepare": [P(Mesh), vp, vp, vp, vp],
     "xk_beam_prepare32": [P(Mesh), vp, vp, vp],
     "xk_beam_assemble32": [P(Mesh), P(Section), vp, P(BeamPlan), vp, vp, vp, vp],
-    "xk_pairs_to32": [P(Pairs), P(Pairs32), vp],
+    "xk_pairs_to32": [P(Mesh), P(Pairs), P(ContactPattern), P(Pairs32), vp],
     "xk_pairs_from32": [P(Pairs32), P(Pairs), vp],
-    "xk_pair_step32": [P(Mesh), P(Pairs), P(Pairs32), P(ContactPattern), vp, vp, P(ContactParams), vp, vp],
+    "xk_pair_step32": [P(Pairs32), vp, P(ContactParams), vp, vp],
 }
 NODE32_STRIDE = 16
 ELEM32_STRIDE = 16

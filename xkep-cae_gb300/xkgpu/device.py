@@ -287,12 +287,12 @@ class DevicePairTable:
         self.refresh()
 
 
-F32_FIELDS = {"s": 1, "t": 1, "gap": 1, "normal": 3, "t1": 3, "t2": 3, "p_n": 1, "z_t": 2, "q_trial_norm": 1,
-              "dissipation": 1, "k_pen": 1, "k_t": 1}
+F32_FIELDS = {"rad": 2, "s": 1, "t": 1, "gap": 1, "normal": 3, "t1": 3, "t2": 3, "p_n": 1, "z_t": 2,
+              "q_trial_norm": 1, "dissipation": 1, "k_pen": 1, "k_t": 1}
 
 
 class DevicePairTable32:
-    """Float copy of the pair-state fields (``xk_pairs32``) for the mixed per-iteration kernels."""
+    """Slot-ordered float copy of the pair state (``xk_pairs32``) for the mixed per-iteration kernels."""
 
     def __init__(self, device):
         self.device = device
@@ -304,9 +304,16 @@ class DevicePairTable32:
         if cap <= self.cap:
             return
         cap = int(cap)
-        self.t = {k: torch.zeros(w * cap, dtype=torch.float32, device=self.device) for k, w in F32_FIELDS.items()}
+        t = {"pair": torch.zeros(cap, dtype=torch.int32, device=self.device),
+             "nodes": torch.zeros(4 * cap, dtype=torch.int32, device=self.device)}
+        t.update({k: torch.zeros(w * cap, dtype=torch.float32, device=self.device) for k, w in F32_FIELDS.items()})
+        t["status"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
+        t["stick"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
+        self.t = t
         self.cap = cap
-        self.c = L.Pairs32(0, cap, *(ptr(self.t[k]) for k in F32_FIELDS))
+        self.c = L.Pairs32(0, cap, 0, *(ptr(t[k]) for k in (
+            "pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
+            "dissipation", "k_pen", "k_t", "status", "stick")))
 
 
 # ----------------------------------------------------------------------------- contact pattern

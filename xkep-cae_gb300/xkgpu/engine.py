@@ -89,6 +89,12 @@ class AssemblyEngine:
         L.call("xk_beam_prepare32", C.byref(self.mesh.c), ptr(self.beam.elem_ref), ptr(self.elem32),
                stream_handle(stream))
 
+    def _to32(self, s):
+        self.pairs32.ensure(self.pairs.cap)
+        L.call("xk_pairs_to32", C.byref(self.mesh.c), C.byref(self.pairs.c), C.byref(self.pattern.c),
+               C.byref(self.pairs32.c), s)
+        self._state_in32 = True
+
     def sync_state(self, stream=None):
         """Bring the double pair table up to date with the float copy (mixed path)."""
         if self._state_in32:
@@ -125,9 +131,7 @@ class AssemblyEngine:
         L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), C.byref(self.cp), 1, s)
         self.pattern.build(self.pairs, stream)
         if self.precision == L.XK_MIXED:
-            self.pairs32.ensure(self.pairs.cap)
-            L.call("xk_pairs_to32", C.byref(self.pairs.c), C.byref(self.pairs32.c), s)
-            self._state_in32 = True
+            self._to32(s)
         if (self.rec.numel() != L.REC_STRIDE[L.XK_OUT_COMBINED] * self.pattern.cap_members
                 or self.K_c.numel() < 9 * self.pattern.cap_blocks):
             self._alloc_outputs()
@@ -162,12 +166,9 @@ class AssemblyEngine:
         pat = C.byref(self.pattern.c)
         if self.precision == L.XK_MIXED:
             if not self._state_in32:
-                self.pairs32.ensure(self.pairs.cap)
-                L.call("xk_pairs_to32", C.byref(self.pairs.c), C.byref(self.pairs32.c), s)
-                self._state_in32 = True
+                self._to32(s)
             L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u_ref), ptr(self.node32), s)
-            L.call("xk_pair_step32", C.byref(self.mesh.c), C.byref(self.pairs.c), C.byref(self.pairs32.c), pat,
-                   ptr(self.node32), ptr(self.elem32), C.byref(self.cp), ptr(self.rec), s)
+            L.call("xk_pair_step32", C.byref(self.pairs32.c), ptr(self.node32), C.byref(self.cp), ptr(self.rec), s)
         else:
             L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
                    C.byref(self.cp), L.XK_STAGE_ALL, self.precision, L.XK_OUT_COMBINED, ptr(self.rec), s)
