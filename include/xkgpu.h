@@ -183,9 +183,6 @@ typedef struct {
   int32_t* blk_row;      /* [cap_blocks] */
   int32_t* blk_ptr;      /* [cap_blocks+1] */
   int32_t* contrib;      /* [16*cap_members] (member << 4) | (k << 2) | l */
-  int32_t n_heavy;       /* blocks with more than 8 contributors */
-  int32_t* heavy;        /* [cap_blocks] block ids with many contributors, ascending */
-  int32_t* light;        /* [cap_blocks] the other block ids, ascending */
 } xk_contact_pattern;
 
 /* Returns XK_ERR_CAPACITY (with n_members, n_others, nnzb set) when a capacity

@@ -218,13 +218,14 @@ __global__ void k_gather_force(int n_nodes, const int32_t* __restrict__ ptr, con
   }
 }
 
-// Contributor counts are very uneven: a node's diagonal block and the blocks
-// of an element's own node pair collect every member at that node (~30 at the
-// 1027-wire strand), a cross block one or two.  Light blocks (<= 8
-// contributors) take a thread each, heavy blocks a warp each whose lanes split
-// the contributors and combine them by a fixed shuffle tree.
-constexpr int HEAVY_MIN = 9;
-
+// Contributor counts are very uneven: 61% of the blocks of a strand have one
+// contributor, a node's diagonal block up to ~36.  A warp therefore owns 32
+// consecutive blocks and spreads their contributors evenly over its lanes
+// (32 per round): each lane forms c_k c_l B of one contributor, a segmented
+// inclusive scan over the lanes (fixed shuffle tree, segments = blocks) sums
+// each block's run within the round, the run's last lane adds it to the
+// block's shared-memory accumulator, and after the last round the warp stores
+// its 32 x 9 values contiguously.  Every sum is taken in a fixed order.
 template <typename T, int RS, int BCOL>
 XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
   const int k = (code >> 2) & 3, l = code & 3;
@@ -240,71 +241,65 @@ XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
   for (int q = 0; q < 9; ++q) acc[q] += w * r[BCOL + q];
 }
 
-template <typename T, int RS, int BCOL>
-__global__ void k_gather_tangent_light(int n_light, const int32_t* __restrict__ light, const int32_t* __restrict__ bptr,
-                                       const int32_t* __restrict__ contrib, const T* __restrict__ rec,
-                                       T* __restrict__ K) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n_light) return;
-  const int b = light[j];
-  T acc[9];
-#pragma unroll
-  for (int q = 0; q < 9; ++q) acc[q] = T(0);
-  for (int x = bptr[b]; x < bptr[b + 1]; ++x) add_contrib<T, RS, BCOL>(rec, contrib[x], acc);
-#pragma unroll
-  for (int q = 0; q < 9; ++q) K[9LL * b + q] = acc[q];
-}
+constexpr int GT_WARPS = 4;
 
-constexpr int GH_LANES = 8;
 template <typename T, int RS, int BCOL>
-__global__ void k_gather_tangent_heavy(int n_heavy, const int32_t* __restrict__ heavy, const int32_t* __restrict__ bptr,
-                                       const int32_t* __restrict__ contrib, const T* __restrict__ rec,
-                                       T* __restrict__ K) {
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int w = gid / GH_LANES, sub = gid % GH_LANES;
-  const bool live = w < n_heavy;
-  const int b = live ? heavy[w] : 0;
-  T acc[9];
+__global__ void __launch_bounds__(32 * GT_WARPS) k_gather_tangent(long long nnzb, const int32_t* __restrict__ bptr,
+                                                                 const int32_t* __restrict__ contrib,
+                                                                 const T* __restrict__ rec, T* __restrict__ K) {
+  __shared__ T acc[GT_WARPS][32 * 9];
+  __shared__ int ptr_s[GT_WARPS][33];
+  const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long b0 = ((long long)blockIdx.x * GT_WARPS + wl) * 32;
+  if (b0 >= nnzb) return;  // whole warp
+  const int nblk = (int)((nnzb - b0) < 32 ? (nnzb - b0) : 32);
+  T* A = acc[wl];
+  int* P = ptr_s[wl];
 #pragma unroll
-  for (int q = 0; q < 9; ++q) acc[q] = T(0);
-  if (live)
-    for (int x = bptr[b] + sub; x < bptr[b + 1]; x += GH_LANES) add_contrib<T, RS, BCOL>(rec, contrib[x], acc);
+  for (int q = 0; q < 9; ++q) A[q * 32 + lane] = T(0);
+  P[lane] = bptr[b0 + (lane < nblk ? lane : nblk)];
+  if (lane == 0) P[32] = bptr[b0 + nblk];
+  __syncwarp();
+  const int x0 = P[0], x1 = P[nblk];
+  for (int base = x0; base < x1; base += 32) {
+    const int x = base + lane;
+    const bool valid = x < x1;
+    // block slot of contribution x: the last slot whose start is <= x
+    int slot = 0;
+    if (valid) {
+      int lo = 0, hi = nblk - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P[mid] <= x) lo = mid; else hi = mid - 1;
+      }
+      slot = lo;
+    }
+    T v[9];
 #pragma unroll
-  for (int o = GH_LANES / 2; o > 0; o >>= 1)
+    for (int q = 0; q < 9; ++q) v[q] = T(0);
+    if (valid) add_contrib<T, RS, BCOL>(rec, contrib[x], v);
+    const int prev_slot = __shfl_up_sync(0xffffffffu, slot, 1);
+    const bool head = valid && (lane == 0 || prev_slot != slot);
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const int seg_start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
 #pragma unroll
-    for (int q = 0; q < 9; ++q) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o, GH_LANES);
+    for (int d = 1; d < 32; d <<= 1) {
 #pragma unroll
-  for (int q = 0; q < 9; ++q) acc[q] = __shfl_sync(0xffffffffu, acc[q], 0, GH_LANES);  // group lane 0: totals
-  T v = acc[0];
+      for (int q = 0; q < 9; ++q) {
+        const T y = __shfl_up_sync(0xffffffffu, v[q], d);
+        if (lane - d >= seg_start) v[q] += y;
+      }
+    }
+    const int next_slot = __shfl_down_sync(0xffffffffu, slot, 1);
+    const bool next_valid = __shfl_down_sync(0xffffffffu, (int)valid, 1) != 0;
+    const bool tail = valid && (lane == 31 || !next_valid || next_slot != slot);
+    if (tail) {
 #pragma unroll
-  for (int q = 1; q < 8; ++q) if (sub == q) v = acc[q];
-  if (live) {
-    K[9LL * b + sub] = v;
-    if (sub == 0) K[9LL * b + 8] = acc[8];
+      for (int q = 0; q < 9; ++q) A[slot * 9 + q] += v[q];
+    }
+    __syncwarp();
   }
-}
-
-__global__ void k_light_keys(int n_light, const int32_t* __restrict__ light, const int32_t* __restrict__ bptr,
-                             unsigned long long* __restrict__ key, int32_t* __restrict__ val) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n_light) return;
-  const int b = light[j];
-  key[j] = ((unsigned long long)(bptr[b + 1] - bptr[b]) << 32) | (unsigned)b;
-  val[j] = b;
-}
-
-__global__ void k_block_class(long long nnzb, const int32_t* __restrict__ bptr, int32_t* __restrict__ flag) {
-  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < nnzb) flag[b] = (bptr[b + 1] - bptr[b]) >= HEAVY_MIN ? 1 : 0;
-  else if (b == nnzb) flag[b] = 0;
-}
-
-__global__ void k_block_split(long long nnzb, const int32_t* __restrict__ flag, const int32_t* __restrict__ hpos,
-                              int32_t* __restrict__ heavy, int32_t* __restrict__ light) {
-  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nnzb) return;
-  const int h = hpos[b];
-  if (flag[b]) heavy[h] = (int32_t)b; else light[b - h] = (int32_t)b;
+  for (int i = lane; i < 9 * nblk; i += 32) K[9 * b0 + i] = A[i];
 }
 
 struct Scratch {
@@ -409,26 +404,6 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
                                                                 bfill, pat->blk_ptr, pat->contrib, err);
   if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
   XK_CHECK_LAUNCH();
-  // heavy / light block lists
-  k_block_class<<<xk_blocks(nb + 1, 256), 256, 0, st>>>(nb, pat->blk_ptr, bcnt);
-  XK_CHECK_LAUNCH();
-  XK_TRY(xk_exclusive_scan_i32(bcnt, bfill, nb + 1, tot + 2, st));
-  if (nb > 0) k_block_split<<<xk_blocks(nb, 256), 256, 0, st>>>(nb, bcnt, bfill, pat->heavy, pat->light);
-  XK_CHECK_LAUNCH();
-  XK_TRY(fetch_i64(tot + 2, h + 2, 1, st));
-  pat->n_heavy = (int32_t)h[2];
-  // light blocks ordered by contributor count, so that a warp's loops have equal trip counts
-  const long long nl = nb - h[2];
-  if (nl > 1) {
-    unsigned long long* lkey;
-    int32_t* lval;
-    XK_TRY(S.get(&lkey, nl));
-    XK_TRY(S.get(&lval, nl));
-    k_light_keys<<<xk_blocks(nl, 256), 256, 0, st>>>((int)nl, pat->light, pat->blk_ptr, lkey, lval);
-    XK_CHECK_LAUNCH();
-    XK_TRY(xk_radix_sort_u64((uint64_t*)lkey, lval, nl, 36, st));
-    XK_CUDA(cudaMemcpyAsync(pat->light, lval, sizeof(int32_t) * nl, cudaMemcpyDeviceToDevice, st));
-  }
   XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
   if (herr) return xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: inconsistent block pattern");
@@ -491,18 +466,11 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   const int rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
   if (pat->nnzb == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
-  const int nl = (int)(pat->nnzb - pat->n_heavy), nh = pat->n_heavy;
-  const int bl = xk_blocks(nl, 128), bh = xk_blocks((long long)GH_LANES * nh, 128);
+  const int nb = xk_blocks((pat->nnzb + 31) / 32, GT_WARPS);
   const bool comb = out_mode == XK_OUT_COMBINED;
-#define XK_GT(TT, RSV, BC)                                                                                      \
-  do {                                                                                                         \
-    if (nl > 0)                                                                                                \
-      k_gather_tangent_light<TT, RSV, BC><<<bl, 128, 0, st>>>(nl, pat->light, pat->blk_ptr, pat->contrib,      \
-                                                              (const TT*)rec, (TT*)Kc_vals);                   \
-    if (nh > 0)                                                                                                \
-      k_gather_tangent_heavy<TT, RSV, BC><<<bh, 128, 0, st>>>(nh, pat->heavy, pat->blk_ptr, pat->contrib,      \
-                                                              (const TT*)rec, (TT*)Kc_vals);                   \
-  } while (0)
+#define XK_GT(TT, RSV, BC)                                                                                  \
+  k_gather_tangent<TT, RSV, BC><<<nb, 32 * GT_WARPS, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib,        \
+                                                              (const TT*)rec, (TT*)Kc_vals)
   if (precision == XK_FP64) {
     if (comb) XK_GT(double, 16, 5);
     else if (c1 == 8) XK_GT(double, 32, 8);

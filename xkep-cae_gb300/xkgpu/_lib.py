@@ -64,7 +64,7 @@ class ContactPattern(C.Structure):
                 ("nnzb", C.c_int64), ("n_contrib", C.c_int64), ("cap_members", C.c_int64),
                 ("cap_others", C.c_int64), ("cap_blocks", C.c_int64)] + [
         (n, vp) for n in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row",
-                          "blk_ptr", "contrib")] + [("n_heavy", C.c_int32), ("heavy", vp), ("light", vp)]
+                          "blk_ptr", "contrib")]
 
 
 P = C.POINTER

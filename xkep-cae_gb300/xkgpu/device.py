@@ -350,7 +350,6 @@ class DeviceContactPattern:
     def _alloc_blocks(self, cap):
         cap = int(cap)
         self.col, self.blk_row, self.blk_ptr = self._i32(cap), self._i32(cap), self._i32(cap + 1)
-        self.heavy, self.light = self._i32(cap), self._i32(cap)
         self.cap_blocks = cap
 
     def _sync_struct(self):
@@ -358,7 +357,7 @@ class DeviceContactPattern:
         c.n_nodes = self.mesh.n_nodes
         c.cap_members, c.cap_others, c.cap_blocks = self.cap_members, self.cap_others, self.cap_blocks
         for k in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row", "blk_ptr",
-                  "contrib", "heavy", "light"):
+                  "contrib"):
             setattr(c, k, ptr(getattr(self, k)))
 
     def build(self, pairs: DevicePairTable, stream=None):
