@@ -432,6 +432,68 @@ def run_profile(args):
     print(json.dumps({"profile": args.profile, "workload": args.workload, **stats}))
 
 
+def run_breakdown(args):
+    """Warm per-phase times of one assembly (CUDA events around each phase, eager launches)."""
+    import ctypes as C
+
+    import torch
+
+    from xkgpu import _lib as L
+    from xkgpu import workloads as W
+    from xkgpu.device import ptr, stream_handle
+    from xkgpu.engine import AssemblyEngine
+
+    w = W.config_workload(args.workload, seed=0)
+    st = w.strand
+    out = {"workload": args.workload}
+    for prec in ("mixed", "fp64"):
+        eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=prec, **w.engine_kwargs())
+        u0 = torch.as_tensor(w.u, device="cuda")
+        u1 = u0 * 1.001
+        eng.detect(u0)
+        p = eng.precision
+        s = torch.cuda.current_stream()
+        sh = stream_handle(s)
+        pat = C.byref(eng.pattern.c)
+
+        def beam():
+            if p == L.XK_MIXED:
+                L.call("xk_beam_assemble32", C.byref(eng.mesh.c), C.byref(eng.beam.section), ptr(eng.elem32),
+                       C.byref(eng.beam.plan), ptr(eng.node32), ptr(eng.f_int), ptr(eng.K_beam), sh)
+            else:
+                eng.beam.assemble(u1, p, eng.f_int, eng.K_beam, s)
+
+        phases = {
+            "pair_step": lambda: eng.pair_step(u1, u0, s),
+            "beam": beam,
+            "force_gather+norm": lambda: L.call("xk_contact_gather_force", pat, ptr(eng.rec), p, L.XK_OUT_COMBINED,
+                                                L.XK_WHICH_COMBINED, ptr(eng.f_int), -1.0, None, None, ptr(eng.R),
+                                                ptr(eng.norm2), sh),
+            "tangent_gather_lanes": lambda: L.call("xk_contact_gather_tangent", pat, ptr(eng.rec), p,
+                                                   L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_LANES,
+                                                   ptr(eng.K_c), sh),
+            "tangent_gather_chunks": lambda: L.call("xk_contact_gather_tangent", pat, ptr(eng.rec), p,
+                                                    L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_CHUNKS,
+                                                    ptr(eng.K_c), sh),
+            "assemble": lambda: eng.assemble(u1, u0, stream=s),
+        }
+        res = {}
+        for name, fn in phases.items():
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            for _ in range(args.steps):
+                fn()
+            b.record(s)
+            torch.cuda.synchronize()
+            res[name] = a.elapsed_time(b) / args.steps
+        out[prec] = {k: round(v, 4) for k, v in res.items()}
+        del eng
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -442,7 +504,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
                     help="profiling driver: detect once, then --steps eager assemblies, no timing")
+    ap.add_argument("--breakdown", action="store_true", help="warm per-phase times (ms) of one assembly")
     args = ap.parse_args()
+    if args.breakdown:
+        run_breakdown(args)
+        return
     if args.profile:
         run_profile(args)
         return

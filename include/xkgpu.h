@@ -221,9 +221,15 @@ xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec
 
 /* K_c block values (9 per block, double|float, nnzb blocks): sum over each
  * block's contributors of c_k c_l B; which selects B_n - B_f (combined
- * records), B_n or B_f (split records). */
+ * records), B_n or B_f (split records).  variant picks the reduction schedule
+ * (0 default, 1 one contributor per lane, 2 chunks of contributors per lane);
+ * all give the same values for a given precision up to rounding order, each
+ * deterministic. */
+#define XK_GATHER_DEFAULT 0
+#define XK_GATHER_LANES 1
+#define XK_GATHER_CHUNKS 2
 xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* rec, int precision, int out_mode,
-                                    int which, void* Kc_vals, xk_stream s);
+                                    int which, int variant, void* Kc_vals, xk_stream s);
 
 /* ------------------------------------------- mixed-precision fast path
  * The per-iteration kernels of the mixed path execute no double-precision

@@ -270,3 +270,30 @@ def test_mixed_engine_vs_fp64_strand37():
         h64, hmx = e64.pair_state(), emx.pair_state()
         assert np.array_equal(h64["status"], hmx["status"])
         assert rel_err(hmx["gap"], h64["gap"]) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tangent_gather_schedules_agree(precision):
+    """Both contact-tangent reduction schedules give the same K_c, each deterministically."""
+    import ctypes as C
+
+    from xkgpu import workloads as W
+    from xkgpu.device import ptr, stream_handle
+
+    w = W.config_workload("strand37", seed=5)
+    st = w.strand
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=precision, **w.engine_kwargs())
+    u0 = _dev(w.u)
+    eng.detect(u0)
+    eng.assemble(u0 * 1.001, u0)
+    nb = eng.pattern.nnzb
+    outs = []
+    for v in (L.XK_GATHER_LANES, L.XK_GATHER_CHUNKS, L.XK_GATHER_LANES):
+        K = torch.zeros_like(eng.K_c)
+        L.call("xk_contact_gather_tangent", C.byref(eng.pattern.c), ptr(eng.rec), eng.precision, L.XK_OUT_COMBINED,
+               L.XK_WHICH_COMBINED, v, ptr(K), stream_handle(None))
+        torch.cuda.synchronize()
+        outs.append(K[: 9 * nb].double().cpu().numpy())
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert rel_err(outs[1], outs[0]) < tol
+    assert np.array_equal(outs[0], outs[2])

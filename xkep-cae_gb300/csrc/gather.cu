@@ -218,14 +218,6 @@ __global__ void k_gather_force(int n_nodes, const int32_t* __restrict__ ptr, con
   }
 }
 
-// Contributor counts are very uneven: 61% of the blocks of a strand have one
-// contributor, a node's diagonal block up to ~36.  A warp therefore owns 32
-// consecutive blocks and spreads their contributors evenly over its lanes
-// (32 per round): each lane forms c_k c_l B of one contributor, a segmented
-// inclusive scan over the lanes (fixed shuffle tree, segments = blocks) sums
-// each block's run within the round, the run's last lane adds it to the
-// block's shared-memory accumulator, and after the last round the warp stores
-// its 32 x 9 values contiguously.  Every sum is taken in a fixed order.
 template <typename T, int RS, int BCOL>
 XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
   const int k = (code >> 2) & 3, l = code & 3;
@@ -241,16 +233,20 @@ XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
   for (int q = 0; q < 9; ++q) acc[q] += w * r[BCOL + q];
 }
 
-constexpr int GT_WARPS = 4;
-
+// Variant "lanes": a warp owns 32 consecutive blocks and spreads their
+// contributors one per lane (32 per round); a segmented inclusive scan over
+// the lanes (fixed shuffle tree, segments = blocks) sums each block's run in
+// the round and the run's last lane adds it to the block's shared-memory
+// accumulator.  Fewer serial steps per lane than the chunked variant below,
+// more shuffles per contributor.
 template <typename T, int RS, int BCOL>
-__global__ void __launch_bounds__(32 * GT_WARPS) k_gather_tangent(long long nnzb, const int32_t* __restrict__ bptr,
-                                                                 const int32_t* __restrict__ contrib,
-                                                                 const T* __restrict__ rec, T* __restrict__ K) {
-  __shared__ T acc[GT_WARPS][32 * 9];
-  __shared__ int ptr_s[GT_WARPS][33];
+__global__ void __launch_bounds__(128) k_gather_tangent_lanes(long long nnzb, const int32_t* __restrict__ bptr,
+                                                             const int32_t* __restrict__ contrib,
+                                                             const T* __restrict__ rec, T* __restrict__ K) {
+  __shared__ T acc[4][32 * 9];
+  __shared__ int ptr_s[4][33];
   const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long b0 = ((long long)blockIdx.x * GT_WARPS + wl) * 32;
+  const long long b0 = ((long long)blockIdx.x * 4 + wl) * 32;
   if (b0 >= nnzb) return;  // whole warp
   const int nblk = (int)((nnzb - b0) < 32 ? (nnzb - b0) : 32);
   T* A = acc[wl];
@@ -264,7 +260,6 @@ __global__ void __launch_bounds__(32 * GT_WARPS) k_gather_tangent(long long nnzb
   for (int base = x0; base < x1; base += 32) {
     const int x = base + lane;
     const bool valid = x < x1;
-    // block slot of contribution x: the last slot whose start is <= x
     int slot = 0;
     if (valid) {
       int lo = 0, hi = nblk - 1;
@@ -296,6 +291,125 @@ __global__ void __launch_bounds__(32 * GT_WARPS) k_gather_tangent(long long nnzb
     if (tail) {
 #pragma unroll
       for (int q = 0; q < 9; ++q) A[slot * 9 + q] += v[q];
+    }
+    __syncwarp();
+  }
+  for (int i = lane; i < 9 * nblk; i += 32) K[9 * b0 + i] = A[i];
+}
+
+// Variant "chunks" (default for double): Contributor counts are very uneven: 61% of the blocks of a strand have one
+// contributor, a node's diagonal block up to ~36.  A warp owns 32 consecutive
+// blocks and cuts their contributor list into chunks of GT_CH, one per lane
+// (a round covers 32 * GT_CH contributors).  A lane sums its chunk serially;
+// a block whose contributors end inside the chunk is added to the block's
+// shared-memory accumulator by that lane, with the partial sums of the lanes
+// before it (a segmented inclusive scan of the lanes' last partial sums over
+// a fixed shuffle tree).  After the last round the warp stores its 32 x 9
+// values contiguously.  Every sum is taken in a fixed order.
+constexpr int GT_WARPS = 4;
+constexpr int GT_CH = 4;
+
+template <typename T, int RS, int BCOL>
+__global__ void __launch_bounds__(32 * GT_WARPS) k_gather_tangent(long long nnzb, const int32_t* __restrict__ bptr,
+                                                                 const int32_t* __restrict__ contrib,
+                                                                 const T* __restrict__ rec, T* __restrict__ K) {
+  __shared__ T acc[GT_WARPS][32 * 9];
+  __shared__ int ptr_s[GT_WARPS][33];
+  const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long b0 = ((long long)blockIdx.x * GT_WARPS + wl) * 32;
+  if (b0 >= nnzb) return;  // whole warp
+  const int nblk = (int)((nnzb - b0) < 32 ? (nnzb - b0) : 32);
+  T* A = acc[wl];
+  int* P = ptr_s[wl];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) A[q * 32 + lane] = T(0);
+  P[lane] = bptr[b0 + (lane < nblk ? lane : nblk)];
+  if (lane == 0) P[32] = bptr[b0 + nblk];
+  __syncwarp();
+  const int x0 = P[0], x1 = P[nblk];
+  for (int base = x0; base < x1; base += 32 * GT_CH) {
+    const int c0 = base + lane * GT_CH;
+    const int c1 = min(c0 + GT_CH, x1);
+    const bool has = c0 < c1;
+    // slot of the chunk's first contributor: last slot whose start <= c0
+    int slot = 0;
+    if (has) {
+      int lo = 0, hi = nblk - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P[mid] <= c0) lo = mid; else hi = mid - 1;
+      }
+      slot = lo;
+    }
+    const int first_slot = slot;
+    const bool first_open = has && P[slot] < c0;  // first block began before this chunk
+    T part[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) part[q] = T(0);
+    T head[9];  // sum over the first block's contributors in this chunk, once it is closed
+    bool head_closed = false;
+    for (int x = c0; x < c1; ++x) {
+      while (x >= P[slot + 1]) {  // the current block ends before x: close it
+        if (slot == first_slot && first_open) {
+#pragma unroll
+          for (int q = 0; q < 9; ++q) head[q] = part[q];
+          head_closed = true;
+        } else {
+#pragma unroll
+          for (int q = 0; q < 9; ++q) A[slot * 9 + q] += part[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 9; ++q) part[q] = T(0);
+        ++slot;
+      }
+      add_contrib<T, RS, BCOL>(rec, contrib[x], part);
+    }
+    const int last_slot = slot;
+    // lanes whose last block is open at the end of the chunk pass its partial on
+    // (lane 31 closes at the end of the round; the next round adds the rest)
+    const bool tail_open = has && lane < 31 && c1 < P[last_slot + 1] && c1 < x1;
+    // segmented inclusive scan over lanes of the last partials; a lane starts a
+    // segment unless its first block continues the previous lane's last block
+    const int prev_last = __shfl_up_sync(0xffffffffu, last_slot, 1);
+    const bool prev_open = __shfl_up_sync(0xffffffffu, (int)tail_open, 1) != 0;
+    const bool cont = lane > 0 && has && prev_open && prev_last == first_slot;
+    // value entering the scan: the lane's last partial when its last block is the
+    // continued first block, else its last partial alone (a new segment)
+    T v[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) v[q] = part[q];
+    const bool seg_head = !(cont && last_slot == first_slot && !head_closed);
+    const unsigned heads = __ballot_sync(0xffffffffu, seg_head);
+    const int seg_start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        const T y = __shfl_up_sync(0xffffffffu, v[q], d);
+        if (lane - d >= seg_start) v[q] += y;
+      }
+    }
+    // carry into this lane's first block = the previous lane's scanned value
+    T carry[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      const T y = __shfl_up_sync(0xffffffffu, v[q], 1);
+      carry[q] = cont ? y : T(0);
+    }
+    if (has) {
+      if (head_closed) {  // the first block ended inside this chunk
+#pragma unroll
+        for (int q = 0; q < 9; ++q) A[first_slot * 9 + q] += carry[q] + head[q];
+      }
+      if (!tail_open) {  // the last block ends here (or the round ends)
+        if (last_slot == first_slot && !head_closed) {
+#pragma unroll
+          for (int q = 0; q < 9; ++q) A[last_slot * 9 + q] += v[q];  // scanned: carry + own
+        } else {
+#pragma unroll
+          for (int q = 0; q < 9; ++q) A[last_slot * 9 + q] += part[q];
+        }
+      }
     }
     __syncwarp();
   }
@@ -459,7 +573,7 @@ extern "C" xk_status xk_contact_gather_force(const xk_contact_pattern* pat, cons
 }
 
 extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* rec, int precision,
-                                               int out_mode, int which, void* Kc_vals, xk_stream s) {
+                                               int out_mode, int which, int variant, void* Kc_vals, xk_stream s) {
   if (!pat || !rec || !Kc_vals) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: null argument");
   int c1, c2;
   XK_TRY(rec_columns(out_mode, which, true, &c1, &c2));
@@ -468,9 +582,17 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   cudaStream_t st = (cudaStream_t)s;
   const int nb = xk_blocks((pat->nnzb + 31) / 32, GT_WARPS);
   const bool comb = out_mode == XK_OUT_COMBINED;
-#define XK_GT(TT, RSV, BC)                                                                                  \
-  k_gather_tangent<TT, RSV, BC><<<nb, 32 * GT_WARPS, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib,        \
-                                                              (const TT*)rec, (TT*)Kc_vals)
+  // variant: 0 default (chunks for double, lanes for float), 1 lanes, 2 chunks
+  const bool chunks = variant == 2 || (variant == 0 && precision == XK_FP64);
+#define XK_GT(TT, RSV, BC)                                                                                   \
+  do {                                                                                                      \
+    if (chunks)                                                                                             \
+      k_gather_tangent<TT, RSV, BC><<<nb, 32 * GT_WARPS, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib,     \
+                                                                  (const TT*)rec, (TT*)Kc_vals);            \
+    else                                                                                                    \
+      k_gather_tangent_lanes<TT, RSV, BC><<<xk_blocks((pat->nnzb + 31) / 32, 4), 128, 0, st>>>(             \
+          pat->nnzb, pat->blk_ptr, pat->contrib, (const TT*)rec, (TT*)Kc_vals);                             \
+  } while (0)
   if (precision == XK_FP64) {
     if (comb) XK_GT(double, 16, 5);
     else if (c1 == 8) XK_GT(double, 32, 8);

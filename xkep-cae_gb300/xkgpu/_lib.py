@@ -18,6 +18,7 @@ XK_STAGE_ALL = 15
 XK_OUT_COMBINED, XK_OUT_SPLIT = 0, 1
 XK_WHICH_COMBINED, XK_WHICH_NORMAL, XK_WHICH_FRICTION = 0, 1, 2
 REC_STRIDE = {XK_OUT_COMBINED: 16, XK_OUT_SPLIT: 32}
+XK_GATHER_DEFAULT, XK_GATHER_LANES, XK_GATHER_CHUNKS = 0, 1, 2
 
 vp = C.c_void_p
 
@@ -83,7 +84,7 @@ SIGNATURES = {
                      vp],
     "xk_contact_gather_force": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, vp, C.c_double, vp, vp, vp, vp,
                                 vp],
-    "xk_contact_gather_tangent": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, vp, vp],
+    "xk_contact_gather_tangent": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp],
     "xk_constraint_jacobian": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
     "xk_norm2": [vp, C.c_int64, vp, vp],
     "xk_nodes_prepare": [P(Mesh), vp, vp, vp, vp],

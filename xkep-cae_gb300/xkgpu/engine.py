@@ -69,6 +69,9 @@ class AssemblyEngine:
         self._alloc_outputs()
         self.stats: dict = {}
         self.graph = None
+        self.gather_variant = L.XK_GATHER_DEFAULT
+        self.autotune = True
+        self._tuned_for = None
 
     # ------------------------------------------------------------------ buffers
     @property
@@ -157,7 +160,7 @@ class AssemblyEngine:
                ptr(self.f_int), -1.0, ptr(f_ext), ptr(fixed), ptr(self.R), ptr(self.norm2), s)
         if tangent and self.pattern.nnzb > 0:
             L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
-                   ptr(self.K_c), s)
+                   self.gather_variant, ptr(self.K_c), s)
         return self.R
 
     def pair_step(self, u: torch.Tensor, u_ref: torch.Tensor | None = None, stream=None):
@@ -173,6 +176,32 @@ class AssemblyEngine:
             L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
                    C.byref(self.cp), L.XK_STAGE_ALL, self.precision, L.XK_OUT_COMBINED, ptr(self.rec), s)
 
+    def tune(self, reps: int = 5) -> dict:
+        """Time the contact-tangent reduction schedules on the current records and keep the fastest.
+
+        Run after an ``assemble`` of the increment (the records must be current);
+        values do not depend on the choice beyond rounding order.
+        """
+        times = {}
+        if self.pattern.nnzb == 0:
+            return times
+        s = torch.cuda.current_stream()
+        for v in (L.XK_GATHER_LANES, L.XK_GATHER_CHUNKS):
+            for _ in range(2):
+                L.call("xk_contact_gather_tangent", C.byref(self.pattern.c), ptr(self.rec), self.precision,
+                       L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, v, ptr(self.K_c), stream_handle(s))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            for _ in range(reps):
+                L.call("xk_contact_gather_tangent", C.byref(self.pattern.c), ptr(self.rec), self.precision,
+                       L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, v, ptr(self.K_c), stream_handle(s))
+            b.record(s)
+            torch.cuda.synchronize()
+            times[v] = a.elapsed_time(b) / reps
+        self.gather_variant = min(times, key=times.get)
+        self._tuned_for = (self.pattern.version, self.precision)
+        return times
+
     def capture(self, u, u_ref=None, f_ext=None, fixed=None):
         """Record ``assemble`` on these (static) buffers as a CUDA graph."""
         st = torch.cuda.Stream(device=self.device)
@@ -180,6 +209,9 @@ class AssemblyEngine:
         with torch.cuda.stream(st):
             self.assemble(u, u_ref, f_ext, fixed, stream=st)  # warm-up outside capture
         torch.cuda.current_stream().wait_stream(st)
+        if self.autotune and self._tuned_for != (self.pattern.version, self.precision):
+            torch.cuda.synchronize()
+            self.tune()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, stream=st):
             self.assemble(u, u_ref, f_ext, fixed, stream=st)
