@@ -288,6 +288,26 @@ xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p, int32_t* r
                                  double* vals, int32_t* pair_index, int64_t cap, int64_t* n_rows,
                                  xk_stream s);
 
+/* xk_constraint_jacobian without any device allocation, for callers that may
+ * not allocate device memory while they run (a host whose device memory is all
+ * handed to its own pool, a loop that must not go through the allocator).  No
+ * counterpart in the reference: it is the same operation with the same
+ * results; only where the scratch lives differs.
+ *   - Scratch (a flag per pair, the scan's block sums, the active count) is a
+ *     static 4 MiB device array in the library, so the pair table may hold at
+ *     most XK_JACOBIAN_NOALLOC_MAX_PAIRS pairs; larger tables give XK_ERR_ARG
+ *     (use xk_constraint_jacobian for them).
+ *   - The first call on each device looks the array up (cudaGetSymbolAddress,
+ *     with that device current); make that call before work that must not see
+ *     a set-up step.
+ *   - The array is shared: calls on one device that overlap (two streams, two
+ *     host threads) race on it and must be serialised by the caller.
+ *   - Like xk_constraint_jacobian it synchronises the stream. */
+#define XK_JACOBIAN_NOALLOC_MAX_PAIRS 1048576
+xk_status xk_constraint_jacobian_noalloc(const xk_mesh* m, const xk_pairs* p, int32_t* rows, int32_t* cols,
+                                         double* vals, int32_t* pair_index, int64_t cap, int64_t* n_rows,
+                                         xk_stream s);
+
 /* Fixed-order FP64 sum of squares of x[0..n) into *out (device). */
 xk_status xk_norm2(const double* x, int64_t n, double* out, xk_stream s);
 

@@ -2,6 +2,8 @@
 // the factorised pair tangent.  One thread per pair; contributing pairs and
 // the rest run as two launches over the per-increment lists so that warps do
 // not diverge between the two kinds of work.
+#include <atomic>
+
 #include "xk_common.cuh"
 
 namespace {
@@ -949,6 +951,77 @@ extern "C" xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p,
   cudaFreeAsync(flag, st);
   cudaFreeAsync(tot, st);
   return r;
+}
+
+// ---------------------------------------------------------------------------
+// xk_constraint_jacobian_noalloc: the same kernels with their scratch in one
+// static device array instead of stream-ordered allocations, for callers that
+// may not allocate device memory while they run (a host that has handed all
+// of the device's memory to its own pool, or a loop that must not go through
+// the allocator).  Layout in int64 words: [0, 32) the active-pair count,
+// [32, 32 + JNA_TILES) the scan's block sums, then one int32 flag/offset per
+// pair.  Every word is written before it is read, so nothing has to start at
+// zero.  The array is shared by every call on a device: calls that overlap
+// (two streams or two host threads) race on it and must be serialised.
+namespace {
+constexpr long long JNA_MAX_PAIRS = XK_JACOBIAN_NOALLOC_MAX_PAIRS;
+constexpr long long JNA_TILES = 1024;  // block sums for up to 2,097,152 scanned elements
+constexpr long long JNA_WORDS = 32 + JNA_TILES + JNA_MAX_PAIRS / 2;
+static_assert(JNA_MAX_PAIRS % 2 == 0, "flags are packed two per word");
+
+static __device__ __align__(256) int64_t g_jna_scratch[JNA_WORDS];
+std::atomic<int64_t*> g_jna_ptr[64];
+
+// Address of this device's scratch array.  The first call on each device looks
+// the symbol up (which loads this module's device globals there); make it
+// before any work that must not see a set-up call.
+xk_status jna_scratch(int64_t** out) {
+  int dev = 0;
+  XK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return xk_set_error(XK_ERR_ARG, "device ordinal out of range");
+  int64_t* p = g_jna_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    XK_CUDA(cudaGetSymbolAddress((void**)&p, g_jna_scratch));
+    g_jna_ptr[dev].store(p, std::memory_order_release);
+  }
+  *out = p;
+  return XK_OK;
+}
+}  // namespace
+
+extern "C" xk_status xk_constraint_jacobian_noalloc(const xk_mesh* m, const xk_pairs* p, int32_t* rows,
+                                                    int32_t* cols, double* vals, int32_t* pair_index, int64_t cap,
+                                                    int64_t* n_rows, xk_stream s) {
+  if (!m || !p || !n_rows) return xk_set_error(XK_ERR_ARG, "xk_constraint_jacobian_noalloc: null argument");
+  *n_rows = 0;
+  if (p->n < 0 || (long long)p->n > JNA_MAX_PAIRS)
+    return xk_set_error(XK_ERR_ARG,
+                        "xk_constraint_jacobian_noalloc: pair table larger than XK_JACOBIAN_NOALLOC_MAX_PAIRS "
+                        "(1048576); use xk_constraint_jacobian");
+  if (xk_scan_tiles(p->n) > JNA_TILES) return xk_set_error(XK_ERR_ARG, "xk_constraint_jacobian_noalloc: scan tiles");
+  int64_t* scratch = nullptr;
+  xk_status r = jna_scratch(&scratch);
+  if (r != XK_OK) return r;
+  if (p->n == 0) return XK_OK;
+  cudaStream_t st = (cudaStream_t)s;
+  int64_t* tot = scratch;
+  int64_t* bsum = scratch + 32;
+  int32_t* flag = (int32_t*)(scratch + 32 + JNA_TILES);
+  k_active_flags<<<xk_blocks(p->n, 256), 256, 0, st>>>(*p, flag);
+  XK_CHECK_LAUNCH();
+  r = xk_exclusive_scan_i32_scratch(flag, flag, p->n, tot, bsum, JNA_TILES, st);
+  if (r != XK_OK) return r;
+  int64_t h = 0;
+  XK_CUDA(cudaMemcpyAsync(&h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaStreamSynchronize(st));
+  *n_rows = h;
+  if (h > cap) return xk_set_error(XK_ERR_CAPACITY, "xk_constraint_jacobian_noalloc: capacity below the number "
+                                                    "of active pairs");
+  if (h > 0) {
+    k_jacobian<<<xk_blocks(p->n, 256), 256, 0, st>>>(*m, *p, flag, rows, cols, vals, pair_index);
+    XK_CHECK_LAUNCH();
+  }
+  return XK_OK;
 }
 
 extern "C" xk_status xk_nodes_prepare(const xk_mesh* m, const double* u, const double* u_ref, float* node32,

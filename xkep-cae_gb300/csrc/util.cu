@@ -131,6 +131,23 @@ xk_status xk_exclusive_scan_i64(const int64_t* in, int64_t* out, long long n, in
   return scan_impl<int64_t, int64_t>(in, out, n, total_dev, s);
 }
 
+long long xk_scan_tiles(long long n) { return n <= 0 ? 0 : (n + SCAN_TILE - 1) / SCAN_TILE; }
+
+xk_status xk_exclusive_scan_i32_scratch(const int32_t* in, int32_t* out, long long n, int64_t* total_dev,
+                                        int64_t* bsum, long long bsum_cap, cudaStream_t s) {
+  if (n <= 0) {
+    if (total_dev) XK_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int64_t), s));
+    return XK_OK;
+  }
+  long long nb = xk_scan_tiles(n);
+  if (!bsum || nb > bsum_cap) return xk_set_error(XK_ERR_CAPACITY, "scan: block-sum scratch too small");
+  k_tile_sums<int32_t><<<(unsigned)nb, SCAN_T, 0, s>>>(in, n, bsum);
+  k_scan_bsums<<<1, SCAN_T, 0, s>>>(bsum, nb, total_dev);
+  k_tile_scan<int32_t, int32_t><<<(unsigned)nb, SCAN_T, 0, s>>>(in, out, n, bsum);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
 // --------------------------------------------------------------------------- radix sort
 
 namespace {

@@ -106,5 +106,11 @@ xk_status xk_exclusive_scan_i32(const int32_t* in, int32_t* out, long long n, in
                                 cudaStream_t s);
 xk_status xk_exclusive_scan_i64(const int64_t* in, int64_t* out, long long n, int64_t* total_dev,
                                 cudaStream_t s);
+// Number of block sums the scans use for n elements, and the int32 scan with a
+// caller-provided block-sum array of bsum_cap words (same kernels, same result;
+// allocates nothing).
+long long xk_scan_tiles(long long n);
+xk_status xk_exclusive_scan_i32_scratch(const int32_t* in, int32_t* out, long long n, int64_t* total_dev,
+                                        int64_t* bsum, long long bsum_cap, cudaStream_t s);
 // Stable LSD radix sort of 64-bit keys with 32-bit values; `bits` low key bits are sorted.
 xk_status xk_radix_sort_u64(uint64_t* keys, int32_t* vals, long long n, int bits, cudaStream_t s);

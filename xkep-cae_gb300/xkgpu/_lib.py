@@ -86,6 +86,7 @@ SIGNATURES = {
                                 vp],
     "xk_contact_gather_tangent": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp],
     "xk_constraint_jacobian": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
+    "xk_constraint_jacobian_noalloc": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
     "xk_norm2": [vp, C.c_int64, vp, vp],
     "xk_nodes_prepare": [P(Mesh), vp, vp, vp, vp],
     "xk_beam_prepare32": [P(Mesh), vp, vp, vp],
@@ -94,6 +95,7 @@ SIGNATURES = {
     "xk_pairs_from32": [P(Pairs32), P(Pairs), vp],
     "xk_pair_step32": [P(Pairs32), vp, P(ContactParams), vp, vp],
 }
+JACOBIAN_NOALLOC_MAX_PAIRS = 1048576
 NODE32_STRIDE = 16
 ELEM32_STRIDE = 16
 
