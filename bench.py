@@ -172,6 +172,18 @@ def pair_kernel_bytes(n_nodes, n_elems, n_others, n_members, mixed: bool):
     return 72 * n_nodes + 16 * n_elems + 156 * n_others + n_members * (264 + 128)
 
 
+def gather_tangent_bytes(n_members, n_contrib, nnzb, mixed: bool):
+    """Algorithmic DRAM bytes of one contact-tangent gather launch.
+
+    Each contributing pair's record is read once from DRAM (16 values: 64 B
+    float, 128 B double), each contributor list entry once (4 B), each block
+    pointer once (4 B) and each 3x3 block written once (36 B float, 72 B
+    double).  Re-reads of a record by the 16 blocks it feeds are L2 traffic.
+    """
+    w = 4 if mixed else 8
+    return 16 * w * n_members + 4 * n_contrib + 4 * (nnzb + 1) + 9 * w * nnzb
+
+
 # --------------------------------------------------------------------------- GPU arm
 
 
@@ -286,12 +298,34 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / 1e3 / k
 
+    def gather_kernel_time(eng, k):
+        s = torch.cuda.current_stream()
+        sh = stream_handle(s)
+        args_ = (C.byref(eng.pattern.c), ptr(eng.rec), eng.precision, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
+                 eng.gather_variant, ptr(eng.K_c), sh)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(3):
+            L.call("xk_contact_gather_tangent", *args_)
+        torch.cuda.synchronize()
+        a.record(s)
+        for _ in range(k):
+            L.call("xk_contact_gather_tangent", *args_)
+        b.record(s)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / k
+
     kreps = max(20, min(args.steps, 200))
     tk_mixed = pair_kernel_time(engines["mixed"], kreps)
     tk_fp64 = pair_kernel_time(engines["fp64"], kreps)
-    m = engines["mixed"].pattern.n_members
+    tg_mixed = gather_kernel_time(engines["mixed"], kreps)
+    tg_fp64 = gather_kernel_time(engines["fp64"], kreps)
+    pat = engines["mixed"].pattern
+    m = pat.n_members
     by_mixed = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, True)
     by_fp64 = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, False)
+    bg_mixed = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, True)
+    bg_fp64 = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, False)
+    variant_name = {L.XK_GATHER_LANES: "lanes", L.XK_GATHER_CHUNKS: "chunks"}
     peak, peak_kind = _peaks()
 
     # end to end through the public engine API with host buffers
@@ -360,21 +394,32 @@ def run_gpu(args, rank, world):
         "err_vs_fp64": err,
         "detect_ms": {"mixed": results["mixed"]["detect_ms"], "fp64": results["fp64"]["detect_ms"],
                       "first": results["mixed"]["detect_first_ms"]},
-        "roofline": {"bound": "hbm", "kernel": "pair step (mixed: k_nodes_prepare + k_pair_other32 + k_pair_member32; narrowphase, Huber, Coulomb, tangent)",
-                     "achieved": by_mixed / tk_mixed / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": by_mixed / tk_mixed / 1e9 / peak, "peak_kind": peak_kind,
-                     "bytes_per_launch": by_mixed, "launch_ms": 1e3 * tk_mixed, "traffic": None,
-                     "fp64_kernel": {"achieved": by_fp64 / tk_fp64 / 1e9, "launch_ms": 1e3 * tk_fp64,
-                                     "bytes_per_launch": by_fp64}},
+        "roofline": {"bound": "hbm",
+                     "kernel": "contact tangent gather (k_gather_tangent_lanes<float>, schedule "
+                               f"{variant_name.get(engines['mixed'].gather_variant, 'default')})",
+                     "achieved": bg_mixed / tg_mixed / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": bg_mixed / tg_mixed / 1e9 / peak, "peak_kind": peak_kind,
+                     "bytes_per_launch": bg_mixed, "launch_ms": 1e3 * tg_mixed, "traffic": None,
+                     "fp64_kernel": {"achieved": bg_fp64 / tg_fp64 / 1e9, "launch_ms": 1e3 * tg_fp64,
+                                     "bytes_per_launch": bg_fp64,
+                                     "schedule": variant_name.get(engines["fp64"].gather_variant, "default")},
+                     "pair_step": {"kernels": "k_nodes_prepare + k_pair_other32 + k_pair_member32 (narrowphase, "
+                                              "Huber, Coulomb, pair tangent)",
+                                   "achieved": by_mixed / tk_mixed / 1e9, "frac": by_mixed / tk_mixed / 1e9 / peak,
+                                   "bytes_per_launch": by_mixed, "launch_ms": 1e3 * tk_mixed,
+                                   "fp64": {"achieved": by_fp64 / tk_fp64 / 1e9, "launch_ms": 1e3 * tk_fp64,
+                                            "bytes_per_launch": by_fp64}}},
         "e2e": {"value": units / t_e2e * args.steps, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": per_launch * args.steps,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
-    tr = ROOT / "profiles" / "pair_kernel_traffic.json"
+    tr = ROOT / "profiles" / "dram_traffic.json"
     if tr.exists():
-        out["roofline"]["traffic"] = json.loads(tr.read_text()).get("bytes_per_launch_strand1027")
+        d = json.loads(tr.read_text())
+        out["roofline"]["traffic"] = d.get("k_gather_tangent_lanes_float", {}).get("bytes_per_launch")
+        out["roofline"]["pair_step"]["traffic"] = d.get("pair_step_mixed", {}).get("bytes_per_launch")
     return out
 
 
@@ -429,7 +474,10 @@ def run_profile(args):
     for _ in range(args.steps):
         eng.assemble(u1, u0)
     torch.cuda.synchronize()
-    print(json.dumps({"profile": args.profile, "workload": args.workload, **stats}))
+    pat = eng.pattern
+    print(json.dumps({"profile": args.profile, "workload": args.workload, **stats, "nnzb": pat.nnzb,
+                      "n_contrib": pat.n_contrib, "gather_variant": eng.gather_variant,
+                      "device_bytes_peak": torch.cuda.max_memory_allocated()}))
 
 
 def run_breakdown(args):

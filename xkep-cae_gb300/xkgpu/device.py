@@ -383,3 +383,7 @@ class DeviceContactPattern:
     @property
     def nnzb(self) -> int:
         return int(self.c.nnzb)
+
+    @property
+    def n_contrib(self) -> int:
+        return int(self.c.n_contrib)
