@@ -288,6 +288,58 @@ xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p, int32_t* r
                                  double* vals, int32_t* pair_index, int64_t cap, int64_t* n_rows,
                                  xk_stream s);
 
+/* ------------------------------------------------------------------------
+ * Learned pruning of broadphase candidates.  No counterpart in the reference:
+ * an MLP (XK_MLP_IN inputs -> 64 -> 64 -> 64 -> 1, ReLU, BF16 weights and
+ * activations, FP32 accumulation) scores each candidate pair; candidates below
+ * a threshold skip the pair table.  The exact broadphase + narrowphase stays
+ * the judge (AssemblyEngine runs it every N detections).  Parameters are one
+ * float vector of XK_MLP_PARAMS values: W1 (64 x 8), b1, W2 (64 x 64), b2,
+ * W3 (64 x 64), b3, w4 (64), b4.
+ * ---------------------------------------------------------------------- */
+#define XK_MLP_IN 8
+#define XK_MLP_HIDDEN 64
+#define XK_MLP_PARAMS 8961
+#define XK_MLP_ACT 192 /* a1, a2, a3 per sample */
+
+/* Features of candidate pairs cands[2*i], cands[2*i+1] at X + u (u may be
+ * null): midpoint separation, |cos| of the tangent angle, half lengths (all
+ * over r_a + r_b), layer distance, core flag, previous-step gap (from `old`,
+ * sorted by (ea, eb)) or its lower bound, and whether it exists.  feat: n x 8
+ * float; hist[i] = 1 if the pair is in `old` with contact history (status,
+ * p_n, k_pen or z_t set), such pairs are never pruned. */
+xk_status xk_prune_features(const xk_mesh* m, const double* u, const int32_t* cands, int64_t n,
+                            const xk_pairs* old, float* feat, uint8_t* hist, xk_stream s);
+
+/* Logits of n samples on the tensor cores (mma.sync BF16 -> FP32);
+ * params_bf16: XK_MLP_PARAMS bfloat16 values. */
+xk_status xk_mlp_forward(const uint16_t* params_bf16, const float* feat, int64_t n, float* logit, xk_stream s);
+
+/* Training: forward with stored activations (act: XK_MLP_ACT planes of n
+ * floats), backward of the weighted mean binary cross-entropy (dvec: 192
+ * planes of n; g: n; grad: XK_MLP_PARAMS, reduced in a fixed order; *loss on
+ * the device), Adam (also writes the bf16 copy when theta_bf16 != NULL). */
+xk_status xk_mlp_train_forward(const float* theta, const float* feat, int64_t n, float* act, float* logit,
+                               xk_stream s);
+xk_status xk_mlp_backward(const float* theta, const float* feat, const float* act, const float* logit,
+                          const float* y, const float* w, int64_t n, float* dvec, float* g, float* grad,
+                          float* loss, xk_stream s);
+xk_status xk_mlp_adam(float* theta, const float* grad, float* m, float* v, int step, double lr, double beta1,
+                      double beta2, double eps, uint16_t* theta_bf16, xk_stream s);
+xk_status xk_mlp_to_bf16(const float* theta, uint16_t* out, xk_stream s);
+
+/* Keep candidates with logit >= threshold or hist set (order kept), or with
+ * invert != 0 the others (the pruned ones); *n_kept on the host.
+ * Synchronises the stream. */
+xk_status xk_prune_select(const int32_t* cands, int64_t n, const float* logit, const uint8_t* hist,
+                          float threshold, int invert, int32_t* kept, int64_t* n_kept, xk_stream s);
+
+/* Copy `in` to `out` without its pristine pairs (INACTIVE, p_n = k_pen = 0,
+ * z_t = 0) that are not in the sorted list `kept`; order kept.  Synchronises
+ * the stream. */
+xk_status xk_pairs_drop_pristine(const xk_pairs* in, const int32_t* kept, int64_t n_kept, xk_pairs* out,
+                                 xk_stream s);
+
 /* xk_constraint_jacobian without any device allocation, for callers that may
  * not allocate device memory while they run (a host whose device memory is all
  * handed to its own pool, a loop that must not go through the allocator).  No

@@ -1,0 +1,146 @@
+"""CPU oracle of the pair-pruning MLP (test infrastructure only).
+
+The reference has no learned component; this file is the specification the GPU
+kernels are checked against.  Network: F = 8 inputs -> 64 -> 64 -> 64 -> 1,
+ReLU between layers, sigmoid output.  The forward pass rounds the weights, the
+inputs and every hidden activation to bfloat16 (round to nearest even) and
+accumulates in float32, as the GPU does; the backward pass is plain float32
+(no rounding of gradients); the ReLU derivative is taken where the (rounded)
+activation is positive.
+
+Parameters are one flat float32 vector in this order:
+W1 (64 x F, row-major), b1 (64), W2 (64 x 64), b2 (64), W3 (64 x 64), b3 (64), w4 (64), b4 (1).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+F, H = 8, 64
+SIZES = [("W1", (H, F)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)), ("b3", (H,)),
+         ("w4", (H,)), ("b4", (1,))]
+N_PARAMS = sum(int(np.prod(s)) for _, s in SIZES)
+
+
+def unpack(theta: np.ndarray) -> dict:
+    out, o = {}, 0
+    for k, s in SIZES:
+        n = int(np.prod(s))
+        out[k] = theta[o:o + n].reshape(s)
+        o += n
+    return out
+
+
+def bf16(x) -> np.ndarray:
+    """Round float32 to the nearest bfloat16 (ties to even), returned as float32."""
+    a = np.ascontiguousarray(x, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    out = r.astype(np.uint32).view(np.float32)
+    nan = np.isnan(a)
+    if nan.any():
+        out = out.copy()
+        out[nan] = np.nan
+    return out
+
+
+def init_params(seed: int = 0) -> np.ndarray:
+    """He-normal weights, zero biases (float32 master copy)."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for k, s in SIZES:
+        if k.startswith("b"):
+            parts.append(np.zeros(s, np.float32))
+        else:
+            fan_in = s[-1] if len(s) == 2 else H
+            parts.append((rng.normal(size=s) * np.sqrt(2.0 / fan_in)).astype(np.float32))
+    return np.concatenate([p.ravel() for p in parts]).astype(np.float32)
+
+
+def forward(theta: np.ndarray, X: np.ndarray, *, quantize: bool = True):
+    """Scores (logits) and the cached activations of a batch X (n x F).
+
+    quantize=False runs the same network unrounded in float64 (used to pin the
+    backward pass against finite differences).
+    """
+    if quantize:
+        q, dt = bf16, np.float32
+    else:
+        def q(a):
+            return np.asarray(a, np.float64)
+        dt = np.float64
+    p = {k: q(v) for k, v in unpack(np.asarray(theta, dt)).items()}
+    x0 = q(X)
+    z1 = x0 @ p["W1"].T + p["b1"]
+    a1 = q(np.maximum(z1, 0.0))
+    z2 = a1 @ p["W2"].T + p["b2"]
+    a2 = q(np.maximum(z2, 0.0))
+    z3 = a2 @ p["W3"].T + p["b3"]
+    a3 = q(np.maximum(z3, 0.0))
+    logit = a3 @ p["w4"] + p["b4"][0]
+    return logit.astype(dt), dict(x0=x0, a1=a1, a2=a2, a3=a3, z1=z1, z2=z2, z3=z3, p=p)
+
+
+def loss_and_grad(theta: np.ndarray, X: np.ndarray, y: np.ndarray, w: np.ndarray, *, quantize: bool = True):
+    """Weighted mean binary cross-entropy on the logits and its gradient (flat).
+
+    loss = sum_i w_i * (softplus(l_i) - y_i l_i) / n; d loss / d l_i = w_i (sigmoid(l_i) - y_i) / n.
+    With quantize=True the gradient passes through the bfloat16 rounding as the
+    identity (the rounded activations and weights are used in the chain rule).
+    """
+    dt = np.float32 if quantize else np.float64
+    n = X.shape[0]
+    logit, c = forward(theta, X, quantize=quantize)
+    p = c["p"]
+    lf = logit.astype(np.float64)
+    loss = float(np.sum(w * (np.logaddexp(0.0, lf) - y * lf)) / n)
+    g = (w * (1.0 / (1.0 + np.exp(-lf)) - y) / n).astype(dt)
+    grads = {"w4": c["a3"].T @ g, "b4": np.array([g.sum()], dt)}
+    d3 = np.outer(g, p["w4"]) * (c["a3"] > 0)
+    grads["W3"], grads["b3"] = d3.T @ c["a2"], d3.sum(0)
+    d2 = (d3 @ p["W3"]) * (c["a2"] > 0)
+    grads["W2"], grads["b2"] = d2.T @ c["a1"], d2.sum(0)
+    d1 = (d2 @ p["W2"]) * (c["a1"] > 0)
+    grads["W1"], grads["b1"] = d1.T @ c["x0"], d1.sum(0)
+    flat = np.concatenate([np.asarray(grads[k], dt).ravel() for k, _ in SIZES])
+    return loss, flat
+
+
+def adam_step(theta, grad, m, v, step: int, lr: float, b1=0.9, b2=0.999, eps=1e-8):
+    """One Adam update (bias-corrected), float32, returns the new (theta, m, v)."""
+    m = b1 * m + (1 - b1) * grad
+    v = b2 * v + (1 - b2) * grad * grad
+    mh = m / (1 - b1**step)
+    vh = v / (1 - b2**step)
+    return (theta - lr * mh / (np.sqrt(vh) + eps)).astype(np.float32), m.astype(np.float32), v.astype(np.float32)
+
+
+def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
+    """Per-candidate inputs (n x F), float32.
+
+    0: |m_a - m_b| / (r_a + r_b)              midpoint separation
+    1: |d_a . d_b| / (|d_a| |d_b|)            cosine of the tangent angle
+    2: (|d_a| + |d_b|) / (2 (r_a + r_b))      half lengths
+    3: min(|layer_a - layer_b|, 3) / 3        layer distance (0 without layers)
+    4: 1 if either layer is 0 (the core)
+    5: previous-step gap / (r_a + r_b), clipped to [-2, 8]; without one, the
+       lower bound (|m_a - m_b| - (|d_a| + |d_b|)/2 - r_a - r_b) / (r_a + r_b)
+    6: 1 if the previous-step gap exists
+    7: 0
+    """
+    rs = ra + rb
+    ma, mb = 0.5 * (xa0 + xa1), 0.5 * (xb0 + xb1)
+    da, db = xa1 - xa0, xb1 - xb0
+    la_n, lb_n = np.linalg.norm(da, axis=1), np.linalg.norm(db, axis=1)
+    sep = np.linalg.norm(ma - mb, axis=1)
+    X = np.zeros((xa0.shape[0], F), np.float64)
+    X[:, 0] = sep / rs
+    X[:, 1] = np.abs(np.sum(da * db, axis=1)) / np.maximum(la_n * lb_n, 1e-300)
+    X[:, 2] = (la_n + lb_n) / (2.0 * rs)
+    have_layer = (la >= 0) & (lb >= 0)
+    X[:, 3] = np.where(have_layer, np.minimum(np.abs(la - lb), 3) / 3.0, 0.0)
+    X[:, 4] = np.where(have_layer & ((la == 0) | (lb == 0)), 1.0, 0.0)
+    lower = (sep - 0.5 * (la_n + lb_n) - rs) / rs
+    X[:, 5] = np.clip(np.where(has_prev, prev_gap / rs, lower), -2.0, 8.0)
+    X[:, 6] = has_prev.astype(np.float64)
+    return X.astype(np.float32)

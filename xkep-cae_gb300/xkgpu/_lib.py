@@ -94,7 +94,16 @@ SIGNATURES = {
     "xk_pairs_to32": [P(Mesh), P(Pairs), P(ContactPattern), P(Pairs32), vp],
     "xk_pairs_from32": [P(Pairs32), P(Pairs), vp],
     "xk_pair_step32": [P(Pairs32), vp, P(ContactParams), vp, vp],
+    "xk_prune_features": [P(Mesh), vp, vp, C.c_int64, P(Pairs), vp, vp, vp],
+    "xk_mlp_forward": [vp, vp, C.c_int64, vp, vp],
+    "xk_mlp_train_forward": [vp, vp, C.c_int64, vp, vp, vp],
+    "xk_mlp_backward": [vp, vp, vp, vp, vp, vp, C.c_int64, vp, vp, vp, vp, vp],
+    "xk_mlp_adam": [vp, vp, vp, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, vp, vp],
+    "xk_mlp_to_bf16": [vp, vp, vp],
+    "xk_prune_select": [vp, C.c_int64, vp, vp, C.c_float, C.c_int, vp, i64p, vp],
+    "xk_pairs_drop_pristine": [P(Pairs), vp, C.c_int64, P(Pairs), vp],
 }
+MLP_IN, MLP_HIDDEN, MLP_PARAMS, MLP_ACT = 8, 64, 8961, 192
 JACOBIAN_NOALLOC_MAX_PAIRS = 1048576
 NODE32_STRIDE = 16
 ELEM32_STRIDE = 16

@@ -72,6 +72,11 @@ class AssemblyEngine:
         self.gather_variant = L.XK_GATHER_DEFAULT
         self.autotune = True
         self._tuned_for = None
+        # learned candidate pruning (``set_pruner``); the exact path is the judge every ``judge_every`` detections
+        self.pruner = None
+        self.judge_every = 10
+        self._n_detect = 0
+        self.prune_stats = {"detections": 0, "judged": 0, "candidates": 0, "kept": 0, "missed": 0}
 
     # ------------------------------------------------------------------ buffers
     @property
@@ -111,10 +116,9 @@ class AssemblyEngine:
             self._alloc_outputs()
 
     # ------------------------------------------------------------------ per increment
-    def detect(self, u: torch.Tensor, stream=None) -> dict:
-        """Broadphase, pair-table merge, active-set narrowphase and contact pattern at X + u."""
+    def candidates(self, u: torch.Tensor, stream=None):
+        """Broadphase + filters at X + u: (candidate rows int32 [2n] on the device, n)."""
         s = stream_handle(stream)
-        self.sync_state(stream)
         n_out, n_raw, n_pre = C.c_int64(0), C.c_int64(0), C.c_int64(0)
         for _ in range(3):
             code = L.call("xk_broadphase", C.byref(self.mesh.c), ptr(u), C.byref(self.bp), ptr(self.cands),
@@ -123,11 +127,72 @@ class AssemblyEngine:
             if code == L.XK_OK:
                 break
             self.cands = torch.zeros(2 * int(n_out.value * 1.25 + 1024), dtype=torch.int32, device=self.device)
-        nc = int(n_out.value)
+        self._bp_counts = (int(n_raw.value), int(n_pre.value))
+        return self.cands, int(n_out.value)
+
+    def set_pruner(self, pruner, judge_every: int = 10):
+        """Use a trained ``PairPruner`` at detection; every ``judge_every``-th detection checks it exactly."""
+        self.pruner = pruner
+        self.judge_every = max(1, int(judge_every))
+
+    def _prune(self, u, cands, nc, s, stream):
+        """Candidates the pruner keeps (plus every pair with history), judged exactly when due."""
+        pr = self.pruner
+        feat, hist = pr.features(self.mesh, u, cands, nc, self.pairs, stream)
+        logit = pr.logits(feat, nc, stream)
+        kept = torch.empty(2 * max(nc, 1), dtype=torch.int32, device=self.device)
+        nk = C.c_int64(0)
+        L.call("xk_prune_select", ptr(cands), nc, ptr(logit), ptr(hist), pr.threshold, 0, ptr(kept), C.byref(nk), s)
+        nk = int(nk.value)
+        st = self.prune_stats
+        st["detections"] += 1
+        st["candidates"] += nc
+        if self._n_detect % self.judge_every == 0:
+            # judge: the exact narrowphase of every pruned candidate; any that the exact path would
+            # activate is a missed contact and the whole candidate set is used instead
+            st["judged"] += 1
+            dropped = torch.empty(2 * max(nc - nk, 1), dtype=torch.int32, device=self.device)
+            nd = C.c_int64(0)
+            L.call("xk_prune_select", ptr(cands), nc, ptr(logit), ptr(hist), pr.threshold, 1, ptr(dropped),
+                   C.byref(nd), s)
+            nd = int(nd.value)
+            missed = 0
+            if nd:
+                empty = DevicePairTable(self.device, cap=16)
+                tmp = DevicePairTable(self.device, cap=nd + 16)
+                L.call("xk_pairs_merge", C.byref(self.mesh.c), C.byref(empty.c), ptr(dropped), nd, C.byref(tmp.c), s)
+                tmp.set_n(tmp.c.n)
+                L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(tmp.c), ptr(u), C.byref(self.cp), 1, s)
+                missed = int((tmp.t["status"][: tmp.n] != 0).sum().item())
+            st["missed"] += missed
+            st["last_judge_missed"] = missed
+            if missed:
+                st["kept"] += nc
+                return cands, nc
+        st["kept"] += nk
+        # drop pristine old pairs that are not kept, so that pruned pairs leave the table
+        old = self._spare
+        if old.cap < self.pairs.n:
+            old.reserve(self.pairs.n + 64, keep=False)
+        L.call("xk_pairs_drop_pristine", C.byref(self.pairs.c), ptr(kept), nk, C.byref(old.c), s)
+        old.set_n(old.c.n)
+        self.pairs, self._spare = old, self.pairs
+        return kept, nk
+
+    def detect(self, u: torch.Tensor, stream=None) -> dict:
+        """Broadphase, pair-table merge, active-set narrowphase and contact pattern at X + u."""
+        s = stream_handle(stream)
+        self.sync_state(stream)
+        cands, nc = self.candidates(u, stream)
+        n_raw, n_pre = self._bp_counts
+        n_all = nc
+        if self.pruner is not None:
+            cands, nc = self._prune(u, cands, nc, s, stream)
+        self._n_detect += 1
         need = self.pairs.n + nc
         if self._spare.cap < need:
             self._spare.reserve(int(need * 1.25) + 64, keep=False)
-        L.call("xk_pairs_merge", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(self.cands), nc,
+        L.call("xk_pairs_merge", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(cands), nc,
                C.byref(self._spare.c), s)
         self._spare.set_n(self._spare.c.n)
         self.pairs, self._spare = self._spare, self.pairs
@@ -139,7 +204,7 @@ class AssemblyEngine:
                 or self.K_c.numel() < 9 * self.pattern.cap_blocks):
             self._alloc_outputs()
         self.graph = None
-        self.stats = {"raw": int(n_raw.value), "prefilter": int(n_pre.value), "candidates": nc,
+        self.stats = {"raw": n_raw, "prefilter": n_pre, "candidates": n_all, "kept_candidates": nc,
                       "pairs": self.pairs.n, "members": self.pattern.n_members, "contact_blocks": self.pattern.nnzb}
         return self.stats
 
