@@ -325,7 +325,7 @@ def run_gpu(args, rank, world):
     by_fp64 = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, False)
     bg_mixed = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, True)
     bg_fp64 = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, False)
-    variant_name = {L.XK_GATHER_LANES: "lanes", L.XK_GATHER_CHUNKS: "chunks"}
+    variant_name = {L.XK_GATHER_LANES: "lanes", L.XK_GATHER_CHUNKS: "chunks", L.XK_GATHER_SIDES: "sides"}
     peak, peak_kind = _peaks()
 
     # end to end through the public engine API with host buffers
@@ -523,6 +523,9 @@ def run_breakdown(args):
             "tangent_gather_chunks": lambda: L.call("xk_contact_gather_tangent", pat, ptr(eng.rec), p,
                                                     L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_CHUNKS,
                                                     ptr(eng.K_c), sh),
+            "tangent_gather_sides": lambda: L.call("xk_contact_gather_tangent", pat, ptr(eng.rec), p,
+                                                   L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_SIDES,
+                                                   ptr(eng.K_c), sh),
             "assemble": lambda: eng.assemble(u1, u0, stream=s),
         }
         res = {}

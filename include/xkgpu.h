@@ -183,6 +183,20 @@ typedef struct {
   int32_t* blk_row;      /* [cap_blocks] */
   int32_t* blk_ptr;      /* [cap_blocks+1] */
   int32_t* contrib;      /* [16*cap_members] (member << 4) | (k << 2) | l */
+  /* Element-side form of the same sums (gather variant XK_GATHER_SIDES); built
+   * when all of these are non-NULL.  A block's same-side contributions (k, l
+   * on one element) are sums over that element's members, S_e^pq =
+   * sum c_p c_q B (p, q in {0,1}, three distinct per element); its cross
+   * contributions (k, l on different elements) keep a per-block list. */
+  int64_t n_elems;       /* set by the build */
+  int64_t n_xcontrib;    /* cross contributions (8 per member) */
+  int32_t* node_elem_ptr; /* [n_nodes+1] */
+  int32_t* node_elem;     /* [4*n_elems] pairs ((element << 1) | local index, other node) */
+  int32_t* elem_ptr;      /* [n_elems+1] */
+  int32_t* elem_inc;      /* [2*cap_members] (member << 1) | side (0 = A, 1 = B) */
+  int32_t* xblk_ptr;      /* [cap_blocks+1] */
+  int32_t* xcontrib;      /* [8*cap_members] cross codes (member << 4) | (k << 2) | l */
+  void* elem_sums;        /* [27*n_elems] scratch of the record type: S^00, S^01, S^11 per element */
 } xk_contact_pattern;
 
 /* Returns XK_ERR_CAPACITY (with n_members, n_others, nnzb set) when a capacity
@@ -222,12 +236,15 @@ xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec
 /* K_c block values (9 per block, double|float, nnzb blocks): sum over each
  * block's contributors of c_k c_l B; which selects B_n - B_f (combined
  * records), B_n or B_f (split records).  variant picks the reduction schedule
- * (0 default, 1 one contributor per lane, 2 chunks of contributors per lane);
+ * (0 default, 1 one contributor per lane, 2 chunks of contributors per lane,
+ * 3 element-side sums plus per-block cross lists, which needs the element-side
+ * pattern and the elem_sums scratch);
  * all give the same values for a given precision up to rounding order, each
  * deterministic. */
 #define XK_GATHER_DEFAULT 0
 #define XK_GATHER_LANES 1
 #define XK_GATHER_CHUNKS 2
+#define XK_GATHER_SIDES 3  /* element-side sums + cross lists (needs the element-side pattern) */
 xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* rec, int precision, int out_mode,
                                     int which, int variant, void* Kc_vals, xk_stream s);
 

@@ -274,7 +274,7 @@ def test_mixed_engine_vs_fp64_strand37():
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_tangent_gather_schedules_agree(precision):
-    """Both contact-tangent reduction schedules give the same K_c, each deterministically."""
+    """The contact-tangent reduction schedules give the same K_c, each deterministically."""
     import ctypes as C
 
     from xkgpu import workloads as W
@@ -288,7 +288,7 @@ def test_tangent_gather_schedules_agree(precision):
     eng.assemble(u0 * 1.001, u0)
     nb = eng.pattern.nnzb
     outs = []
-    for v in (L.XK_GATHER_LANES, L.XK_GATHER_CHUNKS, L.XK_GATHER_LANES):
+    for v in (L.XK_GATHER_LANES, L.XK_GATHER_CHUNKS, L.XK_GATHER_LANES, L.XK_GATHER_SIDES, L.XK_GATHER_SIDES):
         K = torch.zeros_like(eng.K_c)
         L.call("xk_contact_gather_tangent", C.byref(eng.pattern.c), ptr(eng.rec), eng.precision, L.XK_OUT_COMBINED,
                L.XK_WHICH_COMBINED, v, ptr(K), stream_handle(None))
@@ -296,4 +296,6 @@ def test_tangent_gather_schedules_agree(precision):
         outs.append(K[: 9 * nb].double().cpu().numpy())
     tol = 1e-12 if precision == "fp64" else 1e-6
     assert rel_err(outs[1], outs[0]) < tol
+    assert rel_err(outs[3], outs[0]) < tol
     assert np.array_equal(outs[0], outs[2])
+    assert np.array_equal(outs[3], outs[4])

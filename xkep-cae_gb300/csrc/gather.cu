@@ -131,6 +131,7 @@ XK_D int find_block(const int32_t* __restrict__ rptr, const int32_t* __restrict_
 }
 
 // MODE 0: count contributions per block; MODE 1: fill (member << 4 | k << 2 | l).
+// MODE 2 / 3: the same for the cross pairs only (k and l on different elements).
 template <int MODE>
 __global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int32_t* __restrict__ rptr,
                           const int32_t* __restrict__ col, int32_t* __restrict__ cnt,
@@ -141,17 +142,67 @@ __global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int3
   for (int q = 0; q < 4; ++q) nd[q] = mnodes[4LL * mi + q];
   for (int k = 0; k < 4; ++k)
     for (int l = 0; l < 4; ++l) {
+      if (MODE >= 2 && (k >> 1) == (l >> 1)) continue;
       const int b = find_block(rptr, col, nd[k], nd[l]);
       if (b >= rptr[nd[k] + 1] || col[b] != nd[l]) {  // cannot happen for a consistent pattern
         atomicOr(err, 2);
         continue;
       }
-      if (MODE == 0) {
+      if (MODE == 0 || MODE == 2) {
         atomicAdd(&cnt[b], 1);
       } else {
         contrib[bptr[b] + atomicAdd(&cnt[b], 1)] = (mi << 4) | (k << 2) | l;
       }
     }
+}
+
+// Mesh node -> (element, local index, other node) lists, and member sides per element.
+__global__ void k_node_elem_count(xk_mesh m, int32_t* __restrict__ cnt) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.n_elems) return;
+  atomicAdd(&cnt[m.conn[2 * e]], 1);
+  atomicAdd(&cnt[m.conn[2 * e + 1]], 1);
+}
+
+__global__ void k_node_elem_fill(xk_mesh m, const int32_t* __restrict__ ptr, int32_t* __restrict__ fill,
+                                 int2* __restrict__ ne) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.n_elems) return;
+  for (int p = 0; p < 2; ++p) {
+    const int v = m.conn[2 * e + p];
+    ne[ptr[v] + atomicAdd(&fill[v], 1)] = make_int2((e << 1) | p, m.conn[2 * e + 1 - p]);
+  }
+}
+
+__global__ void k_segment_sort_pairs(const int32_t* __restrict__ ptr, long long nseg, int2* __restrict__ a) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nseg) return;
+  const int lo = ptr[v], hi = ptr[v + 1];
+  for (int x = lo + 1; x < hi; ++x) {
+    const int2 key = a[x];
+    int y = x - 1;
+    while (y >= lo && a[y].x > key.x) { a[y + 1] = a[y]; --y; }
+    a[y + 1] = key;
+  }
+}
+
+__global__ void k_elem_inc_count(xk_pairs p, const int32_t* __restrict__ members, int nm, int32_t* __restrict__ cnt) {
+  const int mi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mi >= nm) return;
+  const int i = members[mi];
+  atomicAdd(&cnt[p.ea[i]], 1);
+  atomicAdd(&cnt[p.eb[i]], 1);
+}
+
+__global__ void k_elem_inc_fill(xk_pairs p, const int32_t* __restrict__ members, int nm,
+                                const int32_t* __restrict__ ptr, int32_t* __restrict__ fill,
+                                int32_t* __restrict__ inc) {
+  const int mi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mi >= nm) return;
+  const int i = members[mi];
+  const int ea = p.ea[i], eb = p.eb[i];
+  inc[ptr[ea] + atomicAdd(&fill[ea], 1)] = mi << 1;
+  inc[ptr[eb] + atomicAdd(&fill[eb], 1)] = (mi << 1) | 1;
 }
 
 // One member record (16 values for combined records) through vector loads.
@@ -231,6 +282,82 @@ XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
   const T w = shape_c<T>(r[0], r[1], k) * shape_c<T>(r[0], r[1], l);
 #pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] += w * r[BCOL + q];
+}
+
+// Variant "sides", step 1: S_e^00, S_e^01, S_e^11 (9 values each) of every
+// element from its members, one thread per (element, B component); the weights
+// are the products c_p c_q of the member's side: (1-s)^2, (1-s)s, s^2 on side A
+// and the same in t on side B (the signs of c_2, c_3 cancel).
+template <typename T, int RS, int BCOL>
+__global__ void k_elem_sums(int ne, const int32_t* __restrict__ eptr, const int32_t* __restrict__ einc,
+                            const T* __restrict__ rec, T* __restrict__ S) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 9LL * ne) return;
+  const int e = (int)(t / 9), q = (int)(t % 9);
+  T s00 = T(0), s01 = T(0), s11 = T(0);
+  const int x1 = eptr[e + 1];
+  for (int x = eptr[e]; x < x1; ++x) {
+    const int code = einc[x];
+    const T* r = rec + (long long)(code >> 1) * RS;
+    const T a = r[code & 1];
+    const T b = r[BCOL + q];
+    const T om = T(1) - a;
+    s00 += (om * om) * b;
+    s01 += (om * a) * b;
+    s11 += (a * a) * b;
+  }
+  T* o = S + 27LL * e;
+  o[q] = s00;
+  o[9 + q] = s01;
+  o[18 + q] = s11;
+}
+
+// Variant "sides", step 2: one thread per block.  Same-side part from the
+// element sums of the row node's elements (diagonal: S^pp, neighbour on the
+// element: S^01), then the block's cross contributors in list order; the
+// block values go out through shared memory so that the stores are coalesced.
+constexpr int GS_T = 128;
+
+template <typename T, int RS, int BCOL>
+__global__ void __launch_bounds__(GS_T) k_gather_tangent_sides(long long nnzb, const int32_t* __restrict__ brow,
+                                                               const int32_t* __restrict__ col,
+                                                               const int32_t* __restrict__ neptr,
+                                                               const int2* __restrict__ ne, const T* __restrict__ S,
+                                                               const int32_t* __restrict__ xptr,
+                                                               const int32_t* __restrict__ xc,
+                                                               const T* __restrict__ rec, T* __restrict__ K) {
+  __shared__ T stage[GS_T * 9];
+  const long long b0 = (long long)blockIdx.x * GS_T;
+  const long long b = b0 + threadIdx.x;
+  T acc[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) acc[q] = T(0);
+  if (b < nnzb) {
+    const int i = brow[b], j = col[b];
+    const int y1 = neptr[i + 1];
+    for (int y = neptr[i]; y < y1; ++y) {
+      const int2 en = ne[y];
+      const T* Se = S + 27LL * (en.x >> 1);
+      if (j == i) {
+        const T* s = Se + ((en.x & 1) ? 18 : 0);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) acc[q] += s[q];
+      }
+      if (j == en.y) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) acc[q] += Se[9 + q];
+      }
+    }
+    const int x1 = xptr[b + 1];
+    for (int x = xptr[b]; x < x1; ++x) add_contrib<T, RS, BCOL>(rec, xc[x], acc);
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) stage[threadIdx.x * 9 + q] = acc[q];
+  __syncthreads();
+  const long long rem = nnzb - b0;
+  const int nv = 9 * (int)(rem < GS_T ? rem : GS_T);
+  T* out = K + 9 * b0;
+  for (int v = threadIdx.x; v < nv; v += GS_T) out[v] = stage[v];
 }
 
 // Variant "lanes": a warp owns 32 consecutive blocks and spreads their
@@ -518,6 +645,52 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
                                                                 bfill, pat->blk_ptr, pat->contrib, err);
   if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
   XK_CHECK_LAUNCH();
+  // element-side form (gather variant XK_GATHER_SIDES)
+  const bool sides = pat->node_elem_ptr && pat->node_elem && pat->elem_ptr && pat->elem_inc && pat->xblk_ptr &&
+                     pat->xcontrib;
+  const int ne = m->n_elems;
+  pat->n_elems = ne;
+  pat->n_xcontrib = 0;
+  if (sides) {
+    int32_t *ecnt, *efill;
+    XK_TRY(S.get(&ecnt, (long long)(ne > nn ? ne : nn) + 1));
+    XK_TRY(S.get(&efill, (long long)(ne > nn ? ne : nn) + 1));
+    // mesh node -> elements
+    XK_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int32_t) * (nn + 1), st));
+    if (ne > 0) k_node_elem_count<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, ecnt);
+    XK_CHECK_LAUNCH();
+    XK_TRY(xk_exclusive_scan_i32(ecnt, pat->node_elem_ptr, nn + 1, nullptr, st));
+    XK_CUDA(cudaMemsetAsync(efill, 0, sizeof(int32_t) * (nn + 1), st));
+    if (ne > 0)
+      k_node_elem_fill<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, pat->node_elem_ptr, efill,
+                                                           reinterpret_cast<int2*>(pat->node_elem));
+    k_segment_sort_pairs<<<xk_blocks(nn, 128), 128, 0, st>>>(pat->node_elem_ptr, nn,
+                                                             reinterpret_cast<int2*>(pat->node_elem));
+    XK_CHECK_LAUNCH();
+    // element -> member sides
+    XK_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int32_t) * (ne + 1), st));
+    if (nm > 0) k_elem_inc_count<<<xk_blocks(nm, 256), 256, 0, st>>>(*p, pat->members, (int)nm, ecnt);
+    XK_CHECK_LAUNCH();
+    XK_TRY(xk_exclusive_scan_i32(ecnt, pat->elem_ptr, ne + 1, nullptr, st));
+    XK_CUDA(cudaMemsetAsync(efill, 0, sizeof(int32_t) * (ne + 1), st));
+    if (nm > 0)
+      k_elem_inc_fill<<<xk_blocks(nm, 256), 256, 0, st>>>(*p, pat->members, (int)nm, pat->elem_ptr, efill,
+                                                          pat->elem_inc);
+    if (ne > 0) k_segment_sort<<<xk_blocks(ne, 128), 128, 0, st>>>(pat->elem_ptr, ne, pat->elem_inc);
+    XK_CHECK_LAUNCH();
+    // cross contributor lists
+    XK_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int32_t) * (nb + 1), st));
+    if (nm > 0) k_contrib<2><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
+                                                                  bcnt, nullptr, nullptr, err);
+    XK_CHECK_LAUNCH();
+    XK_TRY(xk_exclusive_scan_i32(bcnt, pat->xblk_ptr, nb + 1, nullptr, st));
+    XK_CUDA(cudaMemsetAsync(bfill, 0, sizeof(int32_t) * (nb + 1), st));
+    if (nm > 0) k_contrib<3><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
+                                                                  bfill, pat->xblk_ptr, pat->xcontrib, err);
+    if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->xblk_ptr, nb, pat->xcontrib);
+    XK_CHECK_LAUNCH();
+    pat->n_xcontrib = 8 * nm;
+  }
   XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
   if (herr) return xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: inconsistent block pattern");
@@ -577,16 +750,28 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   if (!pat || !rec || !Kc_vals) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: null argument");
   int c1, c2;
   XK_TRY(rec_columns(out_mode, which, true, &c1, &c2));
-  const int rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
+  if (variant < 0 || variant > XK_GATHER_SIDES) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: variant");
+  const bool sides = variant == XK_GATHER_SIDES;
+  if (sides && !(pat->node_elem_ptr && pat->node_elem && pat->elem_ptr && pat->elem_inc && pat->xblk_ptr &&
+                 pat->xcontrib && pat->elem_sums && pat->n_xcontrib == 8LL * pat->n_members))
+    return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: the element-side pattern was not built");
   if (pat->nnzb == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
   const int nb = xk_blocks((pat->nnzb + 31) / 32, GT_WARPS);
   const bool comb = out_mode == XK_OUT_COMBINED;
-  // variant: 0 default (chunks for double, lanes for float), 1 lanes, 2 chunks
+  // variant: 0 default (chunks for double, lanes for float), 1 lanes, 2 chunks, 3 element sides
   const bool chunks = variant == 2 || (variant == 0 && precision == XK_FP64);
+  const int ne = (int)pat->n_elems;
 #define XK_GT(TT, RSV, BC)                                                                                   \
   do {                                                                                                      \
-    if (chunks)                                                                                             \
+    if (sides) {                                                                                            \
+      if (ne > 0)                                                                                           \
+        k_elem_sums<TT, RSV, BC><<<xk_blocks(9LL * ne, 256), 256, 0, st>>>(ne, pat->elem_ptr, pat->elem_inc,   \
+                                                                           (const TT*)rec, (TT*)pat->elem_sums); \
+      k_gather_tangent_sides<TT, RSV, BC><<<xk_blocks(pat->nnzb, GS_T), GS_T, 0, st>>>(                     \
+          pat->nnzb, pat->blk_row, pat->col, pat->node_elem_ptr, reinterpret_cast<const int2*>(pat->node_elem), \
+          (const TT*)pat->elem_sums, pat->xblk_ptr, pat->xcontrib, (const TT*)rec, (TT*)Kc_vals);           \
+    } else if (chunks)                                                                                      \
       k_gather_tangent<TT, RSV, BC><<<nb, 32 * GT_WARPS, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib,     \
                                                                   (const TT*)rec, (TT*)Kc_vals);            \
     else                                                                                                    \

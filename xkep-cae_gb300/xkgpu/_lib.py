@@ -18,7 +18,7 @@ XK_STAGE_ALL = 15
 XK_OUT_COMBINED, XK_OUT_SPLIT = 0, 1
 XK_WHICH_COMBINED, XK_WHICH_NORMAL, XK_WHICH_FRICTION = 0, 1, 2
 REC_STRIDE = {XK_OUT_COMBINED: 16, XK_OUT_SPLIT: 32}
-XK_GATHER_DEFAULT, XK_GATHER_LANES, XK_GATHER_CHUNKS = 0, 1, 2
+XK_GATHER_DEFAULT, XK_GATHER_LANES, XK_GATHER_CHUNKS, XK_GATHER_SIDES = 0, 1, 2, 3
 
 vp = C.c_void_p
 
@@ -65,7 +65,8 @@ class ContactPattern(C.Structure):
                 ("nnzb", C.c_int64), ("n_contrib", C.c_int64), ("cap_members", C.c_int64),
                 ("cap_others", C.c_int64), ("cap_blocks", C.c_int64)] + [
         (n, vp) for n in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row",
-                          "blk_ptr", "contrib")]
+                          "blk_ptr", "contrib")] + [("n_elems", C.c_int64), ("n_xcontrib", C.c_int64)] + [
+        (n, vp) for n in ("node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "xblk_ptr", "xcontrib", "elem_sums")]
 
 
 P = C.POINTER

@@ -329,6 +329,11 @@ class DeviceContactPattern:
         self.c = L.ContactPattern()
         self.inc_ptr = self._i32(mesh.n_nodes + 1)
         self.row_ptr = self._i32(mesh.n_nodes + 1)
+        # element-side form (mesh topology, element incidence, cross lists, element sums)
+        self.node_elem_ptr = self._i32(mesh.n_nodes + 1)
+        self.node_elem = self._i32(4 * mesh.n_elems)
+        self.elem_ptr = self._i32(mesh.n_elems + 1)
+        self.elem_sums = torch.zeros(27 * max(mesh.n_elems, 1), dtype=torch.float64, device=mesh.device)
         self._alloc_members(256)
         self._alloc_others(256)
         self._alloc_blocks(1024)
@@ -341,6 +346,7 @@ class DeviceContactPattern:
         cap = int(cap)
         self.members, self.member_nodes = self._i32(cap), self._i32(4 * cap)
         self.inc, self.contrib = self._i32(4 * cap), self._i32(16 * cap)
+        self.elem_inc, self.xcontrib = self._i32(2 * cap), self._i32(8 * cap)
         self.cap_members = cap
 
     def _alloc_others(self, cap):
@@ -350,6 +356,7 @@ class DeviceContactPattern:
     def _alloc_blocks(self, cap):
         cap = int(cap)
         self.col, self.blk_row, self.blk_ptr = self._i32(cap), self._i32(cap), self._i32(cap + 1)
+        self.xblk_ptr = self._i32(cap + 1)
         self.cap_blocks = cap
 
     def _sync_struct(self):
@@ -357,7 +364,8 @@ class DeviceContactPattern:
         c.n_nodes = self.mesh.n_nodes
         c.cap_members, c.cap_others, c.cap_blocks = self.cap_members, self.cap_others, self.cap_blocks
         for k in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row", "blk_ptr",
-                  "contrib"):
+                  "contrib", "node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "xblk_ptr", "xcontrib",
+                  "elem_sums"):
             setattr(c, k, ptr(getattr(self, k)))
 
     def build(self, pairs: DevicePairTable, stream=None):
