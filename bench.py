@@ -471,6 +471,8 @@ def run_profile(args):
     u0 = torch.as_tensor(w.u, device="cuda")
     u1 = u0 * 1.001
     stats = eng.detect(u0)
+    eng.assemble(u1, u0)
+    eng.tune()  # the schedule the timed graph uses
     for _ in range(args.steps):
         eng.assemble(u1, u0)
     torch.cuda.synchronize()

@@ -184,18 +184,20 @@ typedef struct {
   int32_t* blk_ptr;      /* [cap_blocks+1] */
   int32_t* contrib;      /* [16*cap_members] (member << 4) | (k << 2) | l */
   /* Element-side form of the same sums (gather variant XK_GATHER_SIDES); built
-   * when all of these are non-NULL.  A block's same-side contributions (k, l
-   * on one element) are sums over that element's members, S_e^pq =
-   * sum c_p c_q B (p, q in {0,1}, three distinct per element); its cross
-   * contributions (k, l on different elements) keep a per-block list. */
-  int64_t n_elems;       /* set by the build */
-  int64_t n_xcontrib;    /* cross contributions (8 per member) */
+   * when node_elem_ptr, node_elem, elem_ptr, elem_inc and bcodes are non-NULL.
+   * A block's same-side contributions (k, l on one element) are sums over that
+   * element's members, S_e^pq = sum c_p c_q B (p, q in {0,1}; three distinct
+   * per element, 27 values); each block lists at most four terms inline:
+   * -1 empty, other negative values (offset | 0x80000000) an element sum at
+   * elem_sums[offset], non-negative values a cross code (member << 4) |
+   * (k << 2) | l.  Sorted ascending per block, so every sum has a fixed order. */
+  int64_t n_elems;        /* set by the build */
+  int64_t sides_ok;       /* set by the build: 1 if every block fits four terms (always for wire meshes) */
   int32_t* node_elem_ptr; /* [n_nodes+1] */
   int32_t* node_elem;     /* [4*n_elems] pairs ((element << 1) | local index, other node) */
   int32_t* elem_ptr;      /* [n_elems+1] */
   int32_t* elem_inc;      /* [2*cap_members] (member << 1) | side (0 = A, 1 = B) */
-  int32_t* xblk_ptr;      /* [cap_blocks+1] */
-  int32_t* xcontrib;      /* [8*cap_members] cross codes (member << 4) | (k << 2) | l */
+  int32_t* bcodes;        /* [4*cap_blocks] */
   void* elem_sums;        /* [27*n_elems] scratch of the record type: S^00, S^01, S^11 per element */
 } xk_contact_pattern;
 

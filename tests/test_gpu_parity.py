@@ -213,6 +213,7 @@ def test_graph_replay_matches_eager():
     b.capture(u, u_ref)  # warm-up + capture: runs assemble once
     torch.cuda.synchronize()
     assert torch.equal(a.R, b.R)
+    a.gather_variant = b.gather_variant  # the tangent schedule the capture's autotuner chose
     a.assemble(u, u_ref)
     b.replay()
     torch.cuda.synchronize()

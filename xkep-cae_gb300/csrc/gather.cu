@@ -131,7 +131,6 @@ XK_D int find_block(const int32_t* __restrict__ rptr, const int32_t* __restrict_
 }
 
 // MODE 0: count contributions per block; MODE 1: fill (member << 4 | k << 2 | l).
-// MODE 2 / 3: the same for the cross pairs only (k and l on different elements).
 template <int MODE>
 __global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int32_t* __restrict__ rptr,
                           const int32_t* __restrict__ col, int32_t* __restrict__ cnt,
@@ -142,13 +141,12 @@ __global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int3
   for (int q = 0; q < 4; ++q) nd[q] = mnodes[4LL * mi + q];
   for (int k = 0; k < 4; ++k)
     for (int l = 0; l < 4; ++l) {
-      if (MODE >= 2 && (k >> 1) == (l >> 1)) continue;
       const int b = find_block(rptr, col, nd[k], nd[l]);
       if (b >= rptr[nd[k] + 1] || col[b] != nd[l]) {  // cannot happen for a consistent pattern
         atomicOr(err, 2);
         continue;
       }
-      if (MODE == 0 || MODE == 2) {
+      if (MODE == 0) {
         atomicAdd(&cnt[b], 1);
       } else {
         contrib[bptr[b] + atomicAdd(&cnt[b], 1)] = (mi << 4) | (k << 2) | l;
@@ -284,6 +282,69 @@ XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
   for (int q = 0; q < 9; ++q) acc[q] += w * r[BCOL + q];
 }
 
+// Inline term lists of the blocks (variant "sides").  k_side_codes writes the
+// same-side terms of every block (diagonal: S^pp of each element of the row
+// node; neighbour on an element: S^01) and the count; k_cross_codes appends
+// the cross codes of every member; k_sort_codes sorts each block's four slots.
+constexpr int SIDE_FLAG = (int)0x80000000;
+
+__global__ void k_side_codes(long long nb, const int32_t* __restrict__ brow, const int32_t* __restrict__ col,
+                             const int32_t* __restrict__ neptr, const int2* __restrict__ ne,
+                             int32_t* __restrict__ codes, int32_t* __restrict__ cnt, int32_t* __restrict__ err) {
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const int i = brow[b], j = col[b];
+  int n = 0;
+  for (int y = neptr[i]; y < neptr[i + 1]; ++y) {
+    const int2 en = ne[y];
+    const int base = 27 * (en.x >> 1);
+    if (j == i) {
+      if (n < 4) codes[4 * b + n] = SIDE_FLAG | (base + ((en.x & 1) ? 18 : 0));
+      ++n;
+    }
+    if (j == en.y) {
+      if (n < 4) codes[4 * b + n] = SIDE_FLAG | (base + 9);
+      ++n;
+    }
+  }
+  if (n > 4) atomicOr(err, 1);
+  cnt[b] = n;
+}
+
+__global__ void k_cross_codes(const int32_t* __restrict__ mnodes, int nm, const int32_t* __restrict__ rptr,
+                              const int32_t* __restrict__ col, int32_t* __restrict__ cnt,
+                              int32_t* __restrict__ codes, int32_t* __restrict__ err) {
+  const int mi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (mi >= nm) return;
+  int nd[4];
+  for (int q = 0; q < 4; ++q) nd[q] = mnodes[4LL * mi + q];
+  for (int k = 0; k < 4; ++k)
+    for (int l = 0; l < 4; ++l) {
+      if ((k >> 1) == (l >> 1)) continue;
+      const int b = find_block(rptr, col, nd[k], nd[l]);
+      if (b >= rptr[nd[k] + 1] || col[b] != nd[l]) {
+        atomicOr(err, 2);
+        continue;
+      }
+      const int slot = atomicAdd(&cnt[b], 1);
+      if (slot < 4) codes[4LL * b + slot] = (mi << 4) | (k << 2) | l;
+      else atomicOr(err, 1);
+    }
+}
+
+__global__ void k_sort_codes(long long nb, int4* __restrict__ codes) {
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  int4 c = codes[b];
+  int v[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+  for (int x = 1; x < 4; ++x)
+#pragma unroll
+    for (int y = x; y > 0; --y)
+      if (v[y - 1] > v[y]) { const int t = v[y]; v[y] = v[y - 1]; v[y - 1] = t; }
+  codes[b] = make_int4(v[0], v[1], v[2], v[3]);
+}
+
 // Variant "sides", step 1: S_e^00, S_e^01, S_e^11 (9 values each) of every
 // element from its members, one thread per (element, B component); the weights
 // are the products c_p c_q of the member's side: (1-s)^2, (1-s)s, s^2 on side A
@@ -296,6 +357,7 @@ __global__ void k_elem_sums(int ne, const int32_t* __restrict__ eptr, const int3
   const int e = (int)(t / 9), q = (int)(t % 9);
   T s00 = T(0), s01 = T(0), s11 = T(0);
   const int x1 = eptr[e + 1];
+#pragma unroll 4
   for (int x = eptr[e]; x < x1; ++x) {
     const int code = einc[x];
     const T* r = rec + (long long)(code >> 1) * RS;
@@ -312,20 +374,27 @@ __global__ void k_elem_sums(int ne, const int32_t* __restrict__ eptr, const int3
   o[18 + q] = s11;
 }
 
-// Variant "sides", step 2: one thread per block.  Same-side part from the
-// element sums of the row node's elements (diagonal: S^pp, neighbour on the
-// element: S^01), then the block's cross contributors in list order; the
+// Variant "sides", step 2: one thread per block over its (at most four) inline
+// terms in their sorted order: element sums, then cross contributions; the
 // block values go out through shared memory so that the stores are coalesced.
 constexpr int GS_T = 128;
 
 template <typename T, int RS, int BCOL>
-__global__ void __launch_bounds__(GS_T) k_gather_tangent_sides(long long nnzb, const int32_t* __restrict__ brow,
-                                                               const int32_t* __restrict__ col,
-                                                               const int32_t* __restrict__ neptr,
-                                                               const int2* __restrict__ ne, const T* __restrict__ S,
-                                                               const int32_t* __restrict__ xptr,
-                                                               const int32_t* __restrict__ xc,
-                                                               const T* __restrict__ rec, T* __restrict__ K) {
+XK_D void add_term(const T* __restrict__ S, const T* __restrict__ rec, int code, T* acc) {
+  if (code == -1) return;
+  if (code < 0) {
+    const T* s = S + (code & 0x7fffffff);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] += s[q];
+  } else {
+    add_contrib<T, RS, BCOL>(rec, code, acc);
+  }
+}
+
+template <typename T, int RS, int BCOL>
+__global__ void __launch_bounds__(GS_T) k_gather_tangent_sides(long long nnzb, const int4* __restrict__ codes,
+                                                               const T* __restrict__ S, const T* __restrict__ rec,
+                                                               T* __restrict__ K) {
   __shared__ T stage[GS_T * 9];
   const long long b0 = (long long)blockIdx.x * GS_T;
   const long long b = b0 + threadIdx.x;
@@ -333,23 +402,11 @@ __global__ void __launch_bounds__(GS_T) k_gather_tangent_sides(long long nnzb, c
 #pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] = T(0);
   if (b < nnzb) {
-    const int i = brow[b], j = col[b];
-    const int y1 = neptr[i + 1];
-    for (int y = neptr[i]; y < y1; ++y) {
-      const int2 en = ne[y];
-      const T* Se = S + 27LL * (en.x >> 1);
-      if (j == i) {
-        const T* s = Se + ((en.x & 1) ? 18 : 0);
-#pragma unroll
-        for (int q = 0; q < 9; ++q) acc[q] += s[q];
-      }
-      if (j == en.y) {
-#pragma unroll
-        for (int q = 0; q < 9; ++q) acc[q] += Se[9 + q];
-      }
-    }
-    const int x1 = xptr[b + 1];
-    for (int x = xptr[b]; x < x1; ++x) add_contrib<T, RS, BCOL>(rec, xc[x], acc);
+    const int4 c = codes[b];
+    add_term<T, RS, BCOL>(S, rec, c.x, acc);
+    add_term<T, RS, BCOL>(S, rec, c.y, acc);
+    add_term<T, RS, BCOL>(S, rec, c.z, acc);
+    add_term<T, RS, BCOL>(S, rec, c.w, acc);
   }
 #pragma unroll
   for (int q = 0; q < 9; ++q) stage[threadIdx.x * 9 + q] = acc[q];
@@ -646,15 +703,15 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
   XK_CHECK_LAUNCH();
   // element-side form (gather variant XK_GATHER_SIDES)
-  const bool sides = pat->node_elem_ptr && pat->node_elem && pat->elem_ptr && pat->elem_inc && pat->xblk_ptr &&
-                     pat->xcontrib;
+  const bool sides = pat->node_elem_ptr && pat->node_elem && pat->elem_ptr && pat->elem_inc && pat->bcodes;
   const int ne = m->n_elems;
   pat->n_elems = ne;
-  pat->n_xcontrib = 0;
+  pat->sides_ok = 0;
   if (sides) {
-    int32_t *ecnt, *efill;
+    int32_t *ecnt, *efill, *serr;
     XK_TRY(S.get(&ecnt, (long long)(ne > nn ? ne : nn) + 1));
     XK_TRY(S.get(&efill, (long long)(ne > nn ? ne : nn) + 1));
+    XK_TRY(S.get(&serr, 1));
     // mesh node -> elements
     XK_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int32_t) * (nn + 1), st));
     if (ne > 0) k_node_elem_count<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, ecnt);
@@ -678,18 +735,22 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
                                                           pat->elem_inc);
     if (ne > 0) k_segment_sort<<<xk_blocks(ne, 128), 128, 0, st>>>(pat->elem_ptr, ne, pat->elem_inc);
     XK_CHECK_LAUNCH();
-    // cross contributor lists
-    XK_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int32_t) * (nb + 1), st));
-    if (nm > 0) k_contrib<2><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
-                                                                  bcnt, nullptr, nullptr, err);
+    // inline term lists; a flag in serr (more than four terms somewhere) only disables the variant
+    XK_CUDA(cudaMemsetAsync(serr, 0, sizeof(int32_t), st));
+    XK_CUDA(cudaMemsetAsync(pat->bcodes, 0xff, sizeof(int32_t) * 4 * (nb > 0 ? nb : 1), st));
+    if (nb > 0)
+      k_side_codes<<<xk_blocks(nb, 256), 256, 0, st>>>(nb, pat->blk_row, pat->col, pat->node_elem_ptr,
+                                                       reinterpret_cast<const int2*>(pat->node_elem), pat->bcodes,
+                                                       bcnt, serr);
+    if (nm > 0)
+      k_cross_codes<<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col, bcnt,
+                                                        pat->bcodes, serr);
+    if (nb > 0) k_sort_codes<<<xk_blocks(nb, 256), 256, 0, st>>>(nb, reinterpret_cast<int4*>(pat->bcodes));
     XK_CHECK_LAUNCH();
-    XK_TRY(xk_exclusive_scan_i32(bcnt, pat->xblk_ptr, nb + 1, nullptr, st));
-    XK_CUDA(cudaMemsetAsync(bfill, 0, sizeof(int32_t) * (nb + 1), st));
-    if (nm > 0) k_contrib<3><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
-                                                                  bfill, pat->xblk_ptr, pat->xcontrib, err);
-    if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->xblk_ptr, nb, pat->xcontrib);
-    XK_CHECK_LAUNCH();
-    pat->n_xcontrib = 8 * nm;
+    int32_t herr2 = 0;
+    XK_CUDA(cudaMemcpyAsync(&herr2, serr, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    XK_CUDA(cudaStreamSynchronize(st));
+    pat->sides_ok = herr2 ? 0 : 1;
   }
   XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
@@ -752,8 +813,7 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   XK_TRY(rec_columns(out_mode, which, true, &c1, &c2));
   if (variant < 0 || variant > XK_GATHER_SIDES) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: variant");
   const bool sides = variant == XK_GATHER_SIDES;
-  if (sides && !(pat->node_elem_ptr && pat->node_elem && pat->elem_ptr && pat->elem_inc && pat->xblk_ptr &&
-                 pat->xcontrib && pat->elem_sums && pat->n_xcontrib == 8LL * pat->n_members))
+  if (sides && !(pat->elem_ptr && pat->elem_inc && pat->bcodes && pat->elem_sums && pat->sides_ok == 1))
     return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: the element-side pattern was not built");
   if (pat->nnzb == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
@@ -769,8 +829,8 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
         k_elem_sums<TT, RSV, BC><<<xk_blocks(9LL * ne, 256), 256, 0, st>>>(ne, pat->elem_ptr, pat->elem_inc,   \
                                                                            (const TT*)rec, (TT*)pat->elem_sums); \
       k_gather_tangent_sides<TT, RSV, BC><<<xk_blocks(pat->nnzb, GS_T), GS_T, 0, st>>>(                     \
-          pat->nnzb, pat->blk_row, pat->col, pat->node_elem_ptr, reinterpret_cast<const int2*>(pat->node_elem), \
-          (const TT*)pat->elem_sums, pat->xblk_ptr, pat->xcontrib, (const TT*)rec, (TT*)Kc_vals);           \
+          pat->nnzb, reinterpret_cast<const int4*>(pat->bcodes), (const TT*)pat->elem_sums, (const TT*)rec,    \
+          (TT*)Kc_vals);                                                                                    \
     } else if (chunks)                                                                                      \
       k_gather_tangent<TT, RSV, BC><<<nb, 32 * GT_WARPS, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib,     \
                                                                   (const TT*)rec, (TT*)Kc_vals);            \

@@ -65,8 +65,8 @@ class ContactPattern(C.Structure):
                 ("nnzb", C.c_int64), ("n_contrib", C.c_int64), ("cap_members", C.c_int64),
                 ("cap_others", C.c_int64), ("cap_blocks", C.c_int64)] + [
         (n, vp) for n in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row",
-                          "blk_ptr", "contrib")] + [("n_elems", C.c_int64), ("n_xcontrib", C.c_int64)] + [
-        (n, vp) for n in ("node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "xblk_ptr", "xcontrib", "elem_sums")]
+                          "blk_ptr", "contrib")] + [("n_elems", C.c_int64), ("sides_ok", C.c_int64)] + [
+        (n, vp) for n in ("node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums")]
 
 
 P = C.POINTER

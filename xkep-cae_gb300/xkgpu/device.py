@@ -346,7 +346,7 @@ class DeviceContactPattern:
         cap = int(cap)
         self.members, self.member_nodes = self._i32(cap), self._i32(4 * cap)
         self.inc, self.contrib = self._i32(4 * cap), self._i32(16 * cap)
-        self.elem_inc, self.xcontrib = self._i32(2 * cap), self._i32(8 * cap)
+        self.elem_inc = self._i32(2 * cap)
         self.cap_members = cap
 
     def _alloc_others(self, cap):
@@ -356,7 +356,7 @@ class DeviceContactPattern:
     def _alloc_blocks(self, cap):
         cap = int(cap)
         self.col, self.blk_row, self.blk_ptr = self._i32(cap), self._i32(cap), self._i32(cap + 1)
-        self.xblk_ptr = self._i32(cap + 1)
+        self.bcodes = self._i32(4 * cap)
         self.cap_blocks = cap
 
     def _sync_struct(self):
@@ -364,8 +364,7 @@ class DeviceContactPattern:
         c.n_nodes = self.mesh.n_nodes
         c.cap_members, c.cap_others, c.cap_blocks = self.cap_members, self.cap_others, self.cap_blocks
         for k in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row", "blk_ptr",
-                  "contrib", "node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "xblk_ptr", "xcontrib",
-                  "elem_sums"):
+                  "contrib", "node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums"):
             setattr(c, k, ptr(getattr(self, k)))
 
     def build(self, pairs: DevicePairTable, stream=None):

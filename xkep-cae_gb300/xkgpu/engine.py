@@ -251,7 +251,10 @@ class AssemblyEngine:
         if self.pattern.nnzb == 0:
             return times
         s = torch.cuda.current_stream()
-        for v in (L.XK_GATHER_LANES, L.XK_GATHER_CHUNKS, L.XK_GATHER_SIDES):
+        variants = [L.XK_GATHER_LANES, L.XK_GATHER_CHUNKS]
+        if self.pattern.c.sides_ok == 1:  # every block fits four inline terms (wire meshes)
+            variants.append(L.XK_GATHER_SIDES)
+        for v in variants:
             for _ in range(2):
                 L.call("xk_contact_gather_tangent", C.byref(self.pattern.c), ptr(self.rec), self.precision,
                        L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, v, ptr(self.K_c), stream_handle(s))
