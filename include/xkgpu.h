@@ -308,6 +308,29 @@ xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p, int32_t* r
                                  xk_stream s);
 
 /* ------------------------------------------------------------------------
+ * Generalized-alpha time integration with a lumped mass, no damping
+ * (GeneralizedAlphaProcess, xkep_cae/time_integration/strategy.py:96-232);
+ * alpha_m, alpha_f, gamma, beta from rho_inf as in :133-136.  All vectors are
+ * device doubles of length n.
+ * ---------------------------------------------------------------------- */
+/* predict (:163-174): acc_old = acc, vel_old = vel,
+ * u_pred = u + dt vel + 0.5 dt^2 (1 - 2 beta) acc, v_pred = vel + dt (1 - gamma) acc */
+xk_status xk_genalpha_predict(int64_t n, const double* u, const double* vel, const double* acc,
+                              double* vel_old, double* acc_old, double* u_pred, double* v_pred, double dt,
+                              double beta, double gamma, xk_stream s);
+/* correct (:176-185): acc = c0 (u - u_pred), vel = v_pred + dt gamma acc, c0 = 1 / (beta dt^2) */
+xk_status xk_genalpha_correct(int64_t n, const double* u, const double* u_pred, const double* v_pred,
+                              double* acc, double* vel, double dt, double beta, double gamma, xk_stream s);
+/* effective_residual (:202-216): out = R + m ((1 - alpha_m) acc + alpha_m acc_old) */
+xk_status xk_genalpha_residual(int64_t n, const double* R, const double* m, const double* acc,
+                               const double* acc_old, double alpha_m, double* out, xk_stream s);
+/* K[idx[i]] += c m[i] (K double for XK_FP64, float for XK_MIXED): the mass
+ * term (1 - alpha_m) c0 M of effective_stiffness (:187-200) on the diagonal of
+ * a block matrix, idx = value index of each DOF's diagonal entry (< 0: skipped). */
+xk_status xk_add_diagonal(int64_t n, const int64_t* idx, const double* m, double c, int precision, void* K,
+                          xk_stream s);
+
+/* ------------------------------------------------------------------------
  * Learned pruning of broadphase candidates.  No counterpart in the reference:
  * an MLP (XK_MLP_IN inputs -> 64 -> 64 -> 64 -> 1, ReLU, BF16 weights and
  * activations, FP32 accumulation) scores each candidate pair; candidates below

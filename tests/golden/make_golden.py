@@ -2,7 +2,7 @@
 
 Run in a container that holds the reference source tree:
 
-    python tests/golden/make_golden.py /path/to/xkep-cae
+    python tests/golden/make_golden.py /path/to/xkep-cae [case ...]
 
 The reference is imported read-only (no bytecode written, its process report
 hook switched off) and driven through its own public functions on seeded
@@ -46,8 +46,9 @@ def _import_reference(root: str):
     import xkep_cae.elements._beam_assembly as ba
     import xkep_cae.elements._beam_section as bs
     import xkep_cae.mesh._twisted_wire as tw
+    import xkep_cae.time_integration.strategy as ti
 
-    return dict(mp=mp, cf=cf, fs=fs, gc=gc, gs=gs, ln=ln, ps=ps, cp=cp, ba=ba, bs=bs, tw=tw)
+    return dict(mp=mp, cf=cf, fs=fs, gc=gc, gs=gs, ln=ln, ps=ps, cp=cp, ba=ba, bs=bs, tw=tw, ti=ti)
 
 
 def _section(R, d, E=2.0e5, nu=0.3):
@@ -251,21 +252,61 @@ def laws_case(R, name):
     print(name)
 
 
+def genalpha_case(R, name, seed=4, n=600):
+    """GeneralizedAlphaProcess with a lumped mass: predict / correct / effective terms over three steps."""
+    import scipy.sparse as sp
+
+    ti = R["ti"]
+    rng = np.random.default_rng(seed)
+    m = rng.uniform(1e-9, 1e-6, n)
+    out = {"m": m}
+    for rho, tag in ((0.9, "r09"), (0.5, "r05")):
+        ga = ti.GeneralizedAlphaProcess(sp.diags(m, format="csr"), rho_inf=rho)
+        ga.set_initial_state(velocity=rng.normal(size=n), acceleration=rng.normal(size=n) * 1e3)
+        u = rng.normal(size=n) * 1e-3
+        K = sp.random(n, n, density=0.01, random_state=seed, format="csr") + sp.eye(n, format="csr")
+        for step, dt in enumerate((1e-4, 2e-4, 1e-4)):
+            p = f"{tag}_s{step}_"
+            out[p + "u"] = u.copy()
+            out[p + "dt"] = np.array(dt)
+            out[p + "u_pred"] = ga.predict(u, dt)
+            u1 = out[p + "u_pred"] + rng.normal(size=n) * 1e-6
+            out[p + "u1"] = u1
+            ga.correct(u1, u1 - out[p + "u_pred"], dt)
+            out[p + "acc"], out[p + "vel"] = ga.acc.copy(), ga.vel.copy()
+            R_in = rng.normal(size=n)
+            out[p + "R"] = R_in
+            out[p + "R_eff"] = ga.effective_residual(R_in, dt)
+            out[p + "K_eff_diag"] = ga.effective_stiffness(K, dt).diagonal() - K.diagonal()
+            u = u1
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name)
+
+
+CASES = {
+    "strand7": lambda R: strand_case(R, "strand7", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16,
+                                     gap_frac=-0.005, seed=0, mu=0.1),
+    "strand7_nogap": lambda R: strand_case(R, "strand7_nogap", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16,
+                                           gap_frac=0.0, seed=0, mu=0.1, n_iter=1, n_incr=1),
+    "strand19_slip": lambda R: strand_case(R, "strand19_slip", n_wires=19, d=1.0, pitch=20.0, n_pitches=1, n_el=16,
+                                           gap_frac=-0.01, seed=5, mu=0.3, k_t_ratio=2.0, smoothing_delta=400.0,
+                                           step_frac=2e-3, n_iter=2, n_incr=2),
+    "narrowphase": lambda R: narrowphase_case(R, "narrowphase"),
+    "beam_elements": lambda R: beam_case(R, "beam_elements"),
+    "meshes": lambda R: mesh_case(R, "meshes"),
+    "laws": lambda R: laws_case(R, "laws"),
+    "genalpha": lambda R: genalpha_case(R, "genalpha"),
+}
+
+
 def main():
+    """make_golden.py /path/to/xkep-cae [case ...]  (all cases when none are named)"""
     root = sys.argv[1] if len(sys.argv) > 1 else None
     if root is None:
-        raise SystemExit("usage: make_golden.py /path/to/xkep-cae")
+        raise SystemExit("usage: make_golden.py /path/to/xkep-cae [case ...]")
     R = _import_reference(root)
-    strand_case(R, "strand7", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16, gap_frac=-0.005,
-                seed=0, mu=0.1)
-    strand_case(R, "strand7_nogap", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16, gap_frac=0.0,
-                seed=0, mu=0.1, n_iter=1, n_incr=1)
-    strand_case(R, "strand19_slip", n_wires=19, d=1.0, pitch=20.0, n_pitches=1, n_el=16, gap_frac=-0.01,
-                seed=5, mu=0.3, k_t_ratio=2.0, smoothing_delta=400.0, step_frac=2e-3, n_iter=2, n_incr=2)
-    narrowphase_case(R, "narrowphase")
-    beam_case(R, "beam_elements")
-    mesh_case(R, "meshes")
-    laws_case(R, "laws")
+    for name in (sys.argv[2:] or list(CASES)):
+        CASES[name](R)
 
 
 if __name__ == "__main__":

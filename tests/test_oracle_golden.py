@@ -97,3 +97,28 @@ def test_strand_mesh_generator_matches_reference():
         # bit-identical on the platform the fixtures were made on; libm may differ elsewhere
         assert rel_err(m.coords, z[tag + "_X"]) < 1e-15
         assert np.array_equal(np.array([w.layer for w in m.wires]), z[tag + "_layer"])
+
+
+def test_genalpha_oracle_matches_reference():
+    """The Generalized-alpha restatement against GeneralizedAlphaProcess's own outputs."""
+    from oracle import dynamics as od
+
+    z = golden("genalpha")
+    m = z["m"]
+    rng = np.random.default_rng(4)
+    rng.uniform(1e-9, 1e-6, m.size)  # the fixture's draws, in order
+    for rho, tag in ((0.9, "r09"), (0.5, "r05")):
+        ga = od.GeneralizedAlpha(m, rho)
+        ga.vel = rng.normal(size=m.size)
+        ga.acc = rng.normal(size=m.size) * 1e3
+        rng.normal(size=m.size)  # u
+        for step in range(3):
+            p = f"{tag}_s{step}_"
+            dt = float(z[p + "dt"])
+            assert np.array_equal(ga.predict(z[p + "u"], dt), z[p + "u_pred"])
+            ga.correct(z[p + "u1"], None, dt)
+            assert np.array_equal(ga.acc, z[p + "acc"]) and np.array_equal(ga.vel, z[p + "vel"])
+            assert np.array_equal(ga.effective_residual(z[p + "R"], dt), z[p + "R_eff"])
+            assert np.allclose(ga.effective_stiffness_diag(dt), z[p + "K_eff_diag"], rtol=1e-12, atol=0)
+            rng.normal(size=m.size)  # u1 noise
+            rng.normal(size=m.size)  # R

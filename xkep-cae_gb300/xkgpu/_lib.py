@@ -95,6 +95,10 @@ SIGNATURES = {
     "xk_pairs_to32": [P(Mesh), P(Pairs), P(ContactPattern), P(Pairs32), vp],
     "xk_pairs_from32": [P(Pairs32), P(Pairs), vp],
     "xk_pair_step32": [P(Pairs32), vp, P(ContactParams), vp, vp],
+    "xk_genalpha_predict": [C.c_int64, vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double, vp],
+    "xk_genalpha_correct": [C.c_int64, vp, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double, vp],
+    "xk_genalpha_residual": [C.c_int64, vp, vp, vp, vp, C.c_double, vp, vp],
+    "xk_add_diagonal": [C.c_int64, vp, vp, C.c_double, C.c_int, vp, vp],
     "xk_prune_features": [P(Mesh), vp, vp, C.c_int64, P(Pairs), vp, vp, vp],
     "xk_mlp_forward": [vp, vp, C.c_int64, vp, vp],
     "xk_mlp_train_forward": [vp, vp, C.c_int64, vp, vp, vp],

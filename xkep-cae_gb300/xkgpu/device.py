@@ -191,6 +191,18 @@ class DeviceBeam:
     def nnzb(self) -> int:
         return self.plan_host.nnzb
 
+    def diag_index(self) -> torch.Tensor:
+        """Value index (into the 6x6 block values) of every DOF's diagonal entry; -1 for a node without elements."""
+        if getattr(self, "_diag_index", None) is None:
+            ph = self.plan_host
+            n = self.mesh.n_nodes
+            rows = np.repeat(np.arange(n), np.diff(ph.row_ptr))
+            db = np.nonzero(ph.col == rows)[0]
+            idx = np.full((n, 6), -1, dtype=np.int64)
+            idx[rows[db]] = 36 * db[:, None] + 7 * np.arange(6)[None, :]
+            self._diag_index = torch.as_tensor(idx.ravel(), device=self.mesh.device)
+        return self._diag_index
+
     def k_dtype(self, precision: int):
         return torch.float64 if precision == L.XK_FP64 else torch.float32
 
