@@ -172,19 +172,151 @@ def pair_kernel_bytes(n_nodes, n_elems, n_others, n_members, mixed: bool):
     return 72 * n_nodes + 16 * n_elems + 156 * n_others + n_members * (264 + 128)
 
 
-def gather_tangent_bytes(n_members, n_contrib, nnzb, mixed: bool):
-    """Algorithmic DRAM bytes of one contact-tangent gather launch.
+def gather_tangent_bytes(n_members, n_contrib, nnzb, mixed: bool, sides: bool = False, n_elems: int = 0):
+    """Algorithmic DRAM bytes of one contact-tangent gather (all its launches).
 
-    Each contributing pair's record is read once from DRAM (16 values: 64 B
-    float, 128 B double), each contributor list entry once (4 B), each block
-    pointer once (4 B) and each 3x3 block written once (36 B float, 72 B
-    double).  Re-reads of a record by the 16 blocks it feeds are L2 traffic.
+    Each contributing pair's record is read once (16 values: 64 B float, 128 B
+    double) and each 3x3 block written once (36 B float, 72 B double); re-reads
+    of a record by the blocks it feeds are L2 traffic.  Contributor-list
+    schedules also read each list entry (4 B) and block pointer (4 B).  The
+    element-side schedule instead reads each member's two element-incidence
+    entries (8 B), the element pointers (4 B), writes and reads back the 27
+    element sums of every element, and reads four inline terms per block (16 B).
     """
     w = 4 if mixed else 8
+    if sides:
+        return (16 * w * n_members + 8 * n_members + 4 * (n_elems + 1) + 2 * 27 * w * n_elems + 16 * nnzb
+                + 9 * w * nnzb)
     return 16 * w * n_members + 4 * n_contrib + 4 * (nnzb + 1) + 9 * w * nnzb
 
 
 # --------------------------------------------------------------------------- GPU arm
+
+
+def _time_replay(eng, steps, warmup):
+    import torch
+
+    for _ in range(warmup):
+        eng.replay()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(steps):
+        eng.replay()
+    b.record(s)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def pruning_section(args, dev, w, u0, u1, ms_fp64):
+    """The mixed assembly with the learned candidate pruning, per Newton iteration.
+
+    The network is trained here, on the GPU, on exact-path labels of 7- and
+    37-wire strands; the first detection of the workload is judged exactly
+    (missed contacts are reported; the judge puts any back, so R is unchanged).
+    """
+    import dataclasses
+
+    import torch
+
+    from xkgpu import prune as P
+    from xkgpu import workloads as W
+    from xkgpu.engine import AssemblyEngine
+
+    t0 = time.perf_counter()
+    pr = P.PairPruner(device=dev)
+    feats, ys = [], []
+    # 7- and 37-wire strands at the benchmark configurations' discretisation and at the 1027-wire one
+    # (d 0.5 mm, pitch 20 mm, 24 elements per pitch)
+    train = [(lambda sd: W.config_workload("strand7", seed=sd), range(4)),
+             (lambda sd: W.config_workload("strand37", seed=sd), range(3)),
+             (lambda sd: W.strand_workload("strand7_d05", 7, 0.5, 20.0, 2, 24, seed=sd), range(4)),
+             (lambda sd: W.strand_workload("strand37_d05", 37, 0.5, 20.0, 2, 24, seed=sd), range(3))]
+    for make_w, seeds in train:
+        for sd in seeds:
+            ww = make_w(sd)
+            e = AssemblyEngine(ww.strand.coords, ww.strand.conn, ww.strand.radii, ww.section, precision="fp64",
+                               device=dev, **ww.engine_kwargs())
+            rng = np.random.default_rng(100 + sd)
+            mask = np.tile([1, 1, 1, 0, 0, 0], ww.strand.n_nodes)
+            ua = torch.as_tensor(ww.u, device=dev)
+            ub = torch.as_tensor(ww.u + rng.normal(0.0, 3e-3 * ww.meta["d"], ww.u.shape) * mask, device=dev)
+            f, y, _ = P.candidate_samples(e, ua, ub, pr)
+            feats.append(f)
+            ys.append(y)
+            del e
+    rep = pr.fit(torch.cat(feats), torch.cat(ys), epochs=400)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    st = w.strand
+    # the same first Newton iteration without and with pruning, on fresh engines
+    ref = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", device=dev,
+                         **w.engine_kwargs())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref.detect(u0)
+    torch.cuda.synchronize()
+    t_det_ref = time.perf_counter() - t0
+    ref.assemble(u1, u0)
+    R_ref = ref.R.clone()
+    n_ref = ref.pairs.n
+    del ref
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", device=dev,
+                         **w.engine_kwargs())
+    eng.set_pruner(pr, judge_every=10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    stats = eng.detect(u0)  # the first detection is a judged one
+    torch.cuda.synchronize()
+    t_det = time.perf_counter() - t0
+    eng.assemble(u1, u0)
+    R_diff = float((eng.R - R_ref).abs().max() / R_ref.abs().max())
+    eng.capture(u1, u0)
+    ms = _time_replay(eng, args.steps, args.warmup)
+    ps = eng.prune_stats
+    out = {"ms_per_step": ms, "speedup_vs_fp64_plain_per_iteration": ms_fp64 / ms,
+           "pairs_in_table": eng.pairs.n, "candidates": stats["candidates"],
+           "kept_fraction": ps["kept"] / max(ps["candidates"], 1), "judged_detections": ps["judged"],
+           "missed_contacts": ps["missed"], "members": stats["members"], "pairs_without_pruning": n_ref,
+           "detect_ms_judged": 1e3 * t_det, "detect_ms_without_pruning": 1e3 * t_det_ref,
+           "R_rel_diff_vs_unpruned": R_diff, "train_s": t_train, "train": dataclasses.asdict(rep),
+           "judge_every": eng.judge_every}
+    del eng, pr
+    torch.cuda.empty_cache()
+    return out
+
+
+def batch_section(args, dev):
+    """The 256-strand batch (one friction coefficient per strand) assembled by the same launches."""
+    import torch
+
+    from xkgpu import workloads as W
+    from xkgpu.engine import AssemblyEngine
+
+    w = W.config_workload("batch256", seed=0)
+    st = w.strand
+    u0 = torch.as_tensor(w.u, device=dev)
+    rng = np.random.default_rng(7)
+    du = rng.normal(0.0, 2e-4 * w.meta["d"], (st.n_nodes, 6))
+    du[:, 3:] = 0.0
+    u1 = torch.as_tensor(w.u + du.ravel(), device=dev)
+    out = {"workload": "batch256: 256 strands, wires from {7, 19, 37}, 1-4 pitches, 8-48 el/pitch, d = 2 mm, "
+                       "gap -0.005 d, seeded noise, mu per strand in [0.05, 0.3]",
+           "n_nodes": st.n_nodes, "n_elems": st.n_elems}
+    for prec in ("fp64", "mixed"):
+        eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, layer=st.elem_layer, precision=prec,
+                             k_pen=w.k_pen, mu=w.mu, device=dev)
+        stats = eng.detect(u0)
+        eng.capture(u1, u0)
+        ms = _time_replay(eng, args.steps, args.warmup)
+        units = st.n_elems + stats["pairs"]
+        out[prec] = {"ms_per_step": ms, "evals_per_s": units / ms * 1e3, "pairs": stats["pairs"],
+                     "members": stats["members"]}
+        del eng
+        torch.cuda.empty_cache()
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    return out
 
 
 def run_gpu(args, rank, world):
@@ -323,9 +455,13 @@ def run_gpu(args, rank, world):
     m = pat.n_members
     by_mixed = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, True)
     by_fp64 = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, False)
-    bg_mixed = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, True)
-    bg_fp64 = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, False)
+    bg_mixed = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, True,
+                                    engines["mixed"].gather_variant == L.XK_GATHER_SIDES, n_e)
+    bg_fp64 = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, False,
+                                   engines["fp64"].gather_variant == L.XK_GATHER_SIDES, n_e)
     variant_name = {L.XK_GATHER_LANES: "lanes", L.XK_GATHER_CHUNKS: "chunks", L.XK_GATHER_SIDES: "sides"}
+    kernel_names = {L.XK_GATHER_LANES: "k_gather_tangent_lanes<float>", L.XK_GATHER_CHUNKS: "k_gather_tangent<float>",
+                    L.XK_GATHER_SIDES: "k_elem_sums<float> + k_gather_tangent_sides<float>"}
     peak, peak_kind = _peaks()
 
     # end to end through the public engine API with host buffers
@@ -377,7 +513,18 @@ def run_gpu(args, rank, world):
                "sample": f"NumPy oracle, one Newton-iteration assembly (contact + beam) on the first 1/48 of every "
                          f"wire ({sub.n_elems} elements, {prep[2]['ea'].shape[0]} pairs), host of the GPU box"}
 
-    per_launch = 9  # node prep, 2 pair kernels, 2 beam colours, force gather, 2 norm kernels, tangent gather
+    mixed_variant = engines["mixed"].gather_variant
+    fp64_variant = engines["fp64"].gather_variant
+    contact_blocks = engines["mixed"].pattern.nnzb
+    extras = {}
+    if not args.no_extras and world == 1:
+        del engines, eng
+        torch.cuda.empty_cache()
+        extras["learned_pruning"] = pruning_section(args, dev, w, u0, u1, ms_fp64)
+        extras["batched"] = batch_section(args, dev)
+
+    # node prep, 2 pair kernels, 2 beam colours, force gather, 2 norm kernels, tangent gather (+ element sums)
+    per_launch = 9 + (1 if mixed_variant == L.XK_GATHER_SIDES else 0)
     out = {
         "metric": METRIC, "value": units / t_mixed * args.steps, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
@@ -386,7 +533,7 @@ def run_gpu(args, rank, world):
         "config": {"workload": "strand1027: 1027 wires (18 layers), d=0.5 mm, pitch 20 mm, 4 pitches, "
                                "24 el/pitch, gap -0.005 d, seeded noise", "n_nodes": st.n_nodes,
                    "n_elems": n_e, "n_pairs": n_c, "raw_aabb_pairs": results["mixed"]["stats"]["raw"],
-                   "contributing_pairs": m, "contact_blocks": engines["mixed"].pattern.nnzb,
+                   "contributing_pairs": m, "contact_blocks": contact_blocks,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (pair table alone > 1 GB)", "cuda_graph": True},
         "fp64_plain": {"value": units / t_fp64 * args.steps, "ms_per_step": ms_fp64,
@@ -395,14 +542,14 @@ def run_gpu(args, rank, world):
         "detect_ms": {"mixed": results["mixed"]["detect_ms"], "fp64": results["fp64"]["detect_ms"],
                       "first": results["mixed"]["detect_first_ms"]},
         "roofline": {"bound": "hbm",
-                     "kernel": "contact tangent gather (k_gather_tangent_lanes<float>, schedule "
-                               f"{variant_name.get(engines['mixed'].gather_variant, 'default')})",
+                     "kernel": "contact tangent gather, schedule " + variant_name.get(mixed_variant, "default")
+                               + " (" + kernel_names.get(mixed_variant, "") + ")",
                      "achieved": bg_mixed / tg_mixed / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": bg_mixed / tg_mixed / 1e9 / peak, "peak_kind": peak_kind,
                      "bytes_per_launch": bg_mixed, "launch_ms": 1e3 * tg_mixed, "traffic": None,
                      "fp64_kernel": {"achieved": bg_fp64 / tg_fp64 / 1e9, "launch_ms": 1e3 * tg_fp64,
                                      "bytes_per_launch": bg_fp64,
-                                     "schedule": variant_name.get(engines["fp64"].gather_variant, "default")},
+                                     "schedule": variant_name.get(fp64_variant, "default")},
                      "pair_step": {"kernels": "k_nodes_prepare + k_pair_other32 + k_pair_member32 (narrowphase, "
                                               "Huber, Coulomb, pair tangent)",
                                    "achieved": by_mixed / tk_mixed / 1e9, "frac": by_mixed / tk_mixed / 1e9 / peak,
@@ -414,6 +561,7 @@ def run_gpu(args, rank, world):
         "gpu_launches": per_launch * args.steps,
         "clocks": clocks,
         "cpu_baseline": cpu,
+        **extras,
     }
     tr = ROOT / "profiles" / "dram_traffic.json"
     if tr.exists():
@@ -555,6 +703,7 @@ def main():
     ap.add_argument("--impl", default="xkgpu", choices=["xkgpu", "reference"])
     ap.add_argument("--workload", default="strand1027")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the learned-pruning and batched sections")
     ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
                     help="profiling driver: detect once, then --steps eager assemblies, no timing")
     ap.add_argument("--breakdown", action="store_true", help="warm per-phase times (ms) of one assembly")

@@ -56,6 +56,8 @@ typedef struct {
   const int32_t* conn;  /* [2*n_elems] */
   const double* radii;  /* [n_elems] */
   const int32_t* layer; /* [n_elems], -1 = no layer; NULL = no layer map */
+  const double* mu;     /* [n_elems] friction coefficient per element (a pair uses mu[ea]: batched strands
+                           with their own coefficient, already ramped); NULL = xk_contact_params.mu_eff */
 } xk_mesh;
 
 /* Pair table: _ContactPairOutput / _ContactStateOutput as structure of arrays
@@ -273,6 +275,8 @@ typedef struct {
   float *p_n, *z_t;        /* z_t: [2*cap] */
   float *q_trial_norm, *dissipation, *k_pen, *k_t;
   uint8_t *status, *stick;
+  float* mu;               /* [cap] friction coefficient of each slot, filled from xk_mesh.mu by xk_pairs_to32;
+                              NULL (use xk_contact_params.mu_eff) unless the mesh has per-element mu */
 } xk_pairs32;
 
 /* Per iteration: node records for the mixed kernels from u (and u_ref, nullable). */

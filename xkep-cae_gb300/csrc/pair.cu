@@ -366,7 +366,8 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, c
   double zt0 = p.z_t[i], zt1 = p.z_t[cap + i];
   double qtn = p.q_trial_norm[i];
   bool stick = p.stick[i] != 0;
-  const bool fproc = (p_n > 0.0) && (cp.mu_eff > 0.0);
+  const double mu_eff = m.mu ? m.mu[p.ea[i]] : cp.mu_eff;
+  const bool fproc = (p_n > 0.0) && (mu_eff > 0.0);
   if ((stages & XK_STAGE_FRICTION) && fproc) {
     if (p.k_pen[i] <= 0.0) {
       p.k_pen[i] = cp.k_pen;
@@ -387,7 +388,7 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, c
     const T ktT = (T)kt;
     const T q0 = (T)zt0 + ktT * d0, q1 = (T)zt1 + ktT * d1;
     const T qn = my_sqrt<T>(q0 * q0 + q1 * q1);
-    const T fy = (T)cp.mu_eff * (T)p_n;
+    const T fy = (T)mu_eff * (T)p_n;
     stick = qn <= fy;
     T r0 = q0, r1 = q1;
     if (!stick) { r0 = fy * q0 / qn; r1 = fy * q1 / qn; }
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, c
       T D00 = ktT, D01 = T(0), D11 = ktT;
       if (!stick && (T)qtn >= T(1e-30)) {
         const T qh0 = q0 / qnorm, qh1 = q1 / qnorm;
-        const T ratio = (T)cp.mu_eff * (T)p_n / (T)qtn;
+        const T ratio = (T)mu_eff * (T)p_n / (T)qtn;
         D00 = ratio * ktT * (T(1) - qh0 * qh0);
         D01 = -ratio * ktT * qh0 * qh1;
         D11 = ratio * ktT * (T(1) - qh1 * qh1);
@@ -553,6 +554,7 @@ __global__ void k_pairs_to32(xk_mesh m, xk_pairs p, xk_contact_pattern pat, xk_p
   q.q_trial_norm[j] = (float)p.q_trial_norm[i]; q.dissipation[j] = (float)p.dissipation[i];
   q.k_pen[j] = (float)p.k_pen[i]; q.k_t[j] = (float)p.k_t[i];
   q.status[j] = p.status[i]; q.stick[j] = p.stick[i];
+  if (q.mu && m.mu) q.mu[j] = (float)m.mu[ea];
 }
 
 __global__ void k_pairs_from32(xk_pairs32 q, xk_pairs p) {
@@ -753,7 +755,7 @@ __global__ void __launch_bounds__(PAIR_T, 3) k_pair_member32(xk_pairs32 q, const
       for (int k = 0; k < 3; ++k) vn[k] = p_n * n[k];
   }
   // friction (Coulomb return mapping)
-  const float mu = (float)cp.mu_eff;
+  const float mu = q.mu ? q.mu[i] : (float)cp.mu_eff;
   float kt = q.k_t[i];
   float zt0 = q.z_t[i], zt1 = q.z_t[cq + i];
   float qtn = q.q_trial_norm[i];

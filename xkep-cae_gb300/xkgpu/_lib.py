@@ -29,7 +29,7 @@ class Section(C.Structure):
 
 class Mesh(C.Structure):
     _fields_ = [("n_nodes", C.c_int32), ("n_elems", C.c_int32), ("X", vp), ("conn", vp), ("radii", vp),
-                ("layer", vp)]
+                ("layer", vp), ("mu", vp)]
 
 
 class Pairs(C.Structure):
@@ -41,7 +41,7 @@ class Pairs(C.Structure):
 class Pairs32(C.Structure):
     _fields_ = [("n", C.c_int32), ("cap", C.c_int32), ("n_members", C.c_int32)] + [
         (n, vp) for n in ("pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
-                          "dissipation", "k_pen", "k_t", "status", "stick")]
+                          "dissipation", "k_pen", "k_t", "status", "stick", "mu")]
 
 
 class BeamPlan(C.Structure):

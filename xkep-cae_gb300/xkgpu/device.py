@@ -45,7 +45,7 @@ def as_dev(x, dtype, device) -> torch.Tensor:
 class DeviceMesh:
     """Reference coordinates, connectivity, radii and layer ids on the device."""
 
-    def __init__(self, coords, conn, radii, layer=None, device=None):
+    def __init__(self, coords, conn, radii, layer=None, device=None, mu=None):
         self.device = require_cuda(device)
         coords = np.asarray(coords, dtype=np.float64).reshape(-1, 3)
         conn = np.asarray(conn, dtype=np.int64).reshape(-1, 2)
@@ -60,11 +60,15 @@ class DeviceMesh:
         self.conn = as_dev(conn.ravel().astype(np.int32), torch.int32, self.device)
         self.radii = as_dev(radii, torch.float64, self.device)
         self.layer = None if layer is None else as_dev(np.asarray(layer).astype(np.int32), torch.int32, self.device)
+        if mu is not None and np.asarray(mu).shape != (self.n_elems,):
+            raise ValueError("mu must hold one friction coefficient per element")
+        self.mu = None if mu is None else as_dev(np.asarray(mu, dtype=np.float64), torch.float64, self.device)
         self.conn_host = conn
         self.refresh()
 
     def refresh(self):
-        self.c = L.Mesh(self.n_nodes, self.n_elems, ptr(self.X), ptr(self.conn), ptr(self.radii), ptr(self.layer))
+        self.c = L.Mesh(self.n_nodes, self.n_elems, ptr(self.X), ptr(self.conn), ptr(self.radii), ptr(self.layer),
+                        ptr(self.mu))
 
     def set_coords(self, coords):
         self.X.copy_(as_dev(np.asarray(coords, dtype=np.float64).ravel(), torch.float64, self.device))
@@ -306,11 +310,12 @@ F32_FIELDS = {"rad": 2, "s": 1, "t": 1, "gap": 1, "normal": 3, "t1": 3, "t2": 3,
 class DevicePairTable32:
     """Slot-ordered float copy of the pair state (``xk_pairs32``) for the mixed per-iteration kernels."""
 
-    def __init__(self, device):
+    def __init__(self, device, per_slot_mu: bool = False):
         self.device = device
         self.cap = 0
         self.t: dict[str, torch.Tensor] = {}
         self.c = L.Pairs32()
+        self.per_slot_mu = per_slot_mu  # the mesh has a friction coefficient per element
 
     def ensure(self, cap: int):
         if cap <= self.cap:
@@ -321,11 +326,12 @@ class DevicePairTable32:
         t.update({k: torch.zeros(w * cap, dtype=torch.float32, device=self.device) for k, w in F32_FIELDS.items()})
         t["status"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         t["stick"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
+        t["mu"] = torch.zeros(cap, dtype=torch.float32, device=self.device) if self.per_slot_mu else None
         self.t = t
         self.cap = cap
         self.c = L.Pairs32(0, cap, 0, *(ptr(t[k]) for k in (
             "pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
-            "dissipation", "k_pen", "k_t", "status", "stick")))
+            "dissipation", "k_pen", "k_t", "status", "stick", "mu")))
 
 
 # ----------------------------------------------------------------------------- contact pattern

@@ -40,12 +40,15 @@ PRECISIONS = {"fp64": L.XK_FP64, "mixed": L.XK_MIXED}
 
 class AssemblyEngine:
     def __init__(self, coords, conn, radii, section: dict, *, layer=None, precision: str = "fp64",
-                 k_pen: float, k_t_ratio: float = 0.5, mu: float = 0.1, smoothing_delta: float = 0.0,
+                 k_pen: float, k_t_ratio: float = 0.5, mu: float | np.ndarray = 0.1, smoothing_delta: float = 0.0,
                  g_on: float = 0.0, g_off: float = 1e-6, allow_deactivation: bool = True,
                  exclude_same_layer: bool = True, exclude_shared: bool = True, midpoint_prescreening: bool = True,
                  prescreening_margin: float = 0.0, margin: float = 0.0, v_ref=None, device=None):
         self.device = require_cuda(device)
-        self.mesh = DeviceMesh(coords, conn, radii, layer, device=self.device)
+        mu_elem = None
+        if np.ndim(mu) > 0:  # one friction coefficient per element (batched strands)
+            mu_elem, mu = np.asarray(mu, dtype=np.float64), 0.0
+        self.mesh = DeviceMesh(coords, conn, radii, layer, device=self.device, mu=mu_elem)
         self.beam = DeviceBeam(self.mesh, section, v_ref=v_ref)
         self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         self.cp = L.ContactParams(k_pen, k_t_ratio, mu, smoothing_delta, g_on, g_off, int(allow_deactivation))
@@ -63,7 +66,7 @@ class AssemblyEngine:
         # mixed fast path: float node / element records and the float copy of the pair state
         self.node32 = torch.zeros(L.NODE32_STRIDE * max(self.mesh.n_nodes, 1), dtype=torch.float32, device=dev)
         self.elem32 = torch.zeros(L.ELEM32_STRIDE * max(self.mesh.n_elems, 1), dtype=torch.float32, device=dev)
-        self.pairs32 = DevicePairTable32(dev)
+        self.pairs32 = DevicePairTable32(dev, per_slot_mu=mu_elem is not None)
         self._state_in32 = False
         self.update_reference_frames()
         self._alloc_outputs()

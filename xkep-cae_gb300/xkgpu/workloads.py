@@ -41,7 +41,7 @@ class Workload:
     section: dict
     u: np.ndarray
     k_pen: float
-    mu: float = 0.1
+    mu: float | np.ndarray = 0.1  # one value, or one per element (batched strands)
     k_t_ratio: float = 0.5
     smoothing_delta: float = 0.0
     meta: dict = field(default_factory=dict)
@@ -82,5 +82,40 @@ CONFIGS = {
 }
 
 
+def batch_workload(name: str = "batch256", n_strands: int = 256, seed: int = 0, d: float = 2.0,
+                   pitch: float = 40.0) -> Workload:
+    """Independent strands in one mesh: wire counts drawn from {7, 19, 37}, 1-4 pitches, 8-48
+    elements per pitch, seeded perturbations, a friction coefficient per strand in [0.05, 0.3].
+
+    The strands lie side by side without touching; ``mu`` of the workload holds
+    one coefficient per element and ``meta['instance']`` the strand of every
+    element.  The penalty is the batch's 1e3 EA / L_mean.
+    """
+    rng = np.random.default_rng(seed)
+    strands, us, mus = [], [], []
+    for k in range(n_strands):
+        nw = int(rng.choice([7, 19, 37]))
+        npt = int(rng.integers(1, 5))
+        epp = int(rng.integers(8, 49))
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            st = S.make_strand(nw, d, pitch, npt, epp * npt, gap=-0.005 * d, allow_coarse=True)
+        strands.append(st)
+        us.append(S.perturbation(st, seed * 100003 + k, sigma_pos=1e-3 * d, sigma_rot=1e-3))
+        mus.append(float(rng.uniform(0.05, 0.3)))
+    merged, inst, node_first = S.merge_strands(strands)
+    u = np.concatenate(us)
+    sec = circle_section(d)
+    k_pen = 1e3 * sec["E"] * sec["A"] / mean_element_length(merged.coords, merged.conn)
+    mu_elem = np.asarray(mus)[inst]
+    return Workload(name, merged, sec, u, k_pen, mu=mu_elem,
+                    meta={"n_strands": n_strands, "d": d, "pitch": pitch, "seed": seed, "instance": inst,
+                          "node_first": node_first, "mu_instance": np.asarray(mus),
+                          "n_wires": [len(s.wires) for s in strands]})
+
+
 def config_workload(name: str, seed: int = 0) -> Workload:
+    if name.startswith("batch"):
+        n = int(name[5:]) if name[5:] else 256
+        return batch_workload(name, n_strands=n, seed=seed)
     return strand_workload(name, seed=seed, **CONFIGS[name])
