@@ -160,6 +160,8 @@ xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double* u, const x
 #define XK_STAGE_NORMAL 2   /* HuberContactForceProcess.evaluate (contact_force/strategy.py:126-170) */
 #define XK_STAGE_FRICTION 4 /* CoulombReturnMappingProcess.evaluate (friction/strategy.py:111-148) */
 #define XK_STAGE_TANGENT 8  /* .tangent of both (contact_force/strategy.py:172-254, friction/_assembly.py:108-257) */
+#define XK_STAGE_NO_OTHERS 16  /* skip the other pairs' narrowphase (run it in another launch / stream) */
+#define XK_STAGE_NO_MEMBERS 32 /* skip the member kernel (only the other pairs' narrowphase) */
 #define XK_OUT_COMBINED 0   /* record (s, t, v = v_n + v_f, B = B_n - B_f): 14 values */
 #define XK_OUT_SPLIT 1      /* record (s, t, v_n, v_f, B_n, B_f): 26 values */
 #define XK_REC_STRIDE_COMBINED 16 /* values per record in memory (padded) */
@@ -300,7 +302,10 @@ xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream s);
 /* xk_pair_step with all four stages and combined float records on the float
  * state: slots [0, n_members) are the members (record index = slot), the rest
  * get the narrowphase only. */
-xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk_contact_params* cp, float* rec,
+#define XK_PAIRS_OTHERS 1  /* the narrowphase of the slots [n_members, n) */
+#define XK_PAIRS_MEMBERS 2 /* the member kernel (narrowphase, normal, friction, tangent, records) */
+#define XK_PAIRS_ALL 3
+xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk_contact_params* cp, float* rec, int parts,
                          xk_stream s);
 
 /* Constraint Jacobian rows c_k n of the non-INACTIVE pairs in table order

@@ -885,13 +885,14 @@ extern "C" xk_status xk_pair_step(const xk_mesh* m, xk_pairs* p, const xk_contac
   if (((stages & XK_STAGE_NARROW) || (stages & XK_STAGE_FRICTION)) && !u)
     return xk_set_error(XK_ERR_ARG, "xk_pair_step: u is required for the narrowphase and friction stages");
   const int all = XK_STAGE_NORMAL | XK_STAGE_FRICTION | XK_STAGE_TANGENT;
-  if (out_mode == XK_OUT_COMBINED && (stages & all) != all)
+  const bool members = !(stages & XK_STAGE_NO_MEMBERS);
+  if (members && out_mode == XK_OUT_COMBINED && (stages & all) != all)
     return xk_set_error(XK_ERR_ARG, "xk_pair_step: combined records need the normal, friction and tangent stages");
-  if (pat->n_members > 0 && !rec) return xk_set_error(XK_ERR_ARG, "xk_pair_step: rec is null");
+  if (members && pat->n_members > 0 && !rec) return xk_set_error(XK_ERR_ARG, "xk_pair_step: rec is null");
   if ((long long)pat->n_members + pat->n_others != p->n)
     return xk_set_error(XK_ERR_ARG, "xk_pair_step: pattern was built for another pair table");
   cudaStream_t st = (cudaStream_t)s;
-  if ((stages & XK_STAGE_NARROW) && pat->n_others > 0) {
+  if ((stages & XK_STAGE_NARROW) && !(stages & XK_STAGE_NO_OTHERS) && pat->n_others > 0) {
     const int nb = xk_blocks(pat->n_others, PAIR_T);
     if (precision == XK_FP64)
       k_pair_other<XK_FP64><<<nb, PAIR_T, 0, st>>>(*m, *p, pat->others, pat->n_others, u);
@@ -901,7 +902,7 @@ extern "C" xk_status xk_pair_step(const xk_mesh* m, xk_pairs* p, const xk_contac
       return xk_set_error(XK_ERR_ARG, "xk_pair_step: precision");
     XK_CHECK_LAUNCH();
   }
-  if (pat->n_members == 0) return XK_OK;
+  if (pat->n_members == 0 || (stages & XK_STAGE_NO_MEMBERS)) return XK_OK;
   const int nb = xk_blocks(pat->n_members, PAIR_T);
   const long long rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
 #define XK_MEMBER_LAUNCH(PP, OO, TT)                                                                                \
@@ -1059,13 +1060,14 @@ extern "C" xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream
 }
 
 extern "C" xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk_contact_params* cp, float* rec,
-                                    xk_stream s) {
+                                    int parts, xk_stream s) {
   if (!q || !node32 || !cp) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: null argument");
-  if (q->n_members > 0 && !rec) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: rec is null");
+  if ((parts & XK_PAIRS_MEMBERS) && q->n_members > 0 && !rec)
+    return xk_set_error(XK_ERR_ARG, "xk_pair_step32: rec is null");
   cudaStream_t st = (cudaStream_t)s;
   const int n_o = q->n - q->n_members;
-  if (n_o > 0) k_pair_other32<<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
-  if (q->n_members > 0)
+  if ((parts & XK_PAIRS_OTHERS) && n_o > 0) k_pair_other32<<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
+  if ((parts & XK_PAIRS_MEMBERS) && q->n_members > 0)
     k_pair_member32<<<xk_blocks(q->n_members, PAIR_T), PAIR_T, 0, st>>>(*q, node32, *cp, rec);
   XK_CHECK_LAUNCH();
   return XK_OK;

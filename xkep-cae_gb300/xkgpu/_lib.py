@@ -15,6 +15,8 @@ XK_OK, XK_ERR_ARG, XK_ERR_CUDA, XK_ERR_CAPACITY, XK_ERR_OVERFLOW = 0, 1, 2, 3, 4
 XK_FP64, XK_MIXED = 0, 1
 XK_STAGE_NARROW, XK_STAGE_NORMAL, XK_STAGE_FRICTION, XK_STAGE_TANGENT = 1, 2, 4, 8
 XK_STAGE_ALL = 15
+XK_STAGE_NO_OTHERS, XK_STAGE_NO_MEMBERS = 16, 32
+XK_PAIRS_OTHERS, XK_PAIRS_MEMBERS, XK_PAIRS_ALL = 1, 2, 3
 XK_OUT_COMBINED, XK_OUT_SPLIT = 0, 1
 XK_WHICH_COMBINED, XK_WHICH_NORMAL, XK_WHICH_FRICTION = 0, 1, 2
 REC_STRIDE = {XK_OUT_COMBINED: 16, XK_OUT_SPLIT: 32}
@@ -94,7 +96,7 @@ SIGNATURES = {
     "xk_beam_assemble32": [P(Mesh), P(Section), vp, P(BeamPlan), vp, vp, vp, vp],
     "xk_pairs_to32": [P(Mesh), P(Pairs), P(ContactPattern), P(Pairs32), vp],
     "xk_pairs_from32": [P(Pairs32), P(Pairs), vp],
-    "xk_pair_step32": [P(Pairs32), vp, P(ContactParams), vp, vp],
+    "xk_pair_step32": [P(Pairs32), vp, P(ContactParams), vp, C.c_int, vp],
     "xk_genalpha_predict": [C.c_int64, vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double, vp],
     "xk_genalpha_correct": [C.c_int64, vp, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double, vp],
     "xk_genalpha_residual": [C.c_int64, vp, vp, vp, vp, C.c_double, vp, vp],

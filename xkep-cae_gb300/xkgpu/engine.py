@@ -214,22 +214,65 @@ class AssemblyEngine:
     # ------------------------------------------------------------------ per iteration
     def assemble(self, u: torch.Tensor, u_ref: torch.Tensor | None = None, f_ext: torch.Tensor | None = None,
                  fixed: torch.Tensor | None = None, stream=None, *, tangent: bool = True):
-        s = stream_handle(stream)
+        """One Newton iteration's assembly: R (with its squared norm), K_beam and K_c.
+
+        The independent parts run on separate streams and join before the
+        residual (in a captured graph they become parallel branches): the other
+        pairs' narrowphase, the beam elements, and the member kernel followed by
+        the contact tangent; the force gather waits for the members and the beam.
+        Every kernel writes its own outputs, so the results do not depend on the
+        overlap.
+        """
+        main = stream if stream is not None else torch.cuda.current_stream()
+        s = stream_handle(main)
         p = self.precision
         pat = C.byref(self.pattern.c)
-        self.pair_step(u, u_ref, stream)
+        so, sb, st = self._side_streams()
+        if p == L.XK_MIXED:
+            if not self._state_in32:
+                self._to32(s)
+            L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u_ref), ptr(self.node32), s)
+        so.wait_stream(main)
+        sb.wait_stream(main)
+        # other pairs' narrowphase
+        if p == L.XK_MIXED:
+            L.call("xk_pair_step32", C.byref(self.pairs32.c), ptr(self.node32), C.byref(self.cp), ptr(self.rec),
+                   L.XK_PAIRS_OTHERS, stream_handle(so))
+        else:
+            L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
+                   C.byref(self.cp), L.XK_STAGE_NARROW | L.XK_STAGE_NO_MEMBERS, p, L.XK_OUT_COMBINED,
+                   ptr(self.rec), stream_handle(so))
+        # beam elements
         if p == L.XK_MIXED:
             L.call("xk_beam_assemble32", C.byref(self.mesh.c), C.byref(self.beam.section), ptr(self.elem32),
                    C.byref(self.beam.plan), ptr(self.node32), ptr(self.f_int), ptr(self.K_beam) if tangent else None,
-                   s)
+                   stream_handle(sb))
         else:
-            self.beam.assemble(u, p, self.f_int, self.K_beam if tangent else None, stream)
+            self.beam.assemble(u, p, self.f_int, self.K_beam if tangent else None, sb)
+        # contributing pairs, then the contact tangent from their records
+        if p == L.XK_MIXED:
+            L.call("xk_pair_step32", C.byref(self.pairs32.c), ptr(self.node32), C.byref(self.cp), ptr(self.rec),
+                   L.XK_PAIRS_MEMBERS, s)
+        else:
+            L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
+                   C.byref(self.cp), L.XK_STAGE_ALL | L.XK_STAGE_NO_OTHERS, p, L.XK_OUT_COMBINED, ptr(self.rec), s)
+        if tangent and self.pattern.nnzb > 0:
+            st.wait_stream(main)
+            L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
+                   self.gather_variant, ptr(self.K_c), stream_handle(st))
+        # residual after the members and the beam
+        main.wait_stream(sb)
         L.call("xk_contact_gather_force", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
                ptr(self.f_int), -1.0, ptr(f_ext), ptr(fixed), ptr(self.R), ptr(self.norm2), s)
+        main.wait_stream(so)
         if tangent and self.pattern.nnzb > 0:
-            L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
-                   self.gather_variant, ptr(self.K_c), s)
+            main.wait_stream(st)
         return self.R
+
+    def _side_streams(self):
+        if getattr(self, "_streams", None) is None:
+            self._streams = tuple(torch.cuda.Stream(device=self.device) for _ in range(3))
+        return self._streams
 
     def pair_step(self, u: torch.Tensor, u_ref: torch.Tensor | None = None, stream=None):
         """The pair part of ``assemble``: narrowphase of every pair and the member records."""
@@ -239,7 +282,8 @@ class AssemblyEngine:
             if not self._state_in32:
                 self._to32(s)
             L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u_ref), ptr(self.node32), s)
-            L.call("xk_pair_step32", C.byref(self.pairs32.c), ptr(self.node32), C.byref(self.cp), ptr(self.rec), s)
+            L.call("xk_pair_step32", C.byref(self.pairs32.c), ptr(self.node32), C.byref(self.cp), ptr(self.rec),
+                   L.XK_PAIRS_ALL, s)
         else:
             L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
                    C.byref(self.cp), L.XK_STAGE_ALL, self.precision, L.XK_OUT_COMBINED, ptr(self.rec), s)
