@@ -300,3 +300,41 @@ def test_tangent_gather_schedules_agree(precision):
     assert rel_err(outs[3], outs[0]) < tol
     assert np.array_equal(outs[0], outs[2])
     assert np.array_equal(outs[3], outs[4])
+
+
+def test_host_pipeline_returns_each_steps_outputs():
+    """Pipelined host round trips: every ticket holds its own step's R, K_beam and K_c."""
+    from xkgpu import workloads as W
+    from xkgpu.engine import HostPipeline
+
+    w = W.config_workload("strand37", seed=4)
+    st = w.strand
+    kw = w.engine_kwargs()
+    kw["mu"] = 0.0  # no friction history: every step's outputs depend on its own inputs only
+    ref = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **kw)
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **kw)
+    u0 = _dev(w.u)
+    ref.detect(u0)
+    eng.detect(u0)
+    rng = np.random.default_rng(8)
+    mask = np.tile([1, 1, 1, 0, 0, 0], st.n_nodes)
+    us = [w.u + rng.normal(0.0, 1e-3 * w.meta["d"], w.u.shape) * mask for _ in range(3)]
+    pipe = HostPipeline(eng)
+    ref.gather_variant = eng.gather_variant
+    hosts = [torch.as_tensor(x).pin_memory() for x in us]
+    uref_h = torch.as_tensor(w.u).pin_memory()
+
+    def check(ticket, i):
+        R, Kb, Kc = pipe.result(ticket)
+        ref.assemble(_dev(us[i]), u0)
+        assert torch.equal(R, ref.R.cpu())
+        assert torch.equal(Kb, ref.K_beam.cpu())
+        assert torch.equal(Kc, ref.K_c[: Kc.numel()].cpu())
+
+    # the usual loop: submit step k, then read step k-1 while step k runs
+    prev = pipe.submit(hosts[0], uref_h)
+    for k in range(1, 5):
+        cur = pipe.submit(hosts[k % 3], uref_h)
+        check(prev, (k - 1) % 3)
+        prev = cur
+    check(prev, 4 % 3)

@@ -367,3 +367,84 @@ class AssemblyEngine:
 
     def K_total_csr(self) -> sp.csr_matrix:
         return (self.K_beam_csr() + self.K_contact_csr()).tocsr()
+
+
+class HostPipeline:
+    """Newton-iteration assembly from host inputs to host outputs, copies overlapped with compute.
+
+    ``submit(u, u_ref)`` copies the pinned host inputs into the engine's graph
+    inputs, replays the captured assembly, snapshots R, K_beam and K_c into one
+    of two device staging sets and starts their copy to pinned host memory on a
+    copy stream; ``result(ticket)`` waits for that copy and returns the host
+    arrays.  The read-back of one step runs while the next step is copied in
+    and assembled.  The two staging sets and two host sets are reused in turn,
+    so a ticket's arrays stay valid until two more steps have been submitted.
+    """
+
+    def __init__(self, engine: AssemblyEngine):
+        self.eng = engine
+        dev = engine.device
+        nd = engine.mesh.ndof
+        self.u_in = torch.zeros(nd, dtype=torch.float64, device=dev)
+        self.ur_in = torch.zeros(nd, dtype=torch.float64, device=dev)
+        self.nkc = 9 * engine.pattern.nnzb
+        kd = engine.K_beam.dtype
+        self.dev_out = [(torch.empty(nd, dtype=torch.float64, device=dev),
+                         torch.empty(engine.K_beam.numel(), dtype=kd, device=dev),
+                         torch.empty(max(self.nkc, 1), dtype=engine.K_c.dtype, device=dev)) for _ in range(2)]
+        self.host_out = [tuple(torch.empty(t.numel(), dtype=t.dtype).pin_memory() for t in d) for d in self.dev_out]
+        self.copy_in = torch.cuda.Stream(device=dev)
+        self.copy_out = torch.cuda.Stream(device=dev)
+        self._slot_free = [None, None]  # events: the staging / host set may be overwritten
+        self._inputs_free = None  # event: the replay has read the inputs
+        self._done = {}
+        self.n = 0
+        engine.capture(self.u_in, self.ur_in)
+
+    def submit(self, u_host: torch.Tensor, u_ref_host: torch.Tensor) -> int:
+        eng, main = self.eng, torch.cuda.current_stream()
+        k = self.n % 2
+        if self._inputs_free is not None:
+            self.copy_in.wait_event(self._inputs_free)
+        with torch.cuda.stream(self.copy_in):
+            self.u_in.copy_(u_host, non_blocking=True)
+            self.ur_in.copy_(u_ref_host, non_blocking=True)
+        main.wait_stream(self.copy_in)
+        eng.replay()
+        self._inputs_free = torch.cuda.Event()
+        self._inputs_free.record(main)
+        if self._slot_free[k] is not None:
+            main.wait_event(self._slot_free[k])
+        R, Kb, Kc = self.dev_out[k]
+        R.copy_(eng.R, non_blocking=True)
+        Kb.copy_(eng.K_beam, non_blocking=True)
+        if self.nkc:
+            Kc[: self.nkc].copy_(eng.K_c[: self.nkc], non_blocking=True)
+        self.copy_out.wait_stream(main)
+        hR, hKb, hKc = self.host_out[k]
+        with torch.cuda.stream(self.copy_out):
+            hR.copy_(R, non_blocking=True)
+            hKb.copy_(Kb, non_blocking=True)
+            if self.nkc:
+                hKc[: self.nkc].copy_(Kc[: self.nkc], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(self.copy_out)
+        self._slot_free[k] = ev
+        self._done[self.n] = (ev, k)
+        self.n += 1
+        return self.n - 1
+
+    def result(self, ticket: int):
+        """(R, K_beam values, K_c values) of a submitted step as pinned host tensors."""
+        ev, k = self._done.pop(ticket)
+        ev.synchronize()
+        hR, hKb, hKc = self.host_out[k]
+        return hR, hKb, hKc[: self.nkc]
+
+    @property
+    def bytes_in(self) -> int:
+        return 2 * self.u_in.numel() * 8
+
+    @property
+    def bytes_out(self) -> int:
+        return sum(t.numel() * t.element_size() for t in self.dev_out[0][:2]) + self.nkc * self.dev_out[0][2].element_size()
