@@ -561,7 +561,8 @@ def run_gpu(args, rank, world):
     tr = ROOT / "profiles" / "dram_traffic.json"
     if tr.exists():
         d = json.loads(tr.read_text())
-        out["roofline"]["traffic"] = d.get("k_gather_tangent_lanes_float", {}).get("bytes_per_launch")
+        key = {L.XK_GATHER_SIDES: "gather_tangent_sides_float"}.get(mixed_variant)
+        out["roofline"]["traffic"] = d.get(key, {}).get("bytes_per_launch") if key else None
         out["roofline"]["pair_step"]["traffic"] = d.get("pair_step_mixed", {}).get("bytes_per_launch")
     return out
 
