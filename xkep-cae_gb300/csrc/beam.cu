@@ -525,10 +525,13 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
                                                      const uint8_t* __restrict__ first, const float* __restrict__ n32,
                                                      double* __restrict__ f_int, float* __restrict__ Kv) {
   __shared__ float sx[BEAMQ_T / 4][4][27];
+  __shared__ __align__(16) float kst[BEAMQ_T / 4][4][36];  // the element's four 6x6 blocks, staged
+  __shared__ int s_e[BEAMQ_T / 4];
   const int q = threadIdx.x >> 2, I = threadIdx.x & 3;
   const int k = k0 + blockIdx.x * (BEAMQ_T / 4) + q;
   const bool live = k < k1;
   const int e = live ? order[k] : order[k0];
+  if (I == 0) s_e[q] = live ? e : -1;
   const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
   Frame32 F;
   frame32(e32 + (long long)e * XK_ELEM32_STRIDE, n32 + (long long)a * XK_NODE32_STRIDE + 6,
@@ -636,14 +639,11 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
     sx[q][I][18 + i] = J[i];
   }
   __syncwarp();
-  if (!live) return;
   // row I of the symmetrised tangent: Ks[I][Jb] = (X_IJb + X_JbI^T) / 2 with
-  // X_I0 = G_I, X_I1 = H_I, X_I2 = -G_I, X_I3 = J_I
+  // X_I0 = G_I, X_I1 = H_I, X_I2 = -G_I, X_I3 = J_I, staged per block
 #pragma unroll
   for (int Jb = 0; Jb < 4; ++Jb) {
     const int nb = (I >> 1) * 2 + (Jb >> 1);  // 0 aa, 1 ab, 2 ba, 3 bb
-    float* dst = Kv + 36LL * blk[4LL * e + nb];
-    const bool fw = (fl >> nb) & 1;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -652,10 +652,26 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
         const float* o = sx[q][Jb];
         const int off = i1 ? 9 : ((I == 3) ? 18 : 0);
         const float xji = (i2 ? -1.f : 1.f) * o[off + 3 * c + r];
-        const float v = 0.5f * (xij + xji);
-        const int idx = (3 * (I & 1) + r) * 6 + 3 * (Jb & 1) + c;
-        if (fw) dst[idx] = v; else dst[idx] += v;
+        kst[q][nb][(3 * (I & 1) + r) * 6 + 3 * (Jb & 1) + c] = 0.5f * (xij + xji);
       }
+  }
+  __syncwarp();
+  // the warp's 8 elements x 4 blocks as 9 float4 per block (a block starts at 144 B * index), first
+  // writer of a block stores, later colours add
+  const int lane = threadIdx.x & 31, q0 = (threadIdx.x >> 5) * 8;
+  for (int t = lane; t < 8 * 4 * 9; t += 32) {
+    const int qq = q0 + t / 36, nb = (t % 36) / 9, ch = t % 9;
+    const int ee = s_e[qq];
+    if (ee < 0) continue;
+    const float4 v = reinterpret_cast<const float4*>(kst[qq][nb])[ch];
+    float4* dst = reinterpret_cast<float4*>(Kv + 36LL * blk[4LL * ee + nb]) + ch;
+    if ((first[ee] >> nb) & 1) {
+      *dst = v;
+    } else {
+      float4 o = *dst;
+      o.x += v.x; o.y += v.y; o.z += v.z; o.w += v.w;
+      *dst = o;
+    }
   }
 }
 
