@@ -308,6 +308,15 @@ xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream s);
 xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk_contact_params* cp, float* rec, int parts,
                          xk_stream s);
 
+/* Smooth (softplus) normal law for n gaps, element-wise:
+ * _evaluate_smooth_normal_force_vectorized (contact/penalty/law_normal.py:129-149):
+ * x = -g + lambda / k_pen, p_n = k_pen delta log(1 + exp(x / delta)),
+ * dp_dg = -k_pen sigmoid(x / delta), with |x / delta| > 30 cut off as there.
+ * lambdas may be NULL (all zero).  The reference's default law is the Huber
+ * law of the pair kernels; this one is its C-infinity variant. */
+xk_status xk_softplus_normal_law(int64_t n, const double* gaps, const double* lambdas, double k_pen, double delta,
+                                 double* p_n, double* dp_dg, xk_stream s);
+
 /* Constraint Jacobian rows c_k n of the non-INACTIVE pairs in table order
  * (_build_constraint_jacobian_ptp, xkep_cae/contact/geometry/strategy.py:83-132).
  * rows/cols/vals: [12*cap]; *n_rows (host) gets the number of active pairs;

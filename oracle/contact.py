@@ -324,6 +324,20 @@ def huber_delta(k_pen, smoothing_delta):
     return k_pen / smoothing_delta if smoothing_delta > 0.0 else 0.0
 
 
+def softplus_normal_law(gaps, k_pen: float, lambdas, delta: float = 1e-4):
+    """Smooth (softplus) normal law, ``_evaluate_smooth_normal_force_vectorized``
+    (``contact/penalty/law_normal.py:129-149``): p = k softplus(x, delta),
+    dp/dg = -k sigmoid(x / delta), x = -g + lambda / k, |x / delta| clipped at 30."""
+    gaps = np.asarray(gaps, dtype=float)
+    lambdas = np.asarray(lambdas, dtype=float)
+    x = -gaps + lambdas / k_pen if k_pen > 0.0 else -gaps
+    z = x / delta
+    ez = np.exp(np.clip(z, -30.0, 30.0))
+    sp = np.where(z > 30.0, x, np.where(z < -30.0, 0.0, delta * np.log1p(ez)))
+    sig = np.where(z > 30.0, 1.0, np.where(z < -30.0, 0.0, ez / (1.0 + ez)))
+    return k_pen * sp, -k_pen * sig
+
+
 def huber_evaluate(table: dict, ndof: int, k_pen: float, smoothing_delta: float = 0.0):
     """Normal force; writes ``p_n`` of every non-INACTIVE pair (``strategy.py:126-170``)."""
     t = copy_table(table)

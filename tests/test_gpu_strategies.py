@@ -174,3 +174,14 @@ def test_cr_beam_assembler(precision, tol):
     assert rel_err(M.diagonal(), me) < 1e-14
     with pytest.raises(NotImplementedError):
         asm.assemble_mass(7.85e-9, lumped=False)
+
+
+def test_smooth_normal_law_matches_reference():
+    z = golden("laws")
+    p, dp = S.smooth_normal_force(z["gap"], float(z["k_pen"]), z["lam"], delta=float(z["delta"]))
+    assert rel_err(p, z["p_n"]) < 1e-14 and rel_err(dp, z["dp_dg"]) < 1e-14
+    # the cut-offs and the lambda-free form
+    g = np.linspace(-1e-2, 1e-2, 2001)
+    p0, d0 = S.smooth_normal_force(g, 1e5, None, delta=1e-4)
+    pe, de = oc.softplus_normal_law(g, 1e5, np.zeros_like(g), 1e-4)
+    assert rel_err(p0, pe) < 1e-14 and rel_err(d0, de) < 1e-14

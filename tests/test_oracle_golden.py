@@ -122,3 +122,9 @@ def test_genalpha_oracle_matches_reference():
             assert np.allclose(ga.effective_stiffness_diag(dt), z[p + "K_eff_diag"], rtol=1e-12, atol=0)
             rng.normal(size=m.size)  # u1 noise
             rng.normal(size=m.size)  # R
+
+
+def test_softplus_law_oracle_matches_reference():
+    z = golden("laws")
+    p, dp = oc.softplus_normal_law(z["gap"], float(z["k_pen"]), z["lam"], float(z["delta"]))
+    assert np.array_equal(p, z["p_n"]) and np.array_equal(dp, z["dp_dg"])

@@ -922,6 +922,33 @@ extern "C" xk_status xk_pair_step(const xk_mesh* m, xk_pairs* p, const xk_contac
   return XK_OK;
 }
 
+namespace {
+// Smooth (softplus) normal law, element-wise: _evaluate_smooth_normal_force_vectorized
+// (contact/penalty/law_normal.py:129-149); exp and log1p are the CUDA double functions.
+__global__ void k_softplus_law(long long n, const double* __restrict__ g, const double* __restrict__ lam, double k,
+                               double delta, double* __restrict__ p, double* __restrict__ dp) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x = k > 0.0 ? xadd(-g[i], lam ? xdiv(lam[i], k) : 0.0) : -g[i];
+  const double z = xdiv(x, delta);
+  const double ez = exp(z < -30.0 ? -30.0 : (z > 30.0 ? 30.0 : z));
+  const double sp = z > 30.0 ? x : (z < -30.0 ? 0.0 : xmul(delta, log1p(ez)));
+  const double sig = z > 30.0 ? 1.0 : (z < -30.0 ? 0.0 : xdiv(ez, xadd(1.0, ez)));
+  p[i] = xmul(k, sp);
+  dp[i] = xmul(-k, sig);
+}
+}  // namespace
+
+extern "C" xk_status xk_softplus_normal_law(int64_t n, const double* gaps, const double* lambdas, double k_pen,
+                                            double delta, double* p_n, double* dp_dg, xk_stream s) {
+  if (n < 0 || (n > 0 && (!gaps || !p_n || !dp_dg)) || !(delta > 0.0))
+    return xk_set_error(XK_ERR_ARG, "xk_softplus_normal_law: bad arguments");
+  if (n == 0) return XK_OK;
+  k_softplus_law<<<xk_blocks(n, 256), 256, 0, (cudaStream_t)s>>>(n, gaps, lambdas, k_pen, delta, p_n, dp_dg);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
 extern "C" xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p, int32_t* rows, int32_t* cols,
                                             double* vals, int32_t* pair_index, int64_t cap, int64_t* n_rows,
                                             xk_stream s) {

@@ -91,6 +91,7 @@ SIGNATURES = {
     "xk_constraint_jacobian": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
     "xk_constraint_jacobian_noalloc": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
     "xk_norm2": [vp, C.c_int64, vp, vp],
+    "xk_softplus_normal_law": [C.c_int64, vp, vp, C.c_double, C.c_double, vp, vp, vp],
     "xk_nodes_prepare": [P(Mesh), vp, vp, vp, vp],
     "xk_beam_prepare32": [P(Mesh), vp, vp, vp],
     "xk_beam_assemble32": [P(Mesh), P(Section), vp, P(BeamPlan), vp, vp, vp, vp],

@@ -413,6 +413,22 @@ class GpuHuberContactForce:
         return batch.tangent(L.XK_WHICH_NORMAL, self._ndof)
 
 
+def smooth_normal_force(gaps, k_pen: float, lambdas=None, *, delta: float = 1e-4, device=None):
+    """``_evaluate_smooth_normal_force_vectorized`` (``contact/penalty/law_normal.py:129-149``) on the GPU.
+
+    Returns ``(p_n, dp_dg)`` as NumPy arrays (or device tensors for device input).
+    """
+    dev = require_cuda(device)
+    on_dev = isinstance(gaps, torch.Tensor) and gaps.is_cuda
+    g = _dev_vec(gaps, dev) if not on_dev else gaps.to(torch.float64).contiguous()
+    lam = None if lambdas is None else (_dev_vec(lambdas, dev) if not on_dev else lambdas.to(torch.float64))
+    p = torch.empty_like(g)
+    dp = torch.empty_like(g)
+    L.call("xk_softplus_normal_law", g.numel(), ptr(g), ptr(lam), float(k_pen), float(delta), ptr(p), ptr(dp),
+           stream_handle())
+    return (p, dp) if on_dev else (p.cpu().numpy(), dp.cpu().numpy())
+
+
 # ----------------------------------------------------------------------------- friction
 
 
