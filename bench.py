@@ -209,6 +209,55 @@ def _time_replay(eng, steps, warmup):
     return a.elapsed_time(b) / steps
 
 
+MLP_FLOPS_PER_SAMPLE = 2 * (8 * 64 + 64 * 64 + 64 * 64 + 64)  # algorithmic: inputs 8 -> 64 -> 64 -> 64 -> 1
+
+
+def _bf16_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+def mlp_scoring(pr, sizes, steps, warmup, dev):
+    """Pruning-network scoring time per launch (CUDA events) on both tensor-core
+    kernels, on seeded feature rows in the ranges the geometry produces; the
+    tcgen05 figure carries a tensor roofline against the measured bf16 peak."""
+    import torch
+
+    peak, kind = _bf16_peak()
+    out = {}
+    for n in sizes:
+        rng = np.random.default_rng(11)
+        X = np.zeros((n, 8), np.float32)
+        X[:, 0] = rng.uniform(0.5, 8.0, n)
+        X[:, 1] = rng.uniform(0.0, 1.0, n)
+        X[:, 2] = rng.uniform(1.0, 6.0, n)
+        X[:, 5] = rng.uniform(-2.0, 8.0, n)
+        feat = torch.as_tensor(X.ravel(), device=dev)
+        row = {}
+        for b in ("mma", "tcgen05"):
+            for _ in range(warmup):
+                pr.logits(feat, n, backend=b)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(steps):
+                pr.logits(feat, n, backend=b)
+            e1.record()
+            torch.cuda.synchronize()
+            row[f"{b}_us"] = 1e3 * e0.elapsed_time(e1) / steps
+        if pr.tcgen05_failed():
+            row["tcgen05_failed"] = True
+        tf = n * MLP_FLOPS_PER_SAMPLE / (row["tcgen05_us"] * 1e-6) / 1e12
+        row["tcgen05_tflops"] = tf
+        row["tcgen05_frac_of_" + kind + "_bf16"] = tf / peak
+        row["speedup_vs_mma_sync"] = row["mma_us"] / row["tcgen05_us"]
+        out[str(n)] = row
+        del feat
+    return out
+
+
 def pruning_section(args, dev, w, u0, u1, ms_fp64):
     """The mixed assembly with the learned candidate pruning, per Newton iteration.
 
@@ -282,6 +331,7 @@ def pruning_section(args, dev, w, u0, u1, ms_fp64):
            "detect_ms_judged": 1e3 * t_det, "detect_ms_without_pruning": 1e3 * t_det_ref,
            "R_rel_diff_vs_unpruned": R_diff, "train_s": t_train, "train": dataclasses.asdict(rep),
            "judge_every": eng.judge_every}
+    out["scoring"] = mlp_scoring(pr, (stats["candidates"], 8_000_000), 20, 3, dev)
     del eng, pr
     torch.cuda.empty_cache()
     return out
@@ -609,6 +659,13 @@ def run_profile(args):
     from xkgpu import workloads as W
     from xkgpu.engine import AssemblyEngine
 
+    if args.profile == "mlp":
+        # pruning-network scoring on --mlp-n seeded feature rows, --steps launches of each kernel
+        from xkgpu import prune as P
+
+        print(json.dumps({"profile": "mlp", "n": args.mlp_n,
+                          "scoring": mlp_scoring(P.PairPruner(), (args.mlp_n,), args.steps, 1, "cuda")}))
+        return
     w = W.config_workload(args.workload, seed=0)
     st = w.strand
     eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=args.profile, **w.engine_kwargs())
@@ -700,7 +757,8 @@ def main():
     ap.add_argument("--workload", default="strand1027")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the learned-pruning and batched sections")
-    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+    ap.add_argument("--mlp-n", type=int, default=8_000_000, help="samples scored by --profile mlp")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "mlp"], default=None,
                     help="profiling driver: detect once, then --steps eager assemblies, no timing")
     ap.add_argument("--breakdown", action="store_true", help="warm per-phase times (ms) of one assembly")
     args = ap.parse_args()

@@ -375,6 +375,14 @@ xk_status xk_prune_features(const xk_mesh* m, const double* u, const int32_t* ca
  * params_bf16: XK_MLP_PARAMS bfloat16 values. */
 xk_status xk_mlp_forward(const uint16_t* params_bf16, const float* feat, int64_t n, float* logit, xk_stream s);
 
+/* The same logits on the 5th-generation tensor cores: tcgen05.mma (BF16 ->
+ * FP32) into a TMEM accumulator, 128 samples per tile, bias and ReLU applied
+ * on the read-back.  params_bf16 and feat 16-byte aligned.  *err (device
+ * int, caller-zeroed) is set to 1 if a tensor-core completion wait expired;
+ * the logits are then undefined. */
+xk_status xk_mlp_forward_tcgen05(const uint16_t* params_bf16, const float* feat, int64_t n, float* logit,
+                                 int* err, xk_stream s);
+
 /* Training: forward with stored activations (act: XK_MLP_ACT planes of n
  * floats), backward of the weighted mean binary cross-entropy (dvec: 192
  * planes of n; g: n; grad: XK_MLP_PARAMS, reduced in a fixed order; *loss on

@@ -51,3 +51,17 @@ def test_struct_layouts_match_header():
     assert C.sizeof(L.ContactParams) == 6 * 8 + 8
     assert C.sizeof(L.BPParams) == 8 + 3 * 4 + 4 + 8
     assert C.sizeof(L.ContactPattern) == 16 + 5 * 8 + 10 * 8 + 2 * 8 + 6 * 8
+
+
+def test_argument_checks_before_any_launch(lib):
+    """Malformed calls are refused on the host with XK_ERR_ARG, before any device work (no GPU needed)."""
+    import ctypes as C
+
+    lib.xk_mlp_forward_tcgen05.restype = C.c_int
+    lib.xk_mlp_forward_tcgen05.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.xk_last_error.restype = C.c_char_p
+    # null parameters, negative count, misaligned feature rows
+    assert lib.xk_mlp_forward_tcgen05(None, None, 0, None, None, None) == 1
+    assert lib.xk_mlp_forward_tcgen05(0x1000, 0x2000, -1, 0x3000, 0x4000, None) == 1
+    assert lib.xk_mlp_forward_tcgen05(0x1000, 0x2004, 8, 0x3000, 0x4000, None) == 1
+    assert b"16-byte aligned" in lib.xk_last_error()

@@ -80,22 +80,41 @@ def test_features_match_oracle():
     assert np.array_equal(hist[:nc].cpu().numpy().astype(bool), hist_exp)
 
 
-@pytest.mark.parametrize("n", [1, 37, 4096 + 5])
+@pytest.mark.parametrize("n", [1, 37, 4096 + 5, 128 * 152 * 4 * 2 + 77])
 def test_forward_matches_oracle(n):
     th = _theta(1)
     X = _random_batch(n, 3)
     pr = P.PairPruner(th)
     feat = torch.as_tensor(X.ravel(), device="cuda")
     exp, _ = M.forward(th, X)
-    tc = pr.logits(feat, n).cpu().numpy()          # tensor cores
-    _, lt = pr.train_forward(feat, n)               # training kernel
+    mma = pr.logits(feat, n, backend="mma").cpu().numpy()       # mma.sync tensor cores
+    tc5 = pr.logits(feat, n, backend="tcgen05").cpu().numpy()   # tcgen05, TMEM accumulators
+    assert not pr.tcgen05_failed()
+    _, lt = pr.train_forward(feat, n)                           # training kernel
     scale = max(1.0, float(np.max(np.abs(exp))))
     # float sums in another order round the odd activation that sits at a bfloat16 tie to the
     # neighbouring value: nearly every row agrees to float rounding, the rest by one bfloat16 step
-    for got in (tc, lt.cpu().numpy()):
+    for got in (mma, tc5, lt.cpu().numpy()):
         d = np.abs(got - exp)
         assert np.mean(d > 1e-5 * scale) <= 0.01
         assert np.max(d) <= 2.0**-6 * scale
+
+
+def test_tcgen05_forward_reuses_pruner_and_zero_rows():
+    """Zero feature rows give the network's constant response; repeated calls agree bit for bit."""
+    th = _theta(4)
+    pr = P.PairPruner(th, backend="tcgen05")
+    n = 1000
+    X = _random_batch(n, 5)
+    X[::3] = 0.0
+    feat = torch.as_tensor(X.ravel(), device="cuda")
+    a = pr.logits(feat, n).cpu().numpy()
+    b = pr.logits(feat, n).cpu().numpy()
+    assert not pr.tcgen05_failed()
+    assert np.array_equal(a, b)
+    assert np.all(a[::3] == a[0])
+    exp, _ = M.forward(th, X)
+    assert np.max(np.abs(a - exp)) <= 2.0**-6 * max(1.0, float(np.max(np.abs(exp))))
 
 
 def test_gradient_and_adam_match_oracle():

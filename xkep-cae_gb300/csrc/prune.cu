@@ -4,9 +4,11 @@
 // activations, backward, deterministic weight-gradient reduction, Adam) and the
 // selection / pair-table compaction that apply it at detection time.
 //
-// Inference runs on the tensor cores (mma.sync m16n8k16 BF16 -> FP32): a warp
-// takes 16 candidates, and each layer's accumulator fragments are rounded to
-// BF16 and re-packed in registers as the next layer's A operand.  Training runs
+// Inference runs on the tensor cores, in two forms: tcgen05.mma with the
+// accumulator in TMEM, 128 candidates per CTA tile (the default), and
+// mma.sync m16n8k16 (BF16 -> FP32), where a warp takes 16 candidates and each
+// layer's accumulator fragments are re-packed in registers as the next layer's
+// A operand.  Training runs
 // one sample per thread in FP32 on BF16-rounded operands, which is the same
 // arithmetic up to the order of the float sums.
 #include <cuda_bf16.h>
@@ -180,6 +182,263 @@ __global__ void __launch_bounds__(32 * FW_WARPS) k_mlp_forward_mma(const uint16_
       if (r0 < n) logit[r0] = s0 + b4;
       if (r1 < n) logit[r1] = s1 + b4;
     }
+  }
+}
+
+// ------------------------------------------------------------------ inference (tcgen05, TMEM accumulators)
+//
+// One CTA of 128 threads per tile of 128 candidates, persistent over tiles.
+// Operands live in shared memory in the canonical K-major layout without
+// swizzle: 8-row x 16-byte core matrices (row r of a core at +16 r), cores
+// adjacent along K LBO = 128 B apart, 8-row groups SBO apart.  Thread 0 issues
+// tcgen05.mma (kind::f16, BF16 in, FP32 accumulate, M 128, N 64, K 16 per
+// instruction) into a 64-column TMEM accumulator and commits to an mbarrier;
+// the four warps read their 32 lanes (rows) back with tcgen05.ld, add the bias,
+// apply ReLU, round to BF16 and write the next layer's operand tile.
+// Every wait is bounded: on expiry the kernel sets *err, skips the remaining
+// work, and still frees its TMEM.
+
+constexpr int TC_T = 128;
+constexpr int TC_PER_SM = 5;
+constexpr uint32_t TC_COLS = 64;
+// instruction descriptor: D f32 (bit 4), A bf16 (bits 7-9 = 1), B bf16 (bits 10-12 = 1),
+// K-major A and B (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr long long TC_SPIN = 1LL << 22;
+
+XK_D uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start >> 4 (bits 0-13), LBO >> 4 (16-29), SBO >> 4 (32-45),
+// fixed 0b001 at bits 46-48, no base offset, relative LBO, no swizzle (bits 61-63 = 0)
+XK_D uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+XK_D void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+      :
+      : "r"(dtmem), "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate));
+}
+
+XK_D void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+               : "memory");
+}
+
+// bounded wait for the mbarrier phase `parity`; false on expiry
+XK_D bool tc_wait(uint32_t mbar, uint32_t parity) {
+  for (long long it = 0; it < TC_SPIN; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 16 consecutive fp32 columns of this thread's TMEM lane
+XK_D void tc_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+XK_D void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+XK_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+XK_D void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+XK_D void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// byte offset of element (row, k) (16-bit elements) in a K-major no-swizzle tile with K columns
+XK_D uint32_t core_off(int row, int k, int K) {
+  return (uint32_t)((row >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// The biases ride in the MMAs: layer 1's operand has a constant-one column
+// (k = 8) matched by b1 in W1's padding, and layers 2 and 3 add one K-16 MMA
+// of a constant tile (column 0 = 1) against a bias tile (column 0 = b).  The
+// BF16 biases times 1 are exact in the FP32 accumulator.
+struct __align__(128) TcSmem {
+  // hidden operand (layers 2 and 3); its first 4 KB also hold the layer-1 operand
+  // (128 candidates x K 16: 8 features, 1, 7 zeros), read only before the hidden
+  // operand is first written for the tile
+  uint16_t a2[128 * 64];
+  uint16_t ones[128 * 16];  // 128 x K 16, column 0 = 1
+  uint16_t w1[64 * 16];     // [W1 | b1 | 0] as N 64 x K 16
+  uint16_t w2[64 * 64];
+  uint16_t w3[64 * 64];
+  uint16_t bb2[64 * 16];    // column 0 = b2
+  uint16_t bb3[64 * 16];    // column 0 = b3
+  float w4[64];
+  float b4;
+  uint64_t mbar;
+  uint32_t tmem;
+};
+
+// two floats -> bf16x2 (lo in the low half), each max(x, 0) rounded to nearest even
+XK_D uint32_t pack_relu_bf16(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;\n" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
+__global__ void __launch_bounds__(TC_T) k_mlp_forward_tc(const uint16_t* __restrict__ P,
+                                                         const float* __restrict__ feat, long long n,
+                                                         float* __restrict__ logit, int* __restrict__ err) {
+  __shared__ TcSmem sm;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // weights in the operand layout (N rows = outputs, K = inputs), biases as float
+  constexpr uint16_t BF16_ONE = 0x3F80;
+  for (int i = tid; i < 64 * 16; i += TC_T) {
+    const int nn = i >> 4, k = i & 15;
+    const uint16_t v = k < MF ? P[O_W1 + nn * MF + k] : k == MF ? P[O_B1 + nn] : (uint16_t)0;
+    const uint32_t o = core_off(nn, k, 16);
+    *reinterpret_cast<uint16_t*>(reinterpret_cast<char*>(sm.w1) + o) = v;
+    *reinterpret_cast<uint16_t*>(reinterpret_cast<char*>(sm.bb2) + o) = k == 0 ? P[O_B2 + nn] : (uint16_t)0;
+    *reinterpret_cast<uint16_t*>(reinterpret_cast<char*>(sm.bb3) + o) = k == 0 ? P[O_B3 + nn] : (uint16_t)0;
+  }
+  for (int i = tid; i < 128 * 16; i += TC_T) {
+    const int r = i >> 4, k = i & 15;
+    *reinterpret_cast<uint16_t*>(reinterpret_cast<char*>(sm.ones) + core_off(r, k, 16)) =
+        k == 0 ? BF16_ONE : (uint16_t)0;
+  }
+  // W2, W3: one 16-byte core-matrix row (8 consecutive k of output nn) per copy; the
+  // parameter offsets of both are multiples of 8 elements
+  static_assert(O_W2 % 8 == 0 && O_W3 % 8 == 0, "16-byte weight rows");
+  for (int i = tid; i < 64 * 8; i += TC_T) {
+    const int nn = i >> 3, kc = i & 7;
+    const uint32_t o = core_off(nn, 8 * kc, 64);
+    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm.w2) + o) = *reinterpret_cast<const uint4*>(P + O_W2 + 8 * i);
+    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm.w3) + o) = *reinterpret_cast<const uint4*>(P + O_W3 + 8 * i);
+  }
+  if (tid < 64) sm.w4[tid] = bf16_at(P, O_W4 + tid);
+  if (tid == 0) {
+    sm.b4 = bf16_at(P, O_B4);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sm.mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&sm.tmem)),
+                 "r"(TC_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem;
+  const uint32_t mbar = smem_u32(&sm.mbar);
+  const uint32_t lane_base = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 TMEM lanes
+  uint32_t phase = 0;
+  bool ok = true;
+  const long long tiles = (n + 127) / 128;
+  // features of this thread's row of a tile (zero beyond n); the next tile's are loaded while
+  // the current tile runs its layers
+  auto load_row = [&](long long tile, float4& lo, float4& hi) {
+    const long long row = tile * 128 + tid;
+    if (tile < tiles && row < n) {
+      const float4* f4 = reinterpret_cast<const float4*>(feat + MF * row);
+      lo = __ldcs(f4);
+      hi = __ldcs(f4 + 1);
+    } else {
+      lo = hi = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+  float4 x_lo, x_hi;
+  load_row(blockIdx.x, x_lo, x_hi);
+  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const long long row = tile * 128 + tid;  // thread tid owns tile row tid (its TMEM lane)
+    {  // layer-1 operand: the features rounded to bf16, the one for b1, zeros
+      uint4 v0, v1;
+      v0.x = pack_bf16(x_lo.x, x_lo.y); v0.y = pack_bf16(x_lo.z, x_lo.w);
+      v0.z = pack_bf16(x_hi.x, x_hi.y); v0.w = pack_bf16(x_hi.z, x_hi.w);
+      v1.x = BF16_ONE;  // k = 8: the constant-one column that carries b1
+      v1.y = v1.z = v1.w = 0u;
+      *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm.a2) + core_off(tid, 0, 16)) = v0;
+      *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm.a2) + core_off(tid, 8, 16)) = v1;
+    }
+    load_row(tile + gridDim.x, x_lo, x_hi);
+    float out = 0.f;
+#pragma unroll 1
+    for (int layer = 0; layer < 3 && ok; ++layer) {
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      if (tid == 0) {
+        if (layer == 0) {
+          tc_mma(tmem, tc_desc(smem_u32(sm.a2), 128, 256), tc_desc(smem_u32(sm.w1), 128, 256), 0u);
+        } else {
+          const uint16_t* w = layer == 1 ? sm.w2 : sm.w3;
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks)
+            tc_mma(tmem, tc_desc(smem_u32(sm.a2) + ks * 256, 128, 1024), tc_desc(smem_u32(w) + ks * 256, 128, 1024),
+                   ks > 0 ? 1u : 0u);
+          tc_mma(tmem, tc_desc(smem_u32(sm.ones), 128, 256), tc_desc(smem_u32(layer == 1 ? sm.bb2 : sm.bb3), 128, 256),
+                 1u);
+        }
+        tc_commit(mbar);
+      }
+      // the outcome of the wait is made uniform over the block before anyone acts on it
+      if (__syncthreads_or(tc_wait(mbar, phase) ? 0 : 1)) {
+        ok = false;
+        break;
+      }
+      phase ^= 1u;
+      tc_fence_after();
+      // the MMA that read the operand tile has completed, so the next operand is written in
+      // place; the next MMA is issued only after the barrier at the top of the layer loop,
+      // which every thread reaches after its tcgen05.ld has retired
+      float z[64];
+      tc_ld16(lane_base + 0, z);
+      tc_ld16(lane_base + 16, z + 16);
+      tc_ld16(lane_base + 32, z + 32);
+      tc_ld16(lane_base + 48, z + 48);
+      tc_wait_ld();
+      if (layer < 2) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          uint4 v;
+          v.x = pack_relu_bf16(z[8 * c + 0], z[8 * c + 1]);
+          v.y = pack_relu_bf16(z[8 * c + 2], z[8 * c + 3]);
+          v.z = pack_relu_bf16(z[8 * c + 4], z[8 * c + 5]);
+          v.w = pack_relu_bf16(z[8 * c + 6], z[8 * c + 7]);
+          *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm.a2) + core_off(tid, 8 * c, 64)) = v;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 64; j += 2) {
+          const uint32_t h = pack_relu_bf16(z[j], z[j + 1]);
+          out = fmaf(__uint_as_float(h << 16), sm.w4[j], out);
+          out = fmaf(__uint_as_float(h & 0xFFFF0000u), sm.w4[j + 1], out);
+        }
+      }
+      if (layer == 2) out += sm.b4;
+    }
+    if (ok && row < n) logit[row] = out;
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+  if (!ok && tid == 0) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_COLS) : "memory");
   }
 }
 
@@ -476,6 +735,31 @@ extern "C" xk_status xk_mlp_forward(const uint16_t* params_bf16, const float* fe
   long long blocks = (tiles + FW_WARPS - 1) / FW_WARPS;
   if (blocks > 152 * 16) blocks = 152 * 16;  // grid-stride beyond 16 blocks per SM
   k_mlp_forward_mma<<<(int)blocks, 32 * FW_WARPS, 0, (cudaStream_t)s>>>(params_bf16, feat, n, logit);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
+
+extern "C" xk_status xk_mlp_forward_tcgen05(const uint16_t* params_bf16, const float* feat, int64_t n, float* logit,
+                                            int* err, xk_stream s) {
+  if (!params_bf16 || !err || n < 0 || (n > 0 && (!feat || !logit)))
+    return xk_set_error(XK_ERR_ARG, "xk_mlp_forward_tcgen05: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(params_bf16) & 15) || (reinterpret_cast<uintptr_t>(feat) & 15))
+    return xk_set_error(XK_ERR_ARG, "xk_mlp_forward_tcgen05: params and feat must be 16-byte aligned");
+  if (n == 0) return XK_OK;
+  // persistent grid of TC_PER_SM CTAs per SM: each CTA runs its tiles' three layers back to back
+  // (MMA, completion wait, read-back), so several CTAs per SM overlap one's MMA with another's
+  // read-back; five measured best on 400k-8M samples (4 to 8 within 15%)
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const long long resident = (long long)TC_PER_SM * sms;
+  const long long tiles = (n + 127) / 128;
+  const int blocks = (int)(tiles < resident ? tiles : resident);
+  k_mlp_forward_tc<<<blocks, TC_T, 0, (cudaStream_t)s>>>(params_bf16, feat, n, logit, err);
   XK_CHECK_LAUNCH();
   return XK_OK;
 }

@@ -104,6 +104,7 @@ SIGNATURES = {
     "xk_add_diagonal": [C.c_int64, vp, vp, C.c_double, C.c_int, vp, vp],
     "xk_prune_features": [P(Mesh), vp, vp, C.c_int64, P(Pairs), vp, vp, vp],
     "xk_mlp_forward": [vp, vp, C.c_int64, vp, vp],
+    "xk_mlp_forward_tcgen05": [vp, vp, C.c_int64, vp, vp, vp],
     "xk_mlp_train_forward": [vp, vp, C.c_int64, vp, vp, vp],
     "xk_mlp_backward": [vp, vp, vp, vp, vp, vp, C.c_int64, vp, vp, vp, vp, vp],
     "xk_mlp_adam": [vp, vp, vp, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, vp, vp],

@@ -150,6 +150,11 @@ class AssemblyEngine:
         st = self.prune_stats
         st["detections"] += 1
         st["candidates"] += nc
+        if pr.backend == "tcgen05" and pr.tcgen05_failed():
+            # the scores are undefined after an expired tensor-core wait: keep every candidate
+            st["scoring_failed"] = st.get("scoring_failed", 0) + 1
+            st["kept"] += nc
+            return cands, nc
         if self._n_detect % self.judge_every == 0:
             # judge: the exact narrowphase of every pruned candidate; any that the exact path would
             # activate is a missed contact and the whole candidate set is used instead

@@ -64,7 +64,7 @@ class PairPruner:
     """The pruning network: parameters on the device, training and scoring through the C ABI."""
 
     def __init__(self, theta: np.ndarray | None = None, *, threshold: float = -np.inf, label_margin: float = 0.1,
-                 seed: int = 0, device=None):
+                 seed: int = 0, device=None, backend: str = "tcgen05"):
         self.device = require_cuda(device)
         th = init_params(seed) if theta is None else np.asarray(theta, np.float32)
         if th.size != NPARAM:
@@ -76,6 +76,8 @@ class PairPruner:
         self.step = 0
         self.threshold = float(threshold)
         self.label_margin = float(label_margin)
+        self.backend = backend
+        self._tc_err = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.sync_bf16()
 
     # ------------------------------------------------------------------ parameters
@@ -101,10 +103,24 @@ class PairPruner:
                ptr(hist), stream_handle(stream))
         return feat, hist
 
-    def logits(self, feat: torch.Tensor, n: int, stream=None) -> torch.Tensor:
+    def logits(self, feat: torch.Tensor, n: int, stream=None, backend: str | None = None) -> torch.Tensor:
+        """Scores of n samples.  backend "mma" (mma.sync) or "tcgen05" (TMEM
+        accumulators); default: the pruner's ``backend`` attribute."""
         out = torch.empty(max(n, 1), dtype=torch.float32, device=self.device)
-        L.call("xk_mlp_forward", ptr(self.theta_bf16), ptr(feat), int(n), ptr(out), stream_handle(stream))
+        b = backend or self.backend
+        if b == "tcgen05":
+            self._tc_err.zero_()
+            L.call("xk_mlp_forward_tcgen05", ptr(self.theta_bf16), ptr(feat), int(n), ptr(out), ptr(self._tc_err),
+                   stream_handle(stream))
+        elif b == "mma":
+            L.call("xk_mlp_forward", ptr(self.theta_bf16), ptr(feat), int(n), ptr(out), stream_handle(stream))
+        else:
+            raise ValueError(f"unknown backend {b!r}")
         return out[:n]
+
+    def tcgen05_failed(self) -> bool:
+        """True if the last tcgen05 scoring hit an expired completion wait (synchronises)."""
+        return bool(self._tc_err.item())
 
     def train_forward(self, feat: torch.Tensor, n: int, stream=None):
         act = torch.empty(L.MLP_ACT * n, dtype=torch.float32, device=self.device)
