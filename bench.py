@@ -164,8 +164,9 @@ def pair_kernel_bytes(n_nodes, n_elems, n_others, n_members, mixed: bool):
 
     Mixed path (float state): the node-preparation kernel reads X, u, u_ref
     (72 B) and writes a 64 B node record that the pair kernels read back
-    (64 B); element radii 8 B; a non-contributing pair reads 36 B and writes
-    48 B; a contributing pair reads 78 B, writes 70 B and its 64 B record.
+    (64 B); element radii 8 B; a non-contributing pair reads 48 B (node ids,
+    radius sum, previous normal and t1) and writes 36 B (s, t, gap, normal,
+    t1); a contributing pair reads 78 B, writes 70 B and its 64 B record.
     """
     if mixed:
         return (72 + 64 + 64) * n_nodes + 8 * n_elems + 84 * n_others + 212 * n_members
@@ -180,13 +181,15 @@ def gather_tangent_bytes(n_members, n_contrib, nnzb, mixed: bool, sides: bool = 
     of a record by the blocks it feeds are L2 traffic.  Contributor-list
     schedules also read each list entry (4 B) and block pointer (4 B).  The
     element-side schedule instead reads each member's two element-incidence
-    entries (8 B), the element pointers (4 B), writes and reads back the 27
-    element sums of every element, and reads four inline terms per block (16 B).
+    entries (8 B) and the element pointers (4 B), writes every element's three
+    tangent sums (12 values each: the 9 of the sum and the weight slots that a
+    term load reads) and its 8 force-sum values, reads the tangent sums back
+    once, and reads four inline terms per block (16 B).
     """
     w = 4 if mixed else 8
     if sides:
-        return (16 * w * n_members + 8 * n_members + 4 * (n_elems + 1) + 2 * 27 * w * n_elems + 16 * nnzb
-                + 9 * w * nnzb)
+        return (16 * w * n_members + 8 * n_members + 4 * (n_elems + 1) + (36 + 8 + 36) * w * n_elems
+                + 16 * nnzb + 9 * w * nnzb)
     return 16 * w * n_members + 4 * n_contrib + 4 * (nnzb + 1) + 9 * w * nnzb
 
 
@@ -505,14 +508,16 @@ def run_gpu(args, rank, world):
     m = pat.n_members
     by_mixed = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, True)
     by_fp64 = pair_kernel_bytes(st.n_nodes, n_e, n_c - m, m, False)
-    bg_mixed = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, True,
-                                    engines["mixed"].gather_variant == L.XK_GATHER_SIDES, n_e)
-    bg_fp64 = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, False,
-                                   engines["fp64"].gather_variant == L.XK_GATHER_SIDES, n_e)
+    sides = (L.XK_GATHER_SIDES,)
+    bg_mixed = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, True, engines["mixed"].gather_variant in sides, n_e)
+    bg_fp64 = gather_tangent_bytes(m, pat.n_contrib, pat.nnzb, False, engines["fp64"].gather_variant in sides, n_e)
     variant_name = {L.XK_GATHER_LANES: "lanes", L.XK_GATHER_CHUNKS: "chunks", L.XK_GATHER_SIDES: "sides"}
     kernel_names = {L.XK_GATHER_LANES: "k_gather_tangent_lanes<float>", L.XK_GATHER_CHUNKS: "k_gather_tangent<float>",
                     L.XK_GATHER_SIDES: "k_elem_sums<float> + k_gather_tangent_sides<float>"}
     peak, peak_kind = _peaks()
+    # the autotuner's times of every tangent schedule (ms per call), before the engines are released
+    sched_ms = {p: {variant_name[v]: round(t, 4) for v, t in getattr(engines[p], "tune_times", {}).items()}
+                for p in ("mixed", "fp64")}
 
     # end to end through the public engine API with host buffers: each step copies u and u_ref in from
     # pinned host memory and reads R, K_beam and K_c back; the read-back of one step overlaps the next
@@ -568,8 +573,9 @@ def run_gpu(args, rank, world):
         extras["learned_pruning"] = pruning_section(args, dev, w, u0, u1, ms_fp64)
         extras["batched"] = batch_section(args, dev)
 
-    # node prep, 2 pair kernels, 2 beam colours, force gather, 2 norm kernels, tangent gather (+ element sums)
-    per_launch = 9 + (1 if mixed_variant == L.XK_GATHER_SIDES else 0)
+    # node prep, 2 pair kernels, 2 beam colours, then either element sums + tangent gather + residual from
+    # the element sums (norm fused) or tangent gather + force gather + 2 norm kernels
+    per_launch = 5 + (3 if mixed_variant == L.XK_GATHER_SIDES else 4)
     out = {
         "metric": METRIC, "value": units / t_mixed * args.steps, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
@@ -592,9 +598,11 @@ def run_gpu(args, rank, world):
                      "achieved": bg_mixed / tg_mixed / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": bg_mixed / tg_mixed / 1e9 / peak, "peak_kind": peak_kind,
                      "bytes_per_launch": bg_mixed, "launch_ms": 1e3 * tg_mixed, "traffic": None,
+                     "schedule_ms": sched_ms["mixed"],
                      "fp64_kernel": {"achieved": bg_fp64 / tg_fp64 / 1e9, "launch_ms": 1e3 * tg_fp64,
                                      "bytes_per_launch": bg_fp64,
-                                     "schedule": variant_name.get(fp64_variant, "default")},
+                                     "schedule": variant_name.get(fp64_variant, "default"),
+                                     "schedule_ms": sched_ms["fp64"]},
                      "pair_step": {"kernels": "k_nodes_prepare + k_pair_other32 + k_pair_member32 (narrowphase, "
                                               "Huber, Coulomb, pair tangent)",
                                    "achieved": by_mixed / tk_mixed / 1e9, "frac": by_mixed / tk_mixed / 1e9 / peak,
@@ -680,6 +688,7 @@ def run_profile(args):
     pat = eng.pattern
     print(json.dumps({"profile": args.profile, "workload": args.workload, **stats, "nnzb": pat.nnzb,
                       "n_contrib": pat.n_contrib, "gather_variant": eng.gather_variant,
+                      "schedule_ms": {str(k): v for k, v in eng.tune_times.items()},
                       "device_bytes_peak": torch.cuda.max_memory_allocated()}))
 
 
@@ -720,6 +729,8 @@ def run_breakdown(args):
             "force_gather+norm": lambda: L.call("xk_contact_gather_force", pat, ptr(eng.rec), p, L.XK_OUT_COMBINED,
                                                 L.XK_WHICH_COMBINED, ptr(eng.f_int), -1.0, None, None, ptr(eng.R),
                                                 ptr(eng.norm2), sh),
+            "force_from_elem_sums+norm": lambda: L.call("xk_contact_gather_force_elem", pat, p, ptr(eng.f_int), -1.0,
+                                                        None, None, ptr(eng.R), ptr(eng.norm2), sh),
             "tangent_gather_lanes": lambda: L.call("xk_contact_gather_tangent", pat, ptr(eng.rec), p,
                                                    L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_LANES,
                                                    ptr(eng.K_c), sh),

@@ -91,6 +91,11 @@ typedef struct {
   const uint8_t* first;          /* [n_elems] bits 0..3: this element is the first writer of
                                     block aa, ab, ba, bb (aa / bb also: of the f rows of a / b) */
   int64_t nnzb;
+  const int32_t* node_diag;      /* [n_nodes] or NULL: diagonal block of each node (-1: no element).
+                                    Set only for chain meshes (every node in at most two elements,
+                                    no two elements on the same two nodes); xk_beam_assemble32 then
+                                    runs every element in one launch, adding the two contributions
+                                    of a shared node (an order-free sum of two terms) */
 } xk_beam_plan;
 
 /* Corotational Timoshenko internal force f_int and analytic tangent K_T of all
@@ -108,6 +113,30 @@ xk_status xk_beam_assemble(const xk_mesh* m, const xk_section* sec, const double
  * overwritten. */
 xk_status xk_beam_lumped_mass(const xk_mesh* m, const xk_section* sec, const xk_beam_plan* plan, double rho,
                               double* out, xk_stream s);
+
+/* ------------------------------------------------------- strand meshes */
+
+/* One layered helical strand of a mesh that may hold many (the batched
+ * workload): the twisted-wire geometry of the reference's generator
+ * (mesh/_twisted_wire.py:150-383, _make_twisted_wire_mesh at :271).  The
+ * caller raises a non-negative gap to the generator's minimum safe gap first
+ * (_twisted_wire.py:127-147,307-326). */
+typedef struct {
+  int32_t n_wires;          /* core + layers (3: three wires, no core) */
+  int32_t n_elems_per_wire;
+  int32_t lay_direction;    /* +1 / -1: twist of layer 1 */
+  int32_t pad;
+  double wire_diameter, pitch, length, gap;
+  double x_offset;          /* shift along x of every node */
+  int64_t node_first, elem_first; /* the strand's first node and element in the mesh */
+} xk_strand_spec;
+
+/* Node coordinates X (3 n_nodes), connectivity conn (2 n_elems), the layer of
+ * every element (nullable) and the radii (nullable) of n_specs strands whose
+ * specs (device memory, sorted by node_first and by elem_first) tile
+ * [0, n_nodes) and [0, n_elems).  Elements run wire by wire, node i to i+1. */
+xk_status xk_strand_generate(const xk_strand_spec* specs, int32_t n_specs, int64_t n_nodes, int64_t n_elems,
+                             double* X, int32_t* conn, int32_t* elem_layer, double* radii, xk_stream s);
 
 /* ----------------------------------------------------------- contact path */
 
@@ -162,8 +191,13 @@ xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double* u, const x
 #define XK_STAGE_TANGENT 8  /* .tangent of both (contact_force/strategy.py:172-254, friction/_assembly.py:108-257) */
 #define XK_STAGE_NO_OTHERS 16  /* skip the other pairs' narrowphase (run it in another launch / stream) */
 #define XK_STAGE_NO_MEMBERS 32 /* skip the member kernel (only the other pairs' narrowphase) */
-#define XK_OUT_COMBINED 0   /* record (s, t, v = v_n + v_f, B = B_n - B_f): 14 values */
+#define XK_OUT_COMBINED 0   /* record (B = B_n - B_f, s, t, v = v_n + v_f): 14 values */
 #define XK_OUT_SPLIT 1      /* record (s, t, v_n, v_f, B_n, B_f): 26 values */
+/* Columns of a combined record: B first so that B, s and t are the first
+ * twelve values (three 16-byte loads for float records). */
+#define XK_REC_B 0
+#define XK_REC_S 9          /* s, then t */
+#define XK_REC_V 11
 #define XK_REC_STRIDE_COMBINED 16 /* values per record in memory (padded) */
 #define XK_REC_STRIDE_SPLIT 32
 
@@ -191,7 +225,7 @@ typedef struct {
    * when node_elem_ptr, node_elem, elem_ptr, elem_inc and bcodes are non-NULL.
    * A block's same-side contributions (k, l on one element) are sums over that
    * element's members, S_e^pq = sum c_p c_q B (p, q in {0,1}; three distinct
-   * per element, 27 values); each block lists at most four terms inline:
+   * per element, 48 values with padding); each block lists at most four terms inline:
    * -1 empty, other negative values (offset | 0x80000000) an element sum at
    * elem_sums[offset], non-negative values a cross code (member << 4) |
    * (k << 2) | l.  Sorted ascending per block, so every sum has a fixed order. */
@@ -202,7 +236,12 @@ typedef struct {
   int32_t* elem_ptr;      /* [n_elems+1] */
   int32_t* elem_inc;      /* [2*cap_members] (member << 1) | side (0 = A, 1 = B) */
   int32_t* bcodes;        /* [4*cap_blocks] */
-  void* elem_sums;        /* [27*n_elems] scratch of the record type: S^00, S^01, S^11 per element */
+  void* elem_sums;        /* [56*n_elems] scratch of the record type: S^00, S^01, S^11 per element, each
+                           * as 16 values (the 9 of the sum, then 1, 1 and padding); then, with
+                           * combined records, the element force sums F^0, F^1 (8 values per element) */
+  double* norm_scratch;   /* [(6*n_nodes + 255)/256 + 1] zero-initialised scratch of
+                           * xk_contact_gather_force_elem's fused norm (block sums and a counter
+                           * that each launch leaves at zero) */
 } xk_contact_pattern;
 
 /* Returns XK_ERR_CAPACITY (with n_members, n_others, nnzb set) when a capacity
@@ -244,7 +283,8 @@ xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec
  * records), B_n or B_f (split records).  variant picks the reduction schedule
  * (0 default, 1 one contributor per lane, 2 chunks of contributors per lane,
  * 3 element-side sums plus per-block cross lists, which needs the element-side
- * pattern and the elem_sums scratch);
+ * pattern and the elem_sums scratch; with combined records rec and elem_sums
+ * must then be 32-byte aligned);
  * all give the same values for a given precision up to rounding order, each
  * deterministic. */
 #define XK_GATHER_DEFAULT 0
@@ -253,6 +293,19 @@ xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec
 #define XK_GATHER_SIDES 3  /* element-side sums + cross lists (needs the element-side pattern) */
 xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* rec, int precision, int out_mode,
                                     int which, int variant, void* Kc_vals, xk_stream s);
+
+/* The residual of xk_contact_gather_force (out = base + scale * contact force
+ * - f_ext, zero where fixed; norm2 nullable) from the element force sums that
+ * the last element-side tangent gather (variant XK_GATHER_SIDES, combined
+ * records) left in pat->elem_sums: each node
+ * adds the sums of its incident elements, so the member records are not read
+ * again.  Call it after that gather on the same stream (or after an event
+ * recorded behind it).  The squared norm is fused: block sums in
+ * pat->norm_scratch, added in block order by the last block, a fixed order.
+ * Calls that overlap on one pattern race on norm_scratch. */
+xk_status xk_contact_gather_force_elem(const xk_contact_pattern* pat, int precision, const double* base,
+                                       double scale, const double* f_ext, const uint8_t* fixed, double* out,
+                                       double* norm2, xk_stream s);
 
 /* ------------------------------------------- mixed-precision fast path
  * The per-iteration kernels of the mixed path execute no double-precision
@@ -279,6 +332,10 @@ typedef struct {
   uint8_t *status, *stick;
   float* mu;               /* [cap] friction coefficient of each slot, filled from xk_mesh.mu by xk_pairs_to32;
                               NULL (use xk_contact_params.mu_eff) unless the mesh has per-element mu */
+  int32_t* defer;          /* [2 * (cap + 1)] scratch or NULL: the pair kernels then leave the rare
+                              near-parallel pairs to a second kernel each (other pairs: count in
+                              defer[0], slots after it; members: the same from defer[cap + 1]),
+                              which keeps the exact double routine out of the common kernels */
 } xk_pairs32;
 
 /* Per iteration: node records for the mixed kernels from u (and u_ref, nullable). */

@@ -249,6 +249,74 @@ def test_beam_float_path_large_rotations(scf, v_ref, key):
     assert sparse_rel_err(eng.K_beam_csr(), golden_csr(z, kkey, n)) < TOLMIX
 
 
+def test_beam_float_chain_launch_equals_colours():
+    """The one-launch float beam (wire meshes: shared node rows and diagonal blocks zeroed, then two
+    atomic adds) gives the same bits as the two colour launches (store, then add)."""
+    import ctypes as C
+
+    from xkgpu import workloads as W
+    from xkgpu.device import ptr, stream_handle
+
+    w = W.config_workload("strand37", seed=3)
+    st = w.strand
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **w.engine_kwargs())
+    assert eng.beam.node_diag is not None  # wires are chains
+    u0 = _dev(w.u)
+    eng.detect(u0)
+    eng.assemble(u0 * 1.001, u0)
+    colours = DeviceBeam(eng.mesh, w.section, chain=False)
+    assert colours.node_diag is None and colours.plan.n_colors >= 2
+    f = torch.zeros_like(eng.f_int)
+    K = torch.zeros_like(eng.K_beam)
+    L.call("xk_beam_assemble32", C.byref(eng.mesh.c), C.byref(colours.section), ptr(eng.elem32),
+           C.byref(colours.plan), ptr(eng.node32), ptr(f), ptr(K), stream_handle(None))
+    torch.cuda.synchronize()
+    assert torch.equal(f, eng.f_int)
+    assert torch.equal(K[: 36 * colours.nnzb], eng.K_beam[: 36 * colours.nnzb])
+
+
+def test_near_parallel_pairs_mixed_vs_fp64():
+    """Pairs of (near-)parallel segments, which the float pair kernels hand to their exact-routine
+    kernels: touching parallel wires (members), a wire at 1 degree to them and one parallel just
+    out of contact (other pairs), plus a crossing wire; mixed against FP64."""
+    n_el, r = 8, 1.0
+    xs = np.linspace(0.0, 16.0, n_el + 1)
+    ang = np.deg2rad(1.0)
+    wires = [
+        np.stack([xs, 0 * xs, 0 * xs], 1),
+        np.stack([xs, 0 * xs + 2 * r * (1 - 2e-3), 0 * xs], 1),  # parallel, in contact
+        np.stack([xs, 0 * xs - 2 * r * (1 + 1e-4), 0 * xs], 1),  # parallel, just apart
+        np.stack([xs * np.cos(ang), xs * np.sin(ang) - 2 * r * (1 - 1e-3), 0 * xs + 0.05], 1) + [0.0, 0.0, 0.0],
+        np.stack([8.0 + 0 * xs, xs - 8.0, 0 * xs + 2 * r * (1 - 2e-3)], 1),  # crossing
+    ]
+    coords = np.concatenate(wires)
+    conn = np.concatenate([np.stack([np.arange(n_el), np.arange(1, n_el + 1)], 1) + k * (n_el + 1)
+                           for k in range(len(wires))]).astype(np.int64)
+    layer = np.repeat(np.arange(len(wires)), n_el)
+    sec = {"E": 2.0e5, "G": 2.0e5 / 2.6, "A": np.pi, "Iy": np.pi / 4, "Iz": np.pi / 4, "J": np.pi / 2,
+           "kappa_y": 0.886, "kappa_z": 0.886, "scf": None}
+    rng = np.random.default_rng(7)
+    u = np.zeros(6 * coords.shape[0])
+    u.reshape(-1, 6)[:, :3] = rng.normal(0.0, 1e-4, (coords.shape[0], 3))
+    out = {}
+    for prec in ("fp64", "mixed"):
+        eng = AssemblyEngine(coords, conn, r, sec, layer=layer, precision=prec, k_pen=1e4, mu=0.2, margin=0.05)
+        u0 = _dev(u)
+        stats = eng.detect(u0)
+        eng.assemble(u0 * 1.01, u0)
+        eng.assemble(u0 * 1.02, u0)
+        torch.cuda.synchronize()
+        out[prec] = (eng.R.cpu().numpy(), eng.K_contact_csr(), eng.pair_state(), stats)
+    R64, K64, h64, st64 = out["fp64"]
+    Rmx, Kmx, hmx, stmx = out["mixed"]
+    assert st64 == stmx and st64["members"] > 0 and st64["pairs"] > st64["members"]
+    assert rel_err(Rmx, R64) < TOLMIX
+    assert sparse_rel_err(Kmx, K64) < TOLMIX
+    assert np.array_equal(h64["status"], hmx["status"])
+    assert rel_err(hmx["gap"], h64["gap"]) < 1e-6
+    assert rel_err(hmx["s"], h64["s"]) < 1e-5 and rel_err(hmx["t"], h64["t"]) < 1e-5
+
+
 def test_mixed_engine_vs_fp64_strand37():
     from xkgpu import workloads as W
 
@@ -274,14 +342,16 @@ def test_mixed_engine_vs_fp64_strand37():
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_tangent_gather_schedules_agree(precision):
-    """The contact-tangent reduction schedules give the same K_c, each deterministically."""
+@pytest.mark.parametrize("workload", ["strand7", "strand37"])
+def test_tangent_gather_schedules_agree(precision, workload):
+    """The contact-tangent reduction schedules give the same K_c, each deterministically; the residual
+    from the element-side schedule's force sums equals the one gathered from the member records."""
     import ctypes as C
 
     from xkgpu import workloads as W
     from xkgpu.device import ptr, stream_handle
 
-    w = W.config_workload("strand37", seed=5)
+    w = W.config_workload(workload, seed=5)
     st = w.strand
     eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=precision, **w.engine_kwargs())
     u0 = _dev(w.u)
@@ -300,6 +370,22 @@ def test_tangent_gather_schedules_agree(precision):
     assert rel_err(outs[3], outs[0]) < tol
     assert np.array_equal(outs[0], outs[2])
     assert np.array_equal(outs[3], outs[4])
+    # the residual from the element force sums left by the last gather equals the member-record gather
+    R = {}
+    for name in ("records", "elem_sums"):
+        out = torch.zeros_like(eng.R)
+        n2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+        if name == "records":
+            L.call("xk_contact_gather_force", C.byref(eng.pattern.c), ptr(eng.rec), eng.precision,
+                   L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, ptr(eng.f_int), -1.0, None, None, ptr(out), ptr(n2),
+                   stream_handle(None))
+        else:
+            L.call("xk_contact_gather_force_elem", C.byref(eng.pattern.c), eng.precision, ptr(eng.f_int), -1.0,
+                   None, None, ptr(out), ptr(n2), stream_handle(None))
+        torch.cuda.synchronize()
+        R[name] = (out.cpu().numpy(), float(n2.item()))
+    assert rel_err(R["elem_sums"][0], R["records"][0]) < (1e-12 if precision == "fp64" else 1e-6)
+    assert abs(R["elem_sums"][1] - np.sum(R["elem_sums"][0] ** 2)) <= 1e-12 * R["elem_sums"][1]
 
 
 def test_host_pipeline_returns_each_steps_outputs():

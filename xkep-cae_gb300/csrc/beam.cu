@@ -517,8 +517,17 @@ XK_D void frame32(const float* __restrict__ E, const float* __restrict__ NA, con
 // the unsymmetrised tangent ([G_I, H_I, -G_I, J_I], see beam_tail) and the f
 // rows of DOF group I; the quad exchanges the rows through shared memory to
 // symmetrise, and lane I stores rows 3I..3I+2 of the 12x12 element tangent.
+//
+// CHAIN: all elements in one launch (order == NULL: element k is element k),
+// for meshes in which every node has at most two elements and no two
+// elements share both nodes (wires).  The node rows of f_int and the diagonal
+// blocks, which two elements share, are zeroed first (k_beam_zero32) and
+// receive their two contributions by atomic adds; 0 + a + b = 0 + b + a, so
+// the result does not depend on their order.  The off-diagonal blocks have one
+// writer each.  Otherwise the launch covers one colour of the plan.
 constexpr int BEAMQ_T = 128;
 
+template <bool CHAIN>
 __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, const float* __restrict__ e32,
                                                      const int32_t* __restrict__ order, int k0, int k1,
                                                      const int32_t* __restrict__ blk,
@@ -530,7 +539,7 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
   const int q = threadIdx.x >> 2, I = threadIdx.x & 3;
   const int k = k0 + blockIdx.x * (BEAMQ_T / 4) + q;
   const bool live = k < k1;
-  const int e = live ? order[k] : order[k0];
+  const int e = CHAIN ? (live ? k : k0) : (live ? order[k] : order[k0]);
   if (I == 0) s_e[q] = live ? e : -1;
   const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
   Frame32 F;
@@ -562,7 +571,9 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
       const double v = (double)(Rcr[i] * g0 + Rcr[3 + i] * g1 + Rcr[6 + i] * g2);
       const long long dof = (I < 2 ? 6LL * a : 6LL * b) + 3 * (I & 1) + i;
       const bool fw = (I < 2) ? (fl & 1) : (fl & 8);
-      if (fw) f_int[dof] = v; else f_int[dof] += v;
+      if (CHAIN) atomicAdd(f_int + dof, v);
+      else if (fw) f_int[dof] = v;
+      else f_int[dof] += v;
     }
   }
   if (!Kv) return;  // uniform over the launch
@@ -665,12 +676,36 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
     if (ee < 0) continue;
     const float4 v = reinterpret_cast<const float4*>(kst[qq][nb])[ch];
     float4* dst = reinterpret_cast<float4*>(Kv + 36LL * blk[4LL * ee + nb]) + ch;
-    if ((first[ee] >> nb) & 1) {
+    if (CHAIN) {
+      if (nb == 0 || nb == 3) atomicAdd(dst, v);  // diagonal block, shared with the neighbour element
+      else *dst = v;
+    } else if ((first[ee] >> nb) & 1) {
       *dst = v;
     } else {
       float4 o = *dst;
       o.x += v.x; o.y += v.y; o.z += v.z; o.w += v.w;
       *dst = o;
+    }
+  }
+}
+
+// Chain launches: zero the node rows of f_int and the diagonal blocks that the elements add into,
+// one thread per 16 bytes (nine per 6x6 float block, three per node row of f_int), so that
+// neighbouring threads write neighbouring bytes.
+__global__ void k_beam_zero32(int n_nodes, const int32_t* __restrict__ node_diag, double* __restrict__ f_int,
+                              float* __restrict__ Kv) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (Kv && t < 9LL * n_nodes) {
+    const int d = node_diag[t / 9];
+    if (d >= 0) reinterpret_cast<float4*>(Kv + 36LL * d)[t % 9] = z;  // no element at the node: not written
+  }
+  if (f_int && t < 3LL * n_nodes && node_diag[t / 3] >= 0) {
+    if (((uintptr_t)f_int & 15) == 0) {
+      reinterpret_cast<float4*>(f_int)[t] = z;
+    } else {
+      f_int[2 * t] = 0.0;
+      f_int[2 * t + 1] = 0.0;
     }
   }
 }
@@ -840,12 +875,19 @@ extern "C" xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec,
   if (!m || !sec || !elem32 || !plan || !node32) return xk_set_error(XK_ERR_ARG, "xk_beam_assemble32: null argument");
   if (!f_int && !K_vals) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
+  if (plan->node_diag) {  // chain mesh: one launch over all elements
+    if (m->n_elems == 0) return XK_OK;
+    k_beam_zero32<<<xk_blocks(9LL * m->n_nodes, 256), 256, 0, st>>>(m->n_nodes, plan->node_diag, f_int, K_vals);
+    k_beam32q<true><<<xk_blocks(4LL * m->n_elems, BEAMQ_T), BEAMQ_T, 0, st>>>(
+        *m, *sec, elem32, nullptr, 0, m->n_elems, plan->blk, plan->first, node32, f_int, K_vals);
+    XK_CHECK_LAUNCH();
+    return XK_OK;
+  }
   for (int c = 0; c < plan->n_colors; ++c) {
     const int k0 = plan->color_ptr_host[c], k1 = plan->color_ptr_host[c + 1];
     if (k1 <= k0) continue;
-    k_beam32q<<<xk_blocks(4LL * (k1 - k0), BEAMQ_T), BEAMQ_T, 0, st>>>(*m, *sec, elem32, plan->elem_order, k0, k1,
-                                                                         plan->blk, plan->first, node32, f_int,
-                                                                         K_vals);
+    k_beam32q<false><<<xk_blocks(4LL * (k1 - k0), BEAMQ_T), BEAMQ_T, 0, st>>>(
+        *m, *sec, elem32, plan->elem_order, k0, k1, plan->blk, plan->first, node32, f_int, K_vals);
     XK_CHECK_LAUNCH();
   }
   return XK_OK;

@@ -232,7 +232,7 @@ XK_D void load_rec<double, 16>(const double* __restrict__ r, double* out) {
 constexpr int GF_LANES = 8;
 template <typename T>
 __global__ void k_gather_force(int n_nodes, const int32_t* __restrict__ ptr, const int32_t* __restrict__ inc,
-                               const T* __restrict__ rec, int rs, int vcol, int vcol2,
+                               const T* __restrict__ rec, int rs, int stc, int vcol, int vcol2,
                                const double* __restrict__ base, double scale, const double* __restrict__ f_ext,
                                const uint8_t* __restrict__ fixed, double* __restrict__ out) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -243,7 +243,7 @@ __global__ void k_gather_force(int n_nodes, const int32_t* __restrict__ ptr, con
     for (int x = ptr[v] + lane; x < ptr[v + 1]; x += GF_LANES) {
       const int code = inc[x], k = code & 3;
       const T* r = rec + (long long)(code >> 2) * rs;
-      const T c = shape_c<T>(r[0], r[1], k);
+      const T c = shape_c<T>(r[stc], r[stc + 1], k);
       for (int d = 0; d < 3; ++d) {
         T w = r[vcol + d];
         if (vcol2 >= 0) w += r[vcol2 + d];
@@ -267,8 +267,13 @@ __global__ void k_gather_force(int n_nodes, const int32_t* __restrict__ ptr, con
   }
 }
 
+// Column of s (then t) in a record of RS values: combined records put B first.
+template <int RS>
+__host__ __device__ constexpr int rec_st() { return RS == XK_REC_STRIDE_COMBINED ? XK_REC_S : 0; }
+
 template <typename T, int RS, int BCOL>
 XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
+  constexpr int ST = rec_st<RS>();
   const int k = (code >> 2) & 3, l = code & 3;
   T r[RS];
   if (RS == 16) {
@@ -277,7 +282,7 @@ XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
 #pragma unroll
     for (int q = 0; q < RS; ++q) r[q] = rec[(long long)(code >> 4) * RS + q];
   }
-  const T w = shape_c<T>(r[0], r[1], k) * shape_c<T>(r[0], r[1], l);
+  const T w = shape_c<T>(r[ST], r[ST + 1], k) * shape_c<T>(r[ST], r[ST + 1], l);
 #pragma unroll
   for (int q = 0; q < 9; ++q) acc[q] += w * r[BCOL + q];
 }
@@ -287,6 +292,12 @@ XK_D void add_contrib(const T* __restrict__ rec, int code, T* acc) {
 // node; neighbour on an element: S^01) and the count; k_cross_codes appends
 // the cross codes of every member; k_sort_codes sorts each block's four slots.
 constexpr int SIDE_FLAG = (int)0x80000000;
+// An element's three sums S^00, S^01, S^11, each as 16 values: the 9 of the
+// sum, then 1, 1 in the places of a record's s, t and padding, so that a term
+// loads the same values from an element sum as from a combined record (both
+// 64-byte aligned) and the weight c_1 c_1 = s s of an element-sum term is 1.
+constexpr int SUM_STRIDE = 16;
+constexpr int ELEM_SUMS = 3 * SUM_STRIDE;
 
 __global__ void k_side_codes(long long nb, const int32_t* __restrict__ brow, const int32_t* __restrict__ col,
                              const int32_t* __restrict__ neptr, const int2* __restrict__ ne,
@@ -297,13 +308,13 @@ __global__ void k_side_codes(long long nb, const int32_t* __restrict__ brow, con
   int n = 0;
   for (int y = neptr[i]; y < neptr[i + 1]; ++y) {
     const int2 en = ne[y];
-    const int base = 27 * (en.x >> 1);
+    const int base = ELEM_SUMS * (en.x >> 1);
     if (j == i) {
-      if (n < 4) codes[4 * b + n] = SIDE_FLAG | (base + ((en.x & 1) ? 18 : 0));
+      if (n < 4) codes[4 * b + n] = SIDE_FLAG | (base + ((en.x & 1) ? 2 * SUM_STRIDE : 0));
       ++n;
     }
     if (j == en.y) {
-      if (n < 4) codes[4 * b + n] = SIDE_FLAG | (base + 9);
+      if (n < 4) codes[4 * b + n] = SIDE_FLAG | (base + SUM_STRIDE);
       ++n;
     }
   }
@@ -349,29 +360,248 @@ __global__ void k_sort_codes(long long nb, int4* __restrict__ codes) {
 // element from its members, one thread per (element, B component); the weights
 // are the products c_p c_q of the member's side: (1-s)^2, (1-s)s, s^2 on side A
 // and the same in t on side B (the signs of c_2, c_3 cancel).
+//
+// With combined records the same pass also forms the element's force sums
+// F_e^0 = sum c_p v and F_e^1 = sum c_q v over its members (p, q the element's
+// first and second local node on the member's side: c = 1-s, s on side A and
+// -(1-t), -t on side B), 8 values per element after the 36 * ne tangent sums;
+// a node's contact force is then the sum of F over its incident elements
+// (k_gather_force_elem).
+constexpr int ELEM_FORCE = 8;
+
 template <typename T, int RS, int BCOL>
 __global__ void k_elem_sums(int ne, const int32_t* __restrict__ eptr, const int32_t* __restrict__ einc,
                             const T* __restrict__ rec, T* __restrict__ S) {
+  constexpr int ST = rec_st<RS>();
+  constexpr bool FORCE = RS == XK_REC_STRIDE_COMBINED;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 9LL * ne) return;
   const int e = (int)(t / 9), q = (int)(t % 9);
-  T s00 = T(0), s01 = T(0), s11 = T(0);
+  T s00 = T(0), s01 = T(0), s11 = T(0), f0 = T(0), f1 = T(0);
   const int x1 = eptr[e + 1];
 #pragma unroll 4
   for (int x = eptr[e]; x < x1; ++x) {
     const int code = einc[x];
     const T* r = rec + (long long)(code >> 1) * RS;
-    const T a = r[code & 1];
+    const T a = r[ST + (code & 1)];
     const T b = r[BCOL + q];
     const T om = T(1) - a;
     s00 += (om * om) * b;
     s01 += (om * a) * b;
     s11 += (a * a) * b;
+    if (FORCE && q < 3) {
+      const T v = (code & 1) ? -r[XK_REC_V + q] : r[XK_REC_V + q];
+      f0 += om * v;
+      f1 += a * v;
+    }
   }
-  T* o = S + 27LL * e;
+  T* o = S + (long long)ELEM_SUMS * e;
   o[q] = s00;
-  o[9 + q] = s01;
-  o[18 + q] = s11;
+  o[SUM_STRIDE + q] = s01;
+  o[2 * SUM_STRIDE + q] = s11;
+  if (q < 3) {  // padding of sum q: (s, t) = (1, 1)
+    o[q * SUM_STRIDE + 9] = T(1);
+    o[q * SUM_STRIDE + 10] = T(1);
+    if (FORCE) {
+      T* f = S + (long long)ELEM_SUMS * ne + (long long)ELEM_FORCE * e;
+      f[q] = f0;
+      f[3 + q] = f1;
+      if (q < 2) f[6 + q] = T(0);
+    }
+  }
+}
+
+// The same sums for combined records, four lanes per element: lane q sums the incidences
+// q, q + 4, q + 8, ... of the element (each one record read as two 256-bit loads for float),
+// and the four partial sums are combined by a fixed shuffle tree ((0 + 1) + (2 + 3)), so the
+// result does not depend on timing.  It differs from k_elem_sums' single running sum by
+// rounding only.
+template <typename T>
+XK_D void load16(const T* __restrict__ p, T* v);
+template <>
+XK_D void load16<float>(const float* __restrict__ p, float* v) {  // p 32-byte aligned
+  ldg8(p, v);
+  ldg8(p + 8, v + 8);
+}
+template <>
+XK_D void load16<double>(const double* __restrict__ p, double* v) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const double2 x = __ldg(q + i);
+    v[2 * i] = x.x; v[2 * i + 1] = x.y;
+  }
+}
+
+template <typename T>
+XK_D void store4(T* p, T a, T b, T c, T d);
+template <>
+XK_D void store4<float>(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+template <>
+XK_D void store4<double>(double* p, double a, double b, double c, double d) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+  reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_elem_sums_rec(int ne, const int32_t* __restrict__ eptr,
+                                                       const int32_t* __restrict__ einc, const T* __restrict__ rec,
+                                                       T* __restrict__ S) {
+  static_assert(XK_REC_B == 0 && XK_REC_S == 9 && XK_REC_V == 11, "combined record layout");
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = (int)(gid >> 2), q = (int)(gid & 3);
+  const bool live = e < ne;  // a quad is all live or all dead (4 | 128)
+  T s00[9], s01[9], s11[9], f0[3], f1[3];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) { s00[c] = T(0); s01[c] = T(0); s11[c] = T(0); }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { f0[c] = T(0); f1[c] = T(0); }
+  const int x0 = live ? eptr[e] : 0, x1 = live ? eptr[e + 1] : 0;
+  for (int x = x0 + q; x < x1; x += 4) {
+    const int code = einc[x];
+    T r[16];
+    load16<T>(rec + (long long)(code >> 1) * XK_REC_STRIDE_COMBINED, r);
+    const T a = (code & 1) ? r[XK_REC_S + 1] : r[XK_REC_S];
+    const T om = T(1) - a;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+      s00[c] += (om * om) * r[c];
+      s01[c] += (om * a) * r[c];
+      s11[c] += (a * a) * r[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const T v = (code & 1) ? -r[XK_REC_V + c] : r[XK_REC_V + c];
+      f0[c] += om * v;
+      f1[c] += a * v;
+    }
+  }
+  // (lane 0 + lane 1) + (lane 2 + lane 3) in every lane of the quad
+#pragma unroll
+  for (int m = 1; m <= 2; m <<= 1) {
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+      s00[c] += __shfl_xor_sync(0xffffffffu, s00[c], m);
+      s01[c] += __shfl_xor_sync(0xffffffffu, s01[c], m);
+      s11[c] += __shfl_xor_sync(0xffffffffu, s11[c], m);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      f0[c] += __shfl_xor_sync(0xffffffffu, f0[c], m);
+      f1[c] += __shfl_xor_sync(0xffffffffu, f1[c], m);
+    }
+  }
+  if (!live) return;
+  // vector stores shared by the quad: lanes 0-2 write sum S^00, S^01, S^11 (its 9 values, then
+  // (s, t) = (1, 1) and a zero; the last 4 values of a sum are not read), lane 3 the force sums
+  if (q < 3) {
+    const T* sp = q == 0 ? s00 : (q == 1 ? s01 : s11);
+    T* o = S + (long long)ELEM_SUMS * e + q * SUM_STRIDE;
+    store4<T>(o, sp[0], sp[1], sp[2], sp[3]);
+    store4<T>(o + 4, sp[4], sp[5], sp[6], sp[7]);
+    store4<T>(o + 8, sp[8], T(1), T(1), T(0));
+  } else {
+    T* f = S + (long long)ELEM_SUMS * ne + (long long)ELEM_FORCE * e;
+    store4<T>(f, f0[0], f0[1], f0[2], f1[0]);
+    store4<T>(f + 4, f1[1], f1[2], T(0), T(0));
+  }
+}
+
+// R[dof] = base[dof] + scale * (contact force at the node) - f_ext[dof], zero where fixed, from
+// the element force sums of the last element-side tangent gather: one thread per degree of
+// freedom, the node's incident elements in their list order.  The block partial sums of R^2
+// go to `part`, and the last block to finish adds them in block order into *norm2 (a fixed
+// order whatever the timing); `count` (zero between launches) finds the last block.
+constexpr int GFE_T = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(GFE_T) k_gather_force_elem(int n_nodes, int ne, const int32_t* __restrict__ neptr,
+                                                             const int2* __restrict__ nelem, const T* __restrict__ S,
+                                                             const double* __restrict__ base, double scale,
+                                                             const double* __restrict__ f_ext,
+                                                             const uint8_t* __restrict__ fixed,
+                                                             double* __restrict__ out, double* __restrict__ part,
+                                                             unsigned int* __restrict__ count,
+                                                             double* __restrict__ norm2) {
+  __shared__ double red[GFE_T];
+  __shared__ bool last;
+  const long long i = (long long)blockIdx.x * GFE_T + threadIdx.x;
+  double r = 0.0;
+  if (i < 6LL * n_nodes) {
+    const int v = (int)(i / 6), d = (int)(i % 6);
+    r = base ? base[i] : 0.0;
+    if (d < 3) {
+      const T* F = S + (long long)ELEM_SUMS * ne;
+      T acc = T(0);
+      for (int y = neptr[v]; y < neptr[v + 1]; ++y) {
+        const int ex = nelem[y].x;  // (element << 1) | local index of v in it
+        acc += F[(long long)ELEM_FORCE * (ex >> 1) + 3 * (ex & 1) + d];
+      }
+      r += scale * (double)acc;
+    }
+    if (f_ext) r -= f_ext[i];
+    if (fixed && fixed[i]) r = 0.0;
+    out[i] = r;
+  }
+  if (!norm2) return;  // uniform over the launch
+  red[threadIdx.x] = r * r;
+  __syncthreads();
+  for (int w = GFE_T / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = red[0];
+    __threadfence();
+    last = atomicAdd(count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double a = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += GFE_T) a += __ldcg(part + b);
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int w = GFE_T / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *norm2 = red[0];
+    *count = 0u;  // ready for the next launch
+  }
+}
+
+template <typename T>
+XK_D void load12(const T* __restrict__ p, T* v);
+template <>
+XK_D void load12<float>(const float* __restrict__ p, float* v) {  // p 32-byte aligned
+  ldg8(p, v);
+  const float4 x = __ldg(reinterpret_cast<const float4*>(p) + 2);
+  v[8] = x.x; v[9] = x.y; v[10] = x.z; v[11] = x.w;
+}
+template <>
+XK_D void load12<double>(const double* __restrict__ p, double* v) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const double2 x = __ldg(q + i);
+    v[2 * i] = x.x; v[2 * i + 1] = x.y;
+  }
+}
+
+// acc += one term of a block (-1: none): B and (s, t) of an element sum (s = t = 1) or of a member record
+template <typename T>
+XK_D void sides_term(const T* __restrict__ S, const T* __restrict__ rec, int c, T* acc) {
+  if (c == -1) return;
+  T v[12];
+  load12<T>(c < 0 ? S + (c & 0x7fffffff) : rec + (long long)(c >> 4) * XK_REC_STRIDE_COMBINED, v);
+  const int k = c < 0 ? 1 : (c >> 2) & 3, l = c < 0 ? 1 : c & 3;
+  const T w = shape_c<T>(v[9], v[10], k) * shape_c<T>(v[9], v[10], l);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) acc[q] += w * v[q];
 }
 
 // Variant "sides", step 2: one thread per block over its (at most four) inline
@@ -392,10 +622,10 @@ XK_D void add_term(const T* __restrict__ S, const T* __restrict__ rec, int code,
 }
 
 template <typename T, int RS, int BCOL>
-__global__ void __launch_bounds__(GS_T) k_gather_tangent_sides(long long nnzb, const int4* __restrict__ codes,
+__global__ void __launch_bounds__(GS_T, sizeof(T) == 4 ? 16 : 8) k_gather_tangent_sides(long long nnzb, const int4* __restrict__ codes,
                                                                const T* __restrict__ S, const T* __restrict__ rec,
                                                                T* __restrict__ K) {
-  __shared__ T stage[GS_T * 9];
+  __shared__ __align__(16) T stage[GS_T * 9];
   const long long b0 = (long long)blockIdx.x * GS_T;
   const long long b = b0 + threadIdx.x;
   T acc[9];
@@ -403,10 +633,18 @@ __global__ void __launch_bounds__(GS_T) k_gather_tangent_sides(long long nnzb, c
   for (int q = 0; q < 9; ++q) acc[q] = T(0);
   if (b < nnzb) {
     const int4 c = codes[b];
-    add_term<T, RS, BCOL>(S, rec, c.x, acc);
-    add_term<T, RS, BCOL>(S, rec, c.y, acc);
-    add_term<T, RS, BCOL>(S, rec, c.z, acc);
-    add_term<T, RS, BCOL>(S, rec, c.w, acc);
+    if (RS == XK_REC_STRIDE_COMBINED) {
+      // each term is the first twelve values of its element sum or member record
+      sides_term<T>(S, rec, c.x, acc);
+      sides_term<T>(S, rec, c.y, acc);
+      sides_term<T>(S, rec, c.z, acc);
+      sides_term<T>(S, rec, c.w, acc);
+    } else {
+      add_term<T, RS, BCOL>(S, rec, c.x, acc);
+      add_term<T, RS, BCOL>(S, rec, c.y, acc);
+      add_term<T, RS, BCOL>(S, rec, c.z, acc);
+      add_term<T, RS, BCOL>(S, rec, c.w, acc);
+    }
   }
 #pragma unroll
   for (int q = 0; q < 9; ++q) stage[threadIdx.x * 9 + q] = acc[q];
@@ -414,8 +652,17 @@ __global__ void __launch_bounds__(GS_T) k_gather_tangent_sides(long long nnzb, c
   const long long rem = nnzb - b0;
   const int nv = 9 * (int)(rem < GS_T ? rem : GS_T);
   T* out = K + 9 * b0;
-  for (int v = threadIdx.x; v < nv; v += GS_T) out[v] = stage[v];
+  if (sizeof(T) == 4 && ((uintptr_t)out & 15) == 0) {
+    // 16-byte stores of the staged values (a CTA's 128 blocks are 4608 bytes)
+    const int n4 = nv / 4;
+    for (int v = threadIdx.x; v < n4; v += GS_T)
+      reinterpret_cast<float4*>(out)[v] = reinterpret_cast<const float4*>(stage)[v];
+    for (int v = 4 * n4 + threadIdx.x; v < nv; v += GS_T) out[v] = stage[v];
+  } else {
+    for (int v = threadIdx.x; v < nv; v += GS_T) out[v] = stage[v];
+  }
 }
+
 
 // Variant "lanes": a warp owns 32 consecutive blocks and spreads their
 // contributors one per lane (32 per round); a segmented inclusive scan over
@@ -758,11 +1005,13 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   return XK_OK;
 }
 
+static bool aligned32(const void* p) { return ((uintptr_t)p & 31) == 0; }
+
 static xk_status rec_columns(int out_mode, int which, bool tangent, int* c1, int* c2) {
   *c2 = -1;
   if (out_mode == XK_OUT_COMBINED) {
     if (which != XK_WHICH_COMBINED) return xk_set_error(XK_ERR_ARG, "combined records hold only combined values");
-    *c1 = tangent ? 5 : 2;
+    *c1 = tangent ? XK_REC_B : XK_REC_V;
     return XK_OK;
   }
   if (out_mode != XK_OUT_SPLIT) return xk_set_error(XK_ERR_ARG, "out_mode");
@@ -786,6 +1035,7 @@ extern "C" xk_status xk_contact_gather_force(const xk_contact_pattern* pat, cons
   int c1, c2;
   XK_TRY(rec_columns(out_mode, which, false, &c1, &c2));
   const int rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
+  const int stc = out_mode == XK_OUT_COMBINED ? XK_REC_S : 0;
   const bool use = pat->n_members > 0 && rec;
   const int32_t* ptr = use ? pat->inc_ptr : nullptr;
   const int32_t* inc = use ? pat->inc : nullptr;
@@ -793,16 +1043,45 @@ extern "C" xk_status xk_contact_gather_force(const xk_contact_pattern* pat, cons
   const int nn = pat->n_nodes;
   if (nn > 0) {
     if (precision == XK_FP64)
-      k_gather_force<double><<<xk_blocks((long long)GF_LANES * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const double*)rec, rs, c1, c2,
+      k_gather_force<double><<<xk_blocks((long long)GF_LANES * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const double*)rec, rs, stc, c1, c2,
                                                                          base, scale, f_ext, fixed, out);
     else if (precision == XK_MIXED)
-      k_gather_force<float><<<xk_blocks((long long)GF_LANES * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const float*)rec, rs, c1, c2,
+      k_gather_force<float><<<xk_blocks((long long)GF_LANES * nn, 128), 128, 0, st>>>(nn, ptr, inc, (const float*)rec, rs, stc, c1, c2,
                                                                         base, scale, f_ext, fixed, out);
     else
       return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force: precision");
     XK_CHECK_LAUNCH();
   }
   if (norm2) return xk_sumsq_into(out, 6LL * nn, norm2, st);
+  return XK_OK;
+}
+
+extern "C" xk_status xk_contact_gather_force_elem(const xk_contact_pattern* pat, int precision, const double* base,
+                                                  double scale, const double* f_ext, const uint8_t* fixed,
+                                                  double* out, double* norm2, xk_stream s) {
+  if (!pat || !out) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force_elem: null argument");
+  if (!pat->node_elem_ptr || !pat->node_elem || !pat->elem_sums || (norm2 && !pat->norm_scratch))
+    return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force_elem: the element-side pattern was not built");
+  if (precision != XK_FP64 && precision != XK_MIXED)
+    return xk_set_error(XK_ERR_ARG, "xk_contact_gather_force_elem: precision");
+  const int nn = pat->n_nodes, ne = (int)pat->n_elems;
+  if (nn <= 0) {
+    if (norm2) XK_CUDA(cudaMemsetAsync(norm2, 0, sizeof(double), (cudaStream_t)s));
+    return XK_OK;
+  }
+  const int nb = xk_blocks(6LL * nn, GFE_T);
+  double* part = pat->norm_scratch;
+  unsigned int* count = part ? reinterpret_cast<unsigned int*>(part + nb) : nullptr;
+  const int2* nelem = reinterpret_cast<const int2*>(pat->node_elem);
+  if (precision == XK_FP64)
+    k_gather_force_elem<double><<<nb, GFE_T, 0, (cudaStream_t)s>>>(nn, ne, pat->node_elem_ptr, nelem,
+                                                                  (const double*)pat->elem_sums, base, scale, f_ext,
+                                                                  fixed, out, part, count, norm2);
+  else
+    k_gather_force_elem<float><<<nb, GFE_T, 0, (cudaStream_t)s>>>(nn, ne, pat->node_elem_ptr, nelem,
+                                                                 (const float*)pat->elem_sums, base, scale, f_ext,
+                                                                 fixed, out, part, count, norm2);
+  XK_CHECK_LAUNCH();
   return XK_OK;
 }
 
@@ -813,6 +1092,8 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   XK_TRY(rec_columns(out_mode, which, true, &c1, &c2));
   if (variant < 0 || variant > XK_GATHER_SIDES) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: variant");
   const bool sides = variant == XK_GATHER_SIDES;
+  if (sides && out_mode == XK_OUT_COMBINED && !(aligned32(rec) && aligned32(pat->elem_sums)))
+    return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: rec and elem_sums must be 32-byte aligned");
   if (sides && !(pat->elem_ptr && pat->elem_inc && pat->bcodes && pat->elem_sums && pat->sides_ok == 1))
     return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: the element-side pattern was not built");
   if (pat->nnzb == 0) return XK_OK;
@@ -825,7 +1106,10 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
 #define XK_GT(TT, RSV, BC)                                                                                   \
   do {                                                                                                      \
     if (sides) {                                                                                            \
-      if (ne > 0)                                                                                           \
+      if (ne > 0 && RSV == XK_REC_STRIDE_COMBINED)                                                          \
+        k_elem_sums_rec<TT><<<xk_blocks(4LL * ne, 128), 128, 0, st>>>(ne, pat->elem_ptr, pat->elem_inc,     \
+                                                                (const TT*)rec, (TT*)pat->elem_sums);       \
+      else if (ne > 0)                                                                                      \
         k_elem_sums<TT, RSV, BC><<<xk_blocks(9LL * ne, 256), 256, 0, st>>>(ne, pat->elem_ptr, pat->elem_inc,   \
                                                                            (const TT*)rec, (TT*)pat->elem_sums); \
       k_gather_tangent_sides<TT, RSV, BC><<<xk_blocks(pat->nnzb, GS_T), GS_T, 0, st>>>(                     \
@@ -839,11 +1123,11 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
           pat->nnzb, pat->blk_ptr, pat->contrib, (const TT*)rec, (TT*)Kc_vals);                             \
   } while (0)
   if (precision == XK_FP64) {
-    if (comb) XK_GT(double, 16, 5);
+    if (comb) XK_GT(double, 16, XK_REC_B);
     else if (c1 == 8) XK_GT(double, 32, 8);
     else XK_GT(double, 32, 17);
   } else if (precision == XK_MIXED) {
-    if (comb) XK_GT(float, 16, 5);
+    if (comb) XK_GT(float, 16, XK_REC_B);
     else if (c1 == 8) XK_GT(float, 32, 8);
     else XK_GT(float, 32, 17);
   } else {

@@ -456,12 +456,16 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, c
   }
   // ---------------------------------------------------------------- record
   T* r = rec + (long long)mi * rs;  // array-of-structs record, rs values per member
-  r[0] = (T)s;
-  r[1] = (T)t;
   if (OUT == XK_OUT_COMBINED) {
-    for (int k = 0; k < 3; ++k) r[2 + k] = vn[k] + vf[k];
-    for (int k = 0; k < 9; ++k) r[5 + k] = Bn[k] - Bf[k];
+    for (int k = 0; k < 9; ++k) r[XK_REC_B + k] = Bn[k] - Bf[k];
+    r[XK_REC_S] = (T)s;
+    r[XK_REC_S + 1] = (T)t;
+    for (int k = 0; k < 3; ++k) r[XK_REC_V + k] = vn[k] + vf[k];
+    r[14] = T(0);
+    r[15] = T(0);
   } else {
+    r[0] = (T)s;
+    r[1] = (T)t;
     if (stages & XK_STAGE_NORMAL)
       for (int k = 0; k < 3; ++k) r[2 + k] = vn[k];
     if (stages & XK_STAGE_FRICTION)
@@ -511,20 +515,48 @@ XK_D df df_mulf(df a, float b) {
   return fast_two_sum(p, fmaf(a.l, b, e));
 }
 
+// VEC: u and u_ref are 16-byte aligned and read as double2 (48 bytes per node).
+template <bool VEC>
 __global__ void k_nodes_prepare(xk_mesh m, const double* __restrict__ u, const double* __restrict__ u_ref,
                                 float* __restrict__ n32) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= m.n_nodes) return;
-  float* N = n32 + (long long)v * XK_NODE32_STRIDE;
+  double uv[6], ur[3] = {0.0, 0.0, 0.0};
+  if (VEC) {
+    const double2* up = reinterpret_cast<const double2*>(u + 6LL * v);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double2 a = __ldg(up + i);
+      uv[2 * i] = a.x;
+      uv[2 * i + 1] = a.y;
+    }
+    if (u_ref) {
+      const double2* rp = reinterpret_cast<const double2*>(u_ref + 6LL * v);
+      const double2 a = __ldg(rp), b = __ldg(rp + 1);
+      ur[0] = a.x; ur[1] = a.y; ur[2] = b.x;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) uv[c] = u[6LL * v + c];
+    if (u_ref)
+      for (int c = 0; c < 3; ++c) ur[c] = u_ref[6LL * v + c];
+  }
+  float N[16];
+#pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const double x = m.X[3LL * v + c] + u[6LL * v + c];
+    const double x = m.X[3LL * v + c] + uv[c];
     const float h = (float)x;
     N[c] = h;
     N[3 + c] = (float)(x - (double)h);
   }
-  for (int c = 0; c < 6; ++c) N[6 + c] = (float)u[6LL * v + c];
-  for (int c = 0; c < 3; ++c) N[12 + c] = (float)(u_ref ? u[6LL * v + c] - u_ref[6LL * v + c] : u[6LL * v + c]);
+#pragma unroll
+  for (int c = 0; c < 6; ++c) N[6 + c] = (float)uv[c];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) N[12 + c] = (float)(u_ref ? uv[c] - ur[c] : uv[c]);
   N[15] = 0.0f;
+  float4* out = reinterpret_cast<float4*>(n32 + (long long)v * XK_NODE32_STRIDE);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) out[i] = make_float4(N[4 * i], N[4 * i + 1], N[4 * i + 2], N[4 * i + 3]);
 }
 
 __global__ void k_pairs_to32(xk_mesh m, xk_pairs p, xk_contact_pattern pat, xk_pairs32 q) {
@@ -563,10 +595,17 @@ __global__ void k_pairs_from32(xk_pairs32 q, xk_pairs p) {
   const int i = q.pair[j];
   const long long cp = p.cap, cq = q.cap;
   p.s[i] = q.s[j]; p.t[i] = q.t[j]; p.gap[i] = q.gap[j];
+  float n[3], t1[3], t2[3];
   for (int c = 0; c < 3; ++c) {
-    p.normal[c * cp + i] = q.normal[c * cq + j];
-    p.t1[c * cp + i] = q.t1[c * cq + j];
-    p.t2[c * cp + i] = q.t2[c * cq + j];
+    n[c] = q.normal[c * cq + j];
+    t1[c] = q.t1[c * cq + j];
+    t2[c] = q.t2[c * cq + j];
+  }
+  if (j >= q.n_members) cross3(n, t1, t2);  // the other-pair kernel does not store t2
+  for (int c = 0; c < 3; ++c) {
+    p.normal[c * cp + i] = n[c];
+    p.t1[c * cp + i] = t1[c];
+    p.t2[c * cp + i] = t2[c];
   }
   p.p_n[i] = q.p_n[j];
   p.z_t[i] = q.z_t[j]; p.z_t[cp + i] = q.z_t[cq + j];
@@ -579,16 +618,24 @@ XK_D float clamp01f(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
 
 // Closest point and gap of one pair from prepared nodes; frame transported from
 // the previous float frame.  Near-parallel pairs fall back to the exact routine.
-XK_D void narrow32(const float* __restrict__ n32, const int* nd, df R, float& s, float& t, float& gap, float* n,
+// With DF the difference vector and the gap are taken in float-float arithmetic
+// (contributing pairs: the gap drives the normal force).  Without it they are
+// plain float from the exact float differences of the split positions, an
+// absolute gap error of a few float roundings of the segment length (1e-7 mm
+// at 0.5 mm wires): enough for pairs that carry no force in the increment,
+// whose gap the next detection recomputes exactly.
+// With DEFER the near-parallel case is not handled: the function returns true at once and leaves
+// every output untouched (the caller hands the pair to a kernel compiled without DEFER).
+template <bool DF, bool DEFER = false>
+XK_D bool narrow32(const float* __restrict__ n32, const int* nd, df R, float& s, float& t, float& gap, float* n,
                    float* pt1_io, float* t2) {
   df x[4][3];
   for (int k = 0; k < 4; ++k) {
-    const float* N = n32 + (long long)nd[k] * XK_NODE32_STRIDE;
-    const float4 p0 = __ldg(reinterpret_cast<const float4*>(N));
-    const float2 p1 = __ldg(reinterpret_cast<const float2*>(N + 4));
-    x[k][0] = {p0.x, p0.w};
-    x[k][1] = {p0.y, p1.x};
-    x[k][2] = {p0.z, p1.y};
+    float N[8];  // x_hi (3), x_lo (3) and two values not used here: one 256-bit load of a 64-byte record
+    ldg8(n32 + (long long)nd[k] * XK_NODE32_STRIDE, N);
+    x[k][0] = {N[0], N[3]};
+    x[k][1] = {N[1], N[4]};
+    x[k][2] = {N[2], N[5]};
   }
   float fa[3], fb[3], fw[3];
   for (int c = 0; c < 3; ++c) {
@@ -599,11 +646,16 @@ XK_D void narrow32(const float* __restrict__ n32, const int* nd, df R, float& s,
   const float a = dot3(fa, fa), b = dot3(fa, fb), c = dot3(fb, fb), d = dot3(fa, fw), e = dot3(fb, fw);
   const float ac = a * c, det = ac - b * b;
   float nrm[3];
+  if (DEFER && !(det > 1e-3f * ac)) return true;
   if (!(det > 1e-3f * ac)) {
-    // rare: near-parallel or degenerate segments, exact double routine
+    // rare: near-parallel or degenerate segments, exact double routine on the node records read
+    // again (so that the split positions need not stay live through the common path)
     double xd[4][3], sd, td, dist, nd3[3], diff[3];
-    for (int k = 0; k < 4; ++k)
-      for (int q = 0; q < 3; ++q) xd[k][q] = (double)x[k][q].h + (double)x[k][q].l;
+    for (int k = 0; k < 4; ++k) {
+      float N[8];
+      ldg8(n32 + (long long)nd[k] * XK_NODE32_STRIDE, N);
+      for (int q = 0; q < 3; ++q) xd[k][q] = (double)N[q] + (double)N[3 + q];
+    }
     closest_exact(xd[0], xd[1], xd[2], xd[3], sd, td, dist, nd3, diff);
     s = (float)sd;
     t = (float)td;
@@ -620,6 +672,15 @@ XK_D void narrow32(const float* __restrict__ n32, const int* nd, df R, float& s,
     }
     s = sf;
     t = tf;
+    if (!DF) {
+      float D[3];
+      for (int q = 0; q < 3; ++q) D[q] = fmaf(-tf, fb[q], fmaf(sf, fa[q], fw[q]));
+      const float dist = sqrtf(dot3(D, D));
+      gap = (dist - R.h) - R.l;
+      const float id = 1.0f / dist;
+      for (int q = 0; q < 3; ++q) nrm[q] = D[q] * id;
+      if (!(dist > 1e-30f)) { nrm[0] = 0.0f; nrm[1] = 0.0f; nrm[2] = 1.0f; }
+    } else {
     // diff = (xA0 - xB0) + s (xA1 - xA0) - t (xB1 - xB0) in float-float
     df D[3];
     for (int q = 0; q < 3; ++q) {
@@ -644,6 +705,7 @@ XK_D void narrow32(const float* __restrict__ n32, const int* nd, df R, float& s,
     const float id = 1.0f / dh;
     for (int q = 0; q < 3; ++q) nrm[q] = D[q].h * id;
     if (!(dh > 1e-30f)) { nrm[0] = 0.0f; nrm[1] = 0.0f; nrm[2] = 1.0f; }
+    }
   }
   // frame transport (float)
   float pn[3] = {n[0], n[1], n[2]};  // previous normal on entry
@@ -688,6 +750,7 @@ XK_D void narrow32(const float* __restrict__ n32, const int* nd, df R, float& s,
   }
   cross3(n, t1, t2);
   for (int q = 0; q < 3; ++q) pt1_io[q] = t1[q];
+  return false;
 }
 
 XK_D void load3f(const float* base, long long stride, long long i, float* v) {
@@ -701,9 +764,10 @@ XK_D void store3f(float* base, long long stride, long long i, const float* v) {
   base[2 * stride + i] = v[2];
 }
 
-__global__ void __launch_bounds__(PAIR_T, 3) k_pair_other32(xk_pairs32 q, const float* __restrict__ n32) {
-  const int j = q.n_members + blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= q.n) return;
+// Other-pair narrowphase of slot j.  DEFER: near-parallel pairs are appended to q.defer instead
+// (any order: each is then computed on its own by k_pair_other32_deferred).
+template <bool DEFER>
+XK_D void other32(const xk_pairs32& q, const float* __restrict__ n32, int j) {
   const long long cq = q.cap;
   const int4 nd4 = __ldg(reinterpret_cast<const int4*>(q.nodes) + j);
   const int nd[4] = {nd4.x, nd4.y, nd4.z, nd4.w};
@@ -711,30 +775,51 @@ __global__ void __launch_bounds__(PAIR_T, 3) k_pair_other32(xk_pairs32 q, const 
   float s, t, gap, n[3], t1[3], t2[3];
   load3f(q.normal, cq, j, n);
   load3f(q.t1, cq, j, t1);
-  narrow32(n32, nd, {R2.x, R2.y}, s, t, gap, n, t1, t2);
+  if (narrow32<false, DEFER>(n32, nd, {R2.x, R2.y}, s, t, gap, n, t1, t2)) {
+    q.defer[1 + atomicAdd(q.defer, 1)] = j;
+    return;
+  }
   q.s[j] = s;
   q.t[j] = t;
   q.gap[j] = gap;
   store3f(q.normal, cq, j, n);
   store3f(q.t1, cq, j, t1);
-  store3f(q.t2, cq, j, t2);
+  // t2 = n x t1 is not stored for these pairs; k_pairs_from32 forms it
 }
 
-__global__ void __launch_bounds__(PAIR_T, 3) k_pair_member32(xk_pairs32 q, const float* __restrict__ n32,
-                                                             xk_contact_params cp, float* __restrict__ rec) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // slot = member index
-  if (i >= q.n_members) return;
+template <bool DEFER>
+__global__ void __launch_bounds__(PAIR_T) k_pair_other32(xk_pairs32 q, const float* __restrict__ n32) {
+  const int j = q.n_members + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < q.n) other32<DEFER>(q, n32, j);
+}
+
+// The deferred (near-parallel) other pairs, grid-stride over the list.
+__global__ void __launch_bounds__(PAIR_T) k_pair_other32_deferred(xk_pairs32 q, const float* __restrict__ n32) {
+  const int cnt = *(volatile int32_t*)q.defer;
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < cnt; x += gridDim.x * blockDim.x)
+    other32<false>(q, n32, q.defer[1 + x]);
+}
+
+// Member slot i (record i).  DEFER: a near-parallel member is appended to the member part of
+// q.defer (after the cap + 1 words of the other pairs) and left to k_pair_member32_deferred.
+template <bool DEFER>
+XK_D void member32(const xk_pairs32& q, const float* __restrict__ n32, const xk_contact_params& cp,
+                   float* __restrict__ rec, int i) {
   const int mi = i;
   const long long cq = q.cap;
   const int4 nd4 = __ldg(reinterpret_cast<const int4*>(q.nodes) + i);
   const int nd[4] = {nd4.x, nd4.y, nd4.z, nd4.w};
-  uint8_t status = q.status[i];
   const float2 R2 = __ldg(reinterpret_cast<const float2*>(q.rad) + i);
   const df R = {R2.x, R2.y};
   float s, t, gap, n[3], t1[3], t2[3];
   load3f(q.normal, cq, i, n);
   load3f(q.t1, cq, i, t1);
-  narrow32(n32, nd, R, s, t, gap, n, t1, t2);
+  if (narrow32<true, DEFER>(n32, nd, R, s, t, gap, n, t1, t2)) {
+    int32_t* list = q.defer + (cq + 1);
+    list[1 + atomicAdd(list, 1)] = i;
+    return;
+  }
+  uint8_t status = q.status[i];
   q.s[i] = s;
   q.t[i] = t;
   q.gap[i] = gap;
@@ -836,10 +921,26 @@ __global__ void __launch_bounds__(PAIR_T, 3) k_pair_member32(xk_pairs32 q, const
     }
   }
   float4* r = reinterpret_cast<float4*>(rec + (long long)mi * XK_REC_STRIDE_COMBINED);
-  r[0] = make_float4(s, t, vn[0] + vf[0], vn[1] + vf[1]);
-  r[1] = make_float4(vn[2] + vf[2], B[0], B[1], B[2]);
-  r[2] = make_float4(B[3], B[4], B[5], B[6]);
-  r[3] = make_float4(B[7], B[8], 0.f, 0.f);
+  r[0] = make_float4(B[0], B[1], B[2], B[3]);
+  r[1] = make_float4(B[4], B[5], B[6], B[7]);
+  r[2] = make_float4(B[8], s, t, vn[0] + vf[0]);
+  r[3] = make_float4(vn[1] + vf[1], vn[2] + vf[2], 0.f, 0.f);
+}
+
+template <bool DEFER>
+__global__ void __launch_bounds__(PAIR_T, 4) k_pair_member32(xk_pairs32 q, const float* __restrict__ n32,
+                                                             xk_contact_params cp, float* __restrict__ rec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // slot = member index
+  if (i < q.n_members) member32<DEFER>(q, n32, cp, rec, i);
+}
+
+// The deferred (near-parallel) members, grid-stride over the list.
+__global__ void __launch_bounds__(PAIR_T) k_pair_member32_deferred(xk_pairs32 q, const float* __restrict__ n32,
+                                                                   xk_contact_params cp, float* __restrict__ rec) {
+  const int32_t* list = q.defer + ((long long)q.cap + 1);
+  const int cnt = *(volatile const int32_t*)list;
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < cnt; x += gridDim.x * blockDim.x)
+    member32<false>(q, n32, cp, rec, list[1 + x]);
 }
 
 __global__ void k_active_flags(xk_pairs p, int32_t* __restrict__ flag) {
@@ -1058,7 +1159,12 @@ extern "C" xk_status xk_nodes_prepare(const xk_mesh* m, const double* u, const d
                                       xk_stream s) {
   if (!m || !u || !node32) return xk_set_error(XK_ERR_ARG, "xk_nodes_prepare: null argument");
   if (m->n_nodes == 0) return XK_OK;
-  k_nodes_prepare<<<xk_blocks(m->n_nodes, 256), 256, 0, (cudaStream_t)s>>>(*m, u, u_ref, node32);
+  if (((uintptr_t)node32 & 15) != 0) return xk_set_error(XK_ERR_ARG, "xk_nodes_prepare: node32 must be 16-byte aligned");
+  const bool vec = ((uintptr_t)u & 15) == 0 && ((uintptr_t)u_ref & 15) == 0;
+  if (vec)
+    k_nodes_prepare<true><<<xk_blocks(m->n_nodes, 256), 256, 0, (cudaStream_t)s>>>(*m, u, u_ref, node32);
+  else
+    k_nodes_prepare<false><<<xk_blocks(m->n_nodes, 256), 256, 0, (cudaStream_t)s>>>(*m, u, u_ref, node32);
   XK_CHECK_LAUNCH();
   return XK_OK;
 }
@@ -1089,13 +1195,30 @@ extern "C" xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream
 extern "C" xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk_contact_params* cp, float* rec,
                                     int parts, xk_stream s) {
   if (!q || !node32 || !cp) return xk_set_error(XK_ERR_ARG, "xk_pair_step32: null argument");
+  if (((uintptr_t)node32 & 31) != 0 || ((uintptr_t)rec & 15) != 0)
+    return xk_set_error(XK_ERR_ARG, "xk_pair_step32: node32 must be 32-byte and rec 16-byte aligned");
   if ((parts & XK_PAIRS_MEMBERS) && q->n_members > 0 && !rec)
     return xk_set_error(XK_ERR_ARG, "xk_pair_step32: rec is null");
   cudaStream_t st = (cudaStream_t)s;
   const int n_o = q->n - q->n_members;
-  if ((parts & XK_PAIRS_OTHERS) && n_o > 0) k_pair_other32<<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
-  if ((parts & XK_PAIRS_MEMBERS) && q->n_members > 0)
-    k_pair_member32<<<xk_blocks(q->n_members, PAIR_T), PAIR_T, 0, st>>>(*q, node32, *cp, rec);
+  if ((parts & XK_PAIRS_OTHERS) && n_o > 0) {
+    if (q->defer) {
+      XK_CUDA(cudaMemsetAsync(q->defer, 0, sizeof(int32_t), st));
+      k_pair_other32<true><<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
+      k_pair_other32_deferred<<<152, PAIR_T, 0, st>>>(*q, node32);
+    } else {
+      k_pair_other32<false><<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
+    }
+  }
+  if ((parts & XK_PAIRS_MEMBERS) && q->n_members > 0) {
+    if (q->defer) {
+      XK_CUDA(cudaMemsetAsync(q->defer + ((long long)q->cap + 1), 0, sizeof(int32_t), st));
+      k_pair_member32<true><<<xk_blocks(q->n_members, PAIR_T), PAIR_T, 0, st>>>(*q, node32, *cp, rec);
+      k_pair_member32_deferred<<<152, PAIR_T, 0, st>>>(*q, node32, *cp, rec);
+    } else {
+      k_pair_member32<false><<<xk_blocks(q->n_members, PAIR_T), PAIR_T, 0, st>>>(*q, node32, *cp, rec);
+    }
+  }
   XK_CHECK_LAUNCH();
   return XK_OK;
 }

@@ -76,6 +76,13 @@ struct Prec<XK_FP64> { typedef double T; };
 template <>
 struct Prec<XK_MIXED> { typedef float T; };
 
+// Eight floats from a 32-byte aligned read-only address in one 256-bit load.
+XK_D void ldg8(const float* __restrict__ p, float* v) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+      : "l"(p));
+}
+
 // ---------------------------------------------------------------------------
 // Launch helpers
 // ---------------------------------------------------------------------------

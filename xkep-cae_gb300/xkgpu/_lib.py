@@ -29,6 +29,12 @@ class Section(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("E", "G", "A", "Iy", "Iz", "J", "kappa_y", "kappa_z", "scf")]
 
 
+class StrandSpec(C.Structure):
+    _fields_ = [("n_wires", C.c_int32), ("n_elems_per_wire", C.c_int32), ("lay_direction", C.c_int32),
+                ("pad", C.c_int32), ("wire_diameter", C.c_double), ("pitch", C.c_double), ("length", C.c_double),
+                ("gap", C.c_double), ("x_offset", C.c_double), ("node_first", C.c_int64), ("elem_first", C.c_int64)]
+
+
 class Mesh(C.Structure):
     _fields_ = [("n_nodes", C.c_int32), ("n_elems", C.c_int32), ("X", vp), ("conn", vp), ("radii", vp),
                 ("layer", vp), ("mu", vp)]
@@ -43,12 +49,12 @@ class Pairs(C.Structure):
 class Pairs32(C.Structure):
     _fields_ = [("n", C.c_int32), ("cap", C.c_int32), ("n_members", C.c_int32)] + [
         (n, vp) for n in ("pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
-                          "dissipation", "k_pen", "k_t", "status", "stick", "mu")]
+                          "dissipation", "k_pen", "k_t", "status", "stick", "mu", "defer")]
 
 
 class BeamPlan(C.Structure):
     _fields_ = [("n_colors", C.c_int32), ("color_ptr_host", vp), ("elem_order", vp), ("blk", vp), ("first", vp),
-                ("nnzb", C.c_int64)]
+                ("nnzb", C.c_int64), ("node_diag", vp)]
 
 
 class ContactParams(C.Structure):
@@ -68,7 +74,8 @@ class ContactPattern(C.Structure):
                 ("cap_others", C.c_int64), ("cap_blocks", C.c_int64)] + [
         (n, vp) for n in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row",
                           "blk_ptr", "contrib")] + [("n_elems", C.c_int64), ("sides_ok", C.c_int64)] + [
-        (n, vp) for n in ("node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums")]
+        (n, vp) for n in ("node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums",
+                          "norm_scratch")]
 
 
 P = C.POINTER
@@ -82,12 +89,14 @@ SIGNATURES = {
     "xk_broadphase": [P(Mesh), vp, P(BPParams), vp, C.c_int64, i64p, i64p, i64p, vp],
     "xk_pairs_merge": [P(Mesh), P(Pairs), vp, C.c_int64, P(Pairs), vp],
     "xk_narrowphase": [P(Mesh), P(Pairs), vp, P(ContactParams), C.c_int, vp],
+    "xk_strand_generate": [vp, C.c_int32, C.c_int64, C.c_int64, vp, vp, vp, vp, vp],
     "xk_contact_pattern_build": [P(Mesh), P(Pairs), P(ContactPattern), vp],
     "xk_pair_step": [P(Mesh), P(Pairs), P(ContactPattern), vp, vp, P(ContactParams), C.c_int, C.c_int, C.c_int, vp,
                      vp],
     "xk_contact_gather_force": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, vp, C.c_double, vp, vp, vp, vp,
                                 vp],
     "xk_contact_gather_tangent": [P(ContactPattern), vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp],
+    "xk_contact_gather_force_elem": [P(ContactPattern), C.c_int, vp, C.c_double, vp, vp, vp, vp, vp],
     "xk_constraint_jacobian": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
     "xk_constraint_jacobian_noalloc": [P(Mesh), P(Pairs), vp, vp, vp, vp, C.c_int64, i64p, vp],
     "xk_norm2": [vp, C.c_int64, vp, vp],

@@ -154,10 +154,30 @@ def make_beam_plan(conn: np.ndarray, n_nodes: int) -> BeamPlanHost:
     return BeamPlanHost(row_ptr, col, blk, colors, order, color_ptr, first)
 
 
+def chain_node_diag(conn: np.ndarray, n_nodes: int, plan: BeamPlanHost) -> np.ndarray | None:
+    """Diagonal block of every node (-1 without element) if the mesh is a set of chains, else None.
+
+    A chain mesh has at most two elements at every node and no two elements on
+    the same pair of nodes, so that every shared location of K_T and f_int has
+    exactly two contributions."""
+    conn = np.asarray(conn, dtype=np.int64)
+    if conn.shape[0] == 0 or np.any(conn[:, 0] == conn[:, 1]):
+        return None
+    if np.bincount(conn.ravel(), minlength=n_nodes).max() > 2:
+        return None
+    key = np.sort(conn, axis=1)
+    if np.unique(key[:, 0] * n_nodes + key[:, 1]).shape[0] != conn.shape[0]:
+        return None
+    diag = np.full(n_nodes, -1, dtype=np.int32)
+    diag[conn[:, 0]] = plan.blk[:, 0]
+    diag[conn[:, 1]] = plan.blk[:, 3]
+    return diag
+
+
 class DeviceBeam:
     """CR beam data: section, per-element reference frames and the K_T plan."""
 
-    def __init__(self, mesh: DeviceMesh, section: dict, *, v_ref=None):
+    def __init__(self, mesh: DeviceMesh, section: dict, *, v_ref=None, chain: bool = True):
         self.mesh = mesh
         dev = mesh.device
         scf = section.get("scf")
@@ -173,8 +193,11 @@ class DeviceBeam:
         self.row_ptr = torch.as_tensor(ph.row_ptr, device=dev)
         self.col = torch.as_tensor(ph.col, device=dev)
         self._color_ptr = (C.c_int32 * len(ph.color_ptr))(*ph.color_ptr.tolist())
+        # wires: every node in at most two elements, no two elements on the same nodes -> one-launch float path
+        nd = chain_node_diag(mesh.conn_host, mesh.n_nodes, ph) if chain else None
+        self.node_diag = None if nd is None else torch.as_tensor(nd, device=dev)
         self.plan = L.BeamPlan(len(ph.color_ptr) - 1, C.cast(self._color_ptr, C.c_void_p), ptr(self.order),
-                               ptr(self.blk), ptr(self.first), ph.nnzb)
+                               ptr(self.blk), ptr(self.first), ph.nnzb, ptr(self.node_diag))
         self.elem_ref = torch.empty(10 * max(mesh.n_elems, 1), dtype=torch.float64, device=dev)
         self.update_reference_frames()
 
@@ -327,11 +350,12 @@ class DevicePairTable32:
         t["status"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         t["stick"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         t["mu"] = torch.zeros(cap, dtype=torch.float32, device=self.device) if self.per_slot_mu else None
+        t["defer"] = torch.zeros(2 * (cap + 1), dtype=torch.int32, device=self.device)
         self.t = t
         self.cap = cap
         self.c = L.Pairs32(0, cap, 0, *(ptr(t[k]) for k in (
             "pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
-            "dissipation", "k_pen", "k_t", "status", "stick", "mu")))
+            "dissipation", "k_pen", "k_t", "status", "stick", "mu", "defer")))
 
 
 # ----------------------------------------------------------------------------- contact pattern
@@ -351,7 +375,9 @@ class DeviceContactPattern:
         self.node_elem_ptr = self._i32(mesh.n_nodes + 1)
         self.node_elem = self._i32(4 * mesh.n_elems)
         self.elem_ptr = self._i32(mesh.n_elems + 1)
-        self.elem_sums = torch.zeros(27 * max(mesh.n_elems, 1), dtype=torch.float64, device=mesh.device)
+        self.elem_sums = torch.zeros(56 * max(mesh.n_elems, 1), dtype=torch.float64, device=mesh.device)
+        self.norm_scratch = torch.zeros((6 * mesh.n_nodes + 255) // 256 + 1, dtype=torch.float64,
+                                        device=mesh.device)
         self._alloc_members(256)
         self._alloc_others(256)
         self._alloc_blocks(1024)
@@ -382,7 +408,8 @@ class DeviceContactPattern:
         c.n_nodes = self.mesh.n_nodes
         c.cap_members, c.cap_others, c.cap_blocks = self.cap_members, self.cap_others, self.cap_blocks
         for k in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row", "blk_ptr",
-                  "contrib", "node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums"):
+                  "contrib", "node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums",
+                  "norm_scratch"):
             setattr(c, k, ptr(getattr(self, k)))
 
     def build(self, pairs: DevicePairTable, stream=None):

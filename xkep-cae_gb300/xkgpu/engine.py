@@ -261,16 +261,24 @@ class AssemblyEngine:
         else:
             L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
                    C.byref(self.cp), L.XK_STAGE_ALL | L.XK_STAGE_NO_OTHERS, p, L.XK_OUT_COMBINED, ptr(self.rec), s)
-        if tangent and self.pattern.nnzb > 0:
+        gather = tangent and self.pattern.nnzb > 0
+        # the element-side schedules leave per-element force sums that the residual reads
+        elem_force = gather and self.gather_variant == L.XK_GATHER_SIDES
+        if gather:
             st.wait_stream(main)
             L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
                    self.gather_variant, ptr(self.K_c), stream_handle(st))
-        # residual after the members and the beam
+        # residual after the members (or the tangent gather's element sums) and the beam
         main.wait_stream(sb)
-        L.call("xk_contact_gather_force", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
-               ptr(self.f_int), -1.0, ptr(f_ext), ptr(fixed), ptr(self.R), ptr(self.norm2), s)
+        if elem_force:
+            main.wait_stream(st)
+            L.call("xk_contact_gather_force_elem", pat, p, ptr(self.f_int), -1.0, ptr(f_ext), ptr(fixed),
+                   ptr(self.R), ptr(self.norm2), s)
+        else:
+            L.call("xk_contact_gather_force", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
+                   ptr(self.f_int), -1.0, ptr(f_ext), ptr(fixed), ptr(self.R), ptr(self.norm2), s)
         main.wait_stream(so)
-        if tangent and self.pattern.nnzb > 0:
+        if gather:
             main.wait_stream(st)
         return self.R
 
@@ -319,6 +327,7 @@ class AssemblyEngine:
             torch.cuda.synchronize()
             times[v] = a.elapsed_time(b) / reps
         self.gather_variant = min(times, key=times.get)
+        self.tune_times = times
         self._tuned_for = (self.pattern.version, self.precision)
         return times
 

@@ -212,21 +212,29 @@ def radial_compression(strand: Strand, layer: int, amount: float) -> np.ndarray:
     return u
 
 
+def strand_offsets(strands: list[Strand], spacing: float | None = None) -> list[float]:
+    """x shift of every strand laid side by side: half-widths (outer lay radius + d) plus a spacing."""
+    xs, out = 0.0, []
+    for s in strands:
+        half = max((w.lay_radius for w in s.wires), default=0.0) + s.wire_diameter
+        gap = spacing if spacing is not None else 4.0 * s.wire_diameter
+        out.append(xs + half)
+        xs += 2.0 * half + gap
+    return out
+
+
 def merge_strands(strands: list[Strand], spacing: float | None = None) -> tuple[Strand, np.ndarray, np.ndarray]:
     """Lay several strands side by side in one mesh (the batched workload).
 
     Returns the merged strand, the per-element instance id and the first node of
     every instance.  Strands are shifted along x so that no two instances touch.
     """
-    xs = 0.0
+    offsets = strand_offsets(strands, spacing)
     coords, conns, layers, radii, node_first, inst = [], [], [], [], [], []
     n_off = 0
     for k, s in enumerate(strands):
         c = s.coords.copy()
-        half = float(np.max(np.abs(c[:, 0:2]))) + s.wire_diameter
-        gap = spacing if spacing is not None else 4.0 * s.wire_diameter
-        c[:, 0] += xs + half
-        xs += 2.0 * half + gap
+        c[:, 0] += offsets[k]
         coords.append(c)
         conns.append(s.conn + n_off)
         layers.append(s.elem_layer)
@@ -247,3 +255,41 @@ def merge_strands(strands: list[Strand], spacing: float | None = None) -> tuple[
         meta={"instances": len(strands)},
     )
     return merged, np.concatenate(inst), np.asarray(node_first, dtype=np.int64)
+
+
+def strand_spec(strand: Strand, *, x_offset: float = 0.0, node_first: int = 0, elem_first: int = 0):
+    """The device generator's description (``xk_strand_spec``) of a strand built by ``make_strand``."""
+    from . import _lib as L
+
+    lay = next((w.lay_direction for w in strand.wires if w.layer == 1), 1)
+    return L.StrandSpec(len(strand.wires), strand.n_elems_per_wire, int(lay), 0, strand.wire_diameter,
+                        strand.pitch, strand.length, float(strand.meta.get("gap", 0.0)), float(x_offset),
+                        int(node_first), int(elem_first))
+
+
+def generate_on_device(specs: list, device=None):
+    """Nodes, connectivity, element layers and radii of the strands ``specs`` (``xk_strand_spec``) on the GPU.
+
+    The specs must tile the mesh in order (``node_first`` / ``elem_first``
+    ascending, each strand right after the previous one).  Returns
+    ``(X (n_nodes, 3) float64, conn (n_elems, 2) int32, layer int32, radii float64)`` device tensors.
+    """
+    import ctypes as C
+
+    import torch
+
+    from . import _lib as L
+    from .device import ptr, require_cuda, stream_handle
+
+    dev = require_cuda(device)
+    n_nodes = sum(s.n_wires * (s.n_elems_per_wire + 1) for s in specs)
+    n_elems = sum(s.n_wires * s.n_elems_per_wire for s in specs)
+    raw = (L.StrandSpec * len(specs))(*specs)
+    buf = torch.frombuffer(bytearray(bytes(raw)), dtype=torch.uint8).to(dev)
+    X = torch.empty(3 * max(n_nodes, 1), dtype=torch.float64, device=dev)
+    conn = torch.empty(2 * max(n_elems, 1), dtype=torch.int32, device=dev)
+    layer = torch.empty(max(n_elems, 1), dtype=torch.int32, device=dev)
+    radii = torch.empty(max(n_elems, 1), dtype=torch.float64, device=dev)
+    L.call("xk_strand_generate", ptr(buf), len(specs), n_nodes, n_elems, ptr(X), ptr(conn), ptr(layer), ptr(radii),
+           stream_handle(None))
+    return X[: 3 * n_nodes].view(-1, 3), conn[: 2 * n_elems].view(-1, 2), layer[:n_elems], radii[:n_elems]
