@@ -664,6 +664,7 @@ def run_profile(args):
     """Small driver for ncu: one engine, one detection, ``--steps`` eager assemblies."""
     import torch
 
+    from xkgpu import _lib as L
     from xkgpu import workloads as W
     from xkgpu.engine import AssemblyEngine
 
@@ -680,15 +681,19 @@ def run_profile(args):
     u0 = torch.as_tensor(w.u, device="cuda")
     u1 = u0 * 1.001
     stats = eng.detect(u0)
+    if args.schedule != "auto":  # a fixed tangent schedule (the autotuner's timings are distorted under ncu)
+        eng.gather_variant = {"lanes": L.XK_GATHER_LANES, "chunks": L.XK_GATHER_CHUNKS,
+                              "sides": L.XK_GATHER_SIDES}[args.schedule]
     eng.assemble(u1, u0)
-    eng.tune()  # the schedule the timed graph uses
+    if args.schedule == "auto":
+        eng.tune()  # the schedule the timed graph uses
     for _ in range(args.steps):
         eng.assemble(u1, u0)
     torch.cuda.synchronize()
     pat = eng.pattern
     print(json.dumps({"profile": args.profile, "workload": args.workload, **stats, "nnzb": pat.nnzb,
                       "n_contrib": pat.n_contrib, "gather_variant": eng.gather_variant,
-                      "schedule_ms": {str(k): v for k, v in eng.tune_times.items()},
+                      "schedule_ms": {str(k): v for k, v in getattr(eng, "tune_times", {}).items()},
                       "device_bytes_peak": torch.cuda.max_memory_allocated()}))
 
 
@@ -772,6 +777,8 @@ def main():
     ap.add_argument("--profile", choices=["mixed", "fp64", "mlp"], default=None,
                     help="profiling driver: detect once, then --steps eager assemblies, no timing")
     ap.add_argument("--breakdown", action="store_true", help="warm per-phase times (ms) of one assembly")
+    ap.add_argument("--schedule", choices=["auto", "lanes", "chunks", "sides"], default="auto",
+                    help="tangent schedule of --profile (auto: the autotuner's choice)")
     args = ap.parse_args()
     if args.breakdown:
         run_breakdown(args)

@@ -332,10 +332,11 @@ typedef struct {
   uint8_t *status, *stick;
   float* mu;               /* [cap] friction coefficient of each slot, filled from xk_mesh.mu by xk_pairs_to32;
                               NULL (use xk_contact_params.mu_eff) unless the mesh has per-element mu */
-  int32_t* defer;          /* [2 * (cap + 1)] scratch or NULL: the pair kernels then leave the rare
-                              near-parallel pairs to a second kernel each (other pairs: count in
-                              defer[0], slots after it; members: the same from defer[cap + 1]),
-                              which keeps the exact double routine out of the common kernels */
+  int32_t* defer;          /* [2 * (cap + 2)] zero-initialised scratch or NULL: the pair kernels then
+                              leave the rare near-parallel pairs to a second kernel each (other
+                              pairs: [count, done, slots] from defer[0]; members: the same from
+                              defer[cap + 2]), which keeps the exact double routine out of the common
+                              kernels; each list is back at zero after its kernel */
 } xk_pairs32;
 
 /* Per iteration: node records for the mixed kernels from u (and u_ref, nullable). */
@@ -381,6 +382,15 @@ xk_status xk_softplus_normal_law(int64_t n, const double* gaps, const double* la
 xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p, int32_t* rows, int32_t* cols,
                                  double* vals, int32_t* pair_index, int64_t cap, int64_t* n_rows,
                                  xk_stream s);
+
+/* Gauss-point count of every pair for the line-to-line and mortar geometry
+ * strategies with auto_gauss (_auto_select_n_gauss,
+ * xkep_cae/contact/geometry/_compute.py:264-291, called from
+ * LineToLineGaussProcess.update_geometry, geometry/strategy.py:436-451): from
+ * the segment directions at X + u (u nullable: X), |cos| < 0.866 -> 2,
+ * < 0.985 -> 3, else 5; default_n for a zero-length segment.  out: int8 [n]. */
+xk_status xk_pair_gauss_points(const xk_mesh* m, const xk_pairs* p, const double* u, int32_t default_n,
+                               int8_t* out, xk_stream s);
 
 /* ------------------------------------------------------------------------
  * Generalized-alpha time integration with a lumped mass, no damping

@@ -12,6 +12,7 @@ reference's contact hot path:
 * ``CoulombReturnMappingProcess``   ``xkep_cae/contact/friction/strategy.py:111-164``,
   ``friction/_assembly.py:53-342``, ``friction/law_friction.py:89-153``
 * ``_build_constraint_jacobian_ptp`` ``xkep_cae/contact/geometry/strategy.py:83-132``
+* ``_auto_select_n_gauss``          ``xkep_cae/contact/geometry/_compute.py:264-291``
 
 Where the reference's candidate and active sets hinge on floating-point
 compares, this oracle reproduces its arithmetic operation for operation:
@@ -511,3 +512,24 @@ def contact_iteration(table, X_ref, u, u_ref, ndof, *, k_pen, k_t_ratio, mu_eff,
     Kn = huber_tangent(t, ndof, k_pen, smoothing_delta)
     Kf = friction_tangent(t, fr, ndof)
     return t, -(fn + ff), (Kn - Kf).tocsr(), {"f_n": fn, "f_f": ff, "K_n": Kn, "K_f": Kf, "fric": fr}
+
+
+def auto_n_gauss(dA, dB, default: int = 3) -> np.ndarray:
+    """Gauss-point count per segment pair (``_auto_select_n_gauss``, ``geometry/_compute.py:264-291``).
+
+    Row by row with the reference's own NumPy calls (``np.linalg.norm`` of a
+    3-vector, ``dA @ dB``): |cos| < 0.866 -> 2, < 0.985 -> 3, else 5; ``default``
+    when a segment has zero length.
+    """
+    dA = np.asarray(dA, dtype=float).reshape(-1, 3)
+    dB = np.asarray(dB, dtype=float).reshape(-1, 3)
+    out = np.empty(dA.shape[0], dtype=np.int64)
+    for i in range(dA.shape[0]):
+        len_a = float(np.linalg.norm(dA[i]))
+        len_b = float(np.linalg.norm(dB[i]))
+        if len_a < 1e-30 or len_b < 1e-30:
+            out[i] = default
+            continue
+        c = abs(float(dA[i] @ dB[i] / (len_a * len_b)))
+        out[i] = 2 if c < 0.866 else (3 if c < 0.985 else 5)
+    return out

@@ -283,6 +283,26 @@ def genalpha_case(R, name, seed=4, n=600):
     print(name)
 
 
+def gauss_case(R, name, seed=11, n=1200):
+    """Gauss-point counts of segment pairs at every angle (line-to-line / mortar auto_gauss)."""
+    rng = np.random.default_rng(seed)
+    dA = rng.normal(size=(n, 3))
+    ang = rng.uniform(0.0, np.pi, n)
+    # a unit vector at angle ang to dA, in a random plane through dA
+    a = dA / np.linalg.norm(dA, axis=1, keepdims=True)
+    w = rng.normal(size=(n, 3))
+    w -= np.sum(w * a, axis=1, keepdims=True) * a
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    dB = (np.cos(ang)[:, None] * a + np.sin(ang)[:, None] * w) * rng.uniform(0.1, 3.0, (n, 1))
+    dA[:10] = 0.0            # zero-length A
+    dB[10:20] = 0.0          # zero-length B
+    xA0 = rng.normal(size=(n, 3))
+    xB0 = rng.normal(size=(n, 3))
+    ng = np.array([R["gc"]._auto_select_n_gauss(dA[i], dB[i]) for i in range(n)])
+    np.savez_compressed(HERE / f"{name}.npz", xA0=xA0, xA1=xA0 + dA, xB0=xB0, xB1=xB0 + dB, n_gauss=ng)
+    print(name, n, np.bincount(ng))
+
+
 CASES = {
     "strand7": lambda R: strand_case(R, "strand7", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16,
                                      gap_frac=-0.005, seed=0, mu=0.1),
@@ -296,6 +316,7 @@ CASES = {
     "meshes": lambda R: mesh_case(R, "meshes"),
     "laws": lambda R: laws_case(R, "laws"),
     "genalpha": lambda R: genalpha_case(R, "genalpha"),
+    "gauss_points": lambda R: gauss_case(R, "gauss_points"),
 }
 
 

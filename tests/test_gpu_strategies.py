@@ -185,3 +185,41 @@ def test_smooth_normal_law_matches_reference():
     p0, d0 = S.smooth_normal_force(g, 1e5, None, delta=1e-4)
     pe, de = oc.softplus_normal_law(g, 1e5, np.zeros_like(g), 1e-4)
     assert rel_err(p0, pe) < 1e-14 and rel_err(d0, de) < 1e-14
+
+
+def test_line_to_line_gauss_points_and_geometry():
+    """Gauss-point counts on the GPU equal the reference's (golden), and the line-to-line and mortar
+    strategies update the geometry exactly as point-to-point, setting _n_gauss where a pair has it."""
+    z = golden("gauss_points")
+    n = z["xA0"].shape[0]
+    X = np.concatenate([z["xA0"], z["xA1"], z["xB0"], z["xB1"]])
+    Pair, State, _ = S.pair_types()
+    pairs = [Pair(elem_a=2 * i, elem_b=2 * i + 1, nodes_a=np.array([i, n + i]), nodes_b=np.array([2 * n + i, 3 * n + i]),
+                  state=State(), radius_a=0.1, radius_b=0.1) for i in range(n)]
+    ng = S.pair_gauss_points(pairs, X)
+    assert np.array_equal(ng, z["n_gauss"])
+    assert np.array_equal(ng, oc.auto_n_gauss(z["xA1"] - z["xA0"], z["xB1"] - z["xB0"]))
+
+    import dataclasses
+
+    # a mutable pair type that carries the attribute the reference checks for
+    spec = []
+    for f in dataclasses.fields(Pair):
+        if f.default is not dataclasses.MISSING:
+            spec.append((f.name, f.type, dataclasses.field(default=f.default)))
+        elif f.default_factory is not dataclasses.MISSING:
+            spec.append((f.name, f.type, dataclasses.field(default_factory=f.default_factory)))
+        else:
+            spec.append((f.name, f.type))
+    WithGauss = dataclasses.make_dataclass("WithGauss", spec + [("_n_gauss", int, dataclasses.field(default=0))])
+    tagged = [WithGauss(**{f.name: getattr(p, f.name) for f in dataclasses.fields(p)}) for p in pairs]
+    ptp, l2l = list(pairs), list(tagged)
+    S.GpuPointToPoint().update_geometry(ptp, X)
+    S.create_contact_geometry_strategy(line_contact=True, auto_gauss=True).update_geometry(l2l, X)
+    mortar = list(pairs)
+    S.create_contact_geometry_strategy(use_mortar=True).update_geometry(mortar, X)
+    for a, b, c in zip(ptp, l2l, mortar):
+        for k in ("s", "t", "gap"):
+            assert getattr(a.state, k) == getattr(b.state, k) == getattr(c.state, k)
+        assert np.array_equal(a.state.normal, b.state.normal) and np.array_equal(a.state.tangent1, c.state.tangent1)
+    assert np.array_equal(np.array([p._n_gauss for p in l2l]), z["n_gauss"])

@@ -128,3 +128,11 @@ def test_softplus_law_oracle_matches_reference():
     z = golden("laws")
     p, dp = oc.softplus_normal_law(z["gap"], float(z["k_pen"]), z["lam"], float(z["delta"]))
     assert np.array_equal(p, z["p_n"]) and np.array_equal(dp, z["dp_dg"])
+
+
+def test_gauss_point_counts_match_reference():
+    """auto_n_gauss against _auto_select_n_gauss's own outputs (all three counts and zero-length segments)."""
+    z = golden("gauss_points")
+    ng = oc.auto_n_gauss(z["xA1"] - z["xA0"], z["xB1"] - z["xB0"])
+    assert np.array_equal(ng, z["n_gauss"])
+    assert set(np.unique(ng)) == {2, 3, 5}

@@ -130,6 +130,8 @@ def _reference_protocols():
     ("ContactForceStrategy", S.GpuHuberContactForce),
     ("FrictionStrategy", S.GpuCoulombReturnMapping),
     ("ContactGeometryStrategy", S.GpuPointToPoint),
+    ("ContactGeometryStrategy", S.GpuLineToLineGauss),
+    ("ContactGeometryStrategy", S.GpuMortarSegment),
     ("PenaltyStrategy", P.AutoEALPenalty),
     ("PenaltyStrategy", P.ContinuationPenalty),
 ])
@@ -143,3 +145,17 @@ def test_protocol_signatures(proto, cls):
         want = [q for q in inspect.signature(getattr(p, n)).parameters if q != "self"]
         got = [q for q in inspect.signature(getattr(cls, n)).parameters if q != "self"]
         assert got[: len(want)] == want, (n, got, want)
+
+
+def test_geometry_strategy_factory_selection():
+    """create_contact_geometry_strategy picks classes as _create_contact_geometry_strategy does:
+    use_mortar over line_contact over mode, the mode names, and the options passed on."""
+    f = S.create_contact_geometry_strategy
+    assert type(f()) is S.GpuPointToPoint
+    assert type(f(mode="line_to_line")) is S.GpuLineToLineGauss
+    assert type(f(mode="mortar")) is S.GpuMortarSegment
+    assert type(f(line_contact=True)) is S.GpuLineToLineGauss
+    assert type(f(use_mortar=True, line_contact=True)) is S.GpuMortarSegment
+    assert type(f(mode="unknown")) is S.GpuPointToPoint
+    g = f(mode="line_to_line", n_gauss=4, auto_gauss=True, exclude_same_layer=False)
+    assert (g._n_gauss, g._auto_gauss, g._exclude_same_layer) == (4, True, False)

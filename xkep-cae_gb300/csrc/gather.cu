@@ -510,13 +510,15 @@ __global__ void __launch_bounds__(128) k_elem_sums_rec(int ne, const int32_t* __
 }
 
 // R[dof] = base[dof] + scale * (contact force at the node) - f_ext[dof], zero where fixed, from
-// the element force sums of the last element-side tangent gather: one thread per degree of
-// freedom, the node's incident elements in their list order.  The block partial sums of R^2
-// go to `part`, and the last block to finish adds them in block order into *norm2 (a fixed
-// order whatever the timing); `count` (zero between launches) finds the last block.
+// the element force sums of the last element-side tangent gather: one thread per node, its
+// incident elements in their list order.  The block partial sums of R^2 (each thread's six
+// squares in order, then a fixed shuffle tree over the warp and over the block's warps) go to
+// `part`, and the last block to finish adds them in block order into *norm2 (a fixed order
+// whatever the timing); `count` (zero between launches) finds the last block.  VEC: base,
+// f_ext and out are 16-byte aligned and moved as double2.
 constexpr int GFE_T = 256;
 
-template <typename T>
+template <typename T, bool VEC>
 __global__ void __launch_bounds__(GFE_T) k_gather_force_elem(int n_nodes, int ne, const int32_t* __restrict__ neptr,
                                                              const int2* __restrict__ nelem, const T* __restrict__ S,
                                                              const double* __restrict__ base, double scale,
@@ -525,35 +527,76 @@ __global__ void __launch_bounds__(GFE_T) k_gather_force_elem(int n_nodes, int ne
                                                              double* __restrict__ out, double* __restrict__ part,
                                                              unsigned int* __restrict__ count,
                                                              double* __restrict__ norm2) {
-  __shared__ double red[GFE_T];
+  __shared__ double red[GFE_T / 32];
   __shared__ bool last;
-  const long long i = (long long)blockIdx.x * GFE_T + threadIdx.x;
-  double r = 0.0;
-  if (i < 6LL * n_nodes) {
-    const int v = (int)(i / 6), d = (int)(i % 6);
-    r = base ? base[i] : 0.0;
-    if (d < 3) {
-      const T* F = S + (long long)ELEM_SUMS * ne;
-      T acc = T(0);
-      for (int y = neptr[v]; y < neptr[v + 1]; ++y) {
-        const int ex = nelem[y].x;  // (element << 1) | local index of v in it
-        acc += F[(long long)ELEM_FORCE * (ex >> 1) + 3 * (ex & 1) + d];
+  const int v = blockIdx.x * GFE_T + threadIdx.x;
+  double sq = 0.0;
+  if (v < n_nodes) {
+    double r[6];
+    if (base) {
+      if (VEC) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const double2 x = __ldg(reinterpret_cast<const double2*>(base + 6LL * v) + i);
+          r[2 * i] = x.x;
+          r[2 * i + 1] = x.y;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) r[c] = base[6LL * v + c];
       }
-      r += scale * (double)acc;
+    } else {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) r[c] = 0.0;
     }
-    if (f_ext) r -= f_ext[i];
-    if (fixed && fixed[i]) r = 0.0;
-    out[i] = r;
+    const T* F = S + (long long)ELEM_SUMS * ne;
+    T acc[3] = {T(0), T(0), T(0)};
+    for (int y = neptr[v]; y < neptr[v + 1]; ++y) {
+      const int ex = nelem[y].x;  // (element << 1) | local index of v in it
+      const T* f = F + (long long)ELEM_FORCE * (ex >> 1) + 3 * (ex & 1);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c] += f[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r[c] += scale * (double)acc[c];
+    if (f_ext) {
+      if (VEC) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const double2 x = __ldg(reinterpret_cast<const double2*>(f_ext + 6LL * v) + i);
+          r[2 * i] -= x.x;
+          r[2 * i + 1] -= x.y;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) r[c] -= f_ext[6LL * v + c];
+      }
+    }
+    if (fixed) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c)
+        if (fixed[6LL * v + c]) r[c] = 0.0;
+    }
+    if (VEC) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) reinterpret_cast<double2*>(out + 6LL * v)[i] = make_double2(r[2 * i], r[2 * i + 1]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) out[6LL * v + c] = r[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sq = fma(r[c], r[c], sq);
   }
   if (!norm2) return;  // uniform over the launch
-  red[threadIdx.x] = r * r;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
+  if (lane == 0) red[warp] = sq;
   __syncthreads();
-  for (int w = GFE_T / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
   if (threadIdx.x == 0) {
-    part[blockIdx.x] = red[0];
+    double b = 0.0;
+    for (int w = 0; w < GFE_T / 32; ++w) b += red[w];
+    part[blockIdx.x] = b;
     __threadfence();
     last = atomicAdd(count, 1u) == gridDim.x - 1;
   }
@@ -562,14 +605,14 @@ __global__ void __launch_bounds__(GFE_T) k_gather_force_elem(int n_nodes, int ne
   __threadfence();
   double a = 0.0;
   for (int b = threadIdx.x; b < (int)gridDim.x; b += GFE_T) a += __ldcg(part + b);
-  red[threadIdx.x] = a;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  if (lane == 0) red[warp] = a;
   __syncthreads();
-  for (int w = GFE_T / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
   if (threadIdx.x == 0) {
-    *norm2 = red[0];
+    double t = 0.0;
+    for (int w = 0; w < GFE_T / 32; ++w) t += red[w];
+    *norm2 = t;
     *count = 0u;  // ready for the next launch
   }
 }
@@ -1069,18 +1112,21 @@ extern "C" xk_status xk_contact_gather_force_elem(const xk_contact_pattern* pat,
     if (norm2) XK_CUDA(cudaMemsetAsync(norm2, 0, sizeof(double), (cudaStream_t)s));
     return XK_OK;
   }
-  const int nb = xk_blocks(6LL * nn, GFE_T);
+  const int nb = xk_blocks(nn, GFE_T);  // <= (6 n_nodes + 255) / 256, the partial sums of norm_scratch
   double* part = pat->norm_scratch;
   unsigned int* count = part ? reinterpret_cast<unsigned int*>(part + nb) : nullptr;
   const int2* nelem = reinterpret_cast<const int2*>(pat->node_elem);
-  if (precision == XK_FP64)
-    k_gather_force_elem<double><<<nb, GFE_T, 0, (cudaStream_t)s>>>(nn, ne, pat->node_elem_ptr, nelem,
-                                                                  (const double*)pat->elem_sums, base, scale, f_ext,
-                                                                  fixed, out, part, count, norm2);
-  else
-    k_gather_force_elem<float><<<nb, GFE_T, 0, (cudaStream_t)s>>>(nn, ne, pat->node_elem_ptr, nelem,
-                                                                 (const float*)pat->elem_sums, base, scale, f_ext,
-                                                                 fixed, out, part, count, norm2);
+  const bool vec = ((uintptr_t)base & 15) == 0 && ((uintptr_t)f_ext & 15) == 0 && ((uintptr_t)out & 15) == 0;
+  cudaStream_t st = (cudaStream_t)s;
+#define XK_GFE(TT, VV)                                                                                           \
+  k_gather_force_elem<TT, VV><<<nb, GFE_T, 0, st>>>(nn, ne, pat->node_elem_ptr, nelem, (const TT*)pat->elem_sums, \
+                                                    base, scale, f_ext, fixed, out, part, count, norm2)
+  if (precision == XK_FP64) {
+    if (vec) XK_GFE(double, true); else XK_GFE(double, false);
+  } else {
+    if (vec) XK_GFE(float, true); else XK_GFE(float, false);
+  }
+#undef XK_GFE
   XK_CHECK_LAUNCH();
   return XK_OK;
 }

@@ -515,7 +515,9 @@ XK_D df df_mulf(df a, float b) {
   return fast_two_sum(p, fmaf(a.l, b, e));
 }
 
-// VEC: u and u_ref are 16-byte aligned and read as double2 (48 bytes per node).
+// One thread per node.  The double arithmetic here (X + u, its split, the conversions) runs
+// on the FP64 pipe, a small fraction of the FP32 rate on this GPU, so each value is converted
+// once.  VEC: u and u_ref are 16-byte aligned and read as double2 (48 bytes per node).
 template <bool VEC>
 __global__ void k_nodes_prepare(xk_mesh m, const double* __restrict__ u, const double* __restrict__ u_ref,
                                 float* __restrict__ n32) {
@@ -764,6 +766,12 @@ XK_D void store3f(float* base, long long stride, long long i, const float* v) {
   base[2 * stride + i] = v[2];
 }
 
+// A deferral list: [count, done, slots...].  The pair kernel appends to it; its deferred kernel
+// reads the count, works through the slots grid-stride, and its last CTA to finish (found with
+// the `done` counter after every CTA has read the count) sets both words back to zero for the
+// next launch, so the list needs no reset of its own.
+constexpr int DEFER_SLOTS = 2;
+
 // Other-pair narrowphase of slot j.  DEFER: near-parallel pairs are appended to q.defer instead
 // (any order: each is then computed on its own by k_pair_other32_deferred).
 template <bool DEFER>
@@ -776,7 +784,7 @@ XK_D void other32(const xk_pairs32& q, const float* __restrict__ n32, int j) {
   load3f(q.normal, cq, j, n);
   load3f(q.t1, cq, j, t1);
   if (narrow32<false, DEFER>(n32, nd, {R2.x, R2.y}, s, t, gap, n, t1, t2)) {
-    q.defer[1 + atomicAdd(q.defer, 1)] = j;
+    q.defer[DEFER_SLOTS + atomicAdd(q.defer, 1)] = j;
     return;
   }
   q.s[j] = s;
@@ -793,15 +801,31 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_other32(xk_pairs32 q, const flo
   if (j < q.n) other32<DEFER>(q, n32, j);
 }
 
+XK_D bool last_cta_done(int32_t* done) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(done, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  return last;
+}
+
 // The deferred (near-parallel) other pairs, grid-stride over the list.
 __global__ void __launch_bounds__(PAIR_T) k_pair_other32_deferred(xk_pairs32 q, const float* __restrict__ n32) {
-  const int cnt = *(volatile int32_t*)q.defer;
+  int32_t* list = q.defer;
+  const int cnt = *(volatile int32_t*)list;
   for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < cnt; x += gridDim.x * blockDim.x)
-    other32<false>(q, n32, q.defer[1 + x]);
+    other32<false>(q, n32, list[DEFER_SLOTS + x]);
+  if (last_cta_done(list + 1) && threadIdx.x == 0) {
+    list[0] = 0;
+    list[1] = 0;
+  }
 }
 
 // Member slot i (record i).  DEFER: a near-parallel member is appended to the member part of
-// q.defer (after the cap + 1 words of the other pairs) and left to k_pair_member32_deferred.
+// q.defer (after the cap + 2 words of the other pairs' list) and left to k_pair_member32_deferred.
 template <bool DEFER>
 XK_D void member32(const xk_pairs32& q, const float* __restrict__ n32, const xk_contact_params& cp,
                    float* __restrict__ rec, int i) {
@@ -815,8 +839,8 @@ XK_D void member32(const xk_pairs32& q, const float* __restrict__ n32, const xk_
   load3f(q.normal, cq, i, n);
   load3f(q.t1, cq, i, t1);
   if (narrow32<true, DEFER>(n32, nd, R, s, t, gap, n, t1, t2)) {
-    int32_t* list = q.defer + (cq + 1);
-    list[1 + atomicAdd(list, 1)] = i;
+    int32_t* list = q.defer + (cq + DEFER_SLOTS);
+    list[DEFER_SLOTS + atomicAdd(list, 1)] = i;
     return;
   }
   uint8_t status = q.status[i];
@@ -937,10 +961,14 @@ __global__ void __launch_bounds__(PAIR_T, 4) k_pair_member32(xk_pairs32 q, const
 // The deferred (near-parallel) members, grid-stride over the list.
 __global__ void __launch_bounds__(PAIR_T) k_pair_member32_deferred(xk_pairs32 q, const float* __restrict__ n32,
                                                                    xk_contact_params cp, float* __restrict__ rec) {
-  const int32_t* list = q.defer + ((long long)q.cap + 1);
+  int32_t* list = q.defer + ((long long)q.cap + DEFER_SLOTS);
   const int cnt = *(volatile const int32_t*)list;
   for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < cnt; x += gridDim.x * blockDim.x)
-    member32<false>(q, n32, cp, rec, list[1 + x]);
+    member32<false>(q, n32, cp, rec, list[DEFER_SLOTS + x]);
+  if (last_cta_done(list + 1) && threadIdx.x == 0) {
+    list[0] = 0;
+    list[1] = 0;
+  }
 }
 
 __global__ void k_active_flags(xk_pairs p, int32_t* __restrict__ flag) {
@@ -1039,6 +1067,41 @@ __global__ void k_softplus_law(long long n, const double* __restrict__ g, const 
   dp[i] = xmul(-k, sig);
 }
 }  // namespace
+
+namespace {
+// _auto_select_n_gauss (geometry/_compute.py:264-291) at X + u for one pair
+__global__ void k_gauss_points(xk_mesh m, xk_pairs p, const double* __restrict__ u, int default_n,
+                               int8_t* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const int ea = p.ea[i], eb = p.eb[i];
+  const int nd[4] = {m.conn[2 * ea], m.conn[2 * ea + 1], m.conn[2 * eb], m.conn[2 * eb + 1]};
+  double x[4][3];
+  for (int k = 0; k < 4; ++k)
+    for (int c = 0; c < 3; ++c) x[k][c] = u ? xadd(m.X[3LL * nd[k] + c], u[6LL * nd[k] + c]) : m.X[3LL * nd[k] + c];
+  double dA[3], dB[3];
+  for (int c = 0; c < 3; ++c) {
+    dA[c] = xsub(x[1][c], x[0][c]);
+    dB[c] = xsub(x[3][c], x[2][c]);
+  }
+  const double lenA = xsqrt(xdot_seq(dA, dA)), lenB = xsqrt(xdot_seq(dB, dB));
+  int n = default_n;
+  if (!(lenA < 1e-30 || lenB < 1e-30)) {
+    const double c = fabs(xdiv(xdot_seq(dA, dB), xmul(lenA, lenB)));
+    n = c < 0.866 ? 2 : (c < 0.985 ? 3 : 5);
+  }
+  out[i] = (int8_t)n;
+}
+}  // namespace
+
+extern "C" xk_status xk_pair_gauss_points(const xk_mesh* m, const xk_pairs* p, const double* u, int32_t default_n,
+                                          int8_t* out, xk_stream s) {
+  if (!m || !p || (p->n > 0 && !out)) return xk_set_error(XK_ERR_ARG, "xk_pair_gauss_points: null argument");
+  if (p->n == 0) return XK_OK;
+  k_gauss_points<<<xk_blocks(p->n, 256), 256, 0, (cudaStream_t)s>>>(*m, *p, u, default_n, out);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}
 
 extern "C" xk_status xk_softplus_normal_law(int64_t n, const double* gaps, const double* lambdas, double k_pen,
                                             double delta, double* p_n, double* dp_dg, xk_stream s) {
@@ -1162,9 +1225,9 @@ extern "C" xk_status xk_nodes_prepare(const xk_mesh* m, const double* u, const d
   if (((uintptr_t)node32 & 15) != 0) return xk_set_error(XK_ERR_ARG, "xk_nodes_prepare: node32 must be 16-byte aligned");
   const bool vec = ((uintptr_t)u & 15) == 0 && ((uintptr_t)u_ref & 15) == 0;
   if (vec)
-    k_nodes_prepare<true><<<xk_blocks(m->n_nodes, 256), 256, 0, (cudaStream_t)s>>>(*m, u, u_ref, node32);
+    k_nodes_prepare<true><<<xk_blocks(m->n_nodes, 128), 128, 0, (cudaStream_t)s>>>(*m, u, u_ref, node32);
   else
-    k_nodes_prepare<false><<<xk_blocks(m->n_nodes, 256), 256, 0, (cudaStream_t)s>>>(*m, u, u_ref, node32);
+    k_nodes_prepare<false><<<xk_blocks(m->n_nodes, 128), 128, 0, (cudaStream_t)s>>>(*m, u, u_ref, node32);
   XK_CHECK_LAUNCH();
   return XK_OK;
 }
@@ -1203,7 +1266,6 @@ extern "C" xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk
   const int n_o = q->n - q->n_members;
   if ((parts & XK_PAIRS_OTHERS) && n_o > 0) {
     if (q->defer) {
-      XK_CUDA(cudaMemsetAsync(q->defer, 0, sizeof(int32_t), st));
       k_pair_other32<true><<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
       k_pair_other32_deferred<<<152, PAIR_T, 0, st>>>(*q, node32);
     } else {
@@ -1212,7 +1274,6 @@ extern "C" xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk
   }
   if ((parts & XK_PAIRS_MEMBERS) && q->n_members > 0) {
     if (q->defer) {
-      XK_CUDA(cudaMemsetAsync(q->defer + ((long long)q->cap + 1), 0, sizeof(int32_t), st));
       k_pair_member32<true><<<xk_blocks(q->n_members, PAIR_T), PAIR_T, 0, st>>>(*q, node32, *cp, rec);
       k_pair_member32_deferred<<<152, PAIR_T, 0, st>>>(*q, node32, *cp, rec);
     } else {

@@ -90,6 +90,7 @@ SIGNATURES = {
     "xk_pairs_merge": [P(Mesh), P(Pairs), vp, C.c_int64, P(Pairs), vp],
     "xk_narrowphase": [P(Mesh), P(Pairs), vp, P(ContactParams), C.c_int, vp],
     "xk_strand_generate": [vp, C.c_int32, C.c_int64, C.c_int64, vp, vp, vp, vp, vp],
+    "xk_pair_gauss_points": [P(Mesh), P(Pairs), vp, C.c_int32, vp, vp],
     "xk_contact_pattern_build": [P(Mesh), P(Pairs), P(ContactPattern), vp],
     "xk_pair_step": [P(Mesh), P(Pairs), P(ContactPattern), vp, vp, P(ContactParams), C.c_int, C.c_int, C.c_int, vp,
                      vp],

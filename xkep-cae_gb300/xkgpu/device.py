@@ -350,7 +350,7 @@ class DevicePairTable32:
         t["status"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         t["stick"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         t["mu"] = torch.zeros(cap, dtype=torch.float32, device=self.device) if self.per_slot_mu else None
-        t["defer"] = torch.zeros(2 * (cap + 1), dtype=torch.int32, device=self.device)
+        t["defer"] = torch.zeros(2 * (cap + 2), dtype=torch.int32, device=self.device)
         self.t = t
         self.cap = cap
         self.c = L.Pairs32(0, cap, 0, *(ptr(t[k]) for k in (

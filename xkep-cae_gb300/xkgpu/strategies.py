@@ -8,6 +8,9 @@ can be handed to the reference's Newton loop in place of the original:
 class                           replaces (reference file:line)
 ==============================  ====================================================================
 GpuPointToPoint                 PointToPointProcess (contact/geometry/strategy.py:311-371)
+GpuLineToLineGauss              LineToLineGaussProcess (contact/geometry/strategy.py:374-467)
+GpuMortarSegment                MortarSegmentProcess (contact/geometry/strategy.py:470-535)
+create_contact_geometry_strategy  _create_contact_geometry_strategy (contact/geometry/strategy.py:541-579)
 GpuHuberContactForce            HuberContactForceProcess (contact/contact_force/strategy.py:70-254)
 GpuCoulombReturnMapping         CoulombReturnMappingProcess (contact/friction/strategy.py:48-170)
 GpuDetectCandidatesProcess      DetectCandidatesProcess (contact/_manager_process.py:157-291)
@@ -328,6 +331,70 @@ class GpuPointToPoint:
             return sp.csr_matrix((0, ndof_total)), []
         batch = PairBatch(pairs, _n_nodes(ndof_total), device=self._device)
         return _jacobian(batch, ndof_total)
+
+
+def pair_gauss_points(pairs: list, node_coords, *, default: int = 3, device=None) -> np.ndarray:
+    """Gauss-point count of every pair at ``node_coords`` (``_auto_select_n_gauss``,
+    ``contact/geometry/_compute.py:264-291``), computed on the GPU."""
+    if not pairs:
+        return np.zeros(0, dtype=np.int64)
+    coords = np.asarray(node_coords, dtype=float).reshape(-1, 3)
+    batch = PairBatch(pairs, coords.shape[0], coords=coords, device=device)
+    out = torch.empty(batch.n, dtype=torch.int8, device=batch.device)
+    L.call("xk_pair_gauss_points", C.byref(batch.mesh.c), C.byref(batch.table.c), None, int(default), ptr(out),
+           stream_handle())
+    return out.cpu().numpy().astype(np.int64)
+
+
+class GpuLineToLineGauss(GpuPointToPoint):
+    """``LineToLineGaussProcess`` (``contact/geometry/strategy.py:374-467``) on the GPU.
+
+    The reference evaluates this strategy's geometry exactly as the
+    point-to-point one (``_batch_update_geometry``) and, with ``auto_gauss``,
+    then stores the angle-based Gauss-point count in each pair that has an
+    ``_n_gauss`` attribute (``strategy.py:436-451``); the constraint Jacobian is
+    the point-to-point one.  So is this class's.
+    """
+
+    def __init__(self, *, n_gauss: int = 2, exclude_same_layer: bool = True, auto_gauss: bool = False,
+                 device=None) -> None:
+        super().__init__(exclude_same_layer=exclude_same_layer, device=device)
+        self._n_gauss = n_gauss
+        self._auto_gauss = auto_gauss
+
+    def update_geometry(self, pairs: list, node_coords, *, config=None) -> None:
+        super().update_geometry(pairs, node_coords, config=config)
+        if self._auto_gauss and len(pairs) > 0:
+            n_gp = pair_gauss_points(pairs, node_coords, device=self._device)
+            for pair, n in zip(pairs, n_gp):
+                if hasattr(pair, "_n_gauss"):
+                    pair._n_gauss = int(n)
+
+
+class GpuMortarSegment(GpuPointToPoint):
+    """``MortarSegmentProcess`` (``contact/geometry/strategy.py:470-535``) on the GPU: the
+    point-to-point geometry and Jacobian, as in the reference."""
+
+    def __init__(self, *, n_gauss: int = 2, exclude_same_layer: bool = True, device=None) -> None:
+        super().__init__(exclude_same_layer=exclude_same_layer, device=device)
+        self._n_gauss = n_gauss
+
+
+def create_contact_geometry_strategy(*, mode: str = "point_to_point", exclude_same_layer: bool = True,
+                                     n_gauss: int = 2, auto_gauss: bool = False, line_contact: bool = False,
+                                     use_mortar: bool = False, device=None):
+    """``_create_contact_geometry_strategy`` (``contact/geometry/strategy.py:541-579``): the same
+    mode selection (``use_mortar`` over ``line_contact`` over ``mode``) with the GPU classes."""
+    if use_mortar:
+        mode = "mortar"
+    elif line_contact:
+        mode = "line_to_line"
+    if mode == "mortar":
+        return GpuMortarSegment(n_gauss=n_gauss, exclude_same_layer=exclude_same_layer, device=device)
+    if mode == "line_to_line":
+        return GpuLineToLineGauss(n_gauss=n_gauss, exclude_same_layer=exclude_same_layer, auto_gauss=auto_gauss,
+                                  device=device)
+    return GpuPointToPoint(exclude_same_layer=exclude_same_layer, device=device)
 
 
 def _jacobian(batch: PairBatch, ndof: int):
