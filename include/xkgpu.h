@@ -383,6 +383,50 @@ xk_status xk_constraint_jacobian(const xk_mesh* m, const xk_pairs* p, int32_t* r
                                  double* vals, int32_t* pair_index, int64_t cap, int64_t* n_rows,
                                  xk_stream s);
 
+/* ------------------------------------------------- coated-wire contact
+ * KelvinVoigtCoatingProcess (contact/coating/strategy.py:80-400): a coating of
+ * stiffness k and damping c between the wire cores, with Coulomb friction on
+ * the coating surface.  Pair state of the coating, per pair of the table. */
+typedef struct {
+  double* cc;            /* [cap] coating_compression */
+  double* cc_prev;       /* [cap] coating_compression_prev (the end of the previous step) */
+  double* z_t;           /* [2*cap] coating_z_t, two planes */
+  uint8_t* stick;        /* [cap] coating_stick */
+  double* q_trial_norm;  /* [cap] coating_q_trial_norm */
+  double* dissipation;   /* [cap] coating_dissipation */
+} xk_coating_state;
+
+typedef struct {
+  double stiffness;  /* coating_stiffness k */
+  double damping;    /* coating_damping c */
+  double mu;         /* coating_mu */
+  double k_t_ratio;  /* coating_k_t_ratio: tangential penalty k * ratio */
+  double dt;         /* the step's pseudo-time increment (viscous term when c > 0 and dt > 0) */
+} xk_coating_params;
+
+/* The coating branch of UpdateGeometryProcess (_manager_process.py:351-360,
+ * 386-396), after xk_narrowphase(update_active = 0) on a mesh whose radii are
+ * the core radii (gap = dist - (core_a + core_b)): cc = max(0, coat_total -
+ * gap) with coat_total[i] = (r_a - core_a) + (r_b - core_b); with
+ * update_active, the active-set hysteresis with the coating term
+ * (_update_active_set_state, :475-494: a compressed coating activates and
+ * keeps a pair active). */
+xk_status xk_coating_geometry(xk_pairs* p, const double* coat_total, const xk_contact_params* cp, int update_active,
+                              double* cc, xk_stream s);
+
+#define XK_COAT_FORCE 1            /* forces (strategy.py:97-143): v_n = -(k cc + c dcc/dt) n */
+#define XK_COAT_TANGENT 2          /* stiffness (:145-196): B_n = (k + c / dt) n n^T where cc > 1e-15 */
+#define XK_COAT_FRICTION 4         /* friction_forces (:198-288): return mapping, state update, v_f = -(q0 t1 + q1 t2) */
+#define XK_COAT_FRICTION_TANGENT 8 /* friction_stiffness (:290-370): B_f = T D T^T from the coating friction state */
+/* The selected coating stages over the members of pat (whose pair table
+ * holds the geometry), as split records rec[member * 32 + value] (double):
+ * s, t, v_n, v_f, B_n, B_f; gathered with xk_contact_gather_force /
+ * xk_contact_gather_tangent, which = normal (elastic and viscous coating) or
+ * friction.  u, u_ref (nullable): node-major displacements for the friction
+ * slip. */
+xk_status xk_coating_step(const xk_pairs* p, const xk_contact_pattern* pat, xk_coating_state* cs, const double* u,
+                          const double* u_ref, const xk_coating_params* cp, int stages, double* rec, xk_stream s);
+
 /* Gauss-point count of every pair for the line-to-line and mortar geometry
  * strategies with auto_gauss (_auto_select_n_gauss,
  * xkep_cae/contact/geometry/_compute.py:264-291, called from

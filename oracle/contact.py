@@ -13,6 +13,8 @@ reference's contact hot path:
   ``friction/_assembly.py:53-342``, ``friction/law_friction.py:89-153``
 * ``_build_constraint_jacobian_ptp`` ``xkep_cae/contact/geometry/strategy.py:83-132``
 * ``_auto_select_n_gauss``          ``xkep_cae/contact/geometry/_compute.py:264-291``
+* ``KelvinVoigtCoatingProcess``     ``xkep_cae/contact/coating/strategy.py:80-376`` and the
+  coating branch of ``UpdateGeometryProcess`` (``_manager_process.py:351-360,386-396,475-494``)
 
 Where the reference's candidate and active sets hinge on floating-point
 compares, this oracle reproduces its arithmetic operation for operation:
@@ -533,3 +535,120 @@ def auto_n_gauss(dA, dB, default: int = 3) -> np.ndarray:
         c = abs(float(dA[i] @ dB[i] / (len_a * len_b)))
         out[i] = 2 if c < 0.866 else (3 if c < 0.985 else 5)
     return out
+
+
+# --------------------------------------------------------------------------- coating
+
+
+def coating_geometry(table: dict, coords, *, freeze_active_set=False, g_on=0.0, g_off=1e-6,
+                     allow_deactivation=True):
+    """Geometry with a coating (``_manager_process.py:351-360,386-396,475-494``).
+
+    The gap is taken between the cores, ``dist - (core_a + core_b)``; the
+    coating compression is ``max(0, coat_total - gap)`` with ``coat_total =
+    (r_a - core_a) + (r_b - core_b)``; a compressed coating activates a pair
+    and keeps it active.  Returns the updated table and the compressions.
+    """
+    t = copy_table(table)
+    if t["ea"].shape[0] == 0:
+        return t, np.zeros(0)
+    nd = t["nodes"]
+    s, tt, dist, normal, _ = closest_point(coords[nd[:, 0]], coords[nd[:, 1]], coords[nd[:, 2]], coords[nd[:, 3]])
+    gap = dist - (t["cra"] + t["crb"])
+    coat_total = (t["ra"] - t["cra"]) + (t["rb"] - t["crb"])
+    cc = np.maximum(0.0, coat_total - gap)
+    n, t1, t2 = contact_frame(normal, t["t1"], t["normal"])
+    t.update(s=s, t=tt, gap=gap, normal=n, t1=t1, t2=t2)
+    if not freeze_active_set:
+        st = t["status"]
+        coat = cc > 0.0
+        on = (st == INACTIVE) & ((gap <= g_on) | coat)
+        off = (st != INACTIVE) & allow_deactivation & (gap >= g_off) & ~coat
+        st[on] = ACTIVE
+        st[off] = INACTIVE
+    return t, cc
+
+
+def _assemble_nodal(table, use, v, ndof):
+    f = np.zeros(ndof)
+    if use.any():
+        c = shape_coeffs(table["s"][use], table["t"][use])
+        np.add.at(f, trans_dofs(table["nodes"][use]).ravel(), (c[:, :, None] * v[use][:, None, :]).ravel())
+    return f
+
+
+def coating_forces(table: dict, cc, cc_prev, ndof: int, k: float, c: float, dt: float):
+    """Elastic + viscous coating force (``coating/strategy.py:97-143``): f_n = k cc + c (cc - cc_prev) / dt
+    (the dashpot when c > 0 and dt > 0), on node k of a pair c_k (-f_n n)."""
+    f_n = k * cc
+    if c > 0.0 and dt > 0.0:
+        f_n = f_n + c * ((cc - cc_prev) / dt)
+    use = ~((cc <= 0.0) & (cc_prev <= 0.0)) & ~(np.abs(f_n) < 1e-30)
+    return _assemble_nodal(table, use, -f_n[:, None] * table["normal"], ndof)
+
+
+def coating_stiffness(table: dict, cc, ndof: int, k: float, c: float, dt: float):
+    """Coating stiffness (``coating/strategy.py:145-196``): blocks c_k c_l (k + c/dt) n n^T where cc > 1e-15."""
+    k_eff = k + c / dt if (c > 0.0 and dt > 0.0) else k
+    use = cc > 1e-15
+    if not use.any():
+        return sp.csr_matrix((ndof, ndof))
+    n = table["normal"][use]
+    B = k_eff * n[:, :, None] * n[:, None, :]
+    co = shape_coeffs(table["s"][use], table["t"][use])
+    blocks = (co[:, :, None] * co[:, None, :])[:, :, :, None, None] * B[:, None, None, :, :]
+    return _blocks_to_csr(table["nodes"][use], blocks, ndof)
+
+
+def coating_friction(table: dict, cc, state: dict, u, u_ref, ndof: int, k: float, kt_ratio: float, mu: float):
+    """Coating friction (``coating/strategy.py:198-288``): return mapping on the coating surface with
+    p_n = k cc and k_t = k kt_ratio; the history of uncompressed pairs is reset.  Returns the force and
+    the new state (z_t, stick, q_trial_norm, dissipation)."""
+    P = table["ea"].shape[0]
+    new = {key: np.array(v, copy=True) for key, v in state.items()}
+    if mu <= 0.0:
+        return np.zeros(ndof), new
+    k_t = k * kt_ratio
+    du = (u - u_ref).reshape(-1, 6)[:, 0:3]
+    s, tt, nd = table["s"][:, None], table["t"][:, None], table["nodes"]
+    du_rel = ((1.0 - tt) * du[nd[:, 2]] + tt * du[nd[:, 3]]) - ((1.0 - s) * du[nd[:, 0]] + s * du[nd[:, 1]])
+    dut = np.stack([np.sum(du_rel * table["t1"], axis=1), np.sum(du_rel * table["t2"], axis=1)], axis=1)
+    comp = cc > 0.0
+    p_n = k * cc
+    q_tr = state["z_t"] + k_t * dut
+    qn = np.sqrt(q_tr[:, 0] ** 2 + q_tr[:, 1] ** 2)
+    fy = mu * p_n
+    stick = qn <= fy
+    with np.errstate(invalid="ignore", divide="ignore"):
+        q = np.where(stick[:, None], q_tr, fy[:, None] * q_tr / np.where(qn > 0, qn, 1.0)[:, None])
+    diss = q[:, 0] * dut[:, 0] + q[:, 1] * dut[:, 1]
+    new["z_t"] = np.where(comp[:, None], q, 0.0)
+    new["stick"] = np.where(comp, stick, True)
+    new["q_trial_norm"] = np.where(comp, qn, 0.0)
+    new["dissipation"] = np.where(comp, diss, 0.0)
+    v = -(new["z_t"][:, 0:1] * table["t1"] + new["z_t"][:, 1:2] * table["t2"])
+    return _assemble_nodal(table, comp, v, ndof), new
+
+
+def coating_friction_stiffness(table: dict, cc, state: dict, ndof: int, k: float, kt_ratio: float, mu: float):
+    """Coating friction stiffness (``coating/strategy.py:290-370``): blocks c_k c_l T D T^T, D from
+    ``_tangent_2x2_core`` (``friction/law_friction.py:126-153``) on the coating friction state."""
+    use = (cc > 0.0) & (mu > 0.0)
+    if not use.any():
+        return sp.csr_matrix((ndof, ndof))
+    k_t = k * kt_ratio
+    p_n = k * cc[use]
+    z = state["z_t"][use]
+    qtn = state["q_trial_norm"][use]
+    zn = np.sqrt(z[:, 0] ** 2 + z[:, 1] ** 2)
+    slip = ~state["stick"][use] & (zn >= 1e-30) & (qtn >= 1e-30)
+    D = np.broadcast_to(k_t * np.eye(2), (z.shape[0], 2, 2)).copy()
+    if slip.any():
+        h = z[slip] / zn[slip, None]
+        ratio = mu * p_n[slip] / qtn[slip]
+        D[slip] = (ratio * k_t)[:, None, None] * (np.eye(2)[None] - h[:, :, None] * h[:, None, :])
+    tv = np.stack([table["t1"][use], table["t2"][use]], axis=1)
+    B = np.einsum("pab,pai,pbj->pij", D, tv, tv)
+    co = shape_coeffs(table["s"][use], table["t"][use])
+    blocks = (co[:, :, None] * co[:, None, :])[:, :, :, None, None] * B[:, None, None, :, :]
+    return _blocks_to_csr(table["nodes"][use], blocks, ndof)

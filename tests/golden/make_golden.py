@@ -283,6 +283,84 @@ def genalpha_case(R, name, seed=4, n=600):
     print(name)
 
 
+def _coating_arrays(pairs):
+    order = sorted(range(len(pairs)), key=lambda i: (pairs[i].elem_a, pairs[i].elem_b))
+    st = [pairs[i].state for i in order]
+    return {
+        "cc": np.array([x.coating_compression for x in st]),
+        "cc_prev": np.array([x.coating_compression_prev for x in st]),
+        "coat_z_t": np.array([x.coating_z_t for x in st]).reshape(-1, 2),
+        "coat_stick": np.array([x.coating_stick for x in st], dtype=bool),
+        "coat_qtn": np.array([x.coating_q_trial_norm for x in st]),
+        "coat_diss": np.array([x.coating_dissipation for x in st]),
+        "core_a": np.array([pairs[i].core_radius_a for i in order]),
+        "core_b": np.array([pairs[i].core_radius_b for i in order]),
+    }
+
+
+def coating_case(R, name, *, n_wires=7, d=2.0, pitch=40.0, n_el=16, gap_frac=-0.005, core_frac=0.9, seed=21,
+                 k_coat=1e4, c_coat=50.0, mu_coat=0.2, kt_ratio=0.5, dt=0.1, n_iter=2, step_frac=5e-3):
+    """Kelvin-Voigt coating: detection with core radii, the coating geometry (active set and frozen),
+    then per iteration forces, stiffness, friction forces (state update) and friction stiffness."""
+    import xkep_cae.contact.coating.strategy as cs
+
+    mesh = R["tw"]._make_twisted_wire_mesh(n_wires, d, pitch, 0.0, n_el, n_pitches=1, gap=gap_frac * d)
+    X = mesh.node_coords.copy()
+    conn = mesh.connectivity.astype(np.int64)
+    layer = np.array([mesh.strand_infos[e // n_el].layer for e in range(len(conn))], dtype=np.int32)
+    ndof = 6 * len(X)
+    r = d / 2.0
+    rng = np.random.default_rng(seed)
+    u = np.zeros(ndof)
+    u.reshape(-1, 6)[:, 0:3] = rng.normal(0.0, 1e-3 * d, (len(X), 3))
+    cfg = R["cp"]._ContactConfigInput(exclude_same_layer=True,
+                                      elem_layer_map={int(e): int(layer[e]) for e in range(len(conn))},
+                                      coating_stiffness=k_coat, coating_damping=c_coat, coating_mu=mu_coat,
+                                      coating_k_t_ratio=kt_ratio)
+    mgr = R["cp"]._ContactManagerInput(config=cfg)
+    out = dict(X=X, conn=conn, elem_layer=layer, radius=np.array(r), core_radius=np.array(core_frac * r),
+               k_coat=np.array(k_coat), c_coat=np.array(c_coat), mu_coat=np.array(mu_coat),
+               kt_ratio=np.array(kt_ratio), dt=np.array(dt), n_iter=np.array(n_iter), u0=u.copy())
+    cdef = X + u.reshape(-1, 6)[:, 0:3]
+    det = R["mp"].DetectCandidatesProcess().process(
+        R["mp"].DetectCandidatesInput(manager=mgr, node_coords=cdef, connectivity=conn, radii=r,
+                                      core_radii=core_frac * r))
+    mgr = det.manager
+    for k, v in _pairs_to_arrays(mgr.pairs).items():
+        out["detect_" + k] = v
+    ug = R["mp"].UpdateGeometryProcess().process(R["mp"].UpdateGeometryInput(manager=mgr, node_coords=cdef))
+    mgr = ug.manager
+    for k, v in {**_pairs_to_arrays(mgr.pairs), **_coating_arrays(mgr.pairs)}.items():
+        out["geom_" + k] = v
+    # a previous-step compression for the dashpot term (process.py:539-545 sets it at step ends)
+    mgr.pairs[:] = [R["cp"]._evolve_pair(p, state=R["cp"]._evolve_state(
+        p.state, coating_compression_prev=0.8 * p.state.coating_compression)) for p in mgr.pairs]
+    kv = cs.KelvinVoigtCoatingProcess()
+    u_ref = u.copy()
+    step_rng = np.random.default_rng(seed + 1)
+    for it in range(n_iter):
+        u = u.copy()
+        u.reshape(-1, 6)[:, 0:3] += step_rng.normal(0.0, step_frac * d, (len(X), 3))
+        cdef = X + u.reshape(-1, 6)[:, 0:3]
+        ugf = R["mp"].UpdateGeometryProcess().process(
+            R["mp"].UpdateGeometryInput(manager=mgr, node_coords=cdef, freeze_active_set=True))
+        mgr.pairs[:] = ugf.manager.pairs
+        p = f"it{it}_"
+        out[p + "u"] = u.copy()
+        for k, v in {**_pairs_to_arrays(mgr.pairs), **_coating_arrays(mgr.pairs)}.items():
+            out[p + "pre_" + k] = v
+        out[p + "f_coat"] = kv.forces(mgr.pairs, cdef, cfg, dt)
+        _csr(p + "K_coat", kv.stiffness(mgr.pairs, cdef, cfg, ndof, dt), out)
+        out[p + "f_coat_fric"] = kv.friction_forces(mgr.pairs, cdef, cfg, u, u_ref)
+        _csr(p + "K_coat_fric", kv.friction_stiffness(mgr.pairs, cdef, cfg, ndof), out)
+        for k, v in _coating_arrays(mgr.pairs).items():
+            out[p + "post_" + k] = v
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    cc = out["geom_cc"]
+    print(name, "pairs", len(mgr.pairs), "compressed", int(np.sum(cc > 0)),
+          "slip", int(np.sum(~out[f"it{n_iter - 1}_post_coat_stick"])))
+
+
 def gauss_case(R, name, seed=11, n=1200):
     """Gauss-point counts of segment pairs at every angle (line-to-line / mortar auto_gauss)."""
     rng = np.random.default_rng(seed)
@@ -317,6 +395,7 @@ CASES = {
     "laws": lambda R: laws_case(R, "laws"),
     "genalpha": lambda R: genalpha_case(R, "genalpha"),
     "gauss_points": lambda R: gauss_case(R, "gauss_points"),
+    "coating7": lambda R: coating_case(R, "coating7"),
 }
 
 

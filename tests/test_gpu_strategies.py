@@ -223,3 +223,66 @@ def test_line_to_line_gauss_points_and_geometry():
             assert getattr(a.state, k) == getattr(b.state, k) == getattr(c.state, k)
         assert np.array_equal(a.state.normal, b.state.normal) and np.array_equal(a.state.tangent1, c.state.tangent1)
     assert np.array_equal(np.array([p._n_gauss for p in l2l]), z["n_gauss"])
+
+
+def test_coating_strategy_replays_reference():
+    """GpuKelvinVoigtCoating and the coated geometry update driven as the reference's solver drives
+    KelvinVoigtCoatingProcess, against its recorded outputs (tests/golden/coating7.npz)."""
+    import dataclasses
+
+    z = golden("coating7")
+    X, conn, layer = z["X"], z["conn"], z["elem_layer"]
+    ndof = 6 * len(X)
+    r, cr = float(z["radius"]), float(z["core_radius"])
+    k, c, mu, ktr, dt = (float(z[q]) for q in ("k_coat", "c_coat", "mu_coat", "kt_ratio", "dt"))
+    cfg = S.ContactConfig(exclude_same_layer=True, elem_layer_map={int(e): int(layer[e]) for e in range(len(conn))},
+                          coating_stiffness=k, coating_damping=c, coating_mu=mu, coating_k_t_ratio=ktr)
+    mgr = S.ContactManager(config=cfg)
+    cdef = X + z["u0"].reshape(-1, 6)[:, 0:3]
+    det = S.GpuDetectCandidatesProcess().process(
+        S.DetectCandidatesInput(manager=mgr, node_coords=cdef, connectivity=conn, radii=r, core_radii=cr))
+    mgr = det.manager
+    mgr = S.GpuUpdateGeometryProcess().process(S.UpdateGeometryInput(manager=mgr, node_coords=cdef)).manager
+    _check_geometry(mgr.pairs, z, "geom_")
+    pairs = [S._evolve(p, coating_compression_prev=0.8 * p.state.coating_compression) for p in mgr.pairs]
+    mgr = dataclasses.replace(mgr, pairs=pairs)
+    kv = S.create_coating_strategy(coating_stiffness=k)
+    assert isinstance(kv, S.GpuKelvinVoigtCoating)
+    u_ref = z["u0"]
+    for it in range(int(z["n_iter"])):
+        p = f"it{it}_"
+        u = z[p + "u"]
+        cdef = X + u.reshape(-1, 6)[:, 0:3]
+        mgr = S.GpuUpdateGeometryProcess().process(
+            S.UpdateGeometryInput(manager=mgr, node_coords=cdef, freeze_active_set=True)).manager
+        _check_geometry(mgr.pairs, z, p + "pre_")
+        pl = list(mgr.pairs)
+        assert rel_err(kv.forces(pl, cdef, cfg, dt), z[p + "f_coat"]) < TOL
+        assert sparse_rel_err(kv.stiffness(pl, cdef, cfg, ndof, dt), golden_csr(z, p + "K_coat", ndof)) < TOL
+        assert rel_err(kv.friction_forces(pl, cdef, cfg, u, u_ref), z[p + "f_coat_fric"]) < TOL
+        co = _coating(pl)
+        assert np.array_equal(co["stick"], z[p + "post_coat_stick"])
+        for q, g in (("z_t", "coat_z_t"), ("qtn", "coat_qtn"), ("diss", "coat_diss")):
+            assert rel_err(co[q], z[p + "post_" + g]) < TOL, q
+        K = kv.friction_stiffness(pl, cdef, cfg, ndof)
+        assert sparse_rel_err(K, golden_csr(z, p + "K_coat_fric", ndof)) < TOL
+        mgr = dataclasses.replace(mgr, pairs=pl)
+    none = S.create_coating_strategy(coating_stiffness=0.0)
+    assert not np.any(none.forces(pl, cdef, cfg, dt)) and none.stiffness(pl, cdef, cfg, ndof, dt).nnz == 0
+
+
+def _coating(pairs):
+    order = sorted(range(len(pairs)), key=lambda i: (pairs[i].elem_a, pairs[i].elem_b))
+    st = [pairs[i].state for i in order]
+    return {"cc": np.array([x.coating_compression for x in st]),
+            "z_t": np.array([x.coating_z_t for x in st]).reshape(-1, 2),
+            "stick": np.array([x.coating_stick for x in st], bool),
+            "qtn": np.array([x.coating_q_trial_norm for x in st]),
+            "diss": np.array([x.coating_dissipation for x in st])}
+
+
+def _check_geometry(pairs, z, prefix):
+    a = _arrays(pairs)
+    for q in ("ea", "eb", "s", "t", "gap", "normal", "t1", "t2", "status"):
+        assert np.array_equal(a[q], z[prefix + q]), prefix + q
+    assert np.array_equal(_coating(pairs)["cc"], z[prefix + "cc"])

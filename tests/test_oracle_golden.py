@@ -136,3 +136,44 @@ def test_gauss_point_counts_match_reference():
     ng = oc.auto_n_gauss(z["xA1"] - z["xA0"], z["xB1"] - z["xB0"])
     assert np.array_equal(ng, z["n_gauss"])
     assert set(np.unique(ng)) == {2, 3, 5}
+
+
+def test_coating_oracle_matches_reference():
+    """Coated wires (Kelvin-Voigt coating with friction): the oracle's coating geometry, forces and
+    tangents against KelvinVoigtCoatingProcess's own outputs over two iterations (stick, slip and
+    uncompressed pairs whose coating friction history is reset)."""
+    z = golden("coating7")
+    X, conn, layer = z["X"], z["conn"], z["elem_layer"]
+    n = 6 * len(X)
+    r, cr = float(z["radius"]), float(z["core_radius"])
+    k, c, mu, ktr, dt = (float(z[q]) for q in ("k_coat", "c_coat", "mu_coat", "kt_ratio", "dt"))
+    cd = oc.deformed_coords(X, z["u0"])
+    table, _, _ = oc.detect(oc.empty_table(), cd, conn, np.full(len(conn), r), elem_layer=layer,
+                            exclude_same_layer=True, core_radii=np.full(len(conn), cr))
+    for q in ("ea", "eb", "status"):
+        assert np.array_equal(table[q], z["detect_" + q])
+    table, cc = oc.coating_geometry(table, cd)
+    for q in ("s", "t", "gap", "normal", "t1", "status"):
+        assert np.array_equal(table[q], z["geom_" + q]), q
+    assert np.array_equal(cc, z["geom_cc"])
+    cc_prev = 0.8 * cc
+    state = {"z_t": np.zeros((len(cc), 2)), "stick": np.ones(len(cc), bool), "q_trial_norm": np.zeros(len(cc)),
+             "dissipation": np.zeros(len(cc))}
+    u_ref = z["u0"]
+    for it in range(int(z["n_iter"])):
+        p = f"it{it}_"
+        cd = oc.deformed_coords(X, z[p + "u"])
+        table, cc = oc.coating_geometry(table, cd, freeze_active_set=True)
+        for q in ("s", "t", "gap", "normal", "t1", "t2", "status"):
+            assert np.array_equal(table[q], z[p + "pre_" + q]), q
+        assert np.array_equal(cc, z[p + "pre_cc"])
+        assert rel_err(oc.coating_forces(table, cc, cc_prev, n, k, c, dt), z[p + "f_coat"]) < 1e-12
+        assert sparse_rel_err(oc.coating_stiffness(table, cc, n, k, c, dt), golden_csr(z, p + "K_coat", n)) < 1e-12
+        f, state = oc.coating_friction(table, cc, state, z[p + "u"], u_ref, n, k, ktr, mu)
+        assert rel_err(f, z[p + "f_coat_fric"]) < 1e-12
+        assert np.array_equal(state["stick"], z[p + "post_coat_stick"])
+        assert rel_err(state["z_t"], z[p + "post_coat_z_t"]) < 1e-12
+        assert rel_err(state["q_trial_norm"], z[p + "post_coat_qtn"]) < 1e-12
+        assert rel_err(state["dissipation"], z[p + "post_coat_diss"]) < 1e-10
+        K = oc.coating_friction_stiffness(table, cc, state, n, k, ktr, mu)
+        assert sparse_rel_err(K, golden_csr(z, p + "K_coat_fric", n)) < 1e-12

@@ -21,6 +21,7 @@ XK_OUT_COMBINED, XK_OUT_SPLIT = 0, 1
 XK_WHICH_COMBINED, XK_WHICH_NORMAL, XK_WHICH_FRICTION = 0, 1, 2
 REC_STRIDE = {XK_OUT_COMBINED: 16, XK_OUT_SPLIT: 32}
 XK_GATHER_DEFAULT, XK_GATHER_LANES, XK_GATHER_CHUNKS, XK_GATHER_SIDES = 0, 1, 2, 3
+XK_COAT_FORCE, XK_COAT_TANGENT, XK_COAT_FRICTION, XK_COAT_FRICTION_TANGENT = 1, 2, 4, 8
 
 vp = C.c_void_p
 
@@ -33,6 +34,14 @@ class StrandSpec(C.Structure):
     _fields_ = [("n_wires", C.c_int32), ("n_elems_per_wire", C.c_int32), ("lay_direction", C.c_int32),
                 ("pad", C.c_int32), ("wire_diameter", C.c_double), ("pitch", C.c_double), ("length", C.c_double),
                 ("gap", C.c_double), ("x_offset", C.c_double), ("node_first", C.c_int64), ("elem_first", C.c_int64)]
+
+
+class CoatingState(C.Structure):
+    _fields_ = [(n, vp) for n in ("cc", "cc_prev", "z_t", "stick", "q_trial_norm", "dissipation")]
+
+
+class CoatingParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("stiffness", "damping", "mu", "k_t_ratio", "dt")]
 
 
 class Mesh(C.Structure):
@@ -91,6 +100,8 @@ SIGNATURES = {
     "xk_narrowphase": [P(Mesh), P(Pairs), vp, P(ContactParams), C.c_int, vp],
     "xk_strand_generate": [vp, C.c_int32, C.c_int64, C.c_int64, vp, vp, vp, vp, vp],
     "xk_pair_gauss_points": [P(Mesh), P(Pairs), vp, C.c_int32, vp, vp],
+    "xk_coating_geometry": [P(Pairs), vp, P(ContactParams), C.c_int, vp, vp],
+    "xk_coating_step": [P(Pairs), P(ContactPattern), P(CoatingState), vp, vp, P(CoatingParams), C.c_int, vp, vp],
     "xk_contact_pattern_build": [P(Mesh), P(Pairs), P(ContactPattern), vp],
     "xk_pair_step": [P(Mesh), P(Pairs), P(ContactPattern), vp, vp, P(ContactParams), C.c_int, C.c_int, C.c_int, vp,
                      vp],

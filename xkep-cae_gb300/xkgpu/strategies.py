@@ -11,6 +11,9 @@ GpuPointToPoint                 PointToPointProcess (contact/geometry/strategy.p
 GpuLineToLineGauss              LineToLineGaussProcess (contact/geometry/strategy.py:374-467)
 GpuMortarSegment                MortarSegmentProcess (contact/geometry/strategy.py:470-535)
 create_contact_geometry_strategy  _create_contact_geometry_strategy (contact/geometry/strategy.py:541-579)
+GpuKelvinVoigtCoating           KelvinVoigtCoatingProcess (contact/coating/strategy.py:80-376)
+GpuNoCoating                    NoCoatingProcess (contact/coating/strategy.py:19-77)
+create_coating_strategy         _create_coating_strategy (contact/coating/strategy.py:379-400)
 GpuHuberContactForce            HuberContactForceProcess (contact/contact_force/strategy.py:70-254)
 GpuCoulombReturnMapping         CoulombReturnMappingProcess (contact/friction/strategy.py:48-170)
 GpuDetectCandidatesProcess      DetectCandidatesProcess (contact/_manager_process.py:157-291)
@@ -141,6 +144,13 @@ def pack_pairs(pairs) -> dict:
     d["eb"] = np.array([int(p.elem_b) for p in pairs], np.int64)
     d["ra"] = np.array([float(p.radius_a) for p in pairs], np.float64)
     d["rb"] = np.array([float(p.radius_b) for p in pairs], np.float64)
+    d["ca"] = np.array([float(getattr(p, "core_radius_a", 0.0)) for p in pairs], np.float64)
+    d["cb"] = np.array([float(getattr(p, "core_radius_b", 0.0)) for p in pairs], np.float64)
+    for k in ("coating_compression", "coating_compression_prev", "coating_q_trial_norm", "coating_dissipation"):
+        d[k] = np.array([float(getattr(x, k, 0.0)) for x in st], np.float64)
+    d["coating_z_t"] = np.array([np.asarray(getattr(x, "coating_z_t", np.zeros(2)), np.float64).reshape(2)
+                                 for x in st]).reshape(n, 2)
+    d["coating_stick"] = np.array([bool(getattr(x, "coating_stick", True)) for x in st], bool)
     for k in ("s", "t", "gap", "lambda_n", "k_pen", "k_t", "p_n", "q_trial_norm", "dissipation"):
         d[k] = np.array([float(getattr(x, k)) for x in st], np.float64)
     for k, src, w in (("normal", "normal", 3), ("t1", "tangent1", 3), ("t2", "tangent2", 3), ("z_t", "z_t", 2)):
@@ -159,7 +169,10 @@ class PairBatch:
     state is read).
     """
 
-    def __init__(self, pairs, n_nodes: int, *, coords=None, device=None):
+    def __init__(self, pairs, n_nodes: int, *, coords=None, device=None, core: bool = False,
+                 all_members: bool = False):
+        """``core``: the synthetic elements carry the pairs' core radii (the coating geometry);
+        ``all_members``: every pair is a member of the contact pattern (the coating forces)."""
         self.host = pairs if isinstance(pairs, dict) else pack_pairs(pairs)
         h = self.host
         n = int(h["ea"].shape[0])
@@ -169,7 +182,7 @@ class PairBatch:
         conn = np.empty((2 * n, 2), np.int64)
         conn[0::2], conn[1::2] = nodes[:, 0:2], nodes[:, 2:4]
         radii = np.empty(2 * n, np.float64)
-        radii[0::2], radii[1::2] = h["ra"], h["rb"]
+        radii[0::2], radii[1::2] = (h["ca"], h["cb"]) if core else (h["ra"], h["rb"])
         X = np.zeros((n_nodes, 3)) if coords is None else np.asarray(coords, np.float64).reshape(-1, 3)
         if X.shape[0] < n_nodes:
             X = np.concatenate([X, np.zeros((n_nodes - X.shape[0], 3))])
@@ -179,10 +192,13 @@ class PairBatch:
                                "q_trial_norm", "dissipation", "status", "stick")}
         d["ea"] = np.arange(0, 2 * n, 2, dtype=np.int64)
         d["eb"] = np.arange(1, 2 * n, 2, dtype=np.int64)
+        if all_members:
+            d["status"] = np.ones(n, np.int8)
         self.table.from_host(d, 2 * n)
         self.u0 = torch.zeros(self.mesh.ndof, dtype=torch.float64, device=dev)
         self.pattern = None
         self.rec = None
+        self.coat = None
 
     @property
     def device(self):
@@ -234,6 +250,39 @@ class PairBatch:
     def state(self) -> dict:
         return self.table.to_host()
 
+    # -- coating -------------------------------------------------------------
+    def coating_state(self):
+        """Device copy of the pairs' coating state (``xk_coating_state``)."""
+        if self.coat is None:
+            h, dev = self.host, self.device
+            t = {"cc": h["coating_compression"], "cc_prev": h["coating_compression_prev"],
+                 "z_t": np.ascontiguousarray(h["coating_z_t"].T).ravel(), "q_trial_norm": h["coating_q_trial_norm"],
+                 "dissipation": h["coating_dissipation"]}
+            self.coat_t = {k: as_dev(np.asarray(v, np.float64), torch.float64, dev) for k, v in t.items()}
+            self.coat_t["stick"] = as_dev(h["coating_stick"].astype(np.uint8), torch.uint8, dev)
+            self.coat = L.CoatingState(*(ptr(self.coat_t[k]) for k in ("cc", "cc_prev", "z_t", "stick",
+                                                                         "q_trial_norm", "dissipation")))
+        return self.coat
+
+    def coating_geometry(self, cp, coat_total: np.ndarray, update_active: bool) -> np.ndarray:
+        """Narrowphase on the core radii, then the coating compression (and the active set)."""
+        self.narrowphase(cp, False)
+        ct = as_dev(np.asarray(coat_total, np.float64), torch.float64, self.device)
+        cc = torch.zeros(max(self.n, 1), dtype=torch.float64, device=self.device)
+        L.call("xk_coating_geometry", C.byref(self.table.c), ptr(ct), C.byref(cp), int(update_active), ptr(cc),
+               stream_handle())
+        return cc[: self.n].cpu().numpy()
+
+    def coating_step(self, stages: int, params, u=None, u_ref=None):
+        if self.pattern is None:
+            self.build_pattern()
+        L.call("xk_coating_step", C.byref(self.table.c), C.byref(self.pattern.c), C.byref(self.coating_state()),
+               ptr(u), ptr(u_ref), C.byref(params), int(stages), ptr(self.rec), stream_handle())
+
+    def member_pairs(self) -> np.ndarray:
+        """Pair index of every member (record order)."""
+        return self.pattern.members[: self.pattern.n_members].cpu().numpy().astype(np.int64)
+
 
 def _contact_params(k_pen=0.0, k_t_ratio=0.0, mu_eff=0.0, smoothing_delta=0.0, g_on=0.0, g_off=0.0,
                     allow_deactivation=True):
@@ -257,13 +306,26 @@ def _dev_vec(x, device) -> torch.Tensor | None:
 # ----------------------------------------------------------------------------- geometry
 
 
-def _write_geometry(pairs, st: dict, idx, with_status: bool):
+def _write_geometry(pairs, st: dict, idx, with_status: bool, cc=None):
     for i in idx:
         kw = {"s": float(st["s"][i]), "t": float(st["t"][i]), "gap": float(st["gap"][i]),
               "normal": st["normal"][i].copy(), "tangent1": st["t1"][i].copy(), "tangent2": st["t2"][i].copy()}
         if with_status:
             kw["status"] = _status_like(pairs[i].state.status, st["status"][i])
+        if cc is not None:
+            kw["coating_compression"] = float(cc[i])
         pairs[i] = _evolve(pairs[i], **kw)
+
+
+def _coated_geometry(pairs, coords, cp, update_active: bool, device):
+    """The coating branch of the geometry update (``_manager_process.py:351-360,386-396``,
+    ``geometry/strategy.py:242-254``): the narrowphase on the core radii, gap = dist - (core_a + core_b),
+    coating_compression = max(0, coat_total - gap) and the hysteresis with the coating term."""
+    batch = PairBatch(pairs, coords.shape[0], coords=coords, device=device, core=True)
+    h = batch.host
+    coat_total = (h["ra"] - h["ca"]) + (h["rb"] - h["cb"])
+    cc = batch.coating_geometry(cp, coat_total, update_active)
+    _write_geometry(pairs, batch.state(), range(len(pairs)), update_active, cc)
 
 
 class GpuPointToPoint:
@@ -315,11 +377,13 @@ class GpuPointToPoint:
     def update_geometry(self, pairs: list, node_coords, *, config=None) -> None:
         if not pairs:
             return
-        if config is not None and getattr(config, "coating_stiffness", 0.0) > 0.0:
-            raise NotImplementedError("the coating contact model is not on the GPU path")
         coords = np.asarray(node_coords, dtype=float).reshape(-1, 3)
         g_on = getattr(config, "g_on", 0.0) if config is not None else 0.0
         g_off = getattr(config, "g_off", 0.0) if config is not None else 0.0
+        if config is not None and getattr(config, "coating_stiffness", 0.0) > 0.0:
+            _coated_geometry(pairs, coords, _contact_params(g_on=g_on, g_off=g_off, allow_deactivation=True), True,
+                             self._device)
+            return
         batch = PairBatch(pairs, coords.shape[0], coords=coords, device=self._device)
         batch.narrowphase(_contact_params(g_on=g_on, g_off=g_off, allow_deactivation=True), True)
         _write_geometry(pairs, batch.state(), range(len(pairs)), True)
@@ -607,6 +671,110 @@ class GpuCoulombReturnMapping:
 # ----------------------------------------------------------------------------- manager processes
 
 
+# ----------------------------------------------------------------------------- coating
+
+
+def _coating_params(config, dt: float = 0.0):
+    return L.CoatingParams(float(getattr(config, "coating_stiffness", 0.0)),
+                           float(getattr(config, "coating_damping", 0.0)), float(getattr(config, "coating_mu", 0.0)),
+                           float(getattr(config, "coating_k_t_ratio", 0.5)), float(dt))
+
+
+def _coating_batch(pairs, node_coords, ndof_per_node, device):
+    _check_dofs(ndof_per_node)
+    n_nodes = np.asarray(node_coords, dtype=float).reshape(-1, 3).shape[0]
+    return PairBatch(pairs, n_nodes, device=device, all_members=True), n_nodes
+
+
+class GpuNoCoating:
+    """``NoCoatingProcess`` (``contact/coating/strategy.py:19-77``): zero forces and stiffness."""
+
+    def forces(self, pairs: list, node_coords, config, dt: float) -> np.ndarray:
+        return np.zeros(len(node_coords) * getattr(config, "ndof_per_node", 6))
+
+    def stiffness(self, pairs: list, node_coords, config, ndof_total: int, dt: float) -> sp.csr_matrix:
+        return sp.csr_matrix((ndof_total, ndof_total))
+
+    def friction_forces(self, pairs: list, node_coords, config, u_cur, u_ref) -> np.ndarray:
+        return np.zeros_like(u_cur)
+
+    def friction_stiffness(self, pairs: list, node_coords, config, ndof_total: int) -> sp.csr_matrix:
+        return sp.csr_matrix((ndof_total, ndof_total))
+
+    def process(self, input_data=None):
+        return None
+
+
+class GpuKelvinVoigtCoating:
+    """``KelvinVoigtCoatingProcess`` (``contact/coating/strategy.py:80-400``) on the GPU.
+
+    The coating between two wire cores acts as a spring k and a dashpot c on
+    the coating compression cc (state ``coating_compression``, set by the
+    coating branch of the geometry update), with Coulomb friction on the
+    coating surface (tangential penalty k * coating_k_t_ratio, friction
+    coefficient coating_mu).  Each method packs the pair list, runs the
+    coating stage of ``xk_coating_step`` over every pair and gathers the
+    records; ``friction_forces`` writes the updated coating friction state back
+    into ``pairs`` as the reference does.
+    """
+
+    def __init__(self, device=None) -> None:
+        self._device = device
+
+    def forces(self, pairs: list, node_coords, config, dt: float) -> np.ndarray:
+        ndpn = getattr(config, "ndof_per_node", 6)
+        n_nodes = np.asarray(node_coords, dtype=float).reshape(-1, 3).shape[0]
+        if not pairs:
+            return np.zeros(n_nodes * ndpn)
+        batch, _ = _coating_batch(pairs, node_coords, ndpn, self._device)
+        batch.coating_step(L.XK_COAT_FORCE, _coating_params(config, dt))
+        return batch.force(L.XK_WHICH_NORMAL, n_nodes * ndpn)
+
+    def stiffness(self, pairs: list, node_coords, config, ndof_total: int, dt: float) -> sp.csr_matrix:
+        if not pairs:
+            return sp.csr_matrix((ndof_total, ndof_total))
+        batch, _ = _coating_batch(pairs, node_coords, getattr(config, "ndof_per_node", 6), self._device)
+        batch.coating_step(L.XK_COAT_TANGENT, _coating_params(config, dt))
+        return batch.tangent(L.XK_WHICH_NORMAL, ndof_total)
+
+    def friction_forces(self, pairs: list, node_coords, config, u_cur, u_ref) -> np.ndarray:
+        u_cur = np.asarray(u_cur, dtype=float)
+        if getattr(config, "coating_mu", 0.0) <= 0.0 or not pairs:
+            return np.zeros_like(u_cur)
+        batch, _ = _coating_batch(pairs, node_coords, getattr(config, "ndof_per_node", 6), self._device)
+        dev = batch.device
+        u = as_dev(u_cur.ravel(), torch.float64, dev)
+        ur = as_dev(np.asarray(u_ref, dtype=float).ravel(), torch.float64, dev)
+        batch.coating_step(L.XK_COAT_FRICTION, _coating_params(config), u, ur)
+        f = batch.force(L.XK_WHICH_FRICTION, u_cur.size)
+        t = batch.coat_t
+        z = t["z_t"].view(2, -1).cpu().numpy()
+        stick = t["stick"].cpu().numpy()
+        qtn = t["q_trial_norm"].cpu().numpy()
+        diss = t["dissipation"].cpu().numpy()
+        for i in range(len(pairs)):
+            pairs[i] = _evolve(pairs[i], coating_z_t=np.array([z[0, i], z[1, i]]), coating_stick=bool(stick[i]),
+                               coating_q_trial_norm=float(qtn[i]), coating_dissipation=float(diss[i]))
+        return f.reshape(u_cur.shape)
+
+    def friction_stiffness(self, pairs: list, node_coords, config, ndof_total: int) -> sp.csr_matrix:
+        if getattr(config, "coating_mu", 0.0) <= 0.0 or not pairs:
+            return sp.csr_matrix((ndof_total, ndof_total))
+        batch, _ = _coating_batch(pairs, node_coords, getattr(config, "ndof_per_node", 6), self._device)
+        batch.coating_step(L.XK_COAT_FRICTION_TANGENT, _coating_params(config))
+        return batch.tangent(L.XK_WHICH_FRICTION, ndof_total)
+
+    def process(self, input_data=None):
+        return None
+
+
+def create_coating_strategy(*, coating_stiffness: float = 0.0, device=None):
+    """``_create_coating_strategy`` (``contact/coating/strategy.py:385-400``)."""
+    if coating_stiffness <= 0.0:
+        return GpuNoCoating()
+    return GpuKelvinVoigtCoating(device=device)
+
+
 @dataclass(frozen=True)
 class ContactConfig:
     """The contact settings the assembly path reads, with the reference's names and defaults
@@ -622,6 +790,9 @@ class ContactConfig:
     midpoint_prescreening: bool = True
     prescreening_margin: float = 0.0
     coating_stiffness: float = 0.0
+    coating_damping: float = 0.0
+    coating_mu: float = 0.0
+    coating_k_t_ratio: float = 0.5
     smoothing_delta: float = 0.0
 
 
@@ -779,15 +950,16 @@ class GpuUpdateGeometryProcess:
         pairs = list(manager.pairs)
         if not pairs:
             return UpdateGeometryResult(manager=manager, n_active=0)
-        if getattr(config, "coating_stiffness", 0.0) > 0.0:
-            raise NotImplementedError("the coating contact model is not on the GPU path")
         coords = np.asarray(inp.node_coords, dtype=float).reshape(-1, 3)
         freeze = bool(getattr(inp, "freeze_active_set", False))
-        batch = PairBatch(pairs, coords.shape[0], coords=coords, device=self._device)
         cp = _contact_params(g_on=getattr(config, "g_on", 0.0), g_off=getattr(config, "g_off", 1e-6),
                              allow_deactivation=bool(getattr(inp, "allow_deactivation", True)))
-        batch.narrowphase(cp, not freeze)
-        _write_geometry(pairs, batch.state(), range(len(pairs)), not freeze)
+        if getattr(config, "coating_stiffness", 0.0) > 0.0:
+            _coated_geometry(pairs, coords, cp, not freeze, self._device)
+        else:
+            batch = PairBatch(pairs, coords.shape[0], coords=coords, device=self._device)
+            batch.narrowphase(cp, not freeze)
+            _write_geometry(pairs, batch.state(), range(len(pairs)), not freeze)
         n_active = sum(1 for p in pairs if _code(p.state.status) != 0)
         return UpdateGeometryResult(manager=_replace_pairs(manager, pairs), n_active=n_active)
 
