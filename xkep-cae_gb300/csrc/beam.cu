@@ -139,11 +139,15 @@ XK_D void rotvec_of_quatf(const float* qin, float* th) {
 
 // T_s(theta) = I + c1 S + c2 S^2 and T_s^{-1} = I - S/2 + c3 S^2 (_beam_cr.py:856-908),
 // with series below |theta| = 0.25 so that the float path keeps its accuracy.
+// The float instantiation takes the series up to |theta| = 1, where the truncated terms are
+// below 1e-10 of the sums and the closed forms no longer cancel in float, and evaluates the
+// closed forms with the float sincos: no double arithmetic in the mixed beam kernel.
 template <typename T>
 XK_D void tangent_ops(const T* th, bool inverse, T* M) {
   T a2 = th[0] * th[0] + th[1] * th[1] + th[2] * th[2];
   T c1, c2;
-  if (a2 < T(0.0625)) {
+  constexpr bool F32 = sizeof(T) == 4;
+  if (a2 < (F32 ? T(1) : T(0.0625))) {
     if (!inverse) {
       c1 = T(0.5) + a2 * (T(-1.0 / 24) + a2 * (T(1.0 / 720) + a2 * (T(-1.0 / 40320) + a2 * (T(1.0 / 3628800) + a2 * T(-1.0 / 479001600)))));
       c2 = T(1.0 / 6) + a2 * (T(-1.0 / 120) + a2 * (T(1.0 / 5040) + a2 * (T(-1.0 / 362880) + a2 * (T(1.0 / 39916800) + a2 * T(-1.0 / 6227020800.0)))));
@@ -153,9 +157,18 @@ XK_D void tangent_ops(const T* th, bool inverse, T* M) {
     }
   } else {
     T a = my_sqrt<T>(a2);
-    double sd, cd;
-    sincos((double)a, &sd, &cd);
-    T s = (T)sd, c = (T)cd;
+    T s, c;
+    if (F32) {
+      float sf, cf;
+      sincosf((float)a, &sf, &cf);
+      s = (T)sf;
+      c = (T)cf;
+    } else {
+      double sd, cd;
+      sincos((double)a, &sd, &cd);
+      s = (T)sd;
+      c = (T)cd;
+    }
     if (!inverse) {
       c1 = (T(1) - c) / a2;
       c2 = (T(1) - s / a) / a2;
@@ -458,7 +471,11 @@ struct Frame32 {
   float Rcr[9], exd[3], iLd, th1[3], th2[3], tha[3], thb[3], dax, L0;
 };
 
-XK_D void frame32(const float* __restrict__ E, const float* __restrict__ NA, const float* __restrict__ NB, Frame32& F) {
+// The local rotations th1 (node a) and th2 (node b) each take a quaternion log map: a lane of a
+// quad computes the one of its node (lanes 0, 1: a; lanes 2, 3: b) and takes the other from the
+// lane two places away, so every lane ends with both.
+XK_D void frame32(const float* __restrict__ E, const float* __restrict__ NA, const float* __restrict__ NB, Frame32& F,
+                  int lane_in_quad) {
   const float dx0[3] = {E[0], E[1], E[2]};
   F.L0 = E[3];
   float R0[9];
@@ -486,17 +503,24 @@ XK_D void frame32(const float* __restrict__ E, const float* __restrict__ NA, con
   }
   const float qrc[4] = {qr[0], -qr[1], -qr[2], -qr[3]};
   {
-    float qn[4], qx[4], tx[3];
-    quat_of_rotvecf(ua + 3, qn);
+    const bool node_b = lane_in_quad >= 2;
+    float th[3], qn[4], qx[4], tx[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) th[i] = node_b ? ub[3 + i] : ua[3 + i];
+    quat_of_rotvecf(th, qn);
     qmulf(qrc, qn, qx);
     rotvec_of_quatf(qx, tx);
+    float mine[3], other[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) F.th1[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
-    quat_of_rotvecf(ub + 3, qn);
-    qmulf(qrc, qn, qx);
-    rotvec_of_quatf(qx, tx);
+    for (int i = 0; i < 3; ++i) {
+      mine[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
+      other[i] = __shfl_xor_sync(0xffffffffu, mine[i], 2);
+    }
 #pragma unroll
-    for (int i = 0; i < 3; ++i) F.th2[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
+    for (int i = 0; i < 3; ++i) {
+      F.th1[i] = node_b ? other[i] : mine[i];
+      F.th2[i] = node_b ? mine[i] : other[i];
+    }
   }
   for (int i = 0; i < 3; ++i) { F.tha[i] = ua[3 + i]; F.thb[i] = ub[3 + i]; }
   float Rrod[9];
@@ -544,7 +568,7 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
   const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
   Frame32 F;
   frame32(e32 + (long long)e * XK_ELEM32_STRIDE, n32 + (long long)a * XK_NODE32_STRIDE + 6,
-          n32 + (long long)b * XK_NODE32_STRIDE + 6, F);
+          n32 + (long long)b * XK_NODE32_STRIDE + 6, F, I);
   const KeCoef<float> kc = ke_coef<float>(sec, F.L0);
   const float* t1 = F.th1;
   const float* t2 = F.th2;
@@ -585,21 +609,32 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
 #pragma unroll
     for (int i = 0; i < 9; ++i) dpsi[i] *= F.iLd;
   }
-  // P1, Q1 (node a) or P2, Q2 (node b) are needed by all rows: Ke_{I1} and Ke_{I3}
-  float P1[9], Q1[9], P2[9], Q2[9];
+  // P1 = T^-1(t1) dpsi, Q1 = T^-1(t1) Rcr T(tha), P2, Q2 likewise at node b are needed by all
+  // rows (Ke_{I1} and Ke_{I3}); lane I computes the I-th of (P1, Q1, P2, Q2) and the quad shares
+  // them through shared memory
   {
-    float Ti[9], Ts[9], tmp[9];
-    tangent_ops<float>(t1, true, Ti);
-    mm3(Ti, dpsi, P1);
-    tangent_ops<float>(F.tha, false, Ts);
-    mm3(Ti, Rcr, tmp);
-    mm3(tmp, Ts, Q1);
-    tangent_ops<float>(t2, true, Ti);
-    mm3(Ti, dpsi, P2);
-    tangent_ops<float>(F.thb, false, Ts);
-    mm3(Ti, Rcr, tmp);
-    mm3(tmp, Ts, Q2);
+    float thi[3], Ti[9], X[9];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) thi[c] = I < 2 ? t1[c] : t2[c];
+    tangent_ops<float>(thi, true, Ti);
+    if (I & 1) {
+      float thn[3], Ts[9], tmp[9];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) thn[c] = I < 2 ? F.tha[c] : F.thb[c];
+      tangent_ops<float>(thn, false, Ts);
+      mm3(Ti, Rcr, tmp);
+      mm3(tmp, Ts, X);
+    } else {
+      mm3(Ti, dpsi, X);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) sx[q][I][i] = X[i];
   }
+  __syncwarp();
+  const float* P1 = sx[q][0];
+  const float* Q1 = sx[q][1];
+  const float* P2 = sx[q][2];
+  const float* Q2 = sx[q][3];
   // block row I of the local stiffness against the theta1 (K1), theta2 (K3) and
   // axial (k6) columns, built with selects so that the quad does not diverge
   const bool i0 = I == 0, i1 = I == 1, i2 = I == 2;
@@ -643,6 +678,7 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
     mtm3(Rcr, Hl, H);
     mtm3(Rcr, Jl, J);
   }
+  __syncwarp();  // every lane has read P1..Q2 before sx is overwritten
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
     sx[q][I][i] = G[i];

@@ -459,23 +459,33 @@ __global__ void __launch_bounds__(128) k_elem_sums_rec(int ne, const int32_t* __
 #pragma unroll
   for (int c = 0; c < 3; ++c) { f0[c] = T(0); f1[c] = T(0); }
   const int x0 = live ? eptr[e] : 0, x1 = live ? eptr[e + 1] : 0;
-  for (int x = x0 + q; x < x1; x += 4) {
-    const int code = einc[x];
-    T r[16];
-    load16<T>(rec + (long long)(code >> 1) * XK_REC_STRIDE_COMBINED, r);
-    const T a = (code & 1) ? r[XK_REC_S + 1] : r[XK_REC_S];
-    const T om = T(1) - a;
+  // two incidences per round (x and x + 4), both records loaded before either is summed; the
+  // sums still take the lane's incidences in order
+  for (int x = x0 + q; x < x1; x += 8) {
+    const bool two = x + 4 < x1;
+    const int code0 = einc[x];
+    const int code1 = two ? einc[x + 4] : code0;
+    T r[2][16];
+    load16<T>(rec + (long long)(code0 >> 1) * XK_REC_STRIDE_COMBINED, r[0]);
+    if (two) load16<T>(rec + (long long)(code1 >> 1) * XK_REC_STRIDE_COMBINED, r[1]);
 #pragma unroll
-    for (int c = 0; c < 9; ++c) {
-      s00[c] += (om * om) * r[c];
-      s01[c] += (om * a) * r[c];
-      s11[c] += (a * a) * r[c];
-    }
+    for (int j = 0; j < 2; ++j) {
+      if (j == 1 && !two) break;
+      const int code = j == 0 ? code0 : code1;
+      const T a = (code & 1) ? r[j][XK_REC_S + 1] : r[j][XK_REC_S];
+      const T om = T(1) - a;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const T v = (code & 1) ? -r[XK_REC_V + c] : r[XK_REC_V + c];
-      f0[c] += om * v;
-      f1[c] += a * v;
+      for (int c = 0; c < 9; ++c) {
+        s00[c] += (om * om) * r[j][c];
+        s01[c] += (om * a) * r[j][c];
+        s11[c] += (a * a) * r[j][c];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const T v = (code & 1) ? -r[j][XK_REC_V + c] : r[j][XK_REC_V + c];
+        f0[c] += om * v;
+        f1[c] += a * v;
+      }
     }
   }
   // (lane 0 + lane 1) + (lane 2 + lane 3) in every lane of the quad
