@@ -372,6 +372,24 @@ def batch_section(args, dev):
     return out
 
 
+def rank_aggregate(t_max, n_sum, device=None):
+    """Times maxed and unit counts summed over the ranks of the default process group.
+
+    One rank (or no process group): the values as given.  The bench's value is
+    the units of all ranks over the slowest rank's time.
+    """
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(x) for x in t_max], [float(x) for x in n_sum]
+    a = torch.tensor([float(x) for x in t_max], dtype=torch.float64, device=device)
+    b = torch.tensor([float(x) for x in n_sum], dtype=torch.float64, device=device)
+    dist.all_reduce(a, op=dist.ReduceOp.MAX)
+    dist.all_reduce(b, op=dist.ReduceOp.SUM)
+    return a.tolist(), b.tolist()
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -455,13 +473,9 @@ def run_gpu(args, rank, world):
         t_fp64 = timed(engines["fp64"], args.steps)
     clocks = clk.summary()
 
-    if world > 1:
-        t = torch.tensor([t_mixed, t_fp64], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_mixed, t_fp64 = float(t[0]), float(t[1])
-
     n_c = engines["mixed"].pairs.n
-    units = world * (n_e + n_c)
+    # every rank assembles its own seeded strand: its units count, the slowest rank sets the time
+    (t_mixed, t_fp64), (units,) = rank_aggregate([t_mixed, t_fp64], [n_e + n_c], device=dev)
     ms_mixed = 1e3 * t_mixed / args.steps
     ms_fp64 = 1e3 * t_fp64 / args.steps
 
@@ -545,10 +559,7 @@ def run_gpu(args, rank, world):
     b.record(s)
     torch.cuda.synchronize()
     t_e2e = a.elapsed_time(b) / 1e3
-    if world > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t[0])
+    (t_e2e,), _ = rank_aggregate([t_e2e], [], device=dev)
     h2d = pipe.bytes_in
     d2h = pipe.bytes_out
     del pipe

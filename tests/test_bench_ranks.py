@@ -1,0 +1,60 @@
+"""The multi-GPU bench path's host logic on two CPU ranks (gloo): every rank assembles its own
+strand, the job's value is the units of all ranks over the slowest rank's time."""
+
+from __future__ import annotations
+
+import importlib.util
+import socket
+from pathlib import Path
+
+import pytest
+
+torch = pytest.importorskip("torch")
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _bench():
+    spec = importlib.util.spec_from_file_location("_xk_bench", ROOT / "bench.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank: int, world: int, port: int, q):
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        bench = _bench()
+        # rank r: times (1 + r, 10 - r), units 100 + r
+        t, n = bench.rank_aggregate([1.0 + rank, 10.0 - rank], [100.0 + rank])
+        q.put((rank, t, n))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_rank_aggregate_two_gloo_ranks():
+    ctx = torch.multiprocessing.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, t, n in out:
+        assert t == [2.0, 10.0]  # the slowest rank's time, each entry
+        assert n == [201.0]      # the units of both ranks
+
+
+def test_rank_aggregate_single_process_is_identity():
+    t, n = _bench().rank_aggregate([1.5, 2.5], [7])
+    assert t == [1.5, 2.5] and n == [7.0]
