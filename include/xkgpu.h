@@ -58,6 +58,11 @@ typedef struct {
   const int32_t* layer; /* [n_elems], -1 = no layer; NULL = no layer map */
   const double* mu;     /* [n_elems] friction coefficient per element (a pair uses mu[ea]: batched strands
                            with their own coefficient, already ramped); NULL = xk_contact_params.mu_eff */
+  const double* core_radii; /* [n_elems] or NULL.  Coated wires (set it only when the coating stiffness
+                               is positive, as the reference switches on coating_stiffness > 0): the
+                               narrowphase then takes the gap between the cores, dist - (core_a +
+                               core_b), and the coating compression (_manager_process.py:351-360);
+                               the broadphase keeps the outer radii */
 } xk_mesh;
 
 /* Pair table: _ContactPairOutput / _ContactStateOutput as structure of arrays
@@ -71,6 +76,12 @@ typedef struct {
   double *z_t;              /* [2*cap] */
   double *q_trial_norm, *dissipation;
   uint8_t *status, *stick;  /* status: 0 INACTIVE, 1 ACTIVE, 2 SLIDING (_types.py:8-13) */
+  /* Coating state (_contact_pair.py:57-62), NULL unless the mesh has core radii: coating_compression,
+   * coating_compression_prev, coating_z_t [2*cap], coating_q_trial_norm, coating_dissipation,
+   * coating_stick.  With coating every pair of the table is a member of the contact pattern, since
+   * the reference evaluates the coating force of every pair. */
+  double *coat_cc, *coat_cc_prev, *coat_z_t, *coat_qtn, *coat_diss;
+  uint8_t* coat_stick;
 } xk_pairs;
 
 /* -------------------------------------------------------------- beam path */
@@ -147,6 +158,10 @@ typedef struct {
   double smoothing_delta;  /* Huber smoothing; 0 = plain max(0, x) (contact_force/strategy.py:139) */
   double g_on, g_off;      /* active-set hysteresis (_manager_process.py:475-494) */
   int32_t allow_deactivation;
+  /* Kelvin-Voigt coating (KelvinVoigtCoatingProcess, contact/coating/strategy.py:80-376), used when the
+   * mesh has core radii: stiffness k, damping c, coating friction coefficient and tangential ratio, and
+   * the step's pseudo-time increment for the dashpot (c > 0 and dt > 0). */
+  double coat_k, coat_c, coat_mu, coat_kt_ratio, coat_dt;
 } xk_contact_params;
 
 typedef struct {
@@ -332,6 +347,10 @@ typedef struct {
   uint8_t *status, *stick;
   float* mu;               /* [cap] friction coefficient of each slot, filled from xk_mesh.mu by xk_pairs_to32;
                               NULL (use xk_contact_params.mu_eff) unless the mesh has per-element mu */
+  /* Coating (NULL unless the mesh has core radii): rad then holds the core radius sum; coat_total
+   * (r_a - core_a) + (r_b - core_b) per slot and the coating state as in xk_pairs. */
+  float *coat_total, *coat_cc, *coat_cc_prev, *coat_z_t, *coat_qtn, *coat_diss;
+  uint8_t* coat_stick;
   int32_t* defer;          /* [2 * (cap + 2)] zero-initialised scratch or NULL: the pair kernels then
                               leave the rare near-parallel pairs to a second kernel each (other
                               pairs: [count, done, slots] from defer[0]; members: the same from

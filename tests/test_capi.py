@@ -45,10 +45,10 @@ def test_struct_layouts_match_header():
 
     # field order and sizes as declared in include/xkgpu.h (LP64)
     assert C.sizeof(L.Section) == 9 * 8
-    assert C.sizeof(L.Mesh) == 8 + 5 * 8
-    assert C.sizeof(L.Pairs) == 8 + 17 * 8
+    assert C.sizeof(L.Mesh) == 8 + 6 * 8
+    assert C.sizeof(L.Pairs) == 8 + 23 * 8
     assert C.sizeof(L.BeamPlan) == 8 + 4 * 8 + 8 + 8
-    assert C.sizeof(L.ContactParams) == 6 * 8 + 8
+    assert C.sizeof(L.ContactParams) == 6 * 8 + 8 + 5 * 8
     assert C.sizeof(L.BPParams) == 8 + 3 * 4 + 4 + 8
     assert C.sizeof(L.ContactPattern) == 16 + 5 * 8 + 10 * 8 + 2 * 8 + 7 * 8
 

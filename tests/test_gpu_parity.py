@@ -317,6 +317,63 @@ def test_near_parallel_pairs_mixed_vs_fp64():
     assert rel_err(hmx["s"], h64["s"]) < 1e-5 and rel_err(hmx["t"], h64["t"]) < 1e-5
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("mixed", TOLMIX)])
+def test_engine_coated_wires_vs_oracle(precision, tol):
+    """The coating model fused into the pair kernels (7-wire strand, coating 0.1 r): detection with the
+    core gap, coating compression and the coating term of the active set, then two Newton iterations
+    whose residual and K_c carry the Huber, friction, coating and coating-friction parts; against the
+    oracle (which matches the reference's own outputs on these inputs, tests/golden/coating7.npz)."""
+    from xkgpu import workloads as W
+
+    z = golden("coating7")
+    X, conn, layer = z["X"], z["conn"], z["elem_layer"]
+    n = 6 * len(X)
+    r, cr = float(z["radius"]), float(z["core_radius"])
+    k, c, cmu, ktr, dt = (float(z[q]) for q in ("k_coat", "c_coat", "mu_coat", "kt_ratio", "dt"))
+    sec = W.circle_section(2.0 * r)
+    k_pen, mu, kt_ratio = 2e4, 0.1, 0.5
+    eng = AssemblyEngine(X, conn, r, sec, layer=layer, precision=precision, k_pen=k_pen, k_t_ratio=kt_ratio, mu=mu,
+                         core_radii=cr, coating=dict(stiffness=k, damping=c, mu=cmu, k_t_ratio=ktr, dt=dt))
+    u0 = z["u0"]
+    eng.detect(_dev(u0))
+    table, _, _ = oc.detect(oc.empty_table(), oc.deformed_coords(X, u0), conn, np.full(len(conn), r),
+                            elem_layer=layer, exclude_same_layer=True, core_radii=np.full(len(conn), cr))
+    table, cc = oc.coating_geometry(table, oc.deformed_coords(X, u0))
+    h = eng.pair_state()
+    assert np.array_equal(h["ea"], table["ea"]) and np.array_equal(h["status"], table["status"])
+    if precision == "fp64":  # the detection is exact in both modes; the mixed state is read back as float
+        assert np.array_equal(h["gap"], table["gap"]) and np.array_equal(h["coat_cc"], cc)
+    else:
+        assert rel_err(h["gap"], table["gap"]) < 1e-6 and rel_err(h["coat_cc"], cc) < 1e-6
+    assert eng.pattern.n_members == len(cc)  # every pair of a coated model contributes
+    eng.end_step()  # coating_compression_prev <- coating_compression
+    cc_prev = cc.copy()
+    state = {"z_t": np.zeros((len(cc), 2)), "stick": np.ones(len(cc), bool), "q_trial_norm": np.zeros(len(cc)),
+             "dissipation": np.zeros(len(cc))}
+    sec_o = ob.Section(**sec, scf=None)
+    for it in range(int(z["n_iter"])):
+        u = z[f"it{it}_u"]
+        eng.assemble(_dev(u), _dev(u0))
+        torch.cuda.synchronize()
+        cd = oc.deformed_coords(X, u)
+        table, cc = oc.coating_geometry(table, cd, freeze_active_set=True)
+        table, fn, _ = oc.huber_evaluate(table, n, k_pen)
+        table, ff, _, fr = oc.friction_evaluate(table, u, u0, n, k_pen, kt_ratio, mu)
+        fcn = oc.coating_forces(table, cc, cc_prev, n, k, c, dt)
+        fcf, state = oc.coating_friction(table, cc, state, u, u0, n, k, ktr, cmu)
+        Kb, fb = ob.assemble_beam(X, conn, u, sec_o)
+        R_ref = fb - (fn + ff + fcn + fcf)
+        K_ref = (oc.huber_tangent(table, n, k_pen) - oc.friction_tangent(table, fr, n)
+                 + oc.coating_stiffness(table, cc, n, k, c, dt)
+                 + oc.coating_friction_stiffness(table, cc, state, n, k, ktr, cmu)).tocsr()
+        assert rel_err(eng.R.cpu().numpy(), R_ref) < tol, it
+        assert sparse_rel_err(eng.K_contact_csr(), K_ref) < tol, it
+        h = eng.pair_state()
+        assert rel_err(h["coat_cc"], cc) < (1e-12 if precision == "fp64" else 1e-5)
+        assert np.array_equal(h["coat_stick"], state["stick"])
+        assert rel_err(h["coat_z_t"], state["z_t"]) < (1e-10 if precision == "fp64" else 1e-4)
+
+
 def test_mixed_engine_vs_fp64_strand37():
     from xkgpu import workloads as W
 

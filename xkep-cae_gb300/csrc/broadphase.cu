@@ -329,6 +329,16 @@ XK_D void copy_state(const xk_pairs& a, long long i, xk_pairs& b, long long j) {
   b.dissipation[j] = a.dissipation[i];
   b.status[j] = a.status[i];
   b.stick[j] = a.stick[i];
+  if (b.coat_cc) {  // coated wires: the coating state travels with the pair (fresh if the source has none)
+    const bool has = a.coat_cc != nullptr;
+    b.coat_cc[j] = has ? a.coat_cc[i] : 0.0;
+    b.coat_cc_prev[j] = has ? a.coat_cc_prev[i] : 0.0;
+    b.coat_z_t[j] = has ? a.coat_z_t[i] : 0.0;
+    b.coat_z_t[cb + j] = has ? a.coat_z_t[ca + i] : 0.0;
+    b.coat_qtn[j] = has ? a.coat_qtn[i] : 0.0;
+    b.coat_diss[j] = has ? a.coat_diss[i] : 0.0;
+    b.coat_stick[j] = has ? a.coat_stick[i] : 1;
+  }
 }
 
 __global__ void k_merge_flags(xk_pairs old, const int32_t* __restrict__ cand, long long nc, int32_t* __restrict__ r) {
@@ -373,6 +383,15 @@ __global__ void k_merge_new(xk_pairs old, const int32_t* __restrict__ cand, long
   out.dissipation[pos] = 0.0;
   out.status[pos] = 0;
   out.stick[pos] = 1;
+  if (out.coat_cc) {
+    out.coat_cc[pos] = 0.0;
+    out.coat_cc_prev[pos] = 0.0;
+    out.coat_z_t[pos] = 0.0;
+    out.coat_z_t[cb + pos] = 0.0;
+    out.coat_qtn[pos] = 0.0;
+    out.coat_diss[pos] = 0.0;
+    out.coat_stick[pos] = 1;
+  }
 }
 
 __global__ void k_merge_old(xk_pairs old, const int32_t* __restrict__ cand, long long nc,

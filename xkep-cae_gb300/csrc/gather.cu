@@ -34,7 +34,11 @@ XK_D T shape_c(T s, T t, int k) {
   }
 }
 
-XK_D bool is_member(const xk_pairs& p, int i) { return (p.status[i] != 0) || (p.p_n[i] > 0.0); }
+// A pair contributes in the increment when it is not INACTIVE or still carries a normal force; with
+// coated wires every pair does, since the reference evaluates the coating force of every pair.
+XK_D bool is_member(const xk_pairs& p, int i) {
+  return (p.status[i] != 0) || (p.p_n[i] > 0.0) || (p.coat_cc != nullptr);
+}
 
 __global__ void k_flags(xk_pairs p, int32_t* __restrict__ flag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -229,6 +229,15 @@ XK_D void store3(double* base, long long stride, long long i, const double* v) {
   base[2 * stride + i] = v[2];
 }
 
+// Coated wires (_manager_process.py:351-360): coat_total = (r_a - core_a) + (r_b - core_b) and the
+// compression max(0, coat_total - gap) of the core gap.
+XK_D double coat_total_of(const xk_mesh& m, int ea, int eb) {
+  return xadd(xsub(m.radii[ea], m.core_radii[ea]), xsub(m.radii[eb], m.core_radii[eb]));
+}
+XK_D double coat_compression(const xk_mesh& m, int ea, int eb, double gap) {
+  return fmax(0.0, xsub(coat_total_of(m, ea, eb), gap));
+}
+
 __global__ void k_narrow_exact(xk_mesh m, xk_pairs p, const double* __restrict__ u, double g_on, double g_off,
                                int allow_deact, int update_active) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -239,7 +248,11 @@ __global__ void k_narrow_exact(xk_mesh m, xk_pairs p, const double* __restrict__
   for (int k = 0; k < 4; ++k) deformed(m, u, nd.n[k], x[k]);
   double s, t, dist, nrm[3], diff[3];
   closest_exact(x[0], x[1], x[2], x[3], s, t, dist, nrm, diff);
-  const double gap = xsub(dist, xadd(m.radii[p.ea[i]], m.radii[p.eb[i]]));
+  const bool coat = m.core_radii != nullptr;
+  const double gap = coat ? xsub(dist, xadd(m.core_radii[p.ea[i]], m.core_radii[p.eb[i]]))
+                          : xsub(dist, xadd(m.radii[p.ea[i]], m.radii[p.eb[i]]));
+  const double cc = coat ? coat_compression(m, p.ea[i], p.eb[i], gap) : 0.0;
+  if (coat && p.coat_cc) p.coat_cc[i] = cc;
   double pt1[3], pn[3], n[3], t1[3], t2[3];
   load3(p.t1, cap, i, pt1);
   load3(p.normal, cap, i, pn);
@@ -250,11 +263,12 @@ __global__ void k_narrow_exact(xk_mesh m, xk_pairs p, const double* __restrict__
   store3(p.normal, cap, i, n);
   store3(p.t1, cap, i, t1);
   store3(p.t2, cap, i, t2);
-  if (update_active) {  // _update_active_set_state (_manager_process.py:475-494)
+  if (update_active) {  // _update_active_set_state (_manager_process.py:475-494), coating term included
+    const bool coat_active = coat && cc > 0.0;
     uint8_t st = p.status[i];
     if (st == ST_INACTIVE) {
-      if (gap <= g_on) p.status[i] = ST_ACTIVE;
-    } else if (allow_deact && gap >= g_off) {
+      if (gap <= g_on || coat_active) p.status[i] = ST_ACTIVE;
+    } else if (allow_deact && gap >= g_off && !coat_active) {
       p.status[i] = ST_INACTIVE;
     }
   }
@@ -278,7 +292,9 @@ template <int P>
 XK_D void pair_narrow(const xk_mesh& m, xk_pairs& p, int i, const int* nd, const double* __restrict__ u, double& s,
                       double& t, double& gap, double* n, double* t1, double* t2) {
   const long long cap = p.cap;
-  const double ra = m.radii[p.ea[i]], rb = m.radii[p.eb[i]];
+  const bool coat = m.core_radii != nullptr;  // coated wires: the gap between the cores
+  const double ra = coat ? m.core_radii[p.ea[i]] : m.radii[p.ea[i]];
+  const double rb = coat ? m.core_radii[p.eb[i]] : m.radii[p.eb[i]];
   double x[4][3];
   for (int k = 0; k < 4; ++k)
     for (int c = 0; c < 3; ++c) x[k][c] = xadd(m.X[3LL * nd[k] + c], u[6LL * nd[k] + c]);
@@ -301,6 +317,70 @@ XK_D void pair_narrow(const xk_mesh& m, xk_pairs& p, int i, const int* nd, const
   store3(p.normal, cap, i, n);
   store3(p.t1, cap, i, t1);
   store3(p.t2, cap, i, t2);
+  if (coat && p.coat_cc) p.coat_cc[i] = coat_compression(m, p.ea[i], p.eb[i], gap);
+}
+
+// Kelvin-Voigt coating of one pair (KelvinVoigtCoatingProcess, contact/coating/strategy.py:97-370) as
+// additions to its combined record: the spring / dashpot force v = -(k cc + c (cc - cc_prev) / dt) n
+// with stiffness (k + c / dt) n n^T where cc > 1e-15, and the coating friction (return mapping on the
+// coating surface with p_n = k cc, k_t = k * ratio; an uncompressed pair's history reset) with force
+// -(q0 t1 + q1 t2) and stiffness T D T^T.  The coating state is read and updated in the pair table.
+template <typename T, typename ST>
+XK_D void coating_epilogue(const xk_contact_params& cp, const ST* __restrict__ prev_a,
+                           ST* __restrict__ z_t, ST* __restrict__ qtn_a, ST* __restrict__ diss_a,
+                           uint8_t* __restrict__ stick_a, long long i, long long cap, T cc, T s, T t, const T* n,
+                           const T* t1, const T* t2, const T (*du)[3], T* v, T* B) {
+  const T k = (T)cp.coat_k, c = (T)cp.coat_c, dt = (T)cp.coat_dt;
+  const bool visc = cp.coat_c > 0.0 && cp.coat_dt > 0.0;
+  const T prev = (T)prev_a[i];
+  if (!(cc <= T(0) && prev <= T(0))) {  // forces (strategy.py:97-143)
+    T f = k * cc;
+    if (visc) f += c * ((cc - prev) / dt);
+    if (!(my_abs<T>(f) < T(1e-30)))
+      for (int q = 0; q < 3; ++q) v[q] -= f * n[q];
+  }
+  if (cc > T(1e-15)) {  // stiffness (strategy.py:145-196)
+    const T k_eff = visc ? k + c / dt : k;
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) B[3 * a + b] += k_eff * n[a] * n[b];
+  }
+  if (!(cp.coat_mu > 0.0)) return;
+  const T k_t = k * (T)cp.coat_kt_ratio, mu = (T)cp.coat_mu;
+  if (cc <= T(0)) {  // friction_forces (strategy.py:198-288): no coating contact, history reset
+    z_t[i] = ST(0);
+    z_t[cap + i] = ST(0);
+    stick_a[i] = 1;
+    qtn_a[i] = ST(0);
+    diss_a[i] = ST(0);
+    return;
+  }
+  const T p_n = k * cc;
+  T rel[3];
+  for (int q = 0; q < 3; ++q) rel[q] = ((T(1) - t) * du[2][q] + t * du[3][q]) - ((T(1) - s) * du[0][q] + s * du[1][q]);
+  const T d0 = dot3(rel, t1), d1 = dot3(rel, t2);
+  const T tr0 = (T)z_t[i] + k_t * d0, tr1 = (T)z_t[cap + i] + k_t * d1;
+  const T qn = my_sqrt<T>(tr0 * tr0 + tr1 * tr1);
+  const T fy = mu * p_n;
+  const bool stick = qn <= fy;
+  const T q0 = stick ? tr0 : fy * tr0 / qn, q1 = stick ? tr1 : fy * tr1 / qn;
+  z_t[i] = (ST)q0;
+  z_t[cap + i] = (ST)q1;
+  stick_a[i] = stick ? 1 : 0;
+  qtn_a[i] = (ST)qn;
+  diss_a[i] = (ST)(q0 * d0 + q1 * d1);
+  for (int q = 0; q < 3; ++q) v[q] -= q0 * t1[q] + q1 * t2[q];
+  // friction_stiffness (strategy.py:290-370): D from _tangent_2x2_core on the updated state
+  T D00 = k_t, D01 = T(0), D11 = k_t;
+  const T zn = my_sqrt<T>(q0 * q0 + q1 * q1);
+  if (!stick && zn >= T(1e-30) && qn >= T(1e-30)) {
+    const T h0 = q0 / zn, h1 = q1 / zn, ratio = (mu * p_n) / qn;
+    D00 = ratio * k_t * (T(1) - h0 * h0);
+    D01 = ratio * k_t * (T(0) - h0 * h1);
+    D11 = ratio * k_t * (T(1) - h1 * h1);
+  }
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      B[3 * a + b] += (t1[a] * D00 + t2[a] * D01) * t1[b] + (t1[a] * D01 + t2[a] * D11) * t2[b];
 }
 
 // Pairs that cannot contribute in this increment: only the frozen narrowphase,
@@ -454,13 +534,27 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, c
       Bf[7] -= idist * q1 * t1T[0];
     }
   }
+  // ---------------------------------------------------------------- coating (coated wires)
+  T vc[3] = {T(0), T(0), T(0)}, Bc[9];
+  for (int k = 0; k < 9; ++k) Bc[k] = T(0);
+  constexpr int ALL = XK_STAGE_NORMAL | XK_STAGE_FRICTION | XK_STAGE_TANGENT;
+  if (OUT == XK_OUT_COMBINED && m.core_radii && p.coat_cc && (stages & ALL) == ALL) {
+    T duc[4][3];
+    for (int k = 0; k < 4; ++k)
+      for (int c = 0; c < 3; ++c) {
+        const long long dof = 6LL * nd[k] + c;
+        duc[k][c] = (T)(u_ref ? u[dof] - u_ref[dof] : u[dof]);
+      }
+    coating_epilogue<T, double>(cp, p.coat_cc_prev, p.coat_z_t, p.coat_qtn, p.coat_diss, p.coat_stick, i, cap,
+                                (T)p.coat_cc[i], (T)s, (T)t, nT, t1T, t2T, duc, vc, Bc);
+  }
   // ---------------------------------------------------------------- record
   T* r = rec + (long long)mi * rs;  // array-of-structs record, rs values per member
   if (OUT == XK_OUT_COMBINED) {
-    for (int k = 0; k < 9; ++k) r[XK_REC_B + k] = Bn[k] - Bf[k];
+    for (int k = 0; k < 9; ++k) r[XK_REC_B + k] = (Bn[k] - Bf[k]) + Bc[k];
     r[XK_REC_S] = (T)s;
     r[XK_REC_S + 1] = (T)t;
-    for (int k = 0; k < 3; ++k) r[XK_REC_V + k] = vn[k] + vf[k];
+    for (int k = 0; k < 3; ++k) r[XK_REC_V + k] = (vn[k] + vf[k]) + vc[k];
     r[14] = T(0);
     r[15] = T(0);
   } else {
@@ -573,10 +667,21 @@ __global__ void k_pairs_to32(xk_mesh m, xk_pairs p, xk_contact_pattern pat, xk_p
   q.nodes[4LL * j + 1] = m.conn[2 * ea + 1];
   q.nodes[4LL * j + 2] = m.conn[2 * eb];
   q.nodes[4LL * j + 3] = m.conn[2 * eb + 1];
-  const double R = m.radii[ea] + m.radii[eb];
+  const bool coat = q.coat_total && m.core_radii && p.coat_cc;  // coated wires: the gap between the cores
+  const double R = coat ? m.core_radii[ea] + m.core_radii[eb] : m.radii[ea] + m.radii[eb];
   const float rh = (float)R;
   q.rad[2LL * j] = rh;
   q.rad[2LL * j + 1] = (float)(R - (double)rh);
+  if (coat) {
+    q.coat_total[j] = (float)coat_total_of(m, ea, eb);
+    q.coat_cc[j] = (float)p.coat_cc[i];
+    q.coat_cc_prev[j] = (float)p.coat_cc_prev[i];
+    q.coat_z_t[j] = (float)p.coat_z_t[i];
+    q.coat_z_t[cq + j] = (float)p.coat_z_t[cp + i];
+    q.coat_qtn[j] = (float)p.coat_qtn[i];
+    q.coat_diss[j] = (float)p.coat_diss[i];
+    q.coat_stick[j] = p.coat_stick[i];
+  }
   q.s[j] = (float)p.s[i]; q.t[j] = (float)p.t[i]; q.gap[j] = (float)p.gap[i];
   for (int c = 0; c < 3; ++c) {
     q.normal[c * cq + j] = (float)p.normal[c * cp + i];
@@ -614,6 +719,15 @@ __global__ void k_pairs_from32(xk_pairs32 q, xk_pairs p) {
   p.q_trial_norm[i] = q.q_trial_norm[j]; p.dissipation[i] = q.dissipation[j];
   p.k_pen[i] = q.k_pen[j]; p.k_t[i] = q.k_t[j];
   p.status[i] = q.status[j]; p.stick[i] = q.stick[j];
+  if (q.coat_total && p.coat_cc) {
+    p.coat_cc[i] = q.coat_cc[j];
+    p.coat_cc_prev[i] = q.coat_cc_prev[j];
+    p.coat_z_t[i] = q.coat_z_t[j];
+    p.coat_z_t[cp + i] = q.coat_z_t[cq + j];
+    p.coat_qtn[i] = q.coat_qtn[j];
+    p.coat_diss[i] = q.coat_diss[j];
+    p.coat_stick[i] = q.coat_stick[j];
+  }
 }
 
 XK_D float clamp01f(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
@@ -906,8 +1020,11 @@ XK_D void member32(const xk_pairs32& q, const float* __restrict__ n32, const xk_
   // pair tangent B = B_n - B_f
   float B[9];
   for (int k = 0; k < 9; ++k) B[k] = 0.f;
+  // coated wires: the gap is between the cores; the geometric terms take gap + r_a + r_b as the
+  // reference does (contact_force/strategy.py:230-236, friction/_assembly.py:203-204)
+  const float ct = q.coat_total ? q.coat_total[i] : 0.0f;
   if (status != ST_INACTIVE) {
-    const float dist = gap + (R.h + R.l);
+    const float dist = gap + ((R.h + R.l) + ct);
     const float hd = (dh <= 0.0f) ? (xpen > 0.0f ? 1.0f : 0.0f)
                                   : (xpen < -dh ? 0.0f : (xpen > dh ? 1.0f : (xpen + dh) / (2.0f * dh)));
     if (!(hd < 1e-30f && p_n < 1e-30f)) {
@@ -943,6 +1060,19 @@ XK_D void member32(const xk_pairs32& q, const float* __restrict__ n32, const xk_
       B[6] -= g * t1[1];
       B[7] += g * t1[0];
     }
+  }
+  if (q.coat_total) {  // Kelvin-Voigt coating, added to the record
+    const float cc = fmaxf(0.0f, ct - gap);
+    q.coat_cc[i] = cc;
+    float duc[4][3];
+    for (int k = 0; k < 4; ++k) {
+      const float4 d4 = __ldg(reinterpret_cast<const float4*>(n32 + (long long)nd[k] * XK_NODE32_STRIDE + 12));
+      duc[k][0] = d4.x; duc[k][1] = d4.y; duc[k][2] = d4.z;
+    }
+    float vc[3] = {0.f, 0.f, 0.f};
+    coating_epilogue<float, float>(cp, q.coat_cc_prev, q.coat_z_t, q.coat_qtn, q.coat_diss, q.coat_stick, i, cq, cc,
+                                   s, t, n, t1, t2, duc, vc, B);
+    for (int k = 0; k < 3; ++k) vf[k] += vc[k];
   }
   float4* r = reinterpret_cast<float4*>(rec + (long long)mi * XK_REC_STRIDE_COMBINED);
   r[0] = make_float4(B[0], B[1], B[2], B[3]);

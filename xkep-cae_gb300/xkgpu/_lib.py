@@ -46,19 +46,25 @@ class CoatingParams(C.Structure):
 
 class Mesh(C.Structure):
     _fields_ = [("n_nodes", C.c_int32), ("n_elems", C.c_int32), ("X", vp), ("conn", vp), ("radii", vp),
-                ("layer", vp), ("mu", vp)]
+                ("layer", vp), ("mu", vp), ("core_radii", vp)]
+
+
+COAT64_FIELDS = ("coat_cc", "coat_cc_prev", "coat_z_t", "coat_qtn", "coat_diss", "coat_stick")
+COAT32_FIELDS = ("coat_total", "coat_cc", "coat_cc_prev", "coat_z_t", "coat_qtn", "coat_diss", "coat_stick")
 
 
 class Pairs(C.Structure):
     _fields_ = [("n", C.c_int32), ("cap", C.c_int32)] + [
         (n, vp) for n in ("ea", "eb", "s", "t", "gap", "normal", "t1", "t2", "lambda_n", "k_pen", "k_t", "p_n",
-                          "z_t", "q_trial_norm", "dissipation", "status", "stick")]
+                          "z_t", "q_trial_norm", "dissipation", "status", "stick")] + [
+        (n, vp) for n in COAT64_FIELDS]
 
 
 class Pairs32(C.Structure):
     _fields_ = [("n", C.c_int32), ("cap", C.c_int32), ("n_members", C.c_int32)] + [
         (n, vp) for n in ("pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
-                          "dissipation", "k_pen", "k_t", "status", "stick", "mu", "defer")]
+                          "dissipation", "k_pen", "k_t", "status", "stick", "mu")] + [
+        (n, vp) for n in COAT32_FIELDS] + [("defer", vp)]
 
 
 class BeamPlan(C.Structure):
@@ -69,7 +75,8 @@ class BeamPlan(C.Structure):
 class ContactParams(C.Structure):
     _fields_ = [("k_pen", C.c_double), ("k_t_ratio", C.c_double), ("mu_eff", C.c_double),
                 ("smoothing_delta", C.c_double), ("g_on", C.c_double), ("g_off", C.c_double),
-                ("allow_deactivation", C.c_int32)]
+                ("allow_deactivation", C.c_int32)] + [
+        (n, C.c_double) for n in ("coat_k", "coat_c", "coat_mu", "coat_kt_ratio", "coat_dt")]
 
 
 class BPParams(C.Structure):

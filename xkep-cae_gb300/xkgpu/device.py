@@ -45,7 +45,7 @@ def as_dev(x, dtype, device) -> torch.Tensor:
 class DeviceMesh:
     """Reference coordinates, connectivity, radii and layer ids on the device."""
 
-    def __init__(self, coords, conn, radii, layer=None, device=None, mu=None):
+    def __init__(self, coords, conn, radii, layer=None, device=None, mu=None, core_radii=None):
         self.device = require_cuda(device)
         coords = np.asarray(coords, dtype=np.float64).reshape(-1, 3)
         conn = np.asarray(conn, dtype=np.int64).reshape(-1, 2)
@@ -63,12 +63,16 @@ class DeviceMesh:
         if mu is not None and np.asarray(mu).shape != (self.n_elems,):
             raise ValueError("mu must hold one friction coefficient per element")
         self.mu = None if mu is None else as_dev(np.asarray(mu, dtype=np.float64), torch.float64, self.device)
+        # coated wires: the core radius of every element (the narrowphase's gap is between the cores)
+        self.core_radii = None if core_radii is None else as_dev(
+            np.broadcast_to(np.asarray(core_radii, dtype=np.float64), (self.n_elems,)).copy(), torch.float64,
+            self.device)
         self.conn_host = conn
         self.refresh()
 
     def refresh(self):
         self.c = L.Mesh(self.n_nodes, self.n_elems, ptr(self.X), ptr(self.conn), ptr(self.radii), ptr(self.layer),
-                        ptr(self.mu))
+                        ptr(self.mu), ptr(self.core_radii))
 
     def set_coords(self, coords):
         self.X.copy_(as_dev(np.asarray(coords, dtype=np.float64).ravel(), torch.float64, self.device))
@@ -239,17 +243,27 @@ class DeviceBeam:
 F64_FIELDS = {"s": 1, "t": 1, "gap": 1, "normal": 3, "t1": 3, "t2": 3, "lambda_n": 1, "k_pen": 1, "k_t": 1,
               "p_n": 1, "z_t": 2, "q_trial_norm": 1, "dissipation": 1}
 U8_FIELDS = ("status", "stick")
+# coating state of coated wires (double, then the stick flag)
+COAT_F64 = {"coat_cc": 1, "coat_cc_prev": 1, "coat_z_t": 2, "coat_qtn": 1, "coat_diss": 1}
+COAT_U8 = ("coat_stick",)
 
 
 class DevicePairTable:
     """Structure-of-arrays pair table (``xk_pairs``), vector fields component-major."""
 
-    def __init__(self, device, cap: int = 1024):
+    def __init__(self, device, cap: int = 1024, coating: bool = False):
         self.device = device
         self.n = 0
         self.cap = 0
+        self.coating = coating  # the table carries the coating state (coated wires)
         self.t: dict[str, torch.Tensor] = {}
         self.reserve(max(cap, 16))
+
+    def _f64(self):
+        return {**F64_FIELDS, **COAT_F64} if self.coating else F64_FIELDS
+
+    def _u8(self):
+        return (*U8_FIELDS, *COAT_U8) if self.coating else U8_FIELDS
 
     def reserve(self, cap: int, keep: bool = True):
         if cap <= self.cap:
@@ -257,15 +271,15 @@ class DevicePairTable:
         cap = int(cap)
         new = {"ea": torch.zeros(cap, dtype=torch.int32, device=self.device),
                "eb": torch.zeros(cap, dtype=torch.int32, device=self.device)}
-        for k, w in F64_FIELDS.items():
+        for k, w in self._f64().items():
             new[k] = torch.zeros(w * cap, dtype=torch.float64, device=self.device)
-        for k in U8_FIELDS:
+        for k in self._u8():
             new[k] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         if keep and self.n:
             n, oc = self.n, self.cap
-            for k in ("ea", "eb", *U8_FIELDS):
+            for k in ("ea", "eb", *self._u8()):
                 new[k][:n] = self.t[k][:n]
-            for k, w in F64_FIELDS.items():
+            for k, w in self._f64().items():
                 for c in range(w):
                     new[k][c * cap : c * cap + n] = self.t[k][c * oc : c * oc + n]
         self.t = new
@@ -276,7 +290,7 @@ class DevicePairTable:
         t = self.t
         self.c = L.Pairs(self.n, self.cap, *(ptr(t[k]) for k in (
             "ea", "eb", "s", "t", "gap", "normal", "t1", "t2", "lambda_n", "k_pen", "k_t", "p_n", "z_t",
-            "q_trial_norm", "dissipation", "status", "stick")))
+            "q_trial_norm", "dissipation", "status", "stick")), *(ptr(t.get(k)) for k in L.COAT64_FIELDS))
 
     def set_n(self, n: int):
         self.n = int(n)
@@ -287,11 +301,13 @@ class DevicePairTable:
         n, cap = self.n, self.cap
         out = {"ea": self.t["ea"][:n].cpu().numpy().astype(np.int64),
                "eb": self.t["eb"][:n].cpu().numpy().astype(np.int64)}
-        for k, w in F64_FIELDS.items():
+        for k, w in self._f64().items():
             a = self.t[k].view(w, cap)[:, :n].cpu().numpy() if w > 1 else self.t[k][:n].cpu().numpy()
             out[k] = a.T.copy() if w > 1 else a.copy()
         out["status"] = self.t["status"][:n].cpu().numpy().astype(np.int8)
         out["stick"] = self.t["stick"][:n].cpu().numpy().astype(bool)
+        if self.coating:
+            out["coat_stick"] = self.t["coat_stick"][:n].cpu().numpy().astype(bool)
         return out
 
     def from_host(self, d: dict, n_elems: int | None = None):
@@ -303,7 +319,9 @@ class DevicePairTable:
         cap = self.cap
         self.t["ea"][:n] = torch.as_tensor(np.asarray(d["ea"], dtype=np.int32), device=self.device)
         self.t["eb"][:n] = torch.as_tensor(np.asarray(d["eb"], dtype=np.int32), device=self.device)
-        for k, w in F64_FIELDS.items():
+        for k, w in self._f64().items():
+            if k not in d:  # coating state absent from the source: fresh (zero)
+                continue
             a = np.asarray(d[k], dtype=np.float64).reshape(n, w) if w > 1 else np.asarray(d[k], dtype=np.float64)
             if w > 1:
                 self.t[k].view(w, cap)[:, :n] = torch.as_tensor(a.T.copy(), device=self.device)
@@ -311,15 +329,18 @@ class DevicePairTable:
                 self.t[k][:n] = torch.as_tensor(a, device=self.device)
         self.t["status"][:n] = torch.as_tensor(np.asarray(d["status"]).astype(np.uint8), device=self.device)
         self.t["stick"][:n] = torch.as_tensor(np.asarray(d["stick"]).astype(np.uint8), device=self.device)
+        if self.coating:
+            self.t["coat_stick"][:n] = torch.as_tensor(np.asarray(d.get("coat_stick", np.ones(n, bool)))
+                                                       .astype(np.uint8), device=self.device)
         self.set_n(n)
         self.refresh()
 
     def copy_from(self, other: "DevicePairTable"):
         self.reserve(other.n, keep=False)
         n, cap, oc = other.n, self.cap, other.cap
-        for k in ("ea", "eb", *U8_FIELDS):
+        for k in ("ea", "eb", *self._u8()):
             self.t[k][:n] = other.t[k][:n]
-        for k, w in F64_FIELDS.items():
+        for k, w in self._f64().items():
             for c in range(w):
                 self.t[k][c * cap : c * cap + n] = other.t[k][c * oc : c * oc + n]
         self.set_n(n)
@@ -333,12 +354,13 @@ F32_FIELDS = {"rad": 2, "s": 1, "t": 1, "gap": 1, "normal": 3, "t1": 3, "t2": 3,
 class DevicePairTable32:
     """Slot-ordered float copy of the pair state (``xk_pairs32``) for the mixed per-iteration kernels."""
 
-    def __init__(self, device, per_slot_mu: bool = False):
+    def __init__(self, device, per_slot_mu: bool = False, coating: bool = False):
         self.device = device
         self.cap = 0
         self.t: dict[str, torch.Tensor] = {}
         self.c = L.Pairs32()
         self.per_slot_mu = per_slot_mu  # the mesh has a friction coefficient per element
+        self.coating = coating  # coated wires: coat_total and the coating state per slot
 
     def ensure(self, cap: int):
         if cap <= self.cap:
@@ -351,11 +373,17 @@ class DevicePairTable32:
         t["stick"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         t["mu"] = torch.zeros(cap, dtype=torch.float32, device=self.device) if self.per_slot_mu else None
         t["defer"] = torch.zeros(2 * (cap + 2), dtype=torch.int32, device=self.device)
+        if self.coating:
+            for k, w in (("coat_total", 1), ("coat_cc", 1), ("coat_cc_prev", 1), ("coat_z_t", 2), ("coat_qtn", 1),
+                         ("coat_diss", 1)):
+                t[k] = torch.zeros(w * cap, dtype=torch.float32, device=self.device)
+            t["coat_stick"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         self.t = t
         self.cap = cap
         self.c = L.Pairs32(0, cap, 0, *(ptr(t[k]) for k in (
             "pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
-            "dissipation", "k_pen", "k_t", "status", "stick", "mu", "defer")))
+            "dissipation", "k_pen", "k_t", "status", "stick", "mu")), *(ptr(t.get(k)) for k in L.COAT32_FIELDS),
+            ptr(t["defer"]))
 
 
 # ----------------------------------------------------------------------------- contact pattern

@@ -43,21 +43,33 @@ class AssemblyEngine:
                  k_pen: float, k_t_ratio: float = 0.5, mu: float | np.ndarray = 0.1, smoothing_delta: float = 0.0,
                  g_on: float = 0.0, g_off: float = 1e-6, allow_deactivation: bool = True,
                  exclude_same_layer: bool = True, exclude_shared: bool = True, midpoint_prescreening: bool = True,
-                 prescreening_margin: float = 0.0, margin: float = 0.0, v_ref=None, device=None):
+                 prescreening_margin: float = 0.0, margin: float = 0.0, v_ref=None, device=None,
+                 core_radii=None, coating: dict | None = None):
+        """``core_radii`` and ``coating`` (keys ``stiffness``, ``damping``, ``mu``, ``k_t_ratio``, ``dt``)
+        switch on the coated-wire model of ``KelvinVoigtCoatingProcess``: the gap is taken between the
+        cores and every pair's coating force and friction enter the records (the model is on when the
+        coating stiffness is positive, as in the reference)."""
         self.device = require_cuda(device)
         mu_elem = None
         if np.ndim(mu) > 0:  # one friction coefficient per element (batched strands)
             mu_elem, mu = np.asarray(mu, dtype=np.float64), 0.0
-        self.mesh = DeviceMesh(coords, conn, radii, layer, device=self.device, mu=mu_elem)
+        co = dict(coating or {})
+        self.coated = float(co.get("stiffness", 0.0)) > 0.0
+        if self.coated and core_radii is None:
+            raise ValueError("the coating model needs the core radius of every element")
+        self.mesh = DeviceMesh(coords, conn, radii, layer, device=self.device, mu=mu_elem,
+                               core_radii=core_radii if self.coated else None)
         self.beam = DeviceBeam(self.mesh, section, v_ref=v_ref)
         self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
-        self.cp = L.ContactParams(k_pen, k_t_ratio, mu, smoothing_delta, g_on, g_off, int(allow_deactivation))
+        self.cp = L.ContactParams(k_pen, k_t_ratio, mu, smoothing_delta, g_on, g_off, int(allow_deactivation),
+                                  float(co.get("stiffness", 0.0)), float(co.get("damping", 0.0)),
+                                  float(co.get("mu", 0.0)), float(co.get("k_t_ratio", 0.5)), float(co.get("dt", 0.0)))
         self.bp = L.BPParams(margin, int(exclude_shared), int(exclude_same_layer and layer is not None),
                              int(midpoint_prescreening), prescreening_margin)
         dev = self.device
         nd = self.mesh.ndof
-        self.pairs = DevicePairTable(dev)
-        self._spare = DevicePairTable(dev)
+        self.pairs = DevicePairTable(dev, coating=self.coated)
+        self._spare = DevicePairTable(dev, coating=self.coated)
         self.pattern = DeviceContactPattern(self.mesh)
         self.f_int = torch.zeros(nd, dtype=torch.float64, device=dev)
         self.R = torch.zeros(nd, dtype=torch.float64, device=dev)
@@ -66,7 +78,7 @@ class AssemblyEngine:
         # mixed fast path: float node / element records and the float copy of the pair state
         self.node32 = torch.zeros(L.NODE32_STRIDE * max(self.mesh.n_nodes, 1), dtype=torch.float32, device=dev)
         self.elem32 = torch.zeros(L.ELEM32_STRIDE * max(self.mesh.n_elems, 1), dtype=torch.float32, device=dev)
-        self.pairs32 = DevicePairTable32(dev, per_slot_mu=mu_elem is not None)
+        self.pairs32 = DevicePairTable32(dev, per_slot_mu=mu_elem is not None, coating=self.coated)
         self._state_in32 = False
         self.update_reference_frames()
         self._alloc_outputs()
@@ -133,8 +145,28 @@ class AssemblyEngine:
         self._bp_counts = (int(n_raw.value), int(n_pre.value))
         return self.cands, int(n_out.value)
 
+    def set_coating_dt(self, dt: float):
+        """The step's pseudo-time increment of the coating dashpot (``load_frac - load_frac_prev`` in the
+        reference's Newton loop, ``_newton_steps.py:112``); a captured graph is recorded again."""
+        self.cp.coat_dt = float(dt)
+        self.graph = None
+
+    def end_step(self, stream=None):
+        """At a converged step: coating_compression_prev <- coating_compression for every pair
+        (``contact/solver/process.py:539-545``)."""
+        if not self.coated:
+            return
+        if self._state_in32:
+            t = self.pairs32.t
+            t["coat_cc_prev"].copy_(t["coat_cc"])
+        else:
+            n = self.pairs.n
+            self.pairs.t["coat_cc_prev"][:n].copy_(self.pairs.t["coat_cc"][:n])
+
     def set_pruner(self, pruner, judge_every: int = 10):
         """Use a trained ``PairPruner`` at detection; every ``judge_every``-th detection checks it exactly."""
+        if self.coated:
+            raise NotImplementedError("candidate pruning is not combined with the coating model")
         self.pruner = pruner
         self.judge_every = max(1, int(judge_every))
 
