@@ -372,6 +372,46 @@ def batch_section(args, dev):
     return out
 
 
+def coated_section(args, dev):
+    """The 91-wire strand with coated wires (core radius 0.9 r; coating stiffness 1e4 N/mm, damping 50,
+    coating friction 0.2): every candidate pair is a member and carries the fused coating epilogue.
+    (At strand1027 every candidate pair as a member gives contact rows with more than 256 blocks, the
+    contact pattern's row limit.)"""
+    import torch
+
+    from xkgpu import workloads as W
+    from xkgpu.engine import AssemblyEngine
+
+    w = W.config_workload("strand91", seed=0)
+    st = w.strand
+    r = float(st.radii[0])
+    coat = dict(stiffness=1e4, damping=50.0, mu=0.2, k_t_ratio=0.5, dt=0.1)
+    u0 = torch.as_tensor(w.u, device=dev)
+    rng = np.random.default_rng(11)
+    du = rng.normal(0.0, 2e-4 * w.meta["d"], (st.n_nodes, 6))
+    du[:, 3:] = 0.0
+    u1 = torch.as_tensor(w.u + du.ravel(), device=dev)
+    out = {"workload": "strand91 (91 wires, d = 2 mm, 4 pitches, 32 el/pitch) with coated wires (core 0.9 r, "
+                       "k 1e4, c 50, coating mu 0.2, dt 0.1)", "n_elems": st.n_elems}
+    R = {}
+    for prec in ("fp64", "mixed"):
+        eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=prec, device=dev,
+                             core_radii=0.9 * r, coating=coat, **w.engine_kwargs())
+        stats = eng.detect(u0)
+        eng.end_step()
+        eng.capture(u1, u0)
+        ms = _time_replay(eng, max(5, args.steps // 4), args.warmup)
+        units = st.n_elems + stats["pairs"]
+        out[prec] = {"ms_per_step": ms, "evals_per_s": units / ms * 1e3, "pairs": stats["pairs"],
+                     "members": stats["members"], "contact_blocks": stats["contact_blocks"]}
+        R[prec] = eng.R.double().cpu().numpy()
+        del eng
+        torch.cuda.empty_cache()
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    out["R_err_mixed_vs_fp64"] = float(np.max(np.abs(R["mixed"] - R["fp64"])) / np.max(np.abs(R["fp64"])))
+    return out
+
+
 def rank_aggregate(t_max, n_sum, device=None):
     """Times maxed and unit counts summed over the ranks of the default process group.
 
@@ -583,6 +623,7 @@ def run_gpu(args, rank, world):
         torch.cuda.empty_cache()
         extras["learned_pruning"] = pruning_section(args, dev, w, u0, u1, ms_fp64)
         extras["batched"] = batch_section(args, dev)
+        extras["coated"] = coated_section(args, dev)
 
     # node prep, 2 pair kernels, 2 beam colours, then either element sums + tangent gather + residual from
     # the element sums (norm fused) or tangent gather + force gather + 2 norm kernels

@@ -401,7 +401,9 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_other(xk_mesh m, xk_pairs p, co
 
 // Contributing pairs: narrowphase, Huber normal force, Coulomb return mapping
 // and the pair tangent, one record (s, t, v, B) per member.
-template <int P, int OUT>
+// COAT: the coated-wire epilogue is compiled in (a launch with coating selects it), so the plain
+// kernel keeps its registers.
+template <int P, int OUT, bool COAT>
 __global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, const int32_t* __restrict__ members,
                                                         const int32_t* __restrict__ mnodes, int n_m,
                                                         const double* __restrict__ u, const double* __restrict__ u_ref,
@@ -538,7 +540,7 @@ __global__ void __launch_bounds__(PAIR_T) k_pair_member(xk_mesh m, xk_pairs p, c
   T vc[3] = {T(0), T(0), T(0)}, Bc[9];
   for (int k = 0; k < 9; ++k) Bc[k] = T(0);
   constexpr int ALL = XK_STAGE_NORMAL | XK_STAGE_FRICTION | XK_STAGE_TANGENT;
-  if (OUT == XK_OUT_COMBINED && m.core_radii && p.coat_cc && (stages & ALL) == ALL) {
+  if (COAT && OUT == XK_OUT_COMBINED && m.core_radii && p.coat_cc && (stages & ALL) == ALL) {
     T duc[4][3];
     for (int k = 0; k < 4; ++k)
       for (int c = 0; c < 3; ++c) {
@@ -1164,15 +1166,24 @@ extern "C" xk_status xk_pair_step(const xk_mesh* m, xk_pairs* p, const xk_contac
   if (pat->n_members == 0 || (stages & XK_STAGE_NO_MEMBERS)) return XK_OK;
   const int nb = xk_blocks(pat->n_members, PAIR_T);
   const long long rs = out_mode == XK_OUT_COMBINED ? XK_REC_STRIDE_COMBINED : XK_REC_STRIDE_SPLIT;
-#define XK_MEMBER_LAUNCH(PP, OO, TT)                                                                                \
-  k_pair_member<PP, OO><<<nb, PAIR_T, 0, st>>>(*m, *p, pat->members, pat->member_nodes, pat->n_members, u, u_ref, \
-                                               *cp, stages, (TT*)rec, rs)
+  const bool coat = m->core_radii && p->coat_cc;
+#define XK_MEMBER_LAUNCH(PP, OO, CC, TT)                                                                        \
+  k_pair_member<PP, OO, CC><<<nb, PAIR_T, 0, st>>>(*m, *p, pat->members, pat->member_nodes, pat->n_members, u,  \
+                                                   u_ref, *cp, stages, (TT*)rec, rs)
   if (precision == XK_FP64) {
-    if (out_mode == XK_OUT_COMBINED) XK_MEMBER_LAUNCH(XK_FP64, XK_OUT_COMBINED, double);
-    else XK_MEMBER_LAUNCH(XK_FP64, XK_OUT_SPLIT, double);
+    if (out_mode == XK_OUT_COMBINED) {
+      if (coat) XK_MEMBER_LAUNCH(XK_FP64, XK_OUT_COMBINED, true, double);
+      else XK_MEMBER_LAUNCH(XK_FP64, XK_OUT_COMBINED, false, double);
+    } else {
+      XK_MEMBER_LAUNCH(XK_FP64, XK_OUT_SPLIT, false, double);
+    }
   } else if (precision == XK_MIXED) {
-    if (out_mode == XK_OUT_COMBINED) XK_MEMBER_LAUNCH(XK_MIXED, XK_OUT_COMBINED, float);
-    else XK_MEMBER_LAUNCH(XK_MIXED, XK_OUT_SPLIT, float);
+    if (out_mode == XK_OUT_COMBINED) {
+      if (coat) XK_MEMBER_LAUNCH(XK_MIXED, XK_OUT_COMBINED, true, float);
+      else XK_MEMBER_LAUNCH(XK_MIXED, XK_OUT_COMBINED, false, float);
+    } else {
+      XK_MEMBER_LAUNCH(XK_MIXED, XK_OUT_SPLIT, false, float);
+    }
   } else {
     return xk_set_error(XK_ERR_ARG, "xk_pair_step: precision");
   }
