@@ -479,6 +479,38 @@ xk_status xk_add_diagonal(int64_t n, const int64_t* idx, const double* m, double
                           xk_stream s);
 
 /* ------------------------------------------------------------------------
+ * The Newton step's linear system on the device.  LinearSolveProcess
+ * (xkep_cae/contact/solver/_newton_steps.py:338-366) solves K du = -R with the
+ * rows and columns of the Dirichlet DOFs replaced by the identity, by a
+ * sparse direct factorisation on the host.  Here K = K_beam + K_c stays in the
+ * engine's block formats and is solved iteratively.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t n_nodes;
+  int32_t precision;            /* values double (XK_FP64) or float (XK_MIXED) */
+  const int32_t* kb_row_ptr;    /* K_beam: 6x6 block CSR over the nodes [n_nodes+1] */
+  const int32_t* kb_col;
+  const void* kb_vals;          /* 36 per block, row-major */
+  const int32_t* kc_row_ptr;    /* K_c: 3x3 block CSR over the nodes' translational DOFs (nullable) */
+  const int32_t* kc_col;
+  const void* kc_vals;          /* 9 per block */
+  const uint8_t* fixed;         /* [6*n_nodes] Dirichlet DOFs (nullable): identity rows and columns */
+} xk_system;
+
+/* y = A x with A = K_beam + K_c, Dirichlet rows and columns as the identity; x, y double [6*n_nodes]. */
+xk_status xk_system_spmv(const xk_system* A, const double* x, double* y, xk_stream s);
+/* dinv[36 v ...]: the inverse of every node's 6x6 diagonal block of A (the block-Jacobi preconditioner). */
+xk_status xk_system_block_jacobi(const xk_system* A, double* dinv, xk_stream s);
+/* BiCGStab with the block-Jacobi preconditioner dinv, from the initial x: until
+ * ||b - A x|| <= rtol ||b|| (checked every check_every iterations) or max_iter.
+ * work: double [8*6*n_nodes + 2*304 + 8].  The reductions are fixed-order, so
+ * a solve is repeatable bit for bit; the iteration's scalars stay on the
+ * device.  *iters and *rel_res (host, nullable) report the run. */
+xk_status xk_bicgstab(const xk_system* A, const double* b, double* x, const double* dinv, double* work,
+                      int32_t max_iter, int32_t check_every, double rtol, int32_t* iters, double* rel_res,
+                      xk_stream s);
+
+/* ------------------------------------------------------------------------
  * Learned pruning of broadphase candidates.  No counterpart in the reference:
  * an MLP (XK_MLP_IN inputs -> 64 -> 64 -> 64 -> 1, ReLU, BF16 weights and
  * activations, FP32 accumulation) scores each candidate pair; candidates below

@@ -51,6 +51,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(L.ContactParams) == 6 * 8 + 8 + 5 * 8
     assert C.sizeof(L.BPParams) == 8 + 3 * 4 + 4 + 8
     assert C.sizeof(L.ContactPattern) == 16 + 5 * 8 + 10 * 8 + 2 * 8 + 7 * 8
+    assert C.sizeof(L.System) == 8 + 7 * 8
 
 
 def test_argument_checks_before_any_launch(lib):
@@ -65,3 +66,10 @@ def test_argument_checks_before_any_launch(lib):
     assert lib.xk_mlp_forward_tcgen05(0x1000, 0x2000, -1, 0x3000, 0x4000, None) == 1
     assert lib.xk_mlp_forward_tcgen05(0x1000, 0x2004, 8, 0x3000, 0x4000, None) == 1
     assert b"16-byte aligned" in lib.xk_last_error()
+    # the device linear solve: null system, check interval below one
+    from xkgpu import _lib as L
+
+    assert lib.xk_bicgstab(None, None, None, None, None, 10, 1, 1e-8, None, None, None) == 1
+    s = L.System(4, 0, 0x1000, 0x2000, 0x3000, None, None, None, None)
+    assert lib.xk_bicgstab(C.byref(s), 0x1000, 0x2000, 0x3000, 0x4000, 10, 0, 1e-8, None, None, None) == 1
+    assert lib.xk_system_spmv(None, 0x1000, 0x2000, None) == 1

@@ -79,6 +79,11 @@ class ContactParams(C.Structure):
         (n, C.c_double) for n in ("coat_k", "coat_c", "coat_mu", "coat_kt_ratio", "coat_dt")]
 
 
+class System(C.Structure):
+    _fields_ = [("n_nodes", C.c_int32), ("precision", C.c_int32)] + [
+        (n, vp) for n in ("kb_row_ptr", "kb_col", "kb_vals", "kc_row_ptr", "kc_col", "kc_vals", "fixed")]
+
+
 class BPParams(C.Structure):
     _fields_ = [("margin", C.c_double), ("exclude_shared", C.c_int32), ("exclude_same_layer", C.c_int32),
                 ("midpoint_prescreening", C.c_int32), ("prescreening_margin", C.c_double)]
@@ -139,7 +144,11 @@ SIGNATURES = {
     "xk_mlp_to_bf16": [vp, vp, vp],
     "xk_prune_select": [vp, C.c_int64, vp, vp, C.c_float, C.c_int, vp, i64p, vp],
     "xk_pairs_drop_pristine": [P(Pairs), vp, C.c_int64, P(Pairs), vp],
+    "xk_system_spmv": [P(System), vp, vp, vp],
+    "xk_system_block_jacobi": [P(System), vp, vp],
+    "xk_bicgstab": [P(System), vp, vp, vp, vp, C.c_int32, C.c_int32, C.c_double, P(C.c_int32), P(C.c_double), vp],
 }
+SOLVE_REDUCE_BLOCKS = 304
 MLP_IN, MLP_HIDDEN, MLP_PARAMS, MLP_ACT = 8, 64, 8961, 192
 JACOBIAN_NOALLOC_MAX_PAIRS = 1048576
 NODE32_STRIDE = 16

@@ -7,8 +7,9 @@ assembly (``AssemblyEngine.assemble``: R and K_T), the time integrator's
 effective residual / stiffness, the convergence check and a linear solve with
 the Dirichlet DOFs eliminated (rows and columns replaced by the identity, as
 ``LinearSolveProcess``, ``_newton_steps.py:338-366``).  The linear solve runs on
-the host (scipy by default, or any ``solver(K, rhs)``); it is not part of the
-assembly path.
+the host (scipy by default, or any ``solver(K, rhs)``), or with
+``solver="device"`` on the GPU (``DeviceLinearSolver``: BiCGStab on the
+engine's block matrices), so that no matrix leaves the device.
 """
 
 from __future__ import annotations
@@ -21,6 +22,7 @@ import scipy.sparse.linalg as spla
 import torch
 
 from .dynamics import QuasiStatic
+from .solve import DeviceLinearSolver
 
 
 @dataclass
@@ -47,14 +49,25 @@ def solve_increment(engine, u_start: torch.Tensor, u_ref: torch.Tensor, *, f_ext
     Convergence: ``||R|| <= tol * f_ref`` with ``f_ref`` the first residual norm
     unless given.  ``fixed``: boolean per DOF (host).  ``graph``: record the
     assembly once as a CUDA graph on static buffers and replay it every
-    iteration.
+    iteration.  ``solver``: ``None`` (scipy's direct solve), ``"device"`` (a
+    ``DeviceLinearSolver``), a ``DeviceLinearSolver`` instance, or any host
+    ``solver(K, rhs)``.
     """
     dyn = dynamics if dynamics is not None else QuasiStatic()
-    solve = solver if solver is not None else (lambda K, b: spla.spsolve(K, b))
+    dsolve = None
+    if isinstance(solver, DeviceLinearSolver):
+        dsolve = solver
+    elif isinstance(solver, str):
+        if solver != "device":
+            raise ValueError(f"unknown solver {solver!r}")
+        dsolve = DeviceLinearSolver(engine)
+    solve = solver if callable(solver) and dsolve is None else (lambda K, b: spla.spsolve(K, b))
     nd = engine.mesh.ndof
     fx = np.zeros(nd, dtype=bool) if fixed is None else np.asarray(fixed, dtype=bool)
     fx_dev = torch.as_tensor(fx.astype(np.uint8), device=engine.device)
     free_dev = torch.as_tensor(~fx, device=engine.device)
+    if dsolve is not None:
+        dsolve.set_fixed(fx)
     if detect:
         engine.detect(u_start)
     u = dyn.predict(u_start, dt) if dyn.is_dynamic else u_start.clone()
@@ -82,6 +95,14 @@ def solve_increment(engine, u_start: torch.Tensor, u_ref: torch.Tensor, *, f_ext
             return NewtonResult(u, True, it, history)
         if it == max_iter:
             break
+        if dsolve is not None:
+            if dyn.is_dynamic:
+                dyn.add_mass_to(engine.K_beam, engine.beam.diag_index(), dt, engine.precision)
+            rhs = torch.where(free_dev, -R.to(torch.float64), torch.zeros((), dtype=torch.float64,
+                                                                            device=engine.device))
+            du = dsolve.solve(rhs)
+            u = u + torch.where(free_dev, du, torch.zeros_like(du))
+            continue
         K = engine.K_total_csr()
         if dyn.is_dynamic:
             K = dyn.effective_stiffness(K, dt)
