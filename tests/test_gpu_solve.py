@@ -100,3 +100,22 @@ def test_dynamic_newton_device_solve_matches_host_solve():
             u = res.u
         us[solver] = u.cpu().numpy()
     assert rel_err(us["device"], us[None]) < 1e-7
+
+
+def test_unconverged_solve_raises():
+    """At the workload state (initial penetration, k_pen = 1e3 EA/L, mu = 0.1) the tangent is indefinite:
+    a short solve must raise instead of returning an unconverged increment."""
+    from xkgpu import workloads as W
+    from xkgpu.engine import AssemblyEngine
+    from xkgpu.solve import LinearSolveError
+
+    w = W.config_workload("strand7", seed=0)
+    st = w.strand
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="fp64", **w.engine_kwargs())
+    u = torch.as_tensor(w.u, device="cuda")
+    eng.detect(u)
+    R = eng.assemble(u, u)
+    ds = DeviceLinearSolver(eng, rtol=1e-12, max_iter=50)
+    with pytest.raises(LinearSolveError):
+        ds.solve(-R.double())
+    assert ds.iterations == 50 and not ds.rel_res <= 1e-12
