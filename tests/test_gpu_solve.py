@@ -118,4 +118,4 @@ def test_unconverged_solve_raises():
     ds = DeviceLinearSolver(eng, rtol=1e-12, max_iter=50)
     with pytest.raises(LinearSolveError):
         ds.solve(-R.double())
-    assert ds.iterations == 50 and not ds.rel_res <= 1e-12
+    assert 0 < ds.iterations <= 50 and not ds.rel_res <= 1e-12
