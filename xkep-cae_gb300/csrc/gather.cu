@@ -678,18 +678,29 @@ XK_D void add_term(const T* __restrict__ S, const T* __restrict__ rec, int code,
   }
 }
 
+// The grid is persistent (as many CTAs per SM as are resident, each taking every gridDim.x-th tile of
+// GS_T blocks): a thread loads its code of the CTA's next tile before it gathers the terms of the
+// current one, so the code load's latency hides behind the term loads.
+XK_D int4 sides_code(const int4* __restrict__ codes, long long nnzb, long long tile) {
+  const long long b = tile * GS_T + threadIdx.x;
+  return b < nnzb ? __ldcs(codes + b) : make_int4(-1, -1, -1, -1);
+}
+
 template <typename T, int RS, int BCOL>
 __global__ void __launch_bounds__(GS_T, sizeof(T) == 4 ? 16 : 8) k_gather_tangent_sides(long long nnzb, const int4* __restrict__ codes,
                                                                const T* __restrict__ S, const T* __restrict__ rec,
                                                                T* __restrict__ K) {
   __shared__ __align__(16) T stage[GS_T * 9];
-  const long long b0 = (long long)blockIdx.x * GS_T;
-  const long long b = b0 + threadIdx.x;
-  T acc[9];
+  const long long ntiles = (nnzb + GS_T - 1) / GS_T;
+  long long tile = blockIdx.x;
+  int4 cn = tile < ntiles ? sides_code(codes, nnzb, tile) : make_int4(-1, -1, -1, -1);
+  for (; tile < ntiles; tile += gridDim.x) {
+    const long long b0 = tile * GS_T;
+    const int4 c = cn;
+    if (tile + gridDim.x < ntiles) cn = sides_code(codes, nnzb, tile + gridDim.x);
+    T acc[9];
 #pragma unroll
-  for (int q = 0; q < 9; ++q) acc[q] = T(0);
-  if (b < nnzb) {
-    const int4 c = codes[b];
+    for (int q = 0; q < 9; ++q) acc[q] = T(0);
     if (RS == XK_REC_STRIDE_COMBINED) {
       // each term is the first twelve values of its element sum or member record
       sides_term<T>(S, rec, c.x, acc);
@@ -702,22 +713,36 @@ __global__ void __launch_bounds__(GS_T, sizeof(T) == 4 ? 16 : 8) k_gather_tangen
       add_term<T, RS, BCOL>(S, rec, c.z, acc);
       add_term<T, RS, BCOL>(S, rec, c.w, acc);
     }
-  }
 #pragma unroll
-  for (int q = 0; q < 9; ++q) stage[threadIdx.x * 9 + q] = acc[q];
-  __syncthreads();
-  const long long rem = nnzb - b0;
-  const int nv = 9 * (int)(rem < GS_T ? rem : GS_T);
-  T* out = K + 9 * b0;
-  if (sizeof(T) == 4 && ((uintptr_t)out & 15) == 0) {
-    // 16-byte stores of the staged values (a CTA's 128 blocks are 4608 bytes)
-    const int n4 = nv / 4;
-    for (int v = threadIdx.x; v < n4; v += GS_T)
-      reinterpret_cast<float4*>(out)[v] = reinterpret_cast<const float4*>(stage)[v];
-    for (int v = 4 * n4 + threadIdx.x; v < nv; v += GS_T) out[v] = stage[v];
-  } else {
-    for (int v = threadIdx.x; v < nv; v += GS_T) out[v] = stage[v];
+    for (int q = 0; q < 9; ++q) stage[threadIdx.x * 9 + q] = acc[q];
+    __syncthreads();
+    const long long rem = nnzb - b0;
+    const int nv = 9 * (int)(rem < GS_T ? rem : GS_T);
+    T* out = K + 9 * b0;
+    if (sizeof(T) == 4 && ((uintptr_t)out & 15) == 0) {
+      // 16-byte stores of the staged values (a CTA's 128 blocks are 4608 bytes)
+      const int n4 = nv / 4;
+      for (int v = threadIdx.x; v < n4; v += GS_T)
+        reinterpret_cast<float4*>(out)[v] = reinterpret_cast<const float4*>(stage)[v];
+      for (int v = 4 * n4 + threadIdx.x; v < nv; v += GS_T) out[v] = stage[v];
+    } else {
+      for (int v = threadIdx.x; v < nv; v += GS_T) out[v] = stage[v];
+    }
+    __syncthreads();  // the stage is read out before the next tile overwrites it
   }
+}
+
+// persistent grid of the sides gather: every SM's share of CTAs, or one CTA per tile when fewer
+int sides_grid(long long nnzb, int per_sm) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+  }
+  const long long tiles = (nnzb + GS_T - 1) / GS_T;
+  const long long cap = (long long)sms * per_sm;
+  return (int)(tiles < cap ? (tiles > 0 ? tiles : 1) : cap);
 }
 
 
@@ -1172,7 +1197,7 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
       else if (ne > 0)                                                                                      \
         k_elem_sums<TT, RSV, BC><<<xk_blocks(9LL * ne, 256), 256, 0, st>>>(ne, pat->elem_ptr, pat->elem_inc,   \
                                                                            (const TT*)rec, (TT*)pat->elem_sums); \
-      k_gather_tangent_sides<TT, RSV, BC><<<xk_blocks(pat->nnzb, GS_T), GS_T, 0, st>>>(                     \
+      k_gather_tangent_sides<TT, RSV, BC><<<sides_grid(pat->nnzb, sizeof(TT) == 4 ? 16 : 8), GS_T, 0, st>>>( \
           pat->nnzb, reinterpret_cast<const int4*>(pat->bcodes), (const TT*)pat->elem_sums, (const TT*)rec,    \
           (TT*)Kc_vals);                                                                                    \
     } else if (chunks)                                                                                      \
