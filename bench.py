@@ -177,7 +177,9 @@ def gather_tangent_bytes(n_members, n_contrib, nnzb, mixed: bool, sides: bool = 
     """Algorithmic DRAM bytes of one contact-tangent gather (all its launches).
 
     Each contributing pair's record is read once (16 values: 64 B float, 128 B
-    double) and each 3x3 block written once (36 B float, 72 B double); re-reads
+    double) and each stored 3x3 block (row <= column; the block at the mirrored
+    position has the same values and is not written) once (36 B float, 72 B
+    double); re-reads
     of a record by the blocks it feeds are L2 traffic.  Contributor-list
     schedules also read each list entry (4 B) and block pointer (4 B).  The
     element-side schedule instead reads each member's two element-incidence
@@ -403,7 +405,8 @@ def coated_section(args, dev):
         ms = _time_replay(eng, max(5, args.steps // 4), args.warmup)
         units = st.n_elems + stats["pairs"]
         out[prec] = {"ms_per_step": ms, "evals_per_s": units / ms * 1e3, "pairs": stats["pairs"],
-                     "members": stats["members"], "contact_blocks": stats["contact_blocks"]}
+                     "members": stats["members"], "contact_blocks": stats["contact_blocks"],
+                     "contact_blocks_full_matrix": stats["contact_blocks_full"]}
         R[prec] = eng.R.double().cpu().numpy()
         del eng
         torch.cuda.empty_cache()
@@ -617,6 +620,7 @@ def run_gpu(args, rank, world):
     mixed_variant = engines["mixed"].gather_variant
     fp64_variant = engines["fp64"].gather_variant
     contact_blocks = engines["mixed"].pattern.nnzb
+    contact_blocks_full = engines["mixed"].pattern.nnzb_full
     extras = {}
     if not args.no_extras and world == 1:
         del engines, eng
@@ -637,6 +641,7 @@ def run_gpu(args, rank, world):
                                "24 el/pitch, gap -0.005 d, seeded noise", "n_nodes": st.n_nodes,
                    "n_elems": n_e, "n_pairs": n_c, "raw_aabb_pairs": results["mixed"]["stats"]["raw"],
                    "contributing_pairs": m, "contact_blocks": contact_blocks,
+                   "contact_blocks_full_matrix": contact_blocks_full,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (pair table alone > 1 GB)", "cuda_graph": True},
         "fp64_plain": {"value": units / t_fp64 * args.steps, "ms_per_step": ms_fp64,

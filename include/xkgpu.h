@@ -219,12 +219,19 @@ xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double* u, const x
 /* The pairs that can contribute in an increment ("members": status != INACTIVE
  * or p_n > 0 after detection and the active-set update), the rest, the node
  * incidence of the members and the block pattern of K_c with each block's
- * contributor list.  Built once per increment; every array is caller-owned. */
+ * contributor list.  Built once per increment; every array is caller-owned.
+ *
+ * Block storage of K_c: a member adds c_k c_l B to block (node_k, node_l) and
+ * the same c_l c_k B to block (node_l, node_k), so the block at (w, v) always
+ * equals the block at (v, w) (the same 3x3 values, not the transpose).  The
+ * pattern, and every K_c written by the gathers, hold the blocks with
+ * row <= column only, in (row, column) order; the full matrix has the mirror
+ * of every off-diagonal stored block as well (nnzb_full blocks in all). */
 typedef struct {
   int32_t n_nodes;
   int32_t n_members, n_others;
-  int64_t nnzb;        /* contact blocks */
-  int64_t n_contrib;   /* 16 per member */
+  int64_t nnzb;        /* stored contact blocks (row <= column) */
+  int64_t n_contrib;   /* contributions to the stored blocks (set by the build) */
   int64_t cap_members, cap_others, cap_blocks;
   int32_t* members;      /* [cap_members] pair index of each member, ascending */
   int32_t* member_nodes; /* [4*cap_members] nodes A0 A1 B0 B1 of each member */
@@ -257,6 +264,12 @@ typedef struct {
   double* norm_scratch;   /* [(6*n_nodes + 255)/256 + 1] zero-initialised scratch of
                            * xk_contact_gather_force_elem's fused norm (block sums and a counter
                            * that each launch leaves at zero) */
+  /* Lower index (built when both are non-NULL): for node w, low_blk[low_ptr[w] ..
+   * low_ptr[w+1]) are the stored blocks (v, w) with v < w, ascending in v; the
+   * full row w of K_c is those blocks' mirrors followed by the stored row. */
+  int64_t nnzb_full;      /* set by the build: blocks of the full matrix (nnzb without the index) */
+  int32_t* low_ptr;       /* [n_nodes+1] */
+  int32_t* low_blk;       /* [cap_blocks] */
 } xk_contact_pattern;
 
 /* Returns XK_ERR_CAPACITY (with n_members, n_others, nnzb set) when a capacity
@@ -293,8 +306,9 @@ xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec
                                   int which, const double* base, double scale, const double* f_ext,
                                   const uint8_t* fixed, double* out, double* norm2, xk_stream s);
 
-/* K_c block values (9 per block, double|float, nnzb blocks): sum over each
- * block's contributors of c_k c_l B; which selects B_n - B_f (combined
+/* K_c block values (9 per block, double|float, the nnzb stored blocks of the
+ * pattern, row <= column; each off-diagonal one is also the block at the
+ * mirrored position): sum over each block's contributors of c_k c_l B; which selects B_n - B_f (combined
  * records), B_n or B_f (split records).  variant picks the reduction schedule
  * (0 default, 1 one contributor per lane, 2 chunks of contributors per lane,
  * 3 element-side sums plus per-block cross lists, which needs the element-side
@@ -491,13 +505,17 @@ typedef struct {
   const int32_t* kb_row_ptr;    /* K_beam: 6x6 block CSR over the nodes [n_nodes+1] */
   const int32_t* kb_col;
   const void* kb_vals;          /* 36 per block, row-major */
-  const int32_t* kc_row_ptr;    /* K_c: 3x3 block CSR over the nodes' translational DOFs (nullable) */
-  const int32_t* kc_col;
+  const int32_t* kc_row_ptr;    /* K_c: the stored (row <= column) 3x3 blocks of xk_contact_pattern over */
+  const int32_t* kc_col;        /*   the nodes' translational DOFs (nullable) */
   const void* kc_vals;          /* 9 per block */
+  const int32_t* kc_blk_row;    /* the pattern's blk_row, low_ptr and low_blk: the mirrored blocks */
+  const int32_t* kc_low_ptr;
+  const int32_t* kc_low_blk;
   const uint8_t* fixed;         /* [6*n_nodes] Dirichlet DOFs (nullable): identity rows and columns */
 } xk_system;
 
-/* y = A x with A = K_beam + K_c, Dirichlet rows and columns as the identity; x, y double [6*n_nodes]. */
+/* y = A x with A = K_beam + K_c (K_c's stored blocks and their mirrors), Dirichlet rows and columns
+ * as the identity; x, y double [6*n_nodes]. */
 xk_status xk_system_spmv(const xk_system* A, const double* x, double* y, xk_stream s);
 /* dinv[36 v ...]: the inverse of every node's 6x6 diagonal block of A (the block-Jacobi preconditioner). */
 xk_status xk_system_block_jacobi(const xk_system* A, double* dinv, xk_stream s);

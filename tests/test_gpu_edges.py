@@ -127,6 +127,16 @@ def test_table_growth_then_separation(prec):
     Kb, fb = _beam_only(st.coords, st.conn, u, w.section)
     assert rel_err(eng.R.cpu().numpy(), fb + fc) < TOL[prec]
     assert sparse_rel_err(eng.K_contact_csr(), Kc) < TOL[prec]
+    # stored blocks: row <= column; the lower index lists every off-diagonal one under its column
+    pat = eng.pattern
+    nb = pat.nnzb
+    r, c = pat.blk_row[:nb].cpu().numpy(), pat.col[:nb].cpu().numpy()
+    assert np.all(r <= c)
+    lp = pat.low_ptr.cpu().numpy()
+    lb = pat.low_blk[: lp[-1]].cpu().numpy()
+    assert pat.nnzb_full == nb + int(np.sum(r != c)) == nb + lp[-1]
+    assert np.array_equal(np.sort(lb), np.nonzero(r != c)[0])
+    assert np.all(c[lb] == np.repeat(np.arange(st.n_nodes), np.diff(lp)))
     # 3. pushed apart again: every pair stays in the table and switches off
     eng.detect(_dev(u_far))
     table = oracle_detect(table, u_far)

@@ -8,6 +8,13 @@
 // local node k is c_k v and its tangent block (k, l) is c_k c_l B with
 // c = [1-s, s, -(1-t), -t].  Each node sums its incident members and each
 // K_c block sums its contributor list, both in a fixed order.
+//
+// Every contribution to block (v, w) is c_k c_l B and the same member gives
+// c_l c_k B to block (w, v): the block at (w, v) equals the block at (v, w)
+// (the same 3x3 values, not the transpose; K_c itself is not symmetric once
+// friction acts).  So the pattern holds the blocks with row <= column only
+// ("upper" blocks), each computed once, and a lower index lists, per node w,
+// the stored blocks (v, w) with v < w, for readers that need whole rows.
 #include "xk_common.cuh"
 
 xk_status xk_sumsq_into(const double* x, long long n, double* out, cudaStream_t s);
@@ -91,7 +98,8 @@ __global__ void k_segment_sort(const int32_t* __restrict__ ptr, long long nseg, 
   }
 }
 
-// MODE 0: count the distinct column nodes of each row; MODE 1: write them sorted.
+// MODE 0: count the distinct column nodes c >= v of each row v; MODE 1: write them sorted.  The
+// capacity check covers all the row's column nodes.
 template <int MODE>
 __global__ void k_row_cols(const int32_t* __restrict__ mnodes, const int32_t* __restrict__ ptr,
                            const int32_t* __restrict__ inc, int n_nodes, int32_t* __restrict__ rcnt,
@@ -114,15 +122,29 @@ __global__ void k_row_cols(const int32_t* __restrict__ mnodes, const int32_t* __
       ++n;
     }
   }
+  int lo = 0;  // first column >= v
+  while (lo < n && buf[lo] < v) ++lo;
   if (MODE == 0) {
-    rcnt[v] = n;
+    rcnt[v] = n - lo;
   } else {
-    const int o = rptr[v];
-    for (int k = 0; k < n; ++k) {
+    const int o = rptr[v] - lo;
+    for (int k = lo; k < n; ++k) {
       col[o + k] = buf[k];
       brow[o + k] = v;
     }
   }
+}
+
+// Lower index: per node w, the stored blocks (v, w) with v < w in the order of v (MODE 0 counts).
+template <int MODE>
+__global__ void k_lower_index(long long nb, const int32_t* __restrict__ brow, const int32_t* __restrict__ col,
+                              int32_t* __restrict__ cnt, const int32_t* __restrict__ lptr, int32_t* __restrict__ lblk) {
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const int w = col[b];
+  if (brow[b] == w) return;
+  if (MODE == 0) atomicAdd(&cnt[w], 1);
+  else lblk[lptr[w] + atomicAdd(&cnt[w], 1)] = (int)b;
 }
 
 XK_D int find_block(const int32_t* __restrict__ rptr, const int32_t* __restrict__ col, int row, int c) {
@@ -145,6 +167,7 @@ __global__ void k_contrib(const int32_t* __restrict__ mnodes, int nm, const int3
   for (int q = 0; q < 4; ++q) nd[q] = mnodes[4LL * mi + q];
   for (int k = 0; k < 4; ++k)
     for (int l = 0; l < 4; ++l) {
+      if (nd[k] > nd[l]) continue;  // a lower block: the same values as its stored mirror
       const int b = find_block(rptr, col, nd[k], nd[l]);
       if (b >= rptr[nd[k] + 1] || col[b] != nd[l]) {  // cannot happen for a consistent pattern
         atomicOr(err, 2);
@@ -335,7 +358,7 @@ __global__ void k_cross_codes(const int32_t* __restrict__ mnodes, int nm, const 
   for (int q = 0; q < 4; ++q) nd[q] = mnodes[4LL * mi + q];
   for (int k = 0; k < 4; ++k)
     for (int l = 0; l < 4; ++l) {
-      if ((k >> 1) == (l >> 1)) continue;
+      if ((k >> 1) == (l >> 1) || nd[k] > nd[l]) continue;
       const int b = find_block(rptr, col, nd[k], nd[l]);
       if (b >= rptr[nd[k] + 1] || col[b] != nd[l]) {
         atomicOr(err, 2);
@@ -1012,7 +1035,6 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   if (herr) return xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: a node touches more than 256 contact nodes");
   const long long nb = h[1];
   pat->nnzb = nb;
-  pat->n_contrib = 16 * nm;
   if (nb > pat->cap_blocks) return xk_set_error(XK_ERR_CAPACITY, "xk_contact_pattern_build: block capacity too small");
   k_row_cols<1><<<xk_blocks(nn, 64), 64, 0, st>>>(pat->member_nodes, pat->inc_ptr, pat->inc, nn, nullptr,
                                                    pat->row_ptr, pat->col, pat->blk_row, err);
@@ -1025,12 +1047,29 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   if (nm > 0) k_contrib<0><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
                                                                 bcnt, nullptr, nullptr, err);
   XK_CHECK_LAUNCH();
-  XK_TRY(xk_exclusive_scan_i32(bcnt, pat->blk_ptr, nb + 1, nullptr, st));
+  XK_TRY(xk_exclusive_scan_i32(bcnt, pat->blk_ptr, nb + 1, tot + 2, st));
   XK_CUDA(cudaMemsetAsync(bfill, 0, sizeof(int32_t) * (nb + 1), st));
   if (nm > 0) k_contrib<1><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
                                                                 bfill, pat->blk_ptr, pat->contrib, err);
   if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
   XK_CHECK_LAUNCH();
+  // lower index of the stored blocks
+  pat->nnzb_full = nb;
+  if (pat->low_ptr && pat->low_blk) {
+    XK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nn + 1), st));
+    if (nb > 0) k_lower_index<0><<<xk_blocks(nb, 256), 256, 0, st>>>(nb, pat->blk_row, pat->col, cnt, nullptr, nullptr);
+    XK_CHECK_LAUNCH();
+    XK_TRY(xk_exclusive_scan_i32(cnt, pat->low_ptr, nn + 1, tot + 3, st));
+    XK_CUDA(cudaMemsetAsync(fill, 0, sizeof(int32_t) * (nn + 1), st));
+    if (nb > 0)
+      k_lower_index<1><<<xk_blocks(nb, 256), 256, 0, st>>>(nb, pat->blk_row, pat->col, fill, pat->low_ptr,
+                                                           pat->low_blk);
+    k_segment_sort<<<xk_blocks(nn, 128), 128, 0, st>>>(pat->low_ptr, nn, pat->low_blk);
+    XK_CHECK_LAUNCH();
+  }
+  XK_TRY(fetch_i64(tot, h, 4, st));
+  pat->n_contrib = h[2];
+  if (pat->low_ptr && pat->low_blk) pat->nnzb_full = nb + h[3];
   // element-side form (gather variant XK_GATHER_SIDES)
   const bool sides = pat->node_elem_ptr && pat->node_elem && pat->elem_ptr && pat->elem_inc && pat->bcodes;
   const int ne = m->n_elems;

@@ -40,6 +40,17 @@ __global__ void k_spmv(xk_system A, const double* __restrict__ x, double* __rest
   }
   if (d < 3 && A.kc_vals) {
     const T* kc = (const T*)A.kc_vals;
+    // the stored blocks (u, v), u < v, are also the blocks (v, u): row v's entries left of the diagonal
+    for (int q = A.kc_low_ptr[v]; q < A.kc_low_ptr[v + 1]; ++q) {
+      const int b = A.kc_low_blk[q];
+      const int u = A.kc_blk_row[b];
+      const T* blk = kc + 9LL * b + 3 * d;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const long long col = 6LL * u + j;
+        if (!(A.fixed && A.fixed[col])) acc = fma((double)blk[j], x[col], acc);
+      }
+    }
     for (int b = A.kc_row_ptr[v]; b < A.kc_row_ptr[v + 1]; ++b) {
       const int w = A.kc_col[b];
       const T* blk = kc + 9LL * b + 3 * d;
@@ -257,8 +268,12 @@ xk_status dot2(long long n, const double* a0, const double* b0, const double* a1
 
 }  // namespace
 
+static bool kc_complete(const xk_system* A) {
+  return !A->kc_vals || (A->kc_row_ptr && A->kc_col && A->kc_blk_row && A->kc_low_ptr && A->kc_low_blk);
+}
+
 extern "C" xk_status xk_system_spmv(const xk_system* A, const double* x, double* y, xk_stream s) {
-  if (!A || !x || !y || !A->kb_row_ptr || !A->kb_col || !A->kb_vals)
+  if (!A || !x || !y || !A->kb_row_ptr || !A->kb_col || !A->kb_vals || !kc_complete(A))
     return xk_set_error(XK_ERR_ARG, "xk_system_spmv: null argument");
   if (A->n_nodes <= 0) return XK_OK;
   spmv_any(*A, x, y, (cudaStream_t)s);
@@ -267,7 +282,7 @@ extern "C" xk_status xk_system_spmv(const xk_system* A, const double* x, double*
 }
 
 extern "C" xk_status xk_system_block_jacobi(const xk_system* A, double* dinv, xk_stream s) {
-  if (!A || !dinv || !A->kb_row_ptr || !A->kb_col || !A->kb_vals)
+  if (!A || !dinv || !A->kb_row_ptr || !A->kb_col || !A->kb_vals || !kc_complete(A))
     return xk_set_error(XK_ERR_ARG, "xk_system_block_jacobi: null argument");
   if (A->n_nodes <= 0) return XK_OK;
   if (A->precision == XK_FP64)
@@ -281,7 +296,8 @@ extern "C" xk_status xk_system_block_jacobi(const xk_system* A, double* dinv, xk
 extern "C" xk_status xk_bicgstab(const xk_system* A, const double* b, double* x, const double* dinv, double* work,
                                  int32_t max_iter, int32_t check_every, double rtol, int32_t* iters, double* rel_res,
                                  xk_stream s) {
-  if (!A || !b || !x || !dinv || !work || max_iter < 0 || check_every < 1)
+  if (!A || !b || !x || !dinv || !work || max_iter < 0 || check_every < 1 || !A->kb_row_ptr || !A->kb_col ||
+      !A->kb_vals || !kc_complete(A))
     return xk_set_error(XK_ERR_ARG, "xk_bicgstab: bad arguments");
   cudaStream_t st = (cudaStream_t)s;
   const long long n = 6LL * A->n_nodes;

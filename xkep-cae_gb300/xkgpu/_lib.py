@@ -81,7 +81,8 @@ class ContactParams(C.Structure):
 
 class System(C.Structure):
     _fields_ = [("n_nodes", C.c_int32), ("precision", C.c_int32)] + [
-        (n, vp) for n in ("kb_row_ptr", "kb_col", "kb_vals", "kc_row_ptr", "kc_col", "kc_vals", "fixed")]
+        (n, vp) for n in ("kb_row_ptr", "kb_col", "kb_vals", "kc_row_ptr", "kc_col", "kc_vals", "kc_blk_row",
+                          "kc_low_ptr", "kc_low_blk", "fixed")]
 
 
 class BPParams(C.Structure):
@@ -96,7 +97,7 @@ class ContactPattern(C.Structure):
         (n, vp) for n in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row",
                           "blk_ptr", "contrib")] + [("n_elems", C.c_int64), ("sides_ok", C.c_int64)] + [
         (n, vp) for n in ("node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums",
-                          "norm_scratch")]
+                          "norm_scratch")] + [("nnzb_full", C.c_int64), ("low_ptr", vp), ("low_blk", vp)]
 
 
 P = C.POINTER

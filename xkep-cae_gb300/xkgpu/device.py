@@ -10,6 +10,7 @@ import ctypes as C
 from dataclasses import dataclass
 
 import numpy as np
+import scipy.sparse as sp
 import torch
 
 from . import _lib as L
@@ -399,6 +400,7 @@ class DeviceContactPattern:
         self.c = L.ContactPattern()
         self.inc_ptr = self._i32(mesh.n_nodes + 1)
         self.row_ptr = self._i32(mesh.n_nodes + 1)
+        self.low_ptr = self._i32(mesh.n_nodes + 1)
         # element-side form (mesh topology, element incidence, cross lists, element sums)
         self.node_elem_ptr = self._i32(mesh.n_nodes + 1)
         self.node_elem = self._i32(4 * mesh.n_elems)
@@ -428,6 +430,7 @@ class DeviceContactPattern:
     def _alloc_blocks(self, cap):
         cap = int(cap)
         self.col, self.blk_row, self.blk_ptr = self._i32(cap), self._i32(cap), self._i32(cap + 1)
+        self.low_blk = self._i32(cap)
         self.bcodes = self._i32(4 * cap)
         self.cap_blocks = cap
 
@@ -437,7 +440,7 @@ class DeviceContactPattern:
         c.cap_members, c.cap_others, c.cap_blocks = self.cap_members, self.cap_others, self.cap_blocks
         for k in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row", "blk_ptr",
                   "contrib", "node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums",
-                  "norm_scratch"):
+                  "norm_scratch", "low_ptr", "low_blk"):
             setattr(c, k, ptr(getattr(self, k)))
 
     def build(self, pairs: DevicePairTable, stream=None):
@@ -467,3 +470,27 @@ class DeviceContactPattern:
     @property
     def n_contrib(self) -> int:
         return int(self.c.n_contrib)
+
+    @property
+    def nnzb_full(self) -> int:
+        """Blocks of the full K_c: the stored (row <= column) blocks and the mirrors of the off-diagonal ones."""
+        return int(self.c.nnzb_full)
+
+    def to_csr(self, vals: torch.Tensor, ndof: int, drop_tiny: bool = False) -> sp.csr_matrix:
+        """The full K_c (ndof x ndof CSR) from the stored blocks' values (9 per block): every off-diagonal
+        stored block (v, w) also stands at (w, v), with the same values."""
+        nb = self.nnzb
+        if nb == 0:
+            return sp.csr_matrix((ndof, ndof))
+        v = vals[: 9 * nb].double().cpu().numpy().reshape(nb, 3, 3)
+        r = self.blk_row[:nb].cpu().numpy().astype(np.int64)
+        c = self.col[:nb].cpu().numpy().astype(np.int64)
+        off = r != c
+        r, c = np.concatenate([r, c[off]]), np.concatenate([c, r[off]])
+        v = np.concatenate([v, v[off]])
+        rows = np.broadcast_to((6 * r)[:, None, None] + np.arange(3)[None, :, None], v.shape)
+        cols = np.broadcast_to((6 * c)[:, None, None] + np.arange(3)[None, None, :], v.shape)
+        if drop_tiny:
+            keep = np.abs(v) > 1e-30
+            return sp.csr_matrix((v[keep], (rows[keep], cols[keep])), shape=(ndof, ndof))
+        return sp.csr_matrix((v.ravel(), (rows.ravel(), cols.ravel())), shape=(ndof, ndof))

@@ -245,7 +245,8 @@ class AssemblyEngine:
             self._alloc_outputs()
         self.graph = None
         self.stats = {"raw": n_raw, "prefilter": n_pre, "candidates": n_all, "kept_candidates": nc,
-                      "pairs": self.pairs.n, "members": self.pattern.n_members, "contact_blocks": self.pattern.nnzb}
+                      "pairs": self.pairs.n, "members": self.pattern.n_members, "contact_blocks": self.pattern.nnzb,
+                      "contact_blocks_full": self.pattern.nnzb_full}
         return self.stats
 
     # ------------------------------------------------------------------ per iteration
@@ -399,17 +400,8 @@ class AssemblyEngine:
                              shape=(nd, nd)).tocsr()
 
     def K_contact_csr(self, vals: torch.Tensor | None = None) -> sp.csr_matrix:
-        nb = self.pattern.nnzb
-        nd = self.mesh.ndof
-        if nb == 0:
-            return sp.csr_matrix((nd, nd))
-        v = (self.K_c if vals is None else vals)[: 9 * nb].double().cpu().numpy().reshape(nb, 3, 3)
-        r = self.pattern.blk_row[:nb].cpu().numpy().astype(np.int64)
-        c = self.pattern.col[:nb].cpu().numpy().astype(np.int64)
-        rows = (6 * r)[:, None, None] + np.arange(3)[None, :, None]
-        cols = (6 * c)[:, None, None] + np.arange(3)[None, None, :]
-        rows, cols = np.broadcast_to(rows, v.shape), np.broadcast_to(cols, v.shape)
-        return sp.csr_matrix((v.ravel(), (rows.ravel(), cols.ravel())), shape=(nd, nd))
+        """The full contact tangent from its stored (row <= column) blocks and their mirrors."""
+        return self.pattern.to_csr(self.K_c if vals is None else vals, self.mesh.ndof)
 
     def K_total_csr(self) -> sp.csr_matrix:
         return (self.K_beam_csr() + self.K_contact_csr()).tocsr()

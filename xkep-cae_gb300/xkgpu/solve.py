@@ -51,10 +51,11 @@ class DeviceLinearSolver:
         s.kb_row_ptr, s.kb_col = ptr(e.beam.row_ptr), ptr(e.beam.col)
         s.kb_vals = ptr(e.K_beam if K_beam is None else K_beam)
         pat = e.pattern
-        if pat.nnzb > 0:
+        if pat.nnzb > 0:  # the stored (row <= column) blocks; the kernels add their mirrors
             s.kc_row_ptr, s.kc_col, s.kc_vals = ptr(pat.row_ptr), ptr(pat.col), ptr(e.K_c)
+            s.kc_blk_row, s.kc_low_ptr, s.kc_low_blk = ptr(pat.blk_row), ptr(pat.low_ptr), ptr(pat.low_blk)
         else:
-            s.kc_row_ptr = s.kc_col = s.kc_vals = None
+            s.kc_row_ptr = s.kc_col = s.kc_vals = s.kc_blk_row = s.kc_low_ptr = s.kc_low_blk = None
         s.fixed = ptr(self.fixed)
         return s
 

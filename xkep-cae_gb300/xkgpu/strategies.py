@@ -235,13 +235,7 @@ class PairBatch:
         K = torch.zeros(9 * nb, dtype=torch.float64, device=self.device)
         L.call("xk_contact_gather_tangent", C.byref(self.pattern.c), ptr(self.rec), L.XK_FP64, L.XK_OUT_SPLIT,
                which, L.XK_GATHER_DEFAULT, ptr(K), stream_handle())
-        v = K.cpu().numpy().reshape(nb, 3, 3)
-        r = self.pattern.blk_row[:nb].cpu().numpy().astype(np.int64)
-        c = self.pattern.col[:nb].cpu().numpy().astype(np.int64)
-        rows = np.broadcast_to((6 * r)[:, None, None] + np.arange(3)[None, :, None], v.shape)
-        cols = np.broadcast_to((6 * c)[:, None, None] + np.arange(3)[None, None, :], v.shape)
-        keep = np.abs(v) > 1e-30
-        return sp.csr_matrix((v[keep], (rows[keep], cols[keep])), shape=(ndof, ndof))
+        return self.pattern.to_csr(K, ndof, drop_tiny=True)
 
     def narrowphase(self, cp, update_active: bool):
         L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.table.c), ptr(self.u0), C.byref(cp),
