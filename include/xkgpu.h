@@ -93,12 +93,16 @@ typedef struct {
 xk_status xk_beam_reference(const xk_mesh* m, const double* v_ref, double* elem_ref, xk_stream s);
 
 /* Colouring plan for a deterministic, atomic-free write of element blocks into
- * the fixed block-CSR pattern of K_T. */
+ * the fixed block-CSR pattern of K_T.  The element tangents are symmetrised
+ * (_beam_assembly.py:322), so block (w, v) of K_T is the transpose of block
+ * (v, w): the pattern holds the blocks with row <= column only, and each
+ * element's off-diagonal block below the diagonal has block index -1 (not
+ * written; the full K_T has the transpose of the stored block there). */
 typedef struct {
   int32_t n_colors;
   const int32_t* color_ptr_host; /* host [n_colors+1], ranges of elem_order */
   const int32_t* elem_order;     /* [n_elems] elements grouped by colour */
-  const int32_t* blk;            /* [4*n_elems] block index of (aa, ab, ba, bb) per element */
+  const int32_t* blk;            /* [4*n_elems] block index of (aa, ab, ba, bb) per element, -1 below the diagonal */
   const uint8_t* first;          /* [n_elems] bits 0..3: this element is the first writer of
                                     block aa, ab, ba, bb (aa / bb also: of the f rows of a / b) */
   int64_t nnzb;
@@ -502,9 +506,12 @@ xk_status xk_add_diagonal(int64_t n, const int64_t* idx, const double* m, double
 typedef struct {
   int32_t n_nodes;
   int32_t precision;            /* values double (XK_FP64) or float (XK_MIXED) */
-  const int32_t* kb_row_ptr;    /* K_beam: 6x6 block CSR over the nodes [n_nodes+1] */
+  const int32_t* kb_row_ptr;    /* K_beam: its stored (row <= column) 6x6 blocks as block CSR [n_nodes+1] */
   const int32_t* kb_col;
   const void* kb_vals;          /* 36 per block, row-major */
+  const int32_t* kb_blk_row;    /* row of every stored block, and per node w the stored blocks (v, w), */
+  const int32_t* kb_low_ptr;    /*   v < w, ascending in v [n_nodes+1] / ...: their transposes complete */
+  const int32_t* kb_low_blk;    /*   row w */
   const int32_t* kc_row_ptr;    /* K_c: the stored (row <= column) 3x3 blocks of xk_contact_pattern over */
   const int32_t* kc_col;        /*   the nodes' translational DOFs (nullable) */
   const void* kc_vals;          /* 9 per block */
@@ -514,8 +521,8 @@ typedef struct {
   const uint8_t* fixed;         /* [6*n_nodes] Dirichlet DOFs (nullable): identity rows and columns */
 } xk_system;
 
-/* y = A x with A = K_beam + K_c (K_c's stored blocks and their mirrors), Dirichlet rows and columns
- * as the identity; x, y double [6*n_nodes]. */
+/* y = A x with A = K_beam + K_c (K_beam's stored blocks and their transposes, K_c's stored blocks
+ * and their mirrors), Dirichlet rows and columns as the identity; x, y double [6*n_nodes]. */
 xk_status xk_system_spmv(const xk_system* A, const double* x, double* y, xk_stream s);
 /* dinv[36 v ...]: the inverse of every node's 6x6 diagonal block of A (the block-Jacobi preconditioner). */
 xk_status xk_system_block_jacobi(const xk_system* A, double* dinv, xk_stream s);

@@ -50,3 +50,32 @@ def test_mirrored_blocks_are_equal_and_rebuild_the_matrix():
     vals = torch.as_tensor(B[rows, :, cols, :].reshape(-1))
     full = pat.to_csr(vals, K.shape[0]).toarray()
     assert np.abs(full - K).max() <= 1e-14 * scale  # K_c has translational entries only
+
+
+def test_beam_upper_blocks_rebuild_the_symmetric_tangent():
+    """The reference symmetrises each element tangent (_beam_assembly.py:322): K_beam is stored as its
+    row <= column 6x6 blocks, and ``DeviceBeam.to_csr`` puts the transposes below the diagonal."""
+    from types import SimpleNamespace
+
+    from oracle import beam as ob
+    from xkgpu.device import DeviceBeam, make_beam_plan
+
+    w = W.config_workload("strand7", seed=0)
+    st = w.strand
+    Kb, _ = ob.assemble_beam(st.coords, st.conn, w.u, ob.Section(**w.section, scf=None))
+    K = Kb.toarray()
+    assert np.array_equal(K, K.T)
+    conn = np.array(st.conn)
+    conn[::2] = conn[::2, ::-1]  # both element orientations: the lower block id is -1 on either side
+    plan = make_beam_plan(conn, st.n_nodes)
+    assert np.all((plan.blk[:, 1] < 0) == (conn[:, 0] > conn[:, 1]))
+    assert np.all((plan.blk[:, 2] < 0) == (conn[:, 0] < conn[:, 1]))
+    assert np.all(plan.first[:, None] >> np.arange(4) & 1 <= (plan.blk >= 0))
+    rows = np.repeat(np.arange(st.n_nodes), np.diff(plan.row_ptr))
+    assert np.all(rows <= plan.col)
+    B = K.reshape(st.n_nodes, 6, st.n_nodes, 6)
+    vals = torch.as_tensor(B[rows, :, plan.col, :].reshape(-1))
+    beam = DeviceBeam.__new__(DeviceBeam)
+    beam.plan_host = plan
+    beam.mesh = SimpleNamespace(n_nodes=st.n_nodes, ndof=6 * st.n_nodes)
+    assert np.array_equal(beam.to_csr(vals).toarray(), K)

@@ -51,7 +51,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(L.ContactParams) == 6 * 8 + 8 + 5 * 8
     assert C.sizeof(L.BPParams) == 8 + 3 * 4 + 4 + 8
     assert C.sizeof(L.ContactPattern) == 16 + 5 * 8 + 10 * 8 + 2 * 8 + 7 * 8 + 3 * 8
-    assert C.sizeof(L.System) == 8 + 10 * 8
+    assert C.sizeof(L.System) == 8 + 13 * 8
 
 
 def test_argument_checks_before_any_launch(lib):
@@ -70,6 +70,6 @@ def test_argument_checks_before_any_launch(lib):
     from xkgpu import _lib as L
 
     assert lib.xk_bicgstab(None, None, None, None, None, 10, 1, 1e-8, None, None, None) == 1
-    s = L.System(4, 0, 0x1000, 0x2000, 0x3000, None, None, None, None)
+    s = L.System(4, 0, 0x1000, 0x2000, 0x3000, 0x1000, 0x1000, 0x1000)
     assert lib.xk_bicgstab(C.byref(s), 0x1000, 0x2000, 0x3000, 0x4000, 10, 0, 1e-8, None, None, None) == 1
     assert lib.xk_system_spmv(None, 0x1000, 0x2000, None) == 1

@@ -9,7 +9,6 @@ from __future__ import annotations
 
 import numpy as np
 import pytest
-import scipy.sparse as sp
 
 from conftest import golden, golden_csr, rel_err, sparse_rel_err
 
@@ -46,10 +45,7 @@ def _beam_eval(coords, conn, u, sec, precision, v_ref=None):
     K = torch.zeros(36 * beam.nnzb, dtype=beam.k_dtype(precision), device="cuda")
     beam.assemble(_dev(u), precision, f, K)
     torch.cuda.synchronize()
-    nb = beam.nnzb
-    Kc = sp.bsr_matrix((K.double().cpu().numpy().reshape(nb, 6, 6), beam.col.cpu().numpy(),
-                        beam.row_ptr.cpu().numpy()), shape=(mesh.ndof, mesh.ndof)).tocsr()
-    return f.cpu().numpy(), Kc
+    return f.cpu().numpy(), beam.to_csr(K)
 
 
 @pytest.mark.parametrize("precision,tol", [(L.XK_FP64, TOL64), (L.XK_MIXED, TOLMIX)])

@@ -67,12 +67,16 @@ def test_bicgstab_matches_direct_solve(prec):
     assert torch.equal(x, x2)  # fixed-order reductions: the same bits on every run
 
 
-def test_quasi_static_newton_device_solve_matches_host_solve():
+@pytest.mark.parametrize("graph", [False, True])
+def test_quasi_static_newton_device_solve_matches_host_solve(graph):
+    """With ``graph=True`` the whole iteration stays on the device: the replayed assembly graph, the
+    device solve and the update; the host reads only the residual norm and the solver's checks."""
     out = {}
     for solver in (None, "device"):
         w, eng, fixed = _strand7("fp64")
         u0 = torch.zeros(eng.mesh.ndof, dtype=torch.float64, device="cuda")
-        out[solver] = solve_increment(eng, u0, u0, fixed=fixed, tol=1e-9, max_iter=25, solver=solver)
+        out[solver] = solve_increment(eng, u0, u0, fixed=fixed, tol=1e-9, max_iter=25, solver=solver,
+                                      graph=graph and solver == "device")
         print(solver, out[solver].iterations, ["%.2e" % r for r in out[solver].residuals])
     assert out[None].converged and out["device"].converged
     assert abs(out["device"].iterations - out[None].iterations) <= 1

@@ -373,11 +373,14 @@ XK_D void beam_tail(const KeCoef<T>& kc, const T* Rcr, const T* ex, T iL, const 
     mtm3(Rcr, Hl, Hm[I]);
     mtm3(Rcr, Jl, Jm[I]);
   }
-  // symmetrise and write the four 6x6 node blocks
+  // symmetrise and write the stored 6x6 node blocks (the off-diagonal block below the diagonal,
+  // id -1, is the transpose of the stored one)
 #pragma unroll
   for (int nb = 0; nb < 4; ++nb) {  // 0 aa, 1 ab, 2 ba, 3 bb
     const int I0 = (nb >> 1) * 2, J0 = (nb & 1) * 2;
-    T* dst = Kv + 36LL * blk[4LL * e + nb];
+    const int bi = blk[4LL * e + nb];
+    if (bi < 0) continue;
+    T* dst = Kv + 36LL * bi;
     const bool fw = (fl >> nb) & 1;
 #pragma unroll
     for (int ii = 0; ii < 2; ++ii)
@@ -710,8 +713,10 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
     const int qq = q0 + t / 36, nb = (t % 36) / 9, ch = t % 9;
     const int ee = s_e[qq];
     if (ee < 0) continue;
+    const int bi = blk[4LL * ee + nb];
+    if (bi < 0) continue;  // the off-diagonal block below the diagonal: the stored one's transpose
     const float4 v = reinterpret_cast<const float4*>(kst[qq][nb])[ch];
-    float4* dst = reinterpret_cast<float4*>(Kv + 36LL * blk[4LL * ee + nb]) + ch;
+    float4* dst = reinterpret_cast<float4*>(Kv + 36LL * bi) + ch;
     if (CHAIN) {
       if (nb == 0 || nb == 3) atomicAdd(dst, v);  // diagonal block, shared with the neighbour element
       else *dst = v;

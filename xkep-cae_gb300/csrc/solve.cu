@@ -29,6 +29,17 @@ __global__ void k_spmv(xk_system A, const double* __restrict__ x, double* __rest
   }
   const T* kb = (const T*)A.kb_vals;
   double acc = 0.0;
+  // the stored blocks (u, v), u < v, transposed: row v's blocks left of the diagonal
+  for (int q = A.kb_low_ptr[v]; q < A.kb_low_ptr[v + 1]; ++q) {
+    const int b = A.kb_low_blk[q];
+    const int u = A.kb_blk_row[b];
+    const T* blk = kb + 36LL * b + d;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const long long col = 6LL * u + j;
+      if (!(A.fixed && A.fixed[col])) acc = fma((double)blk[6 * j], x[col], acc);
+    }
+  }
   for (int b = A.kb_row_ptr[v]; b < A.kb_row_ptr[v + 1]; ++b) {
     const int w = A.kb_col[b];
     const T* blk = kb + 36LL * b + 6 * d;
@@ -269,7 +280,8 @@ xk_status dot2(long long n, const double* a0, const double* b0, const double* a1
 }  // namespace
 
 static bool kc_complete(const xk_system* A) {
-  return !A->kc_vals || (A->kc_row_ptr && A->kc_col && A->kc_blk_row && A->kc_low_ptr && A->kc_low_blk);
+  return A->kb_blk_row && A->kb_low_ptr && A->kb_low_blk &&
+         (!A->kc_vals || (A->kc_row_ptr && A->kc_col && A->kc_blk_row && A->kc_low_ptr && A->kc_low_blk));
 }
 
 extern "C" xk_status xk_system_spmv(const xk_system* A, const double* x, double* y, xk_stream s) {

@@ -81,8 +81,8 @@ class ContactParams(C.Structure):
 
 class System(C.Structure):
     _fields_ = [("n_nodes", C.c_int32), ("precision", C.c_int32)] + [
-        (n, vp) for n in ("kb_row_ptr", "kb_col", "kb_vals", "kc_row_ptr", "kc_col", "kc_vals", "kc_blk_row",
-                          "kc_low_ptr", "kc_low_blk", "fixed")]
+        (n, vp) for n in ("kb_row_ptr", "kb_col", "kb_vals", "kb_blk_row", "kb_low_ptr", "kb_low_blk", "kc_row_ptr",
+                          "kc_col", "kc_vals", "kc_blk_row", "kc_low_ptr", "kc_low_blk", "fixed")]
 
 
 class BPParams(C.Structure):

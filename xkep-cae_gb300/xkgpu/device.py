@@ -87,25 +87,40 @@ class DeviceMesh:
 
 
 def beam_block_pattern(conn: np.ndarray, n_nodes: int):
-    """6x6 block-CSR pattern of the beam tangent and each element's 4 block ids.
+    """6x6 block-CSR pattern of the beam tangent's stored blocks and each element's 4 block ids.
 
-    Blocks (a,a), (a,b), (b,a), (b,b) of every element a-b, rows sorted by
-    column: the structural pattern of ``assemble_cr_beam3d``'s CSR
-    (``_beam_assembly.py:146-150``) in 6x6 blocks.
+    The structural pattern of ``assemble_cr_beam3d``'s CSR
+    (``_beam_assembly.py:146-150``) in 6x6 blocks is (a,a), (a,b), (b,a), (b,b)
+    of every element a-b.  The reference symmetrises every element tangent
+    (``_beam_assembly.py:322``), so block (w, v) is the transpose of block
+    (v, w): only the blocks with row <= column are stored, rows sorted by
+    column, and the element's id of its other off-diagonal block is -1.
     """
     conn = np.asarray(conn, dtype=np.int64)
     a, b = conn[:, 0], conn[:, 1]
     rows = np.stack([a, a, b, b], axis=1)
     cols = np.stack([a, b, a, b], axis=1)
     keys = rows * n_nodes + cols
-    uk = np.unique(keys.ravel())
+    upper = rows <= cols
+    uk = np.unique(keys[upper])
     brow = uk // n_nodes
     bcol = (uk % n_nodes).astype(np.int32)
     row_ptr = np.zeros(n_nodes + 1, dtype=np.int64)
     np.add.at(row_ptr, brow + 1, 1)
     row_ptr = np.cumsum(row_ptr)
-    blk = np.searchsorted(uk, keys).astype(np.int32)
+    blk = np.where(upper, np.searchsorted(uk, keys), -1).astype(np.int32)
     return row_ptr.astype(np.int32), bcol, blk
+
+
+def lower_index(row_ptr: np.ndarray, col: np.ndarray, n_nodes: int):
+    """Per node w, the stored blocks (v, w) with v < w, ascending in v: (blk_row, low_ptr, low_blk)."""
+    rows = np.repeat(np.arange(n_nodes, dtype=np.int64), np.diff(row_ptr))
+    off = np.nonzero(rows != col)[0]
+    order = np.lexsort((rows[off], col[off]))
+    low_blk = off[order].astype(np.int32)
+    low_ptr = np.zeros(n_nodes + 1, dtype=np.int64)
+    np.add.at(low_ptr, col[off].astype(np.int64) + 1, 1)
+    return rows.astype(np.int32), np.cumsum(low_ptr).astype(np.int32), low_blk
 
 
 def greedy_coloring(conn: np.ndarray, n_nodes: int) -> np.ndarray:
@@ -153,8 +168,9 @@ def make_beam_plan(conn: np.ndarray, n_nodes: int) -> BeamPlanHost:
     nblk = col.shape[0]
     best = np.full(nblk, np.iinfo(np.int32).max, dtype=np.int64)
     ecol = np.repeat(colors[:, None], 4, axis=1)
-    np.minimum.at(best, blk.ravel(), ecol.ravel())
-    isfirst = ecol == best[blk]
+    stored = blk >= 0
+    np.minimum.at(best, blk[stored], ecol[stored])
+    isfirst = stored & (ecol == best[np.where(stored, blk, 0)])
     first = (isfirst * (1 << np.arange(4))[None, :]).sum(axis=1).astype(np.uint8)
     return BeamPlanHost(row_ptr, col, blk, colors, order, color_ptr, first)
 
@@ -197,6 +213,10 @@ class DeviceBeam:
         self.first = torch.as_tensor(ph.first, device=dev)
         self.row_ptr = torch.as_tensor(ph.row_ptr, device=dev)
         self.col = torch.as_tensor(ph.col, device=dev)
+        brow, lptr, lblk = lower_index(ph.row_ptr, ph.col, mesh.n_nodes)
+        self.blk_row = torch.as_tensor(brow, device=dev)
+        self.low_ptr = torch.as_tensor(lptr, device=dev)
+        self.low_blk = torch.as_tensor(lblk if lblk.size else np.zeros(1, np.int32), device=dev)
         self._color_ptr = (C.c_int32 * len(ph.color_ptr))(*ph.color_ptr.tolist())
         # wires: every node in at most two elements, no two elements on the same nodes -> one-launch float path
         nd = chain_node_diag(mesh.conn_host, mesh.n_nodes, ph) if chain else None
@@ -222,6 +242,22 @@ class DeviceBeam:
     @property
     def nnzb(self) -> int:
         return self.plan_host.nnzb
+
+    def to_csr(self, vals: torch.Tensor) -> sp.csr_matrix:
+        """The full beam tangent (ndof x ndof CSR) from its stored (row <= column) 6x6 blocks: every
+        off-diagonal stored block (v, w) stands transposed at (w, v)."""
+        ph = self.plan_host
+        nb = ph.nnzb
+        nd = self.mesh.ndof
+        v = vals[: 36 * nb].double().cpu().numpy().reshape(nb, 6, 6)
+        r = np.repeat(np.arange(self.mesh.n_nodes, dtype=np.int64), np.diff(ph.row_ptr))
+        c = ph.col.astype(np.int64)
+        off = r != c
+        r, c = np.concatenate([r, c[off]]), np.concatenate([c, r[off]])
+        v = np.concatenate([v, v[off].transpose(0, 2, 1)])
+        rows = np.broadcast_to((6 * r)[:, None, None] + np.arange(6)[None, :, None], v.shape)
+        cols = np.broadcast_to((6 * c)[:, None, None] + np.arange(6)[None, None, :], v.shape)
+        return sp.csr_matrix((v.ravel(), (rows.ravel(), cols.ravel())), shape=(nd, nd))
 
     def diag_index(self) -> torch.Tensor:
         """Value index (into the 6x6 block values) of every DOF's diagonal entry; -1 for a node without elements."""

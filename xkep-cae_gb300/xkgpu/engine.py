@@ -393,11 +393,8 @@ class AssemblyEngine:
         return float(np.sqrt(self.norm2.item()))
 
     def K_beam_csr(self) -> sp.csr_matrix:
-        nb = self.beam.nnzb
-        vals = self.K_beam[: 36 * nb].double().cpu().numpy().reshape(nb, 6, 6)
-        nd = self.mesh.ndof
-        return sp.bsr_matrix((vals, self.beam.col.cpu().numpy(), self.beam.row_ptr.cpu().numpy()),
-                             shape=(nd, nd)).tocsr()
+        """The full beam tangent from its stored (row <= column) blocks and their transposes."""
+        return self.beam.to_csr(self.K_beam)
 
     def K_contact_csr(self, vals: torch.Tensor | None = None) -> sp.csr_matrix:
         """The full contact tangent from its stored (row <= column) blocks and their mirrors."""

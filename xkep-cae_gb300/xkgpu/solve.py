@@ -50,6 +50,7 @@ class DeviceLinearSolver:
         s.precision = e.precision
         s.kb_row_ptr, s.kb_col = ptr(e.beam.row_ptr), ptr(e.beam.col)
         s.kb_vals = ptr(e.K_beam if K_beam is None else K_beam)
+        s.kb_blk_row, s.kb_low_ptr, s.kb_low_blk = ptr(e.beam.blk_row), ptr(e.beam.low_ptr), ptr(e.beam.low_blk)
         pat = e.pattern
         if pat.nnzb > 0:  # the stored (row <= column) blocks; the kernels add their mirrors
             s.kc_row_ptr, s.kc_col, s.kc_vals = ptr(pat.row_ptr), ptr(pat.col), ptr(e.K_c)

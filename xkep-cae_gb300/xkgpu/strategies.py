@@ -1033,9 +1033,7 @@ class GpuCRBeamAssembler:
         K = torch.zeros(36 * max(nb, 1), dtype=self.beam.k_dtype(self.precision), device=self.mesh.device)
         f = torch.zeros(self.ndof, dtype=torch.float64, device=self.mesh.device)
         self._run(u_incr, f, K)
-        v = K[: 36 * nb].double().cpu().numpy().reshape(nb, 6, 6)
-        return sp.bsr_matrix((v, self.beam.col.cpu().numpy(), self.beam.row_ptr.cpu().numpy()),
-                             shape=(self.ndof, self.ndof)).tocsr()
+        return self.beam.to_csr(K)
 
     def assemble_internal_force(self, u_incr) -> np.ndarray:
         f = torch.zeros(self.ndof, dtype=torch.float64, device=self.mesh.device)
