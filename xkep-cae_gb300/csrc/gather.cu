@@ -440,7 +440,7 @@ __global__ void k_elem_sums(int ne, const int32_t* __restrict__ eptr, const int3
 
 // The same sums for combined records, four lanes per element: lane q sums the incidences
 // q, q + 4, q + 8, ... of the element (each one record read as two 256-bit loads for float),
-// and the four partial sums are combined by a fixed shuffle tree ((0 + 1) + (2 + 3)), so the
+// and the four partial sums are combined by a fixed shuffle tree ((q + q^2) + (q^1 + q^3)), so the
 // result does not depend on timing.  It differs from k_elem_sums' single running sum by
 // rounding only.
 template <typename T>
@@ -473,7 +473,7 @@ XK_D void store4<double>(double* p, double a, double b, double c, double d) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) k_elem_sums_rec(int ne, const int32_t* __restrict__ eptr,
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 7 : 4) k_elem_sums_rec(int ne, const int32_t* __restrict__ eptr,
                                                        const int32_t* __restrict__ einc, const T* __restrict__ rec,
                                                        T* __restrict__ S) {
   static_assert(XK_REC_B == 0 && XK_REC_S == 9 && XK_REC_V == 11, "combined record layout");
@@ -515,34 +515,40 @@ __global__ void __launch_bounds__(128) k_elem_sums_rec(int ne, const int32_t* __
       }
     }
   }
-  // (lane 0 + lane 1) + (lane 2 + lane 3) in every lane of the quad
+  // Reduce-scatter over the quad: the 33 sums (S^00, S^01, S^11, F^0, F^1, padded to 36) split in
+  // halves between lanes q and q ^ 2, then in quarters between q and q ^ 1, so that lane q ends with
+  // the nine values it stores (lane 0 S^00, 1 S^01, 2 S^11, 3 F^0 F^1) as (l_q + l_q^2) +
+  // (l_q^1 + l_q^3): a fixed tree of 27 shuffles per lane.
+  T v[36];
 #pragma unroll
-  for (int m = 1; m <= 2; m <<= 1) {
+  for (int c = 0; c < 9; ++c) { v[c] = s00[c]; v[9 + c] = s01[c]; v[18 + c] = s11[c]; }
 #pragma unroll
-    for (int c = 0; c < 9; ++c) {
-      s00[c] += __shfl_xor_sync(0xffffffffu, s00[c], m);
-      s01[c] += __shfl_xor_sync(0xffffffffu, s01[c], m);
-      s11[c] += __shfl_xor_sync(0xffffffffu, s11[c], m);
-    }
+  for (int c = 0; c < 3; ++c) { v[27 + c] = f0[c]; v[30 + c] = f1[c]; v[33 + c] = T(0); }
+  const bool hi = (q >> 1) & 1, odd = q & 1;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      f0[c] += __shfl_xor_sync(0xffffffffu, f0[c], m);
-      f1[c] += __shfl_xor_sync(0xffffffffu, f1[c], m);
-    }
+  for (int c = 0; c < 18; ++c) {  // lane q keeps half hi, receives it from q ^ 2
+    const T y = __shfl_xor_sync(0xffffffffu, hi ? v[c] : v[18 + c], 2);
+    if (hi) v[18 + c] += y; else v[c] += y;
+  }
+  T w[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) {  // within the kept half, quarter odd, received from q ^ 1
+    const T a = hi ? v[18 + c] : v[c], b = hi ? v[27 + c] : v[9 + c];
+    const T y = __shfl_xor_sync(0xffffffffu, odd ? a : b, 1);
+    w[c] = (odd ? b : a) + y;
   }
   if (!live) return;
-  // vector stores shared by the quad: lanes 0-2 write sum S^00, S^01, S^11 (its 9 values, then
-  // (s, t) = (1, 1) and a zero; the last 4 values of a sum are not read), lane 3 the force sums
+  // vector stores: lanes 0-2 write sum S^00, S^01, S^11 (its 9 values, then (s, t) = (1, 1) and a
+  // zero; the last 4 values of a sum are not read), lane 3 the force sums
   if (q < 3) {
-    const T* sp = q == 0 ? s00 : (q == 1 ? s01 : s11);
     T* o = S + (long long)ELEM_SUMS * e + q * SUM_STRIDE;
-    store4<T>(o, sp[0], sp[1], sp[2], sp[3]);
-    store4<T>(o + 4, sp[4], sp[5], sp[6], sp[7]);
-    store4<T>(o + 8, sp[8], T(1), T(1), T(0));
+    store4<T>(o, w[0], w[1], w[2], w[3]);
+    store4<T>(o + 4, w[4], w[5], w[6], w[7]);
+    store4<T>(o + 8, w[8], T(1), T(1), T(0));
   } else {
     T* f = S + (long long)ELEM_SUMS * ne + (long long)ELEM_FORCE * e;
-    store4<T>(f, f0[0], f0[1], f0[2], f1[0]);
-    store4<T>(f + 4, f1[1], f1[2], T(0), T(0));
+    store4<T>(f, w[0], w[1], w[2], w[3]);
+    store4<T>(f + 4, w[4], w[5], T(0), T(0));
   }
 }
 
