@@ -629,9 +629,11 @@ def run_gpu(args, rank, world):
         extras["batched"] = batch_section(args, dev)
         extras["coated"] = coated_section(args, dev)
 
-    # node prep, 2 pair kernels, 2 beam colours, then either element sums + tangent gather + residual from
-    # the element sums (norm fused) or tangent gather + force gather + 2 norm kernels
-    per_launch = 5 + (3 if mixed_variant == L.XK_GATHER_SIDES else 4)
+    # node prep, the other-pair kernel and its near-parallel kernel, the beam's zeroing and element
+    # launches, the member kernel and its near-parallel kernel, then either element sums + tangent
+    # gather + residual from the element sums (norm fused) or tangent gather + force gather + 2 norm
+    # kernels (the launch list in profiles/launches_strand1027.md shows the ten of the first form)
+    per_launch = 7 + (3 if mixed_variant == L.XK_GATHER_SIDES else 4)
     out = {
         "metric": METRIC, "value": units / t_mixed * args.steps, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
