@@ -555,13 +555,14 @@ XK_D void frame32(const float* __restrict__ E, const float* __restrict__ NA, con
 constexpr int BEAMQ_T = 128;
 
 template <bool CHAIN>
-__global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, const float* __restrict__ e32,
+__global__ void __launch_bounds__(BEAMQ_T, 7) k_beam32q(xk_mesh m, xk_section sec, const float* __restrict__ e32,
                                                      const int32_t* __restrict__ order, int k0, int k1,
                                                      const int32_t* __restrict__ blk,
                                                      const uint8_t* __restrict__ first, const float* __restrict__ n32,
                                                      double* __restrict__ f_int, float* __restrict__ Kv) {
   __shared__ float sx[BEAMQ_T / 4][4][27];
-  __shared__ __align__(16) float kst[BEAMQ_T / 4][4][36];  // the element's four 6x6 blocks, staged
+  // the element's three stored 6x6 blocks, staged: aa, the off-diagonal one above the diagonal, bb
+  __shared__ __align__(16) float kst[BEAMQ_T / 4][3][36];
   __shared__ int s_e[BEAMQ_T / 4];
   const int q = threadIdx.x >> 2, I = threadIdx.x & 3;
   const int k = k0 + blockIdx.x * (BEAMQ_T / 4) + q;
@@ -690,10 +691,14 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
   }
   __syncwarp();
   // row I of the symmetrised tangent: Ks[I][Jb] = (X_IJb + X_JbI^T) / 2 with
-  // X_I0 = G_I, X_I1 = H_I, X_I2 = -G_I, X_I3 = J_I, staged per block
+  // X_I0 = G_I, X_I1 = H_I, X_I2 = -G_I, X_I3 = J_I, staged per stored block (the off-diagonal
+  // block below the diagonal, ba for a < b and ab for a > b, is the transpose of the other)
+  const int nb_lower = a < b ? 2 : 1;
 #pragma unroll
   for (int Jb = 0; Jb < 4; ++Jb) {
     const int nb = (I >> 1) * 2 + (Jb >> 1);  // 0 aa, 1 ab, 2 ba, 3 bb
+    if (nb == nb_lower) continue;
+    const int slot = nb == 0 ? 0 : (nb == 3 ? 2 : 1);
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -702,20 +707,20 @@ __global__ void __launch_bounds__(BEAMQ_T) k_beam32q(xk_mesh m, xk_section sec, 
         const float* o = sx[q][Jb];
         const int off = i1 ? 9 : ((I == 3) ? 18 : 0);
         const float xji = (i2 ? -1.f : 1.f) * o[off + 3 * c + r];
-        kst[q][nb][(3 * (I & 1) + r) * 6 + 3 * (Jb & 1) + c] = 0.5f * (xij + xji);
+        kst[q][slot][(3 * (I & 1) + r) * 6 + 3 * (Jb & 1) + c] = 0.5f * (xij + xji);
       }
   }
   __syncwarp();
-  // the warp's 8 elements x 4 blocks as 9 float4 per block (a block starts at 144 B * index), first
-  // writer of a block stores, later colours add
+  // the warp's 8 elements x 3 stored blocks as 9 float4 per block (a block starts at 144 B * index),
+  // first writer of a block stores, later colours add
   const int lane = threadIdx.x & 31, q0 = (threadIdx.x >> 5) * 8;
-  for (int t = lane; t < 8 * 4 * 9; t += 32) {
-    const int qq = q0 + t / 36, nb = (t % 36) / 9, ch = t % 9;
+  for (int t = lane; t < 8 * 3 * 9; t += 32) {
+    const int qq = q0 + t / 27, slot = (t % 27) / 9, ch = t % 9;
     const int ee = s_e[qq];
     if (ee < 0) continue;
+    const int nb = slot == 0 ? 0 : (slot == 2 ? 3 : (blk[4LL * ee + 1] >= 0 ? 1 : 2));
     const int bi = blk[4LL * ee + nb];
-    if (bi < 0) continue;  // the off-diagonal block below the diagonal: the stored one's transpose
-    const float4 v = reinterpret_cast<const float4*>(kst[qq][nb])[ch];
+    const float4 v = reinterpret_cast<const float4*>(kst[qq][slot])[ch];
     float4* dst = reinterpret_cast<float4*>(Kv + 36LL * bi) + ch;
     if (CHAIN) {
       if (nb == 0 || nb == 3) atomicAdd(dst, v);  // diagonal block, shared with the neighbour element
