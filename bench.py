@@ -106,18 +106,26 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def slab_workload(w, frac: float):
-    """The first ``frac`` of every wire: a bounded sample of the same strand for CPU timing."""
+def slab_elems(nel: int, frac: float) -> int:
+    return max(2, int(round(nel * frac)))
+
+
+def slab_workload(w, frac: float, index: int = 0):
+    """Slab ``index`` of every wire, ``frac`` of its length each (slab 0 is the first ``frac``): a
+    bounded sample of the same strand for CPU timing."""
     from xkgpu import strand as S
 
     st = w.strand
     nel = st.n_elems_per_wire
-    keep_el = max(2, int(round(nel * frac)))
+    keep_el = slab_elems(nel, frac)
+    e0 = index * keep_el
+    if e0 + keep_el > nel:
+        raise ValueError(f"slab {index} of {keep_el} elements does not fit a wire of {nel}")
     npw = nel + 1
     nodes, elems = [], []
     for wi in range(len(st.wires)):
-        nodes.append(np.arange(wi * npw, wi * npw + keep_el + 1))
-        elems.append(np.arange(wi * nel, wi * nel + keep_el))
+        nodes.append(np.arange(wi * npw + e0, wi * npw + e0 + keep_el + 1))
+        elems.append(np.arange(wi * nel + e0, wi * nel + e0 + keep_el))
     nodes = np.concatenate(nodes)
     elems = np.concatenate(elems)
     remap = -np.ones(st.n_nodes, dtype=np.int64)
@@ -129,13 +137,13 @@ def slab_workload(w, frac: float):
     return sub, u
 
 
-def oracle_sample_timing(w, frac: float, reps: int = 1, prepared=None):
+def oracle_sample_timing(w, frac: float, reps: int = 1, prepared=None, index: int = 0):
     """Time the oracle (NumPy port) on a slab of the strand; returns (units, seconds, prepared)."""
     from oracle import beam as ob
     from oracle import contact as oc
 
     if prepared is None:
-        sub, u = slab_workload(w, frac)
+        sub, u = slab_workload(w, frac, index)
         cd = oc.deformed_coords(sub.coords, u)
         table, _, _ = oc.detect(oc.empty_table(), cd, sub.conn, sub.radii, elem_layer=sub.elem_layer,
                                 exclude_same_layer=True)
@@ -687,35 +695,75 @@ def run_gpu(args, rank, world):
 # --------------------------------------------------------------------------- reference arm
 
 
+def _ref_worker(conn, workload: str, frac: float, index: int) -> None:
+    """One host core's share of the reference arm: slab ``index`` of every wire, prepared once
+    (untimed), then one Newton-iteration assembly of it per request."""
+    from xkgpu import workloads as W
+
+    w = W.config_workload(workload, seed=0)
+    units, dt, prep = oracle_sample_timing(w, frac, index=index)
+    conn.send((units, dt))
+    while conn.recv() == "step":
+        units, dt, _ = oracle_sample_timing(w, frac, prepared=prep)
+        conn.send((units, dt))
+
+
 def run_reference(args):
+    """The reference path (the NumPy port) on every host core: one spawned process per core, each
+    assembling its own slab of every wire; a step ends when every process has finished its slab."""
+    import multiprocessing as mp
+
     from xkgpu import workloads as W
 
     w = W.config_workload(args.workload, seed=0)
     budget = float(os.environ.get("XK_REF_BUDGET_S", "150"))
     frac = 1.0 / 96.0
-    _, dt0, prep = oracle_sample_timing(w, frac)
+    _, dt0, _ = oracle_sample_timing(w, frac)
     per_step = budget / max(1, args.steps + args.warmup)
     # shrink the slab until one step fits its share of the budget
     while dt0 > per_step and frac > 1.0 / 768.0:
         frac /= 2.0
-        _, dt0, prep = oracle_sample_timing(w, frac)
+        _, dt0, _ = oracle_sample_timing(w, frac)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    nel = w.strand.n_elems_per_wire
+    n = max(1, min(cores, nel // slab_elems(nel, frac)))
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"  # one thread per process: the processes are the parallelism
+    ctx = mp.get_context("spawn")
+    pipes, procs = [], []
+    for k in range(n):
+        a, b = ctx.Pipe()
+        pr = ctx.Process(target=_ref_worker, args=(b, args.workload, frac, k), daemon=True)
+        pr.start()
+        pipes.append(a)
+        procs.append(pr)
+    slab_units = [a.recv()[0] for a in pipes]  # prepared
+
+    def step():
+        for a in pipes:
+            a.send("step")
+        return sum(a.recv()[0] for a in pipes)
+
     for _ in range(args.warmup):
-        oracle_sample_timing(w, frac, prepared=prep)
+        step()
     units = 0
-    tt = 0.0
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        u, dt, _ = oracle_sample_timing(w, frac, prepared=prep)
-        units += u
-        tt += dt
+        units += step()
+    tt = time.perf_counter() - t0
+    for a in pipes:
+        a.send("stop")
+    for pr in procs:
+        pr.join(timeout=30)
     v = units / tt
-    sub, _, table = prep
-    sample = (f"NumPy port of the reference path (oracle), one Newton-iteration assembly per step on the first "
-              f"{frac:.4g} of every wire ({sub.n_elems} elements, {table['ea'].shape[0]} pairs)")
+    sample = (f"NumPy port of the reference path (oracle) in {n} processes, one per host core, each one "
+              f"Newton-iteration assembly per step of its own {frac:.4g} slab of every wire "
+              f"({n * slab_elems(nel, frac)} of {nel} elements per wire; {sum(slab_units)} elements + pairs)")
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "strand1027 slab sample", "sample_fraction": frac},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "config": {"workload": "strand1027 slab sample", "sample_fraction": n * frac, "processes": n},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": n, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

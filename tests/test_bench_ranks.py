@@ -58,3 +58,23 @@ def test_rank_aggregate_two_gloo_ranks():
 def test_rank_aggregate_single_process_is_identity():
     t, n = _bench().rank_aggregate([1.5, 2.5], [7])
     assert t == [1.5, 2.5] and n == [7.0]
+
+
+def test_reference_arm_runs_on_every_core():
+    """``bench.py --impl reference`` times the NumPy port in one spawned process per host core, each
+    on its own slab of every wire (CPU; a small strand keeps it to seconds)."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    env = dict(os.environ, XK_REF_BUDGET_S="60")
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--workload", "strand37",
+                          "--steps", "1", "--warmup", "1"], capture_output=True, text=True, timeout=600, env=env,
+                         cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["cores"] == line["config"]["processes"] == min(cores, 128 // 2)
+    assert line["e2e"]["value"] == line["value"]
