@@ -324,6 +324,11 @@ xk_status xk_contact_gather_force(const xk_contact_pattern* pat, const void* rec
 #define XK_GATHER_LANES 1
 #define XK_GATHER_CHUNKS 2
 #define XK_GATHER_SIDES 3  /* element-side sums + cross lists (needs the element-side pattern) */
+/* The two launches of XK_GATHER_SIDES as separate calls: the element sums (which also hold the
+ * force sums that xk_contact_gather_force_elem reads), then the blocks from them.  A caller can
+ * then start the residual while the blocks are gathered. */
+#define XK_GATHER_SIDES_SUMS 4
+#define XK_GATHER_SIDES_BLOCKS 5
 xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, const void* rec, int precision, int out_mode,
                                     int which, int variant, void* Kc_vals, xk_stream s);
 

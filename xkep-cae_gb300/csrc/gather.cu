@@ -1220,8 +1220,10 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
   if (!pat || !rec || !Kc_vals) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: null argument");
   int c1, c2;
   XK_TRY(rec_columns(out_mode, which, true, &c1, &c2));
-  if (variant < 0 || variant > XK_GATHER_SIDES) return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: variant");
-  const bool sides = variant == XK_GATHER_SIDES;
+  if (variant < 0 || variant > XK_GATHER_SIDES_BLOCKS)
+    return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: variant");
+  const bool sides = variant >= XK_GATHER_SIDES;
+  const bool sums = variant != XK_GATHER_SIDES_BLOCKS, blocks = variant != XK_GATHER_SIDES_SUMS;
   if (sides && out_mode == XK_OUT_COMBINED && !(aligned32(rec) && aligned32(pat->elem_sums)))
     return xk_set_error(XK_ERR_ARG, "xk_contact_gather_tangent: rec and elem_sums must be 32-byte aligned");
   if (sides && !(pat->elem_ptr && pat->elem_inc && pat->bcodes && pat->elem_sums && pat->sides_ok == 1))
@@ -1236,15 +1238,16 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
 #define XK_GT(TT, RSV, BC)                                                                                   \
   do {                                                                                                      \
     if (sides) {                                                                                            \
-      if (ne > 0 && RSV == XK_REC_STRIDE_COMBINED)                                                          \
+      if (sums && ne > 0 && RSV == XK_REC_STRIDE_COMBINED)                                                  \
         k_elem_sums_rec<TT><<<xk_blocks(4LL * ne, 128), 128, 0, st>>>(ne, pat->elem_ptr, pat->elem_inc,     \
                                                                 (const TT*)rec, (TT*)pat->elem_sums);       \
-      else if (ne > 0)                                                                                      \
+      else if (sums && ne > 0)                                                                              \
         k_elem_sums<TT, RSV, BC><<<xk_blocks(9LL * ne, 256), 256, 0, st>>>(ne, pat->elem_ptr, pat->elem_inc,   \
                                                                            (const TT*)rec, (TT*)pat->elem_sums); \
-      k_gather_tangent_sides<TT, RSV, BC><<<sides_grid(pat->nnzb, sizeof(TT) == 4 ? 16 : 8), GS_T, 0, st>>>( \
-          pat->nnzb, reinterpret_cast<const int4*>(pat->bcodes), (const TT*)pat->elem_sums, (const TT*)rec,    \
-          (TT*)Kc_vals);                                                                                    \
+      if (blocks)                                                                                           \
+        k_gather_tangent_sides<TT, RSV, BC><<<sides_grid(pat->nnzb, sizeof(TT) == 4 ? 16 : 8), GS_T, 0, st>>>( \
+            pat->nnzb, reinterpret_cast<const int4*>(pat->bcodes), (const TT*)pat->elem_sums, (const TT*)rec,  \
+            (TT*)Kc_vals);                                                                                  \
     } else if (chunks)                                                                                      \
       k_gather_tangent<TT, RSV, BC><<<nb, 32 * GT_WARPS, 0, st>>>(pat->nnzb, pat->blk_ptr, pat->contrib,     \
                                                                   (const TT*)rec, (TT*)Kc_vals);            \

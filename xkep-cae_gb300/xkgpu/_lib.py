@@ -21,6 +21,7 @@ XK_OUT_COMBINED, XK_OUT_SPLIT = 0, 1
 XK_WHICH_COMBINED, XK_WHICH_NORMAL, XK_WHICH_FRICTION = 0, 1, 2
 REC_STRIDE = {XK_OUT_COMBINED: 16, XK_OUT_SPLIT: 32}
 XK_GATHER_DEFAULT, XK_GATHER_LANES, XK_GATHER_CHUNKS, XK_GATHER_SIDES = 0, 1, 2, 3
+XK_GATHER_SIDES_SUMS, XK_GATHER_SIDES_BLOCKS = 4, 5
 XK_COAT_FORCE, XK_COAT_TANGENT, XK_COAT_FRICTION, XK_COAT_FRICTION_TANGENT = 1, 2, 4, 8
 
 vp = C.c_void_p

@@ -297,14 +297,23 @@ class AssemblyEngine:
         gather = tangent and self.pattern.nnzb > 0
         # the element-side schedules leave per-element force sums that the residual reads
         elem_force = gather and self.gather_variant == L.XK_GATHER_SIDES
+        sums_done = None
         if gather:
             st.wait_stream(main)
-            L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
-                   self.gather_variant, ptr(self.K_c), stream_handle(st))
+            if elem_force:  # element sums, then the blocks; the residual needs only the sums
+                L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
+                       L.XK_GATHER_SIDES_SUMS, ptr(self.K_c), stream_handle(st))
+                sums_done = torch.cuda.Event()
+                sums_done.record(st)
+                L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
+                       L.XK_GATHER_SIDES_BLOCKS, ptr(self.K_c), stream_handle(st))
+            else:
+                L.call("xk_contact_gather_tangent", pat, ptr(self.rec), p, L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED,
+                       self.gather_variant, ptr(self.K_c), stream_handle(st))
         # residual after the members (or the tangent gather's element sums) and the beam
         main.wait_stream(sb)
         if elem_force:
-            main.wait_stream(st)
+            main.wait_event(sums_done)
             L.call("xk_contact_gather_force_elem", pat, p, ptr(self.f_int), -1.0, ptr(f_ext), ptr(fixed),
                    ptr(self.R), ptr(self.norm2), s)
         else:
