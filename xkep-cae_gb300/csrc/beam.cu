@@ -756,73 +756,6 @@ __global__ void k_beam_zero32(int n_nodes, const int32_t* __restrict__ node_diag
   }
 }
 
-__global__ void __launch_bounds__(BEAM_T) k_beam32(xk_mesh m, xk_section sec, const float* __restrict__ e32,
-                                                   const int32_t* __restrict__ order, int k0, int k1,
-                                                   const int32_t* __restrict__ blk, const uint8_t* __restrict__ first,
-                                                   const float* __restrict__ n32, double* __restrict__ f_int,
-                                                   float* __restrict__ Kv) {
-  const int k = k0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= k1) return;
-  const int e = order[k];
-  const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
-  const float* E = e32 + (long long)e * XK_ELEM32_STRIDE;
-  const float dx0[3] = {E[0], E[1], E[2]};
-  const float L0 = E[3];
-  float R0[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) R0[i] = E[4 + i];
-  const float* NA = n32 + (long long)a * XK_NODE32_STRIDE + 6;
-  const float* NB = n32 + (long long)b * XK_NODE32_STRIDE + 6;
-  float ua[6], ub[6];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) { ua[i] = NA[i]; ub[i] = NB[i]; }
-  const float du[3] = {ub[0] - ua[0], ub[1] - ua[1], ub[2] - ua[2]};
-  const float dxd[3] = {dx0[0] + du[0], dx0[1] + du[1], dx0[2] + du[2]};
-  const float Ld = sqrtf(dot3(dxd, dxd));
-  const float iLd = 1.0f / Ld;
-  const float two_dx_du[3] = {2.0f * dx0[0] + du[0], 2.0f * dx0[1] + du[1], 2.0f * dx0[2] + du[2]};
-  const float dax = dot3(du, two_dx_du) / (Ld + L0);
-  const float exd[3] = {dxd[0] * iLd, dxd[1] * iLd, dxd[2] * iLd};
-  float qr[4];
-  {
-    float v[3];
-    cross3(R0, du, v);
-    const float opc = fmaxf((Ld + L0 + dot3(R0, du)) * iLd, 1e-12f);
-    const float w = sqrtf(0.5f * opc);
-    const float kk = 0.5f * iLd / w;
-    qr[0] = w; qr[1] = kk * v[0]; qr[2] = kk * v[1]; qr[3] = kk * v[2];
-  }
-  const float qrc[4] = {qr[0], -qr[1], -qr[2], -qr[3]};
-  float th1[3], th2[3];
-  {
-    float qn[4], qx[4], tx[3];
-    quat_of_rotvecf(ua + 3, qn);
-    qmulf(qrc, qn, qx);
-    rotvec_of_quatf(qx, tx);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) th1[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
-    quat_of_rotvecf(ub + 3, qn);
-    qmulf(qrc, qn, qx);
-    rotvec_of_quatf(qx, tx);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) th2[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
-  }
-  float Rrod[9], Rcr[9];
-  {
-    const float w = qr[0], x = qr[1], y = qr[2], z = qr[3];
-    Rrod[0] = 1.f - 2.f * (y * y + z * z); Rrod[1] = 2.f * (x * y - w * z); Rrod[2] = 2.f * (x * z + w * y);
-    Rrod[3] = 2.f * (x * y + w * z); Rrod[4] = 1.f - 2.f * (x * x + z * z); Rrod[5] = 2.f * (y * z - w * x);
-    Rrod[6] = 2.f * (x * z - w * y); Rrod[7] = 2.f * (y * z + w * x); Rrod[8] = 1.f - 2.f * (x * x + y * y);
-  }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      Rcr[3 * i + j] = R0[3 * i] * Rrod[3 * j] + R0[3 * i + 1] * Rrod[3 * j + 1] + R0[3 * i + 2] * Rrod[3 * j + 2];
-  beam_tail<float>(ke_coef<float>(sec, L0), Rcr, exd, iLd, th1, th2, ua + 3, ub + 3, dax, a, b, e, first[e], blk,
-                   f_int, Kv);
-}
-
 __global__ void k_beam_prepare32(xk_mesh m, const double* __restrict__ ref, float* __restrict__ e32) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.n_elems) return;
