@@ -169,3 +169,12 @@ def test_pattern_row_capacity_is_an_error():
         eng.detect(_dev(np.zeros(6 * len(coords))))
     assert e.value.code == L.XK_ERR_OVERFLOW and "256" in str(e.value)
     torch.cuda.synchronize()  # the context is still usable
+
+
+def test_zero_length_element_is_refused():
+    """An element whose two nodes coincide raises ValueError, as in the reference
+    (elements/_beam_cr.py:50-56), before any beam kernel runs."""
+    coords = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 1.0], [0.0, 0.0, 1.0]])
+    conn = np.array([[0, 1], [1, 2]])
+    with pytest.raises(ValueError, match="zero length"):
+        AssemblyEngine(coords, conn, 0.3, _section(), precision="mixed", k_pen=1e4, mu=0.1)

@@ -226,7 +226,20 @@ class DeviceBeam:
         self.elem_ref = torch.empty(10 * max(mesh.n_elems, 1), dtype=torch.float64, device=dev)
         self.update_reference_frames()
 
+    def check_lengths(self):
+        """Raise ValueError for an element whose two nodes coincide (length < 1e-15), as the reference
+        does (``_beam3d_length_and_direction``, ``elements/_beam_cr.py:50-56``)."""
+        if self.mesh.n_elems == 0:
+            return
+        X = self.mesh.X.view(-1, 3)
+        c = self.mesh.conn.view(-1, 2).long()
+        L = torch.linalg.vector_norm(X[c[:, 1]] - X[c[:, 0]], dim=1)
+        bad = torch.nonzero(L < 1e-15)
+        if bad.numel():
+            raise ValueError(f"element {int(bad[0, 0])} has (almost) zero length: its two nodes coincide")
+
     def update_reference_frames(self, stream=None):
+        self.check_lengths()
         vr = None if self.v_ref is None else (C.c_double * 3)(*self.v_ref.tolist())
         L.call("xk_beam_reference", C.byref(self.mesh.c), vr, ptr(self.elem_ref), stream_handle(stream))
 
