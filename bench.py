@@ -65,7 +65,7 @@ class ClockSampler:
         self.path = None
 
     def __enter__(self):
-        out_dir = ROOT / "gpurun_out" if (ROOT / "gpurun_out").is_dir() else Path(tempfile.gettempdir())
+        out_dir = Path(os.environ.get("XK_CLOCKS_DIR", tempfile.gettempdir()))
         self.path = out_dir / f"clocks_{os.getpid()}.csv"
         try:
             self.f = open(self.path, "w")
@@ -275,8 +275,8 @@ def pruning_section(args, dev, w, u0, u1, ms_fp64):
     """The mixed assembly with the learned candidate pruning, per Newton iteration.
 
     The network is trained here, on the GPU, on exact-path labels of 7- and
-    37-wire strands; the first detection of the workload is judged exactly
-    (missed contacts are reported; the judge puts any back, so R is unchanged).
+    37-wire strands; the first detection of the workload is verified exactly
+    (missed contacts are reported; the verification puts any back, so R is unchanged).
     """
     import dataclasses
 
@@ -326,10 +326,10 @@ def pruning_section(args, dev, w, u0, u1, ms_fp64):
     del ref
     eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", device=dev,
                          **w.engine_kwargs())
-    eng.set_pruner(pr, judge_every=10)
+    eng.set_pruner(pr, verify_every=10)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    stats = eng.detect(u0)  # the first detection is a judged one
+    stats = eng.detect(u0)  # the first detection is a verified one
     torch.cuda.synchronize()
     t_det = time.perf_counter() - t0
     eng.assemble(u1, u0)
@@ -339,11 +339,11 @@ def pruning_section(args, dev, w, u0, u1, ms_fp64):
     ps = eng.prune_stats
     out = {"ms_per_step": ms, "speedup_vs_fp64_plain_per_iteration": ms_fp64 / ms,
            "pairs_in_table": eng.pairs.n, "candidates": stats["candidates"],
-           "kept_fraction": ps["kept"] / max(ps["candidates"], 1), "judged_detections": ps["judged"],
+           "kept_fraction": ps["kept"] / max(ps["candidates"], 1), "verified_detections": ps["verified"],
            "missed_contacts": ps["missed"], "members": stats["members"], "pairs_without_pruning": n_ref,
-           "detect_ms_judged": 1e3 * t_det, "detect_ms_without_pruning": 1e3 * t_det_ref,
+           "detect_ms_verified": 1e3 * t_det, "detect_ms_without_pruning": 1e3 * t_det_ref,
            "R_rel_diff_vs_unpruned": R_diff, "train_s": t_train, "train": dataclasses.asdict(rep),
-           "judge_every": eng.judge_every}
+           "verify_every": eng.verify_every}
     out["scoring"] = mlp_scoring(pr, (stats["candidates"], 8_000_000), 20, 3, dev)
     del eng, pr
     torch.cuda.empty_cache()
@@ -623,7 +623,7 @@ def run_gpu(args, rank, world):
         sub = prep[0]
         cpu = {"value": units_c / dt, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"NumPy oracle, one Newton-iteration assembly (contact + beam) on the first 1/48 of every "
-                         f"wire ({sub.n_elems} elements, {prep[2]['ea'].shape[0]} pairs), host of the GPU box"}
+                         f"wire ({sub.n_elems} elements, {prep[2]['ea'].shape[0]} pairs), host cores of the machine that runs the bench"}
 
     mixed_variant = engines["mixed"].gather_variant
     fp64_variant = engines["fp64"].gather_variant

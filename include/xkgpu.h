@@ -545,7 +545,7 @@ xk_status xk_bicgstab(const xk_system* A, const double* b, double* x, const doub
  * an MLP (XK_MLP_IN inputs -> 64 -> 64 -> 64 -> 1, ReLU, BF16 weights and
  * activations, FP32 accumulation) scores each candidate pair; candidates below
  * a threshold skip the pair table.  The exact broadphase + narrowphase stays
- * the judge (AssemblyEngine runs it every N detections).  Parameters are one
+ * the referee (AssemblyEngine runs it every N detections).  Parameters are one
  * float vector of XK_MLP_PARAMS values: W1 (64 x 8), b1, W2 (64 x 64), b2,
  * W3 (64 x 64), b3, w4 (64), b4.
  * ---------------------------------------------------------------------- */

@@ -11,7 +11,7 @@ GPU kernels implement:
   (``xkep_cae/contact/...``)
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may import it, and only as the checker or the timed CPU
+``bench.py`` may import it, and only as the parity reference or the timed CPU
 baseline.  The product path (``xkgpu``) never imports it.
 
 The oracle is pinned to the reference by golden vectors produced by running

@@ -1,6 +1,6 @@
 """Learned candidate pruning on the GPU: features, tensor-core forward, training
 kernels (gradients and Adam against the CPU oracle), and the trained network in
-the detection loop with the exact path as judge: zero missed contacts, identical
+the detection loop with the exact path as referee: zero missed contacts, identical
 assembly, fewer pairs per Newton iteration."""
 
 from __future__ import annotations
@@ -160,10 +160,10 @@ def test_trained_pruner_in_detection_loop():
     rep = pr.fit(feat, y, epochs=300, lr=3e-3)
     assert rep.recall == 1.0
     assert rep.loss_last < rep.loss_first
-    # held-out strand: every detection judged exactly
+    # held-out strand: every detection verified exactly
     w = W.config_workload("strand91", seed=11)
     exact, pruned = _engine(w, "mixed"), _engine(w, "mixed")
-    pruned.set_pruner(pr, judge_every=1)
+    pruned.set_pruner(pr, verify_every=1)
     rng = np.random.default_rng(5)
     u = w.u.copy()
     mask = np.tile([1, 1, 1, 0, 0, 0], w.strand.n_nodes)
@@ -180,7 +180,7 @@ def test_trained_pruner_in_detection_loop():
         assert abs(ke - kp).max() <= 1e-12 * abs(ke).max()
         u = u1.cpu().numpy()
     st = pruned.prune_stats
-    assert st["judged"] == 3 and st["missed"] == 0
+    assert st["verified"] == 3 and st["missed"] == 0
     # the gain: the pair table (narrowphase work per detection and per Newton iteration) shrinks
     assert pruned.pairs.n < 0.8 * exact.pairs.n
     assert st["kept"] < 0.8 * st["candidates"]

@@ -87,11 +87,11 @@ class AssemblyEngine:
         self.gather_variant = L.XK_GATHER_DEFAULT
         self.autotune = True
         self._tuned_for = None
-        # learned candidate pruning (``set_pruner``); the exact path is the judge every ``judge_every`` detections
+        # learned candidate pruning (``set_pruner``); the exact path verifies it every ``verify_every`` detections
         self.pruner = None
-        self.judge_every = 10
+        self.verify_every = 10
         self._n_detect = 0
-        self.prune_stats = {"detections": 0, "judged": 0, "candidates": 0, "kept": 0, "missed": 0}
+        self.prune_stats = {"detections": 0, "verified": 0, "candidates": 0, "kept": 0, "missed": 0}
 
     # ------------------------------------------------------------------ buffers
     @property
@@ -163,15 +163,15 @@ class AssemblyEngine:
             n = self.pairs.n
             self.pairs.t["coat_cc_prev"][:n].copy_(self.pairs.t["coat_cc"][:n])
 
-    def set_pruner(self, pruner, judge_every: int = 10):
-        """Use a trained ``PairPruner`` at detection; every ``judge_every``-th detection checks it exactly."""
+    def set_pruner(self, pruner, verify_every: int = 10):
+        """Use a trained ``PairPruner`` at detection; every ``verify_every``-th detection checks it exactly."""
         if self.coated:
             raise NotImplementedError("candidate pruning is not combined with the coating model")
         self.pruner = pruner
-        self.judge_every = max(1, int(judge_every))
+        self.verify_every = max(1, int(verify_every))
 
     def _prune(self, u, cands, nc, s, stream):
-        """Candidates the pruner keeps (plus every pair with history), judged exactly when due."""
+        """Candidates the pruner keeps (plus every pair with history), verified exactly when due."""
         pr = self.pruner
         feat, hist = pr.features(self.mesh, u, cands, nc, self.pairs, stream)
         logit = pr.logits(feat, nc, stream)
@@ -187,10 +187,10 @@ class AssemblyEngine:
             st["scoring_failed"] = st.get("scoring_failed", 0) + 1
             st["kept"] += nc
             return cands, nc
-        if self._n_detect % self.judge_every == 0:
-            # judge: the exact narrowphase of every pruned candidate; any that the exact path would
+        if self._n_detect % self.verify_every == 0:
+            # verification: the exact narrowphase of every pruned candidate; any that the exact path would
             # activate is a missed contact and the whole candidate set is used instead
-            st["judged"] += 1
+            st["verified"] += 1
             dropped = torch.empty(2 * max(nc - nk, 1), dtype=torch.int32, device=self.device)
             nd = C.c_int64(0)
             L.call("xk_prune_select", ptr(cands), nc, ptr(logit), ptr(hist), pr.threshold, 1, ptr(dropped),
@@ -205,7 +205,7 @@ class AssemblyEngine:
                 L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(tmp.c), ptr(u), C.byref(self.cp), 1, s)
                 missed = int((tmp.t["status"][: tmp.n] != 0).sum().item())
             st["missed"] += missed
-            st["last_judge_missed"] = missed
+            st["last_verify_missed"] = missed
             if missed:
                 st["kept"] += nc
                 return cands, nc

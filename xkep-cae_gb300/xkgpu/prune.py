@@ -4,8 +4,8 @@ A BF16 MLP (8 -> 64 -> 64 -> 64 -> 1) scores every broadphase candidate from
 cheap geometric features; candidates scored below a threshold stay out of the
 pair table, so the per-iteration narrowphase and the detection narrowphase run
 on fewer pairs.  Pairs with contact history are never pruned, and the exact
-broadphase + narrowphase remains the judge: ``AssemblyEngine`` checks the
-pruned candidates exactly every ``judge_every`` detections and puts back any
+broadphase + narrowphase remains the referee: ``AssemblyEngine`` checks the
+pruned candidates exactly every ``verify_every`` detections and puts back any
 that the exact path would activate.
 
 The network is trained on the GPU by the xkgpu kernels (forward with stored
