@@ -423,6 +423,66 @@ def coated_section(args, dev):
     return out
 
 
+def device_solve_section(args, dev):
+    """Newton increments with the linear solve on the device against scipy's direct solve.
+
+    The 7-wire strand with its initial penetration relaxed to equilibrium (frictionless, k_pen 1e4 N/mm,
+    both wire ends clamped), FP64, the well-posed increment of the Newton tests: ``solve_increment(graph=True, solver=DeviceLinearSolver)`` keeps
+    the iteration on the device (assembly graph, block-Jacobi BiCGStab, update), the other run solves
+    each Newton step with ``scipy.sparse.linalg.spsolve`` on the host.  One untimed increment first.
+    """
+    import torch
+
+    from xkgpu import workloads as W
+    from xkgpu.engine import AssemblyEngine
+    from xkgpu.newton import solve_increment
+    from xkgpu.solve import DeviceLinearSolver
+
+    w = W.config_workload("strand7", seed=0)
+    st = w.strand
+    kw = w.engine_kwargs()
+    kw.update(k_pen=1e4, mu=0.0)
+    npw = st.n_elems_per_wire + 1
+    fixed = np.zeros((st.n_nodes, 6), dtype=bool)
+    for wi in range(len(st.wires)):
+        fixed[wi * npw] = True
+        fixed[wi * npw + npw - 1] = True
+    fixed = fixed.ravel()
+    out = {"workload": "strand7 (7 wires, 119 nodes, 714 DOFs), frictionless, k_pen 1e4 N/mm, clamped ends, "
+                       "FP64; one Newton increment from the initial penetration to equilibrium (tol 1e-9)"}
+    u_ref = {}
+    for name in ("device", "host"):
+        eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="fp64", device=dev, **kw)
+        u0 = torch.zeros(eng.mesh.ndof, dtype=torch.float64, device=dev)
+        ds = DeviceLinearSolver(eng, rtol=1e-10, max_iter=2000) if name == "device" else None
+        try:
+            for rep in range(2):
+                if ds is not None:
+                    ds.history.clear()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                res = solve_increment(eng, u0, u0, fixed=fixed, tol=1e-9, max_iter=25, solver=ds,
+                                      graph=ds is not None)
+                torch.cuda.synchronize()
+                t = time.perf_counter() - t0
+        except Exception as exc:  # noqa: BLE001 - reported in the bench line
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+            continue
+        u_ref[name] = res.u.cpu().numpy()
+        rec = {"converged": res.converged, "newton_iterations": res.iterations, "ms_per_increment": 1e3 * t,
+               "ms_per_newton_iteration": 1e3 * t / max(res.iterations, 1)}
+        if ds is not None and ds.history:
+            its = [h[0] for h in ds.history]
+            rec.update(bicgstab_iterations_per_solve=float(np.mean(its)), solves=len(its))
+        out[name] = rec
+    if "device" in u_ref and "host" in u_ref:
+        a, b = u_ref["device"], u_ref["host"]
+        out["u_rel_diff_device_vs_host"] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+        if "ms_per_increment" in out["device"] and "ms_per_increment" in out["host"]:
+            out["speedup_device_vs_host"] = out["host"]["ms_per_increment"] / out["device"]["ms_per_increment"]
+    return out
+
+
 def rank_aggregate(t_max, n_sum, device=None):
     """Times maxed and unit counts summed over the ranks of the default process group.
 
@@ -636,6 +696,7 @@ def run_gpu(args, rank, world):
         extras["learned_pruning"] = pruning_section(args, dev, w, u0, u1, ms_fp64)
         extras["batched"] = batch_section(args, dev)
         extras["coated"] = coated_section(args, dev)
+        extras["device_solve"] = device_solve_section(args, dev)
 
     # node prep, the other-pair kernel and its near-parallel kernel, the beam's zeroing and element
     # launches, the member kernel and its near-parallel kernel, then either element sums + tangent

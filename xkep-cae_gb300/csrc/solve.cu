@@ -305,6 +305,48 @@ extern "C" xk_status xk_system_block_jacobi(const xk_system* A, double* dinv, xk
   return XK_OK;
 }
 
+namespace {
+
+// One BiCGStab iteration on stream st (scalars on the device).
+void bicgstab_iteration(const xk_system& A, long long n, int nb, const double* dinv, double* x, double* r,
+                        const double* rh, double* p, double* v, double* y, double* sv, double* z, double* t,
+                        double* part, double* sc, cudaStream_t st) {
+  dot2(n, rh, r, nullptr, nullptr, part, st);
+  k_scalars<1><<<1, SV_T, 0, st>>>(part, sc);  // beta, rho
+  k_update_p<<<nb, SV_T, 0, st>>>(n, r, v, p, sc);
+  k_apply_block_jacobi<<<nb, SV_T, 0, st>>>(A.n_nodes, dinv, p, y);
+  spmv_any(A, y, v, st);
+  dot2(n, rh, v, nullptr, nullptr, part, st);
+  k_scalars<2><<<1, SV_T, 0, st>>>(part, sc);  // alpha
+  k_update_xs<<<nb, SV_T, 0, st>>>(n, x, y, r, v, sv, sc);
+  k_apply_block_jacobi<<<nb, SV_T, 0, st>>>(A.n_nodes, dinv, sv, z);
+  spmv_any(A, z, t, st);
+  dot2(n, t, sv, t, t, part, st);
+  k_scalars<3><<<1, SV_T, 0, st>>>(part, sc);  // omega
+  k_update_xr<<<nb, SV_T, 0, st>>>(n, x, z, sv, t, r, sc);
+}
+
+// ||r||^2 into sc[S_RR]
+void residual_sq(long long n, const double* r, double* part, double* sc, cudaStream_t st) {
+  dot2(n, r, r, nullptr, nullptr, part, st);
+  k_scalars<4><<<1, SV_T, 0, st>>>(part, sc);
+}
+
+struct SolveStream {  // a private stream ordered after the caller's, and the graph of one check interval
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  ~SolveStream() {
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    if (ev) cudaEventDestroy(ev);
+    if (cs) cudaStreamDestroy(cs);
+  }
+};
+
+}  // namespace
+
 extern "C" xk_status xk_bicgstab(const xk_system* A, const double* b, double* x, const double* dinv, double* work,
                                  int32_t max_iter, int32_t check_every, double rtol, int32_t* iters, double* rel_res,
                                  xk_stream s) {
@@ -339,32 +381,43 @@ extern "C" xk_status xk_bicgstab(const xk_system* A, const double* b, double* x,
   const double bb = bb_rr[0] > 0.0 ? bb_rr[0] : 1.0;
   int it = 0;
   double res = 1.0;
-  for (; it < max_iter;) {
-    dot2(n, rh, r, nullptr, nullptr, part, st);
-    k_scalars<1><<<1, SV_T, 0, st>>>(part, sc);  // beta, rho
-    k_update_p<<<nb, SV_T, 0, st>>>(n, r, v, p, sc);
-    k_apply_block_jacobi<<<nb, SV_T, 0, st>>>(A->n_nodes, dinv, p, y);
-    spmv_any(*A, y, v, st);
-    dot2(n, rh, v, nullptr, nullptr, part, st);
-    k_scalars<2><<<1, SV_T, 0, st>>>(part, sc);  // alpha
-    k_update_xs<<<nb, SV_T, 0, st>>>(n, x, y, r, v, sv, sc);
-    k_apply_block_jacobi<<<nb, SV_T, 0, st>>>(A->n_nodes, dinv, sv, z);
-    spmv_any(*A, z, t, st);
-    dot2(n, t, sv, t, t, part, st);
-    k_scalars<3><<<1, SV_T, 0, st>>>(part, sc);  // omega
-    k_update_xr<<<nb, SV_T, 0, st>>>(n, x, z, sv, t, r, sc);
-    XK_CHECK_LAUNCH();
-    ++it;
-    if (it % check_every == 0 || it == max_iter) {
-      dot2(n, r, r, nullptr, nullptr, part, st);
-      k_scalars<4><<<1, SV_T, 0, st>>>(part, sc);
-      double rr = 0.0;
-      XK_CUDA(cudaMemcpyAsync(&rr, sc + S_RR, sizeof(double), cudaMemcpyDeviceToHost, st));
-      XK_CUDA(cudaStreamSynchronize(st));
-      res = sqrt(rr / bb);
-      if (!(res > rtol)) break;  // converged (or a NaN, reported through rel_res)
+  // every check interval (check_every iterations and the residual norm) is one CUDA graph, captured on
+  // a private stream; if capture is not possible the same kernels are launched one by one
+  SolveStream ss;
+  XK_CUDA(cudaStreamCreateWithFlags(&ss.cs, cudaStreamNonBlocking));
+  XK_CUDA(cudaEventCreateWithFlags(&ss.ev, cudaEventDisableTiming));
+  XK_CUDA(cudaEventRecord(ss.ev, st));
+  XK_CUDA(cudaStreamWaitEvent(ss.cs, ss.ev, 0));
+  const int interval = check_every < max_iter ? check_every : (max_iter > 0 ? max_iter : 1);
+  auto chunk = [&](int k, cudaStream_t cs) {
+    for (int q = 0; q < k; ++q) bicgstab_iteration(*A, n, nb, dinv, x, r, rh, p, v, y, sv, z, t, part, sc, cs);
+    residual_sq(n, r, part, sc, cs);
+  };
+  if (max_iter >= interval &&
+      cudaStreamBeginCapture(ss.cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    chunk(interval, ss.cs);
+    if (cudaStreamEndCapture(ss.cs, &ss.g) != cudaSuccess ||
+        cudaGraphInstantiate(&ss.ge, ss.g, 0) != cudaSuccess) {
+      ss.ge = nullptr;
+      cudaGetLastError();  // capture not possible here: launch one by one
     }
+  } else {
+    cudaGetLastError();
   }
+  while (it < max_iter) {
+    const int k = (max_iter - it) < interval ? (max_iter - it) : interval;
+    if (ss.ge && k == interval) XK_CUDA(cudaGraphLaunch(ss.ge, ss.cs));
+    else chunk(k, ss.cs);
+    XK_CHECK_LAUNCH();
+    it += k;
+    double rr = 0.0;
+    XK_CUDA(cudaMemcpyAsync(&rr, sc + S_RR, sizeof(double), cudaMemcpyDeviceToHost, ss.cs));
+    XK_CUDA(cudaStreamSynchronize(ss.cs));
+    res = sqrt(rr / bb);
+    if (!(res > rtol)) break;  // converged (or a NaN, reported through rel_res)
+  }
+  XK_CUDA(cudaEventRecord(ss.ev, ss.cs));
+  XK_CUDA(cudaStreamWaitEvent(st, ss.ev, 0));  // the caller's stream sees x
   if (iters) *iters = it;
   if (rel_res) *rel_res = res;
   return XK_OK;

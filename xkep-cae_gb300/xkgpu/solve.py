@@ -6,7 +6,8 @@ identity, by a direct sparse factorisation on the host.  ``DeviceLinearSolver``
 keeps ``K = K_beam + K_c`` in the engine's block matrices and runs BiCGStab
 with a block-Jacobi preconditioner (each node's 6x6 diagonal block) in the
 ``xk_bicgstab`` kernels: no matrix leaves the device, and the only host
-synchronisations are the convergence checks.
+synchronisations are the convergence checks (each check interval of
+iterations replays as one CUDA graph).
 """
 
 from __future__ import annotations
@@ -39,6 +40,7 @@ class DeviceLinearSolver:
         self.sys = L.System()
         self.iterations = 0
         self.rel_res = 0.0
+        self.history: list[tuple[int, float]] = []  # (iterations, relative residual) of every solve
 
     def set_fixed(self, fixed) -> None:
         f = torch.as_tensor(np.asarray(fixed, dtype=np.uint8) if not torch.is_tensor(fixed) else fixed)
@@ -77,6 +79,7 @@ class DeviceLinearSolver:
         L.call("xk_bicgstab", C.byref(sysc), ptr(b), ptr(x), ptr(self.dinv), ptr(self.work), self.max_iter,
                self.check_every, self.rtol, C.byref(it), C.byref(rr), h)
         self.iterations, self.rel_res = int(it.value), float(rr.value)
+        self.history.append((self.iterations, self.rel_res))
         if self.strict and not (self.rel_res <= self.rtol):
             raise LinearSolveError(f"BiCGStab: relative residual {self.rel_res:.3e} after {self.iterations} "
                                    f"iterations (tolerance {self.rtol:.1e})")
