@@ -469,6 +469,9 @@ def test_host_pipeline_returns_each_steps_outputs():
         assert torch.equal(R, ref.R.cpu())
         assert torch.equal(Kb, ref.K_beam.cpu())
         assert torch.equal(Kc, ref.K_c[: Kc.numel()].cpu())
+        # the full matrices rebuilt from the host copies equal the engine's own views
+        assert (eng.K_beam_csr(Kb) != ref.K_beam_csr()).nnz == 0
+        assert (eng.K_contact_csr(Kc) != ref.K_contact_csr()).nnz == 0
 
     # the usual loop: submit step k, then read step k-1 while step k runs
     prev = pipe.submit(hosts[0], uref_h)

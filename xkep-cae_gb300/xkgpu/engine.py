@@ -401,9 +401,10 @@ class AssemblyEngine:
     def residual_norm(self) -> float:
         return float(np.sqrt(self.norm2.item()))
 
-    def K_beam_csr(self) -> sp.csr_matrix:
-        """The full beam tangent from its stored (row <= column) blocks and their transposes."""
-        return self.beam.to_csr(self.K_beam)
+    def K_beam_csr(self, vals: torch.Tensor | None = None) -> sp.csr_matrix:
+        """The full beam tangent from its stored (row <= column) blocks and their transposes; ``vals``
+        (e.g. a ``HostPipeline`` result) instead of the engine's own values."""
+        return self.beam.to_csr(self.K_beam if vals is None else vals)
 
     def K_contact_csr(self, vals: torch.Tensor | None = None) -> sp.csr_matrix:
         """The full contact tangent from its stored (row <= column) blocks and their mirrors."""
