@@ -42,8 +42,10 @@ XK_D unsigned long long spread21(unsigned long long v) {
   return v;
 }
 
+// boxf: the same boxes in float, rounded outward (lower corner down, upper corner up), as two float4
+// per segment (32 bytes): a conservative screen for the sweep, which then tests the FP64 boxes.
 __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, double* __restrict__ box,
-                       unsigned long long* __restrict__ ext) {
+                       float4* __restrict__ boxf, unsigned long long* __restrict__ ext) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   const long long ne = m.n_elems;
   unsigned long long lmin[3] = {~0ull, ~0ull, ~0ull}, lmax[3] = {0ull, 0ull, 0ull}, lext = 0ull;
@@ -51,6 +53,7 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
     int a = m.conn[2 * e], b = m.conn[2 * e + 1];
     const double ex = xadd(m.radii[e], margin);
     double mx = 0.0;
+    float lf[3], hf[3];
     for (int c = 0; c < 3; ++c) {
       double x0 = u ? xadd(m.X[3LL * a + c], u[6LL * a + c]) : m.X[3LL * a + c];
       double x1 = u ? xadd(m.X[3LL * b + c], u[6LL * b + c]) : m.X[3LL * b + c];
@@ -58,10 +61,14 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
       double hi = xadd(x0 < x1 ? x1 : x0, ex);
       box[c * ne + e] = lo;
       box[(3 + c) * ne + e] = hi;
+      lf[c] = __double2float_rd(lo);
+      hf[c] = __double2float_ru(hi);
       lmin[c] = enc_min(lo);
       lmax[c] = enc_min(hi);
       mx = fmax(mx, hi - lo);
     }
+    boxf[2LL * e] = make_float4(lf[0], lf[1], lf[2], 0.f);
+    boxf[2LL * e + 1] = make_float4(hf[0], hf[1], hf[2], 0.f);
     lext = (unsigned long long)__double_as_longlong(mx);
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -157,7 +164,8 @@ XK_D bool overlap(const double* box, long long ne, int i, int j) {
 
 // MODE 0: count per segment; MODE 1: emit (i, j) sorted by j within each segment.
 template <int MODE>
-__global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restrict__ box, const Grid* __restrict__ gp,
+__global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restrict__ box,
+                                                const float4* __restrict__ boxf, const Grid* __restrict__ gp,
                                                 const int32_t* __restrict__ segs, const int32_t* __restrict__ cstart,
                                                 const int32_t* __restrict__ cend, int excl_shared, int excl_layer,
                                                 int32_t* __restrict__ cnt, unsigned long long* __restrict__ raw_total,
@@ -173,6 +181,7 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
   cell_of(g, box[i], box[ne + i], box[2 * ne + i], c);
   const int ia = m.conn[2 * i], ib = m.conn[2 * i + 1];
   const int li = (excl_layer && m.layer) ? m.layer[i] : -1;
+  const float4 il = boxf[2LL * i], ih = boxf[2LL * i + 1];
   int n_raw = 0, n_keep = 0;
   const long long base = MODE == 1 ? (long long)off[i] : 0;
   for (int dz = -1; dz <= 1; ++dz) {
@@ -192,7 +201,12 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
           int j = -1;
           if (k < k1) {
             j = segs[k];
-            if (j > i && overlap(box, ne, i, j)) {
+            bool near = j > i;
+            if (near) {  // conservative float screen (outward-rounded boxes), then the exact FP64 test
+              const float4 jl = __ldg(boxf + 2LL * j), jh = __ldg(boxf + 2LL * j + 1);
+              near = il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z;
+            }
+            if (near && overlap(box, ne, i, j)) {
               hit = true;
               keep = true;
               if (excl_shared) {
@@ -440,14 +454,16 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   if (ne < 2) return XK_OK;
   Scratch S{st};
   double* box;
+  float4* boxf;
   unsigned long long* ext;
   Grid* grid;
   XK_TRY(S.get(&box, 6 * ne));
+  XK_TRY(S.get(&boxf, 2 * ne));
   XK_TRY(S.get(&ext, 8));
   XK_TRY(S.get(&grid, 1));
   unsigned long long init[8] = {0ull, ~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull};
   XK_CUDA(cudaMemcpyAsync(ext, init, sizeof(init), cudaMemcpyHostToDevice, st));
-  k_aabb<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, u, bp->margin, box, ext);
+  k_aabb<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, u, bp->margin, box, boxf, ext);
   const long long cap_cells = ne * 8 > 4096 ? ne * 8 : 4096;
   k_grid<<<1, 1, 0, st>>>(ext, cap_cells, grid);
   XK_CHECK_LAUNCH();
@@ -475,7 +491,7 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   XK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (ne + 1), st));
   const int sweep_blocks = xk_blocks(ne * 32, BP_T);
   const int excl_layer = (bp->exclude_same_layer && m->layer) ? 1 : 0;
-  k_sweep<0><<<sweep_blocks, BP_T, 0, st>>>(*m, box, grid, segs, cstart, cend, bp->exclude_shared, excl_layer, cnt,
+  k_sweep<0><<<sweep_blocks, BP_T, 0, st>>>(*m, box, boxf, grid, segs, cstart, cend, bp->exclude_shared, excl_layer, cnt,
                                              raw_dev, nullptr, nullptr, nullptr);
   XK_CHECK_LAUNCH();
   int64_t* tot;
@@ -494,7 +510,7 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   int32_t *tmp, *pairs1;
   XK_TRY(S.get(&tmp, n1));
   XK_TRY(S.get(&pairs1, 2 * n1));
-  k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, box, grid, segs, cstart, cend, bp->exclude_shared, excl_layer, cnt,
+  k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, box, boxf, grid, segs, cstart, cend, bp->exclude_shared, excl_layer, cnt,
                                              raw_dev, off, tmp, pairs1);
   XK_CHECK_LAUNCH();
   if (!bp->midpoint_prescreening) {
