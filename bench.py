@@ -701,7 +701,7 @@ def run_gpu(args, rank, world):
     # node prep, the other-pair kernel and its near-parallel kernel, the beam's zeroing and element
     # launches, the member kernel and its near-parallel kernel, then either element sums + tangent
     # gather + residual from the element sums (norm fused) or tangent gather + force gather + 2 norm
-    # kernels (the launch list in profiles/launches_strand1027.md shows the ten of the first form)
+    # kernels (an ncu launch list of one replayed step shows the ten launches of the first form)
     per_launch = 7 + (3 if mixed_variant == L.XK_GATHER_SIDES else 4)
     out = {
         "metric": METRIC, "value": units / t_mixed * args.steps, "unit": UNIT, "n_gpus": world,
@@ -750,6 +750,9 @@ def run_gpu(args, rank, world):
         key = {L.XK_GATHER_SIDES: "gather_tangent_sides_float"}.get(mixed_variant)
         out["roofline"]["traffic"] = d.get(key, {}).get("bytes_per_launch") if key else None
         out["roofline"]["pair_step"]["traffic"] = d.get("pair_step_mixed", {}).get("bytes_per_launch")
+        out["roofline"]["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a separate "
+                                             "capture, recorded in profiles/dram_traffic.json; not measured "
+                                             "in this run")
     return out
 
 

@@ -609,9 +609,11 @@ xk_status xk_pairs_drop_pristine(const xk_pairs* in, const int32_t* kept, int64_
  *     static 4 MiB device array in the library, so the pair table may hold at
  *     most XK_JACOBIAN_NOALLOC_MAX_PAIRS pairs; larger tables give XK_ERR_ARG
  *     (use xk_constraint_jacobian for them).
- *   - The first call on each device looks the array up (cudaGetSymbolAddress,
+ *   - The first call in each context looks the array up (cudaGetSymbolAddress,
  *     with that device current); make that call before work that must not see
- *     a set-up step.
+ *     a set-up step.  The address is kept per device together with the id of
+ *     its context, so a new context on the device (after cudaDeviceReset, or a
+ *     non-primary one) gets its own look-up.
  *   - The array is shared: calls on one device that overlap (two streams, two
  *     host threads) race on it and must be serialised by the caller.
  *   - Like xk_constraint_jacobian it synchronises the stream. */

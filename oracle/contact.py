@@ -104,38 +104,66 @@ def segment_aabbs(coords, conn, radii, margin=0.0):
     return np.minimum(x0, x1) - ex, np.maximum(x0, x1) + ex
 
 
+def _expand_ranges(first, count):
+    """Flat indices ``first[k] + r`` for ``r < count[k]``, and the owner ``k`` of each."""
+    total = int(count.sum())
+    owner = np.repeat(np.arange(count.size), count)
+    offs = np.arange(total) - np.repeat(np.cumsum(count) - count, count)
+    return owner, np.repeat(first, count) + offs
+
+
 def aabb_overlap_pairs(lo, hi, chunk=1 << 22):
     """All pairs ``i<j`` whose closed AABBs overlap on every axis, sorted.
 
     The reference bins AABBs into a uniform hash grid and then keeps the pairs
     that overlap (``_broadphase.py:52-96``); every overlapping pair shares a
-    cell, so its output is exactly this set whatever the cell size.  Here a
-    sort-and-sweep along the longest extent enumerates the set.
+    cell, so its output is exactly this set whatever the cell size.  Here the
+    cell is the largest box extent (a box covers at most two cells per axis),
+    and a pair is tested only in the cell that holds the lower corner of the
+    two boxes' intersection, the one cell that both boxes cover whenever they
+    overlap, so that no pair is produced twice.
     """
     n = lo.shape[0]
     if n < 2:
         return np.zeros((0, 2), dtype=np.int64)
-    ax = int(np.argmax(hi.max(0) - lo.min(0)))
-    order = np.argsort(lo[:, ax], kind="stable")
-    slo = lo[order, ax]
-    end = np.searchsorted(slo, hi[order, ax], side="right")
-    start = np.arange(n) + 1
-    cnt = np.maximum(end - start, 0)
+    base = lo.min(0)
+    cell = float(np.max(hi - lo))
+    if not cell > 0.0:
+        cell = 1.0
+    c0 = np.floor((lo - base) / cell).astype(np.int64)
+    c1 = np.floor((hi - base) / cell).astype(np.int64)
+    dims = c1.max(0) + 1
+    span = c1 - c0 + 1
+    per = span.prod(1)
+    box, k = _expand_ranges(np.zeros(n, dtype=np.int64), per)
+    sx, sy = span[box, 0], span[box, 1]
+    cx = c0[box, 0] + k % sx
+    cy = c0[box, 1] + (k // sx) % sy
+    cz = c0[box, 2] + k // (sx * sy)
+    key = (cz * dims[1] + cy) * dims[0] + cx
+    order = np.lexsort((box, key))
+    key, box = key[order], box[order]
+    gstart = np.flatnonzero(np.r_[True, key[1:] != key[:-1]])
+    gsize = np.diff(np.r_[gstart, key.size])
+    pos = np.arange(key.size) - np.repeat(gstart, gsize)
+    partners = np.repeat(gsize, gsize) - 1 - pos  # later entries of the same cell
     out = []
-    # expand (i, j) ranges in chunks
-    cum = np.concatenate([[0], np.cumsum(cnt)])
-    total = int(cum[-1])
-    pos = 0
-    while pos < total:
-        hi_pos = min(total, pos + chunk)
-        flat = np.arange(pos, hi_pos)
-        ii = np.searchsorted(cum, flat, side="right") - 1
-        jj = start[ii] + (flat - cum[ii])
-        a, b = order[ii], order[jj]
+    lo_e = np.cumsum(partners) - partners
+    e = 0
+    while e < key.size:  # expand in slices of about ``chunk`` pairs
+        stop = int(np.searchsorted(lo_e, lo_e[e] + chunk, side="right"))
+        stop = max(stop, e + 1)
+        owner, other = _expand_ranges(np.arange(e, stop) + 1, partners[e:stop])
+        owner = owner + e
+        a, b = box[owner], box[other]
         ok = np.all(lo[a] <= hi[b], axis=1) & np.all(lo[b] <= hi[a], axis=1)
-        a, b = a[ok], b[ok]
+        a, b, kk = a[ok], b[ok], key[owner[ok]]
+        home = np.floor((np.maximum(lo[a], lo[b]) - base) / cell).astype(np.int64)
+        hk = (home[:, 2] * dims[1] + home[:, 1]) * dims[0] + home[:, 0]
+        keep = hk == kk
+        a, b = a[keep], b[keep]
         out.append(np.stack([np.minimum(a, b), np.maximum(a, b)], axis=1))
-        pos = hi_pos
+        e = stop
     pairs = np.concatenate(out) if out else np.zeros((0, 2), dtype=np.int64)
     if pairs.shape[0]:
         pairs = pairs[np.lexsort((pairs[:, 1], pairs[:, 0]))]
@@ -183,6 +211,9 @@ def merge_candidates(table: dict, cands, conn, radii, core_radii=None) -> dict:
     cands = np.asarray(cands, dtype=np.int64).reshape(-1, 2)
     old_key = table["ea"].astype(np.int64) * (1 << 32) + table["eb"]
     new_key = cands[:, 0] * (1 << 32) + cands[:, 1]
+    if old_key.size == 0:  # first detection: the fresh records, sorted by key
+        fresh = new_pairs(cands, conn, radii, core_radii)
+        return fresh if np.all(new_key[1:] >= new_key[:-1]) else take(fresh, np.argsort(new_key, kind="stable"))
     t = copy_table(table)
     in_new = np.isin(old_key, new_key)
     t["status"][~in_new] = INACTIVE
@@ -411,14 +442,26 @@ def friction_evaluate(table: dict, u, u_ref, ndof: int, k_pen: float, k_t_ratio:
 
 
 def _blocks_to_csr(nodes, blocks, ndof):
-    """Assemble per-pair (4x4 node) x (3x3) blocks, shape (P,4,4,3,3), to CSR."""
+    """Assemble per-pair (4x4 node) x (3x3) blocks, shape (P,4,4,3,3), to CSR.
+
+    Blocks with the same (row node, column node) are summed, then laid out as
+    3x3 blocks of a block matrix whose block (2a, 2b) is the translational
+    block of nodes a and b.
+    """
     P = nodes.shape[0]
     if P == 0:
         return sp.csr_matrix((ndof, ndof))
-    dofs = trans_dofs(nodes).reshape(P, 4, 3)
-    rows = np.broadcast_to(dofs[:, :, None, :, None], (P, 4, 4, 3, 3))
-    cols = np.broadcast_to(dofs[:, None, :, None, :], (P, 4, 4, 3, 3))
-    return sp.csr_matrix((blocks.ravel(), (rows.ravel(), cols.ravel())), shape=(ndof, ndof))
+    nn = ndof // 6
+    nodes = np.asarray(nodes, dtype=np.int64)
+    key = (nodes[:, :, None] * nn + nodes[:, None, :]).ravel()
+    order = np.argsort(key, kind="stable")
+    key = key[order]
+    start = np.flatnonzero(np.r_[True, key[1:] != key[:-1]])
+    summed = np.add.reduceat(blocks.reshape(-1, 3, 3)[order], start, axis=0)
+    ukey = key[start]
+    brow, bcol = 2 * (ukey // nn), 2 * (ukey % nn)
+    indptr = np.searchsorted(brow, np.arange(2 * nn + 1))
+    return sp.bsr_matrix((summed, bcol, indptr), shape=(ndof, ndof)).tocsr()
 
 
 def huber_tangent(table: dict, ndof: int, k_pen: float, smoothing_delta: float = 0.0):

@@ -381,8 +381,26 @@ def gauss_case(R, name, seed=11, n=1200):
     print(name, n, np.bincount(ng))
 
 
+def protocols_case(R, name):
+    """Method names and parameter names, in order, of the Strategy Protocols
+    (``xkep_cae/core/strategies/protocols.py:17-256``), as JSON."""
+    import importlib
+    import inspect
+    import json
+
+    mod = importlib.import_module("xkep_cae.core.strategies.protocols")
+    out = {}
+    for proto in ("ContactForceStrategy", "FrictionStrategy", "ContactGeometryStrategy", "PenaltyStrategy",
+                  "TimeIntegrationStrategy"):
+        p = getattr(mod, proto)
+        out[proto] = {n: [q for q in inspect.signature(v).parameters if q != "self"]
+                      for n, v in vars(p).items() if callable(v) and not n.startswith("_")}
+    (HERE / f"{name}.json").write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+
+
 CASES = {
-    "strand7": lambda R: strand_case(R, "strand7", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16,
+    "protocols": lambda R: protocols_case(R, "protocols"),
+    "strand7":lambda R: strand_case(R, "strand7", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16,
                                      gap_frac=-0.005, seed=0, mu=0.1),
     "strand7_nogap": lambda R: strand_case(R, "strand7_nogap", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16,
                                            gap_frac=0.0, seed=0, mu=0.1, n_iter=1, n_incr=1),

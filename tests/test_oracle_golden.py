@@ -177,3 +177,20 @@ def test_coating_oracle_matches_reference():
         assert rel_err(state["dissipation"], z[p + "post_coat_diss"]) < 1e-10
         K = oc.coating_friction_stiffness(table, cc, state, n, k, ktr, mu)
         assert sparse_rel_err(K, golden_csr(z, p + "K_coat_fric", n)) < 1e-12
+
+
+def test_oracle_broadphase_equals_all_pairs():
+    """The grid enumeration returns exactly the pairs whose closed boxes overlap: random boxes of mixed
+    sizes, boxes that only touch, duplicates, a degenerate (point) box."""
+    rng = np.random.default_rng(9)
+    n = 400
+    lo = rng.uniform(0.0, 10.0, (n, 3))
+    hi = lo + rng.uniform(0.0, 2.0, (n, 3)) * (rng.random((n, 1)) < 0.9)
+    lo[1], hi[1] = hi[0], hi[0] + 1.0  # touches box 0 at a corner
+    lo[2], hi[2] = lo[3].copy(), hi[3].copy()  # duplicate
+    got = oc.aabb_overlap_pairs(lo, hi, chunk=997)
+    i, j = np.triu_indices(n, 1)
+    ok = np.all(lo[i] <= hi[j], axis=1) & np.all(lo[j] <= hi[i], axis=1)
+    want = np.stack([i[ok], j[ok]], axis=1)
+    assert np.array_equal(got, want)
+    assert [0, 1] in got.tolist() and [2, 3] in got.tolist()

@@ -4,9 +4,8 @@ Strategy Protocols."""
 
 from __future__ import annotations
 
-import importlib.util
 import inspect
-import os
+import json
 from pathlib import Path
 
 import numpy as np
@@ -17,6 +16,7 @@ from conftest import golden
 torch = pytest.importorskip("torch")
 
 from oracle import contact as oc  # noqa: E402
+from xkgpu import dynamics as D  # noqa: E402
 from xkgpu import penalty as P  # noqa: E402
 from xkgpu import strategies as S  # noqa: E402
 
@@ -115,15 +115,9 @@ def test_gpu_classes_need_a_gpu():
         S.PairBatch(_pairs(2), 100)
 
 
-def _reference_protocols():
-    root = Path(os.environ.get("XKEP_CAE_REFERENCE", "/root/reference"))
-    f = root / "xkep_cae" / "core" / "strategies" / "protocols.py"
-    if not f.exists():
-        pytest.skip("the reference source tree is not available")
-    spec = importlib.util.spec_from_file_location("_xkep_protocols", f)
-    mod = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(mod)
-    return mod
+def _reference_protocols() -> dict:
+    """Protocol method and parameter names recorded from the reference by ``tests/golden/make_golden.py``."""
+    return json.loads((Path(__file__).resolve().parent / "golden" / "protocols.json").read_text())
 
 
 @pytest.mark.parametrize("proto,cls", [
@@ -134,15 +128,14 @@ def _reference_protocols():
     ("ContactGeometryStrategy", S.GpuMortarSegment),
     ("PenaltyStrategy", P.AutoEALPenalty),
     ("PenaltyStrategy", P.ContinuationPenalty),
+    ("TimeIntegrationStrategy", D.GpuGeneralizedAlpha),
+    ("TimeIntegrationStrategy", D.QuasiStatic),
 ])
 def test_protocol_signatures(proto, cls):
     """Every Protocol method exists with the reference's parameter names, in order."""
-    mod = _reference_protocols()
-    p = getattr(mod, proto)
-    names = [n for n, v in vars(p).items() if callable(v) and not n.startswith("_")]
-    assert names
-    for n in names:
-        want = [q for q in inspect.signature(getattr(p, n)).parameters if q != "self"]
+    methods = _reference_protocols()[proto]
+    assert methods
+    for n, want in methods.items():
         got = [q for q in inspect.signature(getattr(cls, n)).parameters if q != "self"]
         assert got[: len(want)] == want, (n, got, want)
 

@@ -763,12 +763,7 @@ __global__ void __launch_bounds__(GS_T, sizeof(T) == 4 ? 16 : 8) k_gather_tangen
 
 // persistent grid of the sides gather: every SM's share of CTAs, or one CTA per tile when fewer
 int sides_grid(long long nnzb, int per_sm) {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
-  }
+  const int sms = xk_sm_count();
   const long long tiles = (nnzb + GS_T - 1) / GS_T;
   const long long cap = (long long)sms * per_sm;
   return (int)(tiles < cap ? (tiles > 0 ? tiles : 1) : cap);

@@ -2,7 +2,10 @@
 // the factorised pair tangent.  One thread per pair; contributing pairs and
 // the rest run as two launches over the per-increment lists so that warps do
 // not diverge between the two kinds of work.
+#include <cuda.h>
+
 #include <atomic>
+#include <mutex>
 
 #include "xk_common.cuh"
 
@@ -1305,19 +1308,66 @@ constexpr long long JNA_WORDS = 32 + JNA_TILES + JNA_MAX_PAIRS / 2;
 static_assert(JNA_MAX_PAIRS % 2 == 0, "flags are packed two per word");
 
 static __device__ __align__(256) int64_t g_jna_scratch[JNA_WORDS];
-std::atomic<int64_t*> g_jna_ptr[64];
 
-// Address of this device's scratch array.  The first call on each device looks
-// the symbol up (which loads this module's device globals there); make it
-// before any work that must not see a set-up call.
+// Id of the calling thread's current context (CUDA 12's cuCtxGetId, reached
+// through the runtime's driver entry points so that the library needs no
+// libcuda at link time); false when there is no current context yet or the
+// driver does not offer the calls.
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+bool current_context_id(unsigned long long* id) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PfnCtxGetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PfnCtxGetId>(f);
+  });
+  CUcontext c = nullptr;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c) return false;
+  return get_id(c, id) == CUDA_SUCCESS;
+}
+
+// Address of the scratch array in the current context.  The look-up loads this
+// module's device globals into the context, so the first call in a context is
+// the set-up call; make it before any work that must not see one.  The address
+// is cached per device ordinal together with the id of the context it belongs
+// to: a context created later on that device (after cudaDeviceReset, or a
+// non-primary context) has another id and is looked up again.
+struct JnaCache {
+  unsigned long long ctx = 0;
+  int64_t* ptr = nullptr;
+};
+std::mutex g_jna_mutex;
+JnaCache g_jna_cache[64];
+
 xk_status jna_scratch(int64_t** out) {
   int dev = 0;
   XK_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return xk_set_error(XK_ERR_ARG, "device ordinal out of range");
-  int64_t* p = g_jna_ptr[dev].load(std::memory_order_acquire);
-  if (!p) {
-    XK_CUDA(cudaGetSymbolAddress((void**)&p, g_jna_scratch));
-    g_jna_ptr[dev].store(p, std::memory_order_release);
+  unsigned long long cid = 0;
+  bool have = current_context_id(&cid);
+  if (have) {
+    std::lock_guard<std::mutex> lock(g_jna_mutex);
+    if (g_jna_cache[dev].ptr && g_jna_cache[dev].ctx == cid) {
+      *out = g_jna_cache[dev].ptr;
+      return XK_OK;
+    }
+  }
+  int64_t* p = nullptr;
+  XK_CUDA(cudaGetSymbolAddress((void**)&p, g_jna_scratch));
+  if (!have) have = current_context_id(&cid);  // the look-up made the primary context current
+  if (have) {
+    std::lock_guard<std::mutex> lock(g_jna_mutex);
+    g_jna_cache[dev].ctx = cid;
+    g_jna_cache[dev].ptr = p;
   }
   *out = p;
   return XK_OK;

@@ -749,13 +749,7 @@ extern "C" xk_status xk_mlp_forward_tcgen05(const uint16_t* params_bf16, const f
   // persistent grid of TC_PER_SM CTAs per SM: each CTA runs its tiles' three layers back to back
   // (MMA, completion wait, read-back), so several CTAs per SM overlap one's MMA with another's
   // read-back; five measured best on 400k-8M samples (4 to 8 within 15%)
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
+  const int sms = xk_sm_count();
   const long long resident = (long long)TC_PER_SM * sms;
   const long long tiles = (n + 127) / 128;
   const int blocks = (int)(tiles < resident ? tiles : resident);

@@ -332,12 +332,16 @@ void residual_sq(long long n, const double* r, double* part, double* sc, cudaStr
   k_scalars<4><<<1, SV_T, 0, st>>>(part, sc);
 }
 
-struct SolveStream {  // a private stream ordered after the caller's, and the graph of one check interval
+// A private stream ordered after the caller's, and the graph of one check interval.  On every
+// exit, an error return included, the stream is drained before it is destroyed, so that no
+// kernel queued on it can still write x or the work vectors after xk_bicgstab has returned.
+struct SolveStream {
   cudaStream_t cs = nullptr;
   cudaEvent_t ev = nullptr;
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   ~SolveStream() {
+    if (cs) cudaStreamSynchronize(cs);
     if (ge) cudaGraphExecDestroy(ge);
     if (g) cudaGraphDestroy(g);
     if (ev) cudaEventDestroy(ev);

@@ -1,4 +1,5 @@
 // Error state, device-wide scans, radix sort and FP64 reductions.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 
@@ -16,6 +17,22 @@ xk_status xk_set_cuda_error(cudaError_t e, const char* file, int line) {
 xk_status xk_set_error(xk_status code, const char* msg) {
   snprintf(g_err, sizeof(g_err), "%s", msg);
   return code;
+}
+
+int xk_sm_count() {
+  constexpr int MAX_DEV = 64;
+  static std::atomic<int> cache[MAX_DEV];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+  if (dev >= MAX_DEV) {
+    int n = 0;
+    return (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0) ? n : 1;
+  }
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+  cache[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 // --------------------------------------------------------------------------- scan

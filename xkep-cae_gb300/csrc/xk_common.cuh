@@ -108,6 +108,9 @@ static inline int xk_blocks(long long n, int threads) {
 xk_status xk_set_cuda_error(cudaError_t e, const char* file, int line);
 xk_status xk_set_error(xk_status code, const char* msg);
 
+// SM count of the current device, read once per device ordinal (1 when it cannot be read).
+int xk_sm_count();
+
 // Device-wide exclusive scans (scan.cu).  Scratch is allocated stream-ordered.
 xk_status xk_exclusive_scan_i32(const int32_t* in, int32_t* out, long long n, int64_t* total_dev,
                                 cudaStream_t s);

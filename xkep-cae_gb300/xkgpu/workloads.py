@@ -65,7 +65,9 @@ def strand_workload(name: str, n_wires: int, d: float, pitch: float, n_pitches: 
     k_pen = 1e3 * sec["E"] * sec["A"] / mean_element_length(st.coords, st.conn)
     return Workload(name, st, sec, u, k_pen, mu=mu, meta={"n_wires": n_wires, "d": d, "pitch": pitch,
                                                           "n_pitches": n_pitches, "n_el_per_pitch": n_el_per_pitch,
-                                                          "gap_frac": gap_frac, "seed": seed})
+                                                          "gap_frac": gap_frac, "seed": seed,
+                                                          "compress_layer": compress_layer,
+                                                          "compress_frac": compress_frac})
 
 
 def wires_for_layers(n_layers: int) -> int:
@@ -76,6 +78,10 @@ def wires_for_layers(n_layers: int) -> int:
 CONFIGS = {
     "strand7": dict(n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el_per_pitch=16),
     "strand37": dict(n_wires=37, d=2.0, pitch=40.0, n_pitches=4, n_el_per_pitch=32),
+    # the 37-wire load-step strand: nominal lay (a gap of -1e-12 d skips the minimum-gap bump) with the
+    # outer layer moved radially inward by 0.005 d
+    "strand37c": dict(n_wires=37, d=2.0, pitch=40.0, n_pitches=4, n_el_per_pitch=32, gap_frac=-1e-12,
+                      compress_layer=3, compress_frac=0.005),
     "strand91": dict(n_wires=91, d=2.0, pitch=40.0, n_pitches=4, n_el_per_pitch=32),
     "strand397": dict(n_wires=wires_for_layers(11), d=0.5, pitch=20.0, n_pitches=4, n_el_per_pitch=24),
     "strand1027": dict(n_wires=wires_for_layers(18), d=0.5, pitch=20.0, n_pitches=4, n_el_per_pitch=24),
