@@ -539,6 +539,16 @@ xk_status xk_system_block_jacobi(const xk_system* A, double* dinv, xk_stream s);
 xk_status xk_bicgstab(const xk_system* A, const double* b, double* x, const double* dinv, double* work,
                       int32_t max_iter, int32_t check_every, double rtol, int32_t* iters, double* rel_res,
                       xk_stream s);
+/* A (plus mass_coef * mass on the diagonal when mass is not null) as a dense
+ * block-tridiagonal matrix for a direct factorisation: node v's DOF rows sit in
+ * block row pos[v] / bn at local rows 6 (pos[v] % bn) + d; D, Lo, Up are nb
+ * blocks of (6 bn)^2 doubles each (row-major), the diagonal blocks and the
+ * blocks left and right of them.  Zeroes the three arrays first.  Couplings
+ * more than one block row apart set *overflow (device int32) and are dropped:
+ * choose bn at least the largest |pos[v] - pos[w]| of a stored block.  Padding
+ * positions (n_nodes <= p < nb bn) are left zero for the caller. */
+xk_status xk_system_blocktri(const xk_system* A, const int32_t* pos, int32_t bn, int32_t nb, const double* mass,
+                             double mass_coef, double* D, double* Lo, double* Up, int32_t* overflow, xk_stream s);
 
 /* ------------------------------------------------------------------------
  * Learned pruning of broadphase candidates.  No counterpart in the reference:

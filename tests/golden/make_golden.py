@@ -381,6 +381,93 @@ def gauss_case(R, name, seed=11, n=1200):
     print(name, n, np.bincount(ng))
 
 
+def solve_case(R, name, *, n_wires=7, d=2.0, pitch=40.0, n_el=16, kappa=0.0, twist=0.0, t_total=1e-3, mu=0.1,
+               kpen_scale=1e3, smoothing_delta=0.0, dt_max_fraction=0.1, rho=7.85e-9, rho_inf=0.9):
+    """One run of the reference's own ``ContactFrictionProcess`` (``contact/solver/process.py:139-674``)
+    on a strand clamped at z = 0 whose z = L ends are driven to a prescribed end state: the section
+    of a circular arc of curvature ``kappa`` (bending about x) or a rigid twist by ``twist`` about
+    the strand axis, ramped over ``t_total`` with lumped mass and Generalized-alpha.  Records the
+    inputs, every Newton call's residual history (retries included) and the displacements of every
+    converged increment."""
+    import importlib
+
+    data = importlib.import_module("xkep_cae.core.data")
+    proc_mod = importlib.import_module("xkep_cae.contact.solver.process")
+    nd_mod = importlib.import_module("xkep_cae.contact.solver._newton_dynamic")
+    from xkep_cae.elements._beam_assembler import ULCRBeamAssembler
+
+    m = R["tw"]._make_twisted_wire_mesh(n_wires, d, pitch, 0.0, n_el, n_pitches=1, gap=0.0)
+    X, conn = m.node_coords, m.connectivity
+    sec = _section(R, d)
+    asm = ULCRBeamAssembler(X, conn, sec["E"], sec["G"], sec["A"], sec["Iy"], sec["Iz"], sec["J"], sec["kappa_y"],
+                            sec["kappa_z"])
+    M = asm.assemble_mass(rho, lumped=True)
+    ndof = 6 * len(X)
+    layer = np.zeros(len(conn), dtype=np.int64)
+    for k, (e0, e1) in enumerate(m.strand_elem_ranges):
+        layer[e0:e1] = m.strand_infos[k].layer
+    fixed, pd, pv = [], [], []
+    L = m.length
+    for n0, n1 in m.strand_node_ranges:
+        fixed += list(range(6 * n0, 6 * n0 + 6))
+        ne = n1 - 1
+        x, y = X[ne, 0], X[ne, 1]
+        if twist != 0.0:
+            c, s = math.cos(twist), math.sin(twist)
+            vals = [x * (c - 1.0) - y * s, x * s + y * (c - 1.0), 0.0, 0.0, 0.0, twist]
+        else:
+            phi = kappa * L
+            dyc, dzc = -(1.0 - math.cos(phi)) / kappa, math.sin(phi) / kappa - L
+            vals = [0.0, dyc + y * (math.cos(phi) - 1.0), dzc + y * math.sin(phi), phi, 0.0, 0.0]
+        pd += [6 * ne + k for k in range(6)]
+        pv += vals
+    k_pen = kpen_scale * sec["E"] * sec["A"] / float(np.mean(np.linalg.norm(X[conn[:, 1]] - X[conn[:, 0]], axis=1)))
+    cfg = R["cp"]._ContactConfigInput(k_t_ratio=0.5, mu=mu, g_on=0.0, g_off=1e-6, exclude_same_layer=True,
+                                      elem_layer_map={int(e): int(l) for e, l in enumerate(layer)},
+                                      adjust_initial_penetration=False, smoothing_delta=smoothing_delta,
+                                      beam_E=sec["E"], beam_I=sec["Iy"], beam_A=sec["A"],
+                                      dt_max_fraction=dt_max_fraction)
+    setup = data.ContactSetupData(manager=R["cp"]._ContactManagerInput(config=cfg), k_pen=k_pen, mu=mu)
+    inp = data.ContactFrictionInputData(
+        mesh=data.MeshData(node_coords=X, connectivity=conn, radii=np.full(len(conn), d / 2.0), n_strands=n_wires),
+        boundary=data.BoundaryData(fixed_dofs=np.array(fixed), prescribed_dofs=np.array(pd),
+                                   prescribed_values=np.array(pv), f_ext_total=np.zeros(ndof)),
+        contact=setup,
+        callbacks=data.AssembleCallbacks(assemble_tangent=asm.assemble_tangent,
+                                         assemble_internal_force=asm.assemble_internal_force, ul_assembler=None),
+        mass_matrix=M, dt_physical=t_total, rho_inf=rho_inf)
+    calls = []
+    cls = nd_mod.NewtonDynamicProcess
+    orig = cls.process
+
+    def recording(self, step_input):  # records every Newton call; changes nothing
+        out = orig(self, step_input)
+        calls.append((step_input.load_frac, out.converged, out.n_attempts, out.n_active,
+                      list(out.diagnostics.res_history)))
+        return out
+
+    cls.process = recording
+    try:
+        res = proc_mod.ContactFrictionProcess().process(inp)
+    finally:
+        cls.process = orig
+    out = {"X": X, "conn": conn, "radius": d / 2.0, "elem_layer": layer, "mass": M.diagonal(),
+           "fixed": np.array(fixed), "prescribed_dofs": np.array(pd), "prescribed_values": np.array(pv),
+           "k_pen": k_pen, "mu": mu, "k_t_ratio": 0.5, "smoothing_delta": smoothing_delta, "t_total": t_total,
+           "rho_inf": rho_inf, "dt_max_fraction": dt_max_fraction, "converged": res.converged,
+           "n_increments": res.n_increments, "n_cutbacks": res.n_cutbacks, "u_final": res.u,
+           "load_history": np.array(res.load_history), "u_history": np.array(res.displacement_history),
+           "inc_attempts": np.array([g.n_attempts for g in res.increment_diagnostics]),
+           "inc_active": np.array([g.n_active for g in res.increment_diagnostics]),
+           "call_frac": np.array([c[0] for c in calls]), "call_converged": np.array([c[1] for c in calls]),
+           "call_attempts": np.array([c[2] for c in calls]), "call_active": np.array([c[3] for c in calls]),
+           "call_res_ptr": np.cumsum([0] + [len(c[4]) for c in calls]),
+           "call_res": np.concatenate([c[4] for c in calls]) if calls else np.zeros(0)}
+    for k, v in sec.items():
+        out[k] = v
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+
+
 def protocols_case(R, name):
     """Method names and parameter names, in order, of the Strategy Protocols
     (``xkep_cae/core/strategies/protocols.py:17-256``), as JSON."""
@@ -400,6 +487,7 @@ def protocols_case(R, name):
 
 CASES = {
     "protocols": lambda R: protocols_case(R, "protocols"),
+    "solve7_bend": lambda R: solve_case(R, "solve7_bend", kappa=1.0 / (50.0 * 6.0)),
     "strand7":lambda R: strand_case(R, "strand7", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16,
                                      gap_frac=-0.005, seed=0, mu=0.1),
     "strand7_nogap": lambda R: strand_case(R, "strand7_nogap", n_wires=7, d=2.0, pitch=40.0, n_pitches=1, n_el=16,

@@ -426,3 +426,115 @@ extern "C" xk_status xk_bicgstab(const xk_system* A, const double* b, double* x,
   if (rel_res) *rel_res = res;
   return XK_OK;
 }
+
+// ---------------------------------------------------------------------------
+// The system as dense blocks of a block-tridiagonal matrix, for a direct solve
+// on the device.  Nodes are renumbered by pos[] (an ordering along the strand
+// axis) and grouped bn to a block; a row of DOFs of node v, DOF d sits in
+// block row I = pos[v] / bn at local row 6 (pos[v] % bn) + d.  One thread per
+// DOF row writes every entry of its row (K_beam's blocks, then K_c's added on
+// the translational part, the mass term on the diagonal), so no entry has two
+// writers.  Dirichlet rows and columns become the identity.  A coupling more
+// than one block row away cannot be stored: it sets *overflow.
+namespace {
+
+template <typename T>
+__global__ void k_blocktri(xk_system A, const int32_t* __restrict__ pos, int bn, int nb,
+                           const double* __restrict__ mass, double mass_coef, double* __restrict__ D,
+                           double* __restrict__ Lo, double* __restrict__ Up, int32_t* __restrict__ overflow) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= 6LL * A.n_nodes) return;
+  const int v = (int)(g / 6), d = (int)(g % 6);
+  const long long b = 6LL * bn;
+  const int pv = pos[v];
+  const int I = pv / bn;
+  const long long r = 6LL * (pv % bn) + d;
+  const long long row_off = (long long)I * b * b + r * b;
+  auto at = [&](int w, int j) -> double* {
+    const int pw = pos[w];
+    const int J = pw / bn;
+    const long long c = 6LL * (pw % bn) + j;
+    if (J == I) return D + row_off + c;
+    if (J == I - 1) return Lo + row_off + c;
+    if (J == I + 1) return Up + row_off + c;
+    return nullptr;
+  };
+  if (A.fixed && A.fixed[g]) {  // Dirichlet row: identity (the rest of the row stays zero)
+    D[row_off + 6LL * (pv % bn) + d] = 1.0;
+    return;
+  }
+  bool lost = false;
+  const T* kb = (const T*)A.kb_vals;
+  for (int q = A.kb_low_ptr[v]; q < A.kb_low_ptr[v + 1]; ++q) {  // stored (u, v), u < v, transposed
+    const int bk = A.kb_low_blk[q];
+    const int u = A.kb_blk_row[bk];
+    const T* blk = kb + 36LL * bk + d;
+    for (int j = 0; j < 6; ++j) {
+      if (A.fixed && A.fixed[6LL * u + j]) continue;
+      double* p = at(u, j);
+      if (p) *p += (double)blk[6 * j];
+      else lost = true;
+    }
+  }
+  for (int bk = A.kb_row_ptr[v]; bk < A.kb_row_ptr[v + 1]; ++bk) {
+    const int w = A.kb_col[bk];
+    const T* blk = kb + 36LL * bk + 6 * d;
+    for (int j = 0; j < 6; ++j) {
+      if (A.fixed && A.fixed[6LL * w + j]) continue;
+      double* p = at(w, j);
+      if (p) *p += (double)blk[j];
+      else lost = true;
+    }
+  }
+  if (d < 3 && A.kc_vals) {
+    const T* kc = (const T*)A.kc_vals;
+    for (int q = A.kc_low_ptr[v]; q < A.kc_low_ptr[v + 1]; ++q) {  // stored (u, v), u < v, also (v, u)
+      const int bk = A.kc_low_blk[q];
+      const int u = A.kc_blk_row[bk];
+      const T* blk = kc + 9LL * bk + 3 * d;
+      for (int j = 0; j < 3; ++j) {
+        if (A.fixed && A.fixed[6LL * u + j]) continue;
+        double* p = at(u, j);
+        if (p) *p += (double)blk[j];
+        else lost = true;
+      }
+    }
+    for (int bk = A.kc_row_ptr[v]; bk < A.kc_row_ptr[v + 1]; ++bk) {
+      const int w = A.kc_col[bk];
+      const T* blk = kc + 9LL * bk + 3 * d;
+      for (int j = 0; j < 3; ++j) {
+        if (A.fixed && A.fixed[6LL * w + j]) continue;
+        double* p = at(w, j);
+        if (p) *p += (double)blk[j];
+        else lost = true;
+      }
+    }
+  }
+  if (mass) D[row_off + 6LL * (pv % bn) + d] += mass_coef * mass[g];
+  if (lost) atomicExch(overflow, 1);
+}
+
+}  // namespace
+
+extern "C" xk_status xk_system_blocktri(const xk_system* A, const int32_t* pos, int32_t bn, int32_t nb,
+                                        const double* mass, double mass_coef, double* D, double* Lo, double* Up,
+                                        int32_t* overflow, xk_stream s) {
+  if (!A || !pos || bn < 1 || nb < 1 || !D || !Lo || !Up || !overflow || !A->kb_row_ptr || !A->kb_col ||
+      !A->kb_vals || !kc_complete(A) || (long long)bn * nb < A->n_nodes)
+    return xk_set_error(XK_ERR_ARG, "xk_system_blocktri: bad arguments");
+  cudaStream_t st = (cudaStream_t)s;
+  const long long b = 6LL * bn;
+  const size_t bytes = (size_t)nb * b * b * sizeof(double);
+  XK_CUDA(cudaMemsetAsync(D, 0, bytes, st));
+  XK_CUDA(cudaMemsetAsync(Lo, 0, bytes, st));
+  XK_CUDA(cudaMemsetAsync(Up, 0, bytes, st));
+  XK_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int32_t), st));
+  if (A->n_nodes == 0) return XK_OK;
+  const int nbk = xk_blocks(6LL * A->n_nodes, SV_T);
+  if (A->precision == XK_FP64)
+    k_blocktri<double><<<nbk, SV_T, 0, st>>>(*A, pos, bn, nb, mass, mass_coef, D, Lo, Up, overflow);
+  else
+    k_blocktri<float><<<nbk, SV_T, 0, st>>>(*A, pos, bn, nb, mass, mass_coef, D, Lo, Up, overflow);
+  XK_CHECK_LAUNCH();
+  return XK_OK;
+}

@@ -149,6 +149,7 @@ SIGNATURES = {
     "xk_system_spmv": [P(System), vp, vp, vp],
     "xk_system_block_jacobi": [P(System), vp, vp],
     "xk_bicgstab": [P(System), vp, vp, vp, vp, C.c_int32, C.c_int32, C.c_double, P(C.c_int32), P(C.c_double), vp],
+    "xk_system_blocktri": [P(System), vp, C.c_int32, C.c_int32, vp, C.c_double, vp, vp, vp, vp, vp],
 }
 SOLVE_REDUCE_BLOCKS = 304
 MLP_IN, MLP_HIDDEN, MLP_PARAMS, MLP_ACT = 8, 64, 8961, 192
