@@ -204,6 +204,17 @@ xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const int32_t* c
 xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double* u, const xk_contact_params* cp,
                          int update_active, xk_stream s);
 
+/* The detection narrowphase of the mixed engine: UpdateGeometryProcess with
+ * the active-set update (_manager_process.py:327-403, 475-494), every pair
+ * first in float from node32 (xk_nodes_prepare at this u), and in exact
+ * reference arithmetic (as xk_narrowphase) every pair whose float gap lies
+ * within a bound of its error from [g_on, g_off], or that is near-parallel,
+ * or on coated wires.  The status of every pair is the exact one; the stored
+ * s, t, gap and frame of the others carry float rounding.  *n_exact (device,
+ * nullable): how many pairs took the exact routine. */
+xk_status xk_narrowphase_screened(const xk_mesh* m, xk_pairs* p, const double* u, const float* node32,
+                                  const xk_contact_params* cp, int32_t* n_exact, xk_stream s);
+
 #define XK_STAGE_NARROW 1   /* frozen-active-set narrowphase (_newton_steps.py:91-94) */
 #define XK_STAGE_NORMAL 2   /* HuberContactForceProcess.evaluate (contact_force/strategy.py:126-170) */
 #define XK_STAGE_FRICTION 4 /* CoulombReturnMappingProcess.evaluate (friction/strategy.py:111-148) */

@@ -167,3 +167,56 @@ def test_batch256_sample_vs_oracle(precision):
         assert rel_err(R[6 * n0:6 * n1], fb + fc) < tol, k
         assert sparse_rel_err(Kc[6 * n0:6 * n1, 6 * n0:6 * n1], Kck) < tol, k
         assert sparse_rel_err(Kb[6 * n0:6 * n1, 6 * n0:6 * n1], Kbk) < tol, k
+
+
+@pytest.mark.parametrize("end_rotation", [None, 0.5])
+def test_mixed_at_large_rotation_bent_strand(end_rotation):
+    """The mixed engine against the FP64 engine and the oracle on the 91-wire strand bent into an arc:
+    curvature 1/(50 D) (end sections turned by 0.15 rad), or an arc whose ends turn by 0.5 rad; every
+    element rotates rigidly by up to that angle with little deformation, plus the seeded noise.
+    R, K_beam and K_c within 1e-5 (max-norm relative), active and stick sets equal."""
+    from xkgpu import runs
+
+    w = W.config_workload("strand91", seed=4)
+    st = w.strand
+    D = 2.0 * max(wi.lay_radius for wi in st.wires) + w.meta["d"]
+    kappa = 1.0 / (50.0 * D) if end_rotation is None else end_rotation / st.length
+    u0 = w.u + runs.arc_displacement(st, kappa)
+    assert np.max(np.abs(u0.reshape(-1, 6)[:, 3])) > 0.9 * kappa * st.length
+    iters = _states(st, u0, w.meta["d"], n_iter=1)
+    ref = _oracle(st, w.section, u0, iters, k_pen=w.k_pen, k_t_ratio=w.k_t_ratio, mu=w.mu)
+    out = {}
+    for precision in ("fp64", "mixed"):
+        eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=precision, **w.engine_kwargs())
+        _check(eng, ref, u0, iters, TOL64 if precision == "fp64" else TOLMIX)
+        out[precision] = (eng.R.cpu().numpy(), eng.K_beam_csr(), eng.K_contact_csr())
+    for a, b in zip(out["mixed"], out["fp64"]):
+        err = rel_err(a, b) if isinstance(a, np.ndarray) else sparse_rel_err(a, b)
+        assert err < TOLMIX
+
+
+@pytest.mark.parametrize("name", ["strand91", "strand1027"])
+def test_screened_detection_equals_exact(name):
+    """The mixed engine's detection decides the active set in float wherever the float gap is provably on
+    the same side of the thresholds (``xk_narrowphase_screened``): the status of every pair equals the
+    exact routine's, the float gaps of the other pairs are within 2e-5 of the segment scale of the exact
+    ones, and only a small share of the pairs needs the exact routine."""
+    w = W.config_workload(name, seed=6)
+    st = w.strand
+    u = _dev(w.u)
+    out = {}
+    for screened in (False, True):
+        eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **w.engine_kwargs())
+        eng.screened_detection = screened
+        stats = eng.detect(u)
+        out[screened] = (eng.pair_state(), stats)
+        del eng
+    ex, sc = out[False][0], out[True][0]
+    assert np.array_equal(ex["ea"], sc["ea"]) and np.array_equal(ex["eb"], sc["eb"])
+    assert np.array_equal(ex["status"], sc["status"])
+    n_exact = out[True][1]["narrowphase_exact"]
+    assert n_exact < 0.05 * len(ex["ea"])
+    assert np.max(np.abs(ex["gap"] - sc["gap"])) < 2e-5 * 2.0 * w.meta["d"]
+    near = np.abs(ex["gap"]) < 1e-4
+    print(f"{name}: {len(ex['ea'])} pairs, {n_exact} exact, {int(near.sum())} within 1e-4 of contact, "
+          f"max |gap float - gap exact| = {np.max(np.abs(ex['gap'] - sc['gap'])):.3e}")

@@ -6,7 +6,8 @@ on a bent 7-wire strand (see ``tests/test_solver_loop.py``).  The same loop
 Generalized-alpha integrator reproduces it: the same increments and attempt
 counts, residual histories to 1e-5, every converged increment's
 displacements to 1e-8 of their scale.  The mixed engine converges through the
-same increments to displacements within 1e-6 of the FP64 run's.
+same increments to displacements within 1e-6 of the FP64 run's when both end their increments on the
+force test.
 """
 
 from __future__ import annotations
@@ -28,14 +29,14 @@ from xkgpu.dynamics import GpuGeneralizedAlpha  # noqa: E402
 from xkgpu.engine import AssemblyEngine  # noqa: E402
 
 
-def _run(z, precision):
+def _run(z, precision, settings=None):
     eng = AssemblyEngine(z["X"], z["conn"], float(z["radius"]), _section(z), layer=z["elem_layer"],
                          precision=precision, k_pen=float(z["k_pen"]), k_t_ratio=float(z["k_t_ratio"]),
                          mu=float(z["mu"]), smoothing_delta=float(z["smoothing_delta"]))
     sol = S.ContactFrictionSolver(S.EngineBackend(eng), GpuGeneralizedAlpha(z["mass"], rho_inf=float(z["rho_inf"])),
                                   t_total=float(z["t_total"]), fixed_dofs=z["fixed"],
                                   prescribed_dofs=z["prescribed_dofs"], prescribed_values=z["prescribed_values"],
-                                  settings=_settings(z))
+                                  settings=settings or _settings(z))
     return sol.run()
 
 
@@ -46,9 +47,15 @@ def test_engine_solver_reproduces_reference_run():
 
 
 def test_mixed_engine_solver_converges_to_fp64_run():
+    """The reference's energy test stops an increment at a residual of about 1e-5 of its first value,
+    so two runs that take different iterates agree only to that level.  Here both runs end their
+    increments on the force test alone (the energy test off): FP64 at 1e-10 of the first residual,
+    mixed at 1e-6 (its float residual floor lies below that), over the same fixed increments."""
     z = golden("solve7_bend")
-    r64 = _run(z, "fp64")
-    rmx = _run(z, "mixed")
+    cfg = dict(dt_max_fraction=float(z["dt_max_fraction"]), energy_tol=0.0, tol_disp=1e-12, dt_grow_factor=1.0,
+               dt_shrink_attempt_threshold=1000, dt_contact_change_threshold=1e9)
+    r64 = _run(z, "fp64", S.SolverSettings(tol_force=1e-10, **cfg))
+    rmx = _run(z, "mixed", S.SolverSettings(tol_force=1e-6, **cfg))
     assert rmx.converged and r64.converged
     assert [r.load_frac for r in rmx.increments] == [r.load_frac for r in r64.increments]
     for a, b in zip(rmx.increments, r64.increments):

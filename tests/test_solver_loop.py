@@ -124,3 +124,33 @@ def test_block_tridiagonal_solve_matches_dense():
     got = blocktri_solve(torch.as_tensor(D.copy()), torch.as_tensor(Lo), torch.as_tensor(Up.copy()),
                          torch.as_tensor(rhs.reshape(nb, b, 1))).numpy().reshape(-1)
     assert np.allclose(got, want, rtol=1e-10, atol=1e-12)
+
+
+def test_gmres_with_float32_block_preconditioner():
+    """GMRES in FP64 preconditioned by the float32 block LU on an indefinite, badly scaled
+    block-tridiagonal system (rows scaled over eight decades, condition number ~6e8): it reaches the
+    attainable FP64 residual within two restart cycles and the solution of the dense solve."""
+    from xkgpu.blocktri import blocktri_apply, blocktri_factor, gmres
+
+    rng = np.random.default_rng(8)
+    nb, b = 6, 10
+    D = rng.normal(size=(nb, b, b)) + 4.0 * np.eye(b) * rng.choice([-1.0, 1.0], size=(nb, 1, b))
+    Lo, Up = rng.normal(size=(nb, b, b)) * 0.5, rng.normal(size=(nb, b, b)) * 0.5
+    scale = 10.0 ** rng.uniform(-4, 4, size=(nb, b, 1))
+    D, Lo, Up = D * scale, Lo * scale, Up * scale
+    A = np.zeros((nb * b, nb * b))
+    for i in range(nb):
+        A[i * b:(i + 1) * b, i * b:(i + 1) * b] = D[i]
+        if i > 0:
+            A[i * b:(i + 1) * b, (i - 1) * b:i * b] = Lo[i]
+        if i < nb - 1:
+            A[i * b:(i + 1) * b, (i + 1) * b:(i + 2) * b] = Up[i]
+    F = tuple(torch.as_tensor(x, dtype=torch.float32) for x in (D, Lo, Up))
+    piv = blocktri_factor(*F)
+    At = torch.as_tensor(A)
+    rhs = torch.as_tensor(rng.normal(size=nb * b))
+    x, it, rel = gmres(lambda v: At @ v, rhs,
+                       lambda v: blocktri_apply(*F, piv, v.view(nb, b, 1)).reshape(-1).double(), rtol=1e-12)
+    assert rel <= 1e-8 and it <= 60
+    want = np.linalg.solve(A, rhs.numpy())
+    assert np.max(np.abs(x.numpy() - want)) <= 1e-7 * np.max(np.abs(want))

@@ -162,114 +162,9 @@ XK_D bool overlap(const double* box, long long ne, int i, int j) {
   return true;
 }
 
-// MODE 0: count per segment; MODE 1: emit (i, j) sorted by j within each segment.
-template <int MODE>
-__global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restrict__ box,
-                                                const float4* __restrict__ boxf, const Grid* __restrict__ gp,
-                                                const int32_t* __restrict__ segs, const int32_t* __restrict__ cstart,
-                                                const int32_t* __restrict__ cend, int excl_shared, int excl_layer,
-                                                int32_t* __restrict__ cnt, unsigned long long* __restrict__ raw_total,
-                                                const int32_t* __restrict__ off, int32_t* __restrict__ tmp,
-                                                int32_t* __restrict__ out) {
-  const long long ne = m.n_elems;
-  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (w >= ne) return;
-  const Grid g = *gp;
-  const int i = segs[w];
-  int c[3];
-  cell_of(g, box[i], box[ne + i], box[2 * ne + i], c);
-  const int ia = m.conn[2 * i], ib = m.conn[2 * i + 1];
-  const int li = (excl_layer && m.layer) ? m.layer[i] : -1;
-  const float4 il = boxf[2LL * i], ih = boxf[2LL * i + 1];
-  int n_raw = 0, n_keep = 0;
-  const long long base = MODE == 1 ? (long long)off[i] : 0;
-  for (int dz = -1; dz <= 1; ++dz) {
-    const int z = c[2] + dz;
-    if (z < 0 || z >= g.dims[2]) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int y = c[1] + dy;
-      if (y < 0 || y >= g.dims[1]) continue;
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int x = c[0] + dx;
-        if (x < 0 || x >= g.dims[0]) continue;
-        const long long lin = ((long long)z * g.dims[1] + y) * g.dims[0] + x;
-        const int k0 = cstart[lin], k1 = cend[lin];
-        for (int kk = k0; kk < k1; kk += 32) {
-          const int k = kk + lane;
-          bool hit = false, keep = false;
-          int j = -1;
-          if (k < k1) {
-            j = segs[k];
-            bool near = j > i;
-            if (near) {  // conservative float screen (outward-rounded boxes), then the exact FP64 test
-              const float4 jl = __ldg(boxf + 2LL * j), jh = __ldg(boxf + 2LL * j + 1);
-              near = il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z;
-            }
-            if (near && overlap(box, ne, i, j)) {
-              hit = true;
-              keep = true;
-              if (excl_shared) {
-                const int ja = m.conn[2 * j], jb = m.conn[2 * j + 1];
-                if (ia == ja || ia == jb || ib == ja || ib == jb) keep = false;
-              }
-              if (keep && li >= 0 && m.layer[j] == li) keep = false;
-            }
-          }
-          const unsigned bal = __ballot_sync(0xffffffffu, keep);
-          n_raw += __popc(__ballot_sync(0xffffffffu, hit));
-          if (MODE == 1 && keep) tmp[base + n_keep + __popc(bal & ((1u << lane) - 1u))] = j;
-          n_keep += __popc(bal);
-        }
-      }
-    }
-  }
-  if (MODE == 0) {
-    if (lane == 0) {
-      cnt[i] = n_keep;
-      atomicAdd(raw_total, (unsigned long long)n_raw);
-    }
-  } else {
-    __syncwarp();
-    // rank sort of this segment's list: j values are distinct
-    for (int l = lane; l < n_keep; l += 32) {
-      const int v = tmp[base + l];
-      int r = 0;
-      for (int q = 0; q < n_keep; ++q) r += tmp[base + q] < v;
-      out[2 * (base + r)] = i;
-      out[2 * (base + r) + 1] = v;
-    }
-  }
-}
-
-constexpr int RED_BLOCKS = 304, RED_T = 256;
-
-__global__ void k_radsum_partial(xk_mesh m, const int32_t* __restrict__ pairs, long long n, double* __restrict__ part) {
-  __shared__ double sm[RED_T];
-  double acc = 0.0;
-  for (long long k = (long long)blockIdx.x * RED_T + threadIdx.x; k < n; k += (long long)RED_BLOCKS * RED_T)
-    acc += xadd(m.radii[pairs[2 * k]], m.radii[pairs[2 * k + 1]]);
-  sm[threadIdx.x] = acc;
-  __syncthreads();
-  for (int w = RED_T / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
-}
-
-__global__ void k_margin(const double* __restrict__ part, long long n, double fixed, double* __restrict__ out) {
-  if (fixed > 0.0) { *out = fixed; return; }
-  double s = 0.0;
-  for (int b = 0; b < RED_BLOCKS; ++b) s += part[b];
-  *out = xmul(xdiv(s, (double)n), 0.5);
-}
-
-__global__ void k_midpoint(xk_mesh m, const double* __restrict__ u, const int32_t* __restrict__ pairs, long long n,
-                           const double* __restrict__ extra, int32_t* __restrict__ keep) {
-  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const int i = pairs[2 * k], j = pairs[2 * k + 1];
+// Midpoint prescreen of DetectCandidatesProcess (_manager_process.py:260-286) for one pair: keep
+// when max(0, |m_a - m_b| - L_a/2 - L_b/2) <= r_a + r_b + extra, in the reference's operation order.
+XK_D bool midpoint_keep(const xk_mesh& m, const double* __restrict__ u, int i, int j, double extra) {
   const int nd[4] = {m.conn[2 * i], m.conn[2 * i + 1], m.conn[2 * j], m.conn[2 * j + 1]};
   double x[4][3];
   for (int q = 0; q < 4; ++q)
@@ -287,8 +182,148 @@ __global__ void k_midpoint(xk_mesh m, const double* __restrict__ u, const int32_
   const double md = xsqrt(xdot_seq(dm, dm));
   double mp = xsub(xsub(md, ha), hb);
   mp = (mp > 0.0 || mp != mp) ? mp : 0.0;
-  const double cut = xadd(xadd(m.radii[i], m.radii[j]), *extra);
-  keep[k] = (mp <= cut) ? 1 : 0;
+  return mp <= xadd(xadd(m.radii[i], m.radii[j]), extra);
+}
+
+// A warp per segment i (taken in Morton order of its cell): the 27 neighbouring cells' entries are
+// laid out as one list (lane l < 27 reads cell l's range, a warp scan gives the offsets) and the
+// warp walks it 32 entries at a time, each lane finding its entry's cell by a binary search over the
+// offsets held in the lanes.  A candidate j > i is screened on the outward-rounded float boxes
+// (which can never reject an FP64 overlap), tested on the FP64 boxes, then the shared-node and
+// same-layer filters apply; hits are compacted with ballot/popc.
+// MODE 0: kept count per segment (cnt[i]), the sum of r_i + r_j over its kept candidates in a fixed
+//         lane order (rsum[i], for the prescreen margin), and the raw overlap count.
+// MODE 1: the kept candidates of segment i sorted by j at off[i] (out), and their prescreen flags.
+template <int MODE>
+__global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restrict__ u,
+                                                const double* __restrict__ box, const float4* __restrict__ boxf,
+                                                const Grid* __restrict__ gp, const int32_t* __restrict__ segs,
+                                                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
+                                                int excl_shared, int excl_layer, int32_t* __restrict__ cnt,
+                                                double* __restrict__ rsum, unsigned long long* __restrict__ raw_total,
+                                                const int32_t* __restrict__ off, const double* __restrict__ extra,
+                                                int32_t* __restrict__ tmp, int32_t* __restrict__ out,
+                                                int32_t* __restrict__ keep) {
+  const long long ne = m.n_elems;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= ne) return;
+  const Grid g = *gp;
+  const int i = segs[w];
+  int c[3];
+  cell_of(g, box[i], box[ne + i], box[2 * ne + i], c);
+  // this lane's cell of the 27 and its entry range
+  int s0 = 0, n0 = 0;
+  if (lane < 27) {
+    const int x = c[0] + lane % 3 - 1, y = c[1] + (lane / 3) % 3 - 1, z = c[2] + lane / 9 - 1;
+    if (x >= 0 && x < g.dims[0] && y >= 0 && y < g.dims[1] && z >= 0 && z < g.dims[2]) {
+      const long long lin = ((long long)z * g.dims[1] + y) * g.dims[0] + x;
+      s0 = cstart[lin];
+      n0 = cend[lin] - s0;
+    }
+  }
+  int incl = n0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int pre = incl - n0;
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const int ia = m.conn[2 * i], ib = m.conn[2 * i + 1];
+  const int li = (excl_layer && m.layer) ? m.layer[i] : -1;
+  const float4 il = boxf[2LL * i], ih = boxf[2LL * i + 1];
+  const double ri = m.radii[i];
+  int n_raw = 0, n_keep = 0;
+  double rs = 0.0;
+  const long long base = MODE == 1 ? (long long)off[i] : 0;
+  for (int f0 = 0; f0 < total; f0 += 32) {
+    const int f = f0 + lane;
+    // the last cell q with pre_q <= f (cells of no entries share their successor's offset)
+    int q = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int cand = q + step;
+      const int pc = __shfl_sync(0xffffffffu, pre, cand < 27 ? cand : 26);
+      if (cand < 27 && pc <= f) q = cand;
+    }
+    const int sq = __shfl_sync(0xffffffffu, s0, q);
+    const int pq = __shfl_sync(0xffffffffu, pre, q);
+    bool hit = false, kept = false;
+    int j = -1;
+    if (f < total) {
+      j = segs[sq + (f - pq)];
+      bool near = j > i;
+      if (near) {
+        const float4 jl = __ldg(boxf + 2LL * j), jh = __ldg(boxf + 2LL * j + 1);
+        near = il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z;
+      }
+      if (near && overlap(box, ne, i, j)) {
+        hit = true;
+        kept = true;
+        if (excl_shared) {
+          const int ja = m.conn[2 * j], jb = m.conn[2 * j + 1];
+          if (ia == ja || ia == jb || ib == ja || ib == jb) kept = false;
+        }
+        if (kept && li >= 0 && m.layer[j] == li) kept = false;
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, kept);
+    n_raw += __popc(__ballot_sync(0xffffffffu, hit));
+    if (MODE == 0) {
+      double v = kept ? xadd(ri, m.radii[j]) : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);  // fixed butterfly order
+      rs += v;
+    } else if (kept) {
+      tmp[base + n_keep + __popc(bal & ((1u << lane) - 1u))] = j;
+    }
+    n_keep += __popc(bal);
+  }
+  if (MODE == 0) {
+    if (lane == 0) {
+      cnt[i] = n_keep;
+      rsum[i] = rs;
+      atomicAdd(raw_total, (unsigned long long)n_raw);
+    }
+  } else {
+    __syncwarp();
+    // rank sort of this segment's list (its j values are distinct), then the prescreen flag
+    for (int l = lane; l < n_keep; l += 32) {
+      const int v = tmp[base + l];
+      int r = 0;
+      for (int q2 = 0; q2 < n_keep; ++q2) r += tmp[base + q2] < v;
+      out[2 * (base + r)] = i;
+      out[2 * (base + r) + 1] = v;
+      if (keep) keep[base + r] = (!extra || midpoint_keep(m, u, i, v, *extra)) ? 1 : 0;
+    }
+  }
+}
+
+constexpr int RED_BLOCKS = 304, RED_T = 256;
+
+// prescreen margin: mean(r_a + r_b) / 2 over the candidates after the shared-node and same-layer
+// filters (_manager_process.py:275-279), from the per-segment sums, in a fixed order
+__global__ void k_radsum_partial(const double* __restrict__ rsum, long long ne, double* __restrict__ part) {
+  __shared__ double sm[RED_T];
+  double acc = 0.0;
+  for (long long k = (long long)blockIdx.x * RED_T + threadIdx.x; k < ne; k += (long long)RED_BLOCKS * RED_T)
+    acc += rsum[k];
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = RED_T / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+__global__ void k_margin(const double* __restrict__ part, const int64_t* __restrict__ n, double fixed,
+                         double* __restrict__ out) {
+  if (fixed > 0.0) { *out = fixed; return; }
+  double s = 0.0;
+  for (int b = 0; b < RED_BLOCKS; ++b) s += part[b];
+  *out = *n > 0 ? xmul(xdiv(s, (double)*n), 0.5) : 0.0;
 }
 
 __global__ void k_compact_pairs(const int32_t* __restrict__ in, const int32_t* __restrict__ keep,
@@ -487,16 +522,27 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   k_cells<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, keys, segs, cstart, cend);
   XK_CHECK_LAUNCH();
   unsigned long long* raw_dev = ext + 7;
+  double* rsum;
+  XK_TRY(S.get(&rsum, ne));
   XK_CUDA(cudaMemsetAsync(raw_dev, 0, sizeof(unsigned long long), st));
   XK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (ne + 1), st));
   const int sweep_blocks = xk_blocks(ne * 32, BP_T);
   const int excl_layer = (bp->exclude_same_layer && m->layer) ? 1 : 0;
-  k_sweep<0><<<sweep_blocks, BP_T, 0, st>>>(*m, box, boxf, grid, segs, cstart, cend, bp->exclude_shared, excl_layer, cnt,
-                                             raw_dev, nullptr, nullptr, nullptr);
+  k_sweep<0><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, cend, bp->exclude_shared,
+                                             excl_layer, cnt, rsum, raw_dev, nullptr, nullptr, nullptr, nullptr,
+                                             nullptr);
   XK_CHECK_LAUNCH();
   int64_t* tot;
   XK_TRY(S.get(&tot, 2));
   XK_TRY(xk_exclusive_scan_i32(cnt, off, ne + 1, tot, st));
+  double *part, *extra;
+  XK_TRY(S.get(&part, RED_BLOCKS));
+  XK_TRY(S.get(&extra, 1));
+  if (bp->midpoint_prescreening) {
+    if (!(bp->prescreening_margin > 0.0)) k_radsum_partial<<<RED_BLOCKS, RED_T, 0, st>>>(rsum, ne, part);
+    k_margin<<<1, 1, 0, st>>>(part, tot, bp->prescreening_margin, extra);
+    XK_CHECK_LAUNCH();
+  }
   int64_t h[2];
   unsigned long long hraw = 0;
   XK_CUDA(cudaMemcpyAsync(h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -507,29 +553,22 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   if (n_prefilter) *n_prefilter = n1;
   if (n1 == 0) return XK_OK;
   if (n1 > 0x7fffffffLL) return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: more than 2^31 candidates");
-  int32_t *tmp, *pairs1;
+  int32_t *tmp, *pairs1, *keep = nullptr, *pos = nullptr;
   XK_TRY(S.get(&tmp, n1));
-  XK_TRY(S.get(&pairs1, 2 * n1));
-  k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, box, boxf, grid, segs, cstart, cend, bp->exclude_shared, excl_layer, cnt,
-                                             raw_dev, off, tmp, pairs1);
-  XK_CHECK_LAUNCH();
   if (!bp->midpoint_prescreening) {
     *n_out = n1;
     if (n1 > cap) return xk_set_error(XK_ERR_CAPACITY, "xk_broadphase: output capacity too small");
-    XK_CUDA(cudaMemcpyAsync(out_pairs, pairs1, sizeof(int32_t) * 2 * n1, cudaMemcpyDeviceToDevice, st));
+    k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, cend, bp->exclude_shared,
+                                               excl_layer, cnt, rsum, raw_dev, off, nullptr, tmp, out_pairs, nullptr);
+    XK_CHECK_LAUNCH();
     XK_CUDA(cudaStreamSynchronize(st));
     return XK_OK;
   }
-  double *part, *extra;
-  int32_t *keep, *pos;
-  XK_TRY(S.get(&part, RED_BLOCKS));
-  XK_TRY(S.get(&extra, 1));
+  XK_TRY(S.get(&pairs1, 2 * n1));
   XK_TRY(S.get(&keep, n1));
   XK_TRY(S.get(&pos, n1));
-  if (!(bp->prescreening_margin > 0.0))
-    k_radsum_partial<<<RED_BLOCKS, RED_T, 0, st>>>(*m, pairs1, n1, part);
-  k_margin<<<1, 1, 0, st>>>(part, n1, bp->prescreening_margin, extra);
-  k_midpoint<<<xk_blocks(n1, 256), 256, 0, st>>>(*m, u, pairs1, n1, extra, keep);
+  k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, cend, bp->exclude_shared,
+                                             excl_layer, cnt, rsum, raw_dev, off, extra, tmp, pairs1, keep);
   XK_CHECK_LAUNCH();
   XK_TRY(xk_exclusive_scan_i32(keep, pos, n1, tot + 1, st));
   XK_CUDA(cudaMemcpyAsync(h + 1, tot + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st));

@@ -241,10 +241,8 @@ XK_D double coat_compression(const xk_mesh& m, int ea, int eb, double gap) {
   return fmax(0.0, xsub(coat_total_of(m, ea, eb), gap));
 }
 
-__global__ void k_narrow_exact(xk_mesh m, xk_pairs p, const double* __restrict__ u, double g_on, double g_off,
-                               int allow_deact, int update_active) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.n) return;
+XK_D void narrow_exact_one(const xk_mesh& m, xk_pairs& p, const double* __restrict__ u, double g_on, double g_off,
+                           int allow_deact, int update_active, int i) {
   const long long cap = p.cap;
   PairNodes nd = pair_nodes(m, p.ea[i], p.eb[i]);
   double x[4][3];
@@ -275,6 +273,12 @@ __global__ void k_narrow_exact(xk_mesh m, xk_pairs p, const double* __restrict__
       p.status[i] = ST_INACTIVE;
     }
   }
+}
+
+__global__ void k_narrow_exact(xk_mesh m, xk_pairs p, const double* __restrict__ u, double g_on, double g_off,
+                               int allow_deact, int update_active) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p.n) narrow_exact_one(m, p, u, g_on, g_off, allow_deact, update_active, i);
 }
 
 XK_HD double huber(double x, double d) {  // contact_force/strategy.py:104-113
@@ -885,6 +889,83 @@ XK_D void store3f(float* base, long long stride, long long i, const float* v) {
   base[2 * stride + i] = v[2];
 }
 
+// Detection narrowphase of the mixed engine.  Every pair's closest point, gap and frame are
+// taken in float from the split node positions (narrow32 without float-float), and the
+// active-set update (_manager_process.py:475-494) is decided on that gap wherever it cannot
+// differ from the exact one: the pair goes to the exact FP64 routine instead (appended to
+// `list`) when it is near-parallel, on coated wires, or when its float gap lies within eps of
+// [g_on, g_off].  eps bounds |gap_f - gap|: the inputs are the differences of the split positions
+// rounded once (relative 2^-24 of the scale, the largest |component| of the two segments and of
+// their offset), the 2x2 solve runs only with det > 1e-3 ac, so the parameter error is below
+// about 8e3 2^-24 and the distance at the computed parameters exceeds the segment distance by at
+// most the square of the resulting point error over twice the distance; the rounding of the
+// difference vector and its norm adds a few units of 2^-24 scale.  eps = 2e-5 scale + that square
+// term over (r_a + r_b) covers both with a wide margin.  The frames of the pairs decided in float
+// are transported in float (the per-iteration narrowphase of the mixed path does the same).
+__global__ void __launch_bounds__(PAIR_T) k_narrow_screen(xk_mesh m, xk_pairs p, const float* __restrict__ n32,
+                                                         double g_on, double g_off, int allow_deact,
+                                                         int32_t* __restrict__ list) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n) return;
+  const long long cap = p.cap;
+  const int ea = p.ea[i], eb = p.eb[i];
+  const PairNodes pn = pair_nodes(m, ea, eb);
+  const int nd[4] = {pn.n[0], pn.n[1], pn.n[2], pn.n[3]};
+  const double rs = xadd(m.radii[ea], m.radii[eb]);
+  const float rh = (float)rs;
+  const df R = {rh, (float)(rs - (double)rh)};
+  float scale = 0.0f;
+  {
+    float xh[4][3];
+    for (int k = 0; k < 4; ++k) {
+      float N[8];
+      ldg8(n32 + (long long)nd[k] * XK_NODE32_STRIDE, N);
+      for (int c = 0; c < 3; ++c) xh[k][c] = N[c];
+    }
+    for (int c = 0; c < 3; ++c)
+      scale = fmaxf(scale, fmaxf(fabsf(xh[1][c] - xh[0][c]), fmaxf(fabsf(xh[3][c] - xh[2][c]),
+                                                                   fabsf(xh[0][c] - xh[2][c]))));
+  }
+  float n[3], t1[3], t2[3], sf, tf, gf;
+  {
+    double v[3];
+    load3(p.normal, cap, i, v);
+    for (int c = 0; c < 3; ++c) n[c] = (float)v[c];
+    load3(p.t1, cap, i, v);
+    for (int c = 0; c < 3; ++c) t1[c] = (float)v[c];
+  }
+  const bool deferred = m.core_radii != nullptr || narrow32<false, true>(n32, nd, R, sf, tf, gf, n, t1, t2);
+  const float u24 = 5.9604645e-8f;  // 2^-24
+  const float pe = 8.0e3f * u24 * scale;
+  const double eps = 2e-5 * (double)scale + (double)(pe * pe) / (2.0 * rs);
+  const double g = (double)gf;
+  if (deferred || (g >= g_on - eps && g <= g_off + eps)) {
+    list[1 + atomicAdd(list, 1)] = i;
+    return;
+  }
+  p.s[i] = (double)sf;
+  p.t[i] = (double)tf;
+  p.gap[i] = g;
+  const double nn[3] = {n[0], n[1], n[2]}, tt1[3] = {t1[0], t1[1], t1[2]}, tt2[3] = {t2[0], t2[1], t2[2]};
+  store3(p.normal, cap, i, nn);
+  store3(p.t1, cap, i, tt1);
+  store3(p.t2, cap, i, tt2);
+  const uint8_t st = p.status[i];  // g is outside [g_on - eps, g_off + eps]: the exact gap is on the same side
+  if (st == ST_INACTIVE) {
+    if (g <= g_on) p.status[i] = ST_ACTIVE;
+  } else if (allow_deact && g >= g_off) {
+    p.status[i] = ST_INACTIVE;
+  }
+}
+
+// The exact detection narrowphase of the pairs the screen listed (list[0] of them), grid-stride.
+__global__ void k_narrow_exact_list(xk_mesh m, xk_pairs p, const double* __restrict__ u, double g_on, double g_off,
+                                    int allow_deact, const int32_t* __restrict__ list) {
+  const int n = list[0];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    narrow_exact_one(m, p, u, g_on, g_off, allow_deact, 1, list[1 + k]);
+}
+
 // A deferral list: [count, done, slots...].  The pair kernel appends to it; its deferred kernel
 // reads the count, works through the slots grid-stride, and its last CTA to finish (found with
 // the `done` counter after every CTA has read the count) sets both words back to zero for the
@@ -1140,6 +1221,31 @@ extern "C" xk_status xk_narrowphase(const xk_mesh* m, xk_pairs* p, const double*
                                                                           cp->allow_deactivation, update_active);
   XK_CHECK_LAUNCH();
   return XK_OK;
+}
+
+extern "C" xk_status xk_narrowphase_screened(const xk_mesh* m, xk_pairs* p, const double* u, const float* node32,
+                                             const xk_contact_params* cp, int32_t* n_exact, xk_stream s) {
+  if (!m || !p || !u || !node32 || !cp) return xk_set_error(XK_ERR_ARG, "xk_narrowphase_screened: null argument");
+  cudaStream_t st = (cudaStream_t)s;
+  if (p->n == 0) {
+    if (n_exact) XK_CUDA(cudaMemsetAsync(n_exact, 0, sizeof(int32_t), st));
+    return XK_OK;
+  }
+  int32_t* list = nullptr;
+  XK_CUDA(cudaMallocAsync((void**)&list, sizeof(int32_t) * ((size_t)p->n + 1), st));
+  xk_status r = XK_OK;
+  cudaError_t e = cudaMemsetAsync(list, 0, sizeof(int32_t), st);
+  if (e == cudaSuccess) {
+    k_narrow_screen<<<xk_blocks(p->n, PAIR_T), PAIR_T, 0, st>>>(*m, *p, node32, cp->g_on, cp->g_off,
+                                                               cp->allow_deactivation, list);
+    k_narrow_exact_list<<<2 * xk_sm_count(), PAIR_T, 0, st>>>(*m, *p, u, cp->g_on, cp->g_off, cp->allow_deactivation,
+                                                              list);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && n_exact) e = cudaMemcpyAsync(n_exact, list, sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+  }
+  if (e != cudaSuccess) r = xk_set_cuda_error(e, __FILE__, __LINE__);
+  cudaFreeAsync(list, st);
+  return r;
 }
 
 extern "C" xk_status xk_pair_step(const xk_mesh* m, xk_pairs* p, const xk_contact_pattern* pat, const double* u,

@@ -90,6 +90,10 @@ class AssemblyEngine:
         # learned candidate pruning (``set_pruner``); the exact path verifies it every ``verify_every`` detections
         self.pruner = None
         self.verify_every = 10
+        # mixed engine: detection narrowphase in float with the exact routine for the pairs near the
+        # active-set thresholds (xk_narrowphase_screened); the active set is the exact one either way
+        self.screened_detection = True
+        self._n_exact = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._n_detect = 0
         self.prune_stats = {"detections": 0, "verified": 0, "candidates": 0, "kept": 0, "missed": 0}
 
@@ -236,7 +240,13 @@ class AssemblyEngine:
                C.byref(self._spare.c), s)
         self._spare.set_n(self._spare.c.n)
         self.pairs, self._spare = self._spare, self.pairs
-        L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), C.byref(self.cp), 1, s)
+        screened = self.precision == L.XK_MIXED and self.screened_detection and not self.coated
+        if screened:
+            L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u), ptr(self.node32), s)
+            L.call("xk_narrowphase_screened", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), ptr(self.node32),
+                   C.byref(self.cp), ptr(self._n_exact), s)
+        else:
+            L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), C.byref(self.cp), 1, s)
         self.pattern.build(self.pairs, stream)
         if self.precision == L.XK_MIXED:
             self._to32(s)
@@ -246,7 +256,8 @@ class AssemblyEngine:
         self.graph = None
         self.stats = {"raw": n_raw, "prefilter": n_pre, "candidates": n_all, "kept_candidates": nc,
                       "pairs": self.pairs.n, "members": self.pattern.n_members, "contact_blocks": self.pattern.nnzb,
-                      "contact_blocks_full": self.pattern.nnzb_full}
+                      "contact_blocks_full": self.pattern.nnzb_full,
+                      "narrowphase_exact": int(self._n_exact.item()) if screened else self.pairs.n}
         return self.stats
 
     # ------------------------------------------------------------------ per iteration

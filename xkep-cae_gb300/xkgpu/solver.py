@@ -171,6 +171,10 @@ class SolverSettings:
     dt_contact_change_threshold: float = 0.3
     dt_min_fraction: float = 0.0
     dt_max_fraction: float = 0.0
+    # the energy test |du . R| / (its first value) < energy_tol (the reference's fixed 1e-10,
+    # _newton_steps.py:229-235); 0 switches it off, so that only the force and displacement tests end
+    # an increment (used where two runs are compared to a tighter tolerance than the energy test gives)
+    energy_tol: float = 1e-10
 
 
 @dataclass
@@ -231,26 +235,52 @@ class HostDirectSolve:
 
 
 class EngineBackend:
-    """``AssemblyEngine`` in the solver's terms (FP64 or mixed engine)."""
+    """``AssemblyEngine`` in the solver's terms (FP64 or mixed engine).
 
-    def __init__(self, engine):
+    ``graph=True`` replays the assembly as a CUDA graph: the first assembly
+    after a detection records it on static input buffers (the recording's
+    warm-up launch is that attempt's assembly), the later attempts of the
+    increment copy their inputs in and replay it.
+    """
+
+    def __init__(self, engine, graph: bool = False):
         self.eng = engine
         self.device = engine.device
         self.ndof = engine.mesh.ndof
+        self.graph = graph
         self._fint = torch.zeros(self.ndof, dtype=torch.float64, device=self.device)
+        self._static = None
+        self.counts = {"detect": 0, "assemble": 0, "captures": 0, "replays": 0, "internal_force": 0}
 
     def detect(self, u: torch.Tensor) -> dict:
+        self.counts["detect"] += 1
         return self.eng.detect(u)
 
     def assemble(self, u: torch.Tensor, u_ref: torch.Tensor, f_ext: torch.Tensor, fixed_u8: torch.Tensor):
         """(R, f_c): R = f_int + f_c - f_ext with fixed entries zero; f_c = -(f_n + f_f) on the free DOFs."""
-        R = self.eng.assemble(u, u_ref, f_ext, fixed_u8).clone()
-        f_c = R + f_ext - self.eng.f_int
+        eng = self.eng
+        self.counts["assemble"] += 1
+        if not self.graph:
+            R = eng.assemble(u, u_ref, f_ext, fixed_u8).clone()
+        else:
+            if self._static is None:
+                self._static = tuple(torch.empty_like(t) for t in (u, u_ref, f_ext, fixed_u8))
+            for dst, src in zip(self._static, (u, u_ref, f_ext, fixed_u8)):
+                dst.copy_(src)
+            if eng.graph is None:  # a detection dropped the graph: record it (its warm-up runs this assembly)
+                eng.capture(*self._static)
+                self.counts["captures"] += 1
+            else:
+                eng.replay()
+                self.counts["replays"] += 1
+            R = eng.R.clone()
+        f_c = R + f_ext - eng.f_int
         return R, f_c
 
     def internal_force(self, u: torch.Tensor) -> torch.Tensor:
         """f_int(u) alone, in the engine's precision (the line search's only assembly)."""
         eng = self.eng
+        self.counts["internal_force"] += 1
         if eng.precision == L.XK_MIXED:
             import ctypes as C
 
@@ -284,13 +314,16 @@ class ContactFrictionSolver:
     loads over ``t_total`` (the physical time ``dt_physical``) in adaptive increments.
 
     ``dynamics`` is the time integrator (``GpuGeneralizedAlpha`` or any object with the reference's
-    TimeIntegrationStrategy methods plus ``mass_coefficient(dt)`` and the lumped mass ``m``);
+    TimeIntegrationStrategy methods plus ``mass_coefficient(dt)`` and the lumped mass ``m``), or
+    ``QuasiStatic()`` for a load step without inertia (the reference's loop is dynamic only,
+    ``process.py:179-185``; without inertia its predictor, corrector and mass terms drop out);
     ``linear_solve(backend, R, fixed, mass_diag) -> du or None`` the linear solver.
     """
 
     def __init__(self, backend, dynamics, *, t_total: float, fixed_dofs=(), prescribed_dofs=(),
-                 prescribed_values=(), f_ext_total=None, f_ext_base=None, settings: SolverSettings | None = None,
-                 linear_solve=None, record_u: bool = True, verbose: bool = False):
+                 prescribed_values=(), prescribed_start=None, f_ext_total=None, f_ext_base=None,
+                 settings: SolverSettings | None = None, linear_solve=None, record_u: bool = True,
+                 verbose: bool = False):
         self.b = backend
         self.dyn = dynamics
         self.cfg = settings or SolverSettings()
@@ -306,6 +339,10 @@ class ContactFrictionSolver:
         self.free = torch.as_tensor(~fx, device=dev)
         self.pd = torch.as_tensor(pd, device=dev)
         self.pv = torch.as_tensor(np.asarray(prescribed_values, dtype=np.float64), device=dev)
+        # values at load fraction 0: zero as in the reference (u[dofs] = load_frac * values); a run that
+        # continues from a driven state (the steps of an oscillation) ramps from where the last one ended
+        self.p0 = torch.zeros_like(self.pv) if prescribed_start is None else torch.as_tensor(
+            np.asarray(prescribed_start, dtype=np.float64), device=dev)
         z = torch.zeros(nd, dtype=torch.float64, device=dev)
         self.f_ext_total = z if f_ext_total is None else torch.as_tensor(f_ext_total, dtype=torch.float64,
                                                                           device=dev)
@@ -343,7 +380,7 @@ class ContactFrictionSolver:
         for att in range(cfg.max_nr_attempts):
             attempts += 1
             R, f_c = b.assemble(u, u_ref, f_ext, self.fixed_u8)
-            if dt_sub > 1e-30:
+            if dt_sub > 1e-30 and dyn.is_dynamic:
                 dyn.correct(u, None, dt_sub)
                 R = dyn.effective_residual(R, dt_sub)
                 R = torch.where(self.free, R, zero)
@@ -368,7 +405,7 @@ class ContactFrictionSolver:
                 return False, attempts, n_active, f_c, hist, "diverged", True
             # tangent and solve
             mass = None
-            if dt_sub > 1e-30:
+            if dt_sub > 1e-30 and dyn.is_dynamic:
                 mass = dyn.mass_coefficient(dt_sub) * dyn.m
             du = self.linear_solve(b, R, self.fixed, mass)
             if du is None:
@@ -395,7 +432,7 @@ class ContactFrictionSolver:
             energy = abs(float(torch.dot(du, R)))
             if energy_ref is None:
                 energy_ref = energy if energy > 1e-30 else 1.0
-            if energy_ref > 1e-30 and energy / energy_ref < 1e-10:
+            if cfg.energy_tol > 0.0 and energy_ref > 1e-30 and energy / energy_ref < cfg.energy_tol:
                 return True, attempts, n_active, f_c, hist, "energy", False
         return False, attempts, n_active, f_c, hist, "max attempts", False
 
@@ -438,7 +475,7 @@ class ContactFrictionSolver:
                 if not isinstance(u, torch.Tensor):
                     u = torch.as_tensor(u, dtype=torch.float64, device=dev)
             if self.pd.numel():
-                u[self.pd] = lf * self.pv
+                u[self.pd] = self.p0 + lf * (self.pv - self.p0)
             b.detect(u)
             ok, att, n_active, f_c, hist, kind, diverged = self._newton(u, u_ref, f_ext, dt_sub, f_ext_ref_norm,
                                                                         dynamic_ref)
@@ -457,7 +494,7 @@ class ContactFrictionSolver:
                 out.u, out.converged = u, False
                 out.n_increments, out.total_attempts, out.n_cutbacks = increment, total, ctl.n_cutbacks
                 return out
-            if dt_sub > 1e-30:
+            if dt_sub > 1e-30 and dyn.is_dynamic:
                 dyn.correct(u, None, dt_sub)
             ctl.success(lf, load_prev, att, n_active, prev_n_active)
             prev_n_active = n_active
