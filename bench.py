@@ -203,6 +203,76 @@ def gather_tangent_bytes(n_members, n_contrib, nnzb, mixed: bool, sides: bool = 
     return 16 * w * n_members + 4 * n_contrib + 4 * (nnzb + 1) + 9 * w * nnzb
 
 
+def kernel_roofline_mixed(eng, u1, u0, peak, reps: int = 50) -> list:
+    """Every launch of the mixed assembly alone: CUDA-event time (mean over ``reps`` back-to-back calls on
+    one stream), algorithmic bytes and the fraction of the HBM peak.
+
+    Algorithmic bytes (compulsory traffic, each array read or written once):
+    node preparation 72 B read (X, u, u_ref) + 64 B record written per node; other pairs 48 B read
+    + 36 B written per pair + the 64 B node records; the beam 64 B element record + 432 B of its three
+    stored 6x6 float blocks per element, the node records and the 48 B double f_int rows per node;
+    contributing pairs 78 B read + 70 B written + a 64 B record each + the node records; the element
+    sums 64 B record + 8 B incidence per member, 4 B pointer and 80 floats written per element; the
+    block gather 16 B of inline term codes and 36 B written per stored block, 36 floats of element
+    sums read per element; the residual 48 B f_int read, 48 B R written and 2 x 32 B element force
+    sums per node.
+    """
+    import ctypes as C
+
+    import torch
+
+    from xkgpu import _lib as L
+    from xkgpu.device import ptr, stream_handle
+
+    s = torch.cuda.current_stream()
+    sh = stream_handle(s)
+    pat = eng.pattern
+    n_n, n_e = eng.mesh.n_nodes, eng.mesh.n_elems
+    n_m = pat.n_members
+    n_o = eng.pairs.n - n_m
+    nb = pat.nnzb
+    pc = C.byref(pat.c)
+    eng.assemble(u1, u0)  # records and element sums current
+    launches = [
+        ("k_nodes_prepare", lambda: L.call("xk_nodes_prepare", C.byref(eng.mesh.c), ptr(u1), ptr(u0), ptr(eng.node32),
+                                           sh), 136 * n_n),
+        ("k_pair_other32 (+ near-parallel)", lambda: L.call("xk_pair_step32", C.byref(eng.pairs32.c),
+                                                            ptr(eng.node32), C.byref(eng.cp), ptr(eng.rec),
+                                                            L.XK_PAIRS_OTHERS, sh), 84 * n_o + 64 * n_n),
+        ("k_beam_zero32 + k_beam32q", lambda: L.call("xk_beam_assemble32", C.byref(eng.mesh.c),
+                                                     C.byref(eng.beam.section), ptr(eng.elem32),
+                                                     C.byref(eng.beam.plan), ptr(eng.node32), ptr(eng.f_int),
+                                                     ptr(eng.K_beam), sh), (64 + 432) * n_e + (64 + 48) * n_n),
+        ("k_pair_member32 (+ near-parallel)", lambda: L.call("xk_pair_step32", C.byref(eng.pairs32.c),
+                                                             ptr(eng.node32), C.byref(eng.cp), ptr(eng.rec),
+                                                             L.XK_PAIRS_MEMBERS, sh), 212 * n_m + 64 * n_n),
+        ("k_elem_sums_rec", lambda: L.call("xk_contact_gather_tangent", pc, ptr(eng.rec), eng.precision,
+                                           L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_SIDES_SUMS,
+                                           ptr(eng.K_c), sh), 72 * n_m + 4 * (n_e + 1) + 320 * n_e),
+        ("k_gather_tangent_sides", lambda: L.call("xk_contact_gather_tangent", pc, ptr(eng.rec), eng.precision,
+                                                  L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_SIDES_BLOCKS,
+                                                  ptr(eng.K_c), sh), (16 + 36) * nb + 144 * n_e),
+        ("k_gather_force_elem", lambda: L.call("xk_contact_gather_force_elem", pc, eng.precision, ptr(eng.f_int), -1.0,
+                                               None, None, ptr(eng.R), ptr(eng.norm2), sh), (48 + 48 + 64) * n_n),
+    ]
+    out = []
+    for name, fn, nbytes in launches:
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(reps):
+            fn()
+        b.record(s)
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / 1e3 / reps
+        out.append({"kernel": name, "us": round(1e6 * t, 2), "bytes": int(nbytes),
+                    "achieved_gbs": round(nbytes / t / 1e9, 1), "frac": round(nbytes / t / 1e9 / peak, 3)})
+    eng.assemble(u1, u0)  # leave the engine's outputs as one assembly left them
+    return out
+
+
 # --------------------------------------------------------------------------- GPU arm
 
 
@@ -345,8 +415,168 @@ def pruning_section(args, dev, w, u0, u1, ms_fp64):
            "R_rel_diff_vs_unpruned": R_diff, "train_s": t_train, "train": dataclasses.asdict(rep),
            "verify_every": eng.verify_every}
     out["scoring"] = mlp_scoring(pr, (stats["candidates"], 8_000_000), 20, 3, dev)
-    del eng, pr
+    del eng
     torch.cuda.empty_cache()
+    return out, pr
+
+
+def detection_section(dev, w, u0, reps: int = 3) -> dict:
+    """Per-phase wall times (ms, host-synchronised) of a steady-state detection of the mixed engine
+    (merging into an existing table), and the whole detection of both engines."""
+    import ctypes as C
+
+    import torch
+
+    from xkgpu import _lib as L
+    from xkgpu.device import ptr, stream_handle
+    from xkgpu.engine import AssemblyEngine
+
+    st = w.strand
+    out = {}
+    for prec in ("mixed", "fp64"):
+        eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=prec, device=dev,
+                             **w.engine_kwargs())
+        eng.detect(u0)
+        eng.assemble(u0, u0)
+        tot = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            stats = eng.detect(u0)
+            torch.cuda.synchronize()
+            tot.append(1e3 * (time.perf_counter() - t0))
+        res = {"detect_ms": min(tot), "pairs": stats["pairs"], "narrowphase_exact_pairs": stats["narrowphase_exact"]}
+        if prec == "mixed":
+            s = stream_handle(None)
+            ph = {}
+
+            def tic():
+                torch.cuda.synchronize()
+                return time.perf_counter()
+
+            for _ in range(reps):
+                eng.sync_state()
+                t = tic()
+                cands, nc = eng.candidates(u0)
+                t1 = tic()
+                eng._spare.reserve(max(eng._spare.cap, eng.pairs.n + nc), keep=False)
+                L.call("xk_pairs_merge", C.byref(eng.mesh.c), C.byref(eng.pairs.c), ptr(cands), nc,
+                       C.byref(eng._spare.c), s)
+                eng._spare.set_n(eng._spare.c.n)
+                eng.pairs, eng._spare = eng._spare, eng.pairs
+                t2 = tic()
+                L.call("xk_nodes_prepare", C.byref(eng.mesh.c), ptr(u0), ptr(u0), ptr(eng.node32), s)
+                L.call("xk_narrowphase_screened", C.byref(eng.mesh.c), C.byref(eng.pairs.c), ptr(u0),
+                       ptr(eng.node32), C.byref(eng.cp), ptr(eng._n_exact), s)
+                t3 = tic()
+                eng.pattern.build(eng.pairs)
+                t4 = tic()
+                eng._to32(s)
+                t5 = tic()
+                for k, v in (("broadphase", t1 - t), ("merge", t2 - t1), ("narrowphase", t3 - t2),
+                             ("pattern", t4 - t3), ("float_table", t5 - t4)):
+                    ph[k] = min(ph.get(k, 1e9), 1e3 * v)
+            res["phases_ms"] = {k: round(v, 3) for k, v in ph.items()}
+        out[prec] = res
+        del eng
+        torch.cuda.empty_cache()
+    return out
+
+
+def c5_section(args, dev, w, pr) -> dict:
+    """The 1027-wire strand through a prescribed bending oscillation (curvature 1/(50 D) cos(2 pi k / 30),
+    30 steps, a fresh 3e-4 d jitter per step): every step one detection and two graph-replayed
+    Newton-iteration assemblies, with the trained pruner (verified exactly every 10 detections) and
+    without it."""
+    import torch
+
+    from xkgpu import runs
+
+    st = w.strand
+    D = 2.0 * max(x.lay_radius for x in st.wires) + w.meta["d"]
+    kappa0 = 1.0 / (50.0 * D)
+    n_steps = 30
+    out = {"workload": f"{args.workload}: arc of curvature kappa0 cos(2 pi k / {n_steps}), kappa0 = 1/(50 D), "
+                       f"D = {D:.2f} mm; seeded noise + 3e-4 d jitter per step", "steps": n_steps}
+    res = {}
+    for name, p in (("unpruned", None), ("pruned", pr)):
+        r = runs.run_detection_oscillation(w, kappa0, n_steps=n_steps, iterations=2, pruner=p, verify_every=10)
+        res[name] = r
+        torch.cuda.empty_cache()
+    a, b = res["unpruned"], res["pruned"]
+    ps = b["prune_stats"]
+    out["missed_contacts"] = ps["missed"]
+    out["verified_detections"] = ps["verified"]
+    out["kept_fraction"] = ps["kept"] / max(ps["candidates"], 1)
+    out["kept_fraction_per_step"] = [round(k / max(c, 1), 4) for k, c in zip(b["kept_candidates"], b["candidates"])]
+    out["members_equal_every_step"] = a["members"] == b["members"]
+    for name, r in res.items():
+        det = r["detect_ms"][1:]  # the first detection also sizes the buffers
+        asm = r["assemble_ms"][1:]
+        out[name] = {"detect_ms_mean": float(np.mean(det)), "assemble_ms_mean": float(np.mean(asm)),
+                     "pairs_mean": float(np.mean(r["pairs"][1:])),
+                     "increment_ms (detection + 2 iterations)": float(np.mean(det) + 2 * np.mean(asm))}
+    out["gain_per_increment"] = (out["unpruned"]["increment_ms (detection + 2 iterations)"]
+                                 / out["pruned"]["increment_ms (detection + 2 iterations)"])
+    out["R_rel_diff_last_step"] = float((b["R_last"] - a["R_last"]).abs().max() / a["R_last"].abs().max())
+    return out
+
+
+def c2_section(args, dev) -> dict:
+    """The 37-wire quasi-static load step: the outer layer pressed radially inward by the lay gap plus
+    0.005 d, FP64 and mixed, over the restated solver loop with the device block solve."""
+    import torch
+
+    from xkgpu import runs
+    from xkgpu import solver as S
+    from xkgpu import workloads as W
+
+    out = {}
+    us = {}
+    for prec in ("fp64", "mixed"):
+        w = W.strand_workload("strand37", 37, 2.0, 40.0, 4, 32, gap_frac=0.0, seed=2)
+        lay = max(x.lay_radius for x in w.strand.wires) / 3.0 - w.meta["d"]
+        amount = lay + 0.005 * w.meta["d"]
+        res, b, secs = runs.run_load_step(w, prec, layer=3, amount=amount,
+                                          settings=S.SolverSettings(dt_max_fraction=0.1, max_increments=80))
+        out[prec] = {"converged": res.converged, "increments": res.n_increments, "newton_attempts": res.total_attempts,
+                     "cutbacks": res.n_cutbacks, "wall_s": secs, "solver": dict(getattr(b, "lin_stats", {})),
+                     "active_pairs_end": res.increments[-1].n_active if res.increments else 0}
+        us[prec] = res.u.cpu().numpy()
+        torch.cuda.empty_cache()
+    out["workload"] = ("strand37 (37 wires, d 2 mm, pitch 40 mm, 4 pitches, 32 el/pitch, lay gap "
+                       f"{lay:.4f} mm): outer layer moved radially inward by {amount:.4f} mm, inner wires clamped "
+                       "at both ends")
+    out["u_rel_diff_mixed_vs_fp64"] = float(np.abs(us["mixed"] - us["fp64"]).max() / np.abs(us["fp64"]).max())
+    return out
+
+
+def c3_section(args, dev, n_steps: int = 20) -> dict:
+    """The 91-wire strand: Generalized-alpha (rho_inf 0.9) ramp to curvature 1/(50 D) in 1 ms, then
+    oscillation steps of dt = 1e-4 s with the end curvature following cos(2 pi k / 20); mu = 0.1,
+    graph-replayed assembly, FP64 and mixed."""
+    import torch
+
+    from xkgpu import runs
+    from xkgpu import workloads as W
+
+    out = {}
+    us = {}
+    for prec in ("fp64", "mixed"):
+        w = W.strand_workload("strand91", 91, 2.0, 40.0, 4, 32, gap_frac=0.0, seed=0)
+        D = 2.0 * max(x.lay_radius for x in w.strand.wires) + w.meta["d"]
+        r = runs.run_bend_oscillation(w, prec, kappa=1.0 / (50.0 * D), n_steps=n_steps)
+        n_it = r["counts"]["assemble"]
+        out[prec] = {"converged": r["converged"], "attempts_per_step": [sum(a) for a in r["attempts"]],
+                     "wall_s": r["wall_s"], "solve_s": r["solve_s"], "solves": r["solves"],
+                     "newton_iterations": n_it, "ms_per_newton_iteration": 1e3 * r["wall_s"] / max(n_it, 1),
+                     "ms_per_iteration_without_solve": 1e3 * (r["wall_s"] - r["solve_s"]) / max(n_it, 1),
+                     "solver": r.get("lin")}
+        us[prec] = r["u"]
+        torch.cuda.empty_cache()
+    n = min(len(us["fp64"]), len(us["mixed"]))
+    out["u_rel_diff_per_step"] = [float(np.abs(us["mixed"][k] - us["fp64"][k]).max() / np.abs(us["fp64"][k]).max())
+                                  for k in range(n)]
     return out
 
 
@@ -640,6 +870,9 @@ def run_gpu(args, rank, world):
     kernel_names = {L.XK_GATHER_LANES: "k_gather_tangent_lanes<float>", L.XK_GATHER_CHUNKS: "k_gather_tangent<float>",
                     L.XK_GATHER_SIDES: "k_elem_sums<float> + k_gather_tangent_sides<float>"}
     peak, peak_kind = _peaks()
+    kernels = None
+    if engines["mixed"].gather_variant == L.XK_GATHER_SIDES:
+        kernels = kernel_roofline_mixed(engines["mixed"], u1, u0, peak)
     # the autotuner's times of every tangent schedule (ms per call), before the engines are released
     sched_ms = {p: {variant_name[v]: round(t, 4) for v, t in getattr(engines[p], "tune_times", {}).items()}
                 for p in ("mixed", "fp64")}
@@ -693,7 +926,13 @@ def run_gpu(args, rank, world):
     if not args.no_extras and world == 1:
         del engines, eng
         torch.cuda.empty_cache()
-        extras["learned_pruning"] = pruning_section(args, dev, w, u0, u1, ms_fp64)
+        extras["detection"] = detection_section(dev, w, u0)
+        extras["learned_pruning"], pr = pruning_section(args, dev, w, u0, u1, ms_fp64)
+        extras["c5_oscillation"] = c5_section(args, dev, w, pr)
+        del pr
+        if args.runs:
+            extras["c2_load_step"] = c2_section(args, dev)
+            extras["c3_oscillation"] = c3_section(args, dev)
         extras["batched"] = batch_section(args, dev)
         extras["coated"] = coated_section(args, dev)
         extras["device_solve"] = device_solve_section(args, dev)
@@ -706,7 +945,7 @@ def run_gpu(args, rank, world):
     out = {
         "metric": METRIC, "value": units / t_mixed * args.steps, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed: float arithmetic, double frames/gap/norm)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (mixed: float arithmetic and float quaternion frames; float-float contact gap of contributing pairs; FP64 near-parallel closest points, detection decisions near the thresholds and residual norm)",
         "data": "synthetic (seeded strand geometry and perturbations of the reference's configuration)",
         "config": {"workload": "strand1027: 1027 wires (18 layers), d=0.5 mm, pitch 20 mm, 4 pitches, "
                                "24 el/pitch, gap -0.005 d, seeded noise", "n_nodes": st.n_nodes,
@@ -737,6 +976,7 @@ def run_gpu(args, rank, world):
                                    "bytes_per_launch": by_mixed, "launch_ms": 1e3 * tk_mixed,
                                    "fp64": {"achieved": by_fp64 / tk_fp64 / 1e9, "launch_ms": 1e3 * tk_fp64,
                                             "bytes_per_launch": by_fp64}}},
+        "kernels_mixed": kernels,
         "e2e": {"value": units / t_e2e * args.steps, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": per_launch * args.steps,
@@ -944,6 +1184,8 @@ def main():
     ap.add_argument("--workload", default="strand1027")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the learned-pruning and batched sections")
+    ap.add_argument("--runs", action="store_true", help="also the solver runs (37-wire load step, 91-wire bending "
+                                                        "oscillation), several minutes")
     ap.add_argument("--mlp-n", type=int, default=8_000_000, help="samples scored by --profile mlp")
     ap.add_argument("--profile", choices=["mixed", "fp64", "mlp"], default=None,
                     help="profiling driver: detect once, then --steps eager assemblies, no timing")

@@ -31,7 +31,9 @@ typedef int xk_status;
 #define XK_ERR_OVERFLOW 4  /* a bounded per-item work list overflowed */
 
 #define XK_FP64 0   /* every operation in double */
-#define XK_MIXED 1  /* float arithmetic, double frames / strain / gap / reductions */
+#define XK_MIXED 1  /* float arithmetic and float quaternion frames; contact gaps of contributing pairs in
+                       float-float; near-parallel closest points, detection decisions near the
+                       thresholds and the residual norm in double */
 
 typedef void* xk_stream;
 

@@ -146,7 +146,9 @@ def test_strand_sequence_mixed():
         u0 = _dev(z[f"inc{inc}_u"])
         u_ref = _dev(z[f"inc{inc}_u_ref"])
         s64, smx = e64.detect(u0), emx.detect(u0)
-        assert s64 == smx  # detection is exact FP64 in both modes
+        s64.pop("narrowphase_exact")
+        smx.pop("narrowphase_exact")
+        assert s64 == smx  # the same candidates, pairs and active set in both modes
         for it in range(int(z["n_iter"])):
             u = _dev(z[f"inc{inc}_it{it}_u"])
             e64.assemble(u, u_ref)
