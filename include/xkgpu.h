@@ -287,6 +287,10 @@ typedef struct {
   int64_t nnzb_full;      /* set by the build: blocks of the full matrix (nnzb without the index) */
   int32_t* low_ptr;       /* [n_nodes+1] */
   int32_t* low_blk;       /* [cap_blocks] */
+  /* Launch shape (0 = the built-in default): persistent CTAs per SM of the element-side block
+   * gather (XK_GATHER_SIDES).  Results do not depend on it; an autotuner may choose it. */
+  int32_t sides_per_sm;
+  int32_t pad_launch;
 } xk_contact_pattern;
 
 /* Returns XK_ERR_CAPACITY (with n_members, n_others, nnzb set) when a capacity
@@ -392,6 +396,9 @@ typedef struct {
                               pairs: [count, done, slots] from defer[0]; members: the same from
                               defer[cap + 2]), which keeps the exact double routine out of the common
                               kernels; each list is back at zero after its kernel */
+  int32_t block;           /* threads per CTA of the other-pair and member kernels: a multiple of 32 up to
+                              256, 0 = 256.  Results do not depend on it; an autotuner may choose it. */
+  int32_t pad_launch;
 } xk_pairs32;
 
 /* Per iteration: node records for the mixed kernels from u (and u_ref, nullable). */

@@ -50,13 +50,14 @@ def test_mixed_engine_solver_converges_to_fp64_run():
     """The reference's energy test stops an increment at a residual of about 1e-5 of its first value,
     so two runs that take different iterates agree only to that level.  Here both runs end their
     increments on the force test alone (the energy test off): FP64 at 1e-10 of the first residual,
-    mixed at 1e-6 (its float residual floor lies below that), over the same fixed increments."""
+    mixed at 2e-5 (above its float residual floor), over the same fixed increments."""
     z = golden("solve7_bend")
     cfg = dict(dt_max_fraction=float(z["dt_max_fraction"]), energy_tol=0.0, tol_disp=1e-12, dt_grow_factor=1.0,
                dt_shrink_attempt_threshold=1000, dt_contact_change_threshold=1e9)
     r64 = _run(z, "fp64", S.SolverSettings(tol_force=1e-10, **cfg))
-    rmx = _run(z, "mixed", S.SolverSettings(tol_force=1e-6, **cfg))
+    rmx = _run(z, "mixed", S.SolverSettings(tol_force=2e-5, max_nr_attempts=100, **cfg))
     assert rmx.converged and r64.converged
     assert [r.load_frac for r in rmx.increments] == [r.load_frac for r in r64.increments]
-    for a, b in zip(rmx.increments, r64.increments):
-        assert np.max(np.abs(a.u - b.u)) <= 1e-6 * np.max(np.abs(b.u)), a.step
+    diffs = [float(np.max(np.abs(a.u - b.u)) / np.max(np.abs(b.u))) for a, b in zip(rmx.increments, r64.increments)]
+    print("converged displacements, mixed vs fp64 per increment:", ["%.2e" % d for d in diffs])
+    assert max(diffs) <= 1e-6, diffs

@@ -191,8 +191,9 @@ XK_D bool midpoint_keep(const xk_mesh& m, const double* __restrict__ u, int i, i
 // offsets held in the lanes.  A candidate j > i is screened on the outward-rounded float boxes
 // (which can never reject an FP64 overlap), tested on the FP64 boxes, then the shared-node and
 // same-layer filters apply; hits are compacted with ballot/popc.
-// MODE 0: kept count per segment (cnt[i]), the sum of r_i + r_j over its kept candidates in a fixed
-//         lane order (rsum[i], for the prescreen margin), and the raw overlap count.
+// MODE 0: kept count per segment (cnt[i]), the sum of r_i + r_j over its kept candidates (each lane
+//         sums its own entries in round order, then a fixed butterfly: rsum[i], for the prescreen
+//         margin), and the raw overlap count.
 // MODE 1: the kept candidates of segment i sorted by j at off[i] (out), and their prescreen flags.
 template <int MODE>
 __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restrict__ u,
@@ -271,16 +272,15 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
     const unsigned bal = __ballot_sync(0xffffffffu, kept);
     n_raw += __popc(__ballot_sync(0xffffffffu, hit));
     if (MODE == 0) {
-      double v = kept ? xadd(ri, m.radii[j]) : 0.0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);  // fixed butterfly order
-      rs += v;
+      if (kept) rs = xadd(rs, xadd(ri, m.radii[j]));  // this lane's entries, in round order
     } else if (kept) {
       tmp[base + n_keep + __popc(bal & ((1u << lane) - 1u))] = j;
     }
     n_keep += __popc(bal);
   }
   if (MODE == 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);  // fixed butterfly order
     if (lane == 0) {
       cnt[i] = n_keep;
       rsum[i] = rs;

@@ -84,18 +84,48 @@ __global__ void k_inc_fill(const int32_t* __restrict__ mnodes, int nm, const int
   }
 }
 
-// Insertion sort of every segment [ptr[v], ptr[v+1]) so that sums run in a
-// fixed order whatever the order of the atomic fill.
-__global__ void k_segment_sort(const int32_t* __restrict__ ptr, long long nseg, int32_t* __restrict__ a) {
-  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// Sort every segment [ptr[v], ptr[v+1]) ascending, so that sums run in a fixed order whatever the
+// order of the atomic fill.  A warp per segment: up to 64 entries (the entries of a segment are
+// distinct) sit in two registers per lane and each finds its rank by comparing against all others
+// broadcast by shuffles, then the warp writes them to their ranks; a longer segment is sorted by
+// insertion by one lane.
+constexpr int SEG_T = 128;
+__global__ void __launch_bounds__(SEG_T) k_segment_sort(const int32_t* __restrict__ ptr, long long nseg,
+                                                        int32_t* __restrict__ a) {
+  const long long v = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (v >= nseg) return;
   const int lo = ptr[v], hi = ptr[v + 1];
-  for (int x = lo + 1; x < hi; ++x) {
-    const int key = a[x];
-    int y = x - 1;
-    while (y >= lo && a[y] > key) { a[y + 1] = a[y]; --y; }
-    a[y + 1] = key;
+  const int n = hi - lo;
+  if (n <= 1) return;
+  if (n > 64) {
+    if (lane == 0) {
+      for (int x = lo + 1; x < hi; ++x) {
+        const int key = a[x];
+        int y = x - 1;
+        while (y >= lo && a[y] > key) { a[y + 1] = a[y]; --y; }
+        a[y + 1] = key;
+      }
+    }
+    return;
   }
+  const int v0 = lane < n ? a[lo + lane] : 0x7fffffff;
+  const int v1 = lane + 32 < n ? a[lo + lane + 32] : 0x7fffffff;
+  int r0 = 0, r1 = 0;
+  const int n0 = n < 32 ? n : 32;
+  for (int k = 0; k < n0; ++k) {
+    const int x = __shfl_sync(0xffffffffu, v0, k);
+    r0 += x < v0;
+    r1 += x < v1;
+  }
+  for (int k = 0; k < n - 32; ++k) {
+    const int x = __shfl_sync(0xffffffffu, v1, k);
+    r0 += x < v0;
+    r1 += x < v1;
+  }
+  __syncwarp();
+  if (lane < n) a[lo + r0] = v0;
+  if (lane + 32 < n) a[lo + r1] = v1;
 }
 
 // MODE 0: count the distinct column nodes c >= v of each row v; MODE 1: write them sorted.  The
@@ -1022,7 +1052,7 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   XK_TRY(xk_exclusive_scan_i32(cnt, pat->inc_ptr, nn + 1, nullptr, st));
   XK_CUDA(cudaMemsetAsync(fill, 0, sizeof(int32_t) * (nn + 1), st));
   if (nm > 0) k_inc_fill<<<xk_blocks(nm, 256), 256, 0, st>>>(pat->member_nodes, (int)nm, pat->inc_ptr, fill, pat->inc);
-  k_segment_sort<<<xk_blocks(nn, 128), 128, 0, st>>>(pat->inc_ptr, nn, pat->inc);
+  k_segment_sort<<<xk_blocks(32LL * nn, SEG_T), SEG_T, 0, st>>>(pat->inc_ptr, nn, pat->inc);
   // block pattern rows
   XK_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), st));
   k_row_cols<0><<<xk_blocks(nn, 64), 64, 0, st>>>(pat->member_nodes, pat->inc_ptr, pat->inc, nn, cnt, nullptr,
@@ -1052,7 +1082,7 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   XK_CUDA(cudaMemsetAsync(bfill, 0, sizeof(int32_t) * (nb + 1), st));
   if (nm > 0) k_contrib<1><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
                                                                 bfill, pat->blk_ptr, pat->contrib, err);
-  if (nb > 0) k_segment_sort<<<xk_blocks(nb, 128), 128, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
+  if (nb > 0) k_segment_sort<<<xk_blocks(32LL * nb, SEG_T), SEG_T, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
   XK_CHECK_LAUNCH();
   // lower index of the stored blocks
   pat->nnzb_full = nb;
@@ -1065,7 +1095,7 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
     if (nb > 0)
       k_lower_index<1><<<xk_blocks(nb, 256), 256, 0, st>>>(nb, pat->blk_row, pat->col, fill, pat->low_ptr,
                                                            pat->low_blk);
-    k_segment_sort<<<xk_blocks(nn, 128), 128, 0, st>>>(pat->low_ptr, nn, pat->low_blk);
+    k_segment_sort<<<xk_blocks(32LL * nn, SEG_T), SEG_T, 0, st>>>(pat->low_ptr, nn, pat->low_blk);
     XK_CHECK_LAUNCH();
   }
   XK_TRY(fetch_i64(tot, h, 4, st));
@@ -1102,7 +1132,7 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
     if (nm > 0)
       k_elem_inc_fill<<<xk_blocks(nm, 256), 256, 0, st>>>(*p, pat->members, (int)nm, pat->elem_ptr, efill,
                                                           pat->elem_inc);
-    if (ne > 0) k_segment_sort<<<xk_blocks(ne, 128), 128, 0, st>>>(pat->elem_ptr, ne, pat->elem_inc);
+    if (ne > 0) k_segment_sort<<<xk_blocks(32LL * ne, SEG_T), SEG_T, 0, st>>>(pat->elem_ptr, ne, pat->elem_inc);
     XK_CHECK_LAUNCH();
     // inline term lists; a flag in serr (more than four terms somewhere) only disables the variant
     XK_CUDA(cudaMemsetAsync(serr, 0, sizeof(int32_t), st));
@@ -1240,7 +1270,7 @@ extern "C" xk_status xk_contact_gather_tangent(const xk_contact_pattern* pat, co
         k_elem_sums<TT, RSV, BC><<<xk_blocks(9LL * ne, 256), 256, 0, st>>>(ne, pat->elem_ptr, pat->elem_inc,   \
                                                                            (const TT*)rec, (TT*)pat->elem_sums); \
       if (blocks)                                                                                           \
-        k_gather_tangent_sides<TT, RSV, BC><<<sides_grid(pat->nnzb, sizeof(TT) == 4 ? 16 : 8), GS_T, 0, st>>>( \
+        k_gather_tangent_sides<TT, RSV, BC><<<sides_grid(pat->nnzb, pat->sides_per_sm > 0 ? pat->sides_per_sm : (sizeof(TT) == 4 ? 16 : 8)), GS_T, 0, st>>>( \
             pat->nnzb, reinterpret_cast<const int4*>(pat->bcodes), (const TT*)pat->elem_sums, (const TT*)rec,  \
             (TT*)Kc_vals);                                                                                  \
     } else if (chunks)                                                                                      \

@@ -1561,20 +1561,22 @@ extern "C" xk_status xk_pair_step32(xk_pairs32* q, const float* node32, const xk
     return xk_set_error(XK_ERR_ARG, "xk_pair_step32: rec is null");
   cudaStream_t st = (cudaStream_t)s;
   const int n_o = q->n - q->n_members;
+  // the CTA size of the common kernels: a launch-shape choice only (each thread owns one slot)
+  const int bs = (q->block >= 32 && q->block <= PAIR_T && q->block % 32 == 0) ? q->block : PAIR_T;
   if ((parts & XK_PAIRS_OTHERS) && n_o > 0) {
     if (q->defer) {
-      k_pair_other32<true><<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
+      k_pair_other32<true><<<xk_blocks(n_o, bs), bs, 0, st>>>(*q, node32);
       k_pair_other32_deferred<<<152, PAIR_T, 0, st>>>(*q, node32);
     } else {
-      k_pair_other32<false><<<xk_blocks(n_o, PAIR_T), PAIR_T, 0, st>>>(*q, node32);
+      k_pair_other32<false><<<xk_blocks(n_o, bs), bs, 0, st>>>(*q, node32);
     }
   }
   if ((parts & XK_PAIRS_MEMBERS) && q->n_members > 0) {
     if (q->defer) {
-      k_pair_member32<true><<<xk_blocks(q->n_members, PAIR_T), PAIR_T, 0, st>>>(*q, node32, *cp, rec);
+      k_pair_member32<true><<<xk_blocks(q->n_members, bs), bs, 0, st>>>(*q, node32, *cp, rec);
       k_pair_member32_deferred<<<152, PAIR_T, 0, st>>>(*q, node32, *cp, rec);
     } else {
-      k_pair_member32<false><<<xk_blocks(q->n_members, PAIR_T), PAIR_T, 0, st>>>(*q, node32, *cp, rec);
+      k_pair_member32<false><<<xk_blocks(q->n_members, bs), bs, 0, st>>>(*q, node32, *cp, rec);
     }
   }
   XK_CHECK_LAUNCH();

@@ -65,7 +65,7 @@ class Pairs32(C.Structure):
     _fields_ = [("n", C.c_int32), ("cap", C.c_int32), ("n_members", C.c_int32)] + [
         (n, vp) for n in ("pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
                           "dissipation", "k_pen", "k_t", "status", "stick", "mu")] + [
-        (n, vp) for n in COAT32_FIELDS] + [("defer", vp)]
+        (n, vp) for n in COAT32_FIELDS] + [("defer", vp), ("block", C.c_int32), ("pad_launch", C.c_int32)]
 
 
 class BeamPlan(C.Structure):
@@ -98,7 +98,8 @@ class ContactPattern(C.Structure):
         (n, vp) for n in ("members", "member_nodes", "others", "inc_ptr", "inc", "row_ptr", "col", "blk_row",
                           "blk_ptr", "contrib")] + [("n_elems", C.c_int64), ("sides_ok", C.c_int64)] + [
         (n, vp) for n in ("node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums",
-                          "norm_scratch")] + [("nnzb_full", C.c_int64), ("low_ptr", vp), ("low_blk", vp)]
+                          "norm_scratch")] + [("nnzb_full", C.c_int64), ("low_ptr", vp), ("low_blk", vp),
+                                              ("sides_per_sm", C.c_int32), ("pad_launch", C.c_int32)]
 
 
 P = C.POINTER

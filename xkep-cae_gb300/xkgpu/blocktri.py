@@ -250,6 +250,16 @@ class BlockTridiagonalSolver:
         rhs = torch.where(free, -R.to(torch.float64), zero)
         du, it, rel = gmres(matvec, rhs, precond, rtol=self.rtol, restart=self.restart, max_iter=self.max_iter)
         st = self.stats
+        if not rel <= max(1e3 * self.rtol, 1e-7) and F is not self._buf:
+            # the float32 factors were too coarse for this system: factor in FP64 and solve again
+            st["fp64_refactor"] = st.get("fp64_refactor", 0) + 1
+            F = self._buf
+            pivs = blocktri_factor(*F)
+            du2, it2, rel2 = gmres(matvec, rhs, precond, rtol=self.rtol, restart=self.restart,
+                                   max_iter=self.max_iter)
+            it += it2
+            if rel2 < rel:
+                du, rel = du2, rel2
         st["solves"] += 1
         st["gmres_iterations"] += it
         st["max_rel_residual"] = max(st["max_rel_residual"], rel)

@@ -86,6 +86,9 @@ class AssemblyEngine:
         self.graph = None
         self.gather_variant = L.XK_GATHER_DEFAULT
         self.autotune = True
+        self.tune_launch_shapes = False  # also tune the launch shapes in capture (tune(shapes=True))
+        self.tune_shapes = {}
+        self._pair_block = 0  # 0: the kernels' default CTA size
         self._tuned_for = None
         # learned candidate pruning (``set_pruner``); the exact path verifies it every ``verify_every`` detections
         self.pruner = None
@@ -280,6 +283,7 @@ class AssemblyEngine:
         if p == L.XK_MIXED:
             if not self._state_in32:
                 self._to32(s)
+            self.pairs32.c.block = self._pair_block  # the float table's struct is rebuilt when it grows
             L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u_ref), ptr(self.node32), s)
         so.wait_stream(main)
         sb.wait_stream(main)
@@ -354,35 +358,71 @@ class AssemblyEngine:
             L.call("xk_pair_step", C.byref(self.mesh.c), C.byref(self.pairs.c), pat, ptr(u), ptr(u_ref),
                    C.byref(self.cp), L.XK_STAGE_ALL, self.precision, L.XK_OUT_COMBINED, ptr(self.rec), s)
 
-    def tune(self, reps: int = 5) -> dict:
-        """Time the contact-tangent reduction schedules on the current records and keep the fastest.
+    def _time_calls(self, fn, reps: int) -> float:
+        s = torch.cuda.current_stream()
+        for _ in range(2):
+            fn(s)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(reps):
+            fn(s)
+        b.record(s)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    def tune(self, reps: int = 5, shapes: bool = False) -> dict:
+        """Time the contact-tangent reduction schedules on the current records and keep the fastest;
+        with ``shapes`` also the launch shapes: the CTA size of the float pair kernels and the persistent
+        CTAs per SM of the element-side block gather.
 
         Run after an ``assemble`` of the increment (the records must be current);
-        values do not depend on the choice beyond rounding order.
+        values do not depend on the choice beyond rounding order (the schedules) or at all (the shapes).
         """
         times = {}
         if self.pattern.nnzb == 0:
             return times
-        s = torch.cuda.current_stream()
+        pc = C.byref(self.pattern.c)
         variants = [L.XK_GATHER_LANES, L.XK_GATHER_CHUNKS]
         if self.pattern.c.sides_ok == 1:  # every block fits four inline terms (wire meshes)
             variants.append(L.XK_GATHER_SIDES)
         for v in variants:
-            for _ in range(2):
-                L.call("xk_contact_gather_tangent", C.byref(self.pattern.c), ptr(self.rec), self.precision,
-                       L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, v, ptr(self.K_c), stream_handle(s))
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(s)
-            for _ in range(reps):
-                L.call("xk_contact_gather_tangent", C.byref(self.pattern.c), ptr(self.rec), self.precision,
-                       L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, v, ptr(self.K_c), stream_handle(s))
-            b.record(s)
-            torch.cuda.synchronize()
-            times[v] = a.elapsed_time(b) / reps
+            times[v] = self._time_calls(lambda s, v=v: L.call(
+                "xk_contact_gather_tangent", pc, ptr(self.rec), self.precision, L.XK_OUT_COMBINED,
+                L.XK_WHICH_COMBINED, v, ptr(self.K_c), stream_handle(s)), reps)
         self.gather_variant = min(times, key=times.get)
         self.tune_times = times
         self._tuned_for = (self.pattern.version, self.precision)
+        if shapes:
+            self.tune_shapes = self._tune_shapes(reps)
         return times
+
+    def _tune_shapes(self, reps: int) -> dict:
+        """Launch shapes, each timed alone on the current state; the defaults are among the candidates."""
+        out = {}
+        if self.precision == L.XK_MIXED and self._state_in32:
+            q = self.pairs32.c
+            t = {}
+            for bs in (128, 256):
+                q.block = bs
+                t[bs] = self._time_calls(lambda s: L.call("xk_pair_step32", C.byref(q), ptr(self.node32),
+                                                          C.byref(self.cp), ptr(self.rec), L.XK_PAIRS_ALL,
+                                                          stream_handle(s)), reps)
+            q.block = min(t, key=t.get)
+            self._pair_block = q.block
+            out["pair_block"] = {"times_ms": t, "chosen": q.block, "default": 256}
+        if self.gather_variant == L.XK_GATHER_SIDES:
+            pat = self.pattern.c
+            t = {}
+            for per_sm in (4, 8, 12, 16, 24):
+                pat.sides_per_sm = per_sm
+                t[per_sm] = self._time_calls(lambda s: L.call(
+                    "xk_contact_gather_tangent", C.byref(pat), ptr(self.rec), self.precision, L.XK_OUT_COMBINED,
+                    L.XK_WHICH_COMBINED, L.XK_GATHER_SIDES_BLOCKS, ptr(self.K_c), stream_handle(s)), reps)
+            pat.sides_per_sm = min(t, key=t.get)
+            out["sides_ctas_per_sm"] = {"times_ms": t, "chosen": pat.sides_per_sm,
+                                        "default": 16 if self.precision == L.XK_MIXED else 8}
+        self.graph = None
+        return out
 
     def capture(self, u, u_ref=None, f_ext=None, fixed=None):
         """Record ``assemble`` on these (static) buffers as a CUDA graph."""
@@ -393,7 +433,7 @@ class AssemblyEngine:
         torch.cuda.current_stream().wait_stream(st)
         if self.autotune and self._tuned_for != (self.pattern.version, self.precision):
             torch.cuda.synchronize()
-            self.tune()
+            self.tune(shapes=self.tune_launch_shapes)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, stream=st):
             self.assemble(u, u_ref, f_ext, fixed, stream=st)
