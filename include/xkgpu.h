@@ -587,7 +587,8 @@ xk_status xk_system_blocktri(const xk_system* A, const int32_t* pos, int32_t bn,
 /* Features of candidate pairs cands[2*i], cands[2*i+1] at X + u (u may be
  * null): midpoint separation, |cos| of the tangent angle, half lengths (all
  * over r_a + r_b), layer distance, core flag, previous-step gap (from `old`,
- * sorted by (ea, eb)) or its lower bound, and whether it exists.  feat: n x 8
+ * sorted by (ea, eb)) or, for a pair not in `old`, the current gap from the
+ * exact closest point, and whether the previous one exists.  feat: n x 8
  * float; hist[i] = 1 if the pair is in `old` with contact history (status,
  * p_n, k_pen or z_t set), such pairs are never pruned. */
 xk_status xk_prune_features(const xk_mesh* m, const double* u, const int32_t* cands, int64_t n,

@@ -124,7 +124,8 @@ def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
     3: min(|layer_a - layer_b|, 3) / 3        layer distance (0 without layers)
     4: 1 if either layer is 0 (the core)
     5: previous-step gap / (r_a + r_b), clipped to [-2, 8]; without one, the
-       lower bound (|m_a - m_b| - (|d_a| + |d_b|)/2 - r_a - r_b) / (r_a + r_b)
+       current gap (segment distance - r_a - r_b) / (r_a + r_b) from the exact
+       closest point (``oracle.contact.closest_point``)
     6: 1 if the previous-step gap exists
     7: 0
     """
@@ -140,7 +141,9 @@ def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
     have_layer = (la >= 0) & (lb >= 0)
     X[:, 3] = np.where(have_layer, np.minimum(np.abs(la - lb), 3) / 3.0, 0.0)
     X[:, 4] = np.where(have_layer & ((la == 0) | (lb == 0)), 1.0, 0.0)
-    lower = (sep - 0.5 * (la_n + lb_n) - rs) / rs
-    X[:, 5] = np.clip(np.where(has_prev, prev_gap / rs, lower), -2.0, 8.0)
+    from oracle.contact import closest_point
+
+    cur = (closest_point(xa0, xa1, xb0, xb1)[2] - rs) / rs if xa0.shape[0] else np.zeros(0)
+    X[:, 5] = np.clip(np.where(has_prev, prev_gap / rs, cur), -2.0, 8.0)
     X[:, 6] = has_prev.astype(np.float64)
     return X.astype(np.float32)

@@ -2,12 +2,16 @@
 //
 // The reference bins AABBs into a hash grid (xkep_cae/contact/_broadphase.py:52-87)
 // and keeps the pairs whose closed AABBs overlap (:93-96); its output is the
-// set of all overlapping pairs, whatever the cell size.  Here the segments are
-// binned by the cell of their lower AABB corner on a grid whose cell is at
-// least the largest AABB extent, sorted by the Morton code of that cell, and a
-// warp per segment sweeps the 27 neighbouring cells, testing the exact double
-// AABBs and compacting hits with ballot/popc.  Filters follow
-// DetectCandidatesProcess (_manager_process.py:200-217,260-286).
+// set of all overlapping pairs, whatever the cell size.  Here, as there, every
+// segment is entered in each cell its box covers, on a grid of 1.5 times the
+// mean box extent (the reference's default cell, _broadphase.py:55-60), with
+// a counting sort by cell.  A warp per segment walks the entries of its own
+// cells and keeps a pair only in its home cell, the cell of the lower corner
+// of the two boxes' intersection: both boxes cover that cell whenever they
+// overlap, so each pair is found once.  Candidates are screened on float boxes
+// rounded outward, tested on the exact double AABBs, filtered, and compacted
+// with ballot/popc.  Filters follow DetectCandidatesProcess
+// (_manager_process.py:200-217,260-286).
 #include <cstdio>
 
 #include "xk_common.cuh"
@@ -32,20 +36,10 @@ XK_D double dec_min(unsigned long long k) {
   return __longlong_as_double((long long)b);
 }
 
-XK_D unsigned long long spread21(unsigned long long v) {
-  v &= 0x1fffffull;
-  v = (v | (v << 32)) & 0x1f00000000ffffull;
-  v = (v | (v << 16)) & 0x1f0000ff0000ffull;
-  v = (v | (v << 8)) & 0x100f00f00f00f00full;
-  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
-  v = (v | (v << 2)) & 0x1249249249249249ull;
-  return v;
-}
-
 // boxf: the same boxes in float, rounded outward (lower corner down, upper corner up), as two float4
 // per segment (32 bytes): a conservative screen for the sweep, which then tests the FP64 boxes.
 __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, double* __restrict__ box,
-                       float4* __restrict__ boxf, unsigned long long* __restrict__ ext) {
+                       float4* __restrict__ boxf, unsigned long long* __restrict__ ext, double* __restrict__ ext_sum) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   const long long ne = m.n_elems;
   unsigned long long lmin[3] = {~0ull, ~0ull, ~0ull}, lmax[3] = {0ull, 0ull, 0ull}, lext = 0ull;
@@ -70,6 +64,7 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
     boxf[2LL * e] = make_float4(lf[0], lf[1], lf[2], 0.f);
     boxf[2LL * e + 1] = make_float4(hf[0], hf[1], hf[2], 0.f);
     lext = (unsigned long long)__double_as_longlong(mx);
+    atomicAdd(ext_sum, mx);  // the cell size only sets the work, not the result: any order will do
   }
   for (int o = 16; o > 0; o >>= 1) {
     for (int c = 0; c < 3; ++c) {
@@ -90,8 +85,9 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
   }
 }
 
-__global__ void k_grid(const unsigned long long* __restrict__ ext, long long cap_cells, Grid* g) {
-  double mx = __longlong_as_double((long long)ext[0]);
+__global__ void k_grid(const unsigned long long* __restrict__ ext, const double* __restrict__ ext_sum, long long ne,
+                       long long cap_cells, Grid* g) {
+  double mx = 1.5 * (*ext_sum / (double)ne);
   double lo[3], hi[3];
   for (int c = 0; c < 3; ++c) {
     lo[c] = dec_min(ext[1 + c]);
@@ -131,29 +127,51 @@ XK_D void cell_of(const Grid& g, double lo0, double lo1, double lo2, int* c) {
   }
 }
 
-__global__ void k_keys(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
-                       unsigned long long* __restrict__ keys, int32_t* __restrict__ segs) {
-  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
-  const Grid g = *gp;
-  int c[3];
-  cell_of(g, box[e], box[ne + e], box[2 * ne + e], c);
-  keys[e] = spread21(c[0]) | (spread21(c[1]) << 1) | (spread21(c[2]) << 2);
-  segs[e] = (int32_t)e;
+XK_D void cell_range(const Grid& g, const double* box, long long ne, int e, int* c0, int* c1) {
+  cell_of(g, box[e], box[ne + e], box[2 * ne + e], c0);
+  cell_of(g, box[3 * ne + e], box[4 * ne + e], box[5 * ne + e], c1);
 }
 
-__global__ void k_cells(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
-                        const unsigned long long* __restrict__ keys, const int32_t* __restrict__ segs,
-                        int32_t* __restrict__ cstart, int32_t* __restrict__ cend) {
-  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= ne) return;
+// entries of segment e: one per cell its box covers
+__global__ void k_entry_count(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
+                              int32_t* __restrict__ cnt) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
   const Grid g = *gp;
-  int e = segs[k];
-  int c[3];
-  cell_of(g, box[e], box[ne + e], box[2 * ne + e], c);
-  long long lin = ((long long)c[2] * g.dims[1] + c[1]) * g.dims[0] + c[0];
-  if (k == 0 || keys[k] != keys[k - 1]) cstart[lin] = (int32_t)k;
-  if (k == ne - 1 || keys[k] != keys[k + 1]) cend[lin] = (int32_t)(k + 1);
+  int c0[3], c1[3];
+  cell_range(g, box, ne, (int)e, c0, c1);
+  cnt[e] = (c1[0] - c0[0] + 1) * (c1[1] - c0[1] + 1) * (c1[2] - c0[2] + 1);
+}
+
+// the cell of every entry, and the per-cell entry counts
+__global__ void k_entry_fill(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
+                             const int32_t* __restrict__ eoff, int32_t* __restrict__ ecell,
+                             int32_t* __restrict__ ccnt) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const Grid g = *gp;
+  int c0[3], c1[3];
+  cell_range(g, box, ne, (int)e, c0, c1);
+  long long k = eoff[e];
+  for (int z = c0[2]; z <= c1[2]; ++z)
+    for (int y = c0[1]; y <= c1[1]; ++y)
+      for (int x = c0[0]; x <= c1[0]; ++x) {
+        const int lin = (int)(((long long)z * g.dims[1] + y) * g.dims[0] + x);
+        ecell[k++] = lin;
+        atomicAdd(&ccnt[lin], 1);
+      }
+}
+
+// counting sort of the entries by cell (order within a cell is not used)
+__global__ void k_entry_scatter(const int32_t* __restrict__ eoff, long long ne, const int32_t* __restrict__ ecell,
+                                const int32_t* __restrict__ cstart, int32_t* __restrict__ cfill,
+                                int32_t* __restrict__ segs) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  for (int k = eoff[e]; k < eoff[e + 1]; ++k) {
+    const int c = ecell[k];
+    segs[cstart[c] + atomicAdd(&cfill[c], 1)] = (int32_t)e;
+  }
 }
 
 XK_D bool overlap(const double* box, long long ne, int i, int j) {
@@ -185,23 +203,24 @@ XK_D bool midpoint_keep(const xk_mesh& m, const double* __restrict__ u, int i, i
   return mp <= xadd(xadd(m.radii[i], m.radii[j]), extra);
 }
 
-// A warp per segment i (taken in Morton order of its cell): the 27 neighbouring cells' entries are
-// laid out as one list (lane l < 27 reads cell l's range, a warp scan gives the offsets) and the
-// warp walks it 32 entries at a time, each lane finding its entry's cell by a binary search over the
-// offsets held in the lanes.  A candidate j > i is screened on the outward-rounded float boxes
-// (which can never reject an FP64 overlap), tested on the FP64 boxes, then the shared-node and
-// same-layer filters apply; hits are compacted with ballot/popc.
+// A warp per segment i.  The cells its box covers are taken 32 at a time: lane l reads cell l's
+// entry range, a warp scan lays the ranges out as one list, and the warp walks it 32 entries at a
+// time, each lane finding its entry's cell by a binary search over the offsets held in the lanes.
+// An entry j > i is screened on the outward-rounded float boxes (which can never reject an FP64
+// overlap), tested on the FP64 boxes and kept only in its home cell (the cell of max(lo_i, lo_j),
+// which both boxes cover when they overlap: each pair once); then the shared-node and same-layer
+// filters apply and hits are compacted with ballot/popc.
 // MODE 0: kept count per segment (cnt[i]), the sum of r_i + r_j over its kept candidates (each lane
-//         sums its own entries in round order, then a fixed butterfly: rsum[i], for the prescreen
+//         sums its own entries in walk order, then a fixed butterfly: rsum[i], for the prescreen
 //         margin), and the raw overlap count.
 // MODE 1: the kept candidates of segment i sorted by j at off[i] (out), and their prescreen flags.
 template <int MODE>
 __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restrict__ u,
                                                 const double* __restrict__ box, const float4* __restrict__ boxf,
                                                 const Grid* __restrict__ gp, const int32_t* __restrict__ segs,
-                                                const int32_t* __restrict__ cstart, const int32_t* __restrict__ cend,
-                                                int excl_shared, int excl_layer, int32_t* __restrict__ cnt,
-                                                double* __restrict__ rsum, unsigned long long* __restrict__ raw_total,
+                                                const int32_t* __restrict__ cstart, int excl_shared, int excl_layer,
+                                                int32_t* __restrict__ cnt, double* __restrict__ rsum,
+                                                unsigned long long* __restrict__ raw_total,
                                                 const int32_t* __restrict__ off, const double* __restrict__ extra,
                                                 int32_t* __restrict__ tmp, int32_t* __restrict__ out,
                                                 int32_t* __restrict__ keep) {
@@ -210,73 +229,85 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
   const int lane = threadIdx.x & 31;
   if (w >= ne) return;
   const Grid g = *gp;
-  const int i = segs[w];
-  int c[3];
-  cell_of(g, box[i], box[ne + i], box[2 * ne + i], c);
-  // this lane's cell of the 27 and its entry range
-  int s0 = 0, n0 = 0;
-  if (lane < 27) {
-    const int x = c[0] + lane % 3 - 1, y = c[1] + (lane / 3) % 3 - 1, z = c[2] + lane / 9 - 1;
-    if (x >= 0 && x < g.dims[0] && y >= 0 && y < g.dims[1] && z >= 0 && z < g.dims[2]) {
-      const long long lin = ((long long)z * g.dims[1] + y) * g.dims[0] + x;
-      s0 = cstart[lin];
-      n0 = cend[lin] - s0;
-    }
-  }
-  int incl = n0;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
-  }
-  const int pre = incl - n0;
-  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const int i = (int)w;
+  int c0[3], c1[3];
+  cell_range(g, box, ne, i, c0, c1);
+  const int sx = c1[0] - c0[0] + 1, sy = c1[1] - c0[1] + 1, sz = c1[2] - c0[2] + 1;
+  const int ncell = sx * sy * sz;
   const int ia = m.conn[2 * i], ib = m.conn[2 * i + 1];
   const int li = (excl_layer && m.layer) ? m.layer[i] : -1;
   const float4 il = boxf[2LL * i], ih = boxf[2LL * i + 1];
+  const double ilo[3] = {box[i], box[ne + i], box[2 * ne + i]};
   const double ri = m.radii[i];
   int n_raw = 0, n_keep = 0;
   double rs = 0.0;
   const long long base = MODE == 1 ? (long long)off[i] : 0;
-  for (int f0 = 0; f0 < total; f0 += 32) {
-    const int f = f0 + lane;
-    // the last cell q with pre_q <= f (cells of no entries share their successor's offset)
-    int q = 0;
+  for (int cb = 0; cb < ncell; cb += 32) {
+    // this lane's cell of the batch and its entry range
+    int s0 = 0, n0 = 0, lin = -1;
+    const int q0 = cb + lane;
+    if (q0 < ncell) {
+      const int x = c0[0] + q0 % sx, y = c0[1] + (q0 / sx) % sy, z = c0[2] + q0 / (sx * sy);
+      lin = (int)(((long long)z * g.dims[1] + y) * g.dims[0] + x);
+      s0 = cstart[lin];
+      n0 = cstart[lin + 1] - s0;
+    }
+    int incl = n0;
 #pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
-      const int cand = q + step;
-      const int pc = __shfl_sync(0xffffffffu, pre, cand < 27 ? cand : 26);
-      if (cand < 27 && pc <= f) q = cand;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
     }
-    const int sq = __shfl_sync(0xffffffffu, s0, q);
-    const int pq = __shfl_sync(0xffffffffu, pre, q);
-    bool hit = false, kept = false;
-    int j = -1;
-    if (f < total) {
-      j = segs[sq + (f - pq)];
-      bool near = j > i;
-      if (near) {
-        const float4 jl = __ldg(boxf + 2LL * j), jh = __ldg(boxf + 2LL * j + 1);
-        near = il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z;
+    const int pre = incl - n0;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int nq = (ncell - cb) < 32 ? (ncell - cb) : 32;
+    for (int f0 = 0; f0 < total; f0 += 32) {
+      const int f = f0 + lane;
+      // the last cell q of the batch with pre_q <= f (cells without entries share their successor's offset)
+      int q = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = q + step;
+        const int pc = __shfl_sync(0xffffffffu, pre, cand < nq ? cand : nq - 1);
+        if (cand < nq && pc <= f) q = cand;
       }
-      if (near && overlap(box, ne, i, j)) {
-        hit = true;
-        kept = true;
-        if (excl_shared) {
-          const int ja = m.conn[2 * j], jb = m.conn[2 * j + 1];
-          if (ia == ja || ia == jb || ib == ja || ib == jb) kept = false;
+      const int sq = __shfl_sync(0xffffffffu, s0, q);
+      const int pq = __shfl_sync(0xffffffffu, pre, q);
+      const int lq = __shfl_sync(0xffffffffu, lin, q);
+      bool hit = false, kept = false;
+      int j = -1;
+      if (f < total) {
+        j = segs[sq + (f - pq)];
+        bool near = j > i;
+        if (near) {
+          const float4 jl = __ldg(boxf + 2LL * j), jh = __ldg(boxf + 2LL * j + 1);
+          near = il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z;
         }
-        if (kept && li >= 0 && m.layer[j] == li) kept = false;
+        if (near && overlap(box, ne, i, j)) {
+          int hc[3];
+          const double jlo0 = box[j], jlo1 = box[ne + j], jlo2 = box[2 * ne + j];
+          cell_of(g, ilo[0] > jlo0 ? ilo[0] : jlo0, ilo[1] > jlo1 ? ilo[1] : jlo1, ilo[2] > jlo2 ? ilo[2] : jlo2, hc);
+          const long long home = ((long long)hc[2] * g.dims[1] + hc[1]) * g.dims[0] + hc[0];
+          if (home == lq) {
+            hit = true;
+            kept = true;
+            if (excl_shared) {
+              const int ja = m.conn[2 * j], jb = m.conn[2 * j + 1];
+              if (ia == ja || ia == jb || ib == ja || ib == jb) kept = false;
+            }
+            if (kept && li >= 0 && m.layer[j] == li) kept = false;
+          }
+        }
       }
+      const unsigned bal = __ballot_sync(0xffffffffu, kept);
+      n_raw += __popc(__ballot_sync(0xffffffffu, hit));
+      if (MODE == 0) {
+        if (kept) rs = xadd(rs, xadd(ri, m.radii[j]));  // this lane's entries, in walk order
+      } else if (kept) {
+        tmp[base + n_keep + __popc(bal & ((1u << lane) - 1u))] = j;
+      }
+      n_keep += __popc(bal);
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, kept);
-    n_raw += __popc(__ballot_sync(0xffffffffu, hit));
-    if (MODE == 0) {
-      if (kept) rs = xadd(rs, xadd(ri, m.radii[j]));  // this lane's entries, in round order
-    } else if (kept) {
-      tmp[base + n_keep + __popc(bal & ((1u << lane) - 1u))] = j;
-    }
-    n_keep += __popc(bal);
   }
   if (MODE == 0) {
 #pragma unroll
@@ -494,32 +525,45 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   Grid* grid;
   XK_TRY(S.get(&box, 6 * ne));
   XK_TRY(S.get(&boxf, 2 * ne));
-  XK_TRY(S.get(&ext, 8));
+  XK_TRY(S.get(&ext, 9));
   XK_TRY(S.get(&grid, 1));
-  unsigned long long init[8] = {0ull, ~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull};
+  double* ext_sum = reinterpret_cast<double*>(ext + 8);
+  unsigned long long init[9] = {0ull, ~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull, 0ull};  // word 8: +0.0
   XK_CUDA(cudaMemcpyAsync(ext, init, sizeof(init), cudaMemcpyHostToDevice, st));
-  k_aabb<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, u, bp->margin, box, boxf, ext);
+  k_aabb<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, u, bp->margin, box, boxf, ext, ext_sum);
   const long long cap_cells = ne * 8 > 4096 ? ne * 8 : 4096;
-  k_grid<<<1, 1, 0, st>>>(ext, cap_cells, grid);
+  k_grid<<<1, 1, 0, st>>>(ext, ext_sum, ne, cap_cells, grid);
   XK_CHECK_LAUNCH();
   Grid hg;
   XK_CUDA(cudaMemcpyAsync(&hg, grid, sizeof(Grid), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
   const long long ncell = (long long)hg.dims[0] * hg.dims[1] * hg.dims[2];
-  unsigned long long* keys;
-  int32_t *segs, *cstart, *cend, *cnt, *off;
-  XK_TRY(S.get(&keys, ne));
-  XK_TRY(S.get(&segs, ne));
-  XK_TRY(S.get(&cstart, ncell));
-  XK_TRY(S.get(&cend, ncell));
+  int32_t *segs, *cstart, *cfill, *cnt, *off, *ecnt, *eoff, *ecell;
+  int64_t* etot;
+  XK_TRY(S.get(&ecnt, ne + 1));
+  XK_TRY(S.get(&eoff, ne + 1));
+  XK_TRY(S.get(&etot, 1));
+  XK_TRY(S.get(&cstart, ncell + 1));
+  XK_TRY(S.get(&cfill, ncell + 1));
   XK_TRY(S.get(&cnt, ne + 1));
   XK_TRY(S.get(&off, ne + 1));
-  k_keys<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, keys, segs);
+  // entries: one per covered cell of every box, sorted by cell
+  XK_CUDA(cudaMemsetAsync(ecnt + ne, 0, sizeof(int32_t), st));
+  k_entry_count<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, ecnt);
   XK_CHECK_LAUNCH();
-  XK_TRY(xk_radix_sort_u64((uint64_t*)keys, segs, ne, hg.bits, st));
-  XK_CUDA(cudaMemsetAsync(cstart, 0, sizeof(int32_t) * ncell, st));
-  XK_CUDA(cudaMemsetAsync(cend, 0, sizeof(int32_t) * ncell, st));
-  k_cells<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, keys, segs, cstart, cend);
+  XK_TRY(xk_exclusive_scan_i32(ecnt, eoff, ne + 1, etot, st));
+  int64_t h_e = 0;
+  XK_CUDA(cudaMemcpyAsync(&h_e, etot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaStreamSynchronize(st));
+  if (h_e > 0x7fffffffLL) return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: more than 2^31 grid entries");
+  XK_TRY(S.get(&ecell, h_e));
+  XK_TRY(S.get(&segs, h_e));
+  XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (ncell + 1), st));
+  k_entry_fill<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, eoff, ecell, cfill);
+  XK_CHECK_LAUNCH();
+  XK_TRY(xk_exclusive_scan_i32(cfill, cstart, ncell + 1, nullptr, st));
+  XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (ncell + 1), st));
+  k_entry_scatter<<<xk_blocks(ne, 256), 256, 0, st>>>(eoff, ne, ecell, cstart, cfill, segs);
   XK_CHECK_LAUNCH();
   unsigned long long* raw_dev = ext + 7;
   double* rsum;
@@ -528,7 +572,7 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   XK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (ne + 1), st));
   const int sweep_blocks = xk_blocks(ne * 32, BP_T);
   const int excl_layer = (bp->exclude_same_layer && m->layer) ? 1 : 0;
-  k_sweep<0><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, cend, bp->exclude_shared,
+  k_sweep<0><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, bp->exclude_shared,
                                              excl_layer, cnt, rsum, raw_dev, nullptr, nullptr, nullptr, nullptr,
                                              nullptr);
   XK_CHECK_LAUNCH();
@@ -558,7 +602,7 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   if (!bp->midpoint_prescreening) {
     *n_out = n1;
     if (n1 > cap) return xk_set_error(XK_ERR_CAPACITY, "xk_broadphase: output capacity too small");
-    k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, cend, bp->exclude_shared,
+    k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, bp->exclude_shared,
                                                excl_layer, cnt, rsum, raw_dev, off, nullptr, tmp, out_pairs, nullptr);
     XK_CHECK_LAUNCH();
     XK_CUDA(cudaStreamSynchronize(st));
@@ -567,7 +611,7 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   XK_TRY(S.get(&pairs1, 2 * n1));
   XK_TRY(S.get(&keep, n1));
   XK_TRY(S.get(&pos, n1));
-  k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, cend, bp->exclude_shared,
+  k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, bp->exclude_shared,
                                              excl_layer, cnt, rsum, raw_dev, off, extra, tmp, pairs1, keep);
   XK_CHECK_LAUNCH();
   XK_TRY(xk_exclusive_scan_i32(keep, pos, n1, tot + 1, st));

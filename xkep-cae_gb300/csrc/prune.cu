@@ -14,6 +14,7 @@
 #include <cuda_bf16.h>
 
 #include "xk_common.cuh"
+#include "segment.cuh"
 
 namespace {
 
@@ -89,8 +90,10 @@ __global__ void k_features(xk_mesh m, const double* __restrict__ u, const int32_
   double g5;
   if (at >= 0) {
     g5 = xdiv(old.gap[at], rs);
-  } else {
-    g5 = xdiv(xsub(xsub(sep, xmul(0.5, xadd(lna, lnb))), rs), rs);
+  } else {  // no previous gap: the current one, from the exact closest point (geometry/_compute.py:55-151)
+    double s_, t_, dist, nrm[3], diff[3];
+    closest_exact(x[0], x[1], x[2], x[3], s_, t_, dist, nrm, diff);
+    g5 = xdiv(xsub(dist, rs), rs);
   }
   g5 = g5 < -2.0 ? -2.0 : (g5 > 8.0 ? 8.0 : g5);
   f[5] = (float)g5;
