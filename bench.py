@@ -552,12 +552,13 @@ def c2_section(args, dev) -> dict:
 
 
 def c3_section(args, dev, n_steps: int = 20) -> dict:
-    """The 91-wire strand: Generalized-alpha (rho_inf 0.9) ramp to curvature 1/(50 D) in 1 ms, then
-    oscillation steps of dt = 1e-4 s with the end curvature following cos(2 pi k / 20); mu = 0.1,
-    graph-replayed assembly, FP64 and mixed."""
+    """The 91-wire strand bent quasi-statically to curvature 1/(50 D), then released: 20 Generalized-alpha
+    steps (rho_inf 0.9, dt = 1e-4 s) of its free oscillation from rest; mu = 0.1, k_pen 1e3 EA/L,
+    graph-replayed assembly, device block solve; FP64 and mixed over the same steps."""
     import torch
 
     from xkgpu import runs
+    from xkgpu import solver as S
     from xkgpu import workloads as W
 
     out = {}
@@ -565,25 +566,34 @@ def c3_section(args, dev, n_steps: int = 20) -> dict:
     for prec in ("fp64", "mixed"):
         w = W.strand_workload("strand91", 91, 2.0, 40.0, 4, 32, gap_frac=0.0, seed=0)
         D = 2.0 * max(x.lay_radius for x in w.strand.wires) + w.meta["d"]
-        r = runs.run_bend_oscillation(w, prec, kappa=1.0 / (50.0 * D), n_steps=n_steps)
+        cfg = dict(dt_min_fraction=1e-3, max_nr_attempts=100, use_line_search=False)
+        r = runs.run_bend_oscillation(w, prec, kappa=1.0 / (50.0 * D), n_steps=n_steps,
+                                      bend_settings=S.SolverSettings(dt_max_fraction=0.1, **cfg),
+                                      step_settings=S.SolverSettings(**cfg))
         n_it = r["counts"]["assemble"]
-        out[prec] = {"converged": r["converged"], "attempts_per_step": [sum(a) for a in r["attempts"]],
+        steps = r["attempts"][1:]
+        out[prec] = {"converged": r["converged"], "bend": r.get("bend"), "bend_s": r.get("bend_s"),
+                     "newton_attempts_per_step": [sum(a) for a in steps], "step_ms": [1e3 * t for t in r["step_s"]],
                      "wall_s": r["wall_s"], "solve_s": r["solve_s"], "solves": r["solves"],
-                     "newton_iterations": n_it, "ms_per_newton_iteration": 1e3 * r["wall_s"] / max(n_it, 1),
+                     "assemblies": n_it, "ms_per_newton_iteration": 1e3 * r["wall_s"] / max(n_it, 1),
                      "ms_per_iteration_without_solve": 1e3 * (r["wall_s"] - r["solve_s"]) / max(n_it, 1),
                      "solver": r.get("lin")}
         us[prec] = r["u"]
         torch.cuda.empty_cache()
     n = min(len(us["fp64"]), len(us["mixed"]))
-    out["u_rel_diff_per_step"] = [float(np.abs(us["mixed"][k] - us["fp64"][k]).max() / np.abs(us["fp64"][k]).max())
-                                  for k in range(n)]
+    out["workload"] = (f"strand91 (91 wires, d 2 mm, pitch 40 mm, 4 pitches, 32 el/pitch, gap at the minimum safe "
+                       f"lay gap), curvature 1/(50 D), D = {D:.2f} mm; line search off, at most 100 attempts")
+    out["u_rel_diff_mixed_vs_fp64"] = [float(np.abs(us["mixed"][k] - us["fp64"][k]).max()
+                                             / np.abs(us["fp64"][k]).max()) for k in range(n)]
     return out
 
 
 def batch_section(args, dev):
-    """The 256-strand batch (one friction coefficient per strand) assembled by the same launches."""
+    """The 256-strand batch (one friction coefficient per strand) assembled by the same launches, with
+    the tangent schedule and then the launch shapes chosen by the engine's autotuner."""
     import torch
 
+    from xkgpu import _lib as L
     from xkgpu import workloads as W
     from xkgpu.engine import AssemblyEngine
 
@@ -601,11 +611,22 @@ def batch_section(args, dev):
         eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, layer=st.elem_layer, precision=prec,
                              k_pen=w.k_pen, mu=w.mu, device=dev)
         stats = eng.detect(u0)
-        eng.capture(u1, u0)
+        eng.capture(u1, u0)  # the tangent schedule is tuned here; the launch shapes keep their defaults
         ms = _time_replay(eng, args.steps, args.warmup)
         units = st.n_elems + stats["pairs"]
-        out[prec] = {"ms_per_step": ms, "evals_per_s": units / ms * 1e3, "pairs": stats["pairs"],
-                     "members": stats["members"]}
+        names = {L.XK_GATHER_LANES: "lanes", L.XK_GATHER_CHUNKS: "chunks", L.XK_GATHER_SIDES: "sides"}
+        res = {"ms_per_step": ms, "evals_per_s": units / ms * 1e3, "pairs": stats["pairs"],
+               "members": stats["members"], "schedule": names.get(eng.gather_variant, "default"),
+               "schedule_ms": {names[v]: round(t, 4) for v, t in getattr(eng, "tune_times", {}).items()}}
+        # the autotuner over the launch shapes as well: the pair kernels' CTA size and the block gather's
+        # persistent CTAs per SM, each timed on this workload; the step with the chosen shapes
+        eng.tune(shapes=True)
+        eng.capture(u1, u0)
+        ms_t = _time_replay(eng, args.steps, args.warmup)
+        res["launch_shapes"] = eng.tune_shapes
+        res["ms_per_step_tuned_shapes"] = ms_t
+        res["gain_tuned_shapes_vs_default"] = ms / ms_t
+        out[prec] = res
         del eng
         torch.cuda.empty_cache()
     out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]

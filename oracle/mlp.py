@@ -115,6 +115,37 @@ def adam_step(theta, grad, m, v, step: int, lr: float, b1=0.9, b2=0.999, eps=1e-
     return (theta - lr * mh / (np.sqrt(vh) + eps)).astype(np.float32), m.astype(np.float32), v.astype(np.float32)
 
 
+def current_gap_f(xa0, xa1, xb0, xb1, rs):
+    """(segment distance - rs) / rs in float32: differences in double, the clamped closest point of
+    ``_closest_point_segments_batch`` (``geometry/_compute.py:55-151``) in float32 with every operation
+    rounded on its own; near-parallel pairs (det <= 1e-3 ac) take s = 0."""
+    f = np.float32
+    A, B, Wv = (xa1 - xa0).astype(f), (xb1 - xb0).astype(f), (xa0 - xb0).astype(f)
+
+    def dot(p, q):
+        return (p[:, 0] * q[:, 0] + p[:, 1] * q[:, 1]) + p[:, 2] * q[:, 2]
+
+    a, b, c, d, e = dot(A, A), dot(A, B), dot(B, B), dot(A, Wv), dot(B, Wv)
+    ac = a * c
+    det = ac - b * b
+    par = ~(det > f(1e-3) * ac)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        sdet = np.where(par, f(1.0), det)
+        su, tu = (b * e - c * d) / sdet, (a * e - b * d) / sdet
+        cl = lambda v: np.clip(v, f(0.0), f(1.0))  # noqa: E731
+        csafe, asafe = np.where(c > 0, c, f(1.0)), np.where(a > 0, a, f(1.0))
+        s = np.where(par, f(0.0), cl(su))
+        t = np.where(par, np.where(c > 0, cl(e / csafe), f(0.0)), cl(tu))
+        s_cl = ~par & ((su < 0) | (su > 1))
+        t = np.where(s_cl, np.where(c > 0, cl((b * s + e) / csafe), f(0.0)), t)
+        t_cl = ~par & ((tu < 0) | (tu > 1))
+        s = np.where(t_cl, np.where(a > 0, cl((b * t - d) / asafe), f(0.0)), s)
+        t = np.where(t_cl, np.where(c > 0, cl((b * s + e) / csafe), f(0.0)), t)
+    D = (Wv + s[:, None] * A) - t[:, None] * B
+    rsf = np.asarray(rs, dtype=np.float64).astype(f)
+    return ((np.sqrt(dot(D, D)) - rsf) / rsf).astype(np.float64)
+
+
 def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
     """Per-candidate inputs (n x F), float32.
 
@@ -124,8 +155,8 @@ def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
     3: min(|layer_a - layer_b|, 3) / 3        layer distance (0 without layers)
     4: 1 if either layer is 0 (the core)
     5: previous-step gap / (r_a + r_b), clipped to [-2, 8]; without one, the
-       current gap (segment distance - r_a - r_b) / (r_a + r_b) from the exact
-       closest point (``oracle.contact.closest_point``)
+       current gap (segment distance - r_a - r_b) / (r_a + r_b) in float
+       (``current_gap_f``)
     6: 1 if the previous-step gap exists
     7: 0
     """
@@ -141,9 +172,6 @@ def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
     have_layer = (la >= 0) & (lb >= 0)
     X[:, 3] = np.where(have_layer, np.minimum(np.abs(la - lb), 3) / 3.0, 0.0)
     X[:, 4] = np.where(have_layer & ((la == 0) | (lb == 0)), 1.0, 0.0)
-    from oracle.contact import closest_point
-
-    cur = (closest_point(xa0, xa1, xb0, xb1)[2] - rs) / rs if xa0.shape[0] else np.zeros(0)
-    X[:, 5] = np.clip(np.where(has_prev, prev_gap / rs, cur), -2.0, 8.0)
+    X[:, 5] = np.clip(np.where(has_prev, prev_gap / rs, current_gap_f(xa0, xa1, xb0, xb1, rs)), -2.0, 8.0)
     X[:, 6] = has_prev.astype(np.float64)
     return X.astype(np.float32)

@@ -2,16 +2,15 @@
 //
 // The reference bins AABBs into a hash grid (xkep_cae/contact/_broadphase.py:52-87)
 // and keeps the pairs whose closed AABBs overlap (:93-96); its output is the
-// set of all overlapping pairs, whatever the cell size.  Here, as there, every
-// segment is entered in each cell its box covers, on a grid of 1.5 times the
-// mean box extent (the reference's default cell, _broadphase.py:55-60), with
-// a counting sort by cell.  A warp per segment walks the entries of its own
-// cells and keeps a pair only in its home cell, the cell of the lower corner
-// of the two boxes' intersection: both boxes cover that cell whenever they
-// overlap, so each pair is found once.  Candidates are screened on float boxes
-// rounded outward, tested on the exact double AABBs, filtered, and compacted
-// with ballot/popc.  Filters follow DetectCandidatesProcess
-// (_manager_process.py:200-217,260-286).
+// set of all overlapping pairs, whatever the cell size.  Here every segment is
+// binned once, by the cell of its box's lower corner, on a grid of the mean box
+// extent (counting sort by cell).  A box j can overlap box i only if its lower
+// corner lies in [lo_i - E, hi_i] per axis, E the largest extent of any box on
+// that axis, so a warp per segment i walks the cells of that range (32 cells a
+// batch) and tests every entry j > i: screened on float boxes rounded outward,
+// tested on the exact double AABBs, filtered, compacted with ballot/popc.  Each
+// pair is found once, from its lower-numbered segment.  Filters follow
+// DetectCandidatesProcess (_manager_process.py:200-217,260-286).
 #include <cstdio>
 
 #include "xk_common.cuh"
@@ -24,7 +23,8 @@ struct Grid {
   double origin[3];
   double cell;
   int dims[3];
-  int bits;
+  int pad;
+  double emax[3];  // largest box extent on each axis
 };
 
 XK_D unsigned long long enc_min(double x) {  // order-preserving map of doubles to u64
@@ -42,7 +42,8 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
                        float4* __restrict__ boxf, unsigned long long* __restrict__ ext, double* __restrict__ ext_sum) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   const long long ne = m.n_elems;
-  unsigned long long lmin[3] = {~0ull, ~0ull, ~0ull}, lmax[3] = {0ull, 0ull, 0ull}, lext = 0ull;
+  unsigned long long lmin[3] = {~0ull, ~0ull, ~0ull}, lmax[3] = {0ull, 0ull, 0ull}, lax[3] = {0ull, 0ull, 0ull};
+  double msum = 0.0;
   if (e < m.n_elems) {
     int a = m.conn[2 * e], b = m.conn[2 * e + 1];
     const double ex = xadd(m.radii[e], margin);
@@ -59,12 +60,13 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
       hf[c] = __double2float_ru(hi);
       lmin[c] = enc_min(lo);
       lmax[c] = enc_min(hi);
-      mx = fmax(mx, hi - lo);
+      const double extc = hi - lo;  // >= 0: the bit patterns order as the values
+      lax[c] = (unsigned long long)__double_as_longlong(extc);
+      mx = fmax(mx, extc);
     }
     boxf[2LL * e] = make_float4(lf[0], lf[1], lf[2], 0.f);
     boxf[2LL * e + 1] = make_float4(hf[0], hf[1], hf[2], 0.f);
-    lext = (unsigned long long)__double_as_longlong(mx);
-    atomicAdd(ext_sum, mx);  // the cell size only sets the work, not the result: any order will do
+    msum = mx;
   }
   for (int o = 16; o > 0; o >>= 1) {
     for (int c = 0; c < 3; ++c) {
@@ -72,22 +74,24 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
       lmin[c] = y < lmin[c] ? y : lmin[c];
       y = __shfl_down_sync(0xffffffffu, lmax[c], o);
       lmax[c] = y > lmax[c] ? y : lmax[c];
+      y = __shfl_down_sync(0xffffffffu, lax[c], o);
+      lax[c] = y > lax[c] ? y : lax[c];
     }
-    unsigned long long y = __shfl_down_sync(0xffffffffu, lext, o);
-    lext = y > lext ? y : lext;
+    msum += __shfl_down_sync(0xffffffffu, msum, o);
   }
   if ((threadIdx.x & 31) == 0) {
     for (int c = 0; c < 3; ++c) {
       atomicMin(&ext[1 + c], lmin[c]);
       atomicMax(&ext[4 + c], lmax[c]);
+      atomicMax(&ext[9 + c], lax[c]);
     }
-    atomicMax(&ext[0], lext);
+    atomicAdd(ext_sum, msum);  // the cell size only sets the work, not the result: any order will do
   }
 }
 
 __global__ void k_grid(const unsigned long long* __restrict__ ext, const double* __restrict__ ext_sum, long long ne,
                        long long cap_cells, Grid* g) {
-  double mx = 1.5 * (*ext_sum / (double)ne);
+  double mx = *ext_sum / (double)ne;
   double lo[3], hi[3];
   for (int c = 0; c < 3; ++c) {
     lo[c] = dec_min(ext[1 + c]);
@@ -107,15 +111,12 @@ __global__ void k_grid(const unsigned long long* __restrict__ ext, const double*
     if (tot <= cap_cells) break;
     cell *= 1.25;
   }
-  int md = max(dims[0], max(dims[1], dims[2]));
-  int b = 1;
-  while ((1 << b) < md) ++b;
   for (int c = 0; c < 3; ++c) {
     g->origin[c] = lo[c];
     g->dims[c] = dims[c];
   }
   g->cell = cell;
-  g->bits = 3 * b;
+  for (int c = 0; c < 3; ++c) g->emax[c] = __longlong_as_double((long long)ext[9 + c]);
 }
 
 XK_D void cell_of(const Grid& g, double lo0, double lo1, double lo2, int* c) {
@@ -127,51 +128,26 @@ XK_D void cell_of(const Grid& g, double lo0, double lo1, double lo2, int* c) {
   }
 }
 
-XK_D void cell_range(const Grid& g, const double* box, long long ne, int e, int* c0, int* c1) {
-  cell_of(g, box[e], box[ne + e], box[2 * ne + e], c0);
-  cell_of(g, box[3 * ne + e], box[4 * ne + e], box[5 * ne + e], c1);
-}
-
-// entries of segment e: one per cell its box covers
-__global__ void k_entry_count(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
-                              int32_t* __restrict__ cnt) {
+// per-cell counts of the segments binned by the cell of their box's lower corner
+__global__ void k_cell_count(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
+                             int32_t* __restrict__ ecell, int32_t* __restrict__ ccnt) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const Grid g = *gp;
-  int c0[3], c1[3];
-  cell_range(g, box, ne, (int)e, c0, c1);
-  cnt[e] = (c1[0] - c0[0] + 1) * (c1[1] - c0[1] + 1) * (c1[2] - c0[2] + 1);
+  int c[3];
+  cell_of(g, box[e], box[ne + e], box[2 * ne + e], c);
+  const int lin = (int)(((long long)c[2] * g.dims[1] + c[1]) * g.dims[0] + c[0]);
+  ecell[e] = lin;
+  atomicAdd(&ccnt[lin], 1);
 }
 
-// the cell of every entry, and the per-cell entry counts
-__global__ void k_entry_fill(const double* __restrict__ box, long long ne, const Grid* __restrict__ gp,
-                             const int32_t* __restrict__ eoff, int32_t* __restrict__ ecell,
-                             int32_t* __restrict__ ccnt) {
+// counting sort of the segments by cell (order within a cell is not used)
+__global__ void k_cell_scatter(long long ne, const int32_t* __restrict__ ecell, const int32_t* __restrict__ cstart,
+                               int32_t* __restrict__ cfill, int32_t* __restrict__ segs) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
-  const Grid g = *gp;
-  int c0[3], c1[3];
-  cell_range(g, box, ne, (int)e, c0, c1);
-  long long k = eoff[e];
-  for (int z = c0[2]; z <= c1[2]; ++z)
-    for (int y = c0[1]; y <= c1[1]; ++y)
-      for (int x = c0[0]; x <= c1[0]; ++x) {
-        const int lin = (int)(((long long)z * g.dims[1] + y) * g.dims[0] + x);
-        ecell[k++] = lin;
-        atomicAdd(&ccnt[lin], 1);
-      }
-}
-
-// counting sort of the entries by cell (order within a cell is not used)
-__global__ void k_entry_scatter(const int32_t* __restrict__ eoff, long long ne, const int32_t* __restrict__ ecell,
-                                const int32_t* __restrict__ cstart, int32_t* __restrict__ cfill,
-                                int32_t* __restrict__ segs) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
-  for (int k = eoff[e]; k < eoff[e + 1]; ++k) {
-    const int c = ecell[k];
-    segs[cstart[c] + atomicAdd(&cfill[c], 1)] = (int32_t)e;
-  }
+  const int c = ecell[e];
+  segs[cstart[c] + atomicAdd(&cfill[c], 1)] = (int32_t)e;
 }
 
 XK_D bool overlap(const double* box, long long ne, int i, int j) {
@@ -203,13 +179,13 @@ XK_D bool midpoint_keep(const xk_mesh& m, const double* __restrict__ u, int i, i
   return mp <= xadd(xadd(m.radii[i], m.radii[j]), extra);
 }
 
-// A warp per segment i.  The cells its box covers are taken 32 at a time: lane l reads cell l's
-// entry range, a warp scan lays the ranges out as one list, and the warp walks it 32 entries at a
-// time, each lane finding its entry's cell by a binary search over the offsets held in the lanes.
-// An entry j > i is screened on the outward-rounded float boxes (which can never reject an FP64
-// overlap), tested on the FP64 boxes and kept only in its home cell (the cell of max(lo_i, lo_j),
-// which both boxes cover when they overlap: each pair once); then the shared-node and same-layer
-// filters apply and hits are compacted with ballot/popc.
+// A warp per segment i.  The cells that can hold the lower corner of a box overlapping box i, those
+// of [lo_i - E, hi_i] (E per axis the largest extent of any box, widened by a relative 1e-12 against
+// rounding), are taken 32 at a time: lane l reads cell l's entry range, a warp scan lays the ranges
+// out as one list, and the warp walks it 32 entries at a time, each lane finding its entry's cell
+// by a binary search over the offsets held in the lanes.  An entry j > i is screened on the
+// outward-rounded float boxes (which can never reject an FP64 overlap), tested on the FP64 boxes,
+// then the shared-node and same-layer filters apply and hits are compacted with ballot/popc.
 // MODE 0: kept count per segment (cnt[i]), the sum of r_i + r_j over its kept candidates (each lane
 //         sums its own entries in walk order, then a fixed butterfly: rsum[i], for the prescreen
 //         margin), and the raw overlap count.
@@ -231,13 +207,20 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
   const Grid g = *gp;
   const int i = (int)w;
   int c0[3], c1[3];
-  cell_range(g, box, ne, i, c0, c1);
+  {
+    double lw[3];
+    for (int c = 0; c < 3; ++c) {
+      const double lo = box[c * ne + i];
+      lw[c] = xsub(xsub(lo, g.emax[c]), 1e-12 * (fabs(lo) + g.emax[c]));
+    }
+    cell_of(g, lw[0], lw[1], lw[2], c0);
+    cell_of(g, box[3 * ne + i], box[4 * ne + i], box[5 * ne + i], c1);
+  }
   const int sx = c1[0] - c0[0] + 1, sy = c1[1] - c0[1] + 1, sz = c1[2] - c0[2] + 1;
   const int ncell = sx * sy * sz;
   const int ia = m.conn[2 * i], ib = m.conn[2 * i + 1];
   const int li = (excl_layer && m.layer) ? m.layer[i] : -1;
   const float4 il = boxf[2LL * i], ih = boxf[2LL * i + 1];
-  const double ilo[3] = {box[i], box[ne + i], box[2 * ne + i]};
   const double ri = m.radii[i];
   int n_raw = 0, n_keep = 0;
   double rs = 0.0;
@@ -273,7 +256,6 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
       }
       const int sq = __shfl_sync(0xffffffffu, s0, q);
       const int pq = __shfl_sync(0xffffffffu, pre, q);
-      const int lq = __shfl_sync(0xffffffffu, lin, q);
       bool hit = false, kept = false;
       int j = -1;
       if (f < total) {
@@ -284,19 +266,13 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
           near = il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z;
         }
         if (near && overlap(box, ne, i, j)) {
-          int hc[3];
-          const double jlo0 = box[j], jlo1 = box[ne + j], jlo2 = box[2 * ne + j];
-          cell_of(g, ilo[0] > jlo0 ? ilo[0] : jlo0, ilo[1] > jlo1 ? ilo[1] : jlo1, ilo[2] > jlo2 ? ilo[2] : jlo2, hc);
-          const long long home = ((long long)hc[2] * g.dims[1] + hc[1]) * g.dims[0] + hc[0];
-          if (home == lq) {
-            hit = true;
-            kept = true;
-            if (excl_shared) {
-              const int ja = m.conn[2 * j], jb = m.conn[2 * j + 1];
-              if (ia == ja || ia == jb || ib == ja || ib == jb) kept = false;
-            }
-            if (kept && li >= 0 && m.layer[j] == li) kept = false;
+          hit = true;
+          kept = true;
+          if (excl_shared) {
+            const int ja = m.conn[2 * j], jb = m.conn[2 * j + 1];
+            if (ia == ja || ia == jb || ib == ja || ib == jb) kept = false;
           }
+          if (kept && li >= 0 && m.layer[j] == li) kept = false;
         }
       }
       const unsigned bal = __ballot_sync(0xffffffffu, kept);
@@ -525,10 +501,12 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   Grid* grid;
   XK_TRY(S.get(&box, 6 * ne));
   XK_TRY(S.get(&boxf, 2 * ne));
-  XK_TRY(S.get(&ext, 9));
+  XK_TRY(S.get(&ext, 12));
   XK_TRY(S.get(&grid, 1));
+  // words: 0 unused, 1-3 lowest lower corner, 4-6 highest upper corner, 7 raw count, 8 the sum of the
+  // box extents (a double, +0.0), 9-11 the largest extent on each axis
   double* ext_sum = reinterpret_cast<double*>(ext + 8);
-  unsigned long long init[9] = {0ull, ~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull, 0ull};  // word 8: +0.0
+  unsigned long long init[12] = {0ull, ~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
   XK_CUDA(cudaMemcpyAsync(ext, init, sizeof(init), cudaMemcpyHostToDevice, st));
   k_aabb<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, u, bp->margin, box, boxf, ext, ext_sum);
   const long long cap_cells = ne * 8 > 4096 ? ne * 8 : 4096;
@@ -538,32 +516,20 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   XK_CUDA(cudaMemcpyAsync(&hg, grid, sizeof(Grid), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
   const long long ncell = (long long)hg.dims[0] * hg.dims[1] * hg.dims[2];
-  int32_t *segs, *cstart, *cfill, *cnt, *off, *ecnt, *eoff, *ecell;
-  int64_t* etot;
-  XK_TRY(S.get(&ecnt, ne + 1));
-  XK_TRY(S.get(&eoff, ne + 1));
-  XK_TRY(S.get(&etot, 1));
+  int32_t *segs, *cstart, *cfill, *cnt, *off, *ecell;
+  XK_TRY(S.get(&ecell, ne));
+  XK_TRY(S.get(&segs, ne));
   XK_TRY(S.get(&cstart, ncell + 1));
   XK_TRY(S.get(&cfill, ncell + 1));
   XK_TRY(S.get(&cnt, ne + 1));
   XK_TRY(S.get(&off, ne + 1));
-  // entries: one per covered cell of every box, sorted by cell
-  XK_CUDA(cudaMemsetAsync(ecnt + ne, 0, sizeof(int32_t), st));
-  k_entry_count<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, ecnt);
-  XK_CHECK_LAUNCH();
-  XK_TRY(xk_exclusive_scan_i32(ecnt, eoff, ne + 1, etot, st));
-  int64_t h_e = 0;
-  XK_CUDA(cudaMemcpyAsync(&h_e, etot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  XK_CUDA(cudaStreamSynchronize(st));
-  if (h_e > 0x7fffffffLL) return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: more than 2^31 grid entries");
-  XK_TRY(S.get(&ecell, h_e));
-  XK_TRY(S.get(&segs, h_e));
+  // segments sorted by the cell of their lower corner
   XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (ncell + 1), st));
-  k_entry_fill<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, eoff, ecell, cfill);
+  k_cell_count<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, ecell, cfill);
   XK_CHECK_LAUNCH();
   XK_TRY(xk_exclusive_scan_i32(cfill, cstart, ncell + 1, nullptr, st));
   XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (ncell + 1), st));
-  k_entry_scatter<<<xk_blocks(ne, 256), 256, 0, st>>>(eoff, ne, ecell, cstart, cfill, segs);
+  k_cell_scatter<<<xk_blocks(ne, 256), 256, 0, st>>>(ne, ecell, cstart, cfill, segs);
   XK_CHECK_LAUNCH();
   unsigned long long* raw_dev = ext + 7;
   double* rsum;

@@ -14,7 +14,6 @@
 #include <cuda_bf16.h>
 
 #include "xk_common.cuh"
-#include "segment.cuh"
 
 namespace {
 
@@ -47,6 +46,45 @@ XK_D void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
 // ------------------------------------------------------------------ features
 
 // Exact double arithmetic in the order of the oracle's NumPy expressions, cast to float at the end.
+// Current gap of a candidate over (r_a + r_b), in float: the segment differences in double, then
+// the clamped closest-point parameters of _closest_point_segments_batch (geometry/_compute.py:55-151)
+// in float, each product and sum rounded on its own (no contraction), so that a NumPy float32
+// restatement gives the same value; near-parallel pairs (det <= 1e-3 ac) take s = 0.
+XK_D float current_gap_f(const double (*x)[3], double rs) {
+  float a3[3], b3[3], w3[3];
+  for (int c = 0; c < 3; ++c) {
+    a3[c] = (float)xsub(x[1][c], x[0][c]);
+    b3[c] = (float)xsub(x[3][c], x[2][c]);
+    w3[c] = (float)xsub(x[0][c], x[2][c]);
+  }
+  auto dotf = [](const float* p, const float* q) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(p[0], q[0]), __fmul_rn(p[1], q[1])), __fmul_rn(p[2], q[2]));
+  };
+  auto clampf = [](float v) { return v < 0.f ? 0.f : (v > 1.f ? 1.f : v); };
+  const float a = dotf(a3, a3), b = dotf(a3, b3), c = dotf(b3, b3), d = dotf(a3, w3), e = dotf(b3, w3);
+  const float ac = __fmul_rn(a, c);
+  const float det = __fsub_rn(ac, __fmul_rn(b, b));
+  float s, t;
+  if (!(det > __fmul_rn(1e-3f, ac))) {
+    s = 0.f;
+    t = c > 0.f ? clampf(__fdiv_rn(e, c)) : 0.f;
+  } else {
+    const float su = __fdiv_rn(__fsub_rn(__fmul_rn(b, e), __fmul_rn(c, d)), det);
+    const float tu = __fdiv_rn(__fsub_rn(__fmul_rn(a, e), __fmul_rn(b, d)), det);
+    s = clampf(su);
+    t = clampf(tu);
+    if (su < 0.f || su > 1.f) t = c > 0.f ? clampf(__fdiv_rn(__fadd_rn(__fmul_rn(b, s), e), c)) : 0.f;
+    if (tu < 0.f || tu > 1.f) {
+      s = a > 0.f ? clampf(__fdiv_rn(__fsub_rn(__fmul_rn(b, t), d), a)) : 0.f;
+      t = c > 0.f ? clampf(__fdiv_rn(__fadd_rn(__fmul_rn(b, s), e), c)) : 0.f;
+    }
+  }
+  float D[3];
+  for (int q = 0; q < 3; ++q) D[q] = __fsub_rn(__fadd_rn(w3[q], __fmul_rn(s, a3[q])), __fmul_rn(t, b3[q]));
+  const float rsf = (float)rs;
+  return __fdiv_rn(__fsub_rn(__fsqrt_rn(dotf(D, D)), rsf), rsf);
+}
+
 __global__ void k_features(xk_mesh m, const double* __restrict__ u, const int32_t* __restrict__ cands, long long n,
                            xk_pairs old, float* __restrict__ feat, uint8_t* __restrict__ hist) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -90,10 +128,8 @@ __global__ void k_features(xk_mesh m, const double* __restrict__ u, const int32_
   double g5;
   if (at >= 0) {
     g5 = xdiv(old.gap[at], rs);
-  } else {  // no previous gap: the current one, from the exact closest point (geometry/_compute.py:55-151)
-    double s_, t_, dist, nrm[3], diff[3];
-    closest_exact(x[0], x[1], x[2], x[3], s_, t_, dist, nrm, diff);
-    g5 = xdiv(xsub(dist, rs), rs);
+  } else {  // no previous gap: the current one, in float (feature accuracy is enough)
+    g5 = (double)current_gap_f(x, rs);
   }
   g5 = g5 < -2.0 ? -2.0 : (g5 > 8.0 ? 8.0 : g5);
   f[5] = (float)g5;

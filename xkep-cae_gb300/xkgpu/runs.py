@@ -8,11 +8,10 @@
   every node of the outer layer moved radially inward (its x and y
   prescribed), the inner wires clamped at both ends, the outer wires' axial
   and rotational DOFs clamped at z = 0 only.
-* ``run_bend_oscillation``: the 91-wire run: a Generalized-alpha ramp to the
-  bent state, then oscillation steps of a fixed time increment in which the
-  end curvature follows kappa0 cos(2 pi k / n_steps), each step one solver run
-  that continues from the last (integrator state, pair state and prescribed
-  values carried over).
+* ``run_bend_oscillation``: the 91-wire run: a quasi-static bend to the
+  curvature, then the driven ends are released and the strand oscillates
+  freely under Generalized-alpha, each time step one solver run that continues
+  from the last (integrator state and pair state carried over).
 
 The reference has no strand runner (its ``run_bending_oscillation`` is
 imported but never defined, ``numerical_tests/wire_bending_benchmark.py:191-212``),
@@ -132,18 +131,20 @@ def run_load_step(w, precision: str, *, layer: int, amount: float, settings: Sol
     return res, b, time.perf_counter() - t0
 
 
-def run_bend_oscillation(w, precision: str, *, kappa: float, t_bend: float = 1e-3, dt: float = 1e-4,
-                         n_steps: int = 20, rho_inf: float = 0.9, bend_settings: SolverSettings | None = None,
+def run_bend_oscillation(w, precision: str, *, kappa: float, dt: float = 1e-4, n_steps: int = 20,
+                         rho_inf: float = 0.9, rho: float = RHO_STEEL, bend_settings: SolverSettings | None = None,
                          step_settings: SolverSettings | None = None, graph: bool = True, verbose: bool = False):
-    """Ramp to the bent state over ``t_bend``, then ``n_steps`` oscillation steps of ``dt``.
+    """Bend quasi-statically to the arc of curvature ``kappa`` (z = L wire ends driven to the arc's end
+    section, z = 0 ends clamped), then release the z = L ends and take ``n_steps`` Generalized-alpha steps
+    of ``dt`` from rest: the strand springs back in free oscillation, its contacts sliding and separating.
+    Each step is one solver run continuing from the last (integrator state and pair state carried over).
 
-    Returns a dict: per phase the solver results, the displacements at the end of the ramp and of every
-    oscillation step, the Newton attempt counts, and the time spent in assembly and in linear solves.
+    Returns a dict: the displacements at the end of the bend and of every step, the Newton attempt counts,
+    the time spent in the solver runs and in the linear solves, and the assembly counts.
     """
     eng = strand_engine(w, precision)
     st = w.strand
     fixed, pd, pv = bending_boundary(st, kappa)
-    ga = GpuGeneralizedAlpha(lumped_mass(eng), rho_inf=rho_inf, device=eng.device)
     b = EngineBackend(eng, graph=graph)
     lin = BlockTridiagonalSolver(eng)
     timing = {"solve_s": 0.0, "solves": 0}
@@ -157,45 +158,46 @@ def run_bend_oscillation(w, precision: str, *, kappa: float, t_bend: float = 1e-
         timing["solves"] += 1
         return du
 
-    out = {"steps": [], "u": [], "attempts": [], "increments": []}
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sol = ContactFrictionSolver(b, ga, t_total=t_bend, fixed_dofs=fixed, prescribed_dofs=pd, prescribed_values=pv,
-                                settings=bend_settings or SolverSettings(dt_max_fraction=0.1),
-                                linear_solve=timed_solve, record_u=False, verbose=verbose)
-    res = sol.run()
-    out["bend"] = res
-    out["u"].append(res.u.cpu().numpy())
-    out["attempts"].append([r.attempts for r in res.increments])
-    if not res.converged:
-        out["converged"] = False
+    out = {"u": [], "attempts": [], "step_s": []}
+
+    def finish(converged, t0):
+        torch.cuda.synchronize()
+        out["converged"] = converged
         out["wall_s"] = time.perf_counter() - t0
         out.update(timing)
         out["counts"] = dict(b.counts)
         out["lin"] = dict(lin.stats)
         return out
-    u, prev = res.u, pv
-    for k in range(1, n_steps + 1):
-        _, target = end_arc_values(st, kappa * math.cos(2.0 * math.pi * k / n_steps))
-        sol = ContactFrictionSolver(b, ga, t_total=dt, fixed_dofs=fixed, prescribed_dofs=pd, prescribed_values=target,
-                                    prescribed_start=prev, settings=step_settings or SolverSettings(),
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sol = ContactFrictionSolver(b, QuasiStatic(), t_total=1.0, fixed_dofs=fixed, prescribed_dofs=pd,
+                                prescribed_values=pv, settings=bend_settings or SolverSettings(dt_max_fraction=0.1),
+                                linear_solve=timed_solve, record_u=False, verbose=verbose)
+    res = sol.run()
+    out["bend"] = {"increments": res.n_increments, "attempts": res.total_attempts, "cutbacks": res.n_cutbacks}
+    out["u"].append(res.u.cpu().numpy())
+    out["attempts"].append([r.attempts for r in res.increments])
+    if not res.converged:
+        return finish(False, t0)
+    torch.cuda.synchronize()
+    out["bend_s"] = time.perf_counter() - t0
+    u = res.u
+    ga = GpuGeneralizedAlpha(lumped_mass(eng, rho), rho_inf=rho_inf, device=eng.device)  # from rest
+    clamped = fixed  # the z = L ends are released
+    for _ in range(n_steps):
+        ts = time.perf_counter()
+        sol = ContactFrictionSolver(b, ga, t_total=dt, fixed_dofs=clamped, settings=step_settings or SolverSettings(),
                                     linear_solve=timed_solve, record_u=False, verbose=verbose)
         r = sol.run(u)
-        out["steps"].append(r)
         out["attempts"].append([x.attempts for x in r.increments])
         if not r.converged:
-            out["converged"] = False
-            break
-        u, prev = r.u, target
+            return finish(False, t0)
+        u = r.u
         out["u"].append(u.cpu().numpy())
-    else:
-        out["converged"] = True
-    torch.cuda.synchronize()
-    out["wall_s"] = time.perf_counter() - t0
-    out.update(timing)
-    out["counts"] = dict(b.counts)
-    out["lin"] = dict(lin.stats)
-    return out
+        torch.cuda.synchronize()
+        out["step_s"].append(time.perf_counter() - ts)
+    return finish(True, t0)
 
 
 def oscillation_states(w, kappa0: float, n_steps: int, *, jitter: float = 3e-4, seed: int = 7):
