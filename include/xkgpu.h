@@ -176,6 +176,8 @@ typedef struct {
   int32_t exclude_same_layer;    /* drop pairs of one layer (needs mesh layer) */
   int32_t midpoint_prescreening; /* _manager_process.py:260-286 */
   double prescreening_margin;    /* <= 0: half the mean of r_a + r_b over the candidates */
+  double cell_size;              /* grid cell edge; <= 0: automatic.  Sets the work, never the result
+                                    (the reference's cell_size, contact/_broadphase.py:18,55-58) */
 } xk_bp_params;
 
 /* Broadphase on the deformed coordinates X + u: every element pair (i<j) whose

@@ -90,6 +90,26 @@ def test_step_control_cutback():
     assert not tiny.failure(lf, 0.0, diverged=False)  # at the minimum increment: no retry
 
 
+def test_scheduled_steps():
+    """A load schedule is followed exactly; a failed increment is not retried."""
+    ctl = S.ScheduledSteps(2.0, (0.25, 0.5, 1.0))
+    prev, seen = 0.0, []
+    while True:
+        more, lf, dt = ctl.query(prev)
+        if not more:
+            break
+        assert dt == pytest.approx((lf - prev) * 2.0)
+        ctl.success(lf, prev, 100, 5, 0)  # many attempts, contact change: no growth or shrink
+        seen.append(lf)
+        prev = lf
+    assert seen == [0.25, 0.5, 1.0]
+    assert not S.ScheduledSteps(1.0, (0.5, 1.0)).failure(0.5, 0.0, diverged=True)
+    with pytest.raises(ValueError):
+        S.ScheduledSteps(1.0, (0.5, 0.4, 1.0))
+    with pytest.raises(ValueError):
+        S.ScheduledSteps(1.0, (0.5, 0.9))
+
+
 def test_solver_loop_on_oracle_reproduces_reference_run():
     from oracle_backend import OracleBackend, TorchGA
 
@@ -102,6 +122,15 @@ def test_solver_loop_on_oracle_reproduces_reference_run():
                                   prescribed_values=z["prescribed_values"], settings=_settings(z))
     res = sol.run()
     _compare(res, z, 1e-8)
+    # the same run, on a fresh backend, with the reference's increments given as a fixed schedule
+    b = OracleBackend(z["X"], z["conn"], float(z["radius"]), _section(z), layer=z["elem_layer"],
+                      k_pen=float(z["k_pen"]), k_t_ratio=float(z["k_t_ratio"]), mu=float(z["mu"]),
+                      smoothing_delta=float(z["smoothing_delta"]))
+    sol = S.ContactFrictionSolver(b, TorchGA(z["mass"], float(z["rho_inf"])), t_total=float(z["t_total"]),
+                                  fixed_dofs=z["fixed"], prescribed_dofs=z["prescribed_dofs"],
+                                  prescribed_values=z["prescribed_values"],
+                                  settings=S.SolverSettings(load_schedule=tuple(z["load_history"])))
+    _compare(sol.run(), z, 1e-8)
 
 
 def test_block_tridiagonal_solve_matches_dense():
@@ -146,11 +175,11 @@ def test_gmres_with_float32_block_preconditioner():
         if i < nb - 1:
             A[i * b:(i + 1) * b, (i + 1) * b:(i + 2) * b] = Up[i]
     F = tuple(torch.as_tensor(x, dtype=torch.float32) for x in (D, Lo, Up))
-    piv = blocktri_factor(*F)
+    blocktri_factor(*F)
     At = torch.as_tensor(A)
     rhs = torch.as_tensor(rng.normal(size=nb * b))
     x, it, rel = gmres(lambda v: At @ v, rhs,
-                       lambda v: blocktri_apply(*F, piv, v.view(nb, b, 1)).reshape(-1).double(), rtol=1e-12)
+                       lambda v: blocktri_apply(*F, v.view(nb, b, 1)).reshape(-1).double(), rtol=1e-12)
     assert rel <= 1e-8 and it <= 60
     want = np.linalg.solve(A, rhs.numpy())
     assert np.max(np.abs(x.numpy() - want)) <= 1e-7 * np.max(np.abs(want))

@@ -3,14 +3,19 @@
 // The reference bins AABBs into a hash grid (xkep_cae/contact/_broadphase.py:52-87)
 // and keeps the pairs whose closed AABBs overlap (:93-96); its output is the
 // set of all overlapping pairs, whatever the cell size.  Here every segment is
-// binned once, by the cell of its box's lower corner, on a grid of the mean box
-// extent (counting sort by cell).  A box j can overlap box i only if its lower
-// corner lies in [lo_i - E, hi_i] per axis, E the largest extent of any box on
-// that axis, so a warp per segment i walks the cells of that range (32 cells a
-// batch) and tests every entry j > i: screened on float boxes rounded outward,
-// tested on the exact double AABBs, filtered, compacted with ballot/popc.  Each
-// pair is found once, from its lower-numbered segment.  Filters follow
+// binned once, by the cell of its box's lower corner (counting sort by cell).
+// A box j can overlap box i only if its lower corner lies in [lo_i - E, hi_i]
+// per axis, E the largest extent of any box on that axis, so a warp per
+// segment i walks the cells of that range (32 cells a batch) and tests every
+// entry j > i: screened on float boxes rounded outward, tested on the exact
+// double AABBs, filtered, compacted with ballot/popc into a fixed-size slot list
+// of the segment.  Each pair is found once, from its lower-numbered segment, in
+// a single walk: a second kernel sorts each slot list and applies the midpoint
+// prescreen (whose margin is a mean over all candidates), a third writes the
+// kept pairs out in (i, j) order.  A slot list that overflows is detected at the
+// end and the walk is repeated with longer lists.  Filters follow
 // DetectCandidatesProcess (_manager_process.py:200-217,260-286).
+#include <atomic>
 #include <cstdio>
 
 #include "xk_common.cuh"
@@ -36,12 +41,15 @@ XK_D double dec_min(unsigned long long k) {
   return __longlong_as_double((long long)b);
 }
 
-// boxf: the same boxes in float, rounded outward (lower corner down, upper corner up), as two float4
-// per segment (32 bytes): a conservative screen for the sweep, which then tests the FP64 boxes.
+// box: the FP64 boxes, six doubles per segment (lower corner, upper corner); boxf: the same boxes in
+// float, rounded outward (lower corner down, upper corner up), as two float4 per segment (32 bytes): a
+// conservative screen for the sweep, which then tests the FP64 boxes.  mid: per segment its midpoint and
+// half length in the operation order of the midpoint prescreen (_manager_process.py:265-272), so that
+// the prescreen of a pair reads these 32 bytes of each segment and gives the same values.
 __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, double* __restrict__ box,
-                       float4* __restrict__ boxf, unsigned long long* __restrict__ ext, double* __restrict__ ext_sum) {
+                       float4* __restrict__ boxf, double4* __restrict__ mid, unsigned long long* __restrict__ ext,
+                       double* __restrict__ ext_sum) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
-  const long long ne = m.n_elems;
   unsigned long long lmin[3] = {~0ull, ~0ull, ~0ull}, lmax[3] = {0ull, 0ull, 0ull}, lax[3] = {0ull, 0ull, 0ull};
   double msum = 0.0;
   if (e < m.n_elems) {
@@ -49,13 +57,16 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
     const double ex = xadd(m.radii[e], margin);
     double mx = 0.0;
     float lf[3], hf[3];
+    double ma[3], da[3];
     for (int c = 0; c < 3; ++c) {
       double x0 = u ? xadd(m.X[3LL * a + c], u[6LL * a + c]) : m.X[3LL * a + c];
       double x1 = u ? xadd(m.X[3LL * b + c], u[6LL * b + c]) : m.X[3LL * b + c];
+      ma[c] = xmul(0.5, xadd(x0, x1));
+      da[c] = xsub(x1, x0);
       double lo = xsub(x0 < x1 ? x0 : x1, ex);
       double hi = xadd(x0 < x1 ? x1 : x0, ex);
-      box[c * ne + e] = lo;
-      box[(3 + c) * ne + e] = hi;
+      box[6LL * e + c] = lo;
+      box[6LL * e + 3 + c] = hi;
       lf[c] = __double2float_rd(lo);
       hf[c] = __double2float_ru(hi);
       lmin[c] = enc_min(lo);
@@ -66,6 +77,7 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
     }
     boxf[2LL * e] = make_float4(lf[0], lf[1], lf[2], 0.f);
     boxf[2LL * e + 1] = make_float4(hf[0], hf[1], hf[2], 0.f);
+    mid[e] = make_double4(ma[0], ma[1], ma[2], xmul(0.5, xsqrt(xdot_seq(da, da))));
     msum = mx;
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -88,16 +100,18 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
     atomicAdd(ext_sum, msum);  // the cell size only sets the work, not the result: any order will do
   }
 }
-
+// the grid over the boxes' bounding box: cells of cell_size, or (cell_size <= 0) of AUTO_CELL times the
+// mean of each box's largest extent; coarsened while it would have more than cap_cells cells
+constexpr double AUTO_CELL = 0.5;
 __global__ void k_grid(const unsigned long long* __restrict__ ext, const double* __restrict__ ext_sum, long long ne,
-                       long long cap_cells, Grid* g) {
+                       long long cap_cells, double cell_size, Grid* g) {
   double mx = *ext_sum / (double)ne;
   double lo[3], hi[3];
   for (int c = 0; c < 3; ++c) {
     lo[c] = dec_min(ext[1 + c]);
     hi[c] = dec_min(ext[4 + c]);
   }
-  double cell = mx * (1.0 + 1e-6) + 1e-300;
+  double cell = cell_size > 0.0 ? cell_size : AUTO_CELL * mx * (1.0 + 1e-6) + 1e-300;
   long long tot;
   int dims[3];
   for (int it = 0; it < 200; ++it) {
@@ -135,7 +149,7 @@ __global__ void k_cell_count(const double* __restrict__ box, long long ne, const
   if (e >= ne) return;
   const Grid g = *gp;
   int c[3];
-  cell_of(g, box[e], box[ne + e], box[2 * ne + e], c);
+  cell_of(g, box[6 * e], box[6 * e + 1], box[6 * e + 2], c);
   const int lin = (int)(((long long)c[2] * g.dims[1] + c[1]) * g.dims[0] + c[0]);
   ecell[e] = lin;
   atomicAdd(&ccnt[lin], 1);
@@ -150,33 +164,11 @@ __global__ void k_cell_scatter(long long ne, const int32_t* __restrict__ ecell, 
   segs[cstart[c] + atomicAdd(&cfill[c], 1)] = (int32_t)e;
 }
 
-XK_D bool overlap(const double* box, long long ne, int i, int j) {
-  for (int c = 0; c < 3; ++c)
-    if (!(box[c * ne + i] <= box[(3 + c) * ne + j]) || !(box[c * ne + j] <= box[(3 + c) * ne + i])) return false;
-  return true;
-}
-
-// Midpoint prescreen of DetectCandidatesProcess (_manager_process.py:260-286) for one pair: keep
-// when max(0, |m_a - m_b| - L_a/2 - L_b/2) <= r_a + r_b + extra, in the reference's operation order.
-XK_D bool midpoint_keep(const xk_mesh& m, const double* __restrict__ u, int i, int j, double extra) {
-  const int nd[4] = {m.conn[2 * i], m.conn[2 * i + 1], m.conn[2 * j], m.conn[2 * j + 1]};
-  double x[4][3];
-  for (int q = 0; q < 4; ++q)
-    for (int c = 0; c < 3; ++c) x[q][c] = u ? xadd(m.X[3LL * nd[q] + c], u[6LL * nd[q] + c]) : m.X[3LL * nd[q] + c];
-  double ma[3], mb[3], da[3], db[3], dm[3];
-  for (int c = 0; c < 3; ++c) {
-    ma[c] = xmul(0.5, xadd(x[0][c], x[1][c]));
-    mb[c] = xmul(0.5, xadd(x[2][c], x[3][c]));
-    da[c] = xsub(x[1][c], x[0][c]);
-    db[c] = xsub(x[3][c], x[2][c]);
-  }
-  for (int c = 0; c < 3; ++c) dm[c] = xsub(ma[c], mb[c]);
-  const double ha = xmul(0.5, xsqrt(xdot_seq(da, da)));
-  const double hb = xmul(0.5, xsqrt(xdot_seq(db, db)));
-  const double md = xsqrt(xdot_seq(dm, dm));
-  double mp = xsub(xsub(md, ha), hb);
-  mp = (mp > 0.0 || mp != mp) ? mp : 0.0;
-  return mp <= xadd(xadd(m.radii[i], m.radii[j]), extra);
+// the FP64 boxes of i (registers) and j (six doubles at box + 6 j, 16-byte aligned) overlap, closed
+XK_D bool overlap(const double (&bi)[6], const double* __restrict__ box, int j) {
+  const double2* bj = reinterpret_cast<const double2*>(box + 6LL * j);
+  const double2 p = __ldg(bj), q = __ldg(bj + 1), r = __ldg(bj + 2);  // lo x,y | lo z, hi x | hi y,z
+  return bi[0] <= q.y && p.x <= bi[3] && bi[1] <= r.x && p.y <= bi[4] && bi[2] <= r.y && q.x <= bi[5];
 }
 
 // A warp per segment i.  The cells that can hold the lower corner of a box overlapping box i, those
@@ -185,36 +177,31 @@ XK_D bool midpoint_keep(const xk_mesh& m, const double* __restrict__ u, int i, i
 // out as one list, and the warp walks it 32 entries at a time, each lane finding its entry's cell
 // by a binary search over the offsets held in the lanes.  An entry j > i is screened on the
 // outward-rounded float boxes (which can never reject an FP64 overlap), tested on the FP64 boxes,
-// then the shared-node and same-layer filters apply and hits are compacted with ballot/popc.
-// MODE 0: kept count per segment (cnt[i]), the sum of r_i + r_j over its kept candidates (each lane
-//         sums its own entries in walk order, then a fixed butterfly: rsum[i], for the prescreen
-//         margin), and the raw overlap count.
-// MODE 1: the kept candidates of segment i sorted by j at off[i] (out), and their prescreen flags.
-template <int MODE>
-__global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restrict__ u,
-                                                const double* __restrict__ box, const float4* __restrict__ boxf,
-                                                const Grid* __restrict__ gp, const int32_t* __restrict__ segs,
-                                                const int32_t* __restrict__ cstart, int excl_shared, int excl_layer,
+// then the shared-node and same-layer filters apply and hits are compacted with ballot/popc into
+// segment i's slot list (the first `cap` of them; cnt[i] counts them all).  Also per segment: the sum
+// of r_i + r_j over its kept candidates (each lane sums its own entries in walk order, then a fixed
+// butterfly: rsum[i], for the prescreen margin), the raw overlap count and the longest list.
+__global__ void __launch_bounds__(BP_T, 8) k_sweep(xk_mesh m, const double* __restrict__ box,
+                                                const float4* __restrict__ boxf, const Grid* __restrict__ gp,
+                                                const int32_t* __restrict__ segs, const int32_t* __restrict__ cstart,
+                                                int excl_shared, int excl_layer, int cap, int32_t* __restrict__ slot,
                                                 int32_t* __restrict__ cnt, double* __restrict__ rsum,
                                                 unsigned long long* __restrict__ raw_total,
-                                                const int32_t* __restrict__ off, const double* __restrict__ extra,
-                                                int32_t* __restrict__ tmp, int32_t* __restrict__ out,
-                                                int32_t* __restrict__ keep) {
+                                                int32_t* __restrict__ max_cnt) {
   const long long ne = m.n_elems;
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (w >= ne) return;
   const Grid g = *gp;
   const int i = (int)w;
+  double bi[6];
+  for (int c = 0; c < 6; ++c) bi[c] = box[6LL * i + c];
   int c0[3], c1[3];
   {
     double lw[3];
-    for (int c = 0; c < 3; ++c) {
-      const double lo = box[c * ne + i];
-      lw[c] = xsub(xsub(lo, g.emax[c]), 1e-12 * (fabs(lo) + g.emax[c]));
-    }
+    for (int c = 0; c < 3; ++c) lw[c] = xsub(xsub(bi[c], g.emax[c]), 1e-12 * (fabs(bi[c]) + g.emax[c]));
     cell_of(g, lw[0], lw[1], lw[2], c0);
-    cell_of(g, box[3 * ne + i], box[4 * ne + i], box[5 * ne + i], c1);
+    cell_of(g, bi[3], bi[4], bi[5], c1);
   }
   const int sx = c1[0] - c0[0] + 1, sy = c1[1] - c0[1] + 1, sz = c1[2] - c0[2] + 1;
   const int ncell = sx * sy * sz;
@@ -222,16 +209,16 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
   const int li = (excl_layer && m.layer) ? m.layer[i] : -1;
   const float4 il = boxf[2LL * i], ih = boxf[2LL * i + 1];
   const double ri = m.radii[i];
+  int32_t* const my = slot + (long long)i * cap;
   int n_raw = 0, n_keep = 0;
   double rs = 0.0;
-  const long long base = MODE == 1 ? (long long)off[i] : 0;
   for (int cb = 0; cb < ncell; cb += 32) {
     // this lane's cell of the batch and its entry range
-    int s0 = 0, n0 = 0, lin = -1;
+    int s0 = 0, n0 = 0;
     const int q0 = cb + lane;
     if (q0 < ncell) {
       const int x = c0[0] + q0 % sx, y = c0[1] + (q0 / sx) % sy, z = c0[2] + q0 / (sx * sy);
-      lin = (int)(((long long)z * g.dims[1] + y) * g.dims[0] + x);
+      const int lin = (int)(((long long)z * g.dims[1] + y) * g.dims[0] + x);
       s0 = cstart[lin];
       n0 = cstart[lin + 1] - s0;
     }
@@ -265,7 +252,7 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
           const float4 jl = __ldg(boxf + 2LL * j), jh = __ldg(boxf + 2LL * j + 1);
           near = il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z;
         }
-        if (near && overlap(box, ne, i, j)) {
+        if (near && overlap(bi, box, j)) {
           hit = true;
           kept = true;
           if (excl_shared) {
@@ -277,33 +264,21 @@ __global__ void __launch_bounds__(BP_T) k_sweep(xk_mesh m, const double* __restr
       }
       const unsigned bal = __ballot_sync(0xffffffffu, kept);
       n_raw += __popc(__ballot_sync(0xffffffffu, hit));
-      if (MODE == 0) {
-        if (kept) rs = xadd(rs, xadd(ri, m.radii[j]));  // this lane's entries, in walk order
-      } else if (kept) {
-        tmp[base + n_keep + __popc(bal & ((1u << lane) - 1u))] = j;
+      if (kept) {
+        rs = xadd(rs, xadd(ri, m.radii[j]));  // this lane's entries, in walk order
+        const int at = n_keep + __popc(bal & ((1u << lane) - 1u));
+        if (at < cap) my[at] = j;
       }
       n_keep += __popc(bal);
     }
   }
-  if (MODE == 0) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);  // fixed butterfly order
-    if (lane == 0) {
-      cnt[i] = n_keep;
-      rsum[i] = rs;
-      atomicAdd(raw_total, (unsigned long long)n_raw);
-    }
-  } else {
-    __syncwarp();
-    // rank sort of this segment's list (its j values are distinct), then the prescreen flag
-    for (int l = lane; l < n_keep; l += 32) {
-      const int v = tmp[base + l];
-      int r = 0;
-      for (int q2 = 0; q2 < n_keep; ++q2) r += tmp[base + q2] < v;
-      out[2 * (base + r)] = i;
-      out[2 * (base + r) + 1] = v;
-      if (keep) keep[base + r] = (!extra || midpoint_keep(m, u, i, v, *extra)) ? 1 : 0;
-    }
+  for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);  // fixed butterfly order
+  if (lane == 0) {
+    cnt[i] = n_keep;
+    rsum[i] = rs;
+    atomicAdd(raw_total, (unsigned long long)n_raw);
+    atomicMax(max_cnt, n_keep);
   }
 }
 
@@ -333,13 +308,71 @@ __global__ void k_margin(const double* __restrict__ part, const int64_t* __restr
   *out = *n > 0 ? xmul(xdiv(s, (double)*n), 0.5) : 0.0;
 }
 
-__global__ void k_compact_pairs(const int32_t* __restrict__ in, const int32_t* __restrict__ keep,
-                                const int32_t* __restrict__ pos, long long n, int32_t* __restrict__ out) {
-  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n || !keep[k]) return;
-  long long d = pos[k];
-  out[2 * d] = in[2 * k];
-  out[2 * d + 1] = in[2 * k + 1];
+// Midpoint prescreen of DetectCandidatesProcess (_manager_process.py:260-286) for the pair (i, j), from
+// the segments' midpoints and half lengths: keep when max(0, |m_i - m_j| - h_i - h_j) <= r_i + r_j +
+// extra, in the reference's operation order.
+XK_D bool midpoint_keep(const double4 a, const double4 b, double ra, double rb, double extra) {
+  const double dm[3] = {xsub(a.x, b.x), xsub(a.y, b.y), xsub(a.z, b.z)};
+  const double md = xsqrt(xdot_seq(dm, dm));
+  double mp = xsub(xsub(md, a.w), b.w);
+  mp = (mp > 0.0 || mp != mp) ? mp : 0.0;
+  return mp <= xadd(xadd(ra, rb), extra);
+}
+
+// A warp per segment: its slot list sorted by j (a rank sort; the j are distinct), the prescreen
+// applied (extra null: none), written to srt as j (kept) or ~j (dropped); cnt2[i] = kept count.
+__global__ void __launch_bounds__(BP_T) k_slots_rank(xk_mesh m, const double4* __restrict__ mid,
+                                                     const int32_t* __restrict__ slot, const int32_t* __restrict__ cnt,
+                                                     int cap, const double* __restrict__ extra,
+                                                     int32_t* __restrict__ srt, int32_t* __restrict__ cnt2) {
+  const long long ne = m.n_elems;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= ne) return;
+  const int i = (int)w;
+  const int n = cnt[i] < cap ? cnt[i] : cap;
+  const int32_t* const my = slot + (long long)i * cap;
+  int32_t* const out = srt + (long long)i * cap;
+  const double4 mi = mid[i];
+  const double ri = m.radii[i];
+  const double ex = extra ? *extra : 0.0;
+  int kept = 0;
+  for (int l = lane; l < n; l += 32) {
+    const int v = my[l];
+    int r = 0;
+    for (int q = 0; q < n; ++q) r += my[q] < v;
+    const bool k = !extra || midpoint_keep(mi, mid[v], ri, m.radii[v], ex);
+    out[r] = k ? v : ~v;
+    kept += k;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+  if (lane == 0) cnt2[i] = kept;
+}
+
+// A warp per segment: its kept pairs, in order, at off2[i] of out (rows (i, j); at most cap_out rows).
+__global__ void __launch_bounds__(BP_T) k_slots_emit(long long ne, const int32_t* __restrict__ srt,
+                                                     const int32_t* __restrict__ cnt, int cap,
+                                                     const int32_t* __restrict__ off2, long long cap_out,
+                                                     int32_t* __restrict__ out) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= ne) return;
+  const int i = (int)w;
+  const int n = cnt[i] < cap ? cnt[i] : cap;
+  const int32_t* const my = srt + (long long)i * cap;
+  long long at = off2[i];
+  for (int l0 = 0; l0 < n; l0 += 32) {
+    const int l = l0 + lane;
+    const int v = l < n ? my[l] : -1;
+    const unsigned bal = __ballot_sync(0xffffffffu, v >= 0);
+    const long long d = at + __popc(bal & ((1u << lane) - 1u));
+    if (v >= 0 && d >= 0 && d < cap_out) {
+      out[2 * d] = i;
+      out[2 * d + 1] = v;
+    }
+    at += __popc(bal);
+  }
 }
 
 // ------------------------------------------------------------------------- merge
@@ -485,6 +518,9 @@ struct Scratch {
 
 }  // namespace
 
+// slot-list length of the walk: grows to the longest list seen (a power of two), kept for later calls
+std::atomic<int> g_slot_cap{32};
+
 extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_bp_params* bp, int32_t* out_pairs,
                                    int64_t cap, int64_t* n_out, int64_t* n_raw, int64_t* n_prefilter, xk_stream s) {
   if (!m || !bp || !n_out) return xk_set_error(XK_ERR_ARG, "xk_broadphase: null argument");
@@ -494,101 +530,104 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   if (n_prefilter) *n_prefilter = 0;
   const long long ne = m->n_elems;
   if (ne < 2) return XK_OK;
+  if (ne > 0x7fffffffLL) return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: more than 2^31 segments");
   Scratch S{st};
   double* box;
   float4* boxf;
+  double4* mid;
   unsigned long long* ext;
   Grid* grid;
   XK_TRY(S.get(&box, 6 * ne));
   XK_TRY(S.get(&boxf, 2 * ne));
-  XK_TRY(S.get(&ext, 12));
+  XK_TRY(S.get(&mid, ne));
+  XK_TRY(S.get(&ext, 16));
   XK_TRY(S.get(&grid, 1));
   // words: 0 unused, 1-3 lowest lower corner, 4-6 highest upper corner, 7 raw count, 8 the sum of the
-  // box extents (a double, +0.0), 9-11 the largest extent on each axis
+  // box extents (a double, +0.0), 9-11 the largest extent on each axis, 12 the longest slot list
   double* ext_sum = reinterpret_cast<double*>(ext + 8);
-  unsigned long long init[12] = {0ull, ~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
+  unsigned long long* raw_dev = ext + 7;
+  int32_t* max_cnt = reinterpret_cast<int32_t*>(ext + 12);
+  unsigned long long init[16] = {0ull, ~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull,
+                                 0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
   XK_CUDA(cudaMemcpyAsync(ext, init, sizeof(init), cudaMemcpyHostToDevice, st));
-  k_aabb<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, u, bp->margin, box, boxf, ext, ext_sum);
+  k_aabb<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, u, bp->margin, box, boxf, mid, ext, ext_sum);
+  // the grid has at most cap_cells cells, so the cell arrays are sized without reading it back
   const long long cap_cells = ne * 8 > 4096 ? ne * 8 : 4096;
-  k_grid<<<1, 1, 0, st>>>(ext, ext_sum, ne, cap_cells, grid);
+  k_grid<<<1, 1, 0, st>>>(ext, ext_sum, ne, cap_cells, bp->cell_size, grid);
   XK_CHECK_LAUNCH();
-  Grid hg;
-  XK_CUDA(cudaMemcpyAsync(&hg, grid, sizeof(Grid), cudaMemcpyDeviceToHost, st));
-  XK_CUDA(cudaStreamSynchronize(st));
-  const long long ncell = (long long)hg.dims[0] * hg.dims[1] * hg.dims[2];
-  int32_t *segs, *cstart, *cfill, *cnt, *off, *ecell;
+  int32_t *segs, *cstart, *cfill, *cnt, *cnt2, *off2, *ecell;
   XK_TRY(S.get(&ecell, ne));
   XK_TRY(S.get(&segs, ne));
-  XK_TRY(S.get(&cstart, ncell + 1));
-  XK_TRY(S.get(&cfill, ncell + 1));
+  XK_TRY(S.get(&cstart, cap_cells + 1));
+  XK_TRY(S.get(&cfill, cap_cells + 1));
   XK_TRY(S.get(&cnt, ne + 1));
-  XK_TRY(S.get(&off, ne + 1));
+  XK_TRY(S.get(&cnt2, ne + 1));
+  XK_TRY(S.get(&off2, ne + 1));
   // segments sorted by the cell of their lower corner
-  XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (ncell + 1), st));
+  XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (cap_cells + 1), st));
   k_cell_count<<<xk_blocks(ne, 256), 256, 0, st>>>(box, ne, grid, ecell, cfill);
   XK_CHECK_LAUNCH();
-  XK_TRY(xk_exclusive_scan_i32(cfill, cstart, ncell + 1, nullptr, st));
-  XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (ncell + 1), st));
+  XK_TRY(xk_exclusive_scan_i32(cfill, cstart, cap_cells + 1, nullptr, st));
+  XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (cap_cells + 1), st));
   k_cell_scatter<<<xk_blocks(ne, 256), 256, 0, st>>>(ne, ecell, cstart, cfill, segs);
   XK_CHECK_LAUNCH();
-  unsigned long long* raw_dev = ext + 7;
-  double* rsum;
-  XK_TRY(S.get(&rsum, ne));
-  XK_CUDA(cudaMemsetAsync(raw_dev, 0, sizeof(unsigned long long), st));
-  XK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (ne + 1), st));
-  const int sweep_blocks = xk_blocks(ne * 32, BP_T);
-  const int excl_layer = (bp->exclude_same_layer && m->layer) ? 1 : 0;
-  k_sweep<0><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, bp->exclude_shared,
-                                             excl_layer, cnt, rsum, raw_dev, nullptr, nullptr, nullptr, nullptr,
-                                             nullptr);
-  XK_CHECK_LAUNCH();
+  double *rsum, *part, *extra;
   int64_t* tot;
-  XK_TRY(S.get(&tot, 2));
-  XK_TRY(xk_exclusive_scan_i32(cnt, off, ne + 1, tot, st));
-  double *part, *extra;
+  XK_TRY(S.get(&rsum, ne));
   XK_TRY(S.get(&part, RED_BLOCKS));
   XK_TRY(S.get(&extra, 1));
-  if (bp->midpoint_prescreening) {
-    if (!(bp->prescreening_margin > 0.0)) k_radsum_partial<<<RED_BLOCKS, RED_T, 0, st>>>(rsum, ne, part);
-    k_margin<<<1, 1, 0, st>>>(part, tot, bp->prescreening_margin, extra);
+  XK_TRY(S.get(&tot, 2));
+  const int warp_blocks = xk_blocks(ne * 32, BP_T);
+  const int excl_layer = (bp->exclude_same_layer && m->layer) ? 1 : 0;
+  int slot_cap = g_slot_cap.load();
+  for (int attempt = 0;; ++attempt) {
+    if ((double)ne * slot_cap * 8.0 > 64.0e9)
+      return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: candidate lists too long for the slot buffers");
+    int32_t *slot, *srt;
+    XK_TRY(S.get(&slot, ne * slot_cap));
+    XK_TRY(S.get(&srt, ne * slot_cap));
+    XK_CUDA(cudaMemsetAsync(ext + 7, 0, sizeof(unsigned long long), st));
+    XK_CUDA(cudaMemsetAsync(ext + 12, 0, sizeof(unsigned long long), st));
+    k_sweep<<<warp_blocks, BP_T, 0, st>>>(*m, box, boxf, grid, segs, cstart, bp->exclude_shared, excl_layer,
+                                          slot_cap, slot, cnt, rsum, raw_dev, max_cnt);
     XK_CHECK_LAUNCH();
-  }
-  int64_t h[2];
-  unsigned long long hraw = 0;
-  XK_CUDA(cudaMemcpyAsync(h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  XK_CUDA(cudaMemcpyAsync(&hraw, raw_dev, sizeof(hraw), cudaMemcpyDeviceToHost, st));
-  XK_CUDA(cudaStreamSynchronize(st));
-  const long long n1 = h[0];
-  if (n_raw) *n_raw = (int64_t)hraw;
-  if (n_prefilter) *n_prefilter = n1;
-  if (n1 == 0) return XK_OK;
-  if (n1 > 0x7fffffffLL) return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: more than 2^31 candidates");
-  int32_t *tmp, *pairs1, *keep = nullptr, *pos = nullptr;
-  XK_TRY(S.get(&tmp, n1));
-  if (!bp->midpoint_prescreening) {
-    *n_out = n1;
-    if (n1 > cap) return xk_set_error(XK_ERR_CAPACITY, "xk_broadphase: output capacity too small");
-    k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, bp->exclude_shared,
-                                               excl_layer, cnt, rsum, raw_dev, off, nullptr, tmp, out_pairs, nullptr);
+    XK_TRY(xk_exclusive_scan_i32(cnt, off2, ne, tot, st));  // tot[0]: candidates before the prescreen
+    const double* ex = nullptr;
+    if (bp->midpoint_prescreening) {
+      if (!(bp->prescreening_margin > 0.0)) k_radsum_partial<<<RED_BLOCKS, RED_T, 0, st>>>(rsum, ne, part);
+      k_margin<<<1, 1, 0, st>>>(part, tot, bp->prescreening_margin, extra);
+      XK_CHECK_LAUNCH();
+      ex = extra;
+    }
+    k_slots_rank<<<warp_blocks, BP_T, 0, st>>>(*m, mid, slot, cnt, slot_cap, ex, srt, cnt2);
     XK_CHECK_LAUNCH();
+    XK_TRY(xk_exclusive_scan_i32(cnt2, off2, ne, tot + 1, st));
+    k_slots_emit<<<warp_blocks, BP_T, 0, st>>>(ne, srt, cnt, slot_cap, off2, cap, out_pairs);
+    XK_CHECK_LAUNCH();
+    int64_t h[2];
+    unsigned long long hw[2] = {0ull, 0ull};
+    XK_CUDA(cudaMemcpyAsync(h, tot, sizeof(h), cudaMemcpyDeviceToHost, st));
+    XK_CUDA(cudaMemcpyAsync(hw, ext + 7, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    XK_CUDA(cudaMemcpyAsync(hw + 1, ext + 12, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     XK_CUDA(cudaStreamSynchronize(st));
+    const int longest = (int)(uint32_t)hw[1];
+    if (longest > slot_cap) {  // some lists were cut short: walk again with lists long enough for all
+      if (attempt > 0) return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: slot lists overflowed twice");
+      int c = slot_cap;
+      while (c < longest) c *= 2;
+      slot_cap = c;
+      int prev = g_slot_cap.load();
+      while (prev < c && !g_slot_cap.compare_exchange_weak(prev, c)) {
+      }
+      continue;
+    }
+    if (h[1] > 0x7fffffffLL) return xk_set_error(XK_ERR_OVERFLOW, "xk_broadphase: more than 2^31 candidates");
+    if (n_raw) *n_raw = (int64_t)hw[0];
+    if (n_prefilter) *n_prefilter = h[0];
+    *n_out = h[1];
+    if (h[1] > cap) return xk_set_error(XK_ERR_CAPACITY, "xk_broadphase: output capacity too small");
     return XK_OK;
   }
-  XK_TRY(S.get(&pairs1, 2 * n1));
-  XK_TRY(S.get(&keep, n1));
-  XK_TRY(S.get(&pos, n1));
-  k_sweep<1><<<sweep_blocks, BP_T, 0, st>>>(*m, u, box, boxf, grid, segs, cstart, bp->exclude_shared,
-                                             excl_layer, cnt, rsum, raw_dev, off, extra, tmp, pairs1, keep);
-  XK_CHECK_LAUNCH();
-  XK_TRY(xk_exclusive_scan_i32(keep, pos, n1, tot + 1, st));
-  XK_CUDA(cudaMemcpyAsync(h + 1, tot + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  XK_CUDA(cudaStreamSynchronize(st));
-  *n_out = h[1];
-  if (h[1] > cap) return xk_set_error(XK_ERR_CAPACITY, "xk_broadphase: output capacity too small");
-  k_compact_pairs<<<xk_blocks(n1, 256), 256, 0, st>>>(pairs1, keep, pos, n1, out_pairs);
-  XK_CHECK_LAUNCH();
-  XK_CUDA(cudaStreamSynchronize(st));
-  return XK_OK;
 }
 
 extern "C" xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const int32_t* cands, int64_t n_cands,

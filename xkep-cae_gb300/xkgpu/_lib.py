@@ -88,7 +88,7 @@ class System(C.Structure):
 
 class BPParams(C.Structure):
     _fields_ = [("margin", C.c_double), ("exclude_shared", C.c_int32), ("exclude_same_layer", C.c_int32),
-                ("midpoint_prescreening", C.c_int32), ("prescreening_margin", C.c_double)]
+                ("midpoint_prescreening", C.c_int32), ("prescreening_margin", C.c_double), ("cell_size", C.c_double)]
 
 
 class ContactPattern(C.Structure):

@@ -29,6 +29,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import time
 
 import numpy as np
 import torch
@@ -38,33 +39,31 @@ from .device import ptr, stream_handle
 from .solve import DeviceLinearSolver
 
 
-def blocktri_factor(D: torch.Tensor, Lo: torch.Tensor, Up: torch.Tensor) -> list:
+def blocktri_factor(D: torch.Tensor, Lo: torch.Tensor, Up: torch.Tensor) -> None:
     """Block LU of the block-tridiagonal matrix (diagonal blocks D, blocks left Lo, right Up; (nb, b, b)
-    each), without pivoting between blocks and with partial pivoting inside the diagonal blocks:
-    S_0 = D_0, S_i = D_i - Lo_i S_{i-1}^-1 Up_{i-1}.  D is overwritten by the LU factors of S_i and Up by
-    S_i^-1 Up_i; returns the pivots.  A singular S_i gives non-finite values downstream, as a singular
-    sparse LU does."""
+    each), without pivoting between blocks: S_0 = D_0, S_i = D_i - Lo_i S_{i-1}^-1 Up_{i-1}.  D is
+    overwritten by the inverses S_i^-1 (an LU with partial pivoting inside each block, on the device through
+    ``torch.linalg``) and Up by S_i^-1 Up_i, so that applying the factors is matrix-vector products only.
+    A singular S_i gives non-finite values downstream, as a singular sparse LU does."""
     nb = D.shape[0]
-    pivs = []
     for i in range(nb):
         if i > 0:
             D[i].sub_(Lo[i] @ Up[i - 1])
-        lu, piv, _ = torch.linalg.lu_factor_ex(D[i])
-        D[i].copy_(lu)
-        pivs.append(piv)
+        inv, _ = torch.linalg.inv_ex(D[i])
+        D[i].copy_(inv)
         if i < nb - 1:
-            Up[i].copy_(torch.linalg.lu_solve(lu, piv, Up[i]))
-    return pivs
+            Up[i].copy_(inv @ Up[i])
 
 
-def blocktri_apply(D: torch.Tensor, Lo: torch.Tensor, Up: torch.Tensor, pivs: list, rhs: torch.Tensor) -> torch.Tensor:
-    """Solve with the factors of ``blocktri_factor`` for ``rhs`` (nb, b, k)."""
+def blocktri_apply(D: torch.Tensor, Lo: torch.Tensor, Up: torch.Tensor, rhs: torch.Tensor) -> torch.Tensor:
+    """Solve with the factors of ``blocktri_factor`` for ``rhs`` (nb, b, k): y_i = S_i^-1 (r_i - Lo_i y_{i-1}),
+    then y_i -= (S_i^-1 Up_i) y_{i+1} from the last block back."""
     nb = D.shape[0]
     rhs = rhs.to(D.dtype)
     y = torch.empty_like(rhs)
     for i in range(nb):
         r = rhs[i] if i == 0 else rhs[i] - Lo[i] @ y[i - 1]
-        y[i] = torch.linalg.lu_solve(D[i], pivs[i], r)
+        torch.matmul(D[i], r, out=y[i])
     for i in range(nb - 2, -1, -1):
         y[i] -= Up[i] @ y[i + 1]
     return y
@@ -72,7 +71,8 @@ def blocktri_apply(D: torch.Tensor, Lo: torch.Tensor, Up: torch.Tensor, pivs: li
 
 def blocktri_solve(D: torch.Tensor, Lo: torch.Tensor, Up: torch.Tensor, rhs: torch.Tensor) -> torch.Tensor:
     """Factor (in place) and solve the block-tridiagonal system for ``rhs`` (nb, b, k)."""
-    return blocktri_apply(D, Lo, Up, blocktri_factor(D, Lo, Up), rhs)
+    blocktri_factor(D, Lo, Up)
+    return blocktri_apply(D, Lo, Up, rhs)
 
 
 def gmres(matvec, b: torch.Tensor, precond, *, rtol: float = 1e-10, restart: int = 30, max_iter: int = 300):
@@ -150,10 +150,16 @@ class BlockTridiagonalSolver:
     iteration applies the system itself in FP64 (``xk_system_spmv`` plus the mass term) until the
     relative residual is below ``rtol``.  With ``factor_dtype=torch.float64`` the preconditioned system
     is the identity up to the rounding of the block LU, which has no pivoting between blocks.
+
+    The factors are kept across solves (Newton iterations, increments, contact patterns of the same block
+    layout) while they stay a good preconditioner: a solve that needed more than ``refactor_iters`` Krylov
+    iterations marks them for a new factorisation at the next solve, and a solve that does not reach the
+    tolerance with kept factors factors the current system at once and solves again.  Since the Krylov
+    iteration applies the exact system, the solution's accuracy does not depend on the factors' age.
     """
 
     def __init__(self, engine, axis: int | None = None, *, factor_dtype=torch.float32, rtol: float = 1e-10,
-                 restart: int = 30, max_iter: int = 300):
+                 restart: int = 30, max_iter: int = 300, refactor_iters: int = 12):
         self.eng = engine
         dev = engine.device
         X = engine.mesh.X.reshape(-1, 3).cpu().numpy()
@@ -167,6 +173,9 @@ class BlockTridiagonalSolver:
         self.n = len(X)
         self.factor_dtype = factor_dtype
         self.rtol, self.restart, self.max_iter = float(rtol), int(restart), int(max_iter)
+        self.refactor_iters = int(refactor_iters)
+        self._F = None  # the factors in use (fp32 copies or the FP64 blocks)
+        self._need_factor = True
         self._sysw = DeviceLinearSolver(engine)  # the xk_system view of the engine's matrices and its SpMV
         self.overflow = torch.zeros(1, dtype=torch.int32, device=dev)
         self.bn = 0
@@ -174,7 +183,8 @@ class BlockTridiagonalSolver:
         self._buf = None
         self._fbuf = None
         self._pattern_version = None
-        self.stats = {"solves": 0, "gmres_iterations": 0, "max_rel_residual": 0.0, "not_converged": 0}
+        self.stats = {"solves": 0, "factorizations": 0, "gmres_iterations": 0, "max_rel_residual": 0.0,
+                      "not_converged": 0, "stale_refactor": 0, "fp64_refactor": 0, "factor_s": 0.0, "gmres_s": 0.0}
 
     def _bandwidth(self) -> int:
         e = self.eng
@@ -196,22 +206,25 @@ class BlockTridiagonalSolver:
         ver = getattr(self.eng.pattern, "version", None)
         if self._buf is not None and ver == self._pattern_version:
             return
+        self._pattern_version = ver
         bn = min(self._bandwidth(), max(self.n, 1))
         nb = -(-self.n // bn)
+        if self._buf is not None and (bn, nb) == (self.bn, self.nb):
+            return  # same block layout: kept factors remain a valid preconditioner
         b = 6 * bn
-        if self._buf is None or self._buf[0].shape != (nb, b, b):
-            self._buf = self._fbuf = None
-            torch.cuda.empty_cache()
-            dev = self.eng.device
-            self._buf = tuple(torch.empty((nb, b, b), dtype=torch.float64, device=dev) for _ in range(3))
-            if self.factor_dtype != torch.float64:
-                self._fbuf = tuple(torch.empty((nb, b, b), dtype=self.factor_dtype, device=dev) for _ in range(3))
+        self._buf = self._fbuf = self._F = None
+        torch.cuda.empty_cache()
+        dev = self.eng.device
+        self._buf = tuple(torch.empty((nb, b, b), dtype=torch.float64, device=dev) for _ in range(3))
+        if self.factor_dtype != torch.float64:
+            self._fbuf = tuple(torch.empty((nb, b, b), dtype=self.factor_dtype, device=dev) for _ in range(3))
         self.bn, self.nb = bn, nb
-        self._pattern_version = ver
+        self._need_factor = True
 
-    def __call__(self, backend, R: torch.Tensor, fixed: np.ndarray, mass_diag: torch.Tensor | None):
-        self._sysw.set_fixed(fixed)
-        self._prepare()
+    def _factor(self, mass_diag, fp64: bool):
+        """Scatter the current system into the dense blocks and factor it (in ``factor_dtype``, or FP64)."""
+        torch.cuda.synchronize(self.eng.device)
+        t0 = time.perf_counter()
         D, Lo, Up = self._buf
         nb, bn, b = self.nb, self.bn, 6 * self.bn
         sysc = self._sysw._sync()
@@ -224,13 +237,26 @@ class BlockTridiagonalSolver:
         if pad:  # positions past the last node: identity rows
             idx = torch.arange(6 * (bn - pad), b, device=D.device)
             D[nb - 1, idx, idx] = 1.0
-        if self._fbuf is not None:
+        if self._fbuf is not None and not fp64:
             for dst, src in zip(self._fbuf, (D, Lo, Up)):
                 dst.copy_(src)
             F = self._fbuf
         else:
-            F = (D, Lo, Up)
-        pivs = blocktri_factor(*F)
+            F = self._buf
+        blocktri_factor(*F)
+        self._F = F
+        self._need_factor = False
+        self.stats["factorizations"] += 1
+        torch.cuda.synchronize(self.eng.device)
+        self.stats["factor_s"] += time.perf_counter() - t0
+
+    def __call__(self, backend, R: torch.Tensor, fixed: np.ndarray, mass_diag: torch.Tensor | None):
+        self._sysw.set_fixed(fixed)
+        self._prepare()
+        nb, b = self.nb, 6 * self.bn
+        fresh = self._need_factor or self._F is None
+        if fresh:
+            self._factor(mass_diag, fp64=False)
         perm = self.perm
         free = torch.as_tensor(~np.asarray(fixed, dtype=bool), device=R.device)
         zero = torch.zeros((), dtype=torch.float64, device=R.device)
@@ -244,22 +270,40 @@ class BlockTridiagonalSolver:
         def precond(v):
             rhs = torch.zeros(nb * b, dtype=torch.float64, device=v.device)
             rhs[perm] = v
-            y = blocktri_apply(*F, pivs, rhs.view(nb, b, 1))
+            y = blocktri_apply(*self._F, rhs.view(nb, b, 1))
             return y.reshape(-1)[perm].to(torch.float64)
 
         rhs = torch.where(free, -R.to(torch.float64), zero)
-        du, it, rel = gmres(matvec, rhs, precond, rtol=self.rtol, restart=self.restart, max_iter=self.max_iter)
         st = self.stats
-        if not rel <= max(1e3 * self.rtol, 1e-7) and F is not self._buf:
-            # the float32 factors were too coarse for this system: factor in FP64 and solve again
-            st["fp64_refactor"] = st.get("fp64_refactor", 0) + 1
-            F = self._buf
-            pivs = blocktri_factor(*F)
+        enough = max(1e3 * self.rtol, 1e-7)
+        # kept factors get a short budget of iterations before they are replaced
+        t0 = time.perf_counter()
+        du, it, rel = gmres(matvec, rhs, precond, rtol=self.rtol, restart=self.restart,
+                            max_iter=self.max_iter if fresh else min(self.max_iter, 3 * self.refactor_iters))
+        st["gmres_s"] += time.perf_counter() - t0
+        it_last = it
+        tries = [] if fresh else ["stale"]
+        if self._fbuf is not None:
+            tries.append("fp64")
+        for kind in tries:
+            if rel <= enough:
+                break
+            # kept factors no longer precondition this system (stale), or the float32 factors of the
+            # current one are too coarse (fp64): factor again and solve again
+            st[kind + "_refactor"] += 1
+            self._factor(mass_diag, fp64=(kind == "fp64"))
+            t0 = time.perf_counter()
             du2, it2, rel2 = gmres(matvec, rhs, precond, rtol=self.rtol, restart=self.restart,
                                    max_iter=self.max_iter)
+            st["gmres_s"] += time.perf_counter() - t0
             it += it2
+            it_last = it2
             if rel2 < rel:
                 du, rel = du2, rel2
+            if kind == "fp64":
+                self._need_factor = True  # the next system starts from float32 factors again
+        if it_last > self.refactor_iters:
+            self._need_factor = True
         st["solves"] += 1
         st["gmres_iterations"] += it
         st["max_rel_residual"] = max(st["max_rel_residual"], rel)

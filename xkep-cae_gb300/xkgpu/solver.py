@@ -149,6 +149,26 @@ class StepControl:
         return True
 
 
+class ScheduledSteps(StepControl):
+    """A fixed list of load fractions: no growth, no cutbacks (a failed increment ends the run).  Used to
+    put two runs on the same increments, e.g. the increments a reference run took."""
+
+    def __init__(self, t_total: float, fractions):
+        super().__init__(t_total)
+        fr = [float(f) for f in fractions]
+        if not fr or any(b <= a for a, b in zip(fr, fr[1:])) or fr[0] <= 0.0 or abs(fr[-1] - 1.0) > 1e-12:
+            raise ValueError("load schedule: increasing fractions in (0, 1], ending at 1")
+        self.queue = deque(fr)
+
+    def success(self, load_frac, load_frac_prev, n_attempts, n_active, prev_n_active) -> None:
+        self._last_prev = load_frac
+        if self.queue and self.queue[0] <= load_frac + 1e-15:
+            self.queue.popleft()
+
+    def failure(self, load_frac, load_frac_prev, diverged) -> bool:
+        return False
+
+
 # --------------------------------------------------------------------------- settings and results
 
 
@@ -175,6 +195,8 @@ class SolverSettings:
     # _newton_steps.py:229-235); 0 switches it off, so that only the force and displacement tests end
     # an increment (used where two runs are compared to a tighter tolerance than the energy test gives)
     energy_tol: float = 1e-10
+    # increments at exactly these load fractions (ScheduledSteps) instead of the adaptive control
+    load_schedule: tuple = ()
 
 
 @dataclass
@@ -449,10 +471,14 @@ class ContactFrictionSolver:
         if dynamic_ref:
             f_ext_ref_norm = 1.0
         t = self.t_total
-        ctl = StepControl(t, t, cfg.dt_min_fraction * t if cfg.dt_min_fraction > 0 else t / 32.0,
-                          cfg.dt_max_fraction * t if cfg.dt_max_fraction > 0 else t, cfg.dt_grow_factor,
-                          cfg.dt_shrink_factor, cfg.dt_grow_attempt_threshold if cfg.dt_grow_attempt_threshold > 0
-                          else 5, cfg.dt_shrink_attempt_threshold, cfg.dt_contact_change_threshold)
+        if cfg.load_schedule:
+            ctl = ScheduledSteps(t, cfg.load_schedule)
+        else:
+            ctl = StepControl(t, t, cfg.dt_min_fraction * t if cfg.dt_min_fraction > 0 else t / 32.0,
+                              cfg.dt_max_fraction * t if cfg.dt_max_fraction > 0 else t, cfg.dt_grow_factor,
+                              cfg.dt_shrink_factor, cfg.dt_grow_attempt_threshold
+                              if cfg.dt_grow_attempt_threshold > 0 else 5, cfg.dt_shrink_attempt_threshold,
+                              cfg.dt_contact_change_threshold)
         ckpt = (u.clone(), u_ref.clone())
         dyn.checkpoint()
         load_prev = 0.0

@@ -886,7 +886,8 @@ class GpuDetectCandidatesProcess:
         mesh = DeviceMesh(coords, conn, r, layer=layer, device=self._device)
         bp = L.BPParams(float(getattr(inp, "margin", 0.0)), 1, int(layer is not None),
                         int(bool(getattr(config, "midpoint_prescreening", True))),
-                        float(getattr(config, "prescreening_margin", 0.0)))
+                        float(getattr(config, "prescreening_margin", 0.0)),
+                        float(getattr(inp, "cell_size", None) or 0.0))
         cands = _broadphase(mesh, bp, mesh.device)
         old_pairs = list(manager.pairs)
         old = DevicePairTable(mesh.device, cap=max(len(old_pairs), 16))

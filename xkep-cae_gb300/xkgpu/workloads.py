@@ -3,7 +3,12 @@
 Steel wires (E = 200 GPa, nu = 0.3) in mm-N-MPa units, circular sections with
 Cowper's shear factor (``xkep_cae/elements/_beam_section.py:59-65,129-136``),
 penalty ``k_pen = 1e3 * E A / L_mean`` (``AutoEALPenalty``,
-``xkep_cae/contact/penalty/strategy.py:111-131``), mu = 0.1, k_t_ratio = 0.5,
+``xkep_cae/contact/penalty/strategy.py:111-131``) or, for the solver runs that
+take the reference's default, ``k_pen = 0.1 * 12 E I / L_mean^3``
+(``AutoBeamEIPenalty``, ``strategy.py:59-101``; the contact config's default
+``k_pen_mode = "beam_ei"``, ``k_pen_scale = 0.1``, ``contact/_contact_pair.py:87-88``;
+what ``ContactFrictionProcess`` uses when the setup's k_pen is 0,
+``contact/solver/process.py:203-211``), mu = 0.1, k_t_ratio = 0.5,
 same-layer pairs excluded.  Positions are perturbed by N(0, (1e-3 d)^2) and
 rotations by N(0, (1e-3 rad)^2) from ``numpy.random.default_rng(seed)``.
 """
@@ -51,9 +56,14 @@ class Workload:
                     smoothing_delta=self.smoothing_delta)
 
 
+def beam_ei_penalty(section: dict, l_mean: float, scale: float = 0.1) -> float:
+    """``AutoBeamEIPenalty._compute`` with one contact pair: scale * 12 E I / L^3."""
+    return scale * 12.0 * section["E"] * section["Iy"] / l_mean**3
+
+
 def strand_workload(name: str, n_wires: int, d: float, pitch: float, n_pitches: float, n_el_per_pitch: int, *,
                     gap_frac: float = -0.005, seed: int = 0, mu: float = 0.1, compress_layer: int | None = None,
-                    compress_frac: float = 0.0) -> Workload:
+                    compress_frac: float = 0.0, penalty: str = "ea") -> Workload:
     n_el = int(round(n_el_per_pitch * n_pitches))
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
@@ -62,12 +72,18 @@ def strand_workload(name: str, n_wires: int, d: float, pitch: float, n_pitches: 
     if compress_layer is not None:
         u = u + S.radial_compression(st, compress_layer, compress_frac * d)
     sec = circle_section(d)
-    k_pen = 1e3 * sec["E"] * sec["A"] / mean_element_length(st.coords, st.conn)
+    l_mean = mean_element_length(st.coords, st.conn)
+    if penalty == "ea":
+        k_pen = 1e3 * sec["E"] * sec["A"] / l_mean
+    elif penalty == "beam_ei":
+        k_pen = beam_ei_penalty(sec, l_mean)
+    else:
+        raise ValueError(f"penalty: 'ea' or 'beam_ei', not {penalty!r}")
     return Workload(name, st, sec, u, k_pen, mu=mu, meta={"n_wires": n_wires, "d": d, "pitch": pitch,
                                                           "n_pitches": n_pitches, "n_el_per_pitch": n_el_per_pitch,
                                                           "gap_frac": gap_frac, "seed": seed,
                                                           "compress_layer": compress_layer,
-                                                          "compress_frac": compress_frac})
+                                                          "compress_frac": compress_frac, "penalty": penalty})
 
 
 def wires_for_layers(n_layers: int) -> int:
