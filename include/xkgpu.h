@@ -292,7 +292,8 @@ typedef struct {
   /* Launch shape (0 = the built-in default): persistent CTAs per SM of the element-side block
    * gather (XK_GATHER_SIDES).  Results do not depend on it; an autotuner may choose it. */
   int32_t sides_per_sm;
-  int32_t pad_launch;
+  int32_t node_elem_ready; /* 1: node_elem_ptr / node_elem already hold the mesh's node -> element lists
+                            * (set by the build; reset it to 0 when the mesh or those arrays change) */
 } xk_contact_pattern;
 
 /* Returns XK_ERR_CAPACITY (with n_members, n_others, nnzb set) when a capacity

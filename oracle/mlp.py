@@ -147,7 +147,8 @@ def current_gap_f(xa0, xa1, xb0, xb1, rs):
 
 
 def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
-    """Per-candidate inputs (n x F), float32.
+    """Per-candidate inputs (n x F), float32.  The position differences are taken in double; everything
+    after them in float32 with every operation rounded on its own (the GPU kernel's order).
 
     0: |m_a - m_b| / (r_a + r_b)              midpoint separation
     1: |d_a . d_b| / (|d_a| |d_b|)            cosine of the tangent angle
@@ -160,18 +161,28 @@ def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
     6: 1 if the previous-step gap exists
     7: 0
     """
+    f = np.float32
     rs = ra + rb
-    ma, mb = 0.5 * (xa0 + xa1), 0.5 * (xb0 + xb1)
-    da, db = xa1 - xa0, xb1 - xb0
-    la_n, lb_n = np.linalg.norm(da, axis=1), np.linalg.norm(db, axis=1)
-    sep = np.linalg.norm(ma - mb, axis=1)
-    X = np.zeros((xa0.shape[0], F), np.float64)
-    X[:, 0] = sep / rs
-    X[:, 1] = np.abs(np.sum(da * db, axis=1)) / np.maximum(la_n * lb_n, 1e-300)
-    X[:, 2] = (la_n + lb_n) / (2.0 * rs)
-    have_layer = (la >= 0) & (lb >= 0)
-    X[:, 3] = np.where(have_layer, np.minimum(np.abs(la - lb), 3) / 3.0, 0.0)
-    X[:, 4] = np.where(have_layer & ((la == 0) | (lb == 0)), 1.0, 0.0)
-    X[:, 5] = np.clip(np.where(has_prev, prev_gap / rs, current_gap_f(xa0, xa1, xb0, xb1, rs)), -2.0, 8.0)
-    X[:, 6] = has_prev.astype(np.float64)
-    return X.astype(np.float32)
+    rsf = np.asarray(rs, dtype=np.float64).astype(f)
+    dm = (0.5 * (xa0 + xa1) - 0.5 * (xb0 + xb1)).astype(f)
+    da, db = (xa1 - xa0).astype(f), (xb1 - xb0).astype(f)
+
+    def dot(p, q):
+        return (p[:, 0] * q[:, 0] + p[:, 1] * q[:, 1]) + p[:, 2] * q[:, 2]
+
+    with np.errstate(invalid="ignore", divide="ignore"):
+        sep = np.sqrt(dot(dm, dm))
+        la_n, lb_n = np.sqrt(dot(da, da)), np.sqrt(dot(db, db))
+        den = la_n * lb_n
+        den = np.where((den >= f(1e-30)) | np.isnan(den), den, f(1e-30))
+        X = np.zeros((xa0.shape[0], F), np.float32)
+        X[:, 0] = sep / rsf
+        X[:, 1] = np.abs(dot(da, db)) / den
+        X[:, 2] = (la_n + lb_n) / (f(2.0) * rsf)
+        have_layer = (la >= 0) & (lb >= 0)
+        X[:, 3] = np.where(have_layer, np.minimum(np.abs(la - lb), 3).astype(f) / f(3.0), f(0.0))
+        X[:, 4] = np.where(have_layer & ((la == 0) | (lb == 0)), f(1.0), f(0.0))
+        prev = np.asarray(prev_gap, dtype=np.float64).astype(f) / rsf
+        X[:, 5] = np.clip(np.where(has_prev, prev, current_gap_f(xa0, xa1, xb0, xb1, rs).astype(f)), f(-2.0), f(8.0))
+        X[:, 6] = has_prev.astype(np.float32)
+    return X

@@ -104,6 +104,15 @@ def test_scheduled_steps():
         prev = lf
     assert seen == [0.25, 0.5, 1.0]
     assert not S.ScheduledSteps(1.0, (0.5, 1.0)).failure(0.5, 0.0, diverged=True)
+    # with cutbacks: the failed increment is retried from the shrunk fraction, then the list continues
+    ctl = S.ScheduledSteps(1.0, (0.5, 1.0), cutbacks=True, min_frac=0.01)
+    assert ctl.query(0.0)[1] == 0.5
+    assert ctl.failure(0.5, 0.0, diverged=False)
+    assert ctl.query(0.0)[1] == 0.25
+    ctl.success(0.25, 0.0, 3, 0, 0)
+    assert ctl.query(0.25)[1] == 0.5
+    ctl.success(0.5, 0.25, 3, 0, 0)
+    assert ctl.query(0.5)[1] == 1.0
     with pytest.raises(ValueError):
         S.ScheduledSteps(1.0, (0.5, 0.4, 1.0))
     with pytest.raises(ValueError):

@@ -47,7 +47,7 @@ XK_D double dec_min(unsigned long long k) {
 // half length in the operation order of the midpoint prescreen (_manager_process.py:265-272), so that
 // the prescreen of a pair reads these 32 bytes of each segment and gives the same values.
 __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, double* __restrict__ box,
-                       float4* __restrict__ boxf, double4* __restrict__ mid, unsigned long long* __restrict__ ext,
+                       float4* __restrict__ boxf, double4_32a* __restrict__ mid, unsigned long long* __restrict__ ext,
                        double* __restrict__ ext_sum) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long lmin[3] = {~0ull, ~0ull, ~0ull}, lmax[3] = {0ull, 0ull, 0ull}, lax[3] = {0ull, 0ull, 0ull};
@@ -77,7 +77,12 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
     }
     boxf[2LL * e] = make_float4(lf[0], lf[1], lf[2], 0.f);
     boxf[2LL * e + 1] = make_float4(hf[0], hf[1], hf[2], 0.f);
-    mid[e] = make_double4(ma[0], ma[1], ma[2], xmul(0.5, xsqrt(xdot_seq(da, da))));
+    double4_32a me;
+    me.x = ma[0];
+    me.y = ma[1];
+    me.z = ma[2];
+    me.w = xmul(0.5, xsqrt(xdot_seq(da, da)));
+    mid[e] = me;
     msum = mx;
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -311,7 +316,7 @@ __global__ void k_margin(const double* __restrict__ part, const int64_t* __restr
 // Midpoint prescreen of DetectCandidatesProcess (_manager_process.py:260-286) for the pair (i, j), from
 // the segments' midpoints and half lengths: keep when max(0, |m_i - m_j| - h_i - h_j) <= r_i + r_j +
 // extra, in the reference's operation order.
-XK_D bool midpoint_keep(const double4 a, const double4 b, double ra, double rb, double extra) {
+XK_D bool midpoint_keep(const double4_32a a, const double4_32a b, double ra, double rb, double extra) {
   const double dm[3] = {xsub(a.x, b.x), xsub(a.y, b.y), xsub(a.z, b.z)};
   const double md = xsqrt(xdot_seq(dm, dm));
   double mp = xsub(xsub(md, a.w), b.w);
@@ -321,7 +326,7 @@ XK_D bool midpoint_keep(const double4 a, const double4 b, double ra, double rb, 
 
 // A warp per segment: its slot list sorted by j (a rank sort; the j are distinct), the prescreen
 // applied (extra null: none), written to srt as j (kept) or ~j (dropped); cnt2[i] = kept count.
-__global__ void __launch_bounds__(BP_T) k_slots_rank(xk_mesh m, const double4* __restrict__ mid,
+__global__ void __launch_bounds__(BP_T) k_slots_rank(xk_mesh m, const double4_32a* __restrict__ mid,
                                                      const int32_t* __restrict__ slot, const int32_t* __restrict__ cnt,
                                                      int cap, const double* __restrict__ extra,
                                                      int32_t* __restrict__ srt, int32_t* __restrict__ cnt2) {
@@ -333,7 +338,7 @@ __global__ void __launch_bounds__(BP_T) k_slots_rank(xk_mesh m, const double4* _
   const int n = cnt[i] < cap ? cnt[i] : cap;
   const int32_t* const my = slot + (long long)i * cap;
   int32_t* const out = srt + (long long)i * cap;
-  const double4 mi = mid[i];
+  const double4_32a mi = mid[i];
   const double ri = m.radii[i];
   const double ex = extra ? *extra : 0.0;
   int kept = 0;
@@ -377,23 +382,35 @@ __global__ void __launch_bounds__(BP_T) k_slots_emit(long long ne, const int32_t
 
 // ------------------------------------------------------------------------- merge
 
-XK_D unsigned long long pkey(int a, int b) { return ((unsigned long long)(uint32_t)a << 32) | (uint32_t)b; }
 
-XK_D long long lower_bound_old(const xk_pairs& p, unsigned long long key) {
-  long long lo = 0, hi = p.n;
-  while (lo < hi) {
-    long long mid = (lo + hi) >> 1;
-    if (pkey(p.ea[mid], p.eb[mid]) < key) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-XK_D long long lower_bound_cand(const int32_t* c, long long n, unsigned long long key) {
+// start[s] = the first row of a list sorted by (a, b) whose a >= s, s in [0, ne] (a binary search per s; the
+// rows' a values are read at stride S: 1 for a table, 2 for (a, b) rows)
+template <int S>
+__global__ void k_seg_start(const int32_t* __restrict__ a, long long n, long long ne, int32_t* __restrict__ start) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > ne) return;
   long long lo = 0, hi = n;
   while (lo < hi) {
     long long mid = (lo + hi) >> 1;
-    if (pkey(c[2 * mid], c[2 * mid + 1]) < key) lo = mid + 1; else hi = mid;
+    if (a[S * mid] < s) lo = mid + 1; else hi = mid;
+  }
+  start[s] = (int32_t)lo;
+}
+
+// the first row in [lo, hi) of a list sorted by b within one a whose b >= key
+XK_D long long lower_bound_b(const int32_t* __restrict__ b, int S, long long lo, long long hi, int key) {
+  while (lo < hi) {
+    long long mid = (lo + hi) >> 1;
+    if (b[S * mid] < key) lo = mid + 1; else hi = mid;
   }
   return lo;
+}
+
+XK_D long long lower_bound_old(const xk_pairs& p, const int32_t* __restrict__ start, int a, int b) {
+  return lower_bound_b(p.eb, 1, start[a], start[a + 1], b);
+}
+XK_D long long lower_bound_cand(const int32_t* c, const int32_t* __restrict__ start, int a, int b) {
+  return lower_bound_b(c + 1, 2, start[a], start[a + 1], b);
 }
 
 XK_D void copy_state(const xk_pairs& a, long long i, xk_pairs& b, long long j) {
@@ -430,30 +447,31 @@ XK_D void copy_state(const xk_pairs& a, long long i, xk_pairs& b, long long j) {
   }
 }
 
-__global__ void k_merge_flags(xk_pairs old, const int32_t* __restrict__ cand, long long nc, int32_t* __restrict__ r) {
+__global__ void k_merge_flags(xk_pairs old, const int32_t* __restrict__ cand, const int32_t* __restrict__ cstart,
+                              long long nc, int32_t* __restrict__ r) {
   long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (o > old.n) return;
   if (o == old.n) { r[o] = 0; return; }
-  unsigned long long key = pkey(old.ea[o], old.eb[o]);
-  long long l = lower_bound_cand(cand, nc, key);
-  bool found = l < nc && pkey(cand[2 * l], cand[2 * l + 1]) == key;
+  const int a = old.ea[o], b = old.eb[o];
+  long long l = lower_bound_cand(cand, cstart, a, b);
+  bool found = l < nc && cand[2 * l] == a && cand[2 * l + 1] == b;
   r[o] = found ? 0 : 1;
 }
 
-__global__ void k_merge_new(xk_pairs old, const int32_t* __restrict__ cand, long long nc,
-                            const int32_t* __restrict__ R, xk_pairs out) {
+__global__ void k_merge_new(xk_pairs old, const int32_t* __restrict__ ostart, const int32_t* __restrict__ cand,
+                            long long nc, const int32_t* __restrict__ R, xk_pairs out) {
   long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nc) return;
-  unsigned long long key = pkey(cand[2 * k], cand[2 * k + 1]);
-  long long lo = lower_bound_old(old, key);
+  const int a = cand[2 * k], b = cand[2 * k + 1];
+  long long lo = lower_bound_old(old, ostart, a, b);
   long long pos = k + R[lo];
-  if (lo < old.n && pkey(old.ea[lo], old.eb[lo]) == key) {
+  if (lo < old.n && old.ea[lo] == a && old.eb[lo] == b) {
     copy_state(old, lo, out, pos);
     return;
   }
   const long long cb = out.cap;
-  out.ea[pos] = cand[2 * k];
-  out.eb[pos] = cand[2 * k + 1];
+  out.ea[pos] = a;
+  out.eb[pos] = b;
   out.s[pos] = 0.0;
   out.t[pos] = 0.0;
   out.gap[pos] = 0.0;
@@ -483,11 +501,11 @@ __global__ void k_merge_new(xk_pairs old, const int32_t* __restrict__ cand, long
   }
 }
 
-__global__ void k_merge_old(xk_pairs old, const int32_t* __restrict__ cand, long long nc,
-                            const int32_t* __restrict__ r, const int32_t* __restrict__ R, xk_pairs out) {
+__global__ void k_merge_old(xk_pairs old, const int32_t* __restrict__ cand, const int32_t* __restrict__ cstart,
+                            long long nc, const int32_t* __restrict__ r, const int32_t* __restrict__ R, xk_pairs out) {
   long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= old.n || !r[o]) return;
-  long long pos = R[o] + lower_bound_cand(cand, nc, pkey(old.ea[o], old.eb[o]));
+  long long pos = R[o] + lower_bound_cand(cand, cstart, old.ea[o], old.eb[o]);
   copy_state(old, o, out, pos);
   out.status[pos] = 0;  // INACTIVE
 }
@@ -534,7 +552,7 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   Scratch S{st};
   double* box;
   float4* boxf;
-  double4* mid;
+  double4_32a* mid;
   unsigned long long* ext;
   Grid* grid;
   XK_TRY(S.get(&box, 6 * ne));
@@ -637,16 +655,22 @@ extern "C" xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const
     return xk_set_error(XK_ERR_CAPACITY, "xk_pairs_merge: out->cap < old->n + n_cands");
   cudaStream_t st = (cudaStream_t)s;
   Scratch S{st};
-  int32_t *r, *R;
+  int32_t *r, *R, *ostart, *cstart;
   int64_t* tot;
+  const long long ne = m->n_elems;
   XK_TRY(S.get(&r, (long long)old->n + 1));
   XK_TRY(S.get(&R, (long long)old->n + 1));
+  XK_TRY(S.get(&ostart, ne + 2));
+  XK_TRY(S.get(&cstart, ne + 2));
   XK_TRY(S.get(&tot, 1));
-  k_merge_flags<<<xk_blocks((long long)old->n + 1, 256), 256, 0, st>>>(*old, cands, n_cands, r);
+  // per-segment row ranges of both sorted lists: each lookup searches only its segment's rows
+  k_seg_start<1><<<xk_blocks(ne + 1, 256), 256, 0, st>>>(old->ea, old->n, ne, ostart);
+  k_seg_start<2><<<xk_blocks(ne + 1, 256), 256, 0, st>>>(cands, n_cands, ne, cstart);
+  k_merge_flags<<<xk_blocks((long long)old->n + 1, 256), 256, 0, st>>>(*old, cands, cstart, n_cands, r);
   XK_CHECK_LAUNCH();
   XK_TRY(xk_exclusive_scan_i32(r, R, (long long)old->n + 1, tot, st));
-  if (n_cands > 0) k_merge_new<<<xk_blocks(n_cands, 256), 256, 0, st>>>(*old, cands, n_cands, R, *out);
-  if (old->n > 0) k_merge_old<<<xk_blocks(old->n, 256), 256, 0, st>>>(*old, cands, n_cands, r, R, *out);
+  if (n_cands > 0) k_merge_new<<<xk_blocks(n_cands, 256), 256, 0, st>>>(*old, ostart, cands, n_cands, R, *out);
+  if (old->n > 0) k_merge_old<<<xk_blocks(old->n, 256), 256, 0, st>>>(*old, cands, cstart, n_cands, r, R, *out);
   XK_CHECK_LAUNCH();
   int64_t h = 0;
   XK_CUDA(cudaMemcpyAsync(&h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));

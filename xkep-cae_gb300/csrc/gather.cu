@@ -128,21 +128,21 @@ __global__ void __launch_bounds__(SEG_T) k_segment_sort(const int32_t* __restric
   if (lane + 32 < n) a[lo + r1] = v1;
 }
 
-// MODE 0: count the distinct column nodes c >= v of each row v; MODE 1: write them sorted.  The
-// capacity check covers all the row's column nodes.
-template <int MODE>
-__global__ void k_row_cols(const int32_t* __restrict__ mnodes, const int32_t* __restrict__ ptr,
-                           const int32_t* __restrict__ inc, int n_nodes, int32_t* __restrict__ rcnt,
-                           const int32_t* __restrict__ rptr, int32_t* __restrict__ col, int32_t* __restrict__ brow,
-                           int32_t* __restrict__ err) {
-  int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= n_nodes) return;
-  int buf[MAX_COLS];
+// The distinct column nodes c >= v of row v, in ascending order, from its member incidences (the four nodes
+// of every member touching v).  A warp per node: the candidates (4 per incidence, at most RC_CAP) are staged
+// in shared memory, bitonic-sorted, and the first of each run of equal values >= v is kept (ballot
+// prefix).  MODE 0 counts them (rcnt[v]); MODE 1 writes them at rptr[v] (col, and v in brow).  A node with
+// more than RC_CAP candidates takes the serial path of one lane (insertion into a sorted local buffer of
+// MAX_COLS distinct columns; err bit 1 if that overflows).
+constexpr int RC_WARPS = 4, RC_CAP = 512;
+XK_D int row_cols_serial(const int32_t* __restrict__ mnodes, const int32_t* __restrict__ inc, int x0, int x1, int v,
+                         int* buf, int32_t* __restrict__ err) {
   int n = 0;
-  for (int x = ptr[v]; x < ptr[v + 1]; ++x) {
+  for (int x = x0; x < x1; ++x) {
     const long long mi = inc[x] >> 2;
     for (int k = 0; k < 4; ++k) {
       const int c = mnodes[4 * mi + k];
+      if (c < v) continue;
       int y = n - 1;
       while (y >= 0 && buf[y] > c) --y;
       if (y >= 0 && buf[y] == c) continue;
@@ -152,17 +152,75 @@ __global__ void k_row_cols(const int32_t* __restrict__ mnodes, const int32_t* __
       ++n;
     }
   }
-  int lo = 0;  // first column >= v
-  while (lo < n && buf[lo] < v) ++lo;
-  if (MODE == 0) {
-    rcnt[v] = n - lo;
-  } else {
-    const int o = rptr[v] - lo;
-    for (int k = lo; k < n; ++k) {
-      col[o + k] = buf[k];
-      brow[o + k] = v;
+  return n;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * RC_WARPS) k_row_cols(const int32_t* __restrict__ mnodes,
+                                                            const int32_t* __restrict__ ptr,
+                                                            const int32_t* __restrict__ inc, int n_nodes,
+                                                            int32_t* __restrict__ rcnt,
+                                                            const int32_t* __restrict__ rptr,
+                                                            int32_t* __restrict__ col, int32_t* __restrict__ brow,
+                                                            int32_t* __restrict__ err) {
+  __shared__ int sm[RC_WARPS][RC_CAP];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int v = blockIdx.x * RC_WARPS + wid;
+  if (v >= n_nodes) return;
+  const int x0 = ptr[v], x1 = ptr[v + 1];
+  const int nc = 4 * (x1 - x0);
+  if (nc > RC_CAP) {
+    if (lane == 0) {
+      int buf[MAX_COLS];
+      const int n = row_cols_serial(mnodes, inc, x0, x1, v, buf, err);
+      if (MODE == 0) {
+        rcnt[v] = n;
+      } else {
+        for (int k = 0; k < n; ++k) {
+          col[rptr[v] + k] = buf[k];
+          brow[rptr[v] + k] = v;
+        }
+      }
     }
+    return;
   }
+  int* a = sm[wid];
+  int N = 32;
+  while (N < nc) N <<= 1;
+  for (int i = lane; i < N; i += 32) {
+    int c = 0x7fffffff;
+    if (i < nc) c = mnodes[4LL * (inc[x0 + (i >> 2)] >> 2) + (i & 3)];
+    a[i] = c;
+  }
+  __syncwarp();
+  for (int k = 2; k <= N; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < N; i += 32) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const int p = a[i], q = a[ixj];
+          if (((i & k) == 0) == (p > q)) {
+            a[i] = q;
+            a[ixj] = p;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  int at = 0;
+  for (int i0 = 0; i0 < N; i0 += 32) {
+    const int i = i0 + lane;
+    const int c = a[i];
+    const bool keep = c != 0x7fffffff && c >= v && (i == 0 || a[i - 1] != c);
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (MODE == 1 && keep) {
+      const int o = rptr[v] + at + __popc(bal & ((1u << lane) - 1u));
+      col[o] = c;
+      brow[o] = v;
+    }
+    at += __popc(bal);
+  }
+  if (MODE == 0 && lane == 0) rcnt[v] = at;
 }
 
 // Lower index: per node w, the stored blocks (v, w) with v < w in the order of v (MODE 0 counts).
@@ -1055,7 +1113,8 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   k_segment_sort<<<xk_blocks(32LL * nn, SEG_T), SEG_T, 0, st>>>(pat->inc_ptr, nn, pat->inc);
   // block pattern rows
   XK_CUDA(cudaMemsetAsync(err, 0, sizeof(int32_t), st));
-  k_row_cols<0><<<xk_blocks(nn, 64), 64, 0, st>>>(pat->member_nodes, pat->inc_ptr, pat->inc, nn, cnt, nullptr,
+  if (nn > 0)
+    k_row_cols<0><<<(unsigned)((nn + RC_WARPS - 1) / RC_WARPS), 32 * RC_WARPS, 0, st>>>(pat->member_nodes, pat->inc_ptr, pat->inc, nn, cnt, nullptr,
                                                    nullptr, nullptr, err);
   XK_CHECK_LAUNCH();
   XK_CUDA(cudaMemsetAsync(cnt + nn, 0, sizeof(int32_t), st));
@@ -1067,7 +1126,8 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   const long long nb = h[1];
   pat->nnzb = nb;
   if (nb > pat->cap_blocks) return xk_set_error(XK_ERR_CAPACITY, "xk_contact_pattern_build: block capacity too small");
-  k_row_cols<1><<<xk_blocks(nn, 64), 64, 0, st>>>(pat->member_nodes, pat->inc_ptr, pat->inc, nn, nullptr,
+  if (nn > 0)
+    k_row_cols<1><<<(unsigned)((nn + RC_WARPS - 1) / RC_WARPS), 32 * RC_WARPS, 0, st>>>(pat->member_nodes, pat->inc_ptr, pat->inc, nn, nullptr,
                                                    pat->row_ptr, pat->col, pat->blk_row, err);
   XK_CHECK_LAUNCH();
   // contributor lists of the blocks
@@ -1103,6 +1163,7 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   if (pat->low_ptr && pat->low_blk) pat->nnzb_full = nb + h[3];
   // element-side form (gather variant XK_GATHER_SIDES)
   const bool sides = pat->node_elem_ptr && pat->node_elem && pat->elem_ptr && pat->elem_inc && pat->bcodes;
+  int32_t herr2 = 0;
   const int ne = m->n_elems;
   pat->n_elems = ne;
   pat->sides_ok = 0;
@@ -1111,18 +1172,20 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
     XK_TRY(S.get(&ecnt, (long long)(ne > nn ? ne : nn) + 1));
     XK_TRY(S.get(&efill, (long long)(ne > nn ? ne : nn) + 1));
     XK_TRY(S.get(&serr, 1));
-    // mesh node -> elements
-    XK_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int32_t) * (nn + 1), st));
-    if (ne > 0) k_node_elem_count<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, ecnt);
-    XK_CHECK_LAUNCH();
-    XK_TRY(xk_exclusive_scan_i32(ecnt, pat->node_elem_ptr, nn + 1, nullptr, st));
-    XK_CUDA(cudaMemsetAsync(efill, 0, sizeof(int32_t) * (nn + 1), st));
-    if (ne > 0)
-      k_node_elem_fill<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, pat->node_elem_ptr, efill,
-                                                           reinterpret_cast<int2*>(pat->node_elem));
-    k_segment_sort_pairs<<<xk_blocks(nn, 128), 128, 0, st>>>(pat->node_elem_ptr, nn,
+    // mesh node -> elements (mesh topology: built once per pattern and mesh)
+    if (!pat->node_elem_ready) {
+      XK_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int32_t) * (nn + 1), st));
+      if (ne > 0) k_node_elem_count<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, ecnt);
+      XK_CHECK_LAUNCH();
+      XK_TRY(xk_exclusive_scan_i32(ecnt, pat->node_elem_ptr, nn + 1, nullptr, st));
+      XK_CUDA(cudaMemsetAsync(efill, 0, sizeof(int32_t) * (nn + 1), st));
+      if (ne > 0)
+        k_node_elem_fill<<<xk_blocks(ne, 256), 256, 0, st>>>(*m, pat->node_elem_ptr, efill,
                                                              reinterpret_cast<int2*>(pat->node_elem));
-    XK_CHECK_LAUNCH();
+      k_segment_sort_pairs<<<xk_blocks(nn, 128), 128, 0, st>>>(pat->node_elem_ptr, nn,
+                                                               reinterpret_cast<int2*>(pat->node_elem));
+      XK_CHECK_LAUNCH();
+    }
     // element -> member sides
     XK_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int32_t) * (ne + 1), st));
     if (nm > 0) k_elem_inc_count<<<xk_blocks(nm, 256), 256, 0, st>>>(*p, pat->members, (int)nm, ecnt);
@@ -1146,13 +1209,14 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
                                                         pat->bcodes, serr);
     if (nb > 0) k_sort_codes<<<xk_blocks(nb, 256), 256, 0, st>>>(nb, reinterpret_cast<int4*>(pat->bcodes));
     XK_CHECK_LAUNCH();
-    int32_t herr2 = 0;
     XK_CUDA(cudaMemcpyAsync(&herr2, serr, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    XK_CUDA(cudaStreamSynchronize(st));
-    pat->sides_ok = herr2 ? 0 : 1;
   }
   XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
+  if (sides) {
+    pat->sides_ok = herr2 ? 0 : 1;
+    pat->node_elem_ready = 1;
+  }
   if (herr) return xk_set_error(XK_ERR_OVERFLOW, "xk_contact_pattern_build: inconsistent block pattern");
   return XK_OK;
 }

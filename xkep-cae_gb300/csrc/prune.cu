@@ -85,8 +85,21 @@ XK_D float current_gap_f(const double (*x)[3], double rs) {
   return __fdiv_rn(__fsub_rn(__fsqrt_rn(dotf(D, D)), rsf), rsf);
 }
 
+// start[s] = the first row of the old table (sorted by (ea, eb)) whose ea >= s, s in [0, ne]
+__global__ void k_table_seg_start(xk_pairs p, long long ne, int32_t* __restrict__ start) {
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > ne) return;
+  long long lo = 0, hi = p.n;
+  while (lo < hi) {
+    const long long mid = (lo + hi) >> 1;
+    if (p.ea[mid] < s) lo = mid + 1; else hi = mid;
+  }
+  start[s] = (int32_t)lo;
+}
+
 __global__ void k_features(xk_mesh m, const double* __restrict__ u, const int32_t* __restrict__ cands, long long n,
-                           xk_pairs old, float* __restrict__ feat, uint8_t* __restrict__ hist) {
+                           xk_pairs old, const int32_t* __restrict__ ostart, float* __restrict__ feat,
+                           uint8_t* __restrict__ hist) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int ea = cands[2 * i], eb = cands[2 * i + 1];
@@ -96,43 +109,47 @@ __global__ void k_features(xk_mesh m, const double* __restrict__ u, const int32_
     for (int c = 0; c < 3; ++c)
       x[k][c] = u ? xadd(m.X[3LL * nd[k] + c], u[6LL * nd[k] + c]) : m.X[3LL * nd[k] + c];
   const double rs = xadd(m.radii[ea], m.radii[eb]);
-  double dm[3], da[3], db[3];
+  // differences in double, everything after them in float with each operation rounded on its own
+  float dm[3], da[3], db[3];
   for (int c = 0; c < 3; ++c) {
     const double ma = xmul(0.5, xadd(x[0][c], x[1][c])), mb = xmul(0.5, xadd(x[2][c], x[3][c]));
-    dm[c] = xsub(ma, mb);
-    da[c] = xsub(x[1][c], x[0][c]);
-    db[c] = xsub(x[3][c], x[2][c]);
+    dm[c] = (float)xsub(ma, mb);
+    da[c] = (float)xsub(x[1][c], x[0][c]);
+    db[c] = (float)xsub(x[3][c], x[2][c]);
   }
-  const double sep = xsqrt(xdot_seq(dm, dm));
-  const double lna = xsqrt(xdot_seq(da, da)), lnb = xsqrt(xdot_seq(db, db));
-  double den = xmul(lna, lnb);
-  if (!(den >= 1e-300)) den = (den != den) ? den : 1e-300;
-  const double cosv = xdiv(fabs(xdot_seq(da, db)), den);
+  auto dotf = [](const float* p, const float* q) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(p[0], q[0]), __fmul_rn(p[1], q[1])), __fmul_rn(p[2], q[2]));
+  };
+  const float rsf = (float)rs;
+  const float sep = __fsqrt_rn(dotf(dm, dm));
+  const float lna = __fsqrt_rn(dotf(da, da)), lnb = __fsqrt_rn(dotf(db, db));
+  float den = __fmul_rn(lna, lnb);
+  if (!(den >= 1e-30f)) den = (den != den) ? den : 1e-30f;
   float f[MF];
-  f[0] = (float)xdiv(sep, rs);
-  f[1] = (float)cosv;
-  f[2] = (float)xdiv(xadd(lna, lnb), xmul(2.0, rs));
+  f[0] = __fdiv_rn(sep, rsf);
+  f[1] = __fdiv_rn(fabsf(dotf(da, db)), den);
+  f[2] = __fdiv_rn(__fadd_rn(lna, lnb), __fmul_rn(2.0f, rsf));
   const int la = m.layer ? m.layer[ea] : -1, lb = m.layer ? m.layer[eb] : -1;
   const bool have = la >= 0 && lb >= 0;
   const int dl = la > lb ? la - lb : lb - la;
-  f[3] = have ? (float)xdiv((double)(dl < 3 ? dl : 3), 3.0) : 0.f;
+  f[3] = have ? __fdiv_rn((float)(dl < 3 ? dl : 3), 3.0f) : 0.f;
   f[4] = (have && (la == 0 || lb == 0)) ? 1.f : 0.f;
-  // previous-step gap: the pair in the old table (sorted by (ea, eb))
-  long long lo = 0, hi = (long long)old.n - 1, at = -1;
+  // previous-step gap: the pair in the old table (sorted by (ea, eb)), searched among the rows of ea
+  long long lo = ostart[ea], hi = (long long)ostart[ea + 1] - 1, at = -1;
   while (lo <= hi) {
     const long long mid = (lo + hi) >> 1;
-    const int oa = old.ea[mid], ob = old.eb[mid];
-    if (oa == ea && ob == eb) { at = mid; break; }
-    if (oa < ea || (oa == ea && ob < eb)) lo = mid + 1; else hi = mid - 1;
+    const int ob = old.eb[mid];
+    if (ob == eb) { at = mid; break; }
+    if (ob < eb) lo = mid + 1; else hi = mid - 1;
   }
-  double g5;
+  float g5;
   if (at >= 0) {
-    g5 = xdiv(old.gap[at], rs);
+    g5 = __fdiv_rn((float)old.gap[at], rsf);
   } else {  // no previous gap: the current one, in float (feature accuracy is enough)
-    g5 = (double)current_gap_f(x, rs);
+    g5 = current_gap_f(x, rs);
   }
-  g5 = g5 < -2.0 ? -2.0 : (g5 > 8.0 ? 8.0 : g5);
-  f[5] = (float)g5;
+  g5 = g5 < -2.0f ? -2.0f : (g5 > 8.0f ? 8.0f : g5);
+  f[5] = g5;
   f[6] = at >= 0 ? 1.f : 0.f;
   f[7] = 0.f;
   float4* o = reinterpret_cast<float4*>(feat + MF * i);
@@ -760,8 +777,15 @@ extern "C" xk_status xk_prune_features(const xk_mesh* m, const double* u, const 
   if (!m || !old || (n > 0 && (!cands || !feat || !hist)) || n < 0)
     return xk_set_error(XK_ERR_ARG, "xk_prune_features: bad arguments");
   if (n == 0) return XK_OK;
-  k_features<<<xk_blocks(n, 256), 256, 0, (cudaStream_t)s>>>(*m, u, cands, n, *old, feat, hist);
-  XK_CHECK_LAUNCH();
+  cudaStream_t st = (cudaStream_t)s;
+  const long long ne = m->n_elems;
+  int32_t* ostart = nullptr;
+  XK_CUDA(cudaMallocAsync((void**)&ostart, sizeof(int32_t) * (ne + 2), st));
+  k_table_seg_start<<<xk_blocks(ne + 1, 256), 256, 0, st>>>(*old, ne, ostart);
+  k_features<<<xk_blocks(n, 256), 256, 0, st>>>(*m, u, cands, n, *old, ostart, feat, hist);
+  cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(ostart, st);
+  if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);
   return XK_OK;
 }
 

@@ -99,7 +99,7 @@ class ContactPattern(C.Structure):
                           "blk_ptr", "contrib")] + [("n_elems", C.c_int64), ("sides_ok", C.c_int64)] + [
         (n, vp) for n in ("node_elem_ptr", "node_elem", "elem_ptr", "elem_inc", "bcodes", "elem_sums",
                           "norm_scratch")] + [("nnzb_full", C.c_int64), ("low_ptr", vp), ("low_blk", vp),
-                                              ("sides_per_sm", C.c_int32), ("pad_launch", C.c_int32)]
+                                              ("sides_per_sm", C.c_int32), ("node_elem_ready", C.c_int32)]
 
 
 P = C.POINTER

@@ -159,7 +159,7 @@ class BlockTridiagonalSolver:
     """
 
     def __init__(self, engine, axis: int | None = None, *, factor_dtype=torch.float32, rtol: float = 1e-10,
-                 restart: int = 30, max_iter: int = 300, refactor_iters: int = 12):
+                 restart: int = 30, max_iter: int = 300, refactor_iters: int = 30):
         self.eng = engine
         dev = engine.device
         X = engine.mesh.X.reshape(-1, 3).cpu().numpy()
@@ -176,6 +176,7 @@ class BlockTridiagonalSolver:
         self.refactor_iters = int(refactor_iters)
         self._F = None  # the factors in use (fp32 copies or the FP64 blocks)
         self._need_factor = True
+        self._graphs = {}  # the apply of each factor buffer set, captured as a CUDA graph
         self._sysw = DeviceLinearSolver(engine)  # the xk_system view of the engine's matrices and its SpMV
         self.overflow = torch.zeros(1, dtype=torch.int32, device=dev)
         self.bn = 0
@@ -213,6 +214,7 @@ class BlockTridiagonalSolver:
             return  # same block layout: kept factors remain a valid preconditioner
         b = 6 * bn
         self._buf = self._fbuf = self._F = None
+        self._graphs = {}
         torch.cuda.empty_cache()
         dev = self.eng.device
         self._buf = tuple(torch.empty((nb, b, b), dtype=torch.float64, device=dev) for _ in range(3))
@@ -250,6 +252,25 @@ class BlockTridiagonalSolver:
         torch.cuda.synchronize(self.eng.device)
         self.stats["factor_s"] += time.perf_counter() - t0
 
+    def _apply_graph(self, F):
+        """(graph, input, output): ``blocktri_apply`` over the factor buffers F captured once as a CUDA
+        graph (its ~3 nb launches replayed together); valid while the buffers live, whatever they hold."""
+        key = F[0].data_ptr()
+        g = self._graphs.get(key)
+        if g is None:
+            x_in = torch.zeros((self.nb, 6 * self.bn, 1), dtype=F[0].dtype, device=F[0].device)
+            side = torch.cuda.Stream(device=F[0].device)
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                blocktri_apply(*F, x_in)  # warm-up outside the capture
+            torch.cuda.current_stream().wait_stream(side)
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                y = blocktri_apply(*F, x_in)
+            g = (graph, x_in, y)
+            self._graphs[key] = g
+        return g
+
     def __call__(self, backend, R: torch.Tensor, fixed: np.ndarray, mass_diag: torch.Tensor | None):
         self._sysw.set_fixed(fixed)
         self._prepare()
@@ -268,9 +289,9 @@ class BlockTridiagonalSolver:
             return y
 
         def precond(v):
-            rhs = torch.zeros(nb * b, dtype=torch.float64, device=v.device)
-            rhs[perm] = v
-            y = blocktri_apply(*self._F, rhs.view(nb, b, 1))
+            graph, x_in, y = self._apply_graph(self._F)
+            x_in.view(-1)[perm] = v.to(x_in.dtype)  # positions past the last node stay zero
+            graph.replay()
             return y.reshape(-1)[perm].to(torch.float64)
 
         rhs = torch.where(free, -R.to(torch.float64), zero)

@@ -20,6 +20,7 @@ so these drivers are this package's own, over the restated solver loop.
 
 from __future__ import annotations
 
+import dataclasses
 import math
 import time
 
@@ -131,16 +132,30 @@ def run_load_step(w, precision: str, *, layer: int, amount: float, settings: Sol
     return res, b, time.perf_counter() - t0
 
 
-def run_bend_oscillation(w, precision: str, *, kappa: float, dt: float = 1e-4, n_steps: int = 20,
-                         rho_inf: float = 0.9, rho: float = RHO_STEEL, bend_settings: SolverSettings | None = None,
-                         step_settings: SolverSettings | None = None, graph: bool = True, verbose: bool = False):
-    """Bend quasi-statically to the arc of curvature ``kappa`` (z = L wire ends driven to the arc's end
-    section, z = 0 ends clamped), then release the z = L ends and take ``n_steps`` Generalized-alpha steps
-    of ``dt`` from rest: the strand springs back in free oscillation, its contacts sliding and separating.
-    Each step is one solver run continuing from the last (integrator state and pair state carried over).
+def _closed(fracs) -> tuple:
+    """A followed schedule that ends short of 1 (the run it came from failed there) gets the full load as
+    its last increment, which then fails as well instead of being skipped."""
+    f = tuple(float(x) for x in fracs)
+    return f if f and abs(f[-1] - 1.0) <= 1e-12 else f + (1.0,)
 
-    Returns a dict: the displacements at the end of the bend and of every step, the Newton attempt counts,
-    the time spent in the solver runs and in the linear solves, and the assembly counts.
+
+def run_bend_oscillation(w, precision: str, *, kappa: float, dt: float = 1e-4, n_steps: int = 20,
+                         rho_inf: float = 0.9, rho: float = RHO_STEEL, bend_time: float | None = None,
+                         bend_settings: SolverSettings | None = None, step_settings: SolverSettings | None = None,
+                         follow: list | None = None, graph: bool = True, verbose: bool = False):
+    """Bend to the arc of curvature ``kappa`` (z = L wire ends driven to the arc's end section, z = 0 ends
+    clamped), then release the z = L ends and take ``n_steps`` Generalized-alpha steps of ``dt``: the strand
+    springs back in free oscillation, its contacts sliding and separating.  The bend is quasi-static
+    (``bend_time`` None) or a Generalized-alpha run of ``bend_time`` from rest whose end state (velocities
+    included) the oscillation continues.  Each oscillation step is one solver run continuing from the
+    last (integrator state and pair state carried over).  ``follow``: the ``schedule`` of an earlier run
+    (the load fractions of the bend's and of every step's increments), taken instead of the adaptive step
+    control (an increment that fails is cut back and the list then continues), so that two runs (FP64
+    and mixed) are compared at the same load fractions.
+
+    Returns a dict: the displacements at the end of the bend and of every step (and of every bend
+    increment), the schedule, the Newton attempt counts, the time spent in the solver runs and in the
+    linear solves, and the assembly counts.
     """
     eng = strand_engine(w, precision)
     st = w.strand
@@ -158,7 +173,7 @@ def run_bend_oscillation(w, precision: str, *, kappa: float, dt: float = 1e-4, n
         timing["solves"] += 1
         return du
 
-    out = {"u": [], "attempts": [], "step_s": []}
+    out = {"u": [], "attempts": [], "step_s": [], "increments": []}
 
     def finish(converged, t0):
         torch.cuda.synchronize()
@@ -171,27 +186,45 @@ def run_bend_oscillation(w, precision: str, *, kappa: float, dt: float = 1e-4, n
 
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    sol = ContactFrictionSolver(b, QuasiStatic(), t_total=1.0, fixed_dofs=fixed, prescribed_dofs=pd,
-                                prescribed_values=pv, settings=bend_settings or SolverSettings(dt_max_fraction=0.1),
-                                linear_solve=timed_solve, record_u=False, verbose=verbose)
+    ga = GpuGeneralizedAlpha(lumped_mass(eng, rho), rho_inf=rho_inf, device=eng.device)
+    if bend_time is None:
+        dyn, t_bend = QuasiStatic(), 1.0
+        bs = bend_settings or SolverSettings(dt_max_fraction=0.1)
+    else:
+        dyn, t_bend = ga, float(bend_time)
+        bs = bend_settings or SolverSettings(dt_max_fraction=min(1.0, dt / t_bend))
+    if follow is not None:
+        bs = dataclasses.replace(bs, load_schedule=_closed(follow[0]), schedule_cutbacks=True)
+    sol = ContactFrictionSolver(b, dyn, t_total=t_bend, fixed_dofs=fixed, prescribed_dofs=pd,
+                                prescribed_values=pv, settings=bs, linear_solve=timed_solve, record_u=True,
+                                verbose=verbose)
     res = sol.run()
-    out["bend"] = {"increments": res.n_increments, "attempts": res.total_attempts, "cutbacks": res.n_cutbacks}
+    out["bend"] = {"increments": res.n_increments, "attempts": res.total_attempts, "cutbacks": res.n_cutbacks,
+                   "converged": res.completed, "load_frac": [r.load_frac for r in res.increments]}
+    out["bend_u"] = [r.u for r in res.increments]
+    out["schedule"] = [[r.load_frac for r in res.increments]]
     out["u"].append(res.u.cpu().numpy())
     out["attempts"].append([r.attempts for r in res.increments])
-    if not res.converged:
+    if not res.completed:
         return finish(False, t0)
     torch.cuda.synchronize()
     out["bend_s"] = time.perf_counter() - t0
     u = res.u
-    ga = GpuGeneralizedAlpha(lumped_mass(eng, rho), rho_inf=rho_inf, device=eng.device)  # from rest
     clamped = fixed  # the z = L ends are released
-    for _ in range(n_steps):
+    for k in range(n_steps):
         ts = time.perf_counter()
-        sol = ContactFrictionSolver(b, ga, t_total=dt, fixed_dofs=clamped, settings=step_settings or SolverSettings(),
+        ss = step_settings or SolverSettings()
+        if follow is not None:
+            if k + 1 >= len(follow):
+                break
+            ss = dataclasses.replace(ss, load_schedule=_closed(follow[k + 1]), schedule_cutbacks=True)
+        sol = ContactFrictionSolver(b, ga, t_total=dt, fixed_dofs=clamped, settings=ss,
                                     linear_solve=timed_solve, record_u=False, verbose=verbose)
         r = sol.run(u)
         out["attempts"].append([x.attempts for x in r.increments])
-        if not r.converged:
+        out["increments"].append(r.n_increments)
+        out["schedule"].append([x.load_frac for x in r.increments])
+        if not r.completed:
             return finish(False, t0)
         u = r.u
         out["u"].append(u.cpu().numpy())

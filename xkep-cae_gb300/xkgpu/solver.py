@@ -150,15 +150,19 @@ class StepControl:
 
 
 class ScheduledSteps(StepControl):
-    """A fixed list of load fractions: no growth, no cutbacks (a failed increment ends the run).  Used to
-    put two runs on the same increments, e.g. the increments a reference run took."""
+    """A fixed list of load fractions: no growth.  Used to put two runs on the same increments, e.g. the
+    increments a reference run took.  A failed increment ends the run, or with ``cutbacks`` is retried
+    from a shrunk fraction (as ``StepControl.failure``), after which the list continues."""
 
-    def __init__(self, t_total: float, fractions):
+    def __init__(self, t_total: float, fractions, *, cutbacks: bool = False, min_frac: float = 0.0):
         super().__init__(t_total)
         fr = [float(f) for f in fractions]
         if not fr or any(b <= a for a, b in zip(fr, fr[1:])) or fr[0] <= 0.0 or abs(fr[-1] - 1.0) > 1e-12:
             raise ValueError("load schedule: increasing fractions in (0, 1], ending at 1")
         self.queue = deque(fr)
+        self.cutbacks = cutbacks
+        if min_frac > 0.0:
+            self.min_frac = min_frac
 
     def success(self, load_frac, load_frac_prev, n_attempts, n_active, prev_n_active) -> None:
         self._last_prev = load_frac
@@ -166,7 +170,13 @@ class ScheduledSteps(StepControl):
             self.queue.popleft()
 
     def failure(self, load_frac, load_frac_prev, diverged) -> bool:
-        return False
+        delta = load_frac - load_frac_prev
+        if not self.cutbacks or delta <= self.min_frac + 1e-15:
+            return False
+        self.n_cutbacks += 1
+        shrink = self.shrink * self.shrink if diverged else self.shrink
+        self.queue.appendleft(load_frac_prev + delta * shrink)  # the failed target stays next in line
+        return True
 
 
 # --------------------------------------------------------------------------- settings and results
@@ -195,8 +205,10 @@ class SolverSettings:
     # _newton_steps.py:229-235); 0 switches it off, so that only the force and displacement tests end
     # an increment (used where two runs are compared to a tighter tolerance than the energy test gives)
     energy_tol: float = 1e-10
-    # increments at exactly these load fractions (ScheduledSteps) instead of the adaptive control
+    # increments at exactly these load fractions (ScheduledSteps) instead of the adaptive control;
+    # with schedule_cutbacks a failed one is retried from a shrunk fraction
     load_schedule: tuple = ()
+    schedule_cutbacks: bool = False
 
 
 @dataclass
@@ -221,6 +233,12 @@ class SolverResult:
     n_cutbacks: int
     increments: list = field(default_factory=list)  # converged increments, in order
     attempts_log: list = field(default_factory=list)  # every increment tried, retries included
+
+    @property
+    def completed(self) -> bool:
+        """Converged through the full load.  ``converged`` alone is also True when the run stopped at
+        ``max_increments``, as the reference's is (``process.py:377-381,650-674``)."""
+        return self.converged and bool(self.increments) and self.increments[-1].load_frac >= 1.0 - 1e-12
 
 
 # --------------------------------------------------------------------------- linear solves
@@ -472,7 +490,8 @@ class ContactFrictionSolver:
             f_ext_ref_norm = 1.0
         t = self.t_total
         if cfg.load_schedule:
-            ctl = ScheduledSteps(t, cfg.load_schedule)
+            ctl = ScheduledSteps(t, cfg.load_schedule, cutbacks=cfg.schedule_cutbacks,
+                                 min_frac=cfg.dt_min_fraction)
         else:
             ctl = StepControl(t, t, cfg.dt_min_fraction * t if cfg.dt_min_fraction > 0 else t / 32.0,
                               cfg.dt_max_fraction * t if cfg.dt_max_fraction > 0 else t, cfg.dt_grow_factor,
