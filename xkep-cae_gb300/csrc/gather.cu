@@ -128,6 +128,20 @@ __global__ void __launch_bounds__(SEG_T) k_segment_sort(const int32_t* __restric
   if (lane + 32 < n) a[lo + r1] = v1;
 }
 
+// The same sort with a thread per segment (insertion in place), for many short segments: the contributor
+// lists of the blocks (a few entries each), where a warp per segment spends its time launching warps.
+__global__ void k_segment_sort_thread(const int32_t* __restrict__ ptr, long long nseg, int32_t* __restrict__ a) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nseg) return;
+  const int lo = ptr[v], hi = ptr[v + 1];
+  for (int x = lo + 1; x < hi; ++x) {
+    const int key = a[x];
+    int y = x - 1;
+    while (y >= lo && a[y] > key) { a[y + 1] = a[y]; --y; }
+    a[y + 1] = key;
+  }
+}
+
 // The distinct column nodes c >= v of row v, in ascending order, from its member incidences (the four nodes
 // of every member touching v).  A warp per node: the candidates (4 per incidence, at most RC_CAP) are staged
 // in shared memory, bitonic-sorted, and the first of each run of equal values >= v is kept (ballot
@@ -1142,7 +1156,7 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   XK_CUDA(cudaMemsetAsync(bfill, 0, sizeof(int32_t) * (nb + 1), st));
   if (nm > 0) k_contrib<1><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
                                                                 bfill, pat->blk_ptr, pat->contrib, err);
-  if (nb > 0) k_segment_sort<<<xk_blocks(32LL * nb, SEG_T), SEG_T, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
+  if (nb > 0) k_segment_sort_thread<<<xk_blocks(nb, 256), 256, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
   XK_CHECK_LAUNCH();
   // lower index of the stored blocks
   pat->nnzb_full = nb;

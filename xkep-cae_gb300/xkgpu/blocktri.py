@@ -217,6 +217,11 @@ class BlockTridiagonalSolver:
         self._graphs = {}
         torch.cuda.empty_cache()
         dev = self.eng.device
+        need = nb * b * b * (3 * 8 + (3 * 4 if self.factor_dtype != torch.float64 else 0))
+        if need > 0.5 * torch.cuda.mem_get_info(dev)[0]:
+            # a coupling across much of the mesh (a state far from a strand's): no block layout fits
+            self.bn, self.nb = 0, 0
+            return
         self._buf = tuple(torch.empty((nb, b, b), dtype=torch.float64, device=dev) for _ in range(3))
         if self.factor_dtype != torch.float64:
             self._fbuf = tuple(torch.empty((nb, b, b), dtype=self.factor_dtype, device=dev) for _ in range(3))
@@ -274,6 +279,9 @@ class BlockTridiagonalSolver:
     def __call__(self, backend, R: torch.Tensor, fixed: np.ndarray, mass_diag: torch.Tensor | None):
         self._sysw.set_fixed(fixed)
         self._prepare()
+        if self._buf is None:  # the layout would not fit in device memory: a failed solve (cutback)
+            self.stats["too_large"] = self.stats.get("too_large", 0) + 1
+            return None
         nb, b = self.nb, 6 * self.bn
         fresh = self._need_factor or self._F is None
         if fresh:
