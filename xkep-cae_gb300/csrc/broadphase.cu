@@ -3,11 +3,12 @@
 // The reference bins AABBs into a hash grid (xkep_cae/contact/_broadphase.py:52-87)
 // and keeps the pairs whose closed AABBs overlap (:93-96); its output is the
 // set of all overlapping pairs, whatever the cell size.  Here every segment is
-// binned once, by the cell of its box's lower corner (counting sort by cell).
+// binned once, by the cell of its box's lower corner (counting sort by cell, each cell's entries then
+// in ascending order).
 // A box j can overlap box i only if its lower corner lies in [lo_i - E, hi_i]
 // per axis, E the largest extent of any box on that axis, so a warp per
 // segment i walks the cells of that range (32 cells a batch) and tests every
-// entry j > i: screened on float boxes rounded outward, tested on the exact
+// entry j > i (found in each cell by a binary search): screened on float boxes rounded outward, tested on the exact
 // double AABBs, filtered, compacted with ballot/popc into a fixed-size slot list
 // of the segment.  Each pair is found once, from its lower-numbered segment, in
 // a single walk: a second kernel sorts each slot list and applies the midpoint
@@ -160,13 +161,27 @@ __global__ void k_cell_count(const double* __restrict__ box, long long ne, const
   atomicAdd(&ccnt[lin], 1);
 }
 
-// counting sort of the segments by cell (order within a cell is not used)
+// counting sort of the segments by cell, then each cell's entries in ascending order (a thread per cell;
+// cells of more than CELL_SORTED entries are left as they are)
 __global__ void k_cell_scatter(long long ne, const int32_t* __restrict__ ecell, const int32_t* __restrict__ cstart,
                                int32_t* __restrict__ cfill, int32_t* __restrict__ segs) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const int c = ecell[e];
   segs[cstart[c] + atomicAdd(&cfill[c], 1)] = (int32_t)e;
+}
+constexpr int CELL_SORTED = 64;  // cells with more entries stay unsorted (insertion sort by one thread)
+__global__ void k_cell_sort(long long ncell, const int32_t* __restrict__ cstart, int32_t* __restrict__ segs) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int lo = cstart[c], hi = cstart[c + 1];
+  if (hi - lo > CELL_SORTED) return;
+  for (int x = lo + 1; x < hi; ++x) {
+    const int key = segs[x];
+    int y = x - 1;
+    while (y >= lo && segs[y] > key) { segs[y + 1] = segs[y]; --y; }
+    segs[y + 1] = key;
+  }
 }
 
 // the FP64 boxes of i (registers) and j (six doubles at box + 6 j, 16-byte aligned) overlap, closed
@@ -186,7 +201,7 @@ XK_D bool overlap(const double (&bi)[6], const double* __restrict__ box, int j) 
 // segment i's slot list (the first `cap` of them; cnt[i] counts them all).  Also per segment: the sum
 // of r_i + r_j over its kept candidates (each lane sums its own entries in walk order, then a fixed
 // butterfly: rsum[i], for the prescreen margin), the raw overlap count and the longest list.
-__global__ void __launch_bounds__(BP_T, 8) k_sweep(xk_mesh m, const double* __restrict__ box,
+__global__ void __launch_bounds__(BP_T, 7) k_sweep(xk_mesh m, const double* __restrict__ box,
                                                 const float4* __restrict__ boxf, const Grid* __restrict__ gp,
                                                 const int32_t* __restrict__ segs, const int32_t* __restrict__ cstart,
                                                 int excl_shared, int excl_layer, int cap, int32_t* __restrict__ slot,
@@ -225,7 +240,17 @@ __global__ void __launch_bounds__(BP_T, 8) k_sweep(xk_mesh m, const double* __re
       const int x = c0[0] + q0 % sx, y = c0[1] + (q0 / sx) % sy, z = c0[2] + q0 / (sx * sy);
       const int lin = (int)(((long long)z * g.dims[1] + y) * g.dims[0] + x);
       s0 = cstart[lin];
-      n0 = cstart[lin + 1] - s0;
+      const int e0 = cstart[lin + 1];
+      // a cell of at most CELL_SORTED entries holds them in ascending order: only those past i can pair
+      // with it (each pair is taken from its lower-numbered segment); a larger one is walked whole
+      int lo = s0, hi = e0;
+      if (e0 - s0 <= CELL_SORTED)
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (segs[mid] <= i) lo = mid + 1; else hi = mid;
+        }
+      s0 = lo;
+      n0 = e0 - lo;
     }
     int incl = n0;
 #pragma unroll
@@ -236,10 +261,10 @@ __global__ void __launch_bounds__(BP_T, 8) k_sweep(xk_mesh m, const double* __re
     const int pre = incl - n0;
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const int nq = (ncell - cb) < 32 ? (ncell - cb) : 32;
-    for (int f0 = 0; f0 < total; f0 += 32) {
-      const int f = f0 + lane;
-      // the last cell q of the batch with pre_q <= f (cells without entries share their successor's offset)
-      int q = 0;
+    // two entries per lane and pass (f and f + 32), their loads issued together: half the dependent
+    // round trips of one entry per lane; each lane still meets its entries in increasing f
+    auto entry = [&](int f) {  // the segment at list position f of the batch, or -1
+      int q = 0;  // the last cell q of the batch with pre_q <= f (cells without entries share their successor's offset)
 #pragma unroll
       for (int step = 16; step > 0; step >>= 1) {
         const int cand = q + step;
@@ -248,33 +273,47 @@ __global__ void __launch_bounds__(BP_T, 8) k_sweep(xk_mesh m, const double* __re
       }
       const int sq = __shfl_sync(0xffffffffu, s0, q);
       const int pq = __shfl_sync(0xffffffffu, pre, q);
-      bool hit = false, kept = false;
-      int j = -1;
-      if (f < total) {
-        j = segs[sq + (f - pq)];
-        bool near = j > i;
-        if (near) {
-          const float4 jl = __ldg(boxf + 2LL * j), jh = __ldg(boxf + 2LL * j + 1);
-          near = il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z;
+      return f < total ? segs[sq + (f - pq)] : -1;
+    };
+    for (int f0 = 0; f0 < total; f0 += 64) {
+      const int jA = entry(f0 + lane), jB = entry(f0 + 32 + lane);
+      bool nearA = jA > i, nearB = jB > i;
+      float4 al = make_float4(0.f, 0.f, 0.f, 0.f), ah = al, bl = al, bh = al;
+      if (nearA) { al = __ldg(boxf + 2LL * jA); ah = __ldg(boxf + 2LL * jA + 1); }
+      if (nearB) { bl = __ldg(boxf + 2LL * jB); bh = __ldg(boxf + 2LL * jB + 1); }
+      nearA = nearA && il.x <= ah.x && al.x <= ih.x && il.y <= ah.y && al.y <= ih.y && il.z <= ah.z && al.z <= ih.z;
+      nearB = nearB && il.x <= bh.x && bl.x <= ih.x && il.y <= bh.y && bl.y <= ih.y && il.z <= bh.z && bl.z <= ih.z;
+      const bool hitA = nearA && overlap(bi, box, jA), hitB = nearB && overlap(bi, box, jB);
+      bool keptA = hitA, keptB = hitB;
+      if (excl_shared) {
+        if (keptA) {
+          const int ja = m.conn[2 * jA], jb = m.conn[2 * jA + 1];
+          if (ia == ja || ia == jb || ib == ja || ib == jb) keptA = false;
         }
-        if (near && overlap(bi, box, j)) {
-          hit = true;
-          kept = true;
-          if (excl_shared) {
-            const int ja = m.conn[2 * j], jb = m.conn[2 * j + 1];
-            if (ia == ja || ia == jb || ib == ja || ib == jb) kept = false;
-          }
-          if (kept && li >= 0 && m.layer[j] == li) kept = false;
+        if (keptB) {
+          const int ja = m.conn[2 * jB], jb = m.conn[2 * jB + 1];
+          if (ia == ja || ia == jb || ib == ja || ib == jb) keptB = false;
         }
       }
-      const unsigned bal = __ballot_sync(0xffffffffu, kept);
-      n_raw += __popc(__ballot_sync(0xffffffffu, hit));
-      if (kept) {
-        rs = xadd(rs, xadd(ri, m.radii[j]));  // this lane's entries, in walk order
-        const int at = n_keep + __popc(bal & ((1u << lane) - 1u));
-        if (at < cap) my[at] = j;
+      if (li >= 0) {
+        if (keptA && m.layer[jA] == li) keptA = false;
+        if (keptB && m.layer[jB] == li) keptB = false;
       }
-      n_keep += __popc(bal);
+      n_raw += __popc(__ballot_sync(0xffffffffu, hitA)) + __popc(__ballot_sync(0xffffffffu, hitB));
+      const unsigned balA = __ballot_sync(0xffffffffu, keptA), balB = __ballot_sync(0xffffffffu, keptB);
+      const unsigned below = (1u << lane) - 1u;
+      if (keptA) {
+        rs = xadd(rs, xadd(ri, m.radii[jA]));  // this lane's entries, in walk order
+        const int at = n_keep + __popc(balA & below);
+        if (at < cap) my[at] = jA;
+      }
+      n_keep += __popc(balA);
+      if (keptB) {
+        rs = xadd(rs, xadd(ri, m.radii[jB]));
+        const int at = n_keep + __popc(balB & below);
+        if (at < cap) my[at] = jB;
+      }
+      n_keep += __popc(balB);
     }
   }
 #pragma unroll
@@ -588,6 +627,7 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   XK_TRY(xk_exclusive_scan_i32(cfill, cstart, cap_cells + 1, nullptr, st));
   XK_CUDA(cudaMemsetAsync(cfill, 0, sizeof(int32_t) * (cap_cells + 1), st));
   k_cell_scatter<<<xk_blocks(ne, 256), 256, 0, st>>>(ne, ecell, cstart, cfill, segs);
+  k_cell_sort<<<xk_blocks(cap_cells, 256), 256, 0, st>>>(cap_cells, cstart, segs);
   XK_CHECK_LAUNCH();
   double *rsum, *part, *extra;
   int64_t* tot;

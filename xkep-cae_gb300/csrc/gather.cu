@@ -90,12 +90,7 @@ __global__ void k_inc_fill(const int32_t* __restrict__ mnodes, int nm, const int
 // broadcast by shuffles, then the warp writes them to their ranks; a longer segment is sorted by
 // insertion by one lane.
 constexpr int SEG_T = 128;
-__global__ void __launch_bounds__(SEG_T) k_segment_sort(const int32_t* __restrict__ ptr, long long nseg,
-                                                        int32_t* __restrict__ a) {
-  const long long v = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (v >= nseg) return;
-  const int lo = ptr[v], hi = ptr[v + 1];
+XK_D void warp_sort_segment(int lo, int hi, int32_t* __restrict__ a, int lane) {
   const int n = hi - lo;
   if (n <= 1) return;
   if (n > 64) {
@@ -128,12 +123,27 @@ __global__ void __launch_bounds__(SEG_T) k_segment_sort(const int32_t* __restric
   if (lane + 32 < n) a[lo + r1] = v1;
 }
 
-// The same sort with a thread per segment (insertion in place), for many short segments: the contributor
-// lists of the blocks (a few entries each), where a warp per segment spends its time launching warps.
-__global__ void k_segment_sort_thread(const int32_t* __restrict__ ptr, long long nseg, int32_t* __restrict__ a) {
+__global__ void __launch_bounds__(SEG_T) k_segment_sort(const int32_t* __restrict__ ptr, long long nseg,
+                                                        int32_t* __restrict__ a) {
+  const long long v = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (v >= nseg) return;
+  warp_sort_segment(ptr[v], ptr[v + 1], a, threadIdx.x & 31);
+}
+
+// The same sort for many short segments (the contributor lists of the blocks, a few entries each, where a
+// warp per segment spends its time on warps): a thread per segment sorts one of at most SEG_SHORT entries
+// by insertion in place and lists a longer one (a diagonal block, one entry per member at the node) for
+// k_segment_sort_listed, whose persistent warps take the listed segments in turn.
+constexpr int SEG_SHORT = 12;
+__global__ void k_segment_sort_short(const int32_t* __restrict__ ptr, long long nseg, int32_t* __restrict__ a,
+                                     int32_t* __restrict__ longs, int32_t* __restrict__ n_longs) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nseg) return;
   const int lo = ptr[v], hi = ptr[v + 1];
+  if (hi - lo > SEG_SHORT) {
+    longs[atomicAdd(n_longs, 1)] = (int)v;
+    return;
+  }
   for (int x = lo + 1; x < hi; ++x) {
     const int key = a[x];
     int y = x - 1;
@@ -142,13 +152,28 @@ __global__ void k_segment_sort_thread(const int32_t* __restrict__ ptr, long long
   }
 }
 
+__global__ void __launch_bounds__(SEG_T) k_segment_sort_listed(const int32_t* __restrict__ ptr,
+                                                               int32_t* __restrict__ a,
+                                                               const int32_t* __restrict__ longs,
+                                                               const int32_t* __restrict__ n_longs) {
+  const int n = *n_longs;
+  const int lane = threadIdx.x & 31;
+  const long long nw = (long long)gridDim.x * (SEG_T / 32);
+  for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += nw) {
+    const int v = longs[w];
+    warp_sort_segment(ptr[v], ptr[v + 1], a, lane);
+  }
+}
+
 // The distinct column nodes c >= v of row v, in ascending order, from its member incidences (the four nodes
-// of every member touching v).  A warp per node: the candidates (4 per incidence, at most RC_CAP) are staged
-// in shared memory, bitonic-sorted, and the first of each run of equal values >= v is kept (ballot
-// prefix).  MODE 0 counts them (rcnt[v]); MODE 1 writes them at rptr[v] (col, and v in brow).  A node with
-// more than RC_CAP candidates takes the serial path of one lane (insertion into a sorted local buffer of
-// MAX_COLS distinct columns; err bit 1 if that overflows).
-constexpr int RC_WARPS = 4, RC_CAP = 512;
+// of every member touching v).  A warp per node: the candidates >= v (4 per incidence, at most RC_CAP) go
+// into a per-warp open-addressing hash set in shared memory (twice the candidates' power of two, linear
+// probing, atomicCAS among the warp's lanes), which drops the repeats; the distinct values are gathered
+// by a ballot scan of the set and ranked: by shuffles when at most 64 (two per lane), else by a bitonic
+// sort in shared memory.  MODE 0 counts them (rcnt[v]); MODE 1 writes them at rptr[v] (col, and v in
+// brow).  A node with more than RC_CAP candidates takes the serial path of one lane (insertion into a
+// sorted local buffer of MAX_COLS distinct columns; err bit 1 if that overflows).
+constexpr int RC_WARPS = 4, RC_CAP = 512, RC_TAB = 2 * RC_CAP;
 XK_D int row_cols_serial(const int32_t* __restrict__ mnodes, const int32_t* __restrict__ inc, int x0, int x1, int v,
                          int* buf, int32_t* __restrict__ err) {
   int n = 0;
@@ -177,7 +202,8 @@ __global__ void __launch_bounds__(32 * RC_WARPS) k_row_cols(const int32_t* __res
                                                             const int32_t* __restrict__ rptr,
                                                             int32_t* __restrict__ col, int32_t* __restrict__ brow,
                                                             int32_t* __restrict__ err) {
-  __shared__ int sm[RC_WARPS][RC_CAP];
+  __shared__ int stab[RC_WARPS][RC_TAB];
+  __shared__ int slist[RC_WARPS][RC_CAP];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int v = blockIdx.x * RC_WARPS + wid;
   if (v >= n_nodes) return;
@@ -198,43 +224,79 @@ __global__ void __launch_bounds__(32 * RC_WARPS) k_row_cols(const int32_t* __res
     }
     return;
   }
-  int* a = sm[wid];
-  int N = 32;
-  while (N < nc) N <<= 1;
-  for (int i = lane; i < N; i += 32) {
-    int c = 0x7fffffff;
-    if (i < nc) c = mnodes[4LL * (inc[x0 + (i >> 2)] >> 2) + (i & 3)];
-    a[i] = c;
+  constexpr int EMPTY = -1;
+  int* t = stab[wid];
+  int* l = slist[wid];
+  int ts = 64;
+  while (ts < 2 * nc) ts <<= 1;  // a power of two, at least twice the candidates
+  for (int i = lane; i < ts; i += 32) t[i] = EMPTY;
+  __syncwarp();
+  for (int i = lane; i < nc; i += 32) {
+    const int c = mnodes[4LL * (inc[x0 + (i >> 2)] >> 2) + (i & 3)];
+    if (c < v) continue;
+    unsigned h = ((unsigned)c * 2654435761u) & (unsigned)(ts - 1);
+    while (true) {
+      const int o = atomicCAS(&t[h], EMPTY, c);
+      if (o == EMPTY || o == c) break;
+      h = (h + 1) & (unsigned)(ts - 1);
+    }
   }
+  __syncwarp();
+  int nd = 0;
+  const unsigned below = (1u << lane) - 1u;
+  for (int i0 = 0; i0 < ts; i0 += 32) {
+    const int x = t[i0 + lane];
+    const unsigned bal = __ballot_sync(0xffffffffu, x != EMPTY);
+    if (x != EMPTY) l[nd + __popc(bal & below)] = x;
+    nd += __popc(bal);
+  }
+  __syncwarp();
+  if (MODE == 0) {
+    if (lane == 0) rcnt[v] = nd;
+    return;
+  }
+  const int o = rptr[v];
+  if (nd <= 64) {  // ranks by shuffle-broadcast comparisons (the values are distinct)
+    const int v0 = lane < nd ? l[lane] : 0x7fffffff;
+    const int v1 = lane + 32 < nd ? l[lane + 32] : 0x7fffffff;
+    int r0 = 0, r1 = 0;
+    const int n0 = nd < 32 ? nd : 32;
+    for (int k = 0; k < n0; ++k) {
+      const int x = __shfl_sync(0xffffffffu, v0, k);
+      r0 += x < v0;
+      r1 += x < v1;
+    }
+    for (int k = 0; k < nd - 32; ++k) {
+      const int x = __shfl_sync(0xffffffffu, v1, k);
+      r0 += x < v0;
+      r1 += x < v1;
+    }
+    if (lane < nd) { col[o + r0] = v0; brow[o + r0] = v; }
+    if (lane + 32 < nd) { col[o + r1] = v1; brow[o + r1] = v; }
+    return;
+  }
+  int N = 32;
+  while (N < nd) N <<= 1;
+  for (int i = nd + lane; i < N; i += 32) l[i] = 0x7fffffff;
   __syncwarp();
   for (int k = 2; k <= N; k <<= 1)
     for (int j = k >> 1; j > 0; j >>= 1) {
       for (int i = lane; i < N; i += 32) {
         const int ixj = i ^ j;
         if (ixj > i) {
-          const int p = a[i], q = a[ixj];
+          const int p = l[i], q = l[ixj];
           if (((i & k) == 0) == (p > q)) {
-            a[i] = q;
-            a[ixj] = p;
+            l[i] = q;
+            l[ixj] = p;
           }
         }
       }
       __syncwarp();
     }
-  int at = 0;
-  for (int i0 = 0; i0 < N; i0 += 32) {
-    const int i = i0 + lane;
-    const int c = a[i];
-    const bool keep = c != 0x7fffffff && c >= v && (i == 0 || a[i - 1] != c);
-    const unsigned bal = __ballot_sync(0xffffffffu, keep);
-    if (MODE == 1 && keep) {
-      const int o = rptr[v] + at + __popc(bal & ((1u << lane) - 1u));
-      col[o] = c;
-      brow[o] = v;
-    }
-    at += __popc(bal);
+  for (int i = lane; i < nd; i += 32) {
+    col[o + i] = l[i];
+    brow[o + i] = v;
   }
-  if (MODE == 0 && lane == 0) rcnt[v] = at;
 }
 
 // Lower index: per node w, the stored blocks (v, w) with v < w in the order of v (MODE 0 counts).
@@ -1156,7 +1218,14 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
   XK_CUDA(cudaMemsetAsync(bfill, 0, sizeof(int32_t) * (nb + 1), st));
   if (nm > 0) k_contrib<1><<<xk_blocks(nm, 128), 128, 0, st>>>(pat->member_nodes, (int)nm, pat->row_ptr, pat->col,
                                                                 bfill, pat->blk_ptr, pat->contrib, err);
-  if (nb > 0) k_segment_sort_thread<<<xk_blocks(nb, 256), 256, 0, st>>>(pat->blk_ptr, nb, pat->contrib);
+  if (nb > 0) {
+    int32_t *longs, *n_longs;
+    XK_TRY(S.get(&longs, nb));
+    XK_TRY(S.get(&n_longs, 1));
+    XK_CUDA(cudaMemsetAsync(n_longs, 0, sizeof(int32_t), st));
+    k_segment_sort_short<<<xk_blocks(nb, 256), 256, 0, st>>>(pat->blk_ptr, nb, pat->contrib, longs, n_longs);
+    k_segment_sort_listed<<<xk_sm_count() * 8, SEG_T, 0, st>>>(pat->blk_ptr, pat->contrib, longs, n_longs);
+  }
   XK_CHECK_LAUNCH();
   // lower index of the stored blocks
   pat->nnzb_full = nb;
