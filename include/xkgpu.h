@@ -402,6 +402,9 @@ typedef struct {
   int32_t block;           /* threads per CTA of the other-pair and member kernels: a multiple of 32 up to
                               256, 0 = 256.  Results do not depend on it; an autotuner may choose it. */
   int32_t pad_launch;
+  int32_t* slot;           /* [cap] or NULL: the slot of each pair of the FP64 table (the inverse of pair),
+                              written by xk_pairs_to32, so that xk_pairs_from32 walks the table in its own
+                              order (its writes coalesce) */
 } xk_pairs32;
 
 /* Per iteration: node records for the mixed kernels from u (and u_ref, nullable). */

@@ -47,6 +47,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(L.Section) == 9 * 8
     assert C.sizeof(L.Mesh) == 8 + 6 * 8
     assert C.sizeof(L.Pairs) == 8 + 23 * 8
+    assert C.sizeof(L.Pairs32) == 16 + 26 * 8 + 2 * 4 + 8
     assert C.sizeof(L.BeamPlan) == 8 + 4 * 8 + 8 + 8
     assert C.sizeof(L.ContactParams) == 6 * 8 + 8 + 5 * 8
     assert C.sizeof(L.BPParams) == 8 + 3 * 4 + 4 + 8 + 8

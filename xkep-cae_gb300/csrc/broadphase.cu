@@ -76,7 +76,8 @@ __global__ void k_aabb(xk_mesh m, const double* __restrict__ u, double margin, d
       lax[c] = (unsigned long long)__double_as_longlong(extc);
       mx = fmax(mx, extc);
     }
-    boxf[2LL * e] = make_float4(lf[0], lf[1], lf[2], 0.f);
+    // the spare fourth word carries the element's layer (-1 without layers), read by the walk's filter
+    boxf[2LL * e] = make_float4(lf[0], lf[1], lf[2], __int_as_float(m.layer ? m.layer[e] : -1));
     boxf[2LL * e + 1] = make_float4(hf[0], hf[1], hf[2], 0.f);
     double4_32a me;
     me.x = ma[0];
@@ -184,6 +185,18 @@ __global__ void k_cell_sort(long long ncell, const int32_t* __restrict__ cstart,
   }
 }
 
+// the neighbouring floats above and below x (finite x): the outward-rounded float bounds lf <= lo, hf >= hi
+// of a box satisfy lo <= up1(lf) and hi >= dn1(hf), so boxes whose up1/dn1-shrunk float bounds overlap
+// certainly overlap in FP64 as well
+XK_D float up1(float x) {
+  const int b = __float_as_int(x);
+  return __int_as_float(x == 0.f ? 1 : (x > 0.f ? b + 1 : b - 1));
+}
+XK_D float dn1(float x) {
+  const int b = __float_as_int(x);
+  return __int_as_float(x == 0.f ? (int)0x80000001 : (x > 0.f ? b - 1 : b + 1));
+}
+
 // the FP64 boxes of i (registers) and j (six doubles at box + 6 j, 16-byte aligned) overlap, closed
 XK_D bool overlap(const double (&bi)[6], const double* __restrict__ box, int j) {
   const double2* bj = reinterpret_cast<const double2*>(box + 6LL * j);
@@ -228,6 +241,8 @@ __global__ void __launch_bounds__(BP_T, 7) k_sweep(xk_mesh m, const double* __re
   const int ia = m.conn[2 * i], ib = m.conn[2 * i + 1];
   const int li = (excl_layer && m.layer) ? m.layer[i] : -1;
   const float4 il = boxf[2LL * i], ih = boxf[2LL * i + 1];
+  const float iux = up1(il.x), iuy = up1(il.y), iuz = up1(il.z);  // box i shrunk to within its FP64 bounds
+  const float idx_ = dn1(ih.x), idy = dn1(ih.y), idz = dn1(ih.z);
   const double ri = m.radii[i];
   int32_t* const my = slot + (long long)i * cap;
   int n_raw = 0, n_keep = 0;
@@ -275,29 +290,32 @@ __global__ void __launch_bounds__(BP_T, 7) k_sweep(xk_mesh m, const double* __re
       const int pq = __shfl_sync(0xffffffffu, pre, q);
       return f < total ? segs[sq + (f - pq)] : -1;
     };
+    const int2* conn2 = reinterpret_cast<const int2*>(m.conn);
+    // an outward float overlap is an FP64 overlap when the boxes shrunk by one float step still overlap;
+    // only the rare pair between the two takes the FP64 boxes
+    auto hit_of = [&](int j, const float4& jl, const float4& jh) {
+      if (!(il.x <= jh.x && jl.x <= ih.x && il.y <= jh.y && jl.y <= ih.y && il.z <= jh.z && jl.z <= ih.z))
+        return false;
+      const bool sure = iux <= dn1(jh.x) && up1(jl.x) <= idx_ && iuy <= dn1(jh.y) && up1(jl.y) <= idy &&
+                        iuz <= dn1(jh.z) && up1(jl.z) <= idz;
+      return sure || overlap(bi, box, j);
+    };
     for (int f0 = 0; f0 < total; f0 += 64) {
       const int jA = entry(f0 + lane), jB = entry(f0 + 32 + lane);
-      bool nearA = jA > i, nearB = jB > i;
+      const bool nearA = jA > i, nearB = jB > i;
       float4 al = make_float4(0.f, 0.f, 0.f, 0.f), ah = al, bl = al, bh = al;
-      if (nearA) { al = __ldg(boxf + 2LL * jA); ah = __ldg(boxf + 2LL * jA + 1); }
-      if (nearB) { bl = __ldg(boxf + 2LL * jB); bh = __ldg(boxf + 2LL * jB + 1); }
-      nearA = nearA && il.x <= ah.x && al.x <= ih.x && il.y <= ah.y && al.y <= ih.y && il.z <= ah.z && al.z <= ih.z;
-      nearB = nearB && il.x <= bh.x && bl.x <= ih.x && il.y <= bh.y && bl.y <= ih.y && il.z <= bh.z && bl.z <= ih.z;
-      const bool hitA = nearA && overlap(bi, box, jA), hitB = nearB && overlap(bi, box, jB);
+      int2 ca = make_int2(-1, -1), cb2 = ca;
+      if (nearA) { al = __ldg(boxf + 2LL * jA); ah = __ldg(boxf + 2LL * jA + 1); ca = __ldg(conn2 + jA); }
+      if (nearB) { bl = __ldg(boxf + 2LL * jB); bh = __ldg(boxf + 2LL * jB + 1); cb2 = __ldg(conn2 + jB); }
+      const bool hitA = nearA && hit_of(jA, al, ah), hitB = nearB && hit_of(jB, bl, bh);
       bool keptA = hitA, keptB = hitB;
       if (excl_shared) {
-        if (keptA) {
-          const int ja = m.conn[2 * jA], jb = m.conn[2 * jA + 1];
-          if (ia == ja || ia == jb || ib == ja || ib == jb) keptA = false;
-        }
-        if (keptB) {
-          const int ja = m.conn[2 * jB], jb = m.conn[2 * jB + 1];
-          if (ia == ja || ia == jb || ib == ja || ib == jb) keptB = false;
-        }
+        if (ia == ca.x || ia == ca.y || ib == ca.x || ib == ca.y) keptA = false;
+        if (ia == cb2.x || ia == cb2.y || ib == cb2.x || ib == cb2.y) keptB = false;
       }
       if (li >= 0) {
-        if (keptA && m.layer[jA] == li) keptA = false;
-        if (keptB && m.layer[jB] == li) keptB = false;
+        if (__float_as_int(al.w) == li) keptA = false;
+        if (__float_as_int(bl.w) == li) keptB = false;
       }
       n_raw += __popc(__ballot_sync(0xffffffffu, hitA)) + __popc(__ballot_sync(0xffffffffu, hitB));
       const unsigned balA = __ballot_sync(0xffffffffu, keptA), balB = __ballot_sync(0xffffffffu, keptB);
@@ -381,7 +399,32 @@ __global__ void __launch_bounds__(BP_T) k_slots_rank(xk_mesh m, const double4_32
   const double ri = m.radii[i];
   const double ex = extra ? *extra : 0.0;
   int kept = 0;
-  for (int l = lane; l < n; l += 32) {
+  if (n <= 64) {  // two entries per lane, ranked by shuffle-broadcast comparisons
+    const int v0 = lane < n ? my[lane] : 0x7fffffff;
+    const int v1 = lane + 32 < n ? my[lane + 32] : 0x7fffffff;
+    int r0 = 0, r1 = 0;
+    const int n0 = n < 32 ? n : 32;
+    for (int k = 0; k < n0; ++k) {
+      const int x = __shfl_sync(0xffffffffu, v0, k);
+      r0 += x < v0;
+      r1 += x < v1;
+    }
+    for (int k = 0; k < n - 32; ++k) {
+      const int x = __shfl_sync(0xffffffffu, v1, k);
+      r0 += x < v0;
+      r1 += x < v1;
+    }
+    if (lane < n) {
+      const bool k = !extra || midpoint_keep(mi, mid[v0], ri, m.radii[v0], ex);
+      out[r0] = k ? v0 : ~v0;
+      kept += k;
+    }
+    if (lane + 32 < n) {
+      const bool k = !extra || midpoint_keep(mi, mid[v1], ri, m.radii[v1], ex);
+      out[r1] = k ? v1 : ~v1;
+      kept += k;
+    }
+  } else for (int l = lane; l < n; l += 32) {
     const int v = my[l];
     int r = 0;
     for (int q = 0; q < n; ++q) r += my[q] < v;

@@ -1241,9 +1241,7 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
     k_segment_sort<<<xk_blocks(32LL * nn, SEG_T), SEG_T, 0, st>>>(pat->low_ptr, nn, pat->low_blk);
     XK_CHECK_LAUNCH();
   }
-  XK_TRY(fetch_i64(tot, h, 4, st));
-  pat->n_contrib = h[2];
-  if (pat->low_ptr && pat->low_blk) pat->nnzb_full = nb + h[3];
+  // the contribution and lower-index totals are read with the final synchronisation
   // element-side form (gather variant XK_GATHER_SIDES)
   const bool sides = pat->node_elem_ptr && pat->node_elem && pat->elem_ptr && pat->elem_inc && pat->bcodes;
   int32_t herr2 = 0;
@@ -1295,7 +1293,10 @@ extern "C" xk_status xk_contact_pattern_build(const xk_mesh* m, const xk_pairs* 
     XK_CUDA(cudaMemcpyAsync(&herr2, serr, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   }
   XK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  XK_CUDA(cudaMemcpyAsync(h + 2, tot + 2, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   XK_CUDA(cudaStreamSynchronize(st));
+  pat->n_contrib = h[2];
+  if (pat->low_ptr && pat->low_blk) pat->nnzb_full = nb + h[3];
   if (sides) {
     pat->sides_ok = herr2 ? 0 : 1;
     pat->node_elem_ready = 1;

@@ -635,6 +635,7 @@ __global__ void k_pairs_to32(xk_mesh m, xk_pairs p, xk_contact_pattern pat, xk_p
   const int i = mem ? pat.members[j] : pat.others[j - pat.n_members];
   const long long cp = p.cap, cq = q.cap;
   q.pair[j] = i;
+  if (q.slot) q.slot[i] = j;
   const int ea = p.ea[i], eb = p.eb[i];
   q.nodes[4LL * j] = m.conn[2 * ea];
   q.nodes[4LL * j + 1] = m.conn[2 * ea + 1];
@@ -669,10 +670,14 @@ __global__ void k_pairs_to32(xk_mesh m, xk_pairs p, xk_contact_pattern pat, xk_p
   if (q.mu && m.mu) q.mu[j] = (float)m.mu[ea];
 }
 
+// BY_PAIR: a thread per pair i of the FP64 table (j from q.slot; the writes coalesce, and the reads come
+// from two ascending runs of slots, members' and others'); else a thread per slot j
+template <bool BY_PAIR>
 __global__ void k_pairs_from32(xk_pairs32 q, xk_pairs p) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= q.n) return;
-  const int i = q.pair[j];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= q.n) return;
+  const int j = BY_PAIR ? q.slot[t] : t;
+  const int i = BY_PAIR ? t : q.pair[j];
   const long long cp = p.cap, cq = q.cap;
   p.s[i] = q.s[j]; p.t[i] = q.t[j]; p.gap[i] = q.gap[j];
   float n[3], t1[3], t2[3];
@@ -1511,7 +1516,10 @@ extern "C" xk_status xk_pairs_from32(const xk_pairs32* q, xk_pairs* p, xk_stream
   if (!q || !p) return xk_set_error(XK_ERR_ARG, "xk_pairs_from32: null argument");
   if (q->n != p->n) return xk_set_error(XK_ERR_ARG, "xk_pairs_from32: table sizes differ");
   if (q->n == 0) return XK_OK;
-  k_pairs_from32<<<xk_blocks(q->n, 256), 256, 0, (cudaStream_t)s>>>(*q, *p);
+  if (q->slot)
+    k_pairs_from32<true><<<xk_blocks(q->n, 256), 256, 0, (cudaStream_t)s>>>(*q, *p);
+  else
+    k_pairs_from32<false><<<xk_blocks(q->n, 256), 256, 0, (cudaStream_t)s>>>(*q, *p);
   XK_CHECK_LAUNCH();
   return XK_OK;
 }

@@ -65,7 +65,8 @@ class Pairs32(C.Structure):
     _fields_ = [("n", C.c_int32), ("cap", C.c_int32), ("n_members", C.c_int32)] + [
         (n, vp) for n in ("pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
                           "dissipation", "k_pen", "k_t", "status", "stick", "mu")] + [
-        (n, vp) for n in COAT32_FIELDS] + [("defer", vp), ("block", C.c_int32), ("pad_launch", C.c_int32)]
+        (n, vp) for n in COAT32_FIELDS] + [("defer", vp), ("block", C.c_int32), ("pad_launch", C.c_int32),
+                                           ("slot", vp)]
 
 
 class BeamPlan(C.Structure):

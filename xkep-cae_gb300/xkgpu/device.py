@@ -423,6 +423,7 @@ class DevicePairTable32:
         t["stick"] = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         t["mu"] = torch.zeros(cap, dtype=torch.float32, device=self.device) if self.per_slot_mu else None
         t["defer"] = torch.zeros(2 * (cap + 2), dtype=torch.int32, device=self.device)
+        t["slot"] = torch.zeros(cap, dtype=torch.int32, device=self.device)
         if self.coating:
             for k, w in (("coat_total", 1), ("coat_cc", 1), ("coat_cc_prev", 1), ("coat_z_t", 2), ("coat_qtn", 1),
                          ("coat_diss", 1)):
@@ -434,6 +435,7 @@ class DevicePairTable32:
             "pair", "nodes", "rad", "s", "t", "gap", "normal", "t1", "t2", "p_n", "z_t", "q_trial_norm",
             "dissipation", "k_pen", "k_t", "status", "stick", "mu")), *(ptr(t.get(k)) for k in L.COAT32_FIELDS),
             ptr(t["defer"]))
+        self.c.slot = ptr(t["slot"])
 
 
 # ----------------------------------------------------------------------------- contact pattern
