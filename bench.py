@@ -551,43 +551,60 @@ def c2_section(args, dev) -> dict:
     return out
 
 
-def c3_section(args, dev, n_steps: int = 20) -> dict:
-    """The 91-wire strand bent quasi-statically to curvature 1/(50 D), then released: 20 Generalized-alpha
-    steps (rho_inf 0.9, dt = 1e-4 s) of its free oscillation from rest; mu = 0.1, the reference's default
-    penalty 0.1 * 12 EI / L^3, graph-replayed assembly, device block solve; FP64 and mixed over the same
-    steps."""
+def _c3_run(nw: int, n_pitches: int, n_steps: int, max_increments: int = 0) -> dict:
+    """One bend-and-release run of the reference's solver loop in FP64, then in mixed precision on the FP64
+    run's increments; displacements compared at every common increment and at the end of every step."""
     import torch
 
     from xkgpu import runs
     from xkgpu import solver as S
     from xkgpu import workloads as W
 
-    out = {}
-    us = {}
+    w = W.strand_workload(f"strand{nw}", nw, 2.0, 40.0, n_pitches, 32, gap_frac=0.0, seed=0, penalty="beam_ei")
+    D = 2.0 * max(x.lay_radius for x in w.strand.wires) + w.meta["d"]
+    cfg = dict(dt_min_fraction=1e-3, max_nr_attempts=100, use_line_search=False, max_increments=max_increments,
+               tol_force=1e-6)
+    kw = dict(kappa=1.0 / (50.0 * D), n_steps=n_steps, bend_time=2e-3,
+              bend_settings=S.SolverSettings(dt_max_fraction=0.05, **cfg), step_settings=S.SolverSettings(**cfg))
+    out, res = {}, {}
+    follow = None
     for prec in ("fp64", "mixed"):
-        w = W.strand_workload("strand91", 91, 2.0, 40.0, 4, 32, gap_frac=0.0, seed=0, penalty="beam_ei")
-        D = 2.0 * max(x.lay_radius for x in w.strand.wires) + w.meta["d"]
-        cfg = dict(dt_min_fraction=1e-3, max_nr_attempts=100, use_line_search=False)
-        r = runs.run_bend_oscillation(w, prec, kappa=1.0 / (50.0 * D), n_steps=n_steps,
-                                      bend_settings=S.SolverSettings(dt_max_fraction=0.1, **cfg),
-                                      step_settings=S.SolverSettings(**cfg))
+        r = runs.run_bend_oscillation(w, prec, follow=follow, **kw)
+        follow = r["schedule"] if follow is None else follow
         n_it = r["counts"]["assemble"]
-        steps = r["attempts"][1:]
-        out[prec] = {"converged": r["converged"], "bend": r.get("bend"), "bend_s": r.get("bend_s"),
-                     "newton_attempts_per_step": [sum(a) for a in steps], "step_ms": [1e3 * t for t in r["step_s"]],
-                     "wall_s": r["wall_s"], "solve_s": r["solve_s"], "solves": r["solves"],
-                     "assemblies": n_it, "ms_per_newton_iteration": 1e3 * r["wall_s"] / max(n_it, 1),
-                     "ms_per_iteration_without_solve": 1e3 * (r["wall_s"] - r["solve_s"]) / max(n_it, 1),
-                     "solver": r.get("lin")}
-        us[prec] = r["u"]
+        out[prec] = {"completed": r["converged"], "bend": {k: r["bend"][k] for k in ("increments", "attempts", "cutbacks",
+                                                                                      "converged")},
+                     "bend_reached": r["bend"]["load_frac"][-1] if r["bend"]["load_frac"] else 0.0,
+                     "steps_done": len(r["step_s"]), "newton_iterations": n_it,
+                     "attempts_per_step": [sum(a) for a in r["attempts"][1:]],
+                     "ms_per_newton_iteration": 1e3 * r["wall_s"] / max(n_it, 1),
+                     "ms_per_iteration_without_linear_solve": 1e3 * (r["wall_s"] - r["solve_s"]) / max(n_it, 1),
+                     "wall_s": r["wall_s"], "linear_solve_s": r["solve_s"], "linear_solver": r.get("lin")}
+        res[prec] = r
         torch.cuda.empty_cache()
-    n = min(len(us["fp64"]), len(us["mixed"]))
-    out["workload"] = (f"strand91 (91 wires, d 2 mm, pitch 40 mm, 4 pitches, 32 el/pitch, gap at the minimum safe "
-                       f"lay gap), curvature 1/(50 D), D = {D:.2f} mm; k_pen = 0.1 * 12 EI / L^3 = {w.k_pen:.4g} N/mm; "
-                       f"line search off, at most 100 attempts")
-    out["u_rel_diff_mixed_vs_fp64"] = [float(np.abs(us["mixed"][k] - us["fp64"][k]).max()
-                                             / np.abs(us["fp64"][k]).max()) for k in range(n)]
+    a, b = res["fp64"], res["mixed"]
+    fa = {round(f, 12): k for k, f in enumerate(a["bend"]["load_frac"])}
+    common = [(fa[round(f, 12)], k) for k, f in enumerate(b["bend"]["load_frac"]) if round(f, 12) in fa]
+    db = [float(np.abs(b["bend_u"][kb] - a["bend_u"][ka]).max() / max(np.abs(a["bend_u"][ka]).max(), 1e-300))
+          for ka, kb in common]
+    n = min(len(a["u"]), len(b["u"]))
+    ds = [float(np.abs(b["u"][k] - a["u"][k]).max() / max(np.abs(a["u"][k]).max(), 1e-300)) for k in range(n)]
+    out["workload"] = (f"strand{nw}: {nw} wires, d 2 mm, pitch 40 mm, {n_pitches} pitch(es), 32 el/pitch, at the "
+                       f"minimum safe lay gap; bent over 2 ms of Generalized-alpha (rho_inf 0.9) to curvature "
+                       f"1/(50 D), D = {D:.2f} mm, then released for {n_steps} steps of 1e-4 s; mu 0.1; k_pen = "
+                       f"0.1 * 12 EI / L^3 = {w.k_pen:.4g} N/mm (the reference's default penalty); line search off, at "
+                       f"most 100 attempts, force tolerance 1e-6; mixed follows the FP64 run's increments")
+    out["u_rel_diff_mixed_vs_fp64"] = {"bend_increments": db, "max_bend": max(db) if db else None,
+                                       "steps": ds, "max_steps": max(ds) if ds else None}
     return out
+
+
+def c3_section(args, dev) -> dict:
+    """The 91-wire configuration's bending run (Generalized-alpha bend to curvature 1/(50 D), then 20 steps of
+    free oscillation, mu 0.1, graph-replayed assembly, device block solve), FP64 and mixed, on the strand of
+    the configuration (91 wires, 4 pitches, as far as the reference's loop carries it: 14 increments at most)
+    and in full on a 19-wire strand of one pitch."""
+    return {"strand91": _c3_run(91, 4, 20, max_increments=14), "strand19_full": _c3_run(19, 1, 20)}
 
 
 def batch_section(args, dev):
@@ -1114,7 +1131,16 @@ def run_profile(args):
     eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision=args.profile, **w.engine_kwargs())
     u0 = torch.as_tensor(w.u, device="cuda")
     u1 = u0 * 1.001
-    stats = eng.detect(u0)
+    for k in range(args.detections):
+        # the last detection (steady state: the table merged into itself) in an NVTX range "detect", for
+        # ncu --nvtx --nvtx-include "detect/"
+        if k == args.detections - 1:
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push("detect")
+        stats = eng.detect(u0)
+        if k == args.detections - 1:
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_pop()
     if args.schedule != "auto":  # a fixed tangent schedule (the autotuner's timings are distorted under ncu)
         eng.gather_variant = {"lanes": L.XK_GATHER_LANES, "chunks": L.XK_GATHER_CHUNKS,
                               "sides": L.XK_GATHER_SIDES}[args.schedule]
@@ -1211,10 +1237,12 @@ def main():
                                                         "oscillation), several minutes")
     ap.add_argument("--mlp-n", type=int, default=8_000_000, help="samples scored by --profile mlp")
     ap.add_argument("--profile", choices=["mixed", "fp64", "mlp"], default=None,
-                    help="profiling driver: detect once, then --steps eager assemblies, no timing")
+                    help="profiling driver: --detections detections, then --steps eager assemblies, no timing")
     ap.add_argument("--breakdown", action="store_true", help="warm per-phase times (ms) of one assembly")
     ap.add_argument("--schedule", choices=["auto", "lanes", "chunks", "sides"], default="auto",
                     help="tangent schedule of --profile (auto: the autotuner's choice)")
+    ap.add_argument("--detections", type=int, default=1,
+                    help="detections of --profile; the last one runs in the NVTX range 'detect'")
     args = ap.parse_args()
     if args.breakdown:
         run_breakdown(args)

@@ -251,6 +251,9 @@ class AssemblyEngine:
         else:
             L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), C.byref(self.cp), 1, s)
         self.pattern.build(self.pairs, stream)
+        # read while the stream is idle after the pattern build, before the float copy is queued, so that
+        # detect returns without waiting for it
+        n_exact = int(self._n_exact.item()) if screened else self.pairs.n
         if self.precision == L.XK_MIXED:
             self._to32(s)
         if (self.rec.numel() != L.REC_STRIDE[L.XK_OUT_COMBINED] * self.pattern.cap_members
@@ -260,7 +263,7 @@ class AssemblyEngine:
         self.stats = {"raw": n_raw, "prefilter": n_pre, "candidates": n_all, "kept_candidates": nc,
                       "pairs": self.pairs.n, "members": self.pattern.n_members, "contact_blocks": self.pattern.nnzb,
                       "contact_blocks_full": self.pattern.nnzb_full,
-                      "narrowphase_exact": int(self._n_exact.item()) if screened else self.pairs.n}
+                      "narrowphase_exact": n_exact}
         return self.stats
 
     # ------------------------------------------------------------------ per iteration

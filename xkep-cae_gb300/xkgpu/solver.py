@@ -521,9 +521,15 @@ class ContactFrictionSolver:
                     u = torch.as_tensor(u, dtype=torch.float64, device=dev)
             if self.pd.numel():
                 u[self.pd] = self.p0 + lf * (self.pv - self.p0)
-            b.detect(u)
-            ok, att, n_active, f_c, hist, kind, diverged = self._newton(u, u_ref, f_ext, dt_sub, f_ext_ref_norm,
-                                                                        dynamic_ref)
+            try:
+                b.detect(u)
+            except L.XkError:
+                # a state the engine cannot take (e.g. a node in contact with more nodes than a pattern row
+                # holds), reached from a bad prediction: the increment fails like a diverged one
+                ok, att, n_active, f_c, hist, kind, diverged = False, 0, 0, None, [math.inf], "detection failed", True
+            else:
+                ok, att, n_active, f_c, hist, kind, diverged = self._newton(u, u_ref, f_ext, dt_sub,
+                                                                            f_ext_ref_norm, dynamic_ref)
             total += att
             rec = IncrementRecord(increment, lf, dt_sub, ok, att, n_active, hist, kind)
             out.attempts_log.append(rec)
