@@ -120,20 +120,121 @@ __global__ void k_tile_scan(const TI* __restrict__ in, TO* __restrict__ out, lon
   }
 }
 
+// One-pass scan with decoupled look-back (Merrill and Garland, "Single-pass Parallel Prefix Scan with
+// Decoupled Look-back", NVIDIA technical report NVR-2016-002).  Tiles take their index from a ticket
+// counter in the order they start, so a tile waits only on tiles that are already running and never on a
+// later one.  Each tile publishes its aggregate (flag 1), then walks back over its predecessors, adding
+// aggregates until it meets an inclusive prefix (flag 2), and publishes its own inclusive prefix.  The wait
+// on a predecessor that has not published yet is bounded: past SCAN_SPIN_LIMIT polls the tile sums the
+// inputs before it itself (the same prefix, in a fixed order), so the result never depends on the wait.
+constexpr int SCAN_SPIN_LIMIT = 1 << 20;
+
+template <typename TI, typename TO>
+__global__ void __launch_bounds__(SCAN_T) k_scan_onepass(const TI* __restrict__ in, TO* __restrict__ out,
+                                                         long long n, long long nb, int64_t* __restrict__ total,
+                                                         int64_t* __restrict__ agg, int64_t* __restrict__ inc,
+                                                         int* __restrict__ flag, unsigned* __restrict__ ticket) {
+  __shared__ int64_t wt[SCAN_T / 32];
+  __shared__ long long s_tile;
+  __shared__ int64_t s_prefix;
+  __shared__ int s_fallback;
+  if (threadIdx.x == 0) {
+    s_tile = (long long)atomicAdd(ticket, 1u);
+    s_fallback = 0;
+  }
+  __syncthreads();
+  const long long t = s_tile;
+  const long long base = t * SCAN_TILE + (long long)threadIdx.x * SCAN_I;
+  int64_t loc[SCAN_I];
+  int64_t s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_I; ++i) {
+    loc[i] = (base + i < n) ? (int64_t)in[base + i] : 0;
+    s += loc[i];
+  }
+  int64_t tile_tot;
+  int64_t ex = block_exclusive_scan<int64_t>(s, wt, &tile_tot);
+  if (threadIdx.x == 0) {
+    if (t == 0) {
+      inc[0] = tile_tot;
+      __threadfence();
+      atomicExch(&flag[0], 2);
+      s_prefix = 0;
+    } else {
+      agg[t] = tile_tot;
+      __threadfence();
+      atomicExch(&flag[t], 1);
+      int64_t p = 0;
+      long long j = t - 1;
+      int spins = 0;
+      while (j >= 0) {
+        const int f = atomicAdd(&flag[j], 0);
+        if (f == 0) {
+          if (++spins > SCAN_SPIN_LIMIT) {
+            s_fallback = 1;
+            break;
+          }
+          continue;
+        }
+        __threadfence();
+        if (f == 2) {  // published values are read past L1 (other tiles' lines may sit there stale)
+          p += __ldcg(inc + j);
+          break;
+        }
+        p += __ldcg(agg + j);
+        --j;
+      }
+      if (!s_fallback) {
+        inc[t] = p + tile_tot;
+        __threadfence();
+        atomicExch(&flag[t], 2);
+        s_prefix = p;
+      }
+    }
+  }
+  __syncthreads();
+  if (s_fallback) {  // the prefix from the inputs before this tile
+    int64_t q = 0;
+    for (long long k = threadIdx.x; k < t * SCAN_TILE; k += SCAN_T) q += (int64_t)in[k];
+    int64_t all;
+    block_exclusive_scan<int64_t>(q, wt, &all);
+    if (threadIdx.x == 0) {
+      s_prefix = all;
+      inc[t] = all + tile_tot;
+      __threadfence();
+      atomicExch(&flag[t], 2);
+    }
+    __syncthreads();
+  }
+  ex += s_prefix;
+#pragma unroll
+  for (int i = 0; i < SCAN_I; ++i) {
+    if (base + i < n) out[base + i] = (TO)ex;
+    ex += loc[i];
+  }
+  if (t == nb - 1 && threadIdx.x == 0 && total) *total = s_prefix + tile_tot;
+}
+
 template <typename TI, typename TO>
 xk_status scan_impl(const TI* in, TO* out, long long n, int64_t* total_dev, cudaStream_t s) {
   if (n <= 0) {
     if (total_dev) XK_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int64_t), s));
     return XK_OK;
   }
-  long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-  int64_t* bsum = nullptr;
-  XK_CUDA(cudaMallocAsync((void**)&bsum, sizeof(int64_t) * nb, s));
-  k_tile_sums<TI><<<(unsigned)nb, SCAN_T, 0, s>>>(in, n, bsum);
-  k_scan_bsums<<<1, SCAN_T, 0, s>>>(bsum, nb, total_dev);
-  k_tile_scan<TI, TO><<<(unsigned)nb, SCAN_T, 0, s>>>(in, out, n, bsum);
-  cudaError_t e = cudaGetLastError();
-  cudaFreeAsync(bsum, s);
+  const long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  // one allocation: aggregates, inclusive prefixes, then the flags and the ticket (zeroed)
+  char* buf = nullptr;
+  const size_t words = sizeof(int64_t) * 2 * nb, tail = sizeof(int) * (nb + 1);
+  XK_CUDA(cudaMallocAsync((void**)&buf, words + tail, s));
+  int64_t* agg = reinterpret_cast<int64_t*>(buf);
+  int* flag = reinterpret_cast<int*>(buf + words);
+  cudaError_t e = cudaMemsetAsync(flag, 0, tail, s);
+  if (e == cudaSuccess) {
+    k_scan_onepass<TI, TO><<<(unsigned)nb, SCAN_T, 0, s>>>(in, out, n, nb, total_dev, agg, agg + nb, flag,
+                                                           reinterpret_cast<unsigned*>(flag + nb));
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(buf, s);
   if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);
   return XK_OK;
 }
