@@ -518,6 +518,11 @@ def c5_section(args, dev, w, pr) -> dict:
                      "increment_ms (detection + 2 iterations)": float(np.mean(det) + 2 * np.mean(asm))}
     out["gain_per_increment"] = (out["unpruned"]["increment_ms (detection + 2 iterations)"]
                                  / out["pruned"]["increment_ms (detection + 2 iterations)"])
+    out["gain_per_iteration"] = out["unpruned"]["assemble_ms_mean"] / out["pruned"]["assemble_ms_mean"]
+    # Newton iterations per increment above which the pruned increment is the cheaper one
+    d_det = out["pruned"]["detect_ms_mean"] - out["unpruned"]["detect_ms_mean"]
+    d_asm = out["unpruned"]["assemble_ms_mean"] - out["pruned"]["assemble_ms_mean"]
+    out["break_even_iterations_per_increment"] = d_det / d_asm if d_asm > 0 and d_det > 0 else (0.0 if d_det <= 0 else None)
     out["R_rel_diff_last_step"] = float((b["R_last"] - a["R_last"]).abs().max() / a["R_last"].abs().max())
     return out
 

@@ -381,6 +381,19 @@ XK_D bool midpoint_keep(const double4_32a a, const double4_32a b, double ra, dou
   return mp <= xadd(xadd(ra, rb), extra);
 }
 
+// The same decision with a float screen first: the separation |m_i - m_j| in float (from the exact double
+// differences) against the threshold r_i + r_j + extra + h_i + h_j decides every pair farther than a
+// relative 1e-5 from it (float rounding of the separation stays below 1e-6 relative); the rest take the
+// exact routine, so the decision is the exact one.
+XK_D bool midpoint_keep_fast(const double4_32a a, const double4_32a b, double ra, double rb, double extra) {
+  const float dx = (float)xsub(a.x, b.x), dy = (float)xsub(a.y, b.y), dz = (float)xsub(a.z, b.z);
+  const float md = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+  const float thr = (float)(ra + rb + extra + a.w + b.w);
+  if (md < __fmul_rn(thr, 0.99999f)) return true;
+  if (md > __fmul_rn(thr, 1.00001f)) return false;
+  return midpoint_keep(a, b, ra, rb, extra);
+}
+
 // A warp per segment: its slot list sorted by j (a rank sort; the j are distinct), the prescreen
 // applied (extra null: none), written to srt as j (kept) or ~j (dropped); cnt2[i] = kept count.
 __global__ void __launch_bounds__(BP_T) k_slots_rank(xk_mesh m, const double4_32a* __restrict__ mid,
@@ -415,12 +428,12 @@ __global__ void __launch_bounds__(BP_T) k_slots_rank(xk_mesh m, const double4_32
       r1 += x < v1;
     }
     if (lane < n) {
-      const bool k = !extra || midpoint_keep(mi, mid[v0], ri, m.radii[v0], ex);
+      const bool k = !extra || midpoint_keep_fast(mi, mid[v0], ri, m.radii[v0], ex);
       out[r0] = k ? v0 : ~v0;
       kept += k;
     }
     if (lane + 32 < n) {
-      const bool k = !extra || midpoint_keep(mi, mid[v1], ri, m.radii[v1], ex);
+      const bool k = !extra || midpoint_keep_fast(mi, mid[v1], ri, m.radii[v1], ex);
       out[r1] = k ? v1 : ~v1;
       kept += k;
     }
@@ -428,7 +441,7 @@ __global__ void __launch_bounds__(BP_T) k_slots_rank(xk_mesh m, const double4_32
     const int v = my[l];
     int r = 0;
     for (int q = 0; q < n; ++q) r += my[q] < v;
-    const bool k = !extra || midpoint_keep(mi, mid[v], ri, m.radii[v], ex);
+    const bool k = !extra || midpoint_keep_fast(mi, mid[v], ri, m.radii[v], ex);
     out[r] = k ? v : ~v;
     kept += k;
   }

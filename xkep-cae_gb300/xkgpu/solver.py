@@ -205,6 +205,10 @@ class SolverSettings:
     # _newton_steps.py:229-235); 0 switches it off, so that only the force and displacement tests end
     # an increment (used where two runs are compared to a tighter tolerance than the energy test gives)
     energy_tol: float = 1e-10
+    # the force test also passes when |R| <= residual_floor * |f_int|: the attainable residual of an engine
+    # that assembles in float (about 1e-7 of the internal forces), which a relative test against a small
+    # increment's first residual can ask below; 0 (the reference's test alone) for the FP64 engine
+    residual_floor: float = 0.0
     # increments at exactly these load fractions (ScheduledSteps) instead of the adaptive control;
     # with schedule_cutbacks a failed one is retried from a shrunk fraction
     load_schedule: tuple = ()
@@ -316,6 +320,10 @@ class EngineBackend:
             R = eng.R.clone()
         f_c = R + f_ext - eng.f_int
         return R, f_c
+
+    def f_int_norm(self) -> float:
+        """|f_int| of the last assembly."""
+        return float(torch.linalg.vector_norm(self.eng.f_int))
 
     def internal_force(self, u: torch.Tensor) -> torch.Tensor:
         """f_int(u) alone, in the engine's precision (the line search's only assembly)."""
@@ -435,6 +443,8 @@ class ContactFrictionSolver:
             hist.append(ratio)
             if ratio < cfg.tol_force:
                 return True, attempts, n_active, f_c, hist, "force", False
+            if cfg.residual_floor > 0.0 and res <= cfg.residual_floor * b.f_int_norm():
+                return True, attempts, n_active, f_c, hist, "floor", False
             # divergence (_newton_dynamic.py:262-283)
             if att > 0 and ratio > prev_ratio * 1.01:
                 consecutive += 1
