@@ -637,6 +637,12 @@ xk_status xk_prune_select(const int32_t* cands, int64_t n, const float* logit, c
 xk_status xk_pairs_drop_pristine(const xk_pairs* in, const int32_t* kept, int64_t n_kept, xk_pairs* out,
                                  xk_stream s);
 
+/* xk_pairs_drop_pristine(old, cands) followed by xk_pairs_merge, in one merge: old pairs that are not
+ * candidates stay (INACTIVE, state kept) only when they are not pristine.  The pair-list update of a
+ * detection whose candidates were pruned.  Synchronises the stream. */
+xk_status xk_pairs_merge_pruned(const xk_mesh* m, const xk_pairs* old, const int32_t* cands, int64_t n_cands,
+                                xk_pairs* out, xk_stream s);
+
 /* xk_constraint_jacobian without any device allocation, for callers that may
  * not allocate device memory while they run (a host whose device memory is all
  * handed to its own pool, a loop that must not go through the allocator).  No

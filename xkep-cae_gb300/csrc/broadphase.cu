@@ -542,6 +542,9 @@ XK_D void copy_state(const xk_pairs& a, long long i, xk_pairs& b, long long j) {
   }
 }
 
+// r[o] = 1 for an old pair that stays as an old-only (INACTIVE) pair: not a candidate, and with DROP not
+// pristine either (status INACTIVE, p_n = k_pen = 0, z_t = 0)
+template <bool DROP>
 __global__ void k_merge_flags(xk_pairs old, const int32_t* __restrict__ cand, const int32_t* __restrict__ cstart,
                               long long nc, int32_t* __restrict__ r) {
   long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -550,7 +553,13 @@ __global__ void k_merge_flags(xk_pairs old, const int32_t* __restrict__ cand, co
   const int a = old.ea[o], b = old.eb[o];
   long long l = lower_bound_cand(cand, cstart, a, b);
   bool found = l < nc && cand[2 * l] == a && cand[2 * l + 1] == b;
-  r[o] = found ? 0 : 1;
+  bool stays = !found;
+  if (DROP && stays) {
+    const long long c = old.cap;
+    stays = old.status[o] != 0 || old.p_n[o] != 0.0 || old.k_pen[o] != 0.0 || old.z_t[o] != 0.0 ||
+            old.z_t[c + o] != 0.0;
+  }
+  r[o] = stays ? 1 : 0;
 }
 
 __global__ void k_merge_new(xk_pairs old, const int32_t* __restrict__ ostart, const int32_t* __restrict__ cand,
@@ -744,8 +753,8 @@ extern "C" xk_status xk_broadphase(const xk_mesh* m, const double* u, const xk_b
   }
 }
 
-extern "C" xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const int32_t* cands, int64_t n_cands,
-                                    xk_pairs* out, xk_stream s) {
+static xk_status merge_impl(const xk_mesh* m, const xk_pairs* old, const int32_t* cands, int64_t n_cands,
+                            xk_pairs* out, xk_stream s, bool drop) {
   if (!m || !old || !out || (n_cands > 0 && !cands)) return xk_set_error(XK_ERR_ARG, "xk_pairs_merge: null argument");
   if ((long long)out->cap < (long long)old->n + n_cands)
     return xk_set_error(XK_ERR_CAPACITY, "xk_pairs_merge: out->cap < old->n + n_cands");
@@ -762,7 +771,10 @@ extern "C" xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const
   // per-segment row ranges of both sorted lists: each lookup searches only its segment's rows
   k_seg_start<1><<<xk_blocks(ne + 1, 256), 256, 0, st>>>(old->ea, old->n, ne, ostart);
   k_seg_start<2><<<xk_blocks(ne + 1, 256), 256, 0, st>>>(cands, n_cands, ne, cstart);
-  k_merge_flags<<<xk_blocks((long long)old->n + 1, 256), 256, 0, st>>>(*old, cands, cstart, n_cands, r);
+  if (drop)
+    k_merge_flags<true><<<xk_blocks((long long)old->n + 1, 256), 256, 0, st>>>(*old, cands, cstart, n_cands, r);
+  else
+    k_merge_flags<false><<<xk_blocks((long long)old->n + 1, 256), 256, 0, st>>>(*old, cands, cstart, n_cands, r);
   XK_CHECK_LAUNCH();
   XK_TRY(xk_exclusive_scan_i32(r, R, (long long)old->n + 1, tot, st));
   if (n_cands > 0) k_merge_new<<<xk_blocks(n_cands, 256), 256, 0, st>>>(*old, ostart, cands, n_cands, R, *out);
@@ -773,4 +785,14 @@ extern "C" xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const
   XK_CUDA(cudaStreamSynchronize(st));
   out->n = (int32_t)(n_cands + h);
   return XK_OK;
+}
+
+extern "C" xk_status xk_pairs_merge(const xk_mesh* m, const xk_pairs* old, const int32_t* cands, int64_t n_cands,
+                                    xk_pairs* out, xk_stream s) {
+  return merge_impl(m, old, cands, n_cands, out, s, false);
+}
+
+extern "C" xk_status xk_pairs_merge_pruned(const xk_mesh* m, const xk_pairs* old, const int32_t* cands,
+                                           int64_t n_cands, xk_pairs* out, xk_stream s) {
+  return merge_impl(m, old, cands, n_cands, out, s, true);
 }

@@ -113,6 +113,7 @@ SIGNATURES = {
     "xk_beam_lumped_mass": [P(Mesh), P(Section), P(BeamPlan), C.c_double, vp, vp],
     "xk_broadphase": [P(Mesh), vp, P(BPParams), vp, C.c_int64, i64p, i64p, i64p, vp],
     "xk_pairs_merge": [P(Mesh), P(Pairs), vp, C.c_int64, P(Pairs), vp],
+    "xk_pairs_merge_pruned": [P(Mesh), P(Pairs), vp, C.c_int64, P(Pairs), vp],
     "xk_narrowphase": [P(Mesh), P(Pairs), vp, P(ContactParams), C.c_int, vp],
     "xk_narrowphase_screened": [P(Mesh), P(Pairs), vp, vp, P(ContactParams), vp, vp],
     "xk_strand_generate": [vp, C.c_int32, C.c_int64, C.c_int64, vp, vp, vp, vp, vp],

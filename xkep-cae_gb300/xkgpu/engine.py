@@ -217,13 +217,7 @@ class AssemblyEngine:
                 st["kept"] += nc
                 return cands, nc
         st["kept"] += nk
-        # drop pristine old pairs that are not kept, so that pruned pairs leave the table
-        old = self._spare
-        if old.cap < self.pairs.n:
-            old.reserve(self.pairs.n + 64, keep=False)
-        L.call("xk_pairs_drop_pristine", C.byref(self.pairs.c), ptr(kept), nk, C.byref(old.c), s)
-        old.set_n(old.c.n)
-        self.pairs, self._spare = old, self.pairs
+        self._merge_pruned = True  # the merge drops the pristine old pairs that are not kept
         return kept, nk
 
     def detect(self, u: torch.Tensor, stream=None) -> dict:
@@ -233,14 +227,15 @@ class AssemblyEngine:
         cands, nc = self.candidates(u, stream)
         n_raw, n_pre = self._bp_counts
         n_all = nc
+        self._merge_pruned = False
         if self.pruner is not None:
             cands, nc = self._prune(u, cands, nc, s, stream)
         self._n_detect += 1
         need = self.pairs.n + nc
         if self._spare.cap < need:
             self._spare.reserve(int(need * 1.25) + 64, keep=False)
-        L.call("xk_pairs_merge", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(cands), nc,
-               C.byref(self._spare.c), s)
+        L.call("xk_pairs_merge_pruned" if self._merge_pruned else "xk_pairs_merge", C.byref(self.mesh.c),
+               C.byref(self.pairs.c), ptr(cands), nc, C.byref(self._spare.c), s)
         self._spare.set_n(self._spare.c.n)
         self.pairs, self._spare = self._spare, self.pairs
         screened = self.precision == L.XK_MIXED and self.screened_detection and not self.coated
