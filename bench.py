@@ -204,8 +204,10 @@ def gather_tangent_bytes(n_members, n_contrib, nnzb, mixed: bool, sides: bool = 
 
 
 def kernel_roofline_mixed(eng, u1, u0, peak, reps: int = 50) -> list:
-    """Every launch of the mixed assembly alone: CUDA-event time (mean over ``reps`` back-to-back calls on
-    one stream), algorithmic bytes and the fraction of the HBM peak.
+    """Every launch of the mixed assembly alone: CUDA-event time (mean over ``reps`` back-to-back calls
+    captured in one CUDA graph and replayed, so that host launch overhead does not pace the small
+    kernels; ``us_eager`` is the same loop launched from Python), algorithmic bytes and the fraction of
+    the HBM peak.
 
     Algorithmic bytes (compulsory traffic, each array read or written once):
     node preparation 72 B read (X, u, u_ref) + 64 B record written per node; other pairs 48 B read
@@ -225,7 +227,6 @@ def kernel_roofline_mixed(eng, u1, u0, peak, reps: int = 50) -> list:
     from xkgpu.device import ptr, stream_handle
 
     s = torch.cuda.current_stream()
-    sh = stream_handle(s)
     pat = eng.pattern
     n_n, n_e = eng.mesh.n_nodes, eng.mesh.n_elems
     n_m = pat.n_members
@@ -234,41 +235,59 @@ def kernel_roofline_mixed(eng, u1, u0, peak, reps: int = 50) -> list:
     pc = C.byref(pat.c)
     eng.assemble(u1, u0)  # records and element sums current
     launches = [
-        ("k_nodes_prepare", lambda: L.call("xk_nodes_prepare", C.byref(eng.mesh.c), ptr(u1), ptr(u0), ptr(eng.node32),
-                                           sh), 136 * n_n),
-        ("k_pair_other32 (+ near-parallel)", lambda: L.call("xk_pair_step32", C.byref(eng.pairs32.c),
-                                                            ptr(eng.node32), C.byref(eng.cp), ptr(eng.rec),
-                                                            L.XK_PAIRS_OTHERS, sh), 84 * n_o + 64 * n_n),
-        ("k_beam_zero32 + k_beam32q", lambda: L.call("xk_beam_assemble32", C.byref(eng.mesh.c),
-                                                     C.byref(eng.beam.section), ptr(eng.elem32),
-                                                     C.byref(eng.beam.plan), ptr(eng.node32), ptr(eng.f_int),
-                                                     ptr(eng.K_beam), sh), (64 + 432) * n_e + (64 + 48) * n_n),
-        ("k_pair_member32 (+ near-parallel)", lambda: L.call("xk_pair_step32", C.byref(eng.pairs32.c),
-                                                             ptr(eng.node32), C.byref(eng.cp), ptr(eng.rec),
-                                                             L.XK_PAIRS_MEMBERS, sh), 212 * n_m + 64 * n_n),
-        ("k_elem_sums_rec", lambda: L.call("xk_contact_gather_tangent", pc, ptr(eng.rec), eng.precision,
-                                           L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_SIDES_SUMS,
-                                           ptr(eng.K_c), sh), 72 * n_m + 4 * (n_e + 1) + 320 * n_e),
-        ("k_gather_tangent_sides", lambda: L.call("xk_contact_gather_tangent", pc, ptr(eng.rec), eng.precision,
-                                                  L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_SIDES_BLOCKS,
-                                                  ptr(eng.K_c), sh), (16 + 36) * nb + 144 * n_e),
-        ("k_gather_force_elem", lambda: L.call("xk_contact_gather_force_elem", pc, eng.precision, ptr(eng.f_int), -1.0,
-                                               None, None, ptr(eng.R), ptr(eng.norm2), sh), (48 + 48 + 64) * n_n),
+        ("k_nodes_prepare", lambda sh: L.call("xk_nodes_prepare", C.byref(eng.mesh.c), ptr(u1), ptr(u0), ptr(eng.node32),
+                                              sh), 136 * n_n),
+        ("k_pair_other32 (+ near-parallel)", lambda sh: L.call("xk_pair_step32", C.byref(eng.pairs32.c),
+                                                               ptr(eng.node32), C.byref(eng.cp), ptr(eng.rec),
+                                                               L.XK_PAIRS_OTHERS, sh), 84 * n_o + 64 * n_n),
+        ("k_beam32e (ordered wires, one launch)", lambda sh: L.call("xk_beam_assemble32", C.byref(eng.mesh.c),
+                                                        C.byref(eng.beam.section), ptr(eng.elem32),
+                                                        C.byref(eng.beam.plan), ptr(eng.node32), ptr(eng.f_int),
+                                                        ptr(eng.K_beam), sh), (64 + 432) * n_e + (64 + 48) * n_n),
+        ("k_pair_member32 (+ near-parallel)", lambda sh: L.call("xk_pair_step32", C.byref(eng.pairs32.c),
+                                                                ptr(eng.node32), C.byref(eng.cp), ptr(eng.rec),
+                                                                L.XK_PAIRS_MEMBERS, sh), 212 * n_m + 64 * n_n),
+        ("k_elem_sums_rec", lambda sh: L.call("xk_contact_gather_tangent", pc, ptr(eng.rec), eng.precision,
+                                              L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_SIDES_SUMS,
+                                              ptr(eng.K_c), sh), 72 * n_m + 4 * (n_e + 1) + 320 * n_e),
+        ("k_gather_tangent_sides", lambda sh: L.call("xk_contact_gather_tangent", pc, ptr(eng.rec), eng.precision,
+                                                     L.XK_OUT_COMBINED, L.XK_WHICH_COMBINED, L.XK_GATHER_SIDES_BLOCKS,
+                                                     ptr(eng.K_c), sh), (16 + 36) * nb + 144 * n_e),
+        ("k_gather_force_elem", lambda sh: L.call("xk_contact_gather_force_elem", pc, eng.precision, ptr(eng.f_int), -1.0,
+                                                  None, None, ptr(eng.R), ptr(eng.norm2), sh), (48 + 48 + 64) * n_n),
     ]
     out = []
+    cs = torch.cuda.Stream()
     for name, fn, nbytes in launches:
+        sh = stream_handle(s)
         for _ in range(3):
-            fn()
+            fn(sh)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(s)
         for _ in range(reps):
-            fn()
+            fn(sh)
+        b.record(s)
+        torch.cuda.synchronize()
+        t_eager = a.elapsed_time(b) / 1e3 / reps
+        g = torch.cuda.CUDAGraph()
+        cs.wait_stream(s)
+        with torch.cuda.graph(g, stream=cs):
+            h = stream_handle(cs)
+            for _ in range(reps):
+                fn(h)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        a.record(s)
+        g.replay()
         b.record(s)
         torch.cuda.synchronize()
         t = a.elapsed_time(b) / 1e3 / reps
-        out.append({"kernel": name, "us": round(1e6 * t, 2), "bytes": int(nbytes),
-                    "achieved_gbs": round(nbytes / t / 1e9, 1), "frac": round(nbytes / t / 1e9 / peak, 3)})
+        del g
+        out.append({"kernel": name, "us": round(1e6 * t, 2), "us_eager": round(1e6 * t_eager, 2),
+                    "bytes": int(nbytes), "achieved_gbs": round(nbytes / t / 1e9, 1),
+                    "frac": round(nbytes / t / 1e9 / peak, 3)})
     eng.assemble(u1, u0)  # leave the engine's outputs as one assembly left them
     return out
 
@@ -513,7 +532,14 @@ def c5_section(args, dev, w, pr) -> dict:
     for name, r in res.items():
         det = r["detect_ms"][1:]  # the first detection also sizes the buffers
         asm = r["assemble_ms"][1:]
+        # detections 0, 10, 20 of the pruned run verify the pruner exactly (the first is left out with the
+        # buffer sizing); phase means over the others
+        verified = {k for k in range(1, len(det) + 1) if k % 10 == 0} if name == "pruned" else set()
+        plain = [p for k, p in enumerate(r["phases_ms"]) if k >= 1 and k not in verified]
         out[name] = {"detect_ms_mean": float(np.mean(det)), "assemble_ms_mean": float(np.mean(asm)),
+                     "detect_ms_mean_unverified": float(np.mean([d for k, d in enumerate(det, start=1)
+                                                                 if k not in verified])),
+                     "phases_ms_mean": {k: round(float(np.mean([p[k] for p in plain])), 3) for k in plain[0]},
                      "pairs_mean": float(np.mean(r["pairs"][1:])),
                      "increment_ms (detection + 2 iterations)": float(np.mean(det) + 2 * np.mean(asm))}
     out["gain_per_increment"] = (out["unpruned"]["increment_ms (detection + 2 iterations)"]
@@ -964,6 +990,7 @@ def run_gpu(args, rank, world):
                          f"wire ({sub.n_elems} elements, {prep[2]['ea'].shape[0]} pairs), host cores of the machine that runs the bench"}
 
     mixed_variant = engines["mixed"].gather_variant
+    beam_launches = 1 if engines["mixed"].beam.chain_ordered else 2
     fp64_variant = engines["fp64"].gather_variant
     contact_blocks = engines["mixed"].pattern.nnzb
     contact_blocks_full = engines["mixed"].pattern.nnzb_full
@@ -982,11 +1009,12 @@ def run_gpu(args, rank, world):
         extras["coated"] = coated_section(args, dev)
         extras["device_solve"] = device_solve_section(args, dev)
 
-    # node prep, the other-pair kernel and its near-parallel kernel, the beam's zeroing and element
-    # launches, the member kernel and its near-parallel kernel, then either element sums + tangent
-    # gather + residual from the element sums (norm fused) or tangent gather + force gather + 2 norm
-    # kernels (an ncu launch list of one replayed step shows the ten launches of the first form)
-    per_launch = 7 + (3 if mixed_variant == L.XK_GATHER_SIDES else 4)
+    # node prep, the other-pair kernel and its near-parallel kernel, the beam (one launch for wires whose
+    # elements follow each other; a zeroing launch before it for other chain meshes), the member kernel
+    # and its near-parallel kernel, then either element sums + tangent gather + residual from the element
+    # sums (norm fused) or tangent gather + force gather + 2 norm kernels (an ncu launch list of one
+    # replayed step shows the nine launches of the first form on the strand)
+    per_launch = 5 + beam_launches + (3 if mixed_variant == L.XK_GATHER_SIDES else 4)
     out = {
         "metric": METRIC, "value": units / t_mixed * args.steps, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,

@@ -113,6 +113,10 @@ typedef struct {
                                     no two elements on the same two nodes); xk_beam_assemble32 then
                                     runs every element in one launch, adding the two contributions
                                     of a shared node (an order-free sum of two terms) */
+  int32_t chain_ordered;         /* with node_diag: consecutive elements follow each other along every
+                                    wire (element e's node b is element e+1's node a, or the node has
+                                    one element); xk_beam_assemble32 then writes each shared node's
+                                    sum once, without zeroing or atomics */
 } xk_beam_plan;
 
 /* Corotational Timoshenko internal force f_int and analytic tangent K_T of all

@@ -79,3 +79,20 @@ def test_beam_upper_blocks_rebuild_the_symmetric_tangent():
     beam.plan_host = plan
     beam.mesh = SimpleNamespace(n_nodes=st.n_nodes, ndof=6 * st.n_nodes)
     assert np.array_equal(beam.to_csr(vals).toarray(), K)
+
+
+def test_chain_order_detection():
+    """The ordered one-launch float beam needs every wire's elements in sequence (element e's node b
+    is element e+1's node a) or single-element wire ends; other chain meshes take the atomic form."""
+    from xkgpu.device import chain_is_ordered
+
+    wire = lambda n0, n: np.stack([n0 + np.arange(n), n0 + np.arange(1, n + 1)], 1)
+    two = np.concatenate([wire(0, 5), wire(6, 3)])
+    assert chain_is_ordered(two, 10)
+    assert chain_is_ordered(np.array([[0, 1], [2, 3], [4, 5]]), 6)  # separate elements
+    assert not chain_is_ordered(two[::-1], 10)                     # elements in reverse order
+    assert not chain_is_ordered(two[[1, 0, 2, 3, 4, 5, 6, 7]], 10)  # two elements swapped
+    assert not chain_is_ordered(np.array([[1, 0], [1, 2]]), 3)      # node 1 is node a of both
+    assert not chain_is_ordered(np.zeros((0, 2), dtype=np.int64), 0)
+    w = W.config_workload("strand7", seed=0)
+    assert chain_is_ordered(w.strand.conn, w.strand.n_nodes)

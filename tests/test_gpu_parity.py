@@ -248,8 +248,10 @@ def test_beam_float_path_large_rotations(scf, v_ref, key):
 
 
 def test_beam_float_chain_launch_equals_colours():
-    """The one-launch float beam (wire meshes: shared node rows and diagonal blocks zeroed, then two
-    atomic adds) gives the same bits as the two colour launches (store, then add)."""
+    """The one-launch float beam of wire meshes gives the same bits as the colour launches (store,
+    then add): the ordered form (each shared node's two contributions summed by the lane that owns
+    the node, one writer per block) and the atomic form (node rows and diagonal blocks zeroed, then
+    two atomic adds); every shared value is one order-free sum of two terms."""
     import ctypes as C
 
     from xkgpu import workloads as W
@@ -258,19 +260,62 @@ def test_beam_float_chain_launch_equals_colours():
     w = W.config_workload("strand37", seed=3)
     st = w.strand
     eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **w.engine_kwargs())
-    assert eng.beam.node_diag is not None  # wires are chains
+    assert eng.beam.node_diag is not None and eng.beam.chain_ordered  # wires are chains, in order
     u0 = _dev(w.u)
     eng.detect(u0)
     eng.assemble(u0 * 1.001, u0)
     colours = DeviceBeam(eng.mesh, w.section, chain=False)
     assert colours.node_diag is None and colours.plan.n_colors >= 2
-    f = torch.zeros_like(eng.f_int)
-    K = torch.zeros_like(eng.K_beam)
-    L.call("xk_beam_assemble32", C.byref(eng.mesh.c), C.byref(colours.section), ptr(eng.elem32),
-           C.byref(colours.plan), ptr(eng.node32), ptr(f), ptr(K), stream_handle(None))
-    torch.cuda.synchronize()
-    assert torch.equal(f, eng.f_int)
-    assert torch.equal(K[: 36 * colours.nnzb], eng.K_beam[: 36 * colours.nnzb])
+    atomic = DeviceBeam(eng.mesh, w.section)
+    atomic.plan.chain_ordered = 0
+    for beam in (colours, atomic):
+        f = torch.full_like(eng.f_int, float("nan"))
+        K = torch.full_like(eng.K_beam, float("nan"))
+        L.call("xk_beam_assemble32", C.byref(eng.mesh.c), C.byref(beam.section), ptr(eng.elem32),
+               C.byref(beam.plan), ptr(eng.node32), ptr(f), ptr(K), stream_handle(None))
+        torch.cuda.synchronize()
+        assert torch.equal(f, eng.f_int)
+        assert torch.equal(K[: 36 * beam.nnzb], eng.K_beam[: 36 * beam.nnzb])
+
+
+def test_beam_float_ordered_writes_every_block_once():
+    """The ordered float beam writes every f row and stored block of the mesh (buffers start as NaN),
+    on meshes whose wires end inside a warp's range, at a warp boundary, and as one-element wires."""
+    import ctypes as C
+
+    from xkgpu.device import ptr, stream_handle
+
+    z = golden("beam_elements")
+    sec = _sec(z)
+    for lengths in ([31, 31, 1, 5, 62, 2], [1] * 40, [64, 30, 33]):
+        coords, conn, n0 = [], [], 0
+        for k, n_el in enumerate(lengths):
+            xs = np.linspace(0.0, 2.0 * n_el, n_el + 1)
+            coords.append(np.stack([xs, 0 * xs + 3.0 * k, 0 * xs], 1))
+            conn.append(np.stack([n0 + np.arange(n_el), n0 + np.arange(1, n_el + 1)], 1))
+            n0 += n_el + 1
+        X, cn = np.concatenate(coords), np.concatenate(conn)
+        rng = np.random.default_rng(len(lengths))
+        u = np.concatenate([1e-2 * rng.normal(size=(len(X), 3)), 0.3 * rng.normal(size=(len(X), 3))], 1).ravel()
+        eng = AssemblyEngine(X, cn, 0.25, sec, precision="mixed", k_pen=1.0)
+        assert eng.beam.chain_ordered
+        eng.f_int.fill_(float("nan"))
+        eng.K_beam.fill_(float("nan"))
+        eng.assemble(_dev(u))
+        torch.cuda.synchronize()
+        assert torch.isfinite(eng.f_int).all()
+        assert torch.isfinite(eng.K_beam[: 36 * eng.beam.nnzb]).all()
+        colours = DeviceBeam(eng.mesh, sec, chain=False)
+        f = torch.zeros_like(eng.f_int)
+        K = torch.zeros_like(eng.K_beam)
+        L.call("xk_beam_assemble32", C.byref(eng.mesh.c), C.byref(colours.section), ptr(eng.elem32),
+               C.byref(colours.plan), ptr(eng.node32), ptr(f), ptr(K), stream_handle(None))
+        torch.cuda.synchronize()
+        assert torch.equal(f, eng.f_int)
+        assert torch.equal(K[: 36 * colours.nnzb], eng.K_beam[: 36 * colours.nnzb])
+        Kref, fref = ob.assemble_beam(X, cn, u, ob.Section(**{**sec, "scf": None}))
+        assert rel_err(eng.f_int.cpu().numpy(), fref) < TOLMIX
+        assert sparse_rel_err(eng.K_beam_csr(), Kref) < TOLMIX
 
 
 def test_near_parallel_pairs_mixed_vs_fp64():

@@ -470,17 +470,67 @@ __global__ void __launch_bounds__(BEAM_T) k_beam(xk_mesh m, xk_section sec, cons
 //   1 + e0 . e    = (L + L0 + e0 . Delta u) / L
 // none of which cancels, so the corotated frame keeps float accuracy relative
 // to the (small) deformation instead of to the coordinates.
-struct Frame32 {
-  float Rcr[9], exd[3], iLd, th1[3], th2[3], tha[3], thb[3], dax, L0;
-};
+//
+// The element tangent has more structure than beam_tail uses.  Rows 6..8 of
+// the local stiffness are the negatives of rows 0..2 and f_cr[6..8] = -f_cr[0..2],
+// so the unsymmetrised block rows are
+//   [G0 H0 -G0 J0; G1 H1 -G1 J1; -G0 -H0 G0 -J0; G3 H3 -G3 J3],
+// and the symmetrised tangent Ks_IJ = (X_IJ + X_JI^T) / 2 is fixed by six 3x3
+// blocks:
+//   S00 = sym(G0), S01 = (H0 + G1^T)/2, S11 = sym(H1),
+//   S03 = (J0 + G3^T)/2, S13 = (J1 + H3^T)/2, S33 = sym(J3),
+//   aa = [S00 S01; S01^T S11],  ab = [-S00 S03; -S01^T S13],  bb = [S00 -S03; -S03^T S33].
+// Each local-stiffness row has at most two nonzeros against the rotation
+// columns, so row r of A_I (the material part before the rotation to global
+// axes) is a scaled row of P1 plus one of P2 (or of Q1, Q2), and Rcr^T A_I is
+// the sum of the outer products R_r (x) A_I[r] over its nonzero rows, R_r the
+// rows of Rcr.  The geometric term Rcr^T [f_I]x dpsi equals
+// [g_I]x [e_x]x / L = (e_x g_I^T - (g_I . e_x) I) / L with g_I = Rcr^T f_I, the
+// element's global force of block I.
+// An element's outputs, 54 floats in shared memory (one slot per thread):
+constexpr int EL_S00 = 0, EL_S11 = 6, EL_S33 = 12;   // symmetric: (0,0) (0,1) (0,2) (1,1) (1,2) (2,2)
+constexpr int EL_S01 = 18, EL_S03 = 27, EL_S13 = 36;  // row-major
+constexpr int EL_G0 = 45, EL_G1 = 48, EL_G3 = 51;     // f rows: node a translation g0, rotation g1; node b -g0, g3
+constexpr int EL_STRIDE = 55;  // odd: the threads' slots fall in different banks
 
-// The local rotations th1 (node a) and th2 (node b) each take a quaternion log map: a lane of a
-// quad computes the one of its node (lanes 0, 1: a; lanes 2, 3: b) and takes the other from the
-// lane two places away, so every lane ends with both.
-XK_D void frame32(const float* __restrict__ E, const float* __restrict__ NA, const float* __restrict__ NB, Frame32& F,
-                  int lane_in_quad) {
+XK_D int sym_index(int r, int c) {  // position of (r, c) in a symmetric 3x3 stored as 6 values
+  const int i = r < c ? r : c, j = r < c ? c : r;
+  return i == 0 ? j : (i == 1 ? 2 + j : 5);
+}
+
+// sym(X) of a row-major 3x3 into the 6-value form
+XK_D void sym6(const float* X, float* S) {
+  S[0] = X[0];
+  S[1] = 0.5f * (X[1] + X[3]);
+  S[2] = 0.5f * (X[2] + X[6]);
+  S[3] = X[4];
+  S[4] = 0.5f * (X[5] + X[7]);
+  S[5] = X[8];
+}
+
+// M = sum of the outer products R_k (x) V_k (row-major)
+XK_D void outer2(const float* Ra, const float* Va, const float* Rb, const float* Vb, float* M) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) M[3 * i + c] = Ra[i] * Va[c] + Rb[i] * Vb[c];
+}
+XK_D void outer3(const float* Ra, const float* Va, const float* Rb, const float* Vb, const float* Rc,
+                 const float* Vc, float* M) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) M[3 * i + c] = Ra[i] * Va[c] + Rb[i] * Vb[c] + Rc[i] * Vc[c];
+}
+
+// One element: frame (the rotation vectors of both nodes by one thread), global forces of the
+// blocks and, with want_K, the six symmetrised tangent blocks, written to the element's slot o
+// (shared memory) as they are formed, so that few of them are held in registers at once.
+// E: element record, NA / NB: the displacement part of the node records (u, 6 floats).
+XK_D void beam_elem32(const float* __restrict__ E, const float* __restrict__ NA, const float* __restrict__ NB,
+                      const xk_section& sec, bool want_K, float* o) {
   const float dx0[3] = {E[0], E[1], E[2]};
-  F.L0 = E[3];
+  const float L0 = E[3];
   float R0[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) R0[i] = E[4 + i];
@@ -491,248 +541,381 @@ XK_D void frame32(const float* __restrict__ E, const float* __restrict__ NA, con
   const float dxd[3] = {dx0[0] + du[0], dx0[1] + du[1], dx0[2] + du[2]};
   const float Ld = sqrtf(dot3(dxd, dxd));
   const float iLd = 1.0f / Ld;
-  F.iLd = iLd;
   const float two_dx_du[3] = {2.0f * dx0[0] + du[0], 2.0f * dx0[1] + du[1], 2.0f * dx0[2] + du[2]};
-  F.dax = dot3(du, two_dx_du) / (Ld + F.L0);
-  for (int i = 0; i < 3; ++i) F.exd[i] = dxd[i] * iLd;
+  const float dax = dot3(du, two_dx_du) / (Ld + L0);
+  const float ex[3] = {dxd[0] * iLd, dxd[1] * iLd, dxd[2] * iLd};
   float qr[4];
   {
     float v[3];
     cross3(R0, du, v);
-    const float opc = fmaxf((Ld + F.L0 + dot3(R0, du)) * iLd, 1e-12f);
+    const float opc = fmaxf((Ld + L0 + dot3(R0, du)) * iLd, 1e-12f);
     const float w = sqrtf(0.5f * opc);
     const float kk = 0.5f * iLd / w;
     qr[0] = w; qr[1] = kk * v[0]; qr[2] = kk * v[1]; qr[3] = kk * v[2];
   }
   const float qrc[4] = {qr[0], -qr[1], -qr[2], -qr[3]};
-  {
-    const bool node_b = lane_in_quad >= 2;
-    float th[3], qn[4], qx[4], tx[3];
+  // local rotations theta_1, theta_2 = R0 log(q_rod^* (x) q_node)
+  float t1[3], t2[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) th[i] = node_b ? ub[3 + i] : ua[3 + i];
-    quat_of_rotvecf(th, qn);
+  for (int side = 0; side < 2; ++side) {
+    float qn[4], qx[4], tx[3];
+    quat_of_rotvecf(side ? ub + 3 : ua + 3, qn);
     qmulf(qrc, qn, qx);
     rotvec_of_quatf(qx, tx);
-    float mine[3], other[3];
+    float* t = side ? t2 : t1;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      mine[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
-      other[i] = __shfl_xor_sync(0xffffffffu, mine[i], 2);
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      F.th1[i] = node_b ? other[i] : mine[i];
-      F.th2[i] = node_b ? mine[i] : other[i];
-    }
+    for (int i = 0; i < 3; ++i) t[i] = R0[3 * i] * tx[0] + R0[3 * i + 1] * tx[1] + R0[3 * i + 2] * tx[2];
   }
-  for (int i = 0; i < 3; ++i) { F.tha[i] = ua[3 + i]; F.thb[i] = ub[3 + i]; }
-  float Rrod[9];
+  float Rcr[9];
   {
     const float w = qr[0], x = qr[1], y = qr[2], z = qr[3];
+    float Rrod[9];
     Rrod[0] = 1.f - 2.f * (y * y + z * z); Rrod[1] = 2.f * (x * y - w * z); Rrod[2] = 2.f * (x * z + w * y);
     Rrod[3] = 2.f * (x * y + w * z); Rrod[4] = 1.f - 2.f * (x * x + z * z); Rrod[5] = 2.f * (y * z - w * x);
     Rrod[6] = 2.f * (x * z - w * y); Rrod[7] = 2.f * (y * z + w * x); Rrod[8] = 1.f - 2.f * (x * x + y * y);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        Rcr[3 * i + j] = R0[3 * i] * Rrod[3 * j] + R0[3 * i + 1] * Rrod[3 * j + 1] + R0[3 * i + 2] * Rrod[3 * j + 2];
   }
+  const KeCoef<float> kc = ke_coef<float>(sec, L0);
+  // local forces of blocks 0, 1, 3 (block 2 = -block 0) and their global images g_I = Rcr^T f_I
+  float g0[3], g1[3], g3[3];
+  {
+    const float f0[3] = {-kc.ea * dax, kc.k2z * (t1[2] + t2[2]), -kc.k2y * (t1[1] + t2[1])};
+    const float f1[3] = {kc.gj * (t1[0] - t2[0]), kc.k1ay * t1[1] + kc.k1by * t2[1],
+                         kc.k1az * t1[2] + kc.k1bz * t2[2]};
+    const float f3[3] = {-f1[0], kc.k1by * t1[1] + kc.k1ay * t2[1], kc.k1bz * t1[2] + kc.k1az * t2[2]};
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
+      g0[i] = Rcr[i] * f0[0] + Rcr[3 + i] * f0[1] + Rcr[6 + i] * f0[2];
+      g1[i] = Rcr[i] * f1[0] + Rcr[3 + i] * f1[1] + Rcr[6 + i] * f1[2];
+      g3[i] = Rcr[i] * f3[0] + Rcr[3 + i] * f3[1] + Rcr[6 + i] * f3[2];
+      o[EL_G0 + i] = g0[i];
+      o[EL_G1 + i] = g1[i];
+      o[EL_G3 + i] = g3[i];
+    }
+  }
+  if (!want_K) return;
+  const float* R_0 = Rcr;
+  const float* R_1 = Rcr + 3;
+  const float* R_2 = Rcr + 6;
+  // P_s = T^-1(t_s) dpsi with dpsi = Rcr [e_x]x / L: row i of M [e_x]x is M_i x e_x, M = T^-1 Rcr;
+  // Q_s = T^-1(t_s) Rcr T(theta_node)
+  float P1[9], P2[9], Q1[9], Q2[9];
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
-      F.Rcr[3 * i + j] = R0[3 * i] * Rrod[3 * j] + R0[3 * i + 1] * Rrod[3 * j + 1] + R0[3 * i + 2] * Rrod[3 * j + 2];
+  for (int side = 0; side < 2; ++side) {
+    float Ti[9], Ts[9], M[9];
+    tangent_ops<float>(side ? t2 : t1, true, Ti);
+    tangent_ops<float>(side ? ub + 3 : ua + 3, false, Ts);
+    mm3(Ti, Rcr, M);
+    float* P = side ? P2 : P1;
+    float* Q = side ? Q2 : Q1;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      float c[3];
+      cross3(M + 3 * i, ex, c);
+      P[3 * i] = c[0] * iLd;
+      P[3 * i + 1] = c[1] * iLd;
+      P[3 * i + 2] = c[2] * iLd;
+    }
+    mm3(M, Ts, Q);
+  }
+  // G_I = Rcr^T A_I + geometric term; G1^T / 2 and G3^T / 2 go to the S01 and S03 slots at once
+  // (0.5 x + 0.5 y rounds as 0.5 (x + y)), so that P1, P2 and the forces end here
+  {
+    float v0[3], v1[3], v2[3], G[9];
+    const float d1 = dot3(g1, ex), d3 = dot3(g3, ex), d0 = dot3(g0, ex);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      v0[c] = kc.gj * (P1[c] - P2[c]);
+      v1[c] = kc.k1ay * P1[3 + c] + kc.k1by * P2[3 + c];
+      v2[c] = kc.k1az * P1[6 + c] + kc.k1bz * P2[6 + c];
+    }
+    outer3(R_0, v0, R_1, v1, R_2, v2, G);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        o[EL_S01 + 3 * c + i] = 0.5f * (G[3 * i + c] + iLd * (ex[i] * g1[c] - (i == c ? d1 : 0.f)));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      v0[c] = -v0[c];
+      v1[c] = kc.k1by * P1[3 + c] + kc.k1ay * P2[3 + c];
+      v2[c] = kc.k1bz * P1[6 + c] + kc.k1az * P2[6 + c];
+    }
+    outer3(R_0, v0, R_1, v1, R_2, v2, G);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        o[EL_S03 + 3 * c + i] = 0.5f * (G[3 * i + c] + iLd * (ex[i] * g3[c] - (i == c ? d3 : 0.f)));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      v0[c] = kc.ea * ex[c];
+      v1[c] = kc.k2z * (P1[6 + c] + P2[6 + c]);
+      v2[c] = -kc.k2y * (P1[3 + c] + P2[3 + c]);
+    }
+    outer3(R_0, v0, R_1, v1, R_2, v2, G);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) G[3 * i + c] += iLd * (ex[i] * g0[c] - (i == c ? d0 : 0.f));
+    float S[6];
+    sym6(G, S);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o[EL_S00 + i] = S[i];
+  }
+  {
+    float a1[3], a2[3], b0[3], X[9], S[6];
+    // H0, J0: the I = 0 rows against Q1, Q2, added to the halves of G1^T, G3^T
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      a1[c] = kc.k2z * Q1[6 + c];
+      a2[c] = -kc.k2y * Q1[3 + c];
+    }
+    outer2(R_1, a1, R_2, a2, X);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) o[EL_S01 + i] += 0.5f * X[i];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      a1[c] = kc.k2z * Q2[6 + c];
+      a2[c] = -kc.k2y * Q2[3 + c];
+    }
+    outer2(R_1, a1, R_2, a2, X);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) o[EL_S03 + i] += 0.5f * X[i];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      b0[c] = kc.gj * Q1[c];
+      a1[c] = kc.k1ay * Q1[3 + c];
+      a2[c] = kc.k1az * Q1[6 + c];
+    }
+    outer3(R_0, b0, R_1, a1, R_2, a2, X);  // H1
+    sym6(X, S);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o[EL_S11 + i] = S[i];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      b0[c] = kc.gj * Q2[c];
+      a1[c] = kc.k1ay * Q2[3 + c];
+      a2[c] = kc.k1az * Q2[6 + c];
+    }
+    outer3(R_0, b0, R_1, a1, R_2, a2, X);  // J3
+    sym6(X, S);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o[EL_S33 + i] = S[i];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      b0[c] = -kc.gj * Q1[c];
+      a1[c] = kc.k1by * Q1[3 + c];
+      a2[c] = kc.k1bz * Q1[6 + c];
+    }
+    outer3(R_0, b0, R_1, a1, R_2, a2, X);  // H3
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[EL_S13 + 3 * c + i] = 0.5f * X[3 * i + c];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      b0[c] = -kc.gj * Q2[c];
+      a1[c] = kc.k1by * Q2[3 + c];
+      a2[c] = kc.k1bz * Q2[6 + c];
+    }
+    outer3(R_0, b0, R_1, a1, R_2, a2, X);  // J1
+#pragma unroll
+    for (int i = 0; i < 9; ++i) o[EL_S13 + i] += 0.5f * X[i];
+  }
 }
 
-// Mixed path, four lanes per element: lane I of a quad computes block row I of
-// the unsymmetrised tangent ([G_I, H_I, -G_I, J_I], see beam_tail) and the f
-// rows of DOF group I; the quad exchanges the rows through shared memory to
-// symmetrise, and lane I stores rows 3I..3I+2 of the 12x12 element tangent.
-//
-// CHAIN: all elements in one launch (order == NULL: element k is element k),
-// for meshes in which every node has at most two elements and no two
-// elements share both nodes (wires).  The node rows of f_int and the diagonal
-// blocks, which two elements share, are zeroed first (k_beam_zero32) and
-// receive their two contributions by atomic adds; 0 + a + b = 0 + b + a, so
-// the result does not depend on their order.  The off-diagonal blocks have one
-// writer each.  Otherwise the launch covers one colour of the plan.
-constexpr int BEAMQ_T = 128;
+// Value (r, c) of a stored 6x6 block of one element, from its slot o:
+// aa = [S00 S01; S01^T S11], bb = [S00 -S03; -S03^T S33], ab = [-S00 S03; -S01^T S13] (rows: node a).
+XK_D float blk_aa(const float* o, int r, int c) {
+  if (r < 3) return c < 3 ? o[EL_S00 + sym_index(r, c)] : o[EL_S01 + 3 * r + c - 3];
+  return c < 3 ? o[EL_S01 + 3 * c + r - 3] : o[EL_S11 + sym_index(r - 3, c - 3)];
+}
+XK_D float blk_bb(const float* o, int r, int c) {
+  if (r < 3) return c < 3 ? o[EL_S00 + sym_index(r, c)] : -o[EL_S03 + 3 * r + c - 3];
+  return c < 3 ? -o[EL_S03 + 3 * c + r - 3] : o[EL_S33 + sym_index(r - 3, c - 3)];
+}
+XK_D float blk_ab(const float* o, int r, int c) {
+  if (r < 3) return c < 3 ? -o[EL_S00 + sym_index(r, c)] : o[EL_S03 + 3 * r + c - 3];
+  return c < 3 ? -o[EL_S01 + 3 * c + r - 3] : o[EL_S13 + 3 * (r - 3) + c - 3];
+}
 
-template <bool CHAIN>
-__global__ void __launch_bounds__(BEAMQ_T, 7) k_beam32q(xk_mesh m, xk_section sec, const float* __restrict__ e32,
+// block kinds of an element: 0 aa, 1 ab, 2 ba (the transpose of ab), 3 bb; 4: aa of o plus bb of p
+XK_D float blk_val(int kind, const float* o, const float* p, int r, int c) {
+  switch (kind) {
+    case 0: return blk_aa(o, r, c);
+    case 1: return blk_ab(o, r, c);
+    case 2: return blk_ab(o, c, r);
+    case 3: return blk_bb(o, r, c);
+    default: return blk_aa(o, r, c) + blk_bb(p, r, c);
+  }
+}
+
+// HOW: 0 store, 1 add to the stored value, 2 atomic add
+template <int KIND, int HOW>
+XK_D void put_block(float* __restrict__ dst, const float* o, const float* p) {
+  float4* d = reinterpret_cast<float4*>(dst);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    float v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = blk_val(KIND, o, p, (4 * q + k) / 6, (4 * q + k) % 6);
+    float4 x = make_float4(v[0], v[1], v[2], v[3]);
+    if (HOW == 2) {
+      atomicAdd(d + q, x);
+    } else {
+      if (HOW == 1) {
+        const float4 y = d[q];
+        x.x += y.x; x.y += y.y; x.z += y.z; x.w += y.w;
+      }
+      d[q] = x;
+    }
+  }
+}
+
+// f rows of one node: translation t (3, negated with neg_t) then rotation r (3), as doubles
+template <int HOW>  // 0 store, 1 add, 2 atomic add
+XK_D void put_rows(double* __restrict__ f, long long node, const float* t, const float* r, bool neg_t) {
+  double v[6];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    v[i] = (double)(neg_t ? -t[i] : t[i]);
+    v[3 + i] = (double)r[i];
+  }
+  double* d = f + 6 * node;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    if (HOW == 0) d[i] = v[i];
+    else if (HOW == 1) d[i] += v[i];
+    else atomicAdd(d + i, v[i]);
+  }
+}
+
+// The float CR beam, one thread per element, its outputs staged in a shared-memory slot.
+//
+// BEAM_ORDERED (wire meshes whose elements follow each other along every wire:
+// element e's node b is element e+1's node a, or the node has one element):
+// a warp covers 31 elements; lane j takes element 31 w + j - 1, and lane 0's
+// element (the last of the previous warp) is computed only for its node-b
+// block and rows.  Lane j writes the diagonal block and f rows of its node a
+// as its own block aa plus lane j-1's block bb (read from that lane's slot),
+// so every stored block and f row has one writer and no zeroing pass is
+// needed; the sum a + b equals the other modes' 0 + a + b and their
+// store-then-add bits.  A lane whose predecessor ends its wire (or the mesh)
+// writes the predecessor's bb and node-b rows instead.
+// BEAM_ATOMIC (other chain meshes): node rows and diagonal blocks zeroed
+// first (k_beam_zero32), the two contributions of a shared node added by
+// atomics.  BEAM_COLOUR: elements of one colour of the plan, the first writer
+// of a block stores and later colours add.
+// The mode is a launch argument, not a template parameter: the element's arithmetic is compiled
+// once, so that every mode computes the same bits for an element (with floating-point contraction
+// left to the compiler, separately compiled copies may round differently).
+// Six CTAs of 128 threads per SM (80 registers, 28 KB of slots each): 152 SMs hold 3,648 warps, i.e.
+// up to 113k ordered elements in one wave, without a second round of the long per-thread chain.
+constexpr int BEAMW_T = 128;
+constexpr int BEAM_ORDERED = 0, BEAM_ATOMIC = 1, BEAM_COLOUR = 2;
+
+__global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_section sec,
+                                                     const float* __restrict__ e32,
                                                      const int32_t* __restrict__ order, int k0, int k1,
                                                      const int32_t* __restrict__ blk,
-                                                     const uint8_t* __restrict__ first, const float* __restrict__ n32,
-                                                     double* __restrict__ f_int, float* __restrict__ Kv) {
-  __shared__ float sx[BEAMQ_T / 4][4][27];
-  // the element's three stored 6x6 blocks, staged: aa, the off-diagonal one above the diagonal, bb
-  __shared__ __align__(16) float kst[BEAMQ_T / 4][3][36];
-  __shared__ int s_e[BEAMQ_T / 4];
-  const int q = threadIdx.x >> 2, I = threadIdx.x & 3;
-  const int k = k0 + blockIdx.x * (BEAMQ_T / 4) + q;
-  const bool live = k < k1;
-  const int e = CHAIN ? (live ? k : k0) : (live ? order[k] : order[k0]);
-  if (I == 0) s_e[q] = live ? e : -1;
-  const int a = m.conn[2 * e], b = m.conn[2 * e + 1];
-  Frame32 F;
-  frame32(e32 + (long long)e * XK_ELEM32_STRIDE, n32 + (long long)a * XK_NODE32_STRIDE + 6,
-          n32 + (long long)b * XK_NODE32_STRIDE + 6, F, I);
-  const KeCoef<float> kc = ke_coef<float>(sec, F.L0);
-  const float* t1 = F.th1;
-  const float* t2 = F.th2;
-  float fcr[12];
-  fcr[0] = -kc.ea * F.dax;
-  fcr[1] = kc.k2z * (t1[2] + t2[2]);
-  fcr[2] = -kc.k2y * (t1[1] + t2[1]);
-  fcr[3] = kc.gj * (t1[0] - t2[0]);
-  fcr[4] = kc.k1ay * t1[1] + kc.k1by * t2[1];
-  fcr[5] = kc.k1az * t1[2] + kc.k1bz * t2[2];
-  fcr[6] = kc.ea * F.dax;
-  fcr[7] = -fcr[1];
-  fcr[8] = -fcr[2];
-  fcr[9] = -fcr[3];
-  fcr[10] = kc.k1by * t1[1] + kc.k1ay * t2[1];
-  fcr[11] = kc.k1bz * t1[2] + kc.k1az * t2[2];
-  const float* Rcr = F.Rcr;
-  const uint8_t fl = first[e];
-  if (live && f_int) {
-    const float g0 = I == 0 ? fcr[0] : I == 1 ? fcr[3] : I == 2 ? fcr[6] : fcr[9];
-    const float g1 = I == 0 ? fcr[1] : I == 1 ? fcr[4] : I == 2 ? fcr[7] : fcr[10];
-    const float g2 = I == 0 ? fcr[2] : I == 1 ? fcr[5] : I == 2 ? fcr[8] : fcr[11];
-    for (int i = 0; i < 3; ++i) {
-      const double v = (double)(Rcr[i] * g0 + Rcr[3 + i] * g1 + Rcr[6 + i] * g2);
-      const long long dof = (I < 2 ? 6LL * a : 6LL * b) + 3 * (I & 1) + i;
-      const bool fw = (I < 2) ? (fl & 1) : (fl & 8);
-      if (CHAIN) atomicAdd(f_int + dof, v);
-      else if (fw) f_int[dof] = v;
-      else f_int[dof] += v;
+                                                     const uint8_t* __restrict__ first,
+                                                     const float* __restrict__ n32, double* __restrict__ f_int,
+                                                     float* __restrict__ Kv) {
+  __shared__ float slots[BEAMW_T * EL_STRIDE];
+  const long long t = (long long)blockIdx.x * BEAMW_T + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const long long ne = m.n_elems;
+  long long e;
+  bool live;
+  if (mode == BEAM_ORDERED) {
+    e = 31 * (t >> 5) + lane - 1;
+    live = e >= 0 && e < ne;
+  } else {
+    const long long k = k0 + t;
+    live = k < k1;
+    if (!live) return;  // no exchange between threads in these modes
+    e = mode == BEAM_COLOUR ? order[k] : k;
+  }
+  const bool want_K = Kv != nullptr;
+  float* o = slots + threadIdx.x * EL_STRIDE;
+  int a = -1, b = -1;
+  if (live) {
+    a = m.conn[2 * e];
+    b = m.conn[2 * e + 1];
+    beam_elem32(e32 + e * XK_ELEM32_STRIDE, n32 + (long long)a * XK_NODE32_STRIDE + 6,
+                n32 + (long long)b * XK_NODE32_STRIDE + 6, sec, want_K, o);
+  }
+  if (mode == BEAM_ORDERED) {
+    const int bp = __shfl_up_sync(0xffffffffu, b, 1);  // the predecessor's node b
+    __syncwarp();
+    if (lane == 0 || e > ne) return;
+    const float* p = o - EL_STRIDE;          // the predecessor's slot
+    const bool pred = e >= 1;                // the predecessor exists (e <= ne here)
+    const bool joined = live && pred && bp == a;
+    if (pred && !joined) {                   // the predecessor ends its wire: its node b alone
+      if (f_int) put_rows<0>(f_int, bp, p + EL_G0, p + EL_G3, true);
+      if (want_K) put_block<3, 0>(Kv + 36LL * blk[4 * (e - 1) + 3], p, p);
     }
-  }
-  if (!Kv) return;  // uniform over the launch
-  const float* ex = F.exd;
-  float dpsi[9];
-  {
-    const float Sx[9] = {0.f, -ex[2], ex[1], ex[2], 0.f, -ex[0], -ex[1], ex[0], 0.f};
-    mm3(Rcr, Sx, dpsi);
+    if (!live) return;
+    if (f_int) {
+      double v[6];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) dpsi[i] *= F.iLd;
-  }
-  // P1 = T^-1(t1) dpsi, Q1 = T^-1(t1) Rcr T(tha), P2, Q2 likewise at node b are needed by all
-  // rows (Ke_{I1} and Ke_{I3}); lane I computes the I-th of (P1, Q1, P2, Q2) and the quad shares
-  // them through shared memory
-  {
-    float thi[3], Ti[9], X[9];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) thi[c] = I < 2 ? t1[c] : t2[c];
-    tangent_ops<float>(thi, true, Ti);
-    if (I & 1) {
-      float thn[3], Ts[9], tmp[9];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) thn[c] = I < 2 ? F.tha[c] : F.thb[c];
-      tangent_ops<float>(thn, false, Ts);
-      mm3(Ti, Rcr, tmp);
-      mm3(tmp, Ts, X);
-    } else {
-      mm3(Ti, dpsi, X);
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) sx[q][I][i] = X[i];
-  }
-  __syncwarp();
-  const float* P1 = sx[q][0];
-  const float* Q1 = sx[q][1];
-  const float* P2 = sx[q][2];
-  const float* Q2 = sx[q][3];
-  // block row I of the local stiffness against the theta1 (K1), theta2 (K3) and
-  // axial (k6) columns, built with selects so that the quad does not diverge
-  const bool i0 = I == 0, i1 = I == 1, i2 = I == 2;
-  float K1[9], K3[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) { K1[i] = 0.f; K3[i] = 0.f; }
-  const float tz = i0 ? kc.k2z : -kc.k2z, ty = i0 ? -kc.k2y : kc.k2y;  // rows of I = 0 / 2
-  const bool trans = i0 || i2;
-  K1[5] = trans ? tz : 0.f;
-  K3[5] = K1[5];
-  K1[7] = trans ? ty : 0.f;
-  K3[7] = K1[7];
-  K1[0] = trans ? 0.f : (i1 ? kc.gj : -kc.gj);
-  K3[0] = -K1[0];
-  K1[4] = trans ? 0.f : (i1 ? kc.k1ay : kc.k1by);
-  K3[4] = trans ? 0.f : (i1 ? kc.k1by : kc.k1ay);
-  K1[8] = trans ? 0.f : (i1 ? kc.k1az : kc.k1bz);
-  K3[8] = trans ? 0.f : (i1 ? kc.k1bz : kc.k1az);
-  const float k6 = i0 ? -kc.ea : (i2 ? kc.ea : 0.f);  // only row 3I of the block
-  const float fI0 = i0 ? fcr[0] : i1 ? fcr[3] : i2 ? fcr[6] : fcr[9];
-  const float fI1 = i0 ? fcr[1] : i1 ? fcr[4] : i2 ? fcr[7] : fcr[10];
-  const float fI2 = i0 ? fcr[2] : i1 ? fcr[5] : i2 ? fcr[8] : fcr[11];
-  float G[9], H[9], J[9];
-  {
-    float A[9], Hl[9], Jl[9];
-    mm3(K1, P1, A);
-    float tmp[9];
-    mm3(K3, P2, tmp);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A[i] += tmp[i];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) A[c] -= k6 * ex[c];
-    mm3(K1, Q1, Hl);
-    mm3(K3, Q2, Jl);
-    const float Sf[9] = {0.f, -fI2, fI1, fI2, 0.f, -fI0, -fI1, fI0, 0.f};
-    float SfD[9];
-    mm3(Sf, dpsi, SfD);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A[i] += SfD[i];
-    mtm3(Rcr, A, G);
-    mtm3(Rcr, Hl, H);
-    mtm3(Rcr, Jl, J);
-  }
-  __syncwarp();  // every lane has read P1..Q2 before sx is overwritten
-#pragma unroll
-  for (int i = 0; i < 9; ++i) {
-    sx[q][I][i] = G[i];
-    sx[q][I][9 + i] = H[i];
-    sx[q][I][18 + i] = J[i];
-  }
-  __syncwarp();
-  // row I of the symmetrised tangent: Ks[I][Jb] = (X_IJb + X_JbI^T) / 2 with
-  // X_I0 = G_I, X_I1 = H_I, X_I2 = -G_I, X_I3 = J_I, staged per stored block (the off-diagonal
-  // block below the diagonal, ba for a < b and ab for a > b, is the transpose of the other)
-  const int nb_lower = a < b ? 2 : 1;
-#pragma unroll
-  for (int Jb = 0; Jb < 4; ++Jb) {
-    const int nb = (I >> 1) * 2 + (Jb >> 1);  // 0 aa, 1 ab, 2 ba, 3 bb
-    if (nb == nb_lower) continue;
-    const int slot = nb == 0 ? 0 : (nb == 3 ? 2 : 1);
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float xij = (Jb == 0) ? G[3 * r + c] : (Jb == 1) ? H[3 * r + c] : (Jb == 2) ? -G[3 * r + c] : J[3 * r + c];
-        const float* o = sx[q][Jb];
-        const int off = i1 ? 9 : ((I == 3) ? 18 : 0);
-        const float xji = (i2 ? -1.f : 1.f) * o[off + 3 * c + r];
-        kst[q][slot][(3 * (I & 1) + r) * 6 + 3 * (Jb & 1) + c] = 0.5f * (xij + xji);
+      for (int i = 0; i < 3; ++i) {
+        v[i] = (double)o[EL_G0 + i];
+        v[3 + i] = (double)o[EL_G1 + i];
+        if (joined) {
+          v[i] += (double)(-p[EL_G0 + i]);
+          v[3 + i] += (double)p[EL_G3 + i];
+        }
       }
+      if (((uintptr_t)f_int & 15) == 0) {
+        double2* d = reinterpret_cast<double2*>(f_int + 6LL * a);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) d[i] = make_double2(v[2 * i], v[2 * i + 1]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) f_int[6LL * a + i] = v[i];
+      }
+    }
+    if (!want_K) return;
+    if (joined) put_block<4, 0>(Kv + 36LL * blk[4 * e], o, p);
+    else put_block<0, 0>(Kv + 36LL * blk[4 * e], o, o);
+    const int ab = blk[4 * e + 1];
+    if (ab >= 0) put_block<1, 0>(Kv + 36LL * ab, o, o);
+    else put_block<2, 0>(Kv + 36LL * blk[4 * e + 2], o, o);
+    return;
   }
-  __syncwarp();
-  // the warp's 8 elements x 3 stored blocks as 9 float4 per block (a block starts at 144 B * index),
-  // first writer of a block stores, later colours add
-  const int lane = threadIdx.x & 31, q0 = (threadIdx.x >> 5) * 8;
-  for (int t = lane; t < 8 * 3 * 9; t += 32) {
-    const int qq = q0 + t / 27, slot = (t % 27) / 9, ch = t % 9;
-    const int ee = s_e[qq];
-    if (ee < 0) continue;
-    const int nb = slot == 0 ? 0 : (slot == 2 ? 3 : (blk[4LL * ee + 1] >= 0 ? 1 : 2));
-    const int bi = blk[4LL * ee + nb];
-    const float4 v = reinterpret_cast<const float4*>(kst[qq][slot])[ch];
-    float4* dst = reinterpret_cast<float4*>(Kv + 36LL * bi) + ch;
-    if (CHAIN) {
-      if (nb == 0 || nb == 3) atomicAdd(dst, v);  // diagonal block, shared with the neighbour element
-      else *dst = v;
-    } else if ((first[ee] >> nb) & 1) {
-      *dst = v;
+  const uint8_t fl = mode == BEAM_COLOUR ? first[e] : 0;
+  if (f_int) {
+    if (mode == BEAM_ATOMIC) {
+      put_rows<2>(f_int, a, o + EL_G0, o + EL_G1, false);
+      put_rows<2>(f_int, b, o + EL_G0, o + EL_G3, true);
     } else {
-      float4 o = *dst;
-      o.x += v.x; o.y += v.y; o.z += v.z; o.w += v.w;
-      *dst = o;
+      if (fl & 1) put_rows<0>(f_int, a, o + EL_G0, o + EL_G1, false);
+      else put_rows<1>(f_int, a, o + EL_G0, o + EL_G1, false);
+      if (fl & 8) put_rows<0>(f_int, b, o + EL_G0, o + EL_G3, true);
+      else put_rows<1>(f_int, b, o + EL_G0, o + EL_G3, true);
     }
   }
+  if (!want_K) return;
+  const int4 bi = *reinterpret_cast<const int4*>(blk + 4 * e);  // aa, ab, ba, bb
+  if (mode == BEAM_ATOMIC) {
+    put_block<0, 2>(Kv + 36LL * bi.x, o, o);
+    put_block<3, 2>(Kv + 36LL * bi.w, o, o);
+  } else {
+    if (fl & 1) put_block<0, 0>(Kv + 36LL * bi.x, o, o);
+    else put_block<0, 1>(Kv + 36LL * bi.x, o, o);
+    if (fl & 8) put_block<3, 0>(Kv + 36LL * bi.w, o, o);
+    else put_block<3, 1>(Kv + 36LL * bi.w, o, o);
+  }
+  // the off-diagonal block has one writer
+  if (bi.y >= 0) put_block<1, 0>(Kv + 36LL * bi.y, o, o);
+  else put_block<2, 0>(Kv + 36LL * bi.z, o, o);
 }
 
 // Chain launches: zero the node rows of f_int and the diagonal blocks that the elements add into,
@@ -855,18 +1038,25 @@ extern "C" xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec,
   if (!f_int && !K_vals) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
   if (plan->node_diag) {  // chain mesh: one launch over all elements
-    if (m->n_elems == 0) return XK_OK;
-    k_beam_zero32<<<xk_blocks(9LL * m->n_nodes, 256), 256, 0, st>>>(m->n_nodes, plan->node_diag, f_int, K_vals);
-    k_beam32q<true><<<xk_blocks(4LL * m->n_elems, BEAMQ_T), BEAMQ_T, 0, st>>>(
-        *m, *sec, elem32, nullptr, 0, m->n_elems, plan->blk, plan->first, node32, f_int, K_vals);
+    const long long ne = m->n_elems;
+    if (ne == 0) return XK_OK;
+    if (plan->chain_ordered) {  // 31 elements per warp, the lane before them repeating the previous one
+      const long long warps = ne / 31 + 1;
+      k_beam32e<<<xk_blocks(32 * warps, BEAMW_T), BEAMW_T, 0, st>>>(
+          BEAM_ORDERED, *m, *sec, elem32, nullptr, 0, 0, plan->blk, plan->first, node32, f_int, K_vals);
+    } else {
+      k_beam_zero32<<<xk_blocks(9LL * m->n_nodes, 256), 256, 0, st>>>(m->n_nodes, plan->node_diag, f_int, K_vals);
+      k_beam32e<<<xk_blocks(ne, BEAMW_T), BEAMW_T, 0, st>>>(
+          BEAM_ATOMIC, *m, *sec, elem32, nullptr, 0, (int)ne, plan->blk, plan->first, node32, f_int, K_vals);
+    }
     XK_CHECK_LAUNCH();
     return XK_OK;
   }
   for (int c = 0; c < plan->n_colors; ++c) {
     const int k0 = plan->color_ptr_host[c], k1 = plan->color_ptr_host[c + 1];
     if (k1 <= k0) continue;
-    k_beam32q<false><<<xk_blocks(4LL * (k1 - k0), BEAMQ_T), BEAMQ_T, 0, st>>>(
-        *m, *sec, elem32, plan->elem_order, k0, k1, plan->blk, plan->first, node32, f_int, K_vals);
+    k_beam32e<<<xk_blocks(k1 - k0, BEAMW_T), BEAMW_T, 0, st>>>(
+        BEAM_COLOUR, *m, *sec, elem32, plan->elem_order, k0, k1, plan->blk, plan->first, node32, f_int, K_vals);
     XK_CHECK_LAUNCH();
   }
   return XK_OK;

@@ -123,11 +123,33 @@ __global__ void k_tile_scan(const TI* __restrict__ in, TO* __restrict__ out, lon
 // One-pass scan with decoupled look-back (Merrill and Garland, "Single-pass Parallel Prefix Scan with
 // Decoupled Look-back", NVIDIA technical report NVR-2016-002).  Tiles take their index from a ticket
 // counter in the order they start, so a tile waits only on tiles that are already running and never on a
-// later one.  Each tile publishes its aggregate (flag 1), then walks back over its predecessors, adding
-// aggregates until it meets an inclusive prefix (flag 2), and publishes its own inclusive prefix.  The wait
-// on a predecessor that has not published yet is bounded: past SCAN_SPIN_LIMIT polls the tile sums the
-// inputs before it itself (the same prefix, in a fixed order), so the result never depends on the wait.
+// later one.  Each tile publishes its aggregate (flag 1); the first warp then looks back over a window of
+// 32 predecessors at a time (one flag per lane, ballots to find the nearest inclusive prefix, flag 2, and
+// any predecessor that has not published), adds the window's aggregates up to that prefix with a warp sum,
+// and publishes the tile's inclusive prefix.  The wait on a predecessor that has not published yet is
+// bounded: past SCAN_SPIN_LIMIT polls the tile sums the inputs before it itself (the same prefix: integer
+// sums do not depend on their order), so the result never depends on the wait.
 constexpr int SCAN_SPIN_LIMIT = 1 << 20;
+
+XK_D int ld_flag(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
+// Eight consecutive inputs of one thread; 32-bit inputs at a 16-byte aligned address as two vector loads.
+template <typename TI>
+XK_D void load_tile8(const TI* __restrict__ in, long long base, long long n, int64_t* loc) {
+  if (sizeof(TI) == 4 && base + SCAN_I <= n && ((reinterpret_cast<uintptr_t>(in + base) & 15) == 0)) {
+    const int4* q = reinterpret_cast<const int4*>(in + base);
+    const int4 x = __ldg(q), y = __ldg(q + 1);
+    loc[0] = x.x; loc[1] = x.y; loc[2] = x.z; loc[3] = x.w;
+    loc[4] = y.x; loc[5] = y.y; loc[6] = y.z; loc[7] = y.w;
+    return;
+  }
+#pragma unroll
+  for (int i = 0; i < SCAN_I; ++i) loc[i] = (base + i < n) ? (int64_t)in[base + i] : 0;
+}
 
 template <typename TI, typename TO>
 __global__ void __launch_bounds__(SCAN_T) k_scan_onepass(const TI* __restrict__ in, TO* __restrict__ out,
@@ -146,49 +168,66 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_onepass(const TI* __restrict__ 
   const long long t = s_tile;
   const long long base = t * SCAN_TILE + (long long)threadIdx.x * SCAN_I;
   int64_t loc[SCAN_I];
+  load_tile8<TI>(in, base, n, loc);
   int64_t s = 0;
 #pragma unroll
-  for (int i = 0; i < SCAN_I; ++i) {
-    loc[i] = (base + i < n) ? (int64_t)in[base + i] : 0;
-    s += loc[i];
-  }
+  for (int i = 0; i < SCAN_I; ++i) s += loc[i];
   int64_t tile_tot;
   int64_t ex = block_exclusive_scan<int64_t>(s, wt, &tile_tot);
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
     if (t == 0) {
-      inc[0] = tile_tot;
-      __threadfence();
-      atomicExch(&flag[0], 2);
-      s_prefix = 0;
+      if (lane == 0) {
+        inc[0] = tile_tot;
+        __threadfence();
+        atomicExch(&flag[0], 2);
+        s_prefix = 0;
+      }
     } else {
-      agg[t] = tile_tot;
-      __threadfence();
-      atomicExch(&flag[t], 1);
+      if (lane == 0) {
+        agg[t] = tile_tot;
+        __threadfence();
+        atomicExch(&flag[t], 1);
+      }
       int64_t p = 0;
-      long long j = t - 1;
+      long long j = t - 1;  // the window covers tiles j, j - 1, ..., j - 31 (lane k: tile j - k)
       int spins = 0;
-      while (j >= 0) {
-        const int f = atomicAdd(&flag[j], 0);
-        if (f == 0) {
+      bool fell_back = false;
+      while (true) {
+        const long long k = j - lane;
+        const int f = k >= 0 ? ld_flag(flag + k) : 2;  // before tile 0: an inclusive prefix of 0
+        const unsigned m_inc = __ballot_sync(0xffffffffu, f == 2);
+        const int stop = m_inc ? __ffs(m_inc) - 1 : 32;  // nearest inclusive prefix in the window
+        const unsigned need = stop == 32 ? 0xffffffffu : ((1u << stop) - 1u);
+        if (__ballot_sync(0xffffffffu, f == 0) & need) {  // a nearer predecessor has not published
           if (++spins > SCAN_SPIN_LIMIT) {
-            s_fallback = 1;
+            fell_back = true;
             break;
           }
           continue;
         }
         __threadfence();
-        if (f == 2) {  // published values are read past L1 (other tiles' lines may sit there stale)
-          p += __ldcg(inc + j);
-          break;
+        // published values are read past L1 (other tiles' lines may sit there stale)
+        int64_t v = 0;
+        if (k >= 0) {
+          if (lane < stop) v = __ldcg(agg + k);
+          else if (lane == stop) v = __ldcg(inc + k);
         }
-        p += __ldcg(agg + j);
-        --j;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        p += v;
+        if (stop < 32) break;
+        j -= 32;
       }
-      if (!s_fallback) {
-        inc[t] = p + tile_tot;
-        __threadfence();
-        atomicExch(&flag[t], 2);
-        s_prefix = p;
+      if (lane == 0) {
+        if (fell_back) {
+          s_fallback = 1;
+        } else {
+          inc[t] = p + tile_tot;
+          __threadfence();
+          atomicExch(&flag[t], 2);
+          s_prefix = p;
+        }
       }
     }
   }

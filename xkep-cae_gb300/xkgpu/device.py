@@ -195,6 +195,23 @@ def chain_node_diag(conn: np.ndarray, n_nodes: int, plan: BeamPlanHost) -> np.nd
     return diag
 
 
+def chain_is_ordered(conn: np.ndarray, n_nodes: int) -> bool:
+    """Whether the elements of a chain mesh follow each other along every wire: node b of element e
+    is node a of element e + 1, or the node belongs to one element only (a wire end)."""
+    conn = np.asarray(conn, dtype=np.int64)
+    if conn.shape[0] == 0:
+        return False
+    a, b = conn[:, 0], conn[:, 1]
+    cnt = np.bincount(conn.ravel(), minlength=n_nodes)
+    joined = np.zeros(a.shape[0], dtype=bool)
+    joined[1:] = b[:-1] == a[1:]  # element e continues element e - 1
+    ok_a = (cnt[a] == 1) | (joined & (cnt[a] == 2))
+    nxt = np.zeros(a.shape[0], dtype=bool)
+    nxt[:-1] = joined[1:]
+    ok_b = (cnt[b] == 1) | (nxt & (cnt[b] == 2))
+    return bool(np.all(ok_a & ok_b))
+
+
 class DeviceBeam:
     """CR beam data: section, per-element reference frames and the K_T plan."""
 
@@ -221,8 +238,10 @@ class DeviceBeam:
         # wires: every node in at most two elements, no two elements on the same nodes -> one-launch float path
         nd = chain_node_diag(mesh.conn_host, mesh.n_nodes, ph) if chain else None
         self.node_diag = None if nd is None else torch.as_tensor(nd, device=dev)
+        self.chain_ordered = nd is not None and chain_is_ordered(mesh.conn_host, mesh.n_nodes)
         self.plan = L.BeamPlan(len(ph.color_ptr) - 1, C.cast(self._color_ptr, C.c_void_p), ptr(self.order),
-                               ptr(self.blk), ptr(self.first), ph.nnzb, ptr(self.node_diag))
+                               ptr(self.blk), ptr(self.first), ph.nnzb, ptr(self.node_diag),
+                               int(self.chain_ordered))
         self.elem_ref = torch.empty(10 * max(mesh.n_elems, 1), dtype=torch.float64, device=dev)
         self.update_reference_frames()
 

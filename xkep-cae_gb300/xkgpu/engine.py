@@ -99,6 +99,10 @@ class AssemblyEngine:
         self._n_exact = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._n_detect = 0
         self.prune_stats = {"detections": 0, "verified": 0, "candidates": 0, "kept": 0, "missed": 0}
+        # with trace_phases, detect records a CUDA event after each phase (no extra synchronisation);
+        # phase_ms() reads the times of the last detection
+        self.trace_phases = False
+        self._phase_marks: list = []
 
     # ------------------------------------------------------------------ buffers
     @property
@@ -181,10 +185,13 @@ class AssemblyEngine:
         """Candidates the pruner keeps (plus every pair with history), verified exactly when due."""
         pr = self.pruner
         feat, hist = pr.features(self.mesh, u, cands, nc, self.pairs, stream)
+        self._mark("prune_features", stream)
         logit = pr.logits(feat, nc, stream)
+        self._mark("prune_scores", stream)
         kept = torch.empty(2 * max(nc, 1), dtype=torch.int32, device=self.device)
         nk = C.c_int64(0)
         L.call("xk_prune_select", ptr(cands), nc, ptr(logit), ptr(hist), pr.threshold, 0, ptr(kept), C.byref(nk), s)
+        self._mark("prune_select", stream)
         nk = int(nk.value)
         st = self.prune_stats
         st["detections"] += 1
@@ -220,16 +227,36 @@ class AssemblyEngine:
         self._merge_pruned = True  # the merge drops the pristine old pairs that are not kept
         return kept, nk
 
+    def _mark(self, name: str, stream=None):
+        if self.trace_phases:
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(stream if stream is not None else torch.cuda.current_stream())
+            self._phase_marks.append((name, e))
+
+    def phase_ms(self) -> dict:
+        """GPU-timeline time (ms) of each phase of the last detection, when ``trace_phases`` is set: the
+        span between the events recorded at the ends of consecutive phases."""
+        m = self._phase_marks
+        if len(m) < 2:
+            return {}
+        m[-1][1].synchronize()
+        return {name: m[k - 1][1].elapsed_time(e) for k, (name, e) in enumerate(m) if k > 0}
+
     def detect(self, u: torch.Tensor, stream=None) -> dict:
         """Broadphase, pair-table merge, active-set narrowphase and contact pattern at X + u."""
         s = stream_handle(stream)
+        self._phase_marks = []
+        self._mark("start", stream)
         self.sync_state(stream)
+        self._mark("table_back", stream)
         cands, nc = self.candidates(u, stream)
+        self._mark("broadphase", stream)
         n_raw, n_pre = self._bp_counts
         n_all = nc
         self._merge_pruned = False
         if self.pruner is not None:
             cands, nc = self._prune(u, cands, nc, s, stream)
+            self._mark("prune_verify", stream)
         self._n_detect += 1
         need = self.pairs.n + nc
         if self._spare.cap < need:
@@ -238,6 +265,7 @@ class AssemblyEngine:
                C.byref(self.pairs.c), ptr(cands), nc, C.byref(self._spare.c), s)
         self._spare.set_n(self._spare.c.n)
         self.pairs, self._spare = self._spare, self.pairs
+        self._mark("merge", stream)
         screened = self.precision == L.XK_MIXED and self.screened_detection and not self.coated
         if screened:
             L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u), ptr(self.node32), s)
@@ -245,12 +273,15 @@ class AssemblyEngine:
                    C.byref(self.cp), ptr(self._n_exact), s)
         else:
             L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), C.byref(self.cp), 1, s)
+        self._mark("narrowphase", stream)
         self.pattern.build(self.pairs, stream)
+        self._mark("pattern", stream)
         # read while the stream is idle after the pattern build, before the float copy is queued, so that
         # detect returns without waiting for it
         n_exact = int(self._n_exact.item()) if screened else self.pairs.n
         if self.precision == L.XK_MIXED:
             self._to32(s)
+            self._mark("float_table", stream)
         if (self.rec.numel() != L.REC_STRIDE[L.XK_OUT_COMBINED] * self.pattern.cap_members
                 or self.K_c.numel() < 9 * self.pattern.cap_blocks):
             self._alloc_outputs()

@@ -256,13 +256,15 @@ def run_detection_oscillation(w, kappa0: float, *, n_steps: int = 30, iterations
     eng = strand_engine(w, precision)
     if pruner is not None:
         eng.set_pruner(pruner, verify_every=verify_every)
+    eng.trace_phases = True
     dev = eng.device
     nd = eng.mesh.ndof
     u_in = torch.zeros(nd, dtype=torch.float64, device=dev)
     ur_in = torch.zeros(nd, dtype=torch.float64, device=dev)
     rng = np.random.default_rng(seed + 1)
     mask = np.tile([1.0, 1.0, 1.0, 0.0, 0.0, 0.0], w.strand.n_nodes)
-    out = {"detect_ms": [], "assemble_ms": [], "pairs": [], "members": [], "kept_candidates": [], "candidates": []}
+    out = {"detect_ms": [], "assemble_ms": [], "pairs": [], "members": [], "kept_candidates": [], "candidates": [],
+           "phases_ms": []}
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     for k, uk in enumerate(oscillation_states(w, kappa0, n_steps, seed=seed)):
         ud = torch.as_tensor(uk, device=dev)
@@ -271,6 +273,7 @@ def run_detection_oscillation(w, kappa0: float, *, n_steps: int = 30, iterations
         stats = eng.detect(ud)
         torch.cuda.synchronize()
         out["detect_ms"].append(1e3 * (time.perf_counter() - t0))
+        out["phases_ms"].append(eng.phase_ms())
         for key in ("pairs", "members", "kept_candidates", "candidates"):
             out[key].append(stats[key])
         ur_in.copy_(ud)
