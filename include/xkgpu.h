@@ -594,14 +594,16 @@ xk_status xk_system_blocktri(const xk_system* A, const int32_t* pos, int32_t bn,
 #define XK_MLP_PARAMS 8961
 #define XK_MLP_ACT 192 /* a1, a2, a3 per sample */
 
-/* Features of candidate pairs cands[2*i], cands[2*i+1] at X + u (u may be
- * null): midpoint separation, |cos| of the tangent angle, half lengths (all
- * over r_a + r_b), layer distance, core flag, previous-step gap (from `old`,
+/* Features of candidate pairs cands[2*i], cands[2*i+1] at the positions of
+ * the node records node32 (xk_nodes_prepare: X + u as float hi/lo pairs):
+ * midpoint separation, |cos| of the tangent angle, half lengths (all over
+ * r_a + r_b), layer distance, core flag, previous-step gap (from `old`,
  * sorted by (ea, eb)) or, for a pair not in `old`, the current gap from the
- * exact closest point, and whether the previous one exists.  feat: n x 8
- * float; hist[i] = 1 if the pair is in `old` with contact history (status,
- * p_n, k_pen or z_t set), such pairs are never pruned. */
-xk_status xk_prune_features(const xk_mesh* m, const double* u, const int32_t* cands, int64_t n,
+ * clamped closest point in float, and whether the previous one exists.
+ * feat: n x 8 float; hist[i] = 1 if the pair is in `old` with contact
+ * history (status, p_n, k_pen or z_t set), such pairs are never pruned.
+ * No counterpart in the reference (the learned pruning is this library's). */
+xk_status xk_prune_features(const xk_mesh* m, const float* node32, const int32_t* cands, int64_t n,
                             const xk_pairs* old, float* feat, uint8_t* hist, xk_stream s);
 
 /* Logits of n samples on the tensor cores (mma.sync BF16 -> FP32);
@@ -631,9 +633,13 @@ xk_status xk_mlp_to_bf16(const float* theta, uint16_t* out, xk_stream s);
 
 /* Keep candidates with logit >= threshold or hist set (order kept), or with
  * invert != 0 the others (the pruned ones); *n_kept on the host.
- * Synchronises the stream. */
+ * score_error (device word, nullable): the error word of the tensor-core
+ * scoring; when it is set the scores are undefined and every candidate is
+ * kept.  *score_failed (host, nullable) receives that word.  Synchronises the
+ * stream once.  No counterpart in the reference. */
 xk_status xk_prune_select(const int32_t* cands, int64_t n, const float* logit, const uint8_t* hist,
-                          float threshold, int invert, int32_t* kept, int64_t* n_kept, xk_stream s);
+                          float threshold, int invert, const int32_t* score_error, int32_t* kept,
+                          int64_t* n_kept, int32_t* score_failed, xk_stream s);
 
 /* Copy `in` to `out` without its pristine pairs (INACTIVE, p_n = k_pen = 0,
  * z_t = 0) that are not in the sorted list `kept`; order kept.  Synchronises

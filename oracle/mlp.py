@@ -115,12 +115,25 @@ def adam_step(theta, grad, m, v, step: int, lr: float, b1=0.9, b2=0.999, eps=1e-
     return (theta - lr * mh / (np.sqrt(vh) + eps)).astype(np.float32), m.astype(np.float32), v.astype(np.float32)
 
 
-def current_gap_f(xa0, xa1, xb0, xb1, rs):
-    """(segment distance - rs) / rs in float32: differences in double, the clamped closest point of
-    ``_closest_point_segments_batch`` (``geometry/_compute.py:55-151``) in float32 with every operation
-    rounded on its own; near-parallel pairs (det <= 1e-3 ac) take s = 0."""
+def split(x):
+    """Positions as float hi/lo pairs, as the node records hold them (``xk_nodes_prepare``):
+    hi = float(x), lo = float(x - hi)."""
+    x = np.asarray(x, dtype=np.float64)
+    hi = x.astype(np.float32)
+    return hi, (x - hi.astype(np.float64)).astype(np.float32)
+
+
+def split_diff(p, q):
+    """p - q of two split positions: (p_hi - q_hi) + (p_lo - q_lo), each float32 operation rounded."""
+    return (p[0] - q[0]) + (p[1] - q[1])
+
+
+def current_gap_f(A, B, Wv, rs):
+    """(segment distance - rs) / rs in float32 from the float32 segment differences A = a1 - a0,
+    B = b1 - b0, Wv = a0 - b0: the clamped closest point of ``_closest_point_segments_batch``
+    (``geometry/_compute.py:55-151``) in float32 with every operation rounded on its own; near-parallel
+    pairs (det <= 1e-3 ac) take s = 0."""
     f = np.float32
-    A, B, Wv = (xa1 - xa0).astype(f), (xb1 - xb0).astype(f), (xa0 - xb0).astype(f)
 
     def dot(p, q):
         return (p[:, 0] * q[:, 0] + p[:, 1] * q[:, 1]) + p[:, 2] * q[:, 2]
@@ -147,8 +160,9 @@ def current_gap_f(xa0, xa1, xb0, xb1, rs):
 
 
 def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
-    """Per-candidate inputs (n x F), float32.  The position differences are taken in double; everything
-    after them in float32 with every operation rounded on its own (the GPU kernel's order).
+    """Per-candidate inputs (n x F), float32.  The positions (X + u, double) are split into float hi/lo
+    pairs as the node records hold them; the differences are taken from the pairs and everything after
+    them in float32 with every operation rounded on its own (the GPU kernel's order).
 
     0: |m_a - m_b| / (r_a + r_b)              midpoint separation
     1: |d_a . d_b| / (|d_a| |d_b|)            cosine of the tangent angle
@@ -164,8 +178,9 @@ def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
     f = np.float32
     rs = ra + rb
     rsf = np.asarray(rs, dtype=np.float64).astype(f)
-    dm = (0.5 * (xa0 + xa1) - 0.5 * (xb0 + xb1)).astype(f)
-    da, db = (xa1 - xa0).astype(f), (xb1 - xb0).astype(f)
+    a0, a1, b0, b1 = split(xa0), split(xa1), split(xb0), split(xb1)
+    da, db, dw = split_diff(a1, a0), split_diff(b1, b0), split_diff(a0, b0)
+    dm = f(0.5) * (dw + split_diff(a1, b1))
 
     def dot(p, q):
         return (p[:, 0] * q[:, 0] + p[:, 1] * q[:, 1]) + p[:, 2] * q[:, 2]
@@ -183,6 +198,6 @@ def features(xa0, xa1, xb0, xb1, ra, rb, la, lb, prev_gap, has_prev):
         X[:, 3] = np.where(have_layer, np.minimum(np.abs(la - lb), 3).astype(f) / f(3.0), f(0.0))
         X[:, 4] = np.where(have_layer & ((la == 0) | (lb == 0)), f(1.0), f(0.0))
         prev = np.asarray(prev_gap, dtype=np.float64).astype(f) / rsf
-        X[:, 5] = np.clip(np.where(has_prev, prev, current_gap_f(xa0, xa1, xb0, xb1, rs).astype(f)), f(-2.0), f(8.0))
+        X[:, 5] = np.clip(np.where(has_prev, prev, current_gap_f(da, db, dw, rs).astype(f)), f(-2.0), f(8.0))
         X[:, 6] = has_prev.astype(np.float32)
     return X

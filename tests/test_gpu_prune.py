@@ -48,6 +48,11 @@ def _theta(seed):
 
 
 def test_features_match_oracle():
+    import ctypes as C
+
+    from xkgpu import _lib as L
+    from xkgpu.device import ptr, stream_handle
+
     w = W.config_workload("strand37", seed=2)
     eng = _engine(w)
     u0 = torch.as_tensor(w.u, device="cuda")
@@ -57,7 +62,8 @@ def test_features_match_oracle():
     eng.detect(u0)
     pr = P.PairPruner()
     cands, nc = eng.candidates(u1)
-    feat, hist = pr.features(eng.mesh, u1, cands, nc, eng.pairs)
+    L.call("xk_nodes_prepare", C.byref(eng.mesh.c), ptr(u1), ptr(u1), ptr(eng.node32), stream_handle(None))
+    feat, hist = pr.features(eng.mesh, eng.node32, cands, nc, eng.pairs)
     got = feat[: M.F * nc].view(nc, M.F).cpu().numpy()
     # oracle
     c = cands[: 2 * nc].view(-1, 2).cpu().numpy().astype(np.int64)

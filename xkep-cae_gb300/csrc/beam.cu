@@ -491,7 +491,8 @@ __global__ void __launch_bounds__(BEAM_T) k_beam(xk_mesh m, xk_section sec, cons
 constexpr int EL_S00 = 0, EL_S11 = 6, EL_S33 = 12;   // symmetric: (0,0) (0,1) (0,2) (1,1) (1,2) (2,2)
 constexpr int EL_S01 = 18, EL_S03 = 27, EL_S13 = 36;  // row-major
 constexpr int EL_G0 = 45, EL_G1 = 48, EL_G3 = 51;     // f rows: node a translation g0, rotation g1; node b -g0, g3
-constexpr int EL_STRIDE = 55;  // odd: the threads' slots fall in different banks
+constexpr int EL_BLK = 54;                            // the element's block ids aa, ab, ba, bb (int bits)
+constexpr int EL_STRIDE = 59;  // odd: the threads' slots fall in different banks
 
 XK_D int sym_index(int r, int c) {  // position of (r, c) in a symmetric 3x3 stored as 6 values
   const int i = r < c ? r : c, j = r < c ? c : r;
@@ -529,14 +530,19 @@ XK_D void outer3(const float* Ra, const float* Va, const float* Rb, const float*
 // E: element record, NA / NB: the displacement part of the node records (u, 6 floats).
 XK_D void beam_elem32(const float* __restrict__ E, const float* __restrict__ NA, const float* __restrict__ NB,
                       const xk_section& sec, bool want_K, float* o) {
-  const float dx0[3] = {E[0], E[1], E[2]};
-  const float L0 = E[3];
-  float R0[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) R0[i] = E[4 + i];
+  // the record as four 16-byte loads (64-byte aligned), the nodes' u as three 8-byte loads each
+  const float4* E4 = reinterpret_cast<const float4*>(E);
+  const float4 e0 = __ldg(E4), e1 = __ldg(E4 + 1), e2 = __ldg(E4 + 2), e3 = __ldg(E4 + 3);
+  const float dx0[3] = {e0.x, e0.y, e0.z};
+  const float L0 = e0.w;
+  const float R0[9] = {e1.x, e1.y, e1.z, e1.w, e2.x, e2.y, e2.z, e2.w, e3.x};
   float ua[6], ub[6];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) { ua[i] = NA[i]; ub[i] = NB[i]; }
+  for (int i = 0; i < 3; ++i) {
+    const float2 pa = __ldg(reinterpret_cast<const float2*>(NA) + i), pb = __ldg(reinterpret_cast<const float2*>(NB) + i);
+    ua[2 * i] = pa.x; ua[2 * i + 1] = pa.y;
+    ub[2 * i] = pb.x; ub[2 * i + 1] = pb.y;
+  }
   const float du[3] = {ub[0] - ua[0], ub[1] - ua[1], ub[2] - ua[2]};
   const float dxd[3] = {dx0[0] + du[0], dx0[1] + du[1], dx0[2] + du[2]};
   const float Ld = sqrtf(dot3(dxd, dxd));
@@ -814,7 +820,7 @@ XK_D void put_rows(double* __restrict__ f, long long node, const float* t, const
 // The mode is a launch argument, not a template parameter: the element's arithmetic is compiled
 // once, so that every mode computes the same bits for an element (with floating-point contraction
 // left to the compiler, separately compiled copies may round differently).
-// Six CTAs of 128 threads per SM (80 registers, 28 KB of slots each): 152 SMs hold 3,648 warps, i.e.
+// Six CTAs of 128 threads per SM (80 registers, 30 KB of slots each): 152 SMs hold 3,648 warps, i.e.
 // up to 113k ordered elements in one wave, without a second round of the long per-thread chain.
 constexpr int BEAMW_T = 128;
 constexpr int BEAM_ORDERED = 0, BEAM_ATOMIC = 1, BEAM_COLOUR = 2;
@@ -844,9 +850,16 @@ __global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_
   const bool want_K = Kv != nullptr;
   float* o = slots + threadIdx.x * EL_STRIDE;
   int a = -1, b = -1;
+  int* ob = reinterpret_cast<int*>(o + EL_BLK);
   if (live) {
-    a = m.conn[2 * e];
-    b = m.conn[2 * e + 1];
+    // the block ids are loaded with the connectivity, before the element's chain, and parked in the slot
+    const int2 ab = __ldg(reinterpret_cast<const int2*>(m.conn) + e);
+    if (want_K) {
+      const int4 bi = __ldg(reinterpret_cast<const int4*>(blk) + e);
+      ob[0] = bi.x; ob[1] = bi.y; ob[2] = bi.z; ob[3] = bi.w;
+    }
+    a = ab.x;
+    b = ab.y;
     beam_elem32(e32 + e * XK_ELEM32_STRIDE, n32 + (long long)a * XK_NODE32_STRIDE + 6,
                 n32 + (long long)b * XK_NODE32_STRIDE + 6, sec, want_K, o);
   }
@@ -859,7 +872,7 @@ __global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_
     const bool joined = live && pred && bp == a;
     if (pred && !joined) {                   // the predecessor ends its wire: its node b alone
       if (f_int) put_rows<0>(f_int, bp, p + EL_G0, p + EL_G3, true);
-      if (want_K) put_block<3, 0>(Kv + 36LL * blk[4 * (e - 1) + 3], p, p);
+      if (want_K) put_block<3, 0>(Kv + 36LL * reinterpret_cast<const int*>(p + EL_BLK)[3], p, p);
     }
     if (!live) return;
     if (f_int) {
@@ -883,11 +896,10 @@ __global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_
       }
     }
     if (!want_K) return;
-    if (joined) put_block<4, 0>(Kv + 36LL * blk[4 * e], o, p);
-    else put_block<0, 0>(Kv + 36LL * blk[4 * e], o, o);
-    const int ab = blk[4 * e + 1];
-    if (ab >= 0) put_block<1, 0>(Kv + 36LL * ab, o, o);
-    else put_block<2, 0>(Kv + 36LL * blk[4 * e + 2], o, o);
+    if (joined) put_block<4, 0>(Kv + 36LL * ob[0], o, p);
+    else put_block<0, 0>(Kv + 36LL * ob[0], o, o);
+    if (ob[1] >= 0) put_block<1, 0>(Kv + 36LL * ob[1], o, o);
+    else put_block<2, 0>(Kv + 36LL * ob[2], o, o);
     return;
   }
   const uint8_t fl = mode == BEAM_COLOUR ? first[e] : 0;
@@ -903,19 +915,18 @@ __global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_
     }
   }
   if (!want_K) return;
-  const int4 bi = *reinterpret_cast<const int4*>(blk + 4 * e);  // aa, ab, ba, bb
   if (mode == BEAM_ATOMIC) {
-    put_block<0, 2>(Kv + 36LL * bi.x, o, o);
-    put_block<3, 2>(Kv + 36LL * bi.w, o, o);
+    put_block<0, 2>(Kv + 36LL * ob[0], o, o);
+    put_block<3, 2>(Kv + 36LL * ob[3], o, o);
   } else {
-    if (fl & 1) put_block<0, 0>(Kv + 36LL * bi.x, o, o);
-    else put_block<0, 1>(Kv + 36LL * bi.x, o, o);
-    if (fl & 8) put_block<3, 0>(Kv + 36LL * bi.w, o, o);
-    else put_block<3, 1>(Kv + 36LL * bi.w, o, o);
+    if (fl & 1) put_block<0, 0>(Kv + 36LL * ob[0], o, o);
+    else put_block<0, 1>(Kv + 36LL * ob[0], o, o);
+    if (fl & 8) put_block<3, 0>(Kv + 36LL * ob[3], o, o);
+    else put_block<3, 1>(Kv + 36LL * ob[3], o, o);
   }
   // the off-diagonal block has one writer
-  if (bi.y >= 0) put_block<1, 0>(Kv + 36LL * bi.y, o, o);
-  else put_block<2, 0>(Kv + 36LL * bi.z, o, o);
+  if (ob[1] >= 0) put_block<1, 0>(Kv + 36LL * ob[1], o, o);
+  else put_block<2, 0>(Kv + 36LL * ob[2], o, o);
 }
 
 // Chain launches: zero the node rows of f_int and the diagonal blocks that the elements add into,
@@ -1035,6 +1046,9 @@ extern "C" xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec,
                                         const xk_beam_plan* plan, const float* node32, double* f_int, float* K_vals,
                                         xk_stream s) {
   if (!m || !sec || !elem32 || !plan || !node32) return xk_set_error(XK_ERR_ARG, "xk_beam_assemble32: null argument");
+  if (((uintptr_t)elem32 & 15) || ((uintptr_t)node32 & 7) || ((uintptr_t)m->conn & 7) || ((uintptr_t)plan->blk & 15))
+    return xk_set_error(XK_ERR_ARG, "xk_beam_assemble32: elem32 and the plan's blk must be 16-byte aligned, node32 "
+                                    "and conn 8-byte aligned");
   if (!f_int && !K_vals) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
   if (plan->node_diag) {  // chain mesh: one launch over all elements

@@ -45,18 +45,12 @@ XK_D void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
 
 // ------------------------------------------------------------------ features
 
-// Exact double arithmetic in the order of the oracle's NumPy expressions, cast to float at the end.
-// Current gap of a candidate over (r_a + r_b), in float: the segment differences in double, then
-// the clamped closest-point parameters of _closest_point_segments_batch (geometry/_compute.py:55-151)
-// in float, each product and sum rounded on its own (no contraction), so that a NumPy float32
-// restatement gives the same value; near-parallel pairs (det <= 1e-3 ac) take s = 0.
-XK_D float current_gap_f(const double (*x)[3], double rs) {
-  float a3[3], b3[3], w3[3];
-  for (int c = 0; c < 3; ++c) {
-    a3[c] = (float)xsub(x[1][c], x[0][c]);
-    b3[c] = (float)xsub(x[3][c], x[2][c]);
-    w3[c] = (float)xsub(x[0][c], x[2][c]);
-  }
+// Current gap of a candidate over (r_a + r_b), in float, from the segment differences a3 = a1 - a0,
+// b3 = b1 - b0, w3 = a0 - b0: the clamped closest-point parameters of _closest_point_segments_batch
+// (geometry/_compute.py:55-151) in float, each product and sum rounded on its own (no contraction),
+// so that a NumPy float32 restatement gives the same value; near-parallel pairs (det <= 1e-3 ac)
+// take s = 0.
+XK_D float current_gap_f(const float* a3, const float* b3, const float* w3, float rsf) {
   auto dotf = [](const float* p, const float* q) {
     return __fadd_rn(__fadd_rn(__fmul_rn(p[0], q[0]), __fmul_rn(p[1], q[1])), __fmul_rn(p[2], q[2]));
   };
@@ -81,7 +75,6 @@ XK_D float current_gap_f(const double (*x)[3], double rs) {
   }
   float D[3];
   for (int q = 0; q < 3; ++q) D[q] = __fsub_rn(__fadd_rn(w3[q], __fmul_rn(s, a3[q])), __fmul_rn(t, b3[q]));
-  const float rsf = (float)rs;
   return __fdiv_rn(__fsub_rn(__fsqrt_rn(dotf(D, D)), rsf), rsf);
 }
 
@@ -97,30 +90,41 @@ __global__ void k_table_seg_start(xk_pairs p, long long ne, int32_t* __restrict_
   start[s] = (int32_t)lo;
 }
 
-__global__ void k_features(xk_mesh m, const double* __restrict__ u, const int32_t* __restrict__ cands, long long n,
+// Difference of two positions held as float hi/lo pairs (the node records): the hi and lo parts
+// subtracted separately and then added, each operation rounded on its own.
+XK_D float split_diff(const float* p, const float* q, int c) {
+  return __fadd_rn(__fsub_rn(p[c], q[c]), __fsub_rn(p[3 + c], q[3 + c]));
+}
+
+__global__ void k_features(xk_mesh m, const float* __restrict__ n32, const int32_t* __restrict__ cands, long long n,
                            xk_pairs old, const int32_t* __restrict__ ostart, float* __restrict__ feat,
                            uint8_t* __restrict__ hist) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int ea = cands[2 * i], eb = cands[2 * i + 1];
   const int nd[4] = {m.conn[2 * ea], m.conn[2 * ea + 1], m.conn[2 * eb], m.conn[2 * eb + 1]};
-  double x[4][3];
-  for (int k = 0; k < 4; ++k)
-    for (int c = 0; c < 3; ++c)
-      x[k][c] = u ? xadd(m.X[3LL * nd[k] + c], u[6LL * nd[k] + c]) : m.X[3LL * nd[k] + c];
-  const double rs = xadd(m.radii[ea], m.radii[eb]);
-  // differences in double, everything after them in float with each operation rounded on its own
-  float dm[3], da[3], db[3];
+  float x[4][6];  // x_hi (3), x_lo (3) of the four nodes
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float4* r = reinterpret_cast<const float4*>(n32 + (long long)nd[k] * XK_NODE32_STRIDE);
+    const float4 p = __ldg(r), q = __ldg(r + 1);
+    x[k][0] = p.x; x[k][1] = p.y; x[k][2] = p.z; x[k][3] = p.w; x[k][4] = q.x; x[k][5] = q.y;
+  }
+  const float rsf = (float)xadd(m.radii[ea], m.radii[eb]);
+  // position differences from the split records (no double arithmetic), then everything in float with
+  // each operation rounded on its own
+  float dm[3], da[3], db[3], dw[3];
+#pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const double ma = xmul(0.5, xadd(x[0][c], x[1][c])), mb = xmul(0.5, xadd(x[2][c], x[3][c]));
-    dm[c] = (float)xsub(ma, mb);
-    da[c] = (float)xsub(x[1][c], x[0][c]);
-    db[c] = (float)xsub(x[3][c], x[2][c]);
+    da[c] = split_diff(x[1], x[0], c);
+    db[c] = split_diff(x[3], x[2], c);
+    dw[c] = split_diff(x[0], x[2], c);
+    // m_a - m_b = ((a0 - b0) + (a1 - b1)) / 2
+    dm[c] = __fmul_rn(0.5f, __fadd_rn(dw[c], split_diff(x[1], x[3], c)));
   }
   auto dotf = [](const float* p, const float* q) {
     return __fadd_rn(__fadd_rn(__fmul_rn(p[0], q[0]), __fmul_rn(p[1], q[1])), __fmul_rn(p[2], q[2]));
   };
-  const float rsf = (float)rs;
   const float sep = __fsqrt_rn(dotf(dm, dm));
   const float lna = __fsqrt_rn(dotf(da, da)), lnb = __fsqrt_rn(dotf(db, db));
   float den = __fmul_rn(lna, lnb);
@@ -146,7 +150,7 @@ __global__ void k_features(xk_mesh m, const double* __restrict__ u, const int32_
   if (at >= 0) {
     g5 = __fdiv_rn((float)old.gap[at], rsf);
   } else {  // no previous gap: the current one, in float (feature accuracy is enough)
-    g5 = current_gap_f(x, rs);
+    g5 = current_gap_f(da, db, dw, rsf);
   }
   g5 = g5 < -2.0f ? -2.0f : (g5 > 8.0f ? 8.0f : g5);
   f[5] = g5;
@@ -701,11 +705,13 @@ __global__ void k_to_bf16(const float* __restrict__ theta, uint16_t* __restrict_
 
 // ------------------------------------------------------------------ selection and table compaction
 
+// keep flag of candidate i; a scoring that reported an expired tensor-core wait (*err != 0) keeps every
+// candidate, since its scores are undefined
 __global__ void k_keep_flags(long long n, const float* __restrict__ logit, const uint8_t* __restrict__ hist,
-                             float thr, int invert, int32_t* __restrict__ flag) {
+                             float thr, int invert, const int32_t* __restrict__ err, int32_t* __restrict__ flag) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
-    const int keep = (logit[i] >= thr || (hist && hist[i])) ? 1 : 0;
+    const int keep = (logit[i] >= thr || (hist && hist[i]) || (err && *err)) ? 1 : 0;
     flag[i] = invert ? 1 - keep : keep;
   }
 }
@@ -772,9 +778,9 @@ __global__ void k_compact_table(xk_pairs in, const int32_t* __restrict__ flag, c
 
 // ------------------------------------------------------------------ entry points
 
-extern "C" xk_status xk_prune_features(const xk_mesh* m, const double* u, const int32_t* cands, int64_t n,
+extern "C" xk_status xk_prune_features(const xk_mesh* m, const float* node32, const int32_t* cands, int64_t n,
                                        const xk_pairs* old, float* feat, uint8_t* hist, xk_stream s) {
-  if (!m || !old || (n > 0 && (!cands || !feat || !hist)) || n < 0)
+  if (!m || !old || (n > 0 && (!cands || !feat || !hist || !node32)) || n < 0)
     return xk_set_error(XK_ERR_ARG, "xk_prune_features: bad arguments");
   if (n == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
@@ -782,7 +788,7 @@ extern "C" xk_status xk_prune_features(const xk_mesh* m, const double* u, const 
   int32_t* ostart = nullptr;
   XK_CUDA(cudaMallocAsync((void**)&ostart, sizeof(int32_t) * (ne + 2), st));
   k_table_seg_start<<<xk_blocks(ne + 1, 256), 256, 0, st>>>(*old, ne, ostart);
-  k_features<<<xk_blocks(n, 256), 256, 0, st>>>(*m, u, cands, n, *old, ostart, feat, hist);
+  k_features<<<xk_blocks(n, 256), 256, 0, st>>>(*m, node32, cands, n, *old, ostart, feat, hist);
   cudaError_t e = cudaGetLastError();
   cudaFreeAsync(ostart, st);
   if (e != cudaSuccess) return xk_set_cuda_error(e, __FILE__, __LINE__);
@@ -878,31 +884,40 @@ extern "C" xk_status xk_mlp_to_bf16(const float* theta, uint16_t* out, xk_stream
 }
 
 extern "C" xk_status xk_prune_select(const int32_t* cands, int64_t n, const float* logit, const uint8_t* hist,
-                                     float threshold, int invert, int32_t* kept, int64_t* n_kept, xk_stream s) {
+                                     float threshold, int invert, const int32_t* score_error, int32_t* kept,
+                                     int64_t* n_kept, int32_t* score_failed, xk_stream s) {
   if (!n_kept || n < 0 || (n > 0 && (!cands || !logit || !kept)))
     return xk_set_error(XK_ERR_ARG, "xk_prune_select: bad arguments");
   *n_kept = 0;
+  if (score_failed) *score_failed = 0;
   if (n == 0) return XK_OK;
   cudaStream_t st = (cudaStream_t)s;
   int32_t* flag = nullptr;
-  int64_t* tot = nullptr;
+  int64_t* tot = nullptr;  // [count, scoring error word]
   XK_CUDA(cudaMallocAsync((void**)&flag, sizeof(int32_t) * 2 * n, st));
-  cudaError_t e = cudaMallocAsync((void**)&tot, sizeof(int64_t), st);
+  cudaError_t e = cudaMallocAsync((void**)&tot, 2 * sizeof(int64_t), st);
   if (e != cudaSuccess) {
     cudaFreeAsync(flag, st);
     return xk_set_cuda_error(e, __FILE__, __LINE__);
   }
   int32_t* off = flag + n;
-  k_keep_flags<<<xk_blocks(n, 256), 256, 0, st>>>(n, logit, hist, threshold, invert, flag);
+  k_keep_flags<<<xk_blocks(n, 256), 256, 0, st>>>(n, logit, hist, threshold, invert, score_error, flag);
   xk_status r = xk_exclusive_scan_i32(flag, off, n, tot, st);
   if (r == XK_OK) {
     k_scatter_cands<<<xk_blocks(n, 256), 256, 0, st>>>(n, cands, flag, off, kept);
-    int64_t h = 0;
+    int64_t h[2] = {0, 0};
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    // the count and the scoring's error word come back in one copy
+    if (e == cudaSuccess && score_error)
+      e = cudaMemcpyAsync(tot + 1, score_error, sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, tot, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) r = xk_set_cuda_error(e, __FILE__, __LINE__);
-    else *n_kept = h;
+    if (e != cudaSuccess) {
+      r = xk_set_cuda_error(e, __FILE__, __LINE__);
+    } else {
+      *n_kept = h[0];
+      if (score_failed && score_error) *score_failed = (int32_t)(h[1] & 0xffffffff);
+    }
   }
   cudaFreeAsync(flag, st);
   cudaFreeAsync(tot, st);

@@ -148,7 +148,7 @@ SIGNATURES = {
     "xk_mlp_backward": [vp, vp, vp, vp, vp, vp, C.c_int64, vp, vp, vp, vp, vp],
     "xk_mlp_adam": [vp, vp, vp, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, vp, vp],
     "xk_mlp_to_bf16": [vp, vp, vp],
-    "xk_prune_select": [vp, C.c_int64, vp, vp, C.c_float, C.c_int, vp, i64p, vp],
+    "xk_prune_select": [vp, C.c_int64, vp, vp, C.c_float, C.c_int, vp, vp, i64p, P(C.c_int32), vp],
     "xk_pairs_drop_pristine": [P(Pairs), vp, C.c_int64, P(Pairs), vp],
     "xk_system_spmv": [P(System), vp, vp, vp],
     "xk_system_block_jacobi": [P(System), vp, vp],

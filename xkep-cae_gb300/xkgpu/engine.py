@@ -99,6 +99,7 @@ class AssemblyEngine:
         self._n_exact = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._n_detect = 0
         self.prune_stats = {"detections": 0, "verified": 0, "candidates": 0, "kept": 0, "missed": 0}
+        self._verify_tables = None  # scratch pair tables of the pruner's verification, kept across detections
         # with trace_phases, detect records a CUDA event after each phase (no extra synchronisation);
         # phase_ms() reads the times of the last detection
         self.trace_phases = False
@@ -184,39 +185,50 @@ class AssemblyEngine:
     def _prune(self, u, cands, nc, s, stream):
         """Candidates the pruner keeps (plus every pair with history), verified exactly when due."""
         pr = self.pruner
-        feat, hist = pr.features(self.mesh, u, cands, nc, self.pairs, stream)
+        feat, hist = pr.features(self.mesh, self.node32, cands, nc, self.pairs, stream)
         self._mark("prune_features", stream)
         logit = pr.logits(feat, nc, stream)
         self._mark("prune_scores", stream)
         kept = torch.empty(2 * max(nc, 1), dtype=torch.int32, device=self.device)
-        nk = C.c_int64(0)
-        L.call("xk_prune_select", ptr(cands), nc, ptr(logit), ptr(hist), pr.threshold, 0, ptr(kept), C.byref(nk), s)
+        nk, failed = C.c_int64(0), C.c_int32(0)
+        err = ptr(pr._tc_err) if pr.backend == "tcgen05" else None
+        # one synchronisation: the kept count and the scoring's error word come back together; after an
+        # expired tensor-core wait the scores are undefined and the select keeps every candidate
+        L.call("xk_prune_select", ptr(cands), nc, ptr(logit), ptr(hist), pr.threshold, 0, err, ptr(kept),
+               C.byref(nk), C.byref(failed), s)
         self._mark("prune_select", stream)
         nk = int(nk.value)
         st = self.prune_stats
         st["detections"] += 1
         st["candidates"] += nc
-        if pr.backend == "tcgen05" and pr.tcgen05_failed():
-            # the scores are undefined after an expired tensor-core wait: keep every candidate
+        if failed.value:
             st["scoring_failed"] = st.get("scoring_failed", 0) + 1
             st["kept"] += nc
             return cands, nc
         if self._n_detect % self.verify_every == 0:
-            # verification: the exact narrowphase of every pruned candidate; any that the exact path would
-            # activate is a missed contact and the whole candidate set is used instead
+            # verification: the active-set narrowphase of every pruned candidate (the screened one in the
+            # mixed engine, whose active sets are the exact path's); any that would turn ACTIVE is a missed
+            # contact and the whole candidate set is used instead
             st["verified"] += 1
             dropped = torch.empty(2 * max(nc - nk, 1), dtype=torch.int32, device=self.device)
             nd = C.c_int64(0)
-            L.call("xk_prune_select", ptr(cands), nc, ptr(logit), ptr(hist), pr.threshold, 1, ptr(dropped),
-                   C.byref(nd), s)
+            L.call("xk_prune_select", ptr(cands), nc, ptr(logit), ptr(hist), pr.threshold, 1, None, ptr(dropped),
+                   C.byref(nd), None, s)
             nd = int(nd.value)
             missed = 0
             if nd:
-                empty = DevicePairTable(self.device, cap=16)
-                tmp = DevicePairTable(self.device, cap=nd + 16)
+                if self._verify_tables is None:
+                    self._verify_tables = (DevicePairTable(self.device, cap=16), DevicePairTable(self.device, cap=16))
+                empty, tmp = self._verify_tables
+                empty.set_n(0)
+                tmp.reserve(nd + 16, keep=False)
                 L.call("xk_pairs_merge", C.byref(self.mesh.c), C.byref(empty.c), ptr(dropped), nd, C.byref(tmp.c), s)
                 tmp.set_n(tmp.c.n)
-                L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(tmp.c), ptr(u), C.byref(self.cp), 1, s)
+                if self.precision == L.XK_MIXED and self.screened_detection:
+                    L.call("xk_narrowphase_screened", C.byref(self.mesh.c), C.byref(tmp.c), ptr(u), ptr(self.node32),
+                           C.byref(self.cp), ptr(self._n_exact), s)
+                else:
+                    L.call("xk_narrowphase", C.byref(self.mesh.c), C.byref(tmp.c), ptr(u), C.byref(self.cp), 1, s)
                 missed = int((tmp.t["status"][: tmp.n] != 0).sum().item())
             st["missed"] += missed
             st["last_verify_missed"] = missed
@@ -254,6 +266,9 @@ class AssemblyEngine:
         n_raw, n_pre = self._bp_counts
         n_all = nc
         self._merge_pruned = False
+        screened = self.precision == L.XK_MIXED and self.screened_detection and not self.coated
+        if self.pruner is not None or screened:  # node records at u: pruning features, screened narrowphase
+            L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u), ptr(self.node32), s)
         if self.pruner is not None:
             cands, nc = self._prune(u, cands, nc, s, stream)
             self._mark("prune_verify", stream)
@@ -266,9 +281,7 @@ class AssemblyEngine:
         self._spare.set_n(self._spare.c.n)
         self.pairs, self._spare = self._spare, self.pairs
         self._mark("merge", stream)
-        screened = self.precision == L.XK_MIXED and self.screened_detection and not self.coated
         if screened:
-            L.call("xk_nodes_prepare", C.byref(self.mesh.c), ptr(u), ptr(u), ptr(self.node32), s)
             L.call("xk_narrowphase_screened", C.byref(self.mesh.c), C.byref(self.pairs.c), ptr(u), ptr(self.node32),
                    C.byref(self.cp), ptr(self._n_exact), s)
         else:

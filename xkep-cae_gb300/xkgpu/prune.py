@@ -94,12 +94,13 @@ class PairPruner:
                    label_margin=float(d["label_margin"]), device=device)
 
     # ------------------------------------------------------------------ kernels
-    def features(self, mesh: DeviceMesh, u: torch.Tensor | None, cands: torch.Tensor, n: int,
+    def features(self, mesh: DeviceMesh, node32: torch.Tensor, cands: torch.Tensor, n: int,
                  old: DevicePairTable, stream=None):
-        """(feat [n x 8] float, hist [n] uint8) of candidate rows cands[:n]."""
+        """(feat [n x 8] float, hist [n] uint8) of candidate rows cands[:n] at the positions of the node
+        records ``node32`` (``xk_nodes_prepare``)."""
         feat = torch.empty(max(n, 1) * F, dtype=torch.float32, device=self.device)
         hist = torch.empty(max(n, 1), dtype=torch.uint8, device=self.device)
-        L.call("xk_prune_features", C.byref(mesh.c), ptr(u), ptr(cands), int(n), C.byref(old.c), ptr(feat),
+        L.call("xk_prune_features", C.byref(mesh.c), ptr(node32), ptr(cands), int(n), C.byref(old.c), ptr(feat),
                ptr(hist), stream_handle(stream))
         return feat, hist
 
@@ -183,7 +184,8 @@ def candidate_samples(engine, u0: torch.Tensor, u1: torch.Tensor, pruner: PairPr
     """
     engine.detect(u0)
     cands, nc = engine.candidates(u1)
-    feat, _ = pruner.features(engine.mesh, u1, cands, nc, engine.pairs)
+    L.call("xk_nodes_prepare", C.byref(engine.mesh.c), ptr(u1), ptr(u1), ptr(engine.node32), stream_handle(None))
+    feat, _ = pruner.features(engine.mesh, engine.node32, cands, nc, engine.pairs)
     engine.detect(u1)
     h = engine.pairs
     n = h.n
