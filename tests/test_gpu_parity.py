@@ -532,3 +532,16 @@ def test_host_pipeline_returns_each_steps_outputs():
         check(prev, (k - 1) % 3)
         prev = cur
     check(prev, 4 % 3)
+    # R and its squared norm only (a device linear solve keeps the tangent on the GPU)
+    del pipe
+    lean = HostPipeline(eng, read_tangent=False)
+    assert lean.bytes_out == 8 * (6 * st.n_nodes + 1)
+    prev = lean.submit(hosts[0], uref_h)
+    for k in range(1, 4):
+        cur = lean.submit(hosts[k % 3], uref_h)
+        R, Kb, Kc = lean.result(prev)
+        ref.assemble(_dev(us[(k - 1) % 3]), u0)
+        assert Kb is None and Kc is None
+        assert torch.equal(R, ref.R.cpu())
+        assert lean.residual_norm2() == float(ref.norm2.item())
+        prev = cur

@@ -5,6 +5,7 @@
 #include <cuda.h>
 
 #include <atomic>
+#include <cmath>
 #include <mutex>
 
 #include "xk_common.cuh"
@@ -871,8 +872,12 @@ XK_D void store3f(float* base, long long stride, long long i, const float* v) {
 // difference vector and its norm adds a few units of 2^-24 scale.  eps = 2e-5 scale + that square
 // term over (r_a + r_b) covers both with a wide margin.  The frames of the pairs decided in float
 // are transported in float (the per-iteration narrowphase of the mixed path does the same).
+// g_on_lo / g_off_hi: the thresholds rounded outward to float.  The band test, the error bound and
+// the decisions are all in float (FP64 runs at 1/64 of the FP32 rate on this GPU); the bound is
+// rounded up and the band's ends rounded outward, so that a gap outside the band lies on the same side
+// of the thresholds as the exact one.
 __global__ void __launch_bounds__(PAIR_T) k_narrow_screen(xk_mesh m, xk_pairs p, const float* __restrict__ n32,
-                                                         double g_on, double g_off, int allow_deact,
+                                                         float g_on_lo, float g_off_hi, int allow_deact,
                                                          int32_t* __restrict__ list) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.n) return;
@@ -906,23 +911,25 @@ __global__ void __launch_bounds__(PAIR_T) k_narrow_screen(xk_mesh m, xk_pairs p,
   const bool deferred = m.core_radii != nullptr || narrow32<false, true>(n32, nd, R, sf, tf, gf, n, t1, t2);
   const float u24 = 5.9604645e-8f;  // 2^-24
   const float pe = 8.0e3f * u24 * scale;
-  const double eps = 2e-5 * (double)scale + (double)(pe * pe) / (2.0 * rs);
-  const double g = (double)gf;
-  if (deferred || (g >= g_on - eps && g <= g_off + eps)) {
+  // eps = 2e-5 scale + pe^2 / (2 r_s), raised by 2^-20 of itself for its own roundings (the fast
+  // division's 2 ulp and the float constants included)
+  const float eps = (2e-5f * scale + __fdividef(pe * pe, 2.0f * rh)) * (1.0f + 9.5367432e-7f);
+  const float lo = __fsub_rd(g_on_lo, eps), hi = __fadd_ru(g_off_hi, eps);
+  if (deferred || (gf >= lo && gf <= hi)) {
     list[1 + atomicAdd(list, 1)] = i;
     return;
   }
   p.s[i] = (double)sf;
   p.t[i] = (double)tf;
-  p.gap[i] = g;
+  p.gap[i] = (double)gf;
   const double nn[3] = {n[0], n[1], n[2]}, tt1[3] = {t1[0], t1[1], t1[2]}, tt2[3] = {t2[0], t2[1], t2[2]};
   store3(p.normal, cap, i, nn);
   store3(p.t1, cap, i, tt1);
   store3(p.t2, cap, i, tt2);
-  const uint8_t st = p.status[i];  // g is outside [g_on - eps, g_off + eps]: the exact gap is on the same side
+  const uint8_t st = p.status[i];  // gf is outside [lo, hi]: the exact gap is on the same side of both thresholds
   if (st == ST_INACTIVE) {
-    if (g <= g_on) p.status[i] = ST_ACTIVE;
-  } else if (allow_deact && g >= g_off) {
+    if (gf < lo) p.status[i] = ST_ACTIVE;
+  } else if (allow_deact && gf > hi) {
     p.status[i] = ST_INACTIVE;
   }
 }
@@ -1205,7 +1212,11 @@ extern "C" xk_status xk_narrowphase_screened(const xk_mesh* m, xk_pairs* p, cons
   xk_status r = XK_OK;
   cudaError_t e = cudaMemsetAsync(list, 0, sizeof(int32_t), st);
   if (e == cudaSuccess) {
-    k_narrow_screen<<<xk_blocks(p->n, PAIR_T), PAIR_T, 0, st>>>(*m, *p, node32, cp->g_on, cp->g_off,
+    // the thresholds rounded outward to float
+    float on_lo = (float)cp->g_on, off_hi = (float)cp->g_off;
+    if ((double)on_lo > cp->g_on) on_lo = std::nextafter(on_lo, -INFINITY);
+    if ((double)off_hi < cp->g_off) off_hi = std::nextafter(off_hi, INFINITY);
+    k_narrow_screen<<<xk_blocks(p->n, PAIR_T), PAIR_T, 0, st>>>(*m, *p, node32, on_lo, off_hi,
                                                                cp->allow_deactivation, list);
     k_narrow_exact_list<<<2 * xk_sm_count(), PAIR_T, 0, st>>>(*m, *p, u, cp->g_on, cp->g_off, cp->allow_deactivation,
                                                               list);

@@ -517,18 +517,26 @@ class HostPipeline:
     arrays.  The read-back of one step runs while the next step is copied in
     and assembled.  The two staging sets and two host sets are reused in turn,
     so a ticket's arrays stay valid until two more steps have been submitted.
+
+    With ``read_tangent=False`` only R and its squared norm come back (a caller
+    whose linear solve runs on the device, from the engine's K_beam and K_c,
+    needs nothing else on the host): ``result`` returns (R, None, None) and
+    ``residual_norm2(ticket)`` the norm.
     """
 
-    def __init__(self, engine: AssemblyEngine):
+    def __init__(self, engine: AssemblyEngine, read_tangent: bool = True):
         self.eng = engine
+        self.read_tangent = bool(read_tangent)
         dev = engine.device
         nd = engine.mesh.ndof
         self.u_in = torch.zeros(nd, dtype=torch.float64, device=dev)
         self.ur_in = torch.zeros(nd, dtype=torch.float64, device=dev)
-        self.nkc = 9 * engine.pattern.nnzb
+        self.nkc = 9 * engine.pattern.nnzb if self.read_tangent else 0
         kd = engine.K_beam.dtype
-        self.dev_out = [(torch.empty(nd, dtype=torch.float64, device=dev),
-                         torch.empty(engine.K_beam.numel(), dtype=kd, device=dev),
+        nkb = engine.K_beam.numel() if self.read_tangent else 1
+        # R with its squared norm appended (nd + 1 doubles), K_beam, K_c
+        self.dev_out = [(torch.empty(nd + 1, dtype=torch.float64, device=dev),
+                         torch.empty(nkb, dtype=kd, device=dev),
                          torch.empty(max(self.nkc, 1), dtype=engine.K_c.dtype, device=dev)) for _ in range(2)]
         self.host_out = [tuple(torch.empty(t.numel(), dtype=t.dtype).pin_memory() for t in d) for d in self.dev_out]
         self.copy_in = torch.cuda.Stream(device=dev)
@@ -536,6 +544,7 @@ class HostPipeline:
         self._slot_free = [None, None]  # events: the staging / host set may be overwritten
         self._inputs_free = None  # event: the replay has read the inputs
         self._done = {}
+        self._last = 0
         self.n = 0
         engine.capture(self.u_in, self.ur_in)
 
@@ -554,15 +563,19 @@ class HostPipeline:
         if self._slot_free[k] is not None:
             main.wait_event(self._slot_free[k])
         R, Kb, Kc = self.dev_out[k]
-        R.copy_(eng.R, non_blocking=True)
-        Kb.copy_(eng.K_beam, non_blocking=True)
+        nd = eng.R.numel()
+        R[:nd].copy_(eng.R, non_blocking=True)
+        R[nd:].copy_(eng.norm2, non_blocking=True)
+        if self.read_tangent:
+            Kb.copy_(eng.K_beam, non_blocking=True)
         if self.nkc:
             Kc[: self.nkc].copy_(eng.K_c[: self.nkc], non_blocking=True)
         self.copy_out.wait_stream(main)
         hR, hKb, hKc = self.host_out[k]
         with torch.cuda.stream(self.copy_out):
             hR.copy_(R, non_blocking=True)
-            hKb.copy_(Kb, non_blocking=True)
+            if self.read_tangent:
+                hKb.copy_(Kb, non_blocking=True)
             if self.nkc:
                 hKc[: self.nkc].copy_(Kc[: self.nkc], non_blocking=True)
         ev = torch.cuda.Event()
@@ -573,11 +586,20 @@ class HostPipeline:
         return self.n - 1
 
     def result(self, ticket: int):
-        """(R, K_beam values, K_c values) of a submitted step as pinned host tensors."""
+        """(R, K_beam values, K_c values) of a submitted step as pinned host tensors ((R, None, None) without
+        the tangent read-back)."""
         ev, k = self._done.pop(ticket)
         ev.synchronize()
+        self._last = k
         hR, hKb, hKc = self.host_out[k]
-        return hR, hKb, hKc[: self.nkc]
+        nd = self.u_in.numel()
+        if not self.read_tangent:
+            return hR[:nd], None, None
+        return hR[:nd], hKb, hKc[: self.nkc]
+
+    def residual_norm2(self) -> float:
+        """The squared residual norm of the step whose ``result`` was taken last (FP64, fixed order)."""
+        return float(self.host_out[self._last][0][self.u_in.numel()])
 
     @property
     def bytes_in(self) -> int:
@@ -585,4 +607,7 @@ class HostPipeline:
 
     @property
     def bytes_out(self) -> int:
-        return sum(t.numel() * t.element_size() for t in self.dev_out[0][:2]) + self.nkc * self.dev_out[0][2].element_size()
+        r = self.dev_out[0][0].numel() * 8
+        if not self.read_tangent:
+            return r
+        return r + self.dev_out[0][1].numel() * self.dev_out[0][1].element_size() + self.nkc * self.dev_out[0][2].element_size()
