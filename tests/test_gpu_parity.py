@@ -545,3 +545,53 @@ def test_host_pipeline_returns_each_steps_outputs():
         assert torch.equal(R, ref.R.cpu())
         assert lean.residual_norm2() == float(ref.norm2.item())
         prev = cur
+
+
+def test_conversions_in_integer_arithmetic_are_ieee():
+    """The node records and the float copy of the pair table (and the way back) convert between
+    double and float in integer arithmetic; their bits equal the IEEE conversions (torch's own
+    .float() / .double() on the GPU), zeros and signs included."""
+    import ctypes as C
+
+    from xkgpu import workloads as W
+    from xkgpu.device import ptr, stream_handle
+
+    w = W.config_workload("strand37", seed=5)
+    st = w.strand
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **w.engine_kwargs())
+    u0 = _dev(w.u)
+    rng = np.random.default_rng(3)
+    u1 = _dev(w.u + rng.normal(0.0, 1e-3, w.u.shape))
+    # node records: x = X + u split into float hi / lo, u and u - u_ref in float
+    L.call("xk_nodes_prepare", C.byref(eng.mesh.c), ptr(u1), ptr(u0), ptr(eng.node32), stream_handle(None))
+    torch.cuda.synchronize()
+    N = eng.node32.view(-1, L.NODE32_STRIDE)[: st.n_nodes]
+    x = eng.mesh.X.view(-1, 3) + u1.view(-1, 6)[:, :3]
+    hi = x.float()
+    assert torch.equal(N[:, 0:3], hi)
+    assert torch.equal(N[:, 3:6], (x - hi.double()).float())
+    assert torch.equal(N[:, 6:12], u1.view(-1, 6).float())
+    assert torch.equal(N[:, 12:15], (u1 - u0).view(-1, 6)[:, :3].float())
+    # the pair table: a detection ends with the float copy, the way back must return the float values;
+    # an assembly between two detections gives the pairs their contact state (p_n, z_t, k_pen)
+    eng.detect(u0)
+    eng.assemble(u1, u0)
+    eng.detect(u1)
+    n, cap = eng.pairs.n, eng.pairs.cap
+    t = eng.pairs.t
+    fields = {"s": 1, "t": 1, "gap": 1, "normal": 3, "t1": 3, "t2": 3, "p_n": 1, "z_t": 2, "q_trial_norm": 1,
+              "dissipation": 1, "k_pen": 1, "k_t": 1}
+    before = {k: torch.stack([t[k][c * cap: c * cap + n] for c in range(w_)]).clone() for k, w_ in fields.items()}
+    assert bool((before["p_n"] != 0).any()) and bool((before["gap"] < 0).any())  # a contact state, not zeros only
+    eng.sync_state()
+    torch.cuda.synchronize()
+    others = torch.zeros(n, dtype=torch.bool, device=u0.device)
+    pat = eng.pattern
+    others[eng.pairs32.t["pair"][pat.n_members: n].long()] = True
+    for k, w_ in fields.items():
+        after = torch.stack([t[k][c * cap: c * cap + n] for c in range(w_)])
+        exp = before[k].float().double()
+        if k == "t2":  # the other pairs' t2 is formed again as n x t1
+            after, exp = after[:, ~others], exp[:, ~others]
+        assert torch.equal(after, exp), k
+        assert torch.equal(torch.signbit(after), torch.signbit(exp)), k

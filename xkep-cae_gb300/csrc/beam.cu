@@ -789,8 +789,8 @@ XK_D void put_rows(double* __restrict__ f, long long node, const float* t, const
   double v[6];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    v[i] = (double)(neg_t ? -t[i] : t[i]);
-    v[3 + i] = (double)r[i];
+    v[i] = xk_f2d(neg_t ? -t[i] : t[i]);
+    v[3 + i] = xk_f2d(r[i]);
   }
   double* d = f + 6 * node;
 #pragma unroll
@@ -879,11 +879,11 @@ __global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_
       double v[6];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        v[i] = (double)o[EL_G0 + i];
-        v[3 + i] = (double)o[EL_G1 + i];
+        v[i] = xk_f2d(o[EL_G0 + i]);
+        v[3 + i] = xk_f2d(o[EL_G1 + i]);
         if (joined) {
-          v[i] += (double)(-p[EL_G0 + i]);
-          v[3 + i] += (double)p[EL_G3 + i];
+          v[i] += xk_f2d(-p[EL_G0 + i]);
+          v[3 + i] += xk_f2d(p[EL_G3 + i]);
         }
       }
       if (((uintptr_t)f_int & 15) == 0) {

@@ -725,6 +725,9 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 7 : 4) k_elem_sums_rec(i
 // f_ext and out are 16-byte aligned and moved as double2.
 constexpr int GFE_T = 256;
 
+XK_D double to_f64(float x) { return xk_f2d(x); }  // the conversion in integer arithmetic (the FP64 pipe is slow)
+XK_D double to_f64(double x) { return x; }
+
 template <typename T, bool VEC>
 __global__ void __launch_bounds__(GFE_T) k_gather_force_elem(int n_nodes, int ne, const int32_t* __restrict__ neptr,
                                                              const int2* __restrict__ nelem, const T* __restrict__ S,
@@ -765,7 +768,7 @@ __global__ void __launch_bounds__(GFE_T) k_gather_force_elem(int n_nodes, int ne
       for (int c = 0; c < 3; ++c) acc[c] += f[c];
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) r[c] += scale * (double)acc[c];
+    for (int c = 0; c < 3; ++c) r[c] += scale * to_f64(acc[c]);
     if (f_ext) {
       if (VEC) {
 #pragma unroll

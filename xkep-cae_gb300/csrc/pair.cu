@@ -615,14 +615,14 @@ __global__ void k_nodes_prepare(xk_mesh m, const double* __restrict__ u, const d
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const double x = m.X[3LL * v + c] + uv[c];
-    const float h = (float)x;
+    const float h = xk_d2f(x);
     N[c] = h;
-    N[3 + c] = (float)(x - (double)h);
+    N[3 + c] = xk_d2f(x - xk_f2d(h));
   }
 #pragma unroll
-  for (int c = 0; c < 6; ++c) N[6 + c] = (float)uv[c];
+  for (int c = 0; c < 6; ++c) N[6 + c] = xk_d2f(uv[c]);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) N[12 + c] = (float)(u_ref ? uv[c] - ur[c] : uv[c]);
+  for (int c = 0; c < 3; ++c) N[12 + c] = xk_d2f(u_ref ? uv[c] - ur[c] : uv[c]);
   N[15] = 0.0f;
   float4* out = reinterpret_cast<float4*>(n32 + (long long)v * XK_NODE32_STRIDE);
 #pragma unroll
@@ -644,31 +644,31 @@ __global__ void k_pairs_to32(xk_mesh m, xk_pairs p, xk_contact_pattern pat, xk_p
   q.nodes[4LL * j + 3] = m.conn[2 * eb + 1];
   const bool coat = q.coat_total && m.core_radii && p.coat_cc;  // coated wires: the gap between the cores
   const double R = coat ? m.core_radii[ea] + m.core_radii[eb] : m.radii[ea] + m.radii[eb];
-  const float rh = (float)R;
+  const float rh = xk_d2f(R);
   q.rad[2LL * j] = rh;
-  q.rad[2LL * j + 1] = (float)(R - (double)rh);
+  q.rad[2LL * j + 1] = xk_d2f(R - xk_f2d(rh));
   if (coat) {
-    q.coat_total[j] = (float)coat_total_of(m, ea, eb);
-    q.coat_cc[j] = (float)p.coat_cc[i];
-    q.coat_cc_prev[j] = (float)p.coat_cc_prev[i];
-    q.coat_z_t[j] = (float)p.coat_z_t[i];
-    q.coat_z_t[cq + j] = (float)p.coat_z_t[cp + i];
-    q.coat_qtn[j] = (float)p.coat_qtn[i];
-    q.coat_diss[j] = (float)p.coat_diss[i];
+    q.coat_total[j] = xk_d2f(coat_total_of(m, ea, eb));
+    q.coat_cc[j] = xk_d2f(p.coat_cc[i]);
+    q.coat_cc_prev[j] = xk_d2f(p.coat_cc_prev[i]);
+    q.coat_z_t[j] = xk_d2f(p.coat_z_t[i]);
+    q.coat_z_t[cq + j] = xk_d2f(p.coat_z_t[cp + i]);
+    q.coat_qtn[j] = xk_d2f(p.coat_qtn[i]);
+    q.coat_diss[j] = xk_d2f(p.coat_diss[i]);
     q.coat_stick[j] = p.coat_stick[i];
   }
-  q.s[j] = (float)p.s[i]; q.t[j] = (float)p.t[i]; q.gap[j] = (float)p.gap[i];
+  q.s[j] = xk_d2f(p.s[i]); q.t[j] = xk_d2f(p.t[i]); q.gap[j] = xk_d2f(p.gap[i]);
   for (int c = 0; c < 3; ++c) {
-    q.normal[c * cq + j] = (float)p.normal[c * cp + i];
-    q.t1[c * cq + j] = (float)p.t1[c * cp + i];
-    q.t2[c * cq + j] = (float)p.t2[c * cp + i];
+    q.normal[c * cq + j] = xk_d2f(p.normal[c * cp + i]);
+    q.t1[c * cq + j] = xk_d2f(p.t1[c * cp + i]);
+    q.t2[c * cq + j] = xk_d2f(p.t2[c * cp + i]);
   }
-  q.p_n[j] = (float)p.p_n[i];
-  q.z_t[j] = (float)p.z_t[i]; q.z_t[cq + j] = (float)p.z_t[cp + i];
-  q.q_trial_norm[j] = (float)p.q_trial_norm[i]; q.dissipation[j] = (float)p.dissipation[i];
-  q.k_pen[j] = (float)p.k_pen[i]; q.k_t[j] = (float)p.k_t[i];
+  q.p_n[j] = xk_d2f(p.p_n[i]);
+  q.z_t[j] = xk_d2f(p.z_t[i]); q.z_t[cq + j] = xk_d2f(p.z_t[cp + i]);
+  q.q_trial_norm[j] = xk_d2f(p.q_trial_norm[i]); q.dissipation[j] = xk_d2f(p.dissipation[i]);
+  q.k_pen[j] = xk_d2f(p.k_pen[i]); q.k_t[j] = xk_d2f(p.k_t[i]);
   q.status[j] = p.status[i]; q.stick[j] = p.stick[i];
-  if (q.mu && m.mu) q.mu[j] = (float)m.mu[ea];
+  if (q.mu && m.mu) q.mu[j] = xk_d2f(m.mu[ea]);
 }
 
 // BY_PAIR: a thread per pair i of the FP64 table (j from q.slot; the writes coalesce, and the reads come
@@ -680,7 +680,7 @@ __global__ void k_pairs_from32(xk_pairs32 q, xk_pairs p) {
   const int j = BY_PAIR ? q.slot[t] : t;
   const int i = BY_PAIR ? t : q.pair[j];
   const long long cp = p.cap, cq = q.cap;
-  p.s[i] = q.s[j]; p.t[i] = q.t[j]; p.gap[i] = q.gap[j];
+  p.s[i] = xk_f2d(q.s[j]); p.t[i] = xk_f2d(q.t[j]); p.gap[i] = xk_f2d(q.gap[j]);
   float n[3], t1[3], t2[3];
   for (int c = 0; c < 3; ++c) {
     n[c] = q.normal[c * cq + j];
@@ -689,22 +689,22 @@ __global__ void k_pairs_from32(xk_pairs32 q, xk_pairs p) {
   }
   if (j >= q.n_members) cross3(n, t1, t2);  // the other-pair kernel does not store t2
   for (int c = 0; c < 3; ++c) {
-    p.normal[c * cp + i] = n[c];
-    p.t1[c * cp + i] = t1[c];
-    p.t2[c * cp + i] = t2[c];
+    p.normal[c * cp + i] = xk_f2d(n[c]);
+    p.t1[c * cp + i] = xk_f2d(t1[c]);
+    p.t2[c * cp + i] = xk_f2d(t2[c]);
   }
-  p.p_n[i] = q.p_n[j];
-  p.z_t[i] = q.z_t[j]; p.z_t[cp + i] = q.z_t[cq + j];
-  p.q_trial_norm[i] = q.q_trial_norm[j]; p.dissipation[i] = q.dissipation[j];
-  p.k_pen[i] = q.k_pen[j]; p.k_t[i] = q.k_t[j];
+  p.p_n[i] = xk_f2d(q.p_n[j]);
+  p.z_t[i] = xk_f2d(q.z_t[j]); p.z_t[cp + i] = xk_f2d(q.z_t[cq + j]);
+  p.q_trial_norm[i] = xk_f2d(q.q_trial_norm[j]); p.dissipation[i] = xk_f2d(q.dissipation[j]);
+  p.k_pen[i] = xk_f2d(q.k_pen[j]); p.k_t[i] = xk_f2d(q.k_t[j]);
   p.status[i] = q.status[j]; p.stick[i] = q.stick[j];
   if (q.coat_total && p.coat_cc) {
-    p.coat_cc[i] = q.coat_cc[j];
-    p.coat_cc_prev[i] = q.coat_cc_prev[j];
-    p.coat_z_t[i] = q.coat_z_t[j];
-    p.coat_z_t[cp + i] = q.coat_z_t[cq + j];
-    p.coat_qtn[i] = q.coat_qtn[j];
-    p.coat_diss[i] = q.coat_diss[j];
+    p.coat_cc[i] = xk_f2d(q.coat_cc[j]);
+    p.coat_cc_prev[i] = xk_f2d(q.coat_cc_prev[j]);
+    p.coat_z_t[i] = xk_f2d(q.coat_z_t[j]);
+    p.coat_z_t[cp + i] = xk_f2d(q.coat_z_t[cq + j]);
+    p.coat_qtn[i] = xk_f2d(q.coat_qtn[j]);
+    p.coat_diss[i] = xk_f2d(q.coat_diss[j]);
     p.coat_stick[i] = q.coat_stick[j];
   }
 }
@@ -886,8 +886,8 @@ __global__ void __launch_bounds__(PAIR_T) k_narrow_screen(xk_mesh m, xk_pairs p,
   const PairNodes pn = pair_nodes(m, ea, eb);
   const int nd[4] = {pn.n[0], pn.n[1], pn.n[2], pn.n[3]};
   const double rs = xadd(m.radii[ea], m.radii[eb]);
-  const float rh = (float)rs;
-  const df R = {rh, (float)(rs - (double)rh)};
+  const float rh = xk_d2f(rs);
+  const df R = {rh, xk_d2f(rs - xk_f2d(rh))};
   float scale = 0.0f;
   {
     float xh[4][3];
@@ -904,9 +904,9 @@ __global__ void __launch_bounds__(PAIR_T) k_narrow_screen(xk_mesh m, xk_pairs p,
   {
     double v[3];
     load3(p.normal, cap, i, v);
-    for (int c = 0; c < 3; ++c) n[c] = (float)v[c];
+    for (int c = 0; c < 3; ++c) n[c] = xk_d2f(v[c]);
     load3(p.t1, cap, i, v);
-    for (int c = 0; c < 3; ++c) t1[c] = (float)v[c];
+    for (int c = 0; c < 3; ++c) t1[c] = xk_d2f(v[c]);
   }
   const bool deferred = m.core_radii != nullptr || narrow32<false, true>(n32, nd, R, sf, tf, gf, n, t1, t2);
   const float u24 = 5.9604645e-8f;  // 2^-24
@@ -919,10 +919,12 @@ __global__ void __launch_bounds__(PAIR_T) k_narrow_screen(xk_mesh m, xk_pairs p,
     list[1 + atomicAdd(list, 1)] = i;
     return;
   }
-  p.s[i] = (double)sf;
-  p.t[i] = (double)tf;
-  p.gap[i] = (double)gf;
-  const double nn[3] = {n[0], n[1], n[2]}, tt1[3] = {t1[0], t1[1], t1[2]}, tt2[3] = {t2[0], t2[1], t2[2]};
+  p.s[i] = xk_f2d(sf);
+  p.t[i] = xk_f2d(tf);
+  p.gap[i] = xk_f2d(gf);
+  const double nn[3] = {xk_f2d(n[0]), xk_f2d(n[1]), xk_f2d(n[2])};
+  const double tt1[3] = {xk_f2d(t1[0]), xk_f2d(t1[1]), xk_f2d(t1[2])};
+  const double tt2[3] = {xk_f2d(t2[0]), xk_f2d(t2[1]), xk_f2d(t2[2])};
   store3(p.normal, cap, i, nn);
   store3(p.t1, cap, i, tt1);
   store3(p.t2, cap, i, tt2);

@@ -110,7 +110,7 @@ __global__ void k_features(xk_mesh m, const float* __restrict__ n32, const int32
     const float4 p = __ldg(r), q = __ldg(r + 1);
     x[k][0] = p.x; x[k][1] = p.y; x[k][2] = p.z; x[k][3] = p.w; x[k][4] = q.x; x[k][5] = q.y;
   }
-  const float rsf = (float)xadd(m.radii[ea], m.radii[eb]);
+  const float rsf = xk_d2f(xadd(m.radii[ea], m.radii[eb]));
   // position differences from the split records (no double arithmetic), then everything in float with
   // each operation rounded on its own
   float dm[3], da[3], db[3], dw[3];

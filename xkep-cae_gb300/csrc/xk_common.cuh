@@ -76,6 +76,35 @@ struct Prec<XK_FP64> { typedef double T; };
 template <>
 struct Prec<XK_MIXED> { typedef float T; };
 
+// Double <-> float conversions in integer arithmetic.  On this GPU the conversion instructions issue
+// at the FP64 rate (about 1.8 per clock per SM, like a double add, against about 100 float adds),
+// and the integer operations at the full rate.  Both give the bits of the IEEE conversion (round to
+// nearest, ties to even, for double -> float; exact for float -> double): the fields are moved as
+// integers, and a result or input that is not a normal number (denormal, overflow, inf, nan) takes
+// the conversion instruction.
+XK_D float xk_d2f(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned e = (hi >> 20) & 0x7ffu;  // biased exponent; a normal float result needs e in [897, 1150]
+  if (e - 897u > 253u) {
+    if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);  // +-0
+    return __double2float_rn(x);
+  }
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // the top 23 of the 52 mantissa bits
+  const unsigned r = lo & 0x1fffffffu;                     // the 29 bits rounded away
+  const unsigned up = (r > 0x10000000u || (r == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  // a carry out of the mantissa raises the exponent (and past the largest float gives inf), as rounding does
+  return __uint_as_float(((hi & 0x80000000u) | ((e - 896u) << 23) | m) + up);
+}
+XK_D double xk_f2d(float v) {
+  const unsigned f = __float_as_uint(v);
+  const unsigned e = (f >> 23) & 0xffu;
+  if (e - 1u > 253u) {
+    if ((f & 0x7fffffffu) == 0u) return __hiloint2double((int)(f & 0x80000000u), 0);  // +-0
+    return (double)v;
+  }
+  return __hiloint2double((int)((f & 0x80000000u) | ((e + 896u) << 20) | ((f & 0x7fffffu) >> 3)), (int)(f << 29));
+}
+
 // Eight floats from a 32-byte aligned read-only address in one 256-bit load.
 XK_D void ldg8(const float* __restrict__ p, float* v) {
   asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
