@@ -891,6 +891,22 @@ def run_gpu(args, rank, world):
     ms_mixed = 1e3 * t_mixed / args.steps
     ms_fp64 = 1e3 * t_fp64 / args.steps
 
+    # the float beam beside the pair kernels: its launch capped at a few CTAs per SM (the kernel loops), so
+    # that it shares the SMs with them instead of holding every SM for its one wave; the step with each cap
+    beam_caps = {}
+    em = engines["mixed"]
+    if world == 1 and em.beam.chain_ordered:
+        base = em.beam.plan.beam_ctas_per_sm
+        for per_sm in (1, 2, 3):
+            em.beam.plan.beam_ctas_per_sm = per_sm
+            em.capture(u1, u0)
+            for _ in range(args.warmup):
+                em.replay()
+            beam_caps[str(per_sm)] = 1e3 * timed(em, args.steps) / args.steps
+        em.beam.plan.beam_ctas_per_sm = base
+        em.capture(u1, u0)
+        beam_caps[str(base) + " (the engine's setting)"] = ms_mixed
+
     # dominant kernel alone: the fused pair kernel, CUDA events on its stream
     import ctypes as C
 
@@ -1047,6 +1063,7 @@ def run_gpu(args, rank, world):
                    "contact_blocks_full_matrix": contact_blocks_full,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (pair table alone > 1 GB)", "cuda_graph": True},
+        "beam_ctas_per_sm_ms_per_step": beam_caps,
         "fp64_plain": {"value": units / t_fp64 * args.steps, "ms_per_step": ms_fp64,
                        "speedup_mixed_vs_fp64": t_fp64 / t_mixed},
         "err_vs_fp64": err,

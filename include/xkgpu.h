@@ -117,6 +117,8 @@ typedef struct {
                                     wire (element e's node b is element e+1's node a, or the node has
                                     one element); xk_beam_assemble32 then writes each shared node's
                                     sum once, without zeroing or atomics */
+  int32_t beam_ctas_per_sm;      /* float kernel: 0 for one CTA per 128 threads of work, else at most
+                                    this many CTAs per SM, looping (room for concurrent kernels) */
 } xk_beam_plan;
 
 /* Corotational Timoshenko internal force f_int and analytic tangent K_T of all

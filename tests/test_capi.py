@@ -48,8 +48,8 @@ def test_struct_layouts_match_header():
     assert C.sizeof(L.Mesh) == 8 + 6 * 8
     assert C.sizeof(L.Pairs) == 8 + 23 * 8
     assert C.sizeof(L.Pairs32) == 16 + 26 * 8 + 2 * 4 + 8
-    assert C.sizeof(L.BeamPlan) == 8 + 4 * 8 + 8 + 8 + 8  # chain_ordered (int32) + padding
-    assert L.BeamPlan.chain_ordered.offset == 56
+    assert C.sizeof(L.BeamPlan) == 8 + 4 * 8 + 8 + 8 + 8  # chain_ordered and beam_ctas_per_sm (int32)
+    assert L.BeamPlan.chain_ordered.offset == 56 and L.BeamPlan.beam_ctas_per_sm.offset == 60
     assert C.sizeof(L.ContactParams) == 6 * 8 + 8 + 5 * 8
     assert C.sizeof(L.BPParams) == 8 + 3 * 4 + 4 + 8 + 8
     assert C.sizeof(L.ContactPattern) == 16 + 5 * 8 + 10 * 8 + 2 * 8 + 7 * 8 + 3 * 8 + 2 * 4

@@ -278,6 +278,36 @@ def test_beam_float_chain_launch_equals_colours():
         assert torch.equal(K[: 36 * beam.nnzb], eng.K_beam[: 36 * beam.nnzb])
 
 
+def test_beam_float_capped_launch_loops_to_the_same_bits():
+    """The float beam launch capped at one CTA per SM loops over its work (strand397: 38,112 elements,
+    about twice the capped grid) and gives the bits of the full grid, ordered and colour forms."""
+    import ctypes as C
+
+    from xkgpu import workloads as W
+    from xkgpu.device import ptr, stream_handle
+
+    w = W.config_workload("strand397", seed=1)
+    st = w.strand
+    eng = AssemblyEngine(st.coords, st.conn, st.radii, w.section, precision="mixed", **w.engine_kwargs())
+    u0 = _dev(w.u)
+    eng.assemble(u0 * 1.001, u0)  # node records, element records, the ordered full-grid launch
+    torch.cuda.synchronize()
+    capped = DeviceBeam(eng.mesh, w.section)
+    capped.plan.beam_ctas_per_sm = 1
+    colours = DeviceBeam(eng.mesh, w.section, chain=False)
+    capped_colours = DeviceBeam(eng.mesh, w.section, chain=False)
+    capped_colours.plan.beam_ctas_per_sm = 1
+    assert 32 * (st.n_elems // 31 + 1) > 128 * 152  # the capped ordered launch loops
+    for beam in (capped, colours, capped_colours):
+        f = torch.full_like(eng.f_int, float("nan"))
+        K = torch.full_like(eng.K_beam, float("nan"))
+        L.call("xk_beam_assemble32", C.byref(eng.mesh.c), C.byref(beam.section), ptr(eng.elem32),
+               C.byref(beam.plan), ptr(eng.node32), ptr(f), ptr(K), stream_handle(None))
+        torch.cuda.synchronize()
+        assert torch.equal(f, eng.f_int)
+        assert torch.equal(K[: 36 * beam.nnzb], eng.K_beam[: 36 * beam.nnzb])
+
+
 def test_beam_float_ordered_writes_every_block_once():
     """The ordered float beam writes every f row and stored block of the mesh (buffers start as NaN),
     on meshes whose wires end inside a warp's range, at a warp boundary, and as one-element wires."""

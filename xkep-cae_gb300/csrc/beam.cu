@@ -825,15 +825,11 @@ XK_D void put_rows(double* __restrict__ f, long long node, const float* t, const
 constexpr int BEAMW_T = 128;
 constexpr int BEAM_ORDERED = 0, BEAM_ATOMIC = 1, BEAM_COLOUR = 2;
 
-__global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_section sec,
-                                                     const float* __restrict__ e32,
-                                                     const int32_t* __restrict__ order, int k0, int k1,
-                                                     const int32_t* __restrict__ blk,
-                                                     const uint8_t* __restrict__ first,
-                                                     const float* __restrict__ n32, double* __restrict__ f_int,
-                                                     float* __restrict__ Kv) {
-  __shared__ float slots[BEAMW_T * EL_STRIDE];
-  const long long t = (long long)blockIdx.x * BEAMW_T + threadIdx.x;
+// One element of the launch (t: the thread's logical index), its outputs staged in the slots.
+XK_D void beam_item(int mode, long long t, const xk_mesh& m, const xk_section& sec, const float* __restrict__ e32,
+                    const int32_t* __restrict__ order, int k0, int k1, const int32_t* __restrict__ blk,
+                    const uint8_t* __restrict__ first, const float* __restrict__ n32, double* __restrict__ f_int,
+                    float* __restrict__ Kv, float* slots) {
   const int lane = threadIdx.x & 31;
   const long long ne = m.n_elems;
   long long e;
@@ -927,6 +923,26 @@ __global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_
   // the off-diagonal block has one writer
   if (ob[1] >= 0) put_block<1, 0>(Kv + 36LL * ob[1], o, o);
   else put_block<2, 0>(Kv + 36LL * ob[2], o, o);
+}
+
+// Launch: the logical threads of the mode (32 per warp of 31 ordered elements, or one per element of
+// the colour range), each CTA thread taking every (gridDim.x * BEAMW_T)-th; a full grid gives one
+// element to each thread, a smaller one (the plan's beam_ctas_per_sm) loops, so that the beam can
+// run beside the bandwidth-bound pair kernels on few SMs' worth of warps.  A warp's slots are rewritten
+// only after all of its lanes have finished reading them.
+__global__ void __launch_bounds__(BEAMW_T, 6) k_beam32e(int mode, xk_mesh m, xk_section sec,
+                                                     const float* __restrict__ e32,
+                                                     const int32_t* __restrict__ order, int k0, int k1,
+                                                     const int32_t* __restrict__ blk,
+                                                     const uint8_t* __restrict__ first,
+                                                     const float* __restrict__ n32, double* __restrict__ f_int,
+                                                     float* __restrict__ Kv, long long n_threads) {
+  __shared__ float slots[BEAMW_T * EL_STRIDE];
+  const long long stride = (long long)gridDim.x * BEAMW_T;  // a multiple of 32
+  for (long long t = (long long)blockIdx.x * BEAMW_T + threadIdx.x; t < n_threads; t += stride) {
+    if (mode == BEAM_ORDERED) __syncwarp();  // the whole warp is here: n_threads is a multiple of 32 there
+    beam_item(mode, t, m, sec, e32, order, k0, k1, blk, first, n32, f_int, Kv, slots);
+  }
 }
 
 // Chain launches: zero the node rows of f_int and the diagonal blocks that the elements add into,
@@ -1042,6 +1058,15 @@ extern "C" xk_status xk_beam_prepare32(const xk_mesh* m, const double* elem_ref,
   return XK_OK;
 }
 
+// CTAs of a float beam launch over `threads` logical threads: one per thread, or at most
+// plan->beam_ctas_per_sm per SM (the kernel loops)
+static int beam_grid(long long threads, const xk_beam_plan* plan) {
+  const int full = xk_blocks(threads, BEAMW_T);
+  if (plan->beam_ctas_per_sm <= 0) return full;
+  const long long cap = (long long)plan->beam_ctas_per_sm * xk_sm_count();
+  return full < cap ? full : (int)cap;
+}
+
 extern "C" xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec, const float* elem32,
                                         const xk_beam_plan* plan, const float* node32, double* f_int, float* K_vals,
                                         xk_stream s) {
@@ -1055,13 +1080,13 @@ extern "C" xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec,
     const long long ne = m->n_elems;
     if (ne == 0) return XK_OK;
     if (plan->chain_ordered) {  // 31 elements per warp, the lane before them repeating the previous one
-      const long long warps = ne / 31 + 1;
-      k_beam32e<<<xk_blocks(32 * warps, BEAMW_T), BEAMW_T, 0, st>>>(
-          BEAM_ORDERED, *m, *sec, elem32, nullptr, 0, 0, plan->blk, plan->first, node32, f_int, K_vals);
+      const long long threads = 32 * (ne / 31 + 1);
+      k_beam32e<<<beam_grid(threads, plan), BEAMW_T, 0, st>>>(BEAM_ORDERED, *m, *sec, elem32, nullptr, 0, 0, plan->blk,
+                                                             plan->first, node32, f_int, K_vals, threads);
     } else {
       k_beam_zero32<<<xk_blocks(9LL * m->n_nodes, 256), 256, 0, st>>>(m->n_nodes, plan->node_diag, f_int, K_vals);
-      k_beam32e<<<xk_blocks(ne, BEAMW_T), BEAMW_T, 0, st>>>(
-          BEAM_ATOMIC, *m, *sec, elem32, nullptr, 0, (int)ne, plan->blk, plan->first, node32, f_int, K_vals);
+      k_beam32e<<<beam_grid(ne, plan), BEAMW_T, 0, st>>>(BEAM_ATOMIC, *m, *sec, elem32, nullptr, 0, (int)ne, plan->blk,
+                                                         plan->first, node32, f_int, K_vals, ne);
     }
     XK_CHECK_LAUNCH();
     return XK_OK;
@@ -1069,8 +1094,8 @@ extern "C" xk_status xk_beam_assemble32(const xk_mesh* m, const xk_section* sec,
   for (int c = 0; c < plan->n_colors; ++c) {
     const int k0 = plan->color_ptr_host[c], k1 = plan->color_ptr_host[c + 1];
     if (k1 <= k0) continue;
-    k_beam32e<<<xk_blocks(k1 - k0, BEAMW_T), BEAMW_T, 0, st>>>(
-        BEAM_COLOUR, *m, *sec, elem32, plan->elem_order, k0, k1, plan->blk, plan->first, node32, f_int, K_vals);
+    k_beam32e<<<beam_grid(k1 - k0, plan), BEAMW_T, 0, st>>>(BEAM_COLOUR, *m, *sec, elem32, plan->elem_order, k0, k1,
+                                                           plan->blk, plan->first, node32, f_int, K_vals, k1 - k0);
     XK_CHECK_LAUNCH();
   }
   return XK_OK;

@@ -71,7 +71,8 @@ class Pairs32(C.Structure):
 
 class BeamPlan(C.Structure):
     _fields_ = [("n_colors", C.c_int32), ("color_ptr_host", vp), ("elem_order", vp), ("blk", vp), ("first", vp),
-                ("nnzb", C.c_int64), ("node_diag", vp), ("chain_ordered", C.c_int32)]
+                ("nnzb", C.c_int64), ("node_diag", vp), ("chain_ordered", C.c_int32),
+                ("beam_ctas_per_sm", C.c_int32)]
 
 
 class ContactParams(C.Structure):
