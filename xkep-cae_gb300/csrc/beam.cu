@@ -207,15 +207,25 @@ struct KeCoef {
   T ea, gj, k3y, k2y, k1ay, k1by, k3z, k2z, k1az, k1bz;
 };
 
+// A section value in the element's precision; to float in integer arithmetic (the conversion instruction
+// issues at the FP64 rate), the same bits as the cast.
+template <typename T>
+XK_D T sec_val(double x);
+template <>
+XK_D double sec_val<double>(double x) { return x; }
+template <>
+XK_D float sec_val<float>(double x) { return xk_d2f(x); }
+
 template <typename T>
 XK_D KeCoef<T> ke_coef(const xk_section& s, T L0) {
   T L = L0;
   T iL = T(1) / L;
-  T E = (T)s.E, G = (T)s.G, A = (T)s.A, Iy = (T)s.Iy, Iz = (T)s.Iz, J = (T)s.J;
-  T phy = T(12) * E * Iy / ((T)s.kappa_y * G * A * L * L);
-  T phz = T(12) * E * Iz / ((T)s.kappa_z * G * A * L * L);
-  if (s.scf > 0.0) {
-    T sc = (T)s.scf;
+  T E = sec_val<T>(s.E), G = sec_val<T>(s.G), A = sec_val<T>(s.A), Iy = sec_val<T>(s.Iy), Iz = sec_val<T>(s.Iz),
+    J = sec_val<T>(s.J);
+  T phy = T(12) * E * Iy / (sec_val<T>(s.kappa_y) * G * A * L * L);
+  T phz = T(12) * E * Iz / (sec_val<T>(s.kappa_z) * G * A * L * L);
+  if (__double_as_longlong(s.scf) > 0 && __double_as_longlong(s.scf) <= 0x7ff0000000000000LL) {  // scf > 0
+    T sc = sec_val<T>(s.scf);
     phy = phy / (T(1) + sc * L * L * A / (T(12) * Iy));
     phz = phz / (T(1) + sc * L * L * A / (T(12) * Iz));
   }

@@ -1029,8 +1029,11 @@ XK_D void member32(const xk_pairs32& q, const float* __restrict__ n32, const xk_
   store3f(q.t1, cq, i, t1);
   store3f(q.t2, cq, i, t2);
   // normal force (Huber)
-  const float kpen = (float)cp.k_pen;
-  const float dh = cp.smoothing_delta > 0.0 ? (float)(cp.k_pen / cp.smoothing_delta) : 0.0f;
+  // the parameters converted in integer arithmetic (a conversion instruction issues at the FP64 rate, and
+  // every member thread needs them); smoothing_delta > 0 tested on its bits (positive, at most +inf)
+  const float kpen = xk_d2f(cp.k_pen);
+  const long long sd_bits = __double_as_longlong(cp.smoothing_delta);
+  const float dh = (sd_bits > 0 && sd_bits <= 0x7ff0000000000000LL) ? xk_d2f(cp.k_pen / cp.smoothing_delta) : 0.0f;
   const float xpen = kpen * (-gap);
   float p_n = q.p_n[i];
   float vn[3] = {0.f, 0.f, 0.f}, vf[3] = {0.f, 0.f, 0.f};
@@ -1042,7 +1045,7 @@ XK_D void member32(const xk_pairs32& q, const float* __restrict__ n32, const xk_
       for (int k = 0; k < 3; ++k) vn[k] = p_n * n[k];
   }
   // friction (Coulomb return mapping)
-  const float mu = q.mu ? q.mu[i] : (float)cp.mu_eff;
+  const float mu = q.mu ? q.mu[i] : xk_d2f(cp.mu_eff);
   float kt = q.k_t[i];
   float zt0 = q.z_t[i], zt1 = q.z_t[cq + i];
   float qtn = q.q_trial_norm[i];
