@@ -1,12 +1,13 @@
 // Corotational Timoshenko beam: internal force and analytic tangent per element.
 //
 // Mirrors _assemble_cr_beam3d_batch_impl (xkep_cae/elements/_beam_assembly.py:211-325)
-// one element per thread.  The corotated frame is taken in double in both
-// precision modes, in quaternion form:
+// one element per thread, with the corotated frame in quaternion form:
 //   R_cr = R0 R_rod^T,  theta_def = log(R_cr R_node R0^T) = R0 log(q_rod^* (x) q_node)
 // which equals the reference's matrix Shepperd route for rotations below pi.
-// Everything downstream of the frame (local stiffness, f_cr, B, K_mat, K_geo)
-// runs in Prec<P>::T.
+// k_beam<P> (xk_beam_assemble) takes the frame in double in both precision modes
+// and runs everything downstream of it (local stiffness, f_cr, B, K_mat, K_geo)
+// in Prec<P>::T; k_beam32e (xk_beam_assemble32, the mixed engine) runs all of it
+// in float from the prepared element and node records.
 #include "xk_common.cuh"
 
 namespace {
